@@ -1,0 +1,519 @@
+"""Scenario builders: the initial particle states of the ring-impact and plate-tension
+set-ups, in the reference's own lattice construction, with either the reference's
+constants or the workload constants of the GPU configurations.
+
+Every builder returns a :class:`Scenario` -- per body the 13 input arrays of the
+reference's particle (x, y, X, Y, m, rho, h, quad_weight, vx, vy, Sxx, Sxy, Syy),
+the convex-hull contact boundary and boundary conditions, plus the simulation
+constants and the ordered action list.  All arithmetic is IEEE binary64 in the same
+order as the reference's set-up code, so the initial states are bit-identical to the
+ones its scenario functions build (checked against the compiled reference).
+"""
+from __future__ import annotations
+
+import math
+import struct
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from .actions import (
+    RINGS_MONAGHAN_ACTIONS,
+    RINGS_TL_ACTIONS,
+    TENSILE_TL_ACTIONS,
+    TENSILE_TL_WEAK_ACTIONS,
+)
+
+M_1_PI = 0.31830988618379067154  # the C library's M_1_PI
+
+IN_NAMES = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx", "Sxy", "Syy")
+OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
+
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK = 1, 2, 3
+BC_PULL_TL = 1
+
+
+def cubic_spline(xi: float, yi: float, xj: float, yj: float, h: float):
+    """Scalar 2-D cubic spline W, dW/dx, dW/dy (kernel.cpp:20-55), same operation order."""
+    h1 = 1.0 / h
+    xij = xi - xj
+    yij = yi - yj
+    rij = math.sqrt(xij * xij + yij * yij)
+    fac = 10 * M_1_PI / 7.0 * h1 * h1
+    q = rij * h1
+    if q >= 2.0:
+        return 0.0, 0.0, 0.0
+    if q >= 1.0:
+        w = fac * (0.25 * (2 - q) * (2 - q) * (2 - q))
+        if rij > 1e-12:
+            der = -0.75 * (2 - q) * (2 - q) * h1 / rij
+            return w, xij * der * fac, yij * der * fac
+        return w, 0.0, 0.0
+    w = fac * (1 - 1.5 * q * q * (1 - 0.5 * q))
+    if rij > 1e-12:
+        der = -3.0 * q * (1 - 0.75 * q) * h1 / rij
+        return w, xij * der * fac, yij * der * fac
+    return w, 0.0, 0.0
+
+
+@dataclass
+class BC:
+    kind: int
+    v: float
+    idx: np.ndarray
+
+
+@dataclass
+class Body:
+    arrays: Dict[str, np.ndarray]
+    hull: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint32))
+    bcs: List[BC] = field(default_factory=list)
+    ex: int = 0
+    ey: int = 0
+
+    @property
+    def n(self) -> int:
+        return int(self.arrays["x"].shape[0])
+
+
+@dataclass
+class Scenario:
+    method: int
+    bodies: List[Body]
+    actions: List[int]
+    dt: float
+    nu: float
+    E: float
+    rho0: float
+    wdeltap: float = 0.0
+    corr_exp: float = 0.0
+    mghn_eps: float = 0.0
+    alpha: float = 0.0
+    beta: float = 0.0
+    eta: float = 0.0
+    xsph_eps: float = 0.0
+    do_smooth: int = 0
+    nbh_h: float = 0.0
+    nbh_eps: float = 1e-6
+    gp_h: float = 0.0
+    gp_rho: float = 0.0
+    contact: int = 0
+    name: str = ""
+
+    @property
+    def n_total(self) -> int:
+        return sum(b.n for b in self.bodies)
+
+    # physical_constants, simulation_data.cpp:32-47
+    @property
+    def G(self) -> float:
+        return self.E / (2.0 * (1.0 + self.nu))
+
+    @property
+    def K(self) -> float:
+        g = self.G
+        return 2.0 * g * (1 + self.nu) / (3 * (1 - 2 * self.nu))
+
+    @property
+    def c0(self) -> float:
+        return math.sqrt(self.K / self.rho0)
+
+
+def _body_from_lists(xs, ys, X=None, Y=None) -> Dict[str, np.ndarray]:
+    n = len(xs)
+    a = {k: np.zeros(n, np.float64) for k in IN_NAMES}
+    a["x"][:] = xs
+    a["y"][:] = ys
+    if X is not None:
+        a["X"][:] = X
+        a["Y"][:] = Y
+    return a
+
+
+def _ring_lattice(nbox: int, dx: float, ro: float, ri: float):
+    """Lattice points of one annulus, in the reference's loop order (rings.cpp:40-56)."""
+    pts = []
+    for i in range(nbox):
+        for j in range(nbox):
+            px = -ro + i * dx
+            py = -ro + j * dx
+            dist = math.sqrt(px * px + py * py)
+            if dist < ro and dist >= ri:
+                pts.append((px, py))
+    return pts
+
+
+def convex_hull(x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """Monotone-chain hull indices with collinear points kept (convex_hull.h:62-95).
+
+    Ties in the (x, y) sort are impossible for distinct lattice points, so the order is
+    the unique lexicographic one the reference's std::sort produces.
+    """
+    n = len(x)
+    order = sorted(range(n), key=lambda i: (x[i], y[i]))
+    pts = [(float(x[i]), float(y[i]), i) for i in order]
+
+    def ccw(p1, p2, p3):
+        return (p2[0] - p1[0]) * (p3[1] - p1[1]) - (p2[1] - p1[1]) * (p3[0] - p1[0])
+
+    hull = [None] * n
+    k = 0
+    for i in range(n):
+        while k >= 2 and ccw(hull[k - 2], hull[k - 1], pts[i]) < 0:
+            k -= 1
+        hull[k] = pts[i]
+        k += 1
+    t = k + 1
+    for i in range(n - 2, -1, -1):
+        while k >= t and ccw(hull[k - 2], hull[k - 1], pts[i]) < 0:
+            k -= 1
+        hull[k] = pts[i]
+        k += 1
+    return np.array([hull[i][2] for i in range(k - 1)], np.uint32)
+
+
+def rings(
+    nbox: int,
+    *,
+    ro: float = 0.04,
+    ri: float = 0.03,
+    spacing: Optional[float] = None,
+    rho0: float = 1.0,
+    E: float = 1e7,
+    nu: float = 0.4,
+    hdx: float = 1.7,
+    speed: float = 180.0,
+    dt: Optional[float] = 1e-6,
+    cfl: float = 0.3,
+    method: int = METHOD_UL,
+    two_bodies: bool = False,
+    alpha: float = 1.0,
+    beta: float = 1.0,
+    eta: float = 0.1,
+    art_stress_eps: float = 0.3,
+    stress_exponent: float = 4.0,
+    xsph_eps: float = 0.5,
+    nbh_eps: float = 1e-6,
+    name: str = "",
+) -> Scenario:
+    """Two rings on a square lattice, as rings_monaghan (rings.cpp:20-99),
+    rings_monaghan_contact (:522-621) and rings_tl_contact (:338-429) build them.
+
+    Defaults are the reference's constants; ``dt=None`` selects dt = cfl*h/c0.
+    """
+    if spacing is None:
+        spacing = ro + 0.001
+    dx = 2 * ro / (nbox - 1)
+    pts = _ring_lattice(nbox, dx, ro, ri)
+    tl = method == METHOD_TL
+    sc = Scenario(method=method, bodies=[], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
+    if dt is None:
+        dt = cfl * (hdx * dx) / sc.c0
+    sc.dt = dt
+
+    def finish(a: Dict[str, np.ndarray], vx) -> None:
+        a["rho"][:] = rho0
+        a["h"][:] = hdx * dx
+        a["m"][:] = dx * dx * rho0
+        a["quad_weight"][:] = a["m"] / a["rho"]
+        a["vx"][:] = vx
+
+    if not two_bodies:
+        xs, ys = [], []
+        for px, py in pts:
+            xs += [px - spacing, px + spacing]
+            ys += [py, py]
+        a = _body_from_lists(xs, ys, xs if tl else None, ys if tl else None)
+        vx = np.where(a["x"] < 0.0, speed, -speed)
+        finish(a, vx)
+        sc.bodies = [Body(a)]
+    else:
+        for sgn, v in ((-1.0, speed), (1.0, -speed)):
+            xs = [px + sgn * spacing for px, _ in pts]
+            ys = [py for _, py in pts]
+            a = _body_from_lists(xs, ys, xs if tl else None, ys if tl else None)
+            finish(a, v)
+            sc.bodies.append(Body(a, hull=convex_hull(a["x"], a["y"])))
+        sc.contact = 1
+
+    if method == METHOD_UL:
+        sc.actions = list(RINGS_MONAGHAN_ACTIONS)
+        sc.alpha, sc.beta, sc.eta = alpha, beta, eta
+        sc.wdeltap = cubic_spline(0, 0, dx, 0, hdx * dx)[0]
+        sc.corr_exp = stress_exponent
+        sc.mghn_eps = art_stress_eps
+        sc.xsph_eps = xsph_eps
+    else:
+        sc.actions = list(RINGS_TL_ACTIONS)
+        sc.alpha, sc.beta, sc.eta = alpha, beta, eta
+        sc.nbh_h = hdx * dx
+    sc.nbh_eps = nbh_eps
+    return sc
+
+
+def rings_monaghan(nbox: int) -> Scenario:
+    """The reference's rings_monaghan(nbox), rings.cpp:20-99."""
+    return rings(nbox, name=f"rings_monaghan({nbox})")
+
+
+def rings_monaghan_contact(nbox: int) -> Scenario:
+    """The reference's rings_monaghan_contact(nbox), rings.cpp:522-621."""
+    return rings(nbox, two_bodies=True, name=f"rings_monaghan_contact({nbox})")
+
+
+def rings_tl_contact(nbox: int) -> Scenario:
+    """The reference's rings_tl_contact(nbox), rings.cpp:338-429."""
+    return rings(nbox, method=METHOD_TL, two_bodies=True, dt=1e-7, alpha=3.0, beta=3.0, eta=0.1,
+                 name=f"rings_tl_contact({nbox})")
+
+
+def workload_nbh_eps(dx: float) -> float:
+    """Scale-aware neighbour epsilon: the reference's 1e-6 m^2 at dx = 1 mm, scaled with dx^2.
+
+    The reference's absolute +1e-6 m^2 grows the search radius to ~20 dx at dx = 0.05 mm,
+    overflowing its own MAX_NBH; scaling it keeps the radius sqrt(4 h^2 + dx^2)."""
+    return 1e-6 * (dx / 1e-3) ** 2
+
+
+def c1_rings(dx: float = 1e-3, two_bodies: bool = False, method: int = METHOD_UL, **kw) -> Scenario:
+    """Ring impact with the workload constants: r_in 0.03 m, r_out 0.04 m, centres 0.09 m
+    apart, E 1e7 Pa, nu 0.4, rho 1200 kg/m^3, +-10 m/s, h = 1.3 dx, dt = 0.3 h / c0."""
+    nbox = int(round(0.08 / dx)) + 1
+    params = dict(spacing=0.045, rho0=1200.0, E=1e7, nu=0.4, hdx=1.3, speed=10.0, dt=None, cfl=0.3,
+                  alpha=1.0, beta=1.0, eta=0.1, art_stress_eps=0.3, stress_exponent=4.0, xsph_eps=0.5,
+                  nbh_eps=workload_nbh_eps(2 * 0.04 / (nbox - 1)))
+    if method == METHOD_TL:
+        params.update(alpha=3.0, beta=3.0)
+    params.update(kw)
+    return rings(nbox, method=method, two_bodies=two_bodies, name=f"rings dx={dx}", **params)
+
+
+def c2_rings_tl(dx: float = 5e-5, **kw) -> Scenario:
+    """Ring impact, total-Lagrangian SPH with Randles-Libersky correction, two bodies with
+    penalty contact (the rings_tl_contact structure) and the workload constants."""
+    return c1_rings(dx=dx, two_bodies=True, method=METHOD_TL, **kw)
+
+
+def tensile_plate(
+    nx: int,
+    ny: int,
+    *,
+    Lx: float,
+    method: int = METHOD_TL,
+    rho0: float = 1.0,
+    E: float = 1e7,
+    nu: float = 0.4,
+    hdx: float = 1.0,
+    pull: float = 10.0,
+    dt: Optional[float] = 1e-6,
+    cfl: float = 0.3,
+    jitter: float = 0.0,
+    seed: int = 0,
+    alpha: float = 1.0,
+    beta: float = 1.0,
+    eta: float = 0.1,
+    do_smooth: int = 1,
+    nbh_eps: float = 1e-6,
+    name: str = "",
+) -> Scenario:
+    """A rectangular plate pulled at both ends: tensile_tl (tensile.cpp:213-289) and
+    tensile_tl_weak (:731-826) lattices (px = i*dx, py = j*dx; column i = 0 and
+    i = nx-1 carry the pull), generalised to nx != ny and optional seeded jitter."""
+    dx = Lx / (nx - 1)
+    xs, ys, left, right = [], [], [], []
+    k = 0
+    for i in range(nx):
+        for j in range(ny):
+            xs.append(i * dx)
+            ys.append(j * dx)
+            if i == 0:
+                left.append(k)
+            if i == nx - 1:
+                right.append(k)
+            k += 1
+    xs = np.array(xs)
+    ys = np.array(ys)
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        xs = xs + rng.uniform(-jitter, jitter, xs.shape) * dx
+        ys = ys + rng.uniform(-jitter, jitter, ys.shape) * dx
+    a = _body_from_lists(xs, ys, xs, ys)
+    a["rho"][:] = rho0
+    a["h"][:] = hdx * dx
+    a["m"][:] = dx * dx * rho0
+    a["quad_weight"][:] = a["m"] / a["rho"]
+    body = Body(a, bcs=[BC(BC_PULL_TL, -pull, np.array(left, np.uint32)),
+                        BC(BC_PULL_TL, pull, np.array(right, np.uint32))])
+    sc = Scenario(method=method, bodies=[body], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
+    sc.dt = dt if dt is not None else cfl * (hdx * dx) / sc.c0
+    sc.nbh_h = hdx * dx
+    sc.nbh_eps = nbh_eps
+    if method == METHOD_TL:
+        sc.actions = list(TENSILE_TL_ACTIONS)
+        sc.alpha, sc.beta, sc.eta = alpha, beta, eta
+    else:
+        sc.actions = list(TENSILE_TL_WEAK_ACTIONS)
+        sc.do_smooth = do_smooth
+        sc.gp_h = hdx * dx
+        sc.gp_rho = rho0
+        body.ex, body.ey = nx - 1, ny - 1
+    return sc
+
+
+def tensile_tl(nbox: int) -> Scenario:
+    """The reference's tensile_tl(nbox), tensile.cpp:213-289."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_TL, hdx=1.0, dt=1e-6, name=f"tensile_tl({nbox})")
+
+
+def tensile_tl_weak(nbox: int) -> Scenario:
+    """The reference's tensile_tl_weak(nbox), tensile.cpp:731-826."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_TL_WEAK, hdx=1.3, dt=1e-7, alpha=0.0, beta=0.0,
+                         eta=0.0, name=f"tensile_tl_weak({nbox})")
+
+
+def c3_plate(dx: float = 2e-5, Lx: float = 0.1, Ly: float = 0.02, seed: int = 20261203, **kw) -> Scenario:
+    """Uniaxial tension of a steel plate with the weak-form RKPM structure: E 2e11 Pa,
+    nu 0.3, rho 7850 kg/m^3, ends at +-1 m/s, +-1% dx seeded jitter, h = 1.3 dx."""
+    nx = int(round(Lx / dx)) + 1
+    ny = int(round(Ly / dx)) + 1
+    params = dict(rho0=7850.0, E=2e11, nu=0.3, hdx=1.3, pull=1.0, dt=None, cfl=0.3, jitter=0.01, seed=seed,
+                  alpha=0.0, beta=0.0, eta=0.0, nbh_eps=workload_nbh_eps(dx))
+    params.update(kw)
+    return tensile_plate(nx, ny, Lx=Lx, method=METHOD_TL_WEAK, name=f"plate dx={dx}", **params)
+
+
+# ---------------------------------------------------------------- case files
+def write_case(path: str, sc: Scenario, nsteps: int, dump_every: int = 0) -> None:
+    """Write the binary case file read by the oracle (oracle/mfcase.h)."""
+    out = bytearray(b"MFCASE1\0")
+    u32 = lambda v: out.extend(struct.pack("<I", int(v)))
+    f64 = lambda v: out.extend(struct.pack("<d", float(v)))
+    u32(sc.method); u32(len(sc.bodies)); u32(nsteps); u32(dump_every); u32(sc.contact)
+    u32(len(sc.actions))
+    for a in sc.actions:
+        u32(a)
+    f64(sc.dt)
+    for v in (sc.nu, sc.E, sc.rho0, sc.wdeltap, sc.corr_exp, sc.mghn_eps, sc.alpha, sc.beta, sc.eta, sc.xsph_eps):
+        f64(v)
+    u32(sc.do_smooth)
+    for v in (sc.nbh_h, sc.nbh_eps, sc.gp_h, sc.gp_rho):
+        f64(v)
+    for b in sc.bodies:
+        u32(b.n)
+        for k in IN_NAMES:
+            out.extend(np.ascontiguousarray(b.arrays[k], np.float64).tobytes())
+        u32(len(b.hull))
+        out.extend(np.ascontiguousarray(b.hull, np.uint32).tobytes())
+        u32(len(b.bcs))
+        for bc in b.bcs:
+            u32(bc.kind); f64(bc.v); u32(len(bc.idx))
+            out.extend(np.ascontiguousarray(bc.idx, np.uint32).tobytes())
+        u32(b.ex); u32(b.ey)
+    with open(path, "wb") as f:
+        f.write(bytes(out))
+
+
+def read_case(path: str) -> Scenario:
+    """Read a case file back (inverse of :func:`write_case`)."""
+    buf = open(path, "rb").read()
+    assert buf[:7] == b"MFCASE1"
+    off = 8
+
+    def u32():
+        nonlocal off
+        v = struct.unpack_from("<I", buf, off)[0]
+        off += 4
+        return v
+
+    def f64():
+        nonlocal off
+        v = struct.unpack_from("<d", buf, off)[0]
+        off += 8
+        return v
+
+    def arr(dt, n):
+        nonlocal off
+        a = np.frombuffer(buf, dt, n, off).copy()
+        off += n * np.dtype(dt).itemsize
+        return a
+
+    method, nb, nsteps, dump_every, contact = u32(), u32(), u32(), u32(), u32()
+    actions = list(arr(np.uint32, u32()))
+    dt = f64()
+    vals = [f64() for _ in range(10)]
+    do_smooth = u32()
+    nbh_h, nbh_eps, gp_h, gp_rho = f64(), f64(), f64(), f64()
+    bodies = []
+    for _ in range(nb):
+        n = u32()
+        a = {k: arr(np.float64, n) for k in IN_NAMES}
+        hull = arr(np.uint32, u32())
+        bcs = []
+        for _ in range(u32()):
+            kind = u32(); v = f64(); idx = arr(np.uint32, u32())
+            bcs.append(BC(kind, v, idx))
+        ex, ey = u32(), u32()
+        bodies.append(Body(a, hull, bcs, ex, ey))
+    sc = Scenario(method=method, bodies=bodies, actions=[int(a) for a in actions], dt=dt, nu=vals[0], E=vals[1],
+                  rho0=vals[2], wdeltap=vals[3], corr_exp=vals[4], mghn_eps=vals[5], alpha=vals[6], beta=vals[7],
+                  eta=vals[8], xsph_eps=vals[9], do_smooth=do_smooth, nbh_h=nbh_h, nbh_eps=nbh_eps, gp_h=gp_h,
+                  gp_rho=gp_rho, contact=contact)
+    return sc
+
+
+@dataclass
+class Result:
+    dumps: List[dict]          # [{"step", "time", "bodies": [ {name: array} ]}]
+    neighbors: List[List[np.ndarray]]
+    seconds: float
+    ok: bool
+
+
+def read_result(path: str) -> Result:
+    """Parse a result file written by the oracle or the reference harness."""
+    buf = open(path, "rb").read()
+    assert buf[:6] == b"MFOUT1", "bad result file"
+    off = 8
+    nb = struct.unpack_from("<I", buf, off)[0]
+    off += 4
+    ns = list(struct.unpack_from(f"<{nb}I", buf, off))
+    off += 4 * nb
+    dumps, nbh, secs, ok = [], [], 0.0, False
+    while off < len(buf):
+        tag = struct.unpack_from("<I", buf, off)[0]
+        off += 4
+        if tag == 0:
+            ok = True
+            break
+        if tag == 1:
+            step = struct.unpack_from("<I", buf, off)[0]
+            t = struct.unpack_from("<d", buf, off + 4)[0]
+            off += 12
+            bodies = []
+            for n in ns:
+                d = {}
+                for k in OUT_NAMES:
+                    d[k] = np.frombuffer(buf, np.float64, n, off).copy()
+                    off += 8 * n
+                bodies.append(d)
+            dumps.append({"step": step, "time": t, "bodies": bodies})
+        elif tag == 2:
+            for _ in range(nb):
+                n = struct.unpack_from("<I", buf, off)[0]
+                off += 4
+                counts = np.frombuffer(buf, np.uint32, n, off).copy()
+                off += 4 * n
+                tot = int(counts.sum())
+                flat = np.frombuffer(buf, np.uint32, tot, off).copy()
+                off += 4 * tot
+                starts = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)]).astype(np.int64)
+                nbh.append([flat[int(starts[i]):int(starts[i + 1])] for i in range(n)])
+        elif tag == 3:
+            secs = struct.unpack_from("<d", buf, off)[0]
+            off += 8
+        elif tag == 9:
+            break
+        else:
+            raise ValueError(f"bad record tag {tag}")
+    return Result(dumps, nbh, secs, ok)

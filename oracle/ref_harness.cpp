@@ -1,0 +1,491 @@
+// Test infrastructure: drives the reference's own, unmodified sources (compiled
+// out of tree by oracle/build_ref.sh against the project-written GLM subset) so
+// that the CPU oracle restatement and the golden fixtures can be pinned to the
+// reference itself.  Never shipped, never part of the product.
+//
+//   ref_harness run CASE RESULT
+//       builds the bodies of CASE with the reference's particle classes, body<T>,
+//       action functions, find_neighbors/precomp_* set-up and contact, runs the
+//       step loop of main() (mfree_iwf.cpp:84-97) and writes RESULT.
+//   ref_harness scenario NAME NBOX NSTEPS CASE_OUT RESULT
+//       runs one of the reference's own scenario builders (rings_monaghan,
+//       rings_monaghan_contact, rings_tl_contact, tensile_tl, tensile_tl_weak)
+//       unchanged, writes its initial state as CASE_OUT (so the restatement can
+//       replay it) and the run as RESULT.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "body.h"
+#include "contact.h"
+#include "particle.h"
+#include "benchmarks/rings.h"
+#include "benchmarks/tensile.h"
+
+#include "mfcase.h"
+
+using namespace mfcase;
+
+namespace {
+
+// neighbour lists of the first derivative evaluation, by particle idx
+std::vector<std::vector<std::vector<unsigned>>> g_nbh;
+int g_cur_body = 0;
+std::vector<bool> g_recorded;
+
+template <typename T>
+void record_first_nbh(body<T>& b) {
+	if (g_recorded[g_cur_body]) return;
+	g_recorded[g_cur_body] = true;
+	T** p = b.get_cur_particles();
+	unsigned n = b.get_num_part();
+	auto& L = g_nbh[g_cur_body];
+	L.assign(n, {});
+	for (unsigned i = 0; i < n; i++)
+		for (unsigned j = 0; j < p[i]->num_nbh; j++) L[p[i]->idx].push_back(p[p[i]->nbh[j]]->idx);
+}
+
+template <typename T>
+void record_fixed_nbh(T** p, unsigned n, int b) {
+	auto& L = g_nbh[b];
+	L.assign(n, {});
+	for (unsigned i = 0; i < n; i++)
+		for (unsigned j = 0; j < p[i]->num_nbh; j++) L[p[i]->idx].push_back(p[p[i]->nbh[j]]->idx);
+	g_recorded[b] = true;
+}
+
+typedef void (*UlAct)(body<particle_monaghan>&);
+typedef void (*TlAct)(body<particle_tl>&);
+typedef void (*WkAct)(body<particle_tl_weak>&);
+
+UlAct ul_action(uint32_t a) {
+	typedef particle_monaghan T;
+	switch (a) {
+	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return &riemann_update_integration_weights<T>;
+	case MATERIAL_EOS: return &material_eos<T>;
+	case CORRECTORS_MGHN_ARTIFICIAL_STRESS: return &correctors_mghn_artificial_stress<T>;
+	case DERIVE_STRESS_MONAGHAN: return &derive_stress_monaghan<T>;
+	case DERIVE_VELOCITY: return &derive_velocity<T>;
+	case CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY: return &correctors_mghn_artificial_viscosity<T>;
+	case CORRECTORS_XSPH: return &correctors_xsph<T>;
+	case MATERIAL_STRESS_RATE_JAUMANN: return &material_stress_rate_jaumann<T>;
+	case CONTMECH_CONTINUITY: return &contmech_continuity<T>;
+	case CONTMECH_MOMENTUM_UL: return &contmech_momentum_ul<T>;
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	}
+	return nullptr;
+}
+TlAct tl_action(uint32_t a) {
+	typedef particle_tl T;
+	switch (a) {
+	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return &riemann_update_integration_weights<T>;
+	case MATERIAL_EOS: return &material_eos<T>;
+	case DERIVE_VELOCITY: return &derive_velocity<T>;
+	case CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY: return &correctors_mghn_artificial_viscosity<T>;
+	case CORRECTORS_XSPH: return &correctors_xsph<T>;
+	case MATERIAL_STRESS_RATE_JAUMANN: return &material_stress_rate_jaumann<T>;
+	case CONTMECH_CONTINUITY: return &contmech_continuity<T>;
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case DERIVE_DISPLACEMENT: return &derive_displacement<T>;
+	case MATERIAL_COMPUTE_STRESS_GREEN_STVENANT: return &material_compute_stress_green_stvenant<T>;
+	case CONTMECH_CAUCHY_TO_NOMINAL: return &contmech_cauchy_to_nominal<T>;
+	case DERIVE_STRESS_TL: return &derive_stress_tl<T>;
+	case CONTMECH_MOMENTUM_TL: return &contmech_momentum_tl<T>;
+	case DERIVE_VELOCITY_TL: return &derive_velocity_tl<T>;
+	case CONTMECH_VELOCITY_GRADIENT_TL: return &contmech_velocity_gradient_tl<T>;
+	}
+	return nullptr;
+}
+WkAct wk_action(uint32_t a) {
+	typedef particle_tl_weak T;
+	switch (a) {
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case DERIVE_DISPLACEMENT_WEAK: return &derive_displacement_weak<T>;
+	case DERIVE_VELOCITY_TL_WEAK: return &derive_velocity_tl_weak<T>;
+	case CONTMECH_VELOCITY_GRADIENT_TL_GP: return &contmech_velocity_gradient_tl_gp<T>;
+	case CONTMECH_CONTINUITY_GP: return &contmech_continuity_gp<T>;
+	case MATERIAL_EOS_GP: return &material_eos_gp<T>;
+	case MATERIAL_STRESS_RATE_JAUMANN_GP: return &material_stress_rate_jaumann_gp<T>;
+	case CONTMECH_CAUCHY_TO_NOMINAL_GP: return &contmech_cauchy_to_nominal_gp<T>;
+	case DERIVE_STRESS_WEAK_TL: return &derive_stress_weak_tl<T>;
+	case CONTMECH_MOMENTUM_TL_WEAK: return &contmech_momentum_tl_weak<T>;
+	}
+	return nullptr;
+}
+
+// --- pull boundary conditions of tensile.cpp:20-42 with a case-given speed.  A
+// boundary_conditions<T> functor is a plain function pointer, so each speed in
+// use gets a slot in a small table.
+double g_bc_speed[8];
+template <typename T, int K>
+void pull_bc(T* p) {
+	double v = g_bc_speed[K];
+	p->x = p->X + v * simulation_time::getInstance().get_time();
+	p->y = p->Y;
+	p->vx = v;
+	p->vy = 0.;
+	p->vx_t = 0.;
+	p->vy_t = 0.;
+}
+template <typename T>
+void (*pull_fn(int k))(T*) {
+	switch (k) {
+	case 0: return &pull_bc<T, 0>;
+	case 1: return &pull_bc<T, 1>;
+	case 2: return &pull_bc<T, 2>;
+	case 3: return &pull_bc<T, 3>;
+	}
+	return nullptr;
+}
+
+simulation_data make_sim_data(const Case& c) {
+	physical_constants pc(c.nu, c.E, c.rho0);
+	correction_constants cc(constants_monaghan(c.wdeltap, c.corr_exp, c.mghn_eps),
+	                        constants_artificial_viscosity(c.alpha, c.beta, c.eta), c.xsph_eps, c.do_smooth != 0);
+	return simulation_data(pc, cc);
+}
+
+template <typename T>
+T** make_particles(const BodyIn& in) {
+	T** p = new T*[in.n];
+	for (unsigned i = 0; i < in.n; i++) {
+		p[i] = new T(i);
+		double* f[NIN] = {&p[i]->x, &p[i]->y, &p[i]->X, &p[i]->Y, &p[i]->m, &p[i]->rho, &p[i]->h, &p[i]->quad_weight,
+		                  &p[i]->vx, &p[i]->vy, &p[i]->Sxx, &p[i]->Sxy, &p[i]->Syy};
+		for (int a = 0; a < NIN; a++) *f[a] = in.a[a][i];
+	}
+	return p;
+}
+
+template <typename T>
+boundary_conditions<T> make_bcs(const BodyIn& in, int& slot) {
+	boundary_conditions<T> bc;
+	for (const BC& b : in.bcs) {
+		if (b.kind != BC_PULL_TL || slot >= 4) { fprintf(stderr, "unsupported boundary condition\n"); exit(2); }
+		g_bc_speed[slot] = b.v;
+		bc.add_boundary_condition(b.idx, pull_fn<T>(slot));
+		slot++;
+	}
+	return bc;
+}
+
+void write_header(Writer& w, const Case& c) {
+	w.raw("MFOUT1\0\0", 8);
+	w.u32(c.nbodies);
+	for (auto& b : c.bodies) w.u32(b.n);
+}
+
+template <typename T>
+void dump(Writer& w, unsigned step, std::vector<body<T>>& bodies) {
+	w.u32(1);
+	w.u32(step);
+	w.f64(simulation_time::getInstance().get_time());
+	for (auto& b : bodies) {
+		T** p = b.get_particles();
+		unsigned n = b.get_num_part();
+		for (int k = 0; k < NOUT; k++)
+			for (unsigned i = 0; i < n; i++) {
+				double v = 0.;
+				switch (k) {
+				case 0: v = p[i]->x; break;
+				case 1: v = p[i]->y; break;
+				case 2: v = p[i]->vx; break;
+				case 3: v = p[i]->vy; break;
+				case 4: v = p[i]->rho; break;
+				case 5: v = p[i]->Sxx; break;
+				case 6: v = p[i]->Sxy; break;
+				case 7: v = p[i]->Syy; break;
+				case 8: v = p[i]->fcx; break;
+				case 9: v = p[i]->fcy; break;
+				}
+				w.f64(v);
+			}
+	}
+}
+
+template <typename T>
+void run_loop(Writer& w, const Case& c, std::vector<body<T>>& bodies) {
+	double secs = 0.;
+	for (unsigned s = 1; s <= c.nsteps; s++) {
+		auto t0 = std::chrono::steady_clock::now();
+		for (unsigned i = 0; i < bodies.size(); i++) {
+			g_cur_body = (int)i;
+			bodies[i].step();
+			bodies[i].update_boundary();
+		}
+		if (c.contact)
+			for (unsigned i = 0; i < bodies.size(); i++)
+				for (unsigned j = 0; j < bodies.size(); j++)
+					if (i != j) contact_apply_body_to_boundary(bodies[i], bodies[j]);
+		secs += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+		if ((c.dump_every && s % c.dump_every == 0) || s == c.nsteps) dump(w, s, bodies);
+	}
+	if (c.nsteps == 0) dump(w, 0, bodies);
+	w.u32(2);
+	for (unsigned b = 0; b < bodies.size(); b++) {
+		auto& L = g_nbh[b];
+		unsigned n = bodies[b].get_num_part();
+		w.u32(n);
+		for (unsigned i = 0; i < n; i++) w.u32(i < L.size() ? (uint32_t)L[i].size() : 0u);
+		for (unsigned i = 0; i < n && i < L.size(); i++) w.raw(L[i].data(), L[i].size() * 4);
+	}
+	w.u32(3);
+	w.f64(secs);
+	w.u32(0);
+}
+
+template <typename T>
+void attach_hull(body<T>& b, const std::vector<uint32_t>& hull) {
+	if (hull.empty()) return;
+	std::vector<unsigned int> idx(hull.begin(), hull.end());
+	b.set_boundary(new boundary<T>(idx, b.get_particles()));
+}
+
+int run_case(const Case& c, const char* out) {
+	Writer w(out);
+	write_header(w, c);
+	g_nbh.assign(c.nbodies, {});
+	g_recorded.assign(c.nbodies, false);
+	simulation_data sd = make_sim_data(c);
+	int slot = 0;
+	if (c.nbh_eps != 1e-6 && c.method != UL) {
+		fprintf(stderr, "the reference's find_neighbors has a fixed 1e-6 epsilon\n");
+		return 2;
+	}
+	if (c.method == UL) {
+		if (c.nbh_eps != 1e-6) { fprintf(stderr, "the reference's grid has a fixed 1e-6 epsilon\n"); return 2; }
+		typedef particle_monaghan T;
+		std::vector<body<T>> bodies;
+		for (const BodyIn& in : c.bodies) {
+			T** p = make_particles<T>(in);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot)));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
+			for (uint32_t a : c.actions) {
+				UlAct f = ul_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for UL\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+			bodies[b].add_action(&record_first_nbh<T>);
+		}
+		run_loop(w, c, bodies);
+	} else if (c.method == TL) {
+		typedef particle_tl T;
+		std::vector<body<T>> bodies;
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			const BodyIn& in = c.bodies[b];
+			T** p = make_particles<T>(in);
+			find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
+			precomp_randles_libersky<T>(p, in.n);
+			record_fixed_nbh(p, in.n, (int)b);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot)));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
+			for (uint32_t a : c.actions) {
+				TlAct f = tl_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for TL\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+		}
+		run_loop(w, c, bodies);
+	} else if (c.method == TL_WEAK) {
+		typedef particle_tl_weak T;
+		std::vector<body<T>> bodies;
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			const BodyIn& in = c.bodies[b];
+			T** p = make_particles<T>(in);
+			std::vector<element> elements = element_map_rectangle(in.ex, in.ey);
+			unsigned num_gp = 2 * 2 * elements.size();
+			T** gp = new T*[num_gp];
+			for (unsigned i = 0; i < num_gp; i++) gp[i] = new T(i);
+			gauss_int gi(elements, 2);
+			gi.update_gauss_points(p, gp);
+			for (unsigned i = 0; i < num_gp; i++) { gp[i]->h = c.gp_h; gp[i]->rho = c.gp_rho; }
+			find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
+			find_neighbors(p, in.n, gp, num_gp, c.nbh_h, distance_euclidian);
+			precomp_rkpm<T>(p, gp, num_gp);
+			precomp_rkpm<T>(p, in.n);
+			record_fixed_nbh(p, in.n, (int)b);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot), gp, num_gp));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			for (uint32_t a : c.actions) {
+				WkAct f = wk_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for TL_WEAK\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+		}
+		run_loop(w, c, bodies);
+	}
+	return 0;
+}
+
+// ---------------------------------------------------------------- scenarios
+void write_case(const char* path, const Case& c) {
+	Writer w(path);
+	w.raw("MFCASE1\0", 8);
+	w.u32(c.method); w.u32(c.nbodies); w.u32(c.nsteps); w.u32(c.dump_every); w.u32(c.contact);
+	w.u32((uint32_t)c.actions.size());
+	for (uint32_t a : c.actions) w.u32(a);
+	w.f64(c.dt);
+	w.f64(c.nu); w.f64(c.E); w.f64(c.rho0);
+	w.f64(c.wdeltap); w.f64(c.corr_exp); w.f64(c.mghn_eps);
+	w.f64(c.alpha); w.f64(c.beta); w.f64(c.eta);
+	w.f64(c.xsph_eps);
+	w.u32(c.do_smooth);
+	w.f64(c.nbh_h); w.f64(c.nbh_eps);
+	w.f64(c.gp_h); w.f64(c.gp_rho);
+	for (const BodyIn& b : c.bodies) {
+		w.u32(b.n);
+		for (int k = 0; k < NIN; k++) w.raw(b.a[k].data(), b.n * 8);
+		w.u32((uint32_t)b.hull.size());
+		w.raw(b.hull.data(), b.hull.size() * 4);
+		w.u32((uint32_t)b.bcs.size());
+		for (const BC& bc : b.bcs) {
+			w.u32(bc.kind); w.f64(bc.v); w.u32((uint32_t)bc.idx.size());
+			w.raw(bc.idx.data(), bc.idx.size() * 4);
+		}
+		w.u32(b.ex); w.u32(b.ey);
+	}
+}
+
+template <typename T>
+BodyIn capture(body<T>& b) {
+	BodyIn in;
+	in.n = b.get_num_part();
+	T** p = b.get_particles();
+	for (int k = 0; k < NIN; k++) in.a[k].resize(in.n);
+	for (unsigned i = 0; i < in.n; i++) {
+		double f[NIN] = {p[i]->x, p[i]->y, p[i]->X, p[i]->Y, p[i]->m, p[i]->rho, p[i]->h, p[i]->quad_weight,
+		                 p[i]->vx, p[i]->vy, p[i]->Sxx, p[i]->Sxy, p[i]->Syy};
+		for (int k = 0; k < NIN; k++) in.a[k][i] = f[k];
+	}
+	if (b.has_boundary()) {
+		const unsigned* ix = b.get_boundary()->indexes();
+		in.hull.assign(ix, ix + b.get_boundary()->num_bound());
+	}
+	return in;
+}
+
+void fill_consts(Case& c, simulation_data sd, double dt) {
+	physical_constants pc = sd.get_physical_constants();
+	correction_constants cc = sd.get_correction_constants();
+	c.dt = dt;
+	c.nu = pc.nu(); c.E = pc.E(); c.rho0 = pc.rho0();
+	c.wdeltap = cc.get_monaghan_const().mghn_wdeltap();
+	c.corr_exp = cc.get_monaghan_const().mghn_corr_exp();
+	c.mghn_eps = cc.get_monaghan_const().mghn_eps();
+	c.alpha = cc.get_art_visc_const().artvisc_alpha();
+	c.beta = cc.get_art_visc_const().artvisc_beta();
+	c.eta = cc.get_art_visc_const().artvisc_eta();
+	c.xsph_eps = cc.xsph_eps();
+	c.do_smooth = cc.do_smooth() ? 1 : 0;
+}
+
+int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const char* case_out, const char* out) {
+	Case c;
+	c.nsteps = nsteps;
+	c.nbh_eps = 1e-6;
+	g_nbh.assign(2, {});
+	g_recorded.assign(2, false);
+	const std::vector<uint32_t> ul_actions = {RIEMANN_UPDATE_INTEGRATION_WEIGHTS, MATERIAL_EOS, CORRECTORS_MGHN_ARTIFICIAL_STRESS,
+	                                          DERIVE_STRESS_MONAGHAN, DERIVE_VELOCITY, CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
+	                                          CORRECTORS_XSPH, MATERIAL_STRESS_RATE_JAUMANN, CONTMECH_CONTINUITY,
+	                                          CONTMECH_MOMENTUM_UL, CONTMECH_ADVECTION};  // rings.cpp:86-96,609-619
+	if (name == "rings_monaghan" || name == "rings_monaghan_contact") {
+		std::vector<body<particle_monaghan>> bodies = name == "rings_monaghan" ? rings_monaghan(nbox) : rings_monaghan_contact(nbox);
+		c.method = UL;
+		c.contact = name == "rings_monaghan_contact";
+		c.actions = ul_actions;
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		for (auto& b : bodies) { c.bodies.push_back(capture(b)); b.add_action(&record_first_nbh<particle_monaghan>); }
+		c.nbodies = (uint32_t)bodies.size();
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "rings_tl_contact") {
+		std::vector<body<particle_tl>> bodies = rings_tl_contact(nbox);
+		c.method = TL;
+		c.contact = 1;
+		c.actions = {DERIVE_DISPLACEMENT, MATERIAL_COMPUTE_STRESS_GREEN_STVENANT, CONTMECH_CAUCHY_TO_NOMINAL, DERIVE_STRESS_TL,
+		             CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY, CONTMECH_MOMENTUM_TL, CONTMECH_ADVECTION};  // rings.cpp:419-425
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;  // hdx*dx, rings.cpp:404-407
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			c.bodies.push_back(capture(bodies[b]));
+			record_fixed_nbh(bodies[b].get_particles(), bodies[b].get_num_part(), (int)b);
+		}
+		c.nbodies = (uint32_t)bodies.size();
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "tensile_tl") {
+		std::vector<body<particle_tl>> bodies = tensile_tl(nbox);
+		c.method = TL;
+		c.actions = {DERIVE_DISPLACEMENT, DERIVE_VELOCITY_TL, CONTMECH_VELOCITY_GRADIENT_TL, CONTMECH_CONTINUITY, MATERIAL_EOS,
+		             MATERIAL_STRESS_RATE_JAUMANN, CONTMECH_CAUCHY_TO_NOMINAL, DERIVE_STRESS_TL,
+		             CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY, CONTMECH_MOMENTUM_TL, CONTMECH_ADVECTION};  // tensile.cpp:276-286
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;
+		BodyIn in = capture(bodies[0]);
+		BC l, r;  // tensile.cpp:234-246,262-264
+		l.kind = r.kind = BC_PULL_TL;
+		l.v = -10.; r.v = 10.;
+		for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+		in.bcs = {l, r};
+		c.bodies.push_back(in);
+		record_fixed_nbh(bodies[0].get_particles(), bodies[0].get_num_part(), 0);
+		c.nbodies = 1;
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "tensile_tl_weak") {
+		std::vector<body<particle_tl_weak>> bodies = tensile_tl_weak(nbox);
+		c.method = TL_WEAK;
+		c.actions = {DERIVE_DISPLACEMENT_WEAK, DERIVE_VELOCITY_TL_WEAK, CONTMECH_VELOCITY_GRADIENT_TL_GP, CONTMECH_CONTINUITY_GP,
+		             MATERIAL_EOS_GP, MATERIAL_STRESS_RATE_JAUMANN_GP, CONTMECH_CAUCHY_TO_NOMINAL_GP, DERIVE_STRESS_WEAK_TL,
+		             CONTMECH_MOMENTUM_TL_WEAK, CONTMECH_ADVECTION};  // tensile.cpp:814-823
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;
+		c.gp_h = bodies[0].get_particles()[0]->h;  // Gauss points get hdx*dx too, tensile.cpp:792-795
+		c.gp_rho = c.rho0;
+		BodyIn in = capture(bodies[0]);
+		in.ex = nbox - 1; in.ey = nbox - 1;
+		BC l, r;
+		l.kind = r.kind = BC_PULL_TL;
+		l.v = -10.; r.v = 10.;
+		for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+		in.bcs = {l, r};
+		c.bodies.push_back(in);
+		record_fixed_nbh(bodies[0].get_particles(), bodies[0].get_num_part(), 0);
+		c.nbodies = 1;
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else {
+		fprintf(stderr, "unknown scenario %s\n", name.c_str());
+		return 2;
+	}
+	return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+	if (argc >= 4 && std::string(argv[1]) == "run") {
+		Case c = read_case(argv[2]);
+		return run_case(c, argv[3]);
+	}
+	if (argc >= 7 && std::string(argv[1]) == "scenario")
+		return run_scenario(argv[2], (unsigned)atoi(argv[3]), (unsigned)atoi(argv[4]), argv[5], argv[6]);
+	fprintf(stderr, "usage: %s run CASE RESULT | scenario NAME NBOX NSTEPS CASE_OUT RESULT\n", argv[0]);
+	return 2;
+}
