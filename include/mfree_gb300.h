@@ -1,0 +1,193 @@
+/*
+ * mfree_gb300 -- C ABI of the GB300 (sm_103a) explicit meshless time step.
+ *
+ * This is the drop-in boundary for the reference's step loop: the caller builds
+ * bodies of particles, registers the reference's action callbacks by id, optional
+ * Dirichlet boundary conditions and contact boundaries, and steps.  Plain pointers
+ * and sizes only; the context owns all device memory, the caller owns every host
+ * buffer.  One context per host thread; calls on one context are not reentrant.
+ * Every function returns an mf_status (0 = ok, < 0 = error); mf_last_error() gives
+ * the message of the last failure on a context.
+ *
+ * Reference interfaces replaced (paths within the reference's src/):
+ *   body<T>::body(particles, n, simulation_data, dt, bc)    body.h:216-217,228-233
+ *   body<T>::add_action(void (*)(body<T>&))                  body.h:219-221
+ *   body<T>::step()                                          body.h:223-225
+ *   body<T>::set_boundary / update_boundary                  body.h:153-166,178
+ *   boundary_conditions<T>::add_boundary_condition           boundary_conditions.h:32-34
+ *   contact_apply_body_to_boundary(master, slave)            contact.h:36-80
+ *   convex_hull(particles, n)                                convex_hull.h:62-95
+ *   the step loop of main()                                  mfree_iwf.cpp:84-97
+ */
+#ifndef MFREE_GB300_H
+#define MFREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MF_API __attribute__((visibility("default")))
+#else
+#define MF_API
+#endif
+
+typedef struct mf_ctx mf_ctx;
+typedef int32_t mf_status;
+
+enum {
+	MF_OK = 0,
+	MF_ERR_ARG = -1,           /* invalid argument */
+	MF_ERR_CUDA = -2,          /* CUDA runtime error (message in mf_last_error) */
+	MF_ERR_NBH_OVERFLOW = -3,  /* neighbour count reached the capacity (the reference's assert, grid.h:167) */
+	MF_ERR_NONFINITE = -4,     /* NaN/Inf in the state (the reference traps FE_INVALID|FE_OVERFLOW, mfree_iwf.cpp:40) */
+	MF_ERR_TIMEOUT = -5,       /* a bounded device wait gave up */
+	MF_ERR_PIPELINE = -6,      /* an action list the fused kernels do not implement */
+	MF_ERR_GRID = -7,          /* num_cell >= n (grid.h:114) or a particle outside the grid */
+	MF_ERR_STATE = -8,         /* call not valid in the context's current state */
+	MF_ERR_NO_DEVICE = -9,     /* no CUDA device */
+	MF_ERR_SINGULAR = -10,     /* singular corrector matrix (precomp_shape_functions.h:45) */
+	MF_ERR_NO_NEIGHBOR = -11,  /* a particle without neighbours (grid.h:168) */
+	MF_ERR_CAPACITY = -12      /* a size beyond a documented maximum */
+};
+
+/* Method families (the reference's particle types). */
+typedef enum {
+	MF_METHOD_UL = 1,      /* particle_monaghan: updated-Lagrangian Gray-Monaghan SPH, grid rebuilt per stage */
+	MF_METHOD_TL = 2,      /* particle_tl: total-Lagrangian SPH, fixed neighbours, Randles-Libersky correction */
+	MF_METHOD_TL_WEAK = 3  /* particle_tl_weak: weak-form TL with RKPM shape functions and Gauss points */
+} mf_method;
+
+/* Arithmetic forms. */
+typedef enum {
+	MF_PREC_FP64_STRICT = 0, /* FP64, no FMA contraction: the reference-parity form */
+	MF_PREC_FP64 = 1,        /* FP64 with FMA contraction */
+	MF_PREC_MIXED = 2        /* FP32 pair sums; FP64 position/velocity RK4 state and 2x2/3x3 inversions */
+} mf_precision;
+
+/* Action callbacks of the reference, by id (body<T>::add_action). */
+typedef enum {
+	MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS = 1,     /* riemann_integration.h:28-33 */
+	MF_MATERIAL_EOS = 2,                           /* material.h:56-64 */
+	MF_CORRECTORS_MGHN_ARTIFICIAL_STRESS = 3,      /* correctors.h:43-81 */
+	MF_DERIVE_STRESS_MONAGHAN = 4,                 /* derivatives.h:378-443 */
+	MF_DERIVE_VELOCITY = 5,                        /* derivatives.h:32-66 */
+	MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY = 6,   /* correctors.h:83-137 */
+	MF_CORRECTORS_XSPH = 7,                        /* correctors.h:139-169 */
+	MF_MATERIAL_STRESS_RATE_JAUMANN = 8,           /* material.h:95-100 */
+	MF_CONTMECH_CONTINUITY = 9,                    /* cont_mech.h:122-126 */
+	MF_CONTMECH_MOMENTUM_UL = 10,                  /* cont_mech.h:32-49 */
+	MF_CONTMECH_ADVECTION = 11,                    /* cont_mech.h:134-142 */
+	MF_DERIVE_DISPLACEMENT = 12,                   /* derivatives.h:101-149 */
+	MF_MATERIAL_COMPUTE_STRESS_GREEN_STVENANT = 13,/* material.h:155-161 */
+	MF_CONTMECH_CAUCHY_TO_NOMINAL = 14,            /* cont_mech.h:213-218 */
+	MF_DERIVE_STRESS_TL = 15,                      /* derivatives.h:331-376 */
+	MF_CONTMECH_MOMENTUM_TL = 16,                  /* cont_mech.h:70-87 */
+	MF_DERIVE_VELOCITY_TL = 17,                    /* derivatives.h:483-519 */
+	MF_CONTMECH_VELOCITY_GRADIENT_TL = 18,         /* cont_mech.h:188-203 */
+	MF_DERIVE_DISPLACEMENT_WEAK = 19,              /* derivatives.h:152-200 */
+	MF_DERIVE_VELOCITY_TL_WEAK = 20,               /* derivatives.h:445-481 */
+	MF_CONTMECH_VELOCITY_GRADIENT_TL_GP = 21,      /* cont_mech.h:171-186 */
+	MF_CONTMECH_CONTINUITY_GP = 22,                /* cont_mech.h:128-132 */
+	MF_MATERIAL_EOS_GP = 23,                       /* material.h:46-54 */
+	MF_MATERIAL_STRESS_RATE_JAUMANN_GP = 24,       /* material.h:86-93 */
+	MF_CONTMECH_CAUCHY_TO_NOMINAL_GP = 25,         /* cont_mech.h:206-211 */
+	MF_DERIVE_STRESS_WEAK_TL = 26,                 /* derivatives.h:260-294 */
+	MF_CONTMECH_MOMENTUM_TL_WEAK = 27              /* cont_mech.h:89-106 */
+} mf_action;
+
+/* Boundary-condition kinds (boundary_conditions<T> functors). */
+typedef enum {
+	MF_BC_PULL = 1  /* x = X + v*t, y = Y, vx = v, vy = 0, vx_t = vy_t = 0 (tensile.cpp:20-42) */
+} mf_bc_kind;
+
+typedef struct mf_config {
+	int32_t method;      /* mf_method; every body of a context uses it */
+	int32_t precision;   /* mf_precision */
+	int32_t device;      /* CUDA device ordinal */
+	uint32_t max_nbh;    /* neighbour capacity per particle; the reference's MAX_NBH is 200 (0 = 200) */
+	double nbh_eps;      /* absolute epsilon of the predicate r^2 <= 4h^2 + eps (the reference: 1e-6) */
+	double nbh_h;        /* TL / TL_WEAK: the h given to the set-up neighbour search (neighbor_search.h:116) */
+	int32_t contact;     /* 1: after every step, penalty contact between bodies of a group (mfree_iwf.cpp:91-97) */
+	int32_t reserved;
+} mf_config;
+
+/* simulation_data (simulation_data.h:25-99) */
+typedef struct mf_sim_data {
+	double nu, E, rho0;                          /* physical_constants */
+	double mghn_wdeltap, mghn_corr_exp, mghn_eps;/* constants_monaghan */
+	double artvisc_alpha, artvisc_beta, artvisc_eta; /* constants_artificial_viscosity */
+	double xsph_eps;
+	int32_t do_smooth;                           /* correctors_smooth_vel after each TL_WEAK step */
+	int32_t reserved;
+} mf_sim_data;
+
+/* Initial particle state, host SoA of n doubles each (particle.h:42-47).
+ * X, Y may be NULL for MF_METHOD_UL (they are then copies of x, y). */
+typedef struct mf_particles {
+	const double *x, *y, *X, *Y, *m, *rho, *h, *quad_weight, *vx, *vy, *Sxx, *Sxy, *Syy;
+} mf_particles;
+
+/* Output state, host SoA; any pointer may be NULL to skip that field. */
+typedef struct mf_state {
+	double *x, *y, *vx, *vy, *rho, *Sxx, *Sxy, *Syy, *fcx, *fcy;
+} mf_state;
+
+/* Context lifetime. */
+MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out);
+MF_API void mf_destroy(mf_ctx* ctx);
+MF_API const char* mf_last_error(const mf_ctx* ctx);
+MF_API const char* mf_status_string(mf_status s);
+
+/* A body: n particles, its simulation_data and time step (body.h:228-233).
+ * group: bodies with the same group are one simulation (contact only within a group). */
+MF_API mf_status mf_add_body(mf_ctx* ctx, const mf_particles* p, uint32_t n, const mf_sim_data* sd, double dt,
+                             int32_t group, int32_t* body_id);
+/* Append an action to a body's action list (body.h:219-221). */
+MF_API mf_status mf_add_action(mf_ctx* ctx, int32_t body, int32_t action);
+/* Dirichlet condition on particles idx[0..k) (boundary_conditions.h:32-34). */
+MF_API mf_status mf_add_boundary_condition(mf_ctx* ctx, int32_t body, const uint32_t* idx, uint32_t k, int32_t kind,
+                                           double value);
+/* Contact boundary: particle indices of the body's outline, in tour order (body.h:178, boundary.h:37-48). */
+MF_API mf_status mf_set_boundary(mf_ctx* ctx, int32_t body, const uint32_t* idx, uint32_t nb);
+/* Convex hull (monotone chain, collinear points kept) of n points: the reference's
+ * set-up for contact boundaries (convex_hull.h:62-95).  out_idx holds n entries. */
+MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, uint32_t* out_idx, uint32_t* out_n);
+
+/* Advance every body by nsteps RK4 steps in the reference driver's order: all bodies
+ * step, boundaries are updated, then contact between ordered body pairs. */
+MF_API mf_status mf_step(mf_ctx* ctx, int32_t nsteps);
+/* Block until all queued work is done; returns the first device error. */
+MF_API mf_status mf_synchronize(mf_ctx* ctx);
+
+/* State access (device -> caller-owned host buffers, synchronous). */
+MF_API mf_status mf_get_state(mf_ctx* ctx, int32_t body, const mf_state* out);
+/* Overwrite a body's state (x, y, vx, vy, rho, Sxx, Sxy, Syy; NULL fields kept). */
+MF_API mf_status mf_set_state(mf_ctx* ctx, int32_t body, const mf_particles* p);
+MF_API mf_status mf_get_time(mf_ctx* ctx, int32_t body, double* t);
+MF_API mf_status mf_num_particles(mf_ctx* ctx, int32_t body, uint32_t* n);
+
+/* Neighbour lists of a body's current state, as particle indices within the body:
+ * for MF_METHOD_UL those of the next first-stage grid (grid.h:117-177), for TL the
+ * fixed set-up lists.  counts[n]; idx holds up to cap entries; *total = sum(counts). */
+MF_API mf_status mf_get_neighbors(mf_ctx* ctx, int32_t body, uint32_t* counts, uint32_t* idx, uint64_t cap,
+                                  uint64_t* total);
+
+/* Instrumentation: CUDA-event timing of the kernels, per kernel class. */
+MF_API mf_status mf_set_timing(mf_ctx* ctx, int32_t enable);
+/* kind: 0 = UL pair, 1 = TL pass A, 2 = TL pass B, 3 = contact, 4 = grid build, 5 = weak (Gauss) pass.
+ * Returns the summed event time in ms, the launch count and rows processed. */
+MF_API mf_status mf_kernel_stats(mf_ctx* ctx, int32_t kind, double* total_ms, uint64_t* launches, uint64_t* rows);
+/* Number of kernel launches issued by this context since creation. */
+MF_API mf_status mf_launch_count(mf_ctx* ctx, uint64_t* launches);
+/* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
+MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

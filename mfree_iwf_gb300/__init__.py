@@ -1,0 +1,301 @@
+"""mfree_iwf_gb300 -- the explicit meshless time step of mfree_iwf on one GB300 (sm_103a).
+
+The compute path is the CUDA library ``libmfree_gb300.so`` behind the C ABI declared
+in ``include/mfree_gb300.h``.  This module is a thin host-side mirror of the
+reference's set-up interface -- ``body(particles, n, simulation_data, dt, bc)``,
+``body::add_action``, ``boundary_conditions::add_boundary_condition``,
+``body::set_boundary`` and the step loop of ``main()`` -- over ctypes.  There is no
+CPU fallback: if the library is missing, loading it raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import actions
+from .actions import *  # noqa: F401,F403  (action ids)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmfree_gb300.so")
+
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK = 1, 2, 3
+PREC_FP64_STRICT, PREC_FP64, PREC_MIXED = 0, 1, 2
+PRECISIONS = {"fp64_strict": PREC_FP64_STRICT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
+BC_PULL = 1
+
+STATUS = {
+    0: "MF_OK", -1: "MF_ERR_ARG", -2: "MF_ERR_CUDA", -3: "MF_ERR_NBH_OVERFLOW", -4: "MF_ERR_NONFINITE",
+    -5: "MF_ERR_TIMEOUT", -6: "MF_ERR_PIPELINE", -7: "MF_ERR_GRID", -8: "MF_ERR_STATE", -9: "MF_ERR_NO_DEVICE",
+    -10: "MF_ERR_SINGULAR", -11: "MF_ERR_NO_NEIGHBOR", -12: "MF_ERR_CAPACITY",
+}
+
+_DP = ctypes.POINTER(ctypes.c_double)
+_UP = ctypes.POINTER(ctypes.c_uint32)
+
+
+class MfConfig(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("max_nbh", ctypes.c_uint32), ("nbh_eps", ctypes.c_double), ("nbh_h", ctypes.c_double),
+                ("contact", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class MfSimData(ctypes.Structure):
+    _fields_ = [("nu", ctypes.c_double), ("E", ctypes.c_double), ("rho0", ctypes.c_double),
+                ("mghn_wdeltap", ctypes.c_double), ("mghn_corr_exp", ctypes.c_double), ("mghn_eps", ctypes.c_double),
+                ("artvisc_alpha", ctypes.c_double), ("artvisc_beta", ctypes.c_double),
+                ("artvisc_eta", ctypes.c_double), ("xsph_eps", ctypes.c_double), ("do_smooth", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+_PFIELDS = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx", "Sxy", "Syy")
+_SFIELDS = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
+
+
+class MfParticles(ctypes.Structure):
+    _fields_ = [(f, _DP) for f in _PFIELDS]
+
+
+class MfState(ctypes.Structure):
+    _fields_ = [(f, _DP) for f in _SFIELDS]
+
+
+class MfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the CUDA library (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: run mfree_iwf_gb300.build.build() first (there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    C = ctypes
+    sig = {
+        "mf_create": (C.c_int32, [C.POINTER(MfConfig), C.POINTER(C.c_void_p)]),
+        "mf_destroy": (None, [C.c_void_p]),
+        "mf_last_error": (C.c_char_p, [C.c_void_p]),
+        "mf_status_string": (C.c_char_p, [C.c_int32]),
+        "mf_add_body": (C.c_int32, [C.c_void_p, C.POINTER(MfParticles), C.c_uint32, C.POINTER(MfSimData), C.c_double,
+                                    C.c_int32, C.POINTER(C.c_int32)]),
+        "mf_add_action": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
+        "mf_add_boundary_condition": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32, C.c_int32, C.c_double]),
+        "mf_set_boundary": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32]),
+        "mf_convex_hull": (C.c_int32, [_DP, _DP, C.c_uint32, _UP, _UP]),
+        "mf_step": (C.c_int32, [C.c_void_p, C.c_int32]),
+        "mf_synchronize": (C.c_int32, [C.c_void_p]),
+        "mf_get_state": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(MfState)]),
+        "mf_set_state": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(MfParticles)]),
+        "mf_get_time": (C.c_int32, [C.c_void_p, C.c_int32, _DP]),
+        "mf_num_particles": (C.c_int32, [C.c_void_p, C.c_int32, _UP]),
+        "mf_get_neighbors": (C.c_int32, [C.c_void_p, C.c_int32, _UP, _UP, C.c_uint64, C.POINTER(C.c_uint64)]),
+        "mf_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
+        "mf_kernel_stats": (C.c_int32, [C.c_void_p, C.c_int32, _DP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "mf_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
+        "mf_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(_DP)
+
+
+def convex_hull(x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """The reference's monotone-chain hull (convex_hull.h:62-95), computed by the library."""
+    lib = load_library()
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros(len(x), np.uint32)
+    n = ctypes.c_uint32(0)
+    st = lib.mf_convex_hull(_dptr(x), _dptr(y), len(x), out.ctypes.data_as(_UP), ctypes.byref(n))
+    if st != 0:
+        raise MfError(st, "convex hull")
+    return out[: n.value].copy()
+
+
+@dataclass
+class SimData:
+    """simulation_data (simulation_data.h:25-99)."""
+    nu: float
+    E: float
+    rho0: float
+    mghn_wdeltap: float = 0.0
+    mghn_corr_exp: float = 0.0
+    mghn_eps: float = 0.0
+    artvisc_alpha: float = 0.0
+    artvisc_beta: float = 0.0
+    artvisc_eta: float = 0.0
+    xsph_eps: float = 0.0
+    do_smooth: int = 0
+
+    def _c(self) -> MfSimData:
+        return MfSimData(self.nu, self.E, self.rho0, self.mghn_wdeltap, self.mghn_corr_exp, self.mghn_eps,
+                         self.artvisc_alpha, self.artvisc_beta, self.artvisc_eta, self.xsph_eps, self.do_smooth, 0)
+
+
+class Simulation:
+    """One mf_ctx: a set of bodies stepped together by the reference driver's loop."""
+
+    def __init__(self, method: int = METHOD_UL, precision="fp64_strict", device: int = 0, max_nbh: int = 200,
+                 nbh_eps: float = 1e-6, nbh_h: float = 0.0, contact: bool = False):
+        self._lib = load_library()
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        cfg = MfConfig(method, prec, device, max_nbh, nbh_eps, nbh_h, 1 if contact else 0, 0)
+        h = ctypes.c_void_p()
+        st = self._lib.mf_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise MfError(st, "mf_create")
+        self._h = h
+        self.method = method
+        self.precision = prec
+        self._keep: List[object] = []
+        self.n_bodies = 0
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.mf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st: int, what: str) -> None:
+        if st != 0:
+            msg = self._lib.mf_last_error(self._h)
+            raise MfError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- set-up (body.h:216-233, boundary_conditions.h:32-34)
+    def add_body(self, arrays: Dict[str, np.ndarray], sim_data: SimData, dt: float, group: int = 0) -> int:
+        n = len(arrays["x"])
+        cols = {}
+        for f in _PFIELDS:
+            a = arrays.get(f)
+            cols[f] = None if a is None else np.ascontiguousarray(a, np.float64)
+        p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
+        bid = ctypes.c_int32(-1)
+        sd = sim_data._c()
+        self._check(self._lib.mf_add_body(self._h, ctypes.byref(p), n, ctypes.byref(sd), dt, group, ctypes.byref(bid)),
+                    "mf_add_body")
+        self.n_bodies += 1
+        return bid.value
+
+    def add_action(self, body: int, action: int) -> None:
+        self._check(self._lib.mf_add_action(self._h, body, int(action)), "mf_add_action")
+
+    def add_boundary_condition(self, body: int, idx: Sequence[int], kind: int, value: float) -> None:
+        a = np.ascontiguousarray(idx, np.uint32)
+        self._check(self._lib.mf_add_boundary_condition(self._h, body, a.ctypes.data_as(_UP), len(a), kind, value),
+                    "mf_add_boundary_condition")
+
+    def set_boundary(self, body: int, idx: Sequence[int]) -> None:
+        a = np.ascontiguousarray(idx, np.uint32)
+        self._check(self._lib.mf_set_boundary(self._h, body, a.ctypes.data_as(_UP), len(a)), "mf_set_boundary")
+
+    # -- stepping (mfree_iwf.cpp:84-97)
+    def step(self, nsteps: int = 1) -> None:
+        self._check(self._lib.mf_step(self._h, int(nsteps)), "mf_step")
+
+    def synchronize(self) -> None:
+        self._check(self._lib.mf_synchronize(self._h), "mf_synchronize")
+
+    # -- state
+    def num_particles(self, body: int) -> int:
+        n = ctypes.c_uint32()
+        self._check(self._lib.mf_num_particles(self._h, body, ctypes.byref(n)), "mf_num_particles")
+        return n.value
+
+    def get_state(self, body: int, fields: Sequence[str] = _SFIELDS) -> Dict[str, np.ndarray]:
+        n = self.num_particles(body)
+        out = {f: np.empty(n, np.float64) for f in fields}
+        s = MfState(*[_dptr(out.get(f)) for f in _SFIELDS])
+        self._check(self._lib.mf_get_state(self._h, body, ctypes.byref(s)), "mf_get_state")
+        return out
+
+    def set_state(self, body: int, arrays: Dict[str, np.ndarray]) -> None:
+        cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
+        p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
+        self._check(self._lib.mf_set_state(self._h, body, ctypes.byref(p)), "mf_set_state")
+
+    def time(self, body: int = 0) -> float:
+        t = ctypes.c_double()
+        self._check(self._lib.mf_get_time(self._h, body, ctypes.byref(t)), "mf_get_time")
+        return t.value
+
+    def neighbors(self, body: int) -> List[np.ndarray]:
+        n = self.num_particles(body)
+        counts = np.zeros(n, np.uint32)
+        tot = ctypes.c_uint64()
+        self._check(self._lib.mf_get_neighbors(self._h, body, counts.ctypes.data_as(_UP), None, 0, ctypes.byref(tot)),
+                    "mf_get_neighbors")
+        idx = np.zeros(max(tot.value, 1), np.uint32)
+        self._check(self._lib.mf_get_neighbors(self._h, body, counts.ctypes.data_as(_UP), idx.ctypes.data_as(_UP),
+                                               tot.value, ctypes.byref(tot)), "mf_get_neighbors")
+        starts = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
+        return [idx[int(starts[i]):int(starts[i + 1])] for i in range(n)]
+
+    # -- instrumentation
+    def set_timing(self, enable: bool) -> None:
+        self._check(self._lib.mf_set_timing(self._h, 1 if enable else 0), "mf_set_timing")
+
+    def kernel_stats(self, kind: int):
+        ms = ctypes.c_double()
+        nl = ctypes.c_uint64()
+        rows = ctypes.c_uint64()
+        self._check(self._lib.mf_kernel_stats(self._h, kind, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(rows)),
+                    "mf_kernel_stats")
+        return ms.value, nl.value, rows.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        self._check(self._lib.mf_launch_count(self._h, ctypes.byref(n)), "mf_launch_count")
+        return n.value
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(self._lib.mf_get_stream(self._h, ctypes.byref(s)), "mf_get_stream")
+        return s.value or 0
+
+
+def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 200, contact: Optional[bool] = None,
+                  groups: Optional[Sequence[int]] = None) -> Simulation:
+    """Build a :class:`Simulation` from a :class:`mfree_iwf_gb300.scenarios.Scenario` (the same
+    bodies, constants, action list, boundary conditions and contact boundaries)."""
+    sim = Simulation(method=sc.method, precision=precision, device=device, max_nbh=max_nbh, nbh_eps=sc.nbh_eps,
+                     nbh_h=sc.nbh_h, contact=bool(sc.contact) if contact is None else contact)
+    sd = SimData(sc.nu, sc.E, sc.rho0, sc.wdeltap, sc.corr_exp, sc.mghn_eps, sc.alpha, sc.beta, sc.eta,
+                 sc.xsph_eps, sc.do_smooth)
+    for k, b in enumerate(sc.bodies):
+        bid = sim.add_body(b.arrays, sd, sc.dt, group=0 if groups is None else groups[k])
+        for a in sc.actions:
+            sim.add_action(bid, a)
+        for bc in b.bcs:
+            sim.add_boundary_condition(bid, bc.idx, BC_PULL, bc.v)
+        if len(b.hull):
+            sim.set_boundary(bid, b.hull)
+    return sim

@@ -1,0 +1,1000 @@
+// Host side of the C ABI (include/mfree_gb300.h): contexts, bodies, action-list
+// validation against the fused pipelines, device memory, and the step loop of the
+// reference driver (mfree_iwf.cpp:84-97) expressed as stream-ordered launches.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mfree_gb300.h"
+#include "mf_kernels.h"
+
+using namespace mfk_host;
+
+namespace {
+
+const uint32_t REF_MAX_NBH = 200;  // particle.h:31
+
+struct HostBC {
+	int32_t kind;
+	double v;
+	std::vector<uint32_t> idx;
+};
+
+struct HostBody {
+	uint32_t off = 0, n = 0;
+	mf_sim_data sd{};
+	double dt = 0., time = 0.;
+	int32_t group = 0;
+	std::vector<int32_t> actions;
+	std::vector<uint32_t> hull;
+	std::vector<HostBC> bcs;
+	std::vector<double> in[13];  // x y X Y m rho h qw vx vy Sxx Sxy Syy
+};
+
+template <class T>
+struct DevBuf {
+	T* p = nullptr;
+	size_t n = 0;
+	cudaError_t alloc(size_t count) {
+		n = count;
+		return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+	}
+	void free() {
+		if (p) cudaFree(p);
+		p = nullptr;
+	}
+};
+
+struct Timing {
+	bool on = false;
+	std::vector<cudaEvent_t> pool;
+	std::vector<std::pair<int, int>> used;  // (kind, pool index of start)
+	double ms[8] = {0};
+	uint64_t launches[8] = {0};
+	uint64_t rows[8] = {0};
+};
+
+}  // namespace
+
+struct mf_ctx {
+	mf_config cfg{};
+	cudaStream_t stream = nullptr;
+	std::string err;
+	std::vector<HostBody> bodies;
+	bool ready = false;
+	uint32_t n_total = 0;
+	uint32_t flags = 0;
+	bool mixed = false, strict = false;
+	uint64_t launches = 0;
+	Timing timing;
+
+	DevStatusH* d_status = nullptr;
+	DevStatusH* h_status = nullptr;
+
+	// common per-row arrays
+	DevBuf<uint32_t> body_of;
+	DevBuf<double> m, h, qw0, fcx, fcy, X, Y;
+	DevBuf<double> sd[4][8];   // base, acc, stage, second stage (TL ping-pong): x y vx vy rho Sxx Sxy Syy
+	DevBuf<float> sf[4][4];    // mixed form: rho Sxx Sxy Syy
+	DevBuf<BodyParams> params;
+	std::vector<BodyParams> h_params;
+
+	// UL
+	DevBuf<Geom> geom;
+	DevBuf<unsigned long long> bbox;
+	DevBuf<uint32_t> total_cells, keys, keys_sorted, perm_in, perm, cell_start, rec_body;
+	DevBuf<unsigned char> rec, sort_tmp;
+	int sort_bits = 1;
+
+	// TL: fixed neighbour lists with corrected gradients, per-stage scratch
+	DevBuf<uint32_t> nbr_off, nbr, bc_rows;
+	DevBuf<double> wx64, wy64, P64, dA64, c64, bc_v;
+	DevBuf<float> wx32, wy32, P32, dA32, c32, qw32, m32, h32;
+	DevBuf<unsigned char> pack;
+	uint32_t n_bc = 0;
+
+	// contact
+	bool contact_on = false;
+	DevBuf<uint32_t> bnd_rows, bnd_start, bnd_len, tile_first, tile_end, slave_rows, slave_master, m_tile_off, m_tile_n;
+	DevBuf<double4> bnd;
+	DevBuf<float4> tile_bb;
+	DevBuf<double> slave_dt;
+	uint32_t n_bnd = 0, n_tiles = 0, n_slave = 0;
+
+	~mf_ctx();
+};
+
+namespace {
+
+mf_status fail(mf_ctx* c, mf_status s, const char* fmt, ...) {
+	if (c) {
+		char buf[512];
+		va_list ap;
+		va_start(ap, fmt);
+		vsnprintf(buf, sizeof buf, fmt, ap);
+		va_end(ap);
+		c->err = buf;
+	}
+	return s;
+}
+
+mf_status cuda_fail(mf_ctx* c, cudaError_t e, const char* where) {
+	return fail(c, MF_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+#define CK(call)                                            \
+	do {                                                    \
+		cudaError_t e_ = (call);                            \
+		if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+	} while (0)
+
+inline uint32_t abit(int a) { return 1u << a; }
+
+mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
+mf_status tl_setup(mf_ctx* c);
+mf_status contact_setup(mf_ctx* c);
+
+// UL pipeline: any subsequence of the reference's rings_monaghan list
+// (rings.cpp:86-96), whose ids ascend, with the data dependencies present.
+mf_status validate_ul(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	flags = 0;
+	int prev = 0;
+	for (int32_t a : acts) {
+		if (a < MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS || a > MF_CONTMECH_ADVECTION)
+			return fail(c, MF_ERR_PIPELINE, "action %d is not an updated-Lagrangian action", a);
+		if (a <= prev) return fail(c, MF_ERR_PIPELINE, "action %d out of the order of the fused UL pipeline", a);
+		prev = a;
+		flags |= abit(a);
+	}
+	if ((flags & abit(MF_CONTMECH_MOMENTUM_UL)) && !(flags & abit(MF_DERIVE_STRESS_MONAGHAN)))
+		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_ul needs derive_stress_monaghan before it");
+	if ((flags & (abit(MF_MATERIAL_STRESS_RATE_JAUMANN) | abit(MF_CONTMECH_CONTINUITY))) &&
+	    !(flags & abit(MF_DERIVE_VELOCITY)))
+		return fail(c, MF_ERR_PIPELINE, "Jaumann rate / continuity need derive_velocity before them");
+	return MF_OK;
+}
+
+BodyParams make_params(const HostBody& b) {
+	BodyParams p{};
+	double nu = b.sd.nu, E = b.sd.E, rho0 = b.sd.rho0;
+	// physical_constants, simulation_data.cpp:32-47
+	double G = E / (2. * (1. + nu));
+	double K = 2.0 * G * (1 + nu) / (3 * (1 - 2 * nu));
+	double c0 = sqrt(K / rho0);
+	p.K = K; p.G = G; p.rho0 = rho0; p.c0sq = c0 * c0;
+	p.E = E; p.nu = nu; p.D = E / (1 - nu * nu);
+	p.wdeltap = b.sd.mghn_wdeltap; p.corr_exp = b.sd.mghn_corr_exp; p.mghn_eps = b.sd.mghn_eps;
+	p.alpha = b.sd.artvisc_alpha; p.beta = b.sd.artvisc_beta; p.eta = b.sd.artvisc_eta; p.xsph_eps = b.sd.xsph_eps;
+	p.dt = b.dt; p.time = b.time;
+	p.off = b.off; p.n = b.n;
+	return p;
+}
+
+ULArgs ul_args(mf_ctx* c, uint32_t stage) {
+	ULArgs a{};
+	a.n_total = c->n_total;
+	a.n_bodies = (uint32_t)c->bodies.size();
+	a.stage = stage;
+	a.flags = c->flags;
+	a.max_nbh = c->cfg.max_nbh;
+	a.strict_grid = c->mixed ? 0u : 1u;
+	a.nbh_eps = c->cfg.nbh_eps;
+	a.params = c->params.p;
+	a.geom = c->geom.p;
+	a.bbox = c->bbox.p;
+	a.total_cells = c->total_cells.p;
+	a.body_of = c->body_of.p;
+	a.m = c->m.p; a.h = c->h.p; a.qw0 = c->qw0.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	StateSoA* s[3] = {&a.base, &a.acc, &a.st};
+	for (int k = 0; k < 3; k++) {
+		double** d[8] = {&s[k]->x, &s[k]->y, &s[k]->vx, &s[k]->vy, &s[k]->rho, &s[k]->Sxx, &s[k]->Sxy, &s[k]->Syy};
+		for (int q = 0; q < 8; q++) *d[q] = c->sd[k][q].p;
+		s[k]->rho_f = c->sf[k][0].p; s[k]->Sxx_f = c->sf[k][1].p; s[k]->Sxy_f = c->sf[k][2].p; s[k]->Syy_f = c->sf[k][3].p;
+	}
+	a.keys = c->keys.p; a.keys_sorted = c->keys_sorted.p; a.perm_in = c->perm_in.p; a.perm = c->perm.p;
+	a.cell_start = c->cell_start.p;
+	a.rec = c->rec.p;
+	a.rec_body = c->rec_body.p;
+	a.sort_tmp = c->sort_tmp.p;
+	a.sort_tmp_bytes = c->sort_tmp.n;
+	a.sort_bits = c->sort_bits;
+	a.status = c->d_status;
+	return a;
+}
+
+// ---------------------------------------------------------------- timing
+cudaEvent_t timing_begin(mf_ctx* c, int kind, int& slot) {
+	slot = -1;
+	if (!c->timing.on) return nullptr;
+	Timing& t = c->timing;
+	if (t.used.size() * 2 + 2 > t.pool.size()) {
+		size_t old = t.pool.size();
+		t.pool.resize(old + 512);
+		for (size_t i = old; i < t.pool.size(); i++) cudaEventCreate(&t.pool[i]);
+	}
+	slot = (int)t.used.size() * 2;
+	t.used.push_back({kind, slot});
+	cudaEventRecord(t.pool[slot], c->stream);
+	return t.pool[slot];
+}
+void timing_end(mf_ctx* c, int slot, uint64_t rows) {
+	if (slot < 0) return;
+	Timing& t = c->timing;
+	cudaEventRecord(t.pool[slot + 1], c->stream);
+	int kind = t.used[slot / 2].first;
+	t.launches[kind]++;
+	t.rows[kind] += rows;
+}
+void timing_collect(mf_ctx* c) {
+	Timing& t = c->timing;
+	for (auto& u : t.used) {
+		float ms = 0.f;
+		if (cudaEventElapsedTime(&ms, t.pool[u.second], t.pool[u.second + 1]) == cudaSuccess) t.ms[u.first] += ms;
+	}
+	t.used.clear();
+}
+
+mf_status check_status(mf_ctx* c) {
+	CK(cudaStreamSynchronize(c->stream));
+	if (c->timing.on) timing_collect(c);
+	DevStatusH s = *c->h_status;
+	if (s.flags == 0) return MF_OK;
+	// clear for the next call
+	c->h_status->flags = 0;
+	c->h_status->first_index = 0xffffffffu;
+	CK(cudaMemcpyAsync(c->d_status, c->h_status, sizeof(DevStatusH), cudaMemcpyHostToDevice, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	if (s.flags & 1u) return fail(c, MF_ERR_NBH_OVERFLOW, "neighbour capacity reached at row %u", s.first_index);
+	if (s.flags & 2u) return fail(c, MF_ERR_NO_NEIGHBOR, "particle without neighbours at row %u", s.first_index);
+	if (s.flags & 4u) return fail(c, MF_ERR_GRID, "cell grid invalid (num_cell >= n or particle outside) near row %u", s.first_index);
+	if (s.flags & 8u) return fail(c, MF_ERR_NONFINITE, "non-finite state at row %u", s.first_index);
+	if (s.flags & 16u) return fail(c, MF_ERR_SINGULAR, "singular corrector matrix at row %u", s.first_index);
+	if (s.flags & 32u) return fail(c, MF_ERR_TIMEOUT, "bounded device wait gave up");
+	return fail(c, MF_ERR_CUDA, "device status 0x%x", s.flags);
+}
+
+// ---------------------------------------------------------------- set-up
+mf_status finalize(mf_ctx* c) {
+	if (c->ready) return MF_OK;
+	if (c->bodies.empty()) return fail(c, MF_ERR_STATE, "no bodies");
+	const std::vector<int32_t>& acts = c->bodies[0].actions;
+	for (auto& b : c->bodies)
+		if (b.actions != acts) return fail(c, MF_ERR_PIPELINE, "all bodies of a context must share one action list");
+	c->mixed = c->cfg.precision == MF_PREC_MIXED;
+	c->strict = c->cfg.precision == MF_PREC_FP64_STRICT;
+	mf_status st = MF_OK;
+	if (c->cfg.method == MF_METHOD_UL) {
+		st = validate_ul(c, acts, c->flags);
+	} else {
+		st = validate_tl(c, acts, c->flags);
+	}
+	if (st != MF_OK) return st;
+	for (auto& b : c->bodies)
+		for (auto& bc : b.bcs)
+			if (c->cfg.method == MF_METHOD_UL) return fail(c, MF_ERR_PIPELINE, "boundary conditions are not supported for UL bodies");
+
+	uint32_t n = c->n_total;
+	CK(c->body_of.alloc(n));
+	std::vector<uint32_t> bof(n);
+	for (size_t b = 0; b < c->bodies.size(); b++)
+		for (uint32_t i = 0; i < c->bodies[b].n; i++) bof[c->bodies[b].off + i] = (uint32_t)b;
+	CK(cudaMemcpy(c->body_of.p, bof.data(), n * 4, cudaMemcpyHostToDevice));
+
+	auto upload = [&](DevBuf<double>& d, int field) -> mf_status {
+		CK(d.alloc(n));
+		std::vector<double> v(n);
+		for (auto& b : c->bodies) std::copy(b.in[field].begin(), b.in[field].end(), v.begin() + b.off);
+		CK(cudaMemcpy(d.p, v.data(), n * 8, cudaMemcpyHostToDevice));
+		return MF_OK;
+	};
+	// 0 x 1 y 2 X 3 Y 4 m 5 rho 6 h 7 qw 8 vx 9 vy 10 Sxx 11 Sxy 12 Syy
+	if ((st = upload(c->m, 4)) || (st = upload(c->h, 6)) || (st = upload(c->qw0, 7)) || (st = upload(c->X, 2)) ||
+	    (st = upload(c->Y, 3)))
+		return st;
+	CK(c->fcx.alloc(n)); CK(c->fcy.alloc(n));
+	CK(cudaMemset(c->fcx.p, 0, n * 8)); CK(cudaMemset(c->fcy.p, 0, n * 8));
+	const int fld[8] = {0, 1, 8, 9, 5, 10, 11, 12};
+	for (int k = 0; k < 3; k++) {
+		for (int q = 0; q < 8; q++) {
+			bool fp64 = !c->mixed || q < 4;
+			if (!fp64) continue;
+			if (k == 0) {
+				if ((st = upload(c->sd[0][q], fld[q]))) return st;
+			} else {
+				CK(c->sd[k][q].alloc(n));
+				CK(cudaMemset(c->sd[k][q].p, 0, n * 8));
+			}
+		}
+		if (c->mixed) {
+			for (int q = 0; q < 4; q++) {
+				CK(c->sf[k][q].alloc(n));
+				if (k == 0) {
+					std::vector<float> v(n);
+					for (auto& b : c->bodies)
+						for (uint32_t i = 0; i < b.n; i++) v[b.off + i] = (float)b.in[fld[4 + q]][i];
+					CK(cudaMemcpy(c->sf[0][q].p, v.data(), n * 4, cudaMemcpyHostToDevice));
+				} else {
+					CK(cudaMemset(c->sf[k][q].p, 0, n * 4));
+				}
+			}
+		}
+	}
+	c->h_params.clear();
+	for (auto& b : c->bodies) c->h_params.push_back(make_params(b));
+	CK(c->params.alloc(c->h_params.size()));
+	CK(cudaMemcpy(c->params.p, c->h_params.data(), c->h_params.size() * sizeof(BodyParams), cudaMemcpyHostToDevice));
+
+	// UL grid machinery (also used for the UL neighbour dump)
+	if (c->cfg.method == MF_METHOD_UL) {
+		uint32_t nb = (uint32_t)c->bodies.size();
+		CK(c->geom.alloc(nb));
+		CK(c->bbox.alloc(5 * (size_t)nb));
+		CK(c->total_cells.alloc(1));
+		CK(c->keys.alloc(n)); CK(c->keys_sorted.alloc(n)); CK(c->perm_in.alloc(n)); CK(c->perm.alloc(n));
+		CK(c->cell_start.alloc((size_t)n + 2));
+		CK(c->rec_body.alloc(n));
+		CK(c->rec.alloc((size_t)n * 128));
+		int bits = 1;
+		while (bits < 32 && (1ull << bits) < (uint64_t)n + 2) bits++;
+		c->sort_bits = bits;
+		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
+		CK(c->sort_tmp.alloc(tmp));
+	} else {
+		mf_status s2 = tl_setup(c);
+		if (s2 != MF_OK) return s2;
+	}
+	{
+		mf_status s2 = contact_setup(c);
+		if (s2 != MF_OK) return s2;
+	}
+	c->ready = true;
+	return MF_OK;
+}
+
+mf_status ul_step(mf_ctx* c) {
+	for (uint32_t s = 0; s < 4; s++) {
+		ULArgs a = ul_args(c, s);
+		int slot;
+		timing_begin(c, 0, slot);
+		// the pair kernel is timed together with its gather; the grid build separately
+		cudaError_t e = c->strict ? mf_strict::ul_stage(a, c->mixed, c->stream) : mf_fast::ul_stage(a, c->mixed, c->stream);
+		timing_end(c, slot, c->n_total);
+		if (e != cudaSuccess) return cuda_fail(c, e, "ul_stage");
+		c->launches += (a.strict_grid || s == 0) ? 8 + 4 : 2;
+	}
+	return MF_OK;
+}
+
+TLArgs tl_args(mf_ctx* c) {
+	TLArgs a{};
+	a.n_total = c->n_total;
+	a.n_bodies = (uint32_t)c->bodies.size();
+	a.flags = c->flags;
+	a.params = c->params.p;
+	a.body_of = c->body_of.p;
+	a.X = c->X.p; a.Y = c->Y.p; a.m = c->m.p; a.h = c->h.p; a.qw0 = c->qw0.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	a.qw32 = c->qw32.p; a.m32 = c->m32.p; a.h32 = c->h32.p;
+	StateSoA* s[4] = {&a.base, &a.acc, &a.st, &a.nxt};
+	for (int k = 0; k < 4; k++) {
+		double** d[8] = {&s[k]->x, &s[k]->y, &s[k]->vx, &s[k]->vy, &s[k]->rho, &s[k]->Sxx, &s[k]->Sxy, &s[k]->Syy};
+		for (int q = 0; q < 8; q++) *d[q] = c->sd[k][q].p;
+		s[k]->rho_f = c->sf[k][0].p; s[k]->Sxx_f = c->sf[k][1].p; s[k]->Sxy_f = c->sf[k][2].p; s[k]->Syy_f = c->sf[k][3].p;
+	}
+	a.nbr_off = c->nbr_off.p;
+	a.nbr = c->nbr.p;
+	a.wx = c->mixed ? (const void*)c->wx32.p : (const void*)c->wx64.p;
+	a.wy = c->mixed ? (const void*)c->wy32.p : (const void*)c->wy64.p;
+	a.P = c->mixed ? (void*)c->P32.p : (void*)c->P64.p;
+	a.dA = c->mixed ? (void*)c->dA32.p : (void*)c->dA64.p;
+	a.c = c->mixed ? (void*)c->c32.p : (void*)c->c64.p;
+	a.pack = c->pack.p;
+	a.bc_rows = c->bc_rows.p;
+	a.bc_v = c->bc_v.p;
+	a.n_bc = c->n_bc;
+	a.status = c->d_status;
+	return a;
+}
+
+cudaError_t tl_launch(mf_ctx* c, const TLArgs& a, int part) {
+	return c->strict ? mf_strict::tl_stage(a, c->mixed, part, c->stream) : mf_fast::tl_stage(a, c->mixed, part, c->stream);
+}
+
+// One RK4 step of every TL body: per stage the BCs, (pack), pass A, pass B; the
+// stage state ping-pongs between sets 2 and 3 so that pass B never overwrites data
+// its neighbours still read.
+mf_status tl_step_all(mf_ctx* c) {
+	TLArgs a = tl_args(c);
+	StateSoA S0 = a.st, S1 = a.nxt;
+	for (uint32_t st = 0; st < 4; st++) {
+		a.stage = st;
+		a.st = (st % 2 == 0) ? S0 : S1;
+		a.nxt = (st % 2 == 0) ? S1 : S0;
+		cudaError_t e;
+		if ((e = tl_launch(c, a, 0)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
+		if ((e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
+		int slot;
+		timing_begin(c, 1, slot);
+		if ((e = tl_launch(c, a, 2)) != cudaSuccess) return cuda_fail(c, e, "tl pass A");
+		timing_end(c, slot, c->n_total);
+		timing_begin(c, 2, slot);
+		if ((e = tl_launch(c, a, 3)) != cudaSuccess) return cuda_fail(c, e, "tl pass B");
+		timing_end(c, slot, c->n_total);
+		c->launches += 2 + (c->n_bc ? 1 : 0) + (c->mixed ? 1 : 0);
+	}
+	cudaError_t e;
+	if ((e = tl_launch(c, a, 4)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
+	if ((e = tl_launch(c, a, 5)) != cudaSuccess) return cuda_fail(c, e, "tl clock");
+	c->launches += 1 + (c->n_bc ? 1 : 0);
+	return MF_OK;
+}
+
+// TL pipeline: a subsequence of the union of the reference's two TL lists
+// (rings.cpp:419-425 and tensile.cpp:276-286) in this order.
+mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_DERIVE_DISPLACEMENT, MF_DERIVE_VELOCITY_TL, MF_CONTMECH_VELOCITY_GRADIENT_TL,
+	                            MF_CONTMECH_CONTINUITY, MF_MATERIAL_EOS, MF_MATERIAL_STRESS_RATE_JAUMANN,
+	                            MF_MATERIAL_COMPUTE_STRESS_GREEN_STVENANT, MF_CONTMECH_CAUCHY_TO_NOMINAL,
+	                            MF_DERIVE_STRESS_TL, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY, MF_CONTMECH_MOMENTUM_TL,
+	                            MF_CONTMECH_ADVECTION};
+	if (c->cfg.method != MF_METHOD_TL) return fail(c, MF_ERR_PIPELINE, "method %d is not available", c->cfg.method);
+	flags = 0;
+	size_t pos = 0;
+	for (int32_t a : acts) {
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not part of the fused TL pipeline or out of its order", a);
+		flags |= abit(a);
+		pos++;
+	}
+	if ((flags & abit(MF_CONTMECH_MOMENTUM_TL)) && !(flags & abit(MF_DERIVE_STRESS_TL)))
+		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_tl needs derive_stress_tl before it");
+	if ((flags & abit(MF_CONTMECH_VELOCITY_GRADIENT_TL)) && !(flags & abit(MF_DERIVE_VELOCITY_TL)))
+		return fail(c, MF_ERR_PIPELINE, "contmech_velocity_gradient_tl needs derive_velocity_tl before it");
+	if ((flags & (abit(MF_CONTMECH_CONTINUITY) | abit(MF_MATERIAL_STRESS_RATE_JAUMANN))) &&
+	    !(flags & abit(MF_CONTMECH_VELOCITY_GRADIENT_TL)))
+		return fail(c, MF_ERR_PIPELINE, "continuity / Jaumann rate need contmech_velocity_gradient_tl before them");
+	return MF_OK;
+}
+
+// TL set-up: neighbour lists (find_neighbors), Randles-Libersky gradients, stage
+// buffers.  Runs once, before the first step.
+mf_status tl_setup(mf_ctx* c) {
+	uint32_t n = c->n_total;
+	uint32_t nb = (uint32_t)c->bodies.size();
+	double h = c->cfg.nbh_h, eps = c->cfg.nbh_eps;
+	if (!(h > 0.)) return fail(c, MF_ERR_ARG, "TL needs config.nbh_h > 0 (the h of the set-up neighbour search)");
+	double reach = sqrt(h * h * 2 * 2 + eps) * (1. + 1e-9);
+	std::vector<Geom> g(nb);
+	uint32_t cells = 0;
+	for (uint32_t b = 0; b < nb; b++) {
+		const HostBody& B = c->bodies[b];
+		double mnx = 1e300, mny = 1e300, mxx = -1e300, mxy = -1e300;
+		for (uint32_t i = 0; i < B.n; i++) {
+			mnx = std::min(mnx, B.in[0][i]); mxx = std::max(mxx, B.in[0][i]);
+			mny = std::min(mny, B.in[1][i]); mxy = std::max(mxy, B.in[1][i]);
+		}
+		double fnx = floor((mxx - mnx) / reach) + 1, fny = floor((mxy - mny) / reach) + 1;
+		if (fnx * fny > 1.5e9) return fail(c, MF_ERR_CAPACITY, "set-up grid too large");
+		g[b].bbmin_x = mnx; g[b].bbmin_y = mny; g[b].dx = reach;
+		g[b].nx = (uint32_t)fnx; g[b].ny = (uint32_t)fny;
+		g[b].num_cell = g[b].nx * g[b].ny;
+		g[b].cell_off = cells;
+		if ((uint64_t)cells + g[b].num_cell > 0xfffffff0ull) return fail(c, MF_ERR_CAPACITY, "set-up grid too large");
+		cells += g[b].num_cell;
+	}
+	DevBuf<Geom> dgeom;
+	DevBuf<uint32_t> keys, keys_sorted, vals, perm, cstart, count;
+	DevBuf<unsigned char> tmp;
+	CK(dgeom.alloc(nb));
+	CK(cudaMemcpy(dgeom.p, g.data(), nb * sizeof(Geom), cudaMemcpyHostToDevice));
+	CK(keys.alloc(n)); CK(keys_sorted.alloc(n)); CK(vals.alloc(n)); CK(perm.alloc(n));
+	CK(cstart.alloc((size_t)cells + 2)); CK(count.alloc(n));
+	int bits = 1;
+	while (bits < 32 && (1ull << bits) < (uint64_t)cells + 2) bits++;
+	size_t tb = c->strict ? mf_strict::tl_sort_tmp_bytes(n, bits) : mf_fast::tl_sort_tmp_bytes(n, bits);
+	CK(tmp.alloc(tb));
+	TLSearchArgs sa{};
+	sa.n_from = n; sa.n_to = n;
+	sa.fx = c->sd[0][0].p; sa.fy = c->sd[0][1].p; sa.tx = c->sd[0][0].p; sa.ty = c->sd[0][1].p;
+	sa.from_body = c->body_of.p; sa.to_body = c->body_of.p;
+	sa.geom = dgeom.p; sa.total_cells = cells;
+	sa.h = h; sa.eps = eps; sa.max_nbh = c->cfg.max_nbh;
+	sa.keys = keys.p; sa.keys_sorted = keys_sorted.p; sa.vals = vals.p; sa.perm = perm.p; sa.cell_start = cstart.p;
+	sa.sort_tmp = tmp.p; sa.sort_tmp_bytes = tb; sa.sort_bits = bits;
+	sa.count = count.p; sa.status = c->d_status;
+	auto search = [&](int pass) { return c->strict ? mf_strict::tl_search(sa, pass, c->stream) : mf_fast::tl_search(sa, pass, c->stream); };
+	CK(search(0));
+	mf_status st = check_status(c);
+	if (st != MF_OK) return st;
+	std::vector<uint32_t> hc(n), off(n + 1, 0);
+	CK(cudaMemcpy(hc.data(), count.p, n * 4, cudaMemcpyDeviceToHost));
+	uint64_t tot = 0;
+	for (uint32_t i = 0; i < n; i++) { off[i] = (uint32_t)tot; tot += hc[i]; }
+	if (tot > 0xffffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^32 neighbour pairs");
+	off[n] = (uint32_t)tot;
+	CK(c->nbr_off.alloc(n + 1));
+	CK(cudaMemcpy(c->nbr_off.p, off.data(), (n + 1) * 4, cudaMemcpyHostToDevice));
+	CK(c->nbr.alloc(tot));
+	sa.off = c->nbr_off.p;
+	sa.nbr = c->nbr.p;
+	CK(search(1));
+	dgeom.free(); keys.free(); keys_sorted.free(); vals.free(); perm.free(); cstart.free(); count.free(); tmp.free();
+	// Randles-Libersky corrected gradients, FP64
+	CK(c->wx64.alloc(tot)); CK(c->wy64.alloc(tot));
+	const double* rho64 = c->mixed ? nullptr : c->sd[0][4].p;
+	const float* rho32 = c->mixed ? c->sf[0][0].p : nullptr;
+	cudaError_t e = c->strict ? mf_strict::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
+	                                             rho32, c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream)
+	                          : mf_fast::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
+	                                           rho32, c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "tl_rl");
+	st = check_status(c);
+	if (st != MF_OK) return st;
+	if (c->mixed) {
+		CK(c->wx32.alloc(tot)); CK(c->wy32.alloc(tot));
+		CK(mf_fast::to_float(tot, c->wx64.p, c->wx32.p, c->stream));
+		CK(mf_fast::to_float(tot, c->wy64.p, c->wy32.p, c->stream));
+		CK(cudaStreamSynchronize(c->stream));
+		c->wx64.free(); c->wy64.free();
+		CK(c->P32.alloc(4 * (size_t)n)); CK(c->dA32.alloc(4 * (size_t)n)); CK(c->c32.alloc(n));
+		CK(c->pack.alloc(6 * (size_t)n * 8));
+		auto f32 = [&](DevBuf<float>& d, int field) -> mf_status {
+			CK(d.alloc(n));
+			std::vector<float> v(n);
+			for (auto& b : c->bodies)
+				for (uint32_t i = 0; i < b.n; i++) v[b.off + i] = (float)b.in[field][i];
+			CK(cudaMemcpy(d.p, v.data(), n * 4, cudaMemcpyHostToDevice));
+			return MF_OK;
+		};
+		if ((st = f32(c->qw32, 7)) || (st = f32(c->m32, 4)) || (st = f32(c->h32, 6))) return st;
+	} else {
+		CK(c->P64.alloc(4 * (size_t)n)); CK(c->dA64.alloc(4 * (size_t)n)); CK(c->c64.alloc(n));
+	}
+	// the second stage buffer set; stage 0 starts from a copy of the particles
+	for (int q = 0; q < 8; q++) {
+		if (c->mixed && q >= 4) continue;
+		CK(c->sd[3][q].alloc(n));
+		CK(cudaMemcpy(c->sd[2][q].p, c->sd[0][q].p, n * 8, cudaMemcpyDeviceToDevice));
+	}
+	if (c->mixed)
+		for (int q = 0; q < 4; q++) {
+			CK(c->sf[3][q].alloc(n));
+			CK(cudaMemcpy(c->sf[2][q].p, c->sf[0][q].p, n * 4, cudaMemcpyDeviceToDevice));
+		}
+	// boundary conditions
+	std::vector<uint32_t> rows;
+	std::vector<double> vs;
+	for (auto& b : c->bodies)
+		for (auto& bc : b.bcs)
+			for (uint32_t i : bc.idx) { rows.push_back(b.off + i); vs.push_back(bc.v); }
+	c->n_bc = (uint32_t)rows.size();
+	CK(c->bc_rows.alloc(rows.size())); CK(c->bc_v.alloc(vs.size()));
+	if (!rows.empty()) {
+		CK(cudaMemcpy(c->bc_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->bc_v.p, vs.data(), vs.size() * 8, cudaMemcpyHostToDevice));
+	}
+	return MF_OK;
+}
+
+// Contact set-up: boundary points, 32-point tiles, and for every body with a
+// boundary its master -- the last other body of its group with a boundary, since
+// main() loops over ordered pairs and each call first zeroes the slave's forces
+// (mfree_iwf.cpp:91-97, contact.h:50-53).
+mf_status contact_setup(mf_ctx* c) {
+	uint32_t nb = (uint32_t)c->bodies.size();
+	std::vector<uint32_t> rows, bstart, blen, tfirst, tend, srows, smaster, mtoff(nb, 0), mtn(nb, 0);
+	std::vector<double> sdt;
+	for (uint32_t b = 0; b < nb; b++) {
+		const HostBody& B = c->bodies[b];
+		uint32_t start = (uint32_t)rows.size();
+		mtoff[b] = (uint32_t)tfirst.size();
+		for (uint32_t i = 0; i < B.hull.size(); i++) {
+			rows.push_back(B.off + B.hull[i]);
+			bstart.push_back(start);
+			blen.push_back((uint32_t)B.hull.size());
+		}
+		for (uint32_t t = 0; t < B.hull.size(); t += 32) {
+			tfirst.push_back(start + t);
+			tend.push_back(start + std::min<uint32_t>(t + 32, (uint32_t)B.hull.size()));
+		}
+		mtn[b] = (uint32_t)tfirst.size() - mtoff[b];
+	}
+	if (c->cfg.contact) {
+		for (uint32_t j = 0; j < nb; j++) {
+			if (c->bodies[j].hull.empty()) continue;
+			int master = -1;
+			for (uint32_t i = 0; i < nb; i++)
+				if (i != j && !c->bodies[i].hull.empty() && c->bodies[i].group == c->bodies[j].group) master = (int)i;
+			if (master < 0) continue;
+			for (uint32_t r = 0; r < c->bodies[j].n; r++) {
+				srows.push_back(c->bodies[j].off + r);
+				smaster.push_back((uint32_t)master);
+				sdt.push_back(c->bodies[j].dt);
+			}
+		}
+	}
+	c->n_bnd = (uint32_t)rows.size();
+	c->n_tiles = (uint32_t)tfirst.size();
+	c->n_slave = (uint32_t)srows.size();
+	c->contact_on = c->cfg.contact && c->n_slave > 0;
+	if (!c->contact_on) return MF_OK;
+	auto up = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
+		CK(d.alloc(v.size()));
+		if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+		return MF_OK;
+	};
+	mf_status st;
+	if ((st = up(c->bnd_rows, rows)) || (st = up(c->bnd_start, bstart)) || (st = up(c->bnd_len, blen)) ||
+	    (st = up(c->tile_first, tfirst)) || (st = up(c->tile_end, tend)) || (st = up(c->slave_rows, srows)) ||
+	    (st = up(c->slave_master, smaster)) || (st = up(c->m_tile_off, mtoff)) || (st = up(c->m_tile_n, mtn)))
+		return st;
+	CK(c->slave_dt.alloc(sdt.size()));
+	CK(cudaMemcpy(c->slave_dt.p, sdt.data(), sdt.size() * 8, cudaMemcpyHostToDevice));
+	CK(c->bnd.alloc(c->n_bnd));
+	CK(c->tile_bb.alloc(c->n_tiles));
+	return MF_OK;
+}
+
+mf_status contact_run(mf_ctx* c) {
+	ContactArgs a{};
+	a.n_bnd = c->n_bnd; a.n_tiles = c->n_tiles; a.n_slave = c->n_slave;
+	a.bnd_rows = c->bnd_rows.p; a.bnd_start = c->bnd_start.p; a.bnd_len = c->bnd_len.p;
+	a.bnd = c->bnd.p; a.tile_first = c->tile_first.p; a.tile_end = c->tile_end.p; a.tile_bb = c->tile_bb.p;
+	a.slave_rows = c->slave_rows.p; a.slave_master = c->slave_master.p; a.dt = c->slave_dt.p;
+	a.m_tile_off = c->m_tile_off.p; a.m_tile_n = c->m_tile_n.p;
+	a.x = c->sd[0][0].p; a.y = c->sd[0][1].p; a.m = c->m.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	int slot;
+	timing_begin(c, 3, slot);
+	cudaError_t e = c->strict ? mf_strict::contact_step(a, c->stream) : mf_fast::contact_step(a, c->stream);
+	timing_end(c, slot, c->n_slave);
+	if (e != cudaSuccess) return cuda_fail(c, e, "contact");
+	c->launches += 3;
+	return MF_OK;
+}
+
+}  // namespace
+
+mf_ctx::~mf_ctx() {
+	if (stream) cudaStreamSynchronize(stream);
+	DevBuf<double>* d[] = {&m, &h, &qw0, &fcx, &fcy, &X, &Y};
+	for (auto* p : d) p->free();
+	for (int k = 0; k < 4; k++) {
+		for (int q = 0; q < 8; q++) sd[k][q].free();
+		for (int q = 0; q < 4; q++) sf[k][q].free();
+	}
+	body_of.free(); params.free(); geom.free(); bbox.free(); total_cells.free(); keys.free(); keys_sorted.free();
+	perm_in.free(); perm.free(); cell_start.free(); rec_body.free(); rec.free(); sort_tmp.free();
+	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
+	                            &slave_rows, &slave_master, &m_tile_off, &m_tile_n};
+	for (auto* p : u32s) p->free();
+	DevBuf<double>* f64s[] = {&wx64, &wy64, &P64, &dA64, &c64, &bc_v, &slave_dt};
+	for (auto* p : f64s) p->free();
+	DevBuf<float>* f32s[] = {&wx32, &wy32, &P32, &dA32, &c32, &qw32, &m32, &h32};
+	for (auto* p : f32s) p->free();
+	pack.free(); bnd.free(); tile_bb.free();
+	for (auto e : timing.pool) cudaEventDestroy(e);
+	if (d_status) cudaFree(d_status);
+	if (h_status) cudaFreeHost(h_status);
+	if (stream) cudaStreamDestroy(stream);
+}
+
+// ================================================================== C ABI
+extern "C" {
+
+MF_API const char* mf_status_string(mf_status s) {
+	switch (s) {
+	case MF_OK: return "ok";
+	case MF_ERR_ARG: return "invalid argument";
+	case MF_ERR_CUDA: return "CUDA error";
+	case MF_ERR_NBH_OVERFLOW: return "neighbour capacity reached";
+	case MF_ERR_NONFINITE: return "non-finite state";
+	case MF_ERR_TIMEOUT: return "device wait timed out";
+	case MF_ERR_PIPELINE: return "unsupported action list";
+	case MF_ERR_GRID: return "invalid cell grid";
+	case MF_ERR_STATE: return "invalid call for the context state";
+	case MF_ERR_NO_DEVICE: return "no CUDA device";
+	case MF_ERR_SINGULAR: return "singular corrector matrix";
+	case MF_ERR_NO_NEIGHBOR: return "particle without neighbours";
+	case MF_ERR_CAPACITY: return "size beyond the documented maximum";
+	}
+	return "unknown status";
+}
+
+MF_API const char* mf_last_error(const mf_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out) {
+	if (!cfg || !out) return MF_ERR_ARG;
+	*out = nullptr;
+	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_TL_WEAK) return MF_ERR_ARG;
+	if (cfg->precision < MF_PREC_FP64_STRICT || cfg->precision > MF_PREC_MIXED) return MF_ERR_ARG;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MF_ERR_NO_DEVICE;
+	if (cfg->device < 0 || cfg->device >= ndev) return MF_ERR_ARG;
+	if (cudaSetDevice(cfg->device) != cudaSuccess) return MF_ERR_CUDA;
+	mf_ctx* c = new mf_ctx();
+	c->cfg = *cfg;
+	if (c->cfg.max_nbh == 0) c->cfg.max_nbh = REF_MAX_NBH;
+	if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaMalloc(&c->d_status, sizeof(DevStatusH)) != cudaSuccess ||
+	    cudaMallocHost(&c->h_status, sizeof(DevStatusH)) != cudaSuccess) {
+		delete c;
+		return MF_ERR_CUDA;
+	}
+	c->h_status->flags = 0;
+	c->h_status->first_index = 0xffffffffu;
+	cudaMemcpy(c->d_status, c->h_status, sizeof(DevStatusH), cudaMemcpyHostToDevice);
+	*out = c;
+	return MF_OK;
+}
+
+MF_API void mf_destroy(mf_ctx* c) { delete c; }
+
+MF_API mf_status mf_add_body(mf_ctx* c, const mf_particles* p, uint32_t n, const mf_sim_data* sd, double dt,
+                             int32_t group, int32_t* body_id) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "bodies must be added before the first step");
+	if (!p || !sd || n == 0) return fail(c, MF_ERR_ARG, "null particles/sim_data or n == 0");
+	if (!(dt > 0.)) return fail(c, MF_ERR_ARG, "dt must be positive");
+	if ((uint64_t)c->n_total + n >= 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 particles");
+	const double* src[13] = {p->x, p->y, p->X, p->Y, p->m, p->rho, p->h, p->quad_weight, p->vx, p->vy, p->Sxx, p->Sxy, p->Syy};
+	for (int k = 0; k < 13; k++)
+		if (!src[k] && k != 2 && k != 3) return fail(c, MF_ERR_ARG, "particle field %d is null", k);
+	HostBody b;
+	b.off = c->n_total;
+	b.n = n;
+	b.sd = *sd;
+	b.dt = dt;
+	b.group = group;
+	for (int k = 0; k < 13; k++) {
+		const double* s = src[k] ? src[k] : (k == 2 ? p->x : p->y);
+		b.in[k].assign(s, s + n);
+	}
+	c->n_total += n;
+	c->bodies.push_back(std::move(b));
+	if (body_id) *body_id = (int32_t)c->bodies.size() - 1;
+	return MF_OK;
+}
+
+MF_API mf_status mf_add_action(mf_ctx* c, int32_t body, int32_t action) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "actions must be added before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	if (action < 1 || action > MF_CONTMECH_MOMENTUM_TL_WEAK) return fail(c, MF_ERR_ARG, "bad action id %d", action);
+	c->bodies[body].actions.push_back(action);
+	return MF_OK;
+}
+
+MF_API mf_status mf_add_boundary_condition(mf_ctx* c, int32_t body, const uint32_t* idx, uint32_t k, int32_t kind,
+                                           double value) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "boundary conditions must be added before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	if (kind != MF_BC_PULL) return fail(c, MF_ERR_ARG, "unknown boundary-condition kind %d", kind);
+	if (k && !idx) return fail(c, MF_ERR_ARG, "null index list");
+	for (uint32_t i = 0; i < k; i++)
+		if (idx[i] >= c->bodies[body].n) return fail(c, MF_ERR_ARG, "boundary index %u out of range", idx[i]);
+	c->bodies[body].bcs.push_back(HostBC{kind, value, std::vector<uint32_t>(idx, idx + k)});
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_boundary(mf_ctx* c, int32_t body, const uint32_t* idx, uint32_t nb) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "boundaries must be set before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	if (nb && !idx) return fail(c, MF_ERR_ARG, "null index list");
+	for (uint32_t i = 0; i < nb; i++)
+		if (idx[i] >= c->bodies[body].n) return fail(c, MF_ERR_ARG, "boundary index %u out of range", idx[i]);
+	c->bodies[body].hull.assign(idx, idx + nb);
+	return MF_OK;
+}
+
+MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, uint32_t* out_idx, uint32_t* out_n) {
+	if ((!x || !y || !out_idx || !out_n) && n) return MF_ERR_ARG;
+	if (out_n) *out_n = 0;
+	if (n < 3) return MF_ERR_ARG;
+	struct P {
+		double x, y;
+		uint32_t i;
+	};
+	std::vector<P> pts(n);
+	for (uint32_t i = 0; i < n; i++) pts[i] = P{x[i], y[i], i};
+	// lexicographic (x, y) order, as leftlower (convex_hull.h:44-58)
+	std::sort(pts.begin(), pts.end(), [](const P a, const P b) {
+		if (a.x < b.x) return true;
+		if (a.x > b.x) return false;
+		return a.y < b.y;
+	});
+	auto ccw = [](const P& a, const P& b, const P& q) { return (b.x - a.x) * (q.y - a.y) - (b.y - a.y) * (q.x - a.x); };
+	std::vector<P> hull(n);
+	int k = 0;
+	for (int i = 0; i < (int)n; ++i) {
+		while (k >= 2 && ccw(hull[k - 2], hull[k - 1], pts[i]) < 0) --k;
+		hull[k++] = pts[i];
+	}
+	for (int i = (int)n - 2, t = k + 1; i >= 0; --i) {
+		while (k >= t && ccw(hull[k - 2], hull[k - 1], pts[i]) < 0) --k;
+		hull[k++] = pts[i];
+	}
+	for (int i = 0; i < k - 1; i++) out_idx[i] = hull[i].i;
+	*out_n = (uint32_t)(k - 1);
+	return MF_OK;
+}
+
+MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
+	if (!c) return MF_ERR_ARG;
+	if (nsteps < 0) return fail(c, MF_ERR_ARG, "nsteps < 0");
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	CK(cudaSetDevice(c->cfg.device));
+	for (int32_t k = 0; k < nsteps; k++) {
+		if (c->cfg.method == MF_METHOD_UL) st = ul_step(c);
+		else st = tl_step_all(c);
+		if (st != MF_OK) return st;
+		for (auto& b : c->bodies) b.time += b.dt;  // rk4.h:107 (each body's own clock)
+		if (c->contact_on) {
+			st = contact_run(c);
+			if (st != MF_OK) return st;
+		}
+	}
+	return check_status(c);
+}
+
+MF_API mf_status mf_synchronize(mf_ctx* c) {
+	if (!c) return MF_ERR_ARG;
+	if (!c->ready) return MF_OK;
+	return check_status(c);
+}
+
+MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
+	if (!c || !out) return MF_ERR_ARG;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	const HostBody& b = c->bodies[body];
+	if (!c->ready) {
+		double* o[10] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy, out->fcx, out->fcy};
+		const int fld[8] = {0, 1, 8, 9, 5, 10, 11, 12};
+		for (int q = 0; q < 8; q++)
+			if (o[q]) std::copy(b.in[fld[q]].begin(), b.in[fld[q]].end(), o[q]);
+		for (int q = 8; q < 10; q++)
+			if (o[q]) std::fill(o[q], o[q] + b.n, 0.);
+		return MF_OK;
+	}
+	CK(cudaStreamSynchronize(c->stream));
+	double* o[8] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy};
+	for (int q = 0; q < 8; q++) {
+		if (!o[q]) continue;
+		if (c->mixed && q >= 4) {
+			std::vector<float> tmp(b.n);
+			CK(cudaMemcpy(tmp.data(), c->sf[0][q - 4].p + b.off, b.n * 4, cudaMemcpyDeviceToHost));
+			for (uint32_t i = 0; i < b.n; i++) o[q][i] = tmp[i];
+		} else {
+			CK(cudaMemcpy(o[q], c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
+		}
+	}
+	if (out->fcx) CK(cudaMemcpy(out->fcx, c->fcx.p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
+	if (out->fcy) CK(cudaMemcpy(out->fcy, c->fcy.p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
+	if (!c || !p) return MF_ERR_ARG;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	HostBody& b = c->bodies[body];
+	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
+	const int fld[8] = {0, 1, 8, 9, 5, 10, 11, 12};
+	if (!c->ready) {
+		for (int q = 0; q < 8; q++)
+			if (src[q]) b.in[fld[q]].assign(src[q], src[q] + b.n);
+		return MF_OK;
+	}
+	CK(cudaStreamSynchronize(c->stream));
+	for (int q = 0; q < 8; q++) {
+		if (!src[q]) continue;
+		if (c->mixed && q >= 4) {
+			std::vector<float> tmp(src[q], src[q] + b.n);
+			CK(cudaMemcpy(c->sf[0][q - 4].p + b.off, tmp.data(), b.n * 4, cudaMemcpyHostToDevice));
+		} else {
+			CK(cudaMemcpy(c->sd[0][q].p + b.off, src[q], b.n * 8, cudaMemcpyHostToDevice));
+		}
+	}
+	return MF_OK;
+}
+
+MF_API mf_status mf_get_time(mf_ctx* c, int32_t body, double* t) {
+	if (!c || !t) return MF_ERR_ARG;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	*t = c->bodies[body].time;
+	return MF_OK;
+}
+
+MF_API mf_status mf_num_particles(mf_ctx* c, int32_t body, uint32_t* n) {
+	if (!c || !n) return MF_ERR_ARG;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	*n = c->bodies[body].n;
+	return MF_OK;
+}
+
+MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uint32_t* idx, uint64_t cap,
+                                  uint64_t* total) {
+	if (!c || !counts || !total) return MF_ERR_ARG;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	const HostBody& b = c->bodies[body];
+	uint32_t n = c->n_total;
+	std::vector<uint32_t> all_counts(n);
+	std::vector<uint64_t> offs(n + 1, 0);
+	DevBuf<uint32_t> d_counts, d_idx;
+	DevBuf<uint64_t> d_offs;
+	CK(d_counts.alloc(n));
+	CK(d_offs.alloc(n + 1));
+	std::vector<uint32_t> all_idx;
+	if (c->cfg.method == MF_METHOD_UL) {
+		ULArgs a = ul_args(c, 0);
+		cudaError_t e = mf_strict::ul_neighbors(a, d_counts.p, nullptr, nullptr, 0, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "ul_neighbors");
+		CK(cudaMemcpyAsync(all_counts.data(), d_counts.p, n * 4, cudaMemcpyDeviceToHost, c->stream));
+		CK(cudaStreamSynchronize(c->stream));
+		for (uint32_t i = 0; i < n; i++) offs[i + 1] = offs[i] + all_counts[i];
+		CK(d_idx.alloc(offs[n]));
+		CK(cudaMemcpy(d_offs.p, offs.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+		e = mf_strict::ul_neighbors(a, d_counts.p, d_idx.p, d_offs.p, 1, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "ul_neighbors");
+		all_idx.resize(offs[n]);
+		CK(cudaMemcpyAsync(all_idx.data(), d_idx.p, offs[n] * 4, cudaMemcpyDeviceToHost, c->stream));
+		st = check_status(c);
+		if (st != MF_OK && st != MF_ERR_NBH_OVERFLOW) return st;
+	} else {
+		std::vector<uint32_t> off(n + 1);
+		CK(cudaMemcpy(off.data(), c->nbr_off.p, (n + 1) * 4, cudaMemcpyDeviceToHost));
+		all_idx.resize(off[n]);
+		if (off[n]) CK(cudaMemcpy(all_idx.data(), c->nbr.p, (size_t)off[n] * 4, cudaMemcpyDeviceToHost));
+		for (uint32_t i = 0; i < n; i++) { all_counts[i] = off[i + 1] - off[i]; offs[i + 1] = off[i + 1]; }
+	}
+	d_counts.free(); d_idx.free(); d_offs.free();
+	uint64_t tot = 0;
+	for (uint32_t i = 0; i < b.n; i++) {
+		uint32_t r = b.off + i;
+		counts[i] = all_counts[r];
+		for (uint64_t q = offs[r]; q < offs[r + 1]; q++) {
+			if (idx && tot < cap) idx[tot] = all_idx[q] - b.off;
+			tot++;
+		}
+	}
+	*total = tot;
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_timing(mf_ctx* c, int32_t enable) {
+	if (!c) return MF_ERR_ARG;
+	c->timing.on = enable != 0;
+	for (int k = 0; k < 8; k++) { c->timing.ms[k] = 0.; c->timing.launches[k] = 0; c->timing.rows[k] = 0; }
+	return MF_OK;
+}
+
+MF_API mf_status mf_kernel_stats(mf_ctx* c, int32_t kind, double* total_ms, uint64_t* launches, uint64_t* rows) {
+	if (!c || kind < 0 || kind >= 8) return MF_ERR_ARG;
+	if (total_ms) *total_ms = c->timing.ms[kind];
+	if (launches) *launches = c->timing.launches[kind];
+	if (rows) *rows = c->timing.rows[kind];
+	return MF_OK;
+}
+
+MF_API mf_status mf_launch_count(mf_ctx* c, uint64_t* launches) {
+	if (!c || !launches) return MF_ERR_ARG;
+	*launches = c->launches;
+	return MF_OK;
+}
+
+MF_API mf_status mf_get_stream(mf_ctx* c, void** stream) {
+	if (!c || !stream) return MF_ERR_ARG;
+	*stream = (void*)c->stream;
+	return MF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,142 @@
+// Host-visible declarations of the kernel launchers.  Each launcher exists in
+// two namespaces compiled from the same sources: mf_strict (FP64 without FMA
+// contraction, the parity form) and mf_fast (FP64 and mixed precision with
+// contraction).  All launchers enqueue on the given stream and never synchronise.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mfk_host {
+
+// Action flags of a fused pipeline (bit i = action id i of mf_action).
+inline uint32_t bit(int a) { return 1u << a; }
+
+// Per-body constants (simulation_data.h:25-99 plus the body's dt), device copy.
+struct BodyParams {
+	double K, G, rho0, c0sq;        // c0sq = c0*c0 with c0 = sqrt(K/rho0) (material.h:37-44)
+	double E, nu, D;                // D = E/(1-nu^2) (material.h:136)
+	double wdeltap, corr_exp, mghn_eps;
+	double alpha, beta, eta, xsph_eps;
+	double dt, time;
+	uint32_t off, n;                // particle rows [off, off+n)
+	uint32_t pad0, pad1;
+};
+
+// Per-body cell geometry of one derivative evaluation (grid.h:83-115).
+struct Geom {
+	double bbmin_x, bbmin_y, dx;
+	uint32_t nx, ny, num_cell, cell_off;
+};
+
+struct DevStatusH {
+	uint32_t flags;
+	uint32_t first_index;
+};
+
+// State arrays of a body set (rows of all bodies concatenated).
+// FP64 forms: every pointer is double.  Mixed form: x, y, vx, vy are double,
+// rho and the stresses are float (the *_f pointers).
+struct StateSoA {
+	double *x, *y, *vx, *vy, *rho, *Sxx, *Sxy, *Syy;
+	float *rho_f, *Sxx_f, *Sxy_f, *Syy_f;
+};
+
+struct ULArgs {
+	uint32_t n_total, n_bodies, stage;    // stage 0..3
+	uint32_t flags;                       // action bits
+	uint32_t max_nbh;                     // neighbour capacity (0 = unchecked)
+	uint32_t strict_grid;                 // 1: rebuild the reference grid at this stage
+	double nbh_eps;
+	const BodyParams* params;             // device
+	Geom* geom;                           // device, per body
+	unsigned long long* bbox;             // device, 5 per body
+	uint32_t* total_cells;                // device scalar
+	const uint32_t* body_of;              // device, per row
+	const double *m, *h, *qw0, *fcx, *fcy;  // constants (home order)
+	StateSoA base, acc, st;               // RK4 arrays (home order)
+	uint32_t *keys, *keys_sorted, *perm_in, *perm;  // sort buffers
+	uint32_t* cell_start;                 // capacity n_total + 2
+	void* rec;                            // cell-ordered gathered records
+	uint32_t* rec_body;                   // body of each cell-ordered row
+	void* sort_tmp;
+	size_t sort_tmp_bytes;
+	int sort_bits;
+	mfk_host::DevStatusH* status;
+	cudaEvent_t ev_pair0, ev_pair1;       // optional timing of the pair kernel
+};
+
+// Neighbour search of the total-Lagrangian set-up (find_neighbors,
+// neighbor_search.h:50-147): query points "to" against particles "from".
+struct TLSearchArgs {
+	uint32_t n_from, n_to;
+	const double *fx, *fy, *tx, *ty;
+	const uint32_t *from_body, *to_body;
+	const Geom* geom;          // per body, cell >= search radius
+	uint32_t total_cells;
+	double h, eps;
+	uint32_t max_nbh;
+	uint32_t *keys, *keys_sorted, *vals, *perm, *cell_start;
+	void* sort_tmp;
+	size_t sort_tmp_bytes;
+	int sort_bits;
+	uint32_t* count;           // pass 0 output
+	const uint32_t* off;       // pass 1 input (exclusive scan of count)
+	uint32_t* nbr;             // pass 1 output
+	void* status;
+};
+
+// One total-Lagrangian stage over all bodies.
+struct TLArgs {
+	uint32_t n_total, n_bodies, stage, flags;
+	const BodyParams* params;
+	const uint32_t* body_of;
+	const double *X, *Y, *m, *h, *qw0, *fcx, *fcy;
+	const void *qw32, *m32, *h32;       // mixed form: float copies of the constants
+	StateSoA base, acc, st, nxt;         // st: this stage's state, nxt: the next stage's
+	const uint32_t *nbr_off, *nbr;
+	const void *wx, *wy;                 // corrected kernel gradient per pair
+	void *P, *dA, *c, *pack;             // per-stage scratch
+	const uint32_t* bc_rows;
+	const double* bc_v;
+	uint32_t n_bc;
+	void* status;
+};
+
+// Contact: boundary points of all bodies, their 32-point tiles, and the slave rows
+// with the master body each one is tested against.
+struct ContactArgs {
+	uint32_t n_bnd, n_tiles, n_slave;
+	const uint32_t *bnd_rows, *bnd_start, *bnd_len;   // per boundary point
+	double4* bnd;                                       // x, y, nx, ny
+	const uint32_t *tile_first, *tile_end;
+	float4* tile_bb;
+	const uint32_t *slave_rows, *slave_master;
+	const double* dt;                                   // per slave row
+	const uint32_t *m_tile_off, *m_tile_n;              // per body
+	const double *x, *y, *m;
+	double *fcx, *fcy;
+};
+
+}  // namespace mfk_host
+
+#define MF_DECLARE_LAUNCHERS(NS)                                                                              \
+	namespace NS {                                                                                           \
+	size_t ul_sort_tmp_bytes(uint32_t n, int bits);                                                          \
+	size_t ul_rec_bytes(bool mixed);                                                                         \
+	cudaError_t ul_stage(const mfk_host::ULArgs& a, bool mixed, cudaStream_t s);                             \
+	cudaError_t ul_neighbors(const mfk_host::ULArgs& a, uint32_t* counts, uint32_t* idx, const uint64_t* offs, \
+	                         int pass, cudaStream_t s);                                                      \
+	size_t tl_sort_tmp_bytes(uint32_t n, int bits);                                                          \
+	cudaError_t tl_search(const mfk_host::TLSearchArgs& a, int pass, cudaStream_t s);                        \
+	cudaError_t tl_rl(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y, \
+	                  const double* m, const double* rho, const float* rho_f, const double* h, double* wx,   \
+	                  double* wy, void* status, cudaStream_t s);                                             \
+	cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s);                             \
+	cudaError_t tl_stage(const mfk_host::TLArgs& a, bool mixed, int part, cudaStream_t s);                   \
+	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
+	}
+
+MF_DECLARE_LAUNCHERS(mf_strict)
+MF_DECLARE_LAUNCHERS(mf_fast)

@@ -1,0 +1,552 @@
+// Total-Lagrangian SPH kernels (particle_tl; rings_tl_contact rings.cpp:338-429,
+// tensile_tl tensile.cpp:213-289).
+//
+// Set-up (once): the neighbour lists of find_neighbors (neighbor_search.h:116-147:
+// every j with r^2 <= 4h^2 + eps, ascending j) are built from a cell grid whose cell
+// is at least the search radius, so a 3x3 stencil is complete; each list is sorted
+// ascending so the per-particle summation order is the reference's.  Then the
+// Randles-Libersky correction (precomp_shape_functions.h:231-290) stores the
+// corrected kernel gradient per pair.
+//
+// Per RK4 stage (body.h:110-123 with the action list fused):
+//   k_tl_bc      Dirichlet pull on the stage state (boundary_conditions.h:36-46)
+//   k_tlA        displacement gradient H (derivatives.h:101-149) and, for the rate
+//                form, Fdot (derivatives.h:483-519); then per particle the velocity
+//                gradient L = Fdot F^-1, continuity, EOS, Jaumann rate, Green-St
+//                Venant stress and P = J F^-1 sigma (cont_mech.h, material.h)
+//   k_tlB        divergence of P (derivatives.h:331-376), artificial viscosity
+//                (correctors.h:83-137), momentum (cont_mech.h:70-87), advection and
+//                the RK4 update (rk4.h:52-108)
+#include <cub/device/device_radix_sort.cuh>
+
+#include "mf_common.cuh"
+#include "mf_kernels.h"
+
+using namespace mfk;
+using mfk_host::BodyParams;
+using mfk_host::TLArgs;
+using mfk_host::TLSearchArgs;
+
+namespace MF_NS {
+namespace {
+
+enum : uint32_t {
+	A_EOS = 1u << 2,
+	A_ART_VISC = 1u << 6,
+	A_JAUMANN = 1u << 8,
+	A_CONTINUITY = 1u << 9,
+	A_ADVECTION = 1u << 11,
+	A_DISP = 1u << 12,
+	A_GREEN = 1u << 13,
+	A_C2N = 1u << 14,
+	A_STRESS_TL = 1u << 15,
+	A_MOMENTUM_TL = 1u << 16,
+	A_VEL_TL = 1u << 17,
+	A_VGRAD_TL = 1u << 18,
+};
+
+inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// ---------------------------------------------------------- neighbour search
+__global__ void k_search_hash(TLSearchArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_from) return;
+	const mfk_host::Geom g = a.geom[a.from_body[i]];
+	uint32_t ix = (uint32_t)((a.fx[i] - g.bbmin_x) / g.dx);
+	uint32_t iy = (uint32_t)((a.fy[i] - g.bbmin_y) / g.dx);
+	ix = min(ix, g.nx - 1);
+	iy = min(iy, g.ny - 1);
+	a.keys[i] = g.cell_off + ix * g.ny + iy;
+	a.vals[i] = i;
+}
+
+__global__ void k_search_cells(uint32_t n, const uint32_t* keys, uint32_t tot, uint32_t* cell_start) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k > n) return;
+	if (k == n) {
+		uint32_t last = (n == 0) ? 0u : keys[n - 1] + 1;
+		for (uint32_t c = last; c <= tot; c++) cell_start[c] = n;
+		return;
+	}
+	uint32_t prev = (k == 0) ? 0u : keys[k - 1] + 1;
+	if (k == 0 || keys[k] != keys[k - 1])
+		for (uint32_t c = prev; c <= keys[k]; c++) cell_start[c] = k;
+}
+
+// pass 0: count; pass 1: write the rows (sorted ascending) at off[i].
+__global__ void k_search(TLSearchArgs a, int pass, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_to) return;
+	double xi = a.tx[i], yi = a.ty[i];
+	uint32_t b = a.to_body[i];
+	const mfk_host::Geom g = a.geom[b];
+	double h = a.h;
+	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(h, h), 2.), 2.);
+	double lim = __dadd_rn(radius2, a.eps);
+	long cx = (long)floor((xi - g.bbmin_x) / g.dx), cy = (long)floor((yi - g.bbmin_y) / g.dx);
+	uint32_t cnt = 0;
+	uint32_t base = pass ? a.off[i] : 0u;
+	for (long u = cx - 1; u <= cx + 1; u++) {
+		if (u < 0 || u >= (long)g.nx) continue;
+		long lo = max(cy - 1, 0l), hi = min(cy + 1, (long)g.ny - 1);
+		if (lo > hi) continue;
+		uint32_t c0 = g.cell_off + (uint32_t)u * g.ny + (uint32_t)lo;
+		uint32_t c1 = g.cell_off + (uint32_t)u * g.ny + (uint32_t)hi + 1;
+		for (uint32_t k = a.cell_start[c0]; k < a.cell_start[c1]; k++) {
+			uint32_t j = a.perm[k];
+			double xij = __dsub_rn(xi, a.fx[j]);
+			double yij = __dsub_rn(yi, a.fy[j]);
+			double r2 = __dadd_rn(__dmul_rn(xij, xij), __dmul_rn(yij, yij));
+			if (r2 <= lim) {
+				if (pass && cnt < a.max_nbh) {
+					// insertion into the ascending list
+					uint32_t pos = base + cnt;
+					while (pos > base && a.nbr[pos - 1] > j) {
+						a.nbr[pos] = a.nbr[pos - 1];
+						pos--;
+					}
+					a.nbr[pos] = j;
+				}
+				cnt++;
+			}
+		}
+	}
+	if (pass == 0) {
+		a.count[i] = cnt;
+		if (cnt >= a.max_nbh) raise(st, ERR_NBH_OVERFLOW, i);
+		if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
+	}
+}
+
+// ------------------------------------------------------ Randles-Libersky
+// precomp_randles_libersky, precomp_shape_functions.h:231-290, FP64 always.
+__global__ void k_rl(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                     const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ m,
+                     const double* __restrict__ rho, const float* __restrict__ rho_f, const double* __restrict__ h,
+                     double* wx, double* wy, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	double xi = x[i], yi = y[i], hi = h[i];
+	uint32_t q0 = off[i], q1 = off[i + 1];
+	double C = 0.;
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double rj = rho ? rho[j] : (double)rho_f[j];
+		double volj = m[j] / rj;
+		KR64 w = cubic_spline(xi - x[j], yi - y[j], hi);
+		C += w.w * volj;
+	}
+	M2<double> B = M2<double>::make(0., 0., 0., 0.);
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double xj = x[j], yj = y[j];
+		double rj = rho ? rho[j] : (double)rho_f[j];
+		double volj = m[j] / rj;
+		KR64 w = cubic_spline(xi - xj, yi - yj, hi);
+		B.c[0][0] += (xj - xi) * w.w_x * volj * 1. / C;
+		B.c[1][0] += (xj - xi) * w.w_y * volj * 1. / C;
+		B.c[0][1] += (yj - yi) * w.w_x * volj * 1. / C;
+		B.c[1][1] += (yj - yi) * w.w_y * volj * 1. / C;
+	}
+	if (!(mdet(B) != 0.) || !(C != 0.)) raise(st, ERR_SINGULAR, i);
+	M2<double> invB = minverse(B);
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		KR64 w = cubic_spline(xi - x[j], yi - y[j], hi);
+		wx[q] = (w.w_x * invB.c[0][0] + w.w_y * invB.c[1][0]) * 1. / C;
+		wy[q] = (w.w_x * invB.c[0][1] + w.w_y * invB.c[1][1]) * 1. / C;
+	}
+}
+
+__global__ void k_to_float(uint64_t n, const double* a, float* b) {
+	uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (float)a[i];
+}
+
+// ------------------------------------------------------------ per stage
+__global__ void k_tl_bc(TLArgs a, int on_base) {
+	uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= a.n_bc) return;
+	uint32_t i = a.bc_rows[r];
+	double v = a.bc_v[r];
+	double t = a.params[a.body_of[i]].time;
+	const mfk_host::StateSoA& s = on_base ? a.base : a.st;
+	s.x[i] = a.X[i] + v * t;
+	s.y[i] = a.Y[i];
+	s.vx[i] = v;
+	s.vy[i] = 0.;
+}
+
+// The per-particle part of pass A, shared by both forms (T = double).
+__device__ __forceinline__ void tl_particle(uint32_t flags, const BodyParams& pr, double Hxx, double Hxy, double Hyx,
+                                            double Hyy, double Fxx, double Fxy, double Fyx, double Fyy, double rho,
+                                            double Sxx, double Sxy, double Syy, double& Pxx, double& Pxy, double& Pyx,
+                                            double& Pyy, double& rho_t, double& Sxx_t, double& Sxy_t, double& Syy_t) {
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+	if (flags & A_VGRAD_TL) velocity_gradient_tl<double>(Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, vx_x, vx_y, vy_x, vy_y);
+	rho_t = 0.;
+	if (flags & A_CONTINUITY) rho_t = -(rho * (vx_x + vy_y));
+	double p = 0.;
+	if (flags & A_EOS) p = pr.c0sq * (rho - pr.rho0);
+	Sxx_t = Sxy_t = Syy_t = 0.;
+	if (flags & A_JAUMANN) jaumann<double>(vx_x, vx_y, vy_x, vy_y, Sxx, Sxy, Syy, pr.G, Sxx_t, Sxy_t, Syy_t);
+	if (flags & A_GREEN) green_stvenant<double>(Hxx, Hxy, Hyx, Hyy, pr.D, pr.nu, Sxx, Sxy, Syy);
+	Pxx = Pxy = Pyx = Pyy = 0.;
+	if (flags & A_C2N) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
+}
+
+// ---- FP64 pass A
+__global__ void __launch_bounds__(128) k_tlA64(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double* wx = (const double*)a.wx;
+	const double* wy = (const double*)a.wy;
+	uint32_t flags = a.flags;
+	double uxi = s.x[i] - a.X[i], uyi = s.y[i] - a.Y[i];
+	double vxi = s.vx[i], vyi = s.vy[i];
+	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
+	double Fxx = 0., Fxy = 0., Fyx = 0., Fyy = 0.;
+	uint32_t q1 = a.nbr_off[i + 1];
+	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
+		uint32_t j = a.nbr[q];
+		double wxq = wx[q], wyq = wy[q];
+		double qwj = a.qw0[j];
+		if (flags & A_DISP) {
+			double uxj = s.x[j] - a.X[j], uyj = s.y[j] - a.Y[j];
+			Hxx += (uxj - uxi) * wxq * qwj;
+			Hxy += (uxj - uxi) * wyq * qwj;
+			Hyx += (uyj - uyi) * wxq * qwj;
+			Hyy += (uyj - uyi) * wyq * qwj;
+		}
+		if (flags & A_VEL_TL) {
+			double vxj = s.vx[j], vyj = s.vy[j];
+			Fxx += (vxj - vxi) * wxq * qwj;
+			Fxy += (vxj - vxi) * wyq * qwj;
+			Fyx += (vyj - vyi) * wxq * qwj;
+			Fyy += (vyj - vyi) * wyq * qwj;
+		}
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
+	double rho = s.rho[i];
+	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx[i], s.Sxy[i], s.Syy[i], Pxx, Pxy, Pyx,
+	            Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
+	double* P = (double*)a.P;
+	double* dA = (double*)a.dA;
+	uint32_t n = a.n_total;
+	P[i] = Pxx; P[n + i] = Pxy; P[2 * n + i] = Pyx; P[3 * n + i] = Pyy;
+	dA[i] = rho_t; dA[n + i] = Sxx_t; dA[2 * n + i] = Sxy_t; dA[3 * n + i] = Syy_t;
+	((double*)a.c)[i] = sqrt(pr.K / rho);
+}
+
+// ---- FP64 pass B + RK update
+__global__ void __launch_bounds__(128) k_tlB64(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double* wx = (const double*)a.wx;
+	const double* wy = (const double*)a.wy;
+	const double* P = (const double*)a.P;
+	const double* cc = (const double*)a.c;
+	uint32_t n = a.n_total;
+	uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double rho0 = pr.rho0;
+	double Pxxi = P[i], Pxyi = P[n + i], Pyxi = P[2 * n + i], Pyyi = P[3 * n + i];
+	double r21 = 1. / (rho0 * rho0);
+	double xi = s.x[i], yi = s.y[i], vxi = s.vx[i], vyi = s.vy[i], hi = a.h[i], rhoi = s.rho[i], ci = cc[i];
+	double alpha = pr.alpha, beta = pr.beta, eta = pr.eta;
+	double Pxx_x = 0., Pyx_y = 0., Pxy_x = 0., Pyy_y = 0., av_x = 0., av_y = 0.;
+	uint32_t q1 = a.nbr_off[i + 1];
+	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
+		uint32_t j = a.nbr[q];
+		double wxq = wx[q], wyq = wy[q];
+		double mj = a.m[j];
+		if (flags & A_STRESS_TL) {
+			Pxx_x += mj * (Pxxi * r21 + P[j] * r21) * wxq * rho0;
+			Pyx_y += mj * (Pyxi * r21 + P[2 * n + j] * r21) * wyq * rho0;
+			Pxy_x += mj * (Pxyi * r21 + P[n + j] * r21) * wxq * rho0;
+			Pyy_y += mj * (Pyyi * r21 + P[3 * n + j] * r21) * wyq * rho0;
+		}
+		if (flags & A_ART_VISC) {
+			double vijx = vxi - s.vx[j], vijy = vyi - s.vy[j];
+			double xij = xi - s.x[j], yij = yi - s.y[j];
+			double vijposij = vijx * xij + vijy * yij;
+			if (vijposij < 0.) {
+				double cij = 0.5 * (ci + cc[j]);
+				double hij = 0.5 * (hi + a.h[j]);
+				double rhoij = 0.5 * (rhoi + s.rho[j]);
+				double r2ij = xij * xij + yij * yij;
+				double muij = (hij * vijposij) / (r2ij + eta * eta * hij * hij);
+				double piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
+				av_x += -mj * piij * wxq;
+				av_y += -mj * piij * wyq;
+			}
+		}
+	}
+	const double* dA = (const double*)a.dA;
+	double d[8];
+	d[0] = (flags & A_ADVECTION) ? vxi : 0.;
+	d[1] = (flags & A_ADVECTION) ? vyi : 0.;
+	d[2] = av_x;
+	d[3] = av_y;
+	if (flags & A_MOMENTUM_TL) {
+		d[2] += 1. / rho0 * (Pxx_x + Pyx_y) + a.fcx[i] / a.m[i];
+		d[3] += 1. / rho0 * (Pxy_x + Pyy_y) + a.fcy[i] / a.m[i];
+	}
+	d[4] = dA[i]; d[5] = dA[n + i]; d[6] = dA[2 * n + i]; d[7] = dA[3 * n + i];
+	double* bp[8] = {a.base.x, a.base.y, a.base.vx, a.base.vy, a.base.rho, a.base.Sxx, a.base.Sxy, a.base.Syy};
+	double* ap[8] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy, a.acc.rho, a.acc.Sxx, a.acc.Sxy, a.acc.Syy};
+	double* sp[8] = {a.st.x, a.st.y, a.st.vx, a.st.vy, a.st.rho, a.st.Sxx, a.st.Sxy, a.st.Syy};
+	uint32_t stg = a.stage;
+	double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+		// the next stage state goes to nxt (ping-pong), read by the next stage
+		double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
+#pragma unroll
+		for (int q = 0; q < 8; q++) {
+			ap[q][i] = (stg == 0) ? d[q] : ap[q][i] + 2 * d[q];
+			np[q][i] = bp[q][i] + d[q] * dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+		double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
+#pragma unroll
+		for (int q = 0; q < 8; q++) {
+			double v = bp[q][i] + w6 * (ap[q][i] + d[q]);
+			bp[q][i] = v;
+			np[q][i] = v;  // the next step's first stage starts from a copy of the particles
+		}
+		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
+			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+	(void)sp;
+}
+
+// ---- mixed form: pack the stage state into float-float / float arrays
+__global__ void k_tl_pack(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	double x = s.x[i], y = s.y[i];
+	FF* pk = (FF*)a.pack;
+	uint32_t n = a.n_total;
+	pk[i] = ff_split(x - a.X[i]);
+	pk[n + i] = ff_split(y - a.Y[i]);
+	pk[2 * n + i] = ff_split(x);
+	pk[3 * n + i] = ff_split(y);
+	pk[4 * n + i] = ff_split(s.vx[i]);
+	pk[5 * n + i] = ff_split(s.vy[i]);
+}
+
+__global__ void __launch_bounds__(128) k_tlA32(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const float* wx = (const float*)a.wx;
+	const float* wy = (const float*)a.wy;
+	const FF* pk = (const FF*)a.pack;
+	const float* qw = (const float*)a.qw32;
+	uint32_t n = a.n_total;
+	uint32_t flags = a.flags;
+	FF uxi = pk[i], uyi = pk[n + i], vxi = pk[4 * n + i], vyi = pk[5 * n + i];
+	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
+	float Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
+	uint32_t q1 = a.nbr_off[i + 1];
+	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
+		uint32_t j = a.nbr[q];
+		float qwj = qw[j];
+		float wxq = wx[q] * qwj, wyq = wy[q] * qwj;
+		if (flags & A_DISP) {
+			float dux = ff_diff(pk[j], uxi), duy = ff_diff(pk[n + j], uyi);
+			Hxx += dux * wxq;
+			Hxy += dux * wyq;
+			Hyx += duy * wxq;
+			Hyy += duy * wyq;
+		}
+		if (flags & A_VEL_TL) {
+			float dvx = ff_diff(pk[4 * n + j], vxi), dvy = ff_diff(pk[5 * n + j], vyi);
+			Fxx += dvx * wxq;
+			Fxy += dvx * wyq;
+			Fyx += dvy * wxq;
+			Fyy += dvy * wyq;
+		}
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
+	double rho = (double)s.rho_f[i];
+	// the 2x2 inversions of the per-particle part stay FP64
+	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
+	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
+	float4* P = (float4*)a.P;
+	P[i] = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
+	float4* dA = (float4*)a.dA;
+	dA[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
+	((float*)a.c)[i] = (float)sqrt(pr.K / rho);
+}
+
+__global__ void __launch_bounds__(128) k_tlB32(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const float* wx = (const float*)a.wx;
+	const float* wy = (const float*)a.wy;
+	const float4* P = (const float4*)a.P;
+	const float* cc = (const float*)a.c;
+	const FF* pk = (const FF*)a.pack;
+	const float* mf = (const float*)a.m32;
+	const float* hf = (const float*)a.h32;
+	uint32_t n = a.n_total;
+	uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	float rho0 = (float)pr.rho0;
+	float4 Pi = P[i];
+	float r21 = 1.f / (rho0 * rho0);
+	FF xi = pk[2 * n + i], yi = pk[3 * n + i], vxi = pk[4 * n + i], vyi = pk[5 * n + i];
+	float hi = hf[i], rhoi = s.rho_f[i], ci = cc[i];
+	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
+	uint32_t q1 = a.nbr_off[i + 1];
+	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
+		uint32_t j = a.nbr[q];
+		float wxq = wx[q], wyq = wy[q];
+		float mj = mf[j];
+		if (flags & A_STRESS_TL) {
+			float4 Pj = P[j];
+			float fx = mj * r21 * rho0 * wxq, fy = mj * r21 * rho0 * wyq;
+			Pxx_x += (Pi.x + Pj.x) * fx;
+			Pyx_y += (Pi.z + Pj.z) * fy;
+			Pxy_x += (Pi.y + Pj.y) * fx;
+			Pyy_y += (Pi.w + Pj.w) * fy;
+		}
+		if (flags & A_ART_VISC) {
+			float vijx = ff_diff(vxi, pk[4 * n + j]), vijy = ff_diff(vyi, pk[5 * n + j]);
+			float xij = ff_diff(xi, pk[2 * n + j]), yij = ff_diff(yi, pk[3 * n + j]);
+			float vijposij = vijx * xij + vijy * yij;
+			if (vijposij < 0.f) {
+				float cij = 0.5f * (ci + cc[j]);
+				float hij = 0.5f * (hi + hf[j]);
+				float rhoij = 0.5f * (rhoi + s.rho_f[j]);
+				float r2ij = xij * xij + yij * yij;
+				float muij = (hij * vijposij) / (r2ij + eta2 * hij * hij);
+				float piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
+				av_x += -mj * piij * wxq;
+				av_y += -mj * piij * wyq;
+			}
+		}
+	}
+	float4 dAi = ((const float4*)a.dA)[i];
+	double d[4];
+	d[0] = (flags & A_ADVECTION) ? s.vx[i] : 0.;
+	d[1] = (flags & A_ADVECTION) ? s.vy[i] : 0.;
+	d[2] = av_x;
+	d[3] = av_y;
+	if (flags & A_MOMENTUM_TL) {
+		d[2] += (double)(1.f / rho0 * (Pxx_x + Pyx_y)) + a.fcx[i] / a.m[i];
+		d[3] += (double)(1.f / rho0 * (Pxy_x + Pyy_y)) + a.fcy[i] / a.m[i];
+	}
+	float e[4] = {dAi.x, dAi.y, dAi.z, dAi.w};
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* np[4] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy};
+	float* bq[4] = {a.base.rho_f, a.base.Sxx_f, a.base.Sxy_f, a.base.Syy_f};
+	float* aq[4] = {a.acc.rho_f, a.acc.Sxx_f, a.acc.Sxy_f, a.acc.Syy_f};
+	float* nq[4] = {a.nxt.rho_f, a.nxt.Sxx_f, a.nxt.Sxy_f, a.nxt.Syy_f};
+	uint32_t stg = a.stage;
+	double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ap[q][i] = (stg == 0) ? d[q] : ap[q][i] + 2 * d[q];
+			np[q][i] = bp[q][i] + d[q] * dts;
+			aq[q][i] = (stg == 0) ? e[q] : aq[q][i] + 2.f * e[q];
+			nq[q][i] = bq[q][i] + e[q] * (float)dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			double v = bp[q][i] + w6 * (ap[q][i] + d[q]);
+			bp[q][i] = v;
+			np[q][i] = v;
+			float f = bq[q][i] + (float)w6 * (aq[q][i] + e[q]);
+			bq[q][i] = f;
+			nq[q][i] = f;
+		}
+		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
+			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+}
+
+__global__ void k_advance_time(uint32_t nb, BodyParams* P) {
+	uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b < nb) P[b].time += P[b].dt;
+}
+
+}  // namespace
+
+cudaError_t tl_search(const TLSearchArgs& a, int pass, cudaStream_t s) {
+	DevStatus* st = reinterpret_cast<DevStatus*>(a.status);
+	if (pass == 0) {
+		k_search_hash<<<grid1(a.n_from, 256), 256, 0, s>>>(a);
+		size_t tmp = a.sort_tmp_bytes;
+		cudaError_t e = cub::DeviceRadixSort::SortPairs(a.sort_tmp, tmp, a.keys, a.keys_sorted, a.vals, a.perm,
+		                                                (int)a.n_from, 0, a.sort_bits, s);
+		if (e != cudaSuccess) return e;
+		k_search_cells<<<grid1(a.n_from + 1, 256), 256, 0, s>>>(a.n_from, a.keys_sorted, a.total_cells, a.cell_start);
+	}
+	k_search<<<grid1(a.n_to, 128), 128, 0, s>>>(a, pass, st);
+	return cudaGetLastError();
+}
+
+size_t tl_sort_tmp_bytes(uint32_t n, int bits) {
+	size_t bytes = 0;
+	cub::DeviceRadixSort::SortPairs(nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+	                                (uint32_t*)nullptr, (int)n, 0, bits);
+	return bytes;
+}
+
+cudaError_t tl_rl(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y,
+                  const double* m, const double* rho, const float* rho_f, const double* h, double* wx, double* wy,
+                  void* status, cudaStream_t s) {
+	k_rl<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, x, y, m, rho, rho_f, h, wx, wy, reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s) {
+	k_to_float<<<grid1(n, 256), 256, 0, s>>>(n, a, b);
+	return cudaGetLastError();
+}
+
+cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
+	// part 0: BCs on the stage state, 1: pack (mixed), 2: pass A, 3: pass B,
+	// 4: BCs on the particles after the combine, 5: advance the body clocks
+	switch (part) {
+	case 0:
+		if (a.n_bc) k_tl_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 0);
+		break;
+	case 1:
+		if (mixed) k_tl_pack<<<grid1(a.n_total, 256), 256, 0, s>>>(a);
+		break;
+	case 2:
+		if (mixed) k_tlA32<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+		else k_tlA64<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+		break;
+	case 3:
+		if (mixed) k_tlB32<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+		else k_tlB64<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+		break;
+	case 4:
+		if (a.n_bc) k_tl_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 1);
+		break;
+	case 5:
+		k_advance_time<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, const_cast<BodyParams*>(a.params));
+		break;
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS

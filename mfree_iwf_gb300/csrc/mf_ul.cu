@@ -1,0 +1,779 @@
+// Updated-Lagrangian (Gray-Monaghan) SPH time-step kernels.
+//
+// One derivative evaluation of the reference (body::compute_time_derivatives for
+// particle_ul, body.h:125-148) rebuilds the cell grid, sorts the particles by cell
+// hash, builds Verlet lists, evaluates the kernel per pair and runs the action list
+// (rings.cpp:86-96).  Here that becomes, per RK4 stage, for all bodies at once:
+//
+//   ul_bbox      per-body bounding box and h_max        (grid.h:83-104)
+//   ul_geom      per-body cell geometry, cell offsets   (grid.h:105-115)
+//   ul_hash      global cell key per row                (grid.h:35-41)
+//   CUB radix sort of (key, row)                        (body.h:137)
+//   ul_cells     cell start table, empty cells filled from the right (grid.h:48-81)
+//   ul_gather    the rows' stage state in cell order, with the per-particle actions
+//                EOS (material.h:37-64), artificial stress (correctors.h:37-81) and
+//                integration weights (riemann_integration.h:28-33) fused in
+//   ul_pair      one thread per row: walks the 3x3 cell stencil of the reference grid
+//                (grid.h:117-177), evaluates W/gradW (kernel.cpp:20-55) and every pair
+//                action at once -- derive_stress_monaghan (derivatives.h:378-443),
+//                derive_velocity (:32-66), artificial viscosity (correctors.h:83-137),
+//                XSPH (:139-169) -- then the per-particle actions Jaumann rate
+//                (material.h:66-100), continuity, momentum and advection
+//                (cont_mech.h:32-49,108-142) and the RK4 update (rk4.h:52-108).
+//
+// Neighbour lists are never stored: the pair kernel re-derives them from the cell
+// table with the reference's predicate r^2 <= 4 h_i^2 + eps, evaluated without FMA
+// contraction so the neighbour sets are the reference's, bit for bit.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "mf_common.cuh"
+#include "mf_kernels.h"
+
+using namespace mfk;
+using mfk_host::BodyParams;
+using mfk_host::Geom;
+using mfk_host::ULArgs;
+
+namespace MF_NS {
+namespace {
+
+enum : uint32_t {
+	A_RIEMANN = 1u << 1,
+	A_EOS = 1u << 2,
+	A_ART_STRESS = 1u << 3,
+	A_STRESS_MGHN = 1u << 4,
+	A_DERIVE_VEL = 1u << 5,
+	A_ART_VISC = 1u << 6,
+	A_XSPH = 1u << 7,
+	A_JAUMANN = 1u << 8,
+	A_CONTINUITY = 1u << 9,
+	A_MOMENTUM_UL = 1u << 10,
+	A_ADVECTION = 1u << 11,
+};
+
+// Cell-ordered record of one particle's stage state plus per-particle derived
+// quantities.  FP64 form: 16 doubles = 128 bytes, loaded as 8 x 16 B.
+struct __align__(16) Rec64 {
+	double x, y, vx, vy;
+	double m, h, rho, sxx;   // sxx = Sxx - p
+	double sxy, syy, Rxx, Rxy;
+	double Ryy, c, qw, rho21;  // c = sqrt(K/rho), qw = m/rho (or the stored weight), rho21 = 1/rho^2
+};
+// Mixed form: positions and velocities as float-float, the rest FP32: 80 bytes.
+struct __align__(16) Rec32 {
+	FF x, y, vx, vy;
+	float m, h, rho, sxx;
+	float sxy, syy, Rxx, Rxy;
+	float Ryy, c, qw, rho21;
+};
+
+__device__ __forceinline__ Rec64 load_rec(const Rec64* p) {
+	Rec64 r;
+	const double2* s = reinterpret_cast<const double2*>(p);
+	double2* d = reinterpret_cast<double2*>(&r);
+#pragma unroll
+	for (int i = 0; i < 8; i++) d[i] = __ldg(s + i);
+	return r;
+}
+__device__ __forceinline__ Rec32 load_rec(const Rec32* p) {
+	Rec32 r;
+	const float4* s = reinterpret_cast<const float4*>(p);
+	float4* d = reinterpret_cast<float4*>(&r);
+#pragma unroll
+	for (int i = 0; i < 5; i++) d[i] = __ldg(s + i);
+	return r;
+}
+
+// --------------------------------------------------------------- grid build
+__global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
+	uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b >= nb) return;
+	bb[5 * b + 0] = ord_encode(1.7976931348623157e308);   // min x
+	bb[5 * b + 1] = ord_encode(1.7976931348623157e308);   // min y
+	bb[5 * b + 2] = ord_encode(-1.7976931348623157e308);  // max x
+	bb[5 * b + 3] = ord_encode(-1.7976931348623157e308);  // max y
+	bb[5 * b + 4] = ord_encode(-1.7976931348623157e308);  // h_max (or the mixed-form reach)
+}
+
+// Bounding box and h_max per body (grid.h:83-104).  Rows of a body are contiguous,
+// so a warp whose rows share one body reduces in registers and issues one atomic
+// per quantity.  In the mixed form the fifth slot holds h + 4|v|dt (the reach a
+// particle can have within one step), which sizes cells valid for all four stages.
+__global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
+                       const double* __restrict__ h, const double* __restrict__ vx, const double* __restrict__ vy,
+                       const uint32_t* __restrict__ body_of, const BodyParams* __restrict__ P, int mixed,
+                       unsigned long long* bb) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	bool valid = i < n;
+	uint32_t b = valid ? body_of[i] : 0xffffffffu;
+	unsigned long long mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull, mh = 0ull;
+	if (valid) {
+		mnx = mxx = ord_encode(x[i]);
+		mny = mxy = ord_encode(y[i]);
+		double hh = h[i];
+		if (mixed) hh = hh + 4.0 * sqrt(vx[i] * vx[i] + vy[i] * vy[i]) * P[b].dt;
+		mh = ord_encode(hh);
+	}
+	uint32_t lane = threadIdx.x & 31;
+	uint32_t b0 = __shfl_sync(0xffffffffu, b, 0);
+	bool uniform = __all_sync(0xffffffffu, b == b0) && b0 != 0xffffffffu;
+	if (uniform) {
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+			mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+			mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+			mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+			mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+		}
+		if (lane == 0) {
+			atomicMin(&bb[5 * b0 + 0], mnx);
+			atomicMin(&bb[5 * b0 + 1], mny);
+			atomicMax(&bb[5 * b0 + 2], mxx);
+			atomicMax(&bb[5 * b0 + 3], mxy);
+			atomicMax(&bb[5 * b0 + 4], mh);
+		}
+	} else if (valid) {
+		atomicMin(&bb[5 * b + 0], mnx);
+		atomicMin(&bb[5 * b + 1], mny);
+		atomicMax(&bb[5 * b + 2], mxx);
+		atomicMax(&bb[5 * b + 3], mxy);
+		atomicMax(&bb[5 * b + 4], mh);
+	}
+}
+
+// Cell geometry per body (grid.h:105-115) and the exclusive scan of cell counts.
+// One block; bodies are processed serially in chunks for the scan.
+__global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyParams* P, int mixed, Geom* G,
+                       uint32_t* total_cells, uint32_t cell_cap, DevStatus* st) {
+	__shared__ uint32_t s_cnt[1024];
+	__shared__ uint32_t s_base;
+	if (threadIdx.x == 0) s_base = 0;
+	__syncthreads();
+	for (uint32_t c0 = 0; c0 < nb; c0 += blockDim.x) {
+		uint32_t b = c0 + threadIdx.x;
+		uint32_t cnt = 0;
+		Geom g{};
+		if (b < nb) {
+			double bminx = ord_decode(bb[5 * b + 0]), bminy = ord_decode(bb[5 * b + 1]);
+			double bmaxx = ord_decode(bb[5 * b + 2]), bmaxy = ord_decode(bb[5 * b + 3]);
+			double hmax = ord_decode(bb[5 * b + 4]);
+			bminx -= 1e-6; bminy -= 1e-6;
+			bmaxx += 1e-6; bmaxy += 1e-6;
+			double dx = hmax * 2.;
+			double lx = bmaxx - bminx, ly = bmaxy - bminy;
+			double fnx = ceil(lx / dx), fny = ceil(ly / dx);
+			uint32_t nx = (uint32_t)fnx, ny = (uint32_t)fny;
+			uint32_t num_cell = nx * ny;
+			if (!(num_cell < P[b].n) && !mixed) {
+				raise(st, ERR_GRID, P[b].off);
+			}
+			if (!(fnx * fny < 4.0e9) || nx == 0 || ny == 0) {
+				raise(st, ERR_GRID, P[b].off);
+				nx = ny = 1;
+				num_cell = 1;
+			}
+			g.bbmin_x = bminx; g.bbmin_y = bminy; g.dx = dx;
+			g.nx = nx; g.ny = ny; g.num_cell = num_cell;
+			cnt = num_cell;
+		}
+		s_cnt[threadIdx.x] = cnt;
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			uint32_t run = s_base;
+			uint32_t lim = min((uint32_t)blockDim.x, nb - c0);
+			for (uint32_t t = 0; t < lim; t++) {
+				uint32_t c = s_cnt[t];
+				s_cnt[t] = run;
+				run += c;
+			}
+			s_base = run;
+		}
+		__syncthreads();
+		if (b < nb) {
+			g.cell_off = s_cnt[threadIdx.x];
+			G[b] = g;
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		uint32_t tot = s_base;
+		if (tot > cell_cap) {
+			raise(st, ERR_GRID, 0);
+			tot = 0;  // downstream kernels see an empty grid
+		}
+		*total_cells = tot;
+	}
+}
+
+// Global cell key of each row (grid.h:35-41): cell_off + ix*ny + iy.
+__global__ void k_hash(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
+                       const uint32_t* __restrict__ body_of, const Geom* __restrict__ G,
+                       const uint32_t* __restrict__ total_cells, uint32_t* keys, uint32_t* vals, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	Geom g = G[body_of[i]];
+	uint32_t ix = (uint32_t)((x[i] - g.bbmin_x) / g.dx);
+	uint32_t iy = (uint32_t)((y[i] - g.bbmin_y) / g.dx);
+	if (ix >= g.nx || iy >= g.ny || *total_cells == 0) {
+		raise(st, ERR_GRID, i);
+		ix = min(ix, g.nx - 1);
+		iy = min(iy, g.ny - 1);
+	}
+	uint32_t key = g.cell_off + ix * g.ny + iy;
+	keys[i] = (*total_cells == 0) ? 0u : key;
+	vals[i] = i;
+}
+
+// Cell start table over all bodies' cells (grid.h:48-81): cell_start[c] is the
+// first sorted position with key >= c, so empty cells get the next start.
+__global__ void k_cells(uint32_t n, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ total_cells,
+                        uint32_t* cell_start) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t tot = *total_cells;
+	if (k > n) return;
+	if (k == n) {
+		uint32_t last = (n == 0) ? 0u : keys[n - 1] + 1;
+		for (uint32_t c = last; c <= tot; c++) cell_start[c] = n;
+		return;
+	}
+	uint32_t key = min(keys[k], tot);
+	uint32_t prev = (k == 0) ? 0u : min(keys[k - 1], tot) + 1;
+	if (k == 0 || keys[k] != keys[k - 1])
+		for (uint32_t c = prev; c <= key; c++) cell_start[c] = k;
+}
+
+// ---------------------------------------------------------------- gather
+template <bool MIXED>
+struct StageView;
+
+// Reads the stage state of row i: stage 0 reads the base state (k1 is a copy of
+// the particles, rk4.h:76-78), later stages the RK stage arrays.
+template <>
+struct StageView<false> {
+	const double *x, *y, *vx, *vy, *rho, *Sxx, *Sxy, *Syy;
+	__device__ void load(uint32_t i, double& X, double& Y, double& VX, double& VY, double& R, double& A, double& B,
+	                     double& C) const {
+		X = x[i]; Y = y[i]; VX = vx[i]; VY = vy[i]; R = rho[i]; A = Sxx[i]; B = Sxy[i]; C = Syy[i];
+	}
+};
+template <>
+struct StageView<true> {
+	const double *x, *y, *vx, *vy;
+	const float *rho, *Sxx, *Sxy, *Syy;
+	__device__ void load(uint32_t i, double& X, double& Y, double& VX, double& VY, float& R, float& A, float& B,
+	                     float& C) const {
+		X = x[i]; Y = y[i]; VX = vx[i]; VY = vy[i]; R = rho[i]; A = Sxx[i]; B = Sxy[i]; C = Syy[i];
+	}
+};
+
+template <bool MIXED>
+__device__ StageView<MIXED> stage_view(const ULArgs& a);
+template <>
+__device__ StageView<false> stage_view<false>(const ULArgs& a) {
+	const mfk_host::StateSoA& s = a.stage == 0 ? a.base : a.st;
+	return StageView<false>{s.x, s.y, s.vx, s.vy, s.rho, s.Sxx, s.Sxy, s.Syy};
+}
+template <>
+__device__ StageView<true> stage_view<true>(const ULArgs& a) {
+	const mfk_host::StateSoA& s = a.stage == 0 ? a.base : a.st;
+	return StageView<true>{s.x, s.y, s.vx, s.vy, s.rho_f, s.Sxx_f, s.Sxy_f, s.Syy_f};
+}
+
+// Per-particle actions of one stage: EOS, artificial stress, integration weight.
+template <class T>
+__device__ __forceinline__ void per_particle(uint32_t flags, const BodyParams& pr, T m, T rho, T qw0, T Sxx, T Sxy,
+                                             T Syy, T& sxx_o, T& syy_o, T& Rxx, T& Rxy, T& Ryy, T& c, T& qw,
+                                             T& rho21) {
+	T p = T(0);
+	if (flags & A_EOS) p = T(pr.c0sq) * (rho - T(pr.rho0));  // c0*c0*(rho - rho0)
+	T sxx = Sxx - p, syy = Syy - p, sxy = Sxy;
+	Rxx = Rxy = Ryy = T(0);
+	if (flags & A_ART_STRESS) {
+		T eps = T(pr.mghn_eps);
+		T theta = T(0.5) * atan2(T(2.) * sxy, sxx - syy + T(0.));
+		T cs = cos(theta), sn = sin(theta);
+		T cs2 = cs * cs, sn2 = sn * sn;
+		T rot_sxx = cs2 * sxx + T(2.0) * cs * sn * sxy + sn2 * syy;
+		T rot_syy = sn2 * sxx - T(2.0) * cs * sn * sxy + cs2 * syy;
+		T rot_rxx = T(0), rot_ryy = T(0);
+		if (rot_sxx > T(0)) rot_rxx = -eps * rot_sxx / (rho * rho);
+		if (rot_syy > T(0)) rot_ryy = -eps * rot_syy / (rho * rho);
+		Rxx = cs2 * rot_rxx + sn2 * rot_ryy;
+		Rxy = cs * sn * (rot_rxx - rot_ryy);
+		Ryy = sn2 * rot_rxx + cs2 * rot_ryy;
+	}
+	sxx_o = sxx;
+	syy_o = syy;
+	c = sqrt(T(pr.K) / rho);
+	qw = (flags & A_RIEMANN) ? m / rho : qw0;
+	rho21 = T(1.) / (rho * rho);
+}
+
+__global__ void k_gather64(ULArgs a, const BodyParams* __restrict__ P) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.n_total) return;
+	uint32_t i = a.perm[k];
+	StageView<false> v = stage_view<false>(a);
+	double x, y, vx, vy, rho, Sxx, Sxy, Syy;
+	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
+	uint32_t b = a.body_of[i];
+	Rec64 r;
+	r.x = x; r.y = y; r.vx = vx; r.vy = vy;
+	r.m = a.m[i]; r.h = a.h[i]; r.rho = rho;
+	per_particle<double>(a.flags, P[b], r.m, rho, a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c, r.qw,
+	                     r.rho21);
+	r.sxy = Sxy;
+	Rec64* out = reinterpret_cast<Rec64*>(a.rec) + k;
+	const double2* s = reinterpret_cast<const double2*>(&r);
+	double2* d = reinterpret_cast<double2*>(out);
+#pragma unroll
+	for (int q = 0; q < 8; q++) d[q] = s[q];
+	a.rec_body[k] = b;
+}
+
+__global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.n_total) return;
+	uint32_t i = a.perm[k];
+	StageView<true> v = stage_view<true>(a);
+	double x, y, vx, vy;
+	float rho, Sxx, Sxy, Syy;
+	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
+	uint32_t b = a.body_of[i];
+	Rec32 r;
+	r.x = ff_split(x); r.y = ff_split(y); r.vx = ff_split(vx); r.vy = ff_split(vy);
+	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
+	per_particle<float>(a.flags, P[b], r.m, rho, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c,
+	                    r.qw, r.rho21);
+	r.sxy = Sxy;
+	Rec32* out = reinterpret_cast<Rec32*>(a.rec) + k;
+	const float4* s = reinterpret_cast<const float4*>(&r);
+	float4* d = reinterpret_cast<float4*>(out);
+#pragma unroll
+	for (int q = 0; q < 5; q++) d[q] = s[q];
+	a.rec_body[k] = b;
+}
+
+// --------------------------------------------------------------- RK update
+// rk4.h:52-69 (stage state = particles + c*dt*derivative) and :94-103 (final
+// combine with weights 1,2,2,1 / 6).  d[] = x_t, y_t, vx_t, vy_t, rho_t, Sxx_t, Sxy_t, Syy_t.
+template <class T>
+__device__ __forceinline__ void rk_update_f64(const ULArgs& a, uint32_t i, double dt, const double d[8]) {
+	double* bp[8] = {a.base.x, a.base.y, a.base.vx, a.base.vy, a.base.rho, a.base.Sxx, a.base.Sxy, a.base.Syy};
+	double* ap[8] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy, a.acc.rho, a.acc.Sxx, a.acc.Sxy, a.acc.Syy};
+	double* sp[8] = {a.st.x, a.st.y, a.st.vx, a.st.vy, a.st.rho, a.st.Sxx, a.st.Sxy, a.st.Syy};
+	uint32_t s = a.stage;
+	if (s < 3) {
+		double dts = (s == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 8; q++) {
+			double accv = (s == 0) ? d[q] : ap[q][i] + 2 * d[q];
+			ap[q][i] = accv;
+			sp[q][i] = bp[q][i] + d[q] * dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 8; q++) bp[q][i] = bp[q][i] + w6 * (ap[q][i] + d[q]);
+	}
+}
+
+// Mixed form: x, y, vx, vy accumulate in FP64, rho and the stresses in FP32.
+__device__ __forceinline__ void rk_update_mixed(const ULArgs& a, uint32_t i, double dt, const float d[8]) {
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* sp[4] = {a.st.x, a.st.y, a.st.vx, a.st.vy};
+	float* bq[4] = {a.base.rho_f, a.base.Sxx_f, a.base.Sxy_f, a.base.Syy_f};
+	float* aq[4] = {a.acc.rho_f, a.acc.Sxx_f, a.acc.Sxy_f, a.acc.Syy_f};
+	float* sq[4] = {a.st.rho_f, a.st.Sxx_f, a.st.Sxy_f, a.st.Syy_f};
+	uint32_t s = a.stage;
+	if (s < 3) {
+		double dts = (s == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			double dq = (double)d[q];
+			ap[q][i] = (s == 0) ? dq : ap[q][i] + 2 * dq;
+			sp[q][i] = bp[q][i] + dq * dts;
+			float dr = d[4 + q];
+			aq[q][i] = (s == 0) ? dr : aq[q][i] + 2.f * dr;
+			sq[q][i] = bq[q][i] + dr * (float)dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			bp[q][i] = bp[q][i] + w6 * (ap[q][i] + (double)d[q]);
+			bq[q][i] = bq[q][i] + (float)w6 * (aq[q][i] + d[4 + q]);
+		}
+	}
+}
+
+__device__ __forceinline__ void stencil(const Geom& g, uint32_t key, int& lo_i, int& hi_i, int& lo_j, int& hi_j) {
+	uint32_t b = key - g.cell_off;
+	uint32_t gi = b / g.ny;
+	uint32_t gj = b - gi * g.ny;
+	lo_i = (int)gi - 1 < 0 ? 0 : (int)gi - 1;
+	lo_j = (int)gj - 1 < 0 ? 0 : (int)gj - 1;
+	hi_i = gi + 2 > g.nx ? (int)g.nx : (int)gi + 2;
+	hi_j = gj + 2 > g.ny ? (int)g.ny : (int)gj + 2;
+}
+
+// ----------------------------------------------------------- pair kernel FP64
+__global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __restrict__ P,
+                                                const Geom* __restrict__ G, DevStatus* st) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.n_total) return;
+	const Rec64* rec = reinterpret_cast<const Rec64*>(a.rec);
+	const Rec64 ri = load_rec(rec + k);
+	uint32_t b = a.rec_body[k];
+	const BodyParams& pr = P[b];
+	Geom g = G[b];
+	uint32_t i = a.perm[k];
+	uint32_t flags = a.flags;
+	int lo_i, hi_i, lo_j, hi_j;
+	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+
+	double hi = ri.h;
+	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(hi, hi), 2.), 2.);
+	double lim = __dadd_rn(radius2, a.nbh_eps);
+	double reach2 = 4.0000001 * hi * hi;  // pairs beyond q = 2 contribute exactly zero
+	double rhoi21 = ri.rho21;
+	double wdeltap = pr.wdeltap, corr_exp = pr.corr_exp;
+	double alpha = pr.alpha, beta = pr.beta, eta = pr.eta, xeps = pr.xsph_eps;
+
+	double Sxx_x = 0., Sxy_y = 0., Sxy_x = 0., Syy_y = 0.;
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+	double av_x = 0., av_y = 0., xs_x = 0., xs_y = 0.;
+	uint32_t cnt = 0;
+	for (int ni = lo_i; ni < hi_i; ni++) {
+		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
+		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
+		for (uint32_t kj = j0; kj < j1; kj++) {
+			const Rec64 rj = load_rec(rec + kj);
+			double xij = __dsub_rn(ri.x, rj.x);
+			double yij = __dsub_rn(ri.y, rj.y);
+			double r2 = __dadd_rn(__dmul_rn(xij, xij), __dmul_rn(yij, yij));
+			cnt += (r2 <= lim) ? 1u : 0u;
+			if (r2 > reach2) continue;
+			KR64 w = cubic_spline(xij, yij, hi);
+			if (flags & A_STRESS_MGHN) {
+				double Rxx = 0., Rxy = 0., Ryy = 0.;
+				if (wdeltap > 0) {
+					double fab = w.w / wdeltap;
+					if (corr_exp == 4.) {
+						double f2 = fab * fab;
+						fab = f2 * f2;
+					} else {
+						fab = pow(fab, corr_exp);
+					}
+					Rxx = fab * (ri.Rxx + rj.Rxx);
+					Rxy = fab * (ri.Rxy + rj.Rxy);
+					Ryy = fab * (ri.Ryy + rj.Ryy);
+				}
+				Sxx_x += rj.m * (ri.sxx * rhoi21 + rj.sxx * rj.rho21 + Rxx) * w.w_x;
+				Sxy_y += rj.m * (ri.sxy * rhoi21 + rj.sxy * rj.rho21 + Rxy) * w.w_y;
+				Sxy_x += rj.m * (ri.sxy * rhoi21 + rj.sxy * rj.rho21 + Rxy) * w.w_x;
+				Syy_y += rj.m * (ri.syy * rhoi21 + rj.syy * rj.rho21 + Ryy) * w.w_y;
+			}
+			if (flags & A_DERIVE_VEL) {
+				vx_x += (rj.vx - ri.vx) * w.w_x * rj.qw;
+				vx_y += (rj.vx - ri.vx) * w.w_y * rj.qw;
+				vy_x += (rj.vy - ri.vy) * w.w_x * rj.qw;
+				vy_y += (rj.vy - ri.vy) * w.w_y * rj.qw;
+			}
+			double vijx = ri.vx - rj.vx, vijy = ri.vy - rj.vy;
+			if (flags & A_ART_VISC) {
+				double vijposij = vijx * xij + vijy * yij;
+				if (vijposij < 0.) {
+					double cij = 0.5 * (ri.c + rj.c);
+					double hij = 0.5 * (hi + rj.h);
+					double rhoij = 0.5 * (ri.rho + rj.rho);
+					double r2ij = xij * xij + yij * yij;
+					double muij = (hij * vijposij) / (r2ij + eta * eta * hij * hij);
+					double piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
+					av_x += -rj.m * piij * w.w_x;
+					av_y += -rj.m * piij * w.w_y;
+				}
+			}
+			if (flags & A_XSPH) {
+				double rhoij = 0.5 * (ri.rho + rj.rho);
+				double fac = -xeps * w.w * ri.m / rhoij;
+				xs_x += fac * vijx;
+				xs_y += fac * vijy;
+			}
+		}
+	}
+	if (a.max_nbh && cnt >= a.max_nbh) raise(st, ERR_NBH_OVERFLOW, i);
+	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
+
+	// per-particle actions, in the reference's list order
+	double d[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+	double rhoi = ri.rho;
+	if (flags & A_STRESS_MGHN) { Sxx_x *= rhoi; Sxy_y *= rhoi; Sxy_x *= rhoi; Syy_y *= rhoi; }
+	if (flags & A_ART_VISC) { d[2] = av_x; d[3] = av_y; }
+	if (flags & A_XSPH) { d[0] = xs_x; d[1] = xs_y; }
+	if (flags & A_JAUMANN) {
+		double Sxx = ri.sxx, Syy = ri.syy;
+		// the Jaumann rate uses the stored deviatoric-plus-pressure S (without p)
+		double p = 0.;
+		if (flags & A_EOS) p = pr.c0sq * (rhoi - pr.rho0);
+		Sxx = Sxx + p;
+		Syy = Syy + p;
+		jaumann<double>(vx_x, vx_y, vy_x, vy_y, Sxx, ri.sxy, Syy, pr.G, d[5], d[6], d[7]);
+	}
+	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
+	if (flags & A_MOMENTUM_UL) {
+		d[2] += 1. / rhoi * (Sxx_x + Sxy_y) + a.fcx[i] / ri.m;
+		d[3] += 1. / rhoi * (Sxy_x + Syy_y) + a.fcy[i] / ri.m;
+	}
+	if (flags & A_ADVECTION) { d[0] += ri.vx; d[1] += ri.vy; }
+	rk_update_f64<double>(a, i, pr.dt, d);
+	if (a.stage == 3 && !(isfinite(a.base.x[i]) && isfinite(a.base.y[i]) && isfinite(a.base.vx[i]) &&
+	                      isfinite(a.base.vy[i]) && isfinite(a.base.rho[i])))
+		raise(st, ERR_NONFINITE, i);
+}
+
+// ---------------------------------------------------------- pair kernel mixed
+__global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __restrict__ P,
+                                                const Geom* __restrict__ G, DevStatus* st) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.n_total) return;
+	const Rec32* rec = reinterpret_cast<const Rec32*>(a.rec);
+	const Rec32 ri = load_rec(rec + k);
+	uint32_t b = a.rec_body[k];
+	const BodyParams& pr = P[b];
+	Geom g = G[b];
+	uint32_t i = a.perm[k];
+	uint32_t flags = a.flags;
+	int lo_i, hi_i, lo_j, hi_j;
+	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+
+	float hi = ri.h;
+	float h1 = 1.f / hi;
+	float fac = (float)(10 * (K_1_PI) / 7.0) * h1 * h1;
+	float reach2 = 4.0001f * hi * hi;
+	float rhoi21 = ri.rho21;
+	float wdp1 = pr.wdeltap > 0 ? (float)(1.0 / pr.wdeltap) : 0.f;
+	bool exp4 = pr.corr_exp == 4.;
+	float corr_exp = (float)pr.corr_exp;
+	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta), xeps = (float)pr.xsph_eps;
+
+	float Sxx_x = 0.f, Sxy_y = 0.f, Sxy_x = 0.f, Syy_y = 0.f;
+	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
+	float av_x = 0.f, av_y = 0.f, xs_x = 0.f, xs_y = 0.f;
+	for (int ni = lo_i; ni < hi_i; ni++) {
+		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
+		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
+		for (uint32_t kj = j0; kj < j1; kj++) {
+			const Rec32 rj = load_rec(rec + kj);
+			float xij = ff_diff(ri.x, rj.x);
+			float yij = ff_diff(ri.y, rj.y);
+			float r2 = xij * xij + yij * yij;
+			if (r2 > reach2) continue;
+			KR32 w = cubic_spline_f(xij, yij, h1, fac);
+			if (flags & A_STRESS_MGHN) {
+				float Rxx = 0.f, Rxy = 0.f, Ryy = 0.f;
+				if (wdp1 > 0.f) {
+					float fab = w.w * wdp1;
+					if (exp4) {
+						float f2 = fab * fab;
+						fab = f2 * f2;
+					} else {
+						fab = powf(fab, corr_exp);
+					}
+					Rxx = fab * (ri.Rxx + rj.Rxx);
+					Rxy = fab * (ri.Rxy + rj.Rxy);
+					Ryy = fab * (ri.Ryy + rj.Ryy);
+				}
+				float tsx = rj.m * (ri.sxy * rhoi21 + rj.sxy * rj.rho21 + Rxy);
+				Sxx_x += rj.m * (ri.sxx * rhoi21 + rj.sxx * rj.rho21 + Rxx) * w.w_x;
+				Sxy_y += tsx * w.w_y;
+				Sxy_x += tsx * w.w_x;
+				Syy_y += rj.m * (ri.syy * rhoi21 + rj.syy * rj.rho21 + Ryy) * w.w_y;
+			}
+			float dvx = ff_diff(rj.vx, ri.vx), dvy = ff_diff(rj.vy, ri.vy);
+			if (flags & A_DERIVE_VEL) {
+				float qx = w.w_x * rj.qw, qy = w.w_y * rj.qw;
+				vx_x += dvx * qx;
+				vx_y += dvx * qy;
+				vy_x += dvy * qx;
+				vy_y += dvy * qy;
+			}
+			if (flags & A_ART_VISC) {
+				float vijposij = -(dvx * xij + dvy * yij);
+				if (vijposij < 0.f) {
+					float cij = 0.5f * (ri.c + rj.c);
+					float hij = 0.5f * (hi + rj.h);
+					float rhoij = 0.5f * (ri.rho + rj.rho);
+					float muij = (hij * vijposij) / (r2 + eta2 * hij * hij);
+					float piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
+					av_x += -rj.m * piij * w.w_x;
+					av_y += -rj.m * piij * w.w_y;
+				}
+			}
+			if (flags & A_XSPH) {
+				float rhoij = 0.5f * (ri.rho + rj.rho);
+				float f = -xeps * w.w * ri.m / rhoij;
+				xs_x -= f * dvx;
+				xs_y -= f * dvy;
+			}
+		}
+	}
+	float d[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+	float rhoi = ri.rho;
+	if (flags & A_STRESS_MGHN) { Sxx_x *= rhoi; Sxy_y *= rhoi; Sxy_x *= rhoi; Syy_y *= rhoi; }
+	if (flags & A_ART_VISC) { d[2] = av_x; d[3] = av_y; }
+	if (flags & A_XSPH) { d[0] = xs_x; d[1] = xs_y; }
+	float vxi = ri.vx.hi + ri.vx.lo, vyi = ri.vy.hi + ri.vy.lo;
+	if (flags & A_JAUMANN) {
+		float p = 0.f;
+		if (flags & A_EOS) p = (float)pr.c0sq * (rhoi - (float)pr.rho0);
+		jaumann<float>(vx_x, vx_y, vy_x, vy_y, ri.sxx + p, ri.sxy, ri.syy + p, (float)pr.G, d[5], d[6], d[7]);
+	}
+	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
+	if (flags & A_MOMENTUM_UL) {
+		d[2] += 1.f / rhoi * (Sxx_x + Sxy_y) + (float)(a.fcx[i] / (double)ri.m);
+		d[3] += 1.f / rhoi * (Sxy_x + Syy_y) + (float)(a.fcy[i] / (double)ri.m);
+	}
+	// advection: the FP64 velocity enters the FP64 position update below
+	double dd0 = (double)d[0], dd1 = (double)d[1];
+	if (flags & A_ADVECTION) {
+		const mfk_host::StateSoA& s = a.stage == 0 ? a.base : a.st;
+		dd0 += s.vx[i];
+		dd1 += s.vy[i];
+	}
+	(void)vxi; (void)vyi;
+	// position/velocity in FP64, rho/S in FP32
+	uint32_t s = a.stage;
+	double dt = pr.dt;
+	double dq[4] = {dd0, dd1, (double)d[2], (double)d[3]};
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* sp[4] = {a.st.x, a.st.y, a.st.vx, a.st.vy};
+	float* bq[4] = {a.base.rho_f, a.base.Sxx_f, a.base.Sxy_f, a.base.Syy_f};
+	float* aq[4] = {a.acc.rho_f, a.acc.Sxx_f, a.acc.Sxy_f, a.acc.Syy_f};
+	float* sq[4] = {a.st.rho_f, a.st.Sxx_f, a.st.Sxy_f, a.st.Syy_f};
+	if (s < 3) {
+		double dts = (s == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ap[q][i] = (s == 0) ? dq[q] : ap[q][i] + 2 * dq[q];
+			sp[q][i] = bp[q][i] + dq[q] * dts;
+			float dr = d[4 + q];
+			aq[q][i] = (s == 0) ? dr : aq[q][i] + 2.f * dr;
+			sq[q][i] = bq[q][i] + dr * (float)dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			bp[q][i] = bp[q][i] + w6 * (ap[q][i] + dq[q]);
+			bq[q][i] = bq[q][i] + (float)w6 * (aq[q][i] + d[4 + q]);
+		}
+		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i]) &&
+		      isfinite(bq[0][i])))
+			raise(st, ERR_NONFINITE, i);
+	}
+}
+
+// Neighbour lists of the current grid (test/debug): pass 0 counts, pass 1 writes
+// the rows of each list (as global rows) at offs[row].
+__global__ void k_neighbors(ULArgs a, const Geom* __restrict__ G, uint32_t* counts, uint32_t* idx,
+                            const uint64_t* offs, int pass) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.n_total) return;
+	const Rec64* rec = reinterpret_cast<const Rec64*>(a.rec);
+	const Rec64 ri = load_rec(rec + k);
+	Geom g = G[a.rec_body[k]];
+	uint32_t i = a.perm[k];
+	int lo_i, hi_i, lo_j, hi_j;
+	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+	double hi = ri.h;
+	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(hi, hi), 2.), 2.);
+	double lim = __dadd_rn(radius2, a.nbh_eps);
+	uint32_t cnt = 0;
+	for (int ni = lo_i; ni < hi_i; ni++) {
+		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
+		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		for (uint32_t kj = a.cell_start[c0]; kj < a.cell_start[c1]; kj++) {
+			const Rec64 rj = load_rec(rec + kj);
+			double xij = __dsub_rn(ri.x, rj.x);
+			double yij = __dsub_rn(ri.y, rj.y);
+			double r2 = __dadd_rn(__dmul_rn(xij, xij), __dmul_rn(yij, yij));
+			if (r2 <= lim) {
+				if (pass == 1) idx[offs[i] + cnt] = a.perm[kj];
+				cnt++;
+			}
+		}
+	}
+	if (pass == 0) counts[i] = cnt;
+}
+
+inline unsigned grid1(uint32_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+cudaError_t build_grid(const ULArgs& a, bool mixed, cudaStream_t s) {
+	DevStatus* st = reinterpret_cast<DevStatus*>(a.status);
+	k_bbox_init<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, a.bbox);
+	const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
+	k_bbox<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.h, sv.vx, sv.vy, a.body_of, a.params,
+	                                              mixed ? 1 : 0, a.bbox);
+	k_geom<<<1, 1024, 0, s>>>(a.n_bodies, a.bbox, a.params, mixed ? 1 : 0, a.geom, a.total_cells, a.n_total + 1, st);
+	k_hash<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.body_of, a.geom, a.total_cells, a.keys,
+	                                              a.perm_in, st);
+	size_t tmp = a.sort_tmp_bytes;
+	cudaError_t e = cub::DeviceRadixSort::SortPairs(a.sort_tmp, tmp, a.keys, a.keys_sorted, a.perm_in, a.perm,
+	                                                (int)a.n_total, 0, a.sort_bits, s);
+	if (e != cudaSuccess) return e;
+	k_cells<<<grid1(a.n_total + 1, 256), 256, 0, s>>>(a.n_total, a.keys_sorted, a.total_cells, a.cell_start);
+	return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t ul_sort_tmp_bytes(uint32_t n, int bits) {
+	size_t bytes = 0;
+	cub::DeviceRadixSort::SortPairs(nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+	                                (uint32_t*)nullptr, (int)n, 0, bits);
+	return bytes;
+}
+
+size_t ul_rec_bytes(bool mixed) { return mixed ? sizeof(Rec32) : sizeof(Rec64); }
+
+cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
+	if (a.n_total == 0) return cudaSuccess;
+	DevStatus* st = reinterpret_cast<DevStatus*>(a.status);
+	if (a.strict_grid || a.stage == 0) {
+		cudaError_t e = build_grid(a, mixed, s);
+		if (e != cudaSuccess) return e;
+	}
+	if (mixed) {
+		k_gather32<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
+	} else {
+		k_gather64<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
+	}
+	if (a.ev_pair0) cudaEventRecord(a.ev_pair0, s);
+	if (mixed) {
+		k_pair32<<<grid1(a.n_total, 128), 128, 0, s>>>(a, a.params, a.geom, st);
+	} else {
+		k_pair64<<<grid1(a.n_total, 128), 128, 0, s>>>(a, a.params, a.geom, st);
+	}
+	if (a.ev_pair1) cudaEventRecord(a.ev_pair1, s);
+	return cudaGetLastError();
+}
+
+cudaError_t ul_neighbors(const ULArgs& a, uint32_t* counts, uint32_t* idx, const uint64_t* offs, int pass,
+                         cudaStream_t s) {
+	if (a.n_total == 0) return cudaSuccess;
+	if (pass == 0) {
+		cudaError_t e = build_grid(a, false, s);
+		if (e != cudaSuccess) return e;
+		k_gather64<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
+	}
+	k_neighbors<<<grid1(a.n_total, 128), 128, 0, s>>>(a, a.geom, counts, idx, offs, pass);
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS

@@ -133,15 +133,19 @@ def _body_from_lists(xs, ys, X=None, Y=None) -> Dict[str, np.ndarray]:
 
 def _ring_lattice(nbox: int, dx: float, ro: float, ri: float):
     """Lattice points of one annulus, in the reference's loop order (rings.cpp:40-56)."""
-    pts = []
-    for i in range(nbox):
-        for j in range(nbox):
-            px = -ro + i * dx
-            py = -ro + j * dx
-            dist = math.sqrt(px * px + py * py)
-            if dist < ro and dist >= ri:
-                pts.append((px, py))
-    return pts
+    px, py = _ring_lattice_np(nbox, dx, ro, ri)
+    return list(zip(px.tolist(), py.tolist()))
+
+
+def _ring_lattice_np(nbox: int, dx: float, ro: float, ri: float):
+    """Vectorised :func:`_ring_lattice`: the same IEEE operations elementwise
+    (px = -ro + i*dx, dist = sqrt(px*px + py*py)), i-major order."""
+    i = np.arange(nbox, dtype=np.float64)
+    p = -ro + i * dx
+    PX, PY = np.meshgrid(p, p, indexing="ij")
+    dist = np.sqrt(PX * PX + PY * PY)
+    mask = (dist < ro) & (dist >= ri)
+    return PX[mask], PY[mask]
 
 
 def convex_hull(x: np.ndarray, y: np.ndarray) -> np.ndarray:
@@ -219,22 +223,26 @@ def rings(
         a["quad_weight"][:] = a["m"] / a["rho"]
         a["vx"][:] = vx
 
+    px, py = _ring_lattice_np(nbox, dx, ro, ri)
+    # hull candidates: only lattice points within 3 dx of the outer circle can be hull
+    # vertices or lie on hull edges, and the monotone chain visits any subset in the
+    # same relative order, so the hull of the subset is the hull of the ring
+    cand = np.nonzero(np.sqrt(px * px + py * py) >= ro - 3 * dx)[0]
     if not two_bodies:
-        xs, ys = [], []
-        for px, py in pts:
-            xs += [px - spacing, px + spacing]
-            ys += [py, py]
+        xs = np.stack([px - spacing, px + spacing], axis=1).ravel()
+        ys = np.stack([py, py], axis=1).ravel()
         a = _body_from_lists(xs, ys, xs if tl else None, ys if tl else None)
         vx = np.where(a["x"] < 0.0, speed, -speed)
         finish(a, vx)
         sc.bodies = [Body(a)]
     else:
         for sgn, v in ((-1.0, speed), (1.0, -speed)):
-            xs = [px + sgn * spacing for px, _ in pts]
-            ys = [py for _, py in pts]
+            xs = px + sgn * spacing
+            ys = py.copy()
             a = _body_from_lists(xs, ys, xs if tl else None, ys if tl else None)
             finish(a, v)
-            sc.bodies.append(Body(a, hull=convex_hull(a["x"], a["y"])))
+            hull = cand[convex_hull(xs[cand], ys[cand])].astype(np.uint32)
+            sc.bodies.append(Body(a, hull=hull))
         sc.contact = 1
 
     if method == METHOD_UL:
@@ -321,19 +329,11 @@ def tensile_plate(
     tensile_tl_weak (:731-826) lattices (px = i*dx, py = j*dx; column i = 0 and
     i = nx-1 carry the pull), generalised to nx != ny and optional seeded jitter."""
     dx = Lx / (nx - 1)
-    xs, ys, left, right = [], [], [], []
-    k = 0
-    for i in range(nx):
-        for j in range(ny):
-            xs.append(i * dx)
-            ys.append(j * dx)
-            if i == 0:
-                left.append(k)
-            if i == nx - 1:
-                right.append(k)
-            k += 1
-    xs = np.array(xs)
-    ys = np.array(ys)
+    I, J = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64), indexing="ij")
+    xs = (I * dx).ravel()
+    ys = (J * dx).ravel()
+    left = np.arange(ny, dtype=np.uint32)
+    right = (np.uint32(nx - 1) * np.uint32(ny) + np.arange(ny, dtype=np.uint32)).astype(np.uint32)
     if jitter > 0.0:
         rng = np.random.default_rng(seed)
         xs = xs + rng.uniform(-jitter, jitter, xs.shape) * dx
@@ -343,8 +343,7 @@ def tensile_plate(
     a["h"][:] = hdx * dx
     a["m"][:] = dx * dx * rho0
     a["quad_weight"][:] = a["m"] / a["rho"]
-    body = Body(a, bcs=[BC(BC_PULL_TL, -pull, np.array(left, np.uint32)),
-                        BC(BC_PULL_TL, pull, np.array(right, np.uint32))])
+    body = Body(a, bcs=[BC(BC_PULL_TL, -pull, left), BC(BC_PULL_TL, pull, right)])
     sc = Scenario(method=method, bodies=[body], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
     sc.dt = dt if dt is not None else cfl * (hdx * dx) / sc.c0
     sc.nbh_h = hdx * dx

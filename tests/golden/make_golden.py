@@ -1,0 +1,55 @@
+"""Generates the golden fixtures of this directory from the reference itself.
+
+Runs the reference's own scenario builders and step loop -- compiled out of tree
+from its unmodified sources by oracle/build_ref.sh -- and stores, per case, the
+initial state it built (NAME.case) and the state it reached (NAME.ref.out).  Also
+runs workload-constant cases built by mfree_iwf_gb300.scenarios through the
+reference's body/action machinery.  Needs the reference sources (not on GPU machines).
+
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from mfree_iwf_gb300 import scenarios as S  # noqa: E402
+
+# (reference scenario function, nbox, steps): small enough to keep every file tiny,
+# long enough that the ring contacts engage (rings_*_contact) and the pulls act.
+REFERENCE_CASES = [
+    ("rings_monaghan", 20, 12),
+    ("rings_monaghan_contact", 20, 30),
+    ("rings_tl_contact", 20, 375),
+    ("tensile_tl", 11, 25),
+    ("tensile_tl_weak", 7, 6),
+]
+
+
+def main():
+    ref = oracle.build_ref(force=True)
+    if ref is None:
+        raise SystemExit("reference sources not present")
+    for name, nbox, steps in REFERENCE_CASES:
+        case = os.path.join(HERE, f"{name}.case")
+        out = os.path.join(HERE, f"{name}.ref.out")
+        subprocess.run([ref, "scenario", name, str(nbox), str(steps), case, out], check=True)
+        print("wrote", case, out)
+    # workload constants (rho 1200, +-10 m/s, h = 1.3 dx, CFL dt) at dx = 4 mm
+    sc = S.c1_rings(dx=4e-3, nbh_eps=1e-6)  # the reference predicate has a fixed 1e-6
+    case = os.path.join(HERE, "c1_rings_dx4mm.case")
+    S.write_case(case, sc, 30)
+    subprocess.run([ref, "run", case, os.path.join(HERE, "c1_rings_dx4mm.ref.out")], check=True)
+    sc = S.c2_rings_tl(dx=4e-3, nbh_eps=1e-6)
+    case = os.path.join(HERE, "c2_rings_tl_dx4mm.case")
+    S.write_case(case, sc, 30)
+    subprocess.run([ref, "run", case, os.path.join(HERE, "c2_rings_tl_dx4mm.ref.out")], check=True)
+    print("done")
+
+
+if __name__ == "__main__":
+    main()

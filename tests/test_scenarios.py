@@ -1,0 +1,55 @@
+"""Scenario builders reproduce the reference's set-up bit for bit (golden initial
+states written by the reference's own scenario functions)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from mfree_iwf_gb300 import scenarios as S
+
+BUILDERS = {
+    "rings_monaghan": lambda: S.rings_monaghan(20),
+    "rings_monaghan_contact": lambda: S.rings_monaghan_contact(20),
+    "rings_tl_contact": lambda: S.rings_tl_contact(20),
+    "tensile_tl": lambda: S.tensile_tl(11),
+    "tensile_tl_weak": lambda: S.tensile_tl_weak(7),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BUILDERS))
+def test_builder_matches_reference_setup(name):
+    ref = S.read_case(os.path.join(GOLDEN, f"{name}.case"))
+    sc = BUILDERS[name]()
+    assert sc.method == ref.method and list(sc.actions) == list(ref.actions)
+    for f in ("dt", "nu", "E", "rho0", "wdeltap", "corr_exp", "mghn_eps", "alpha", "beta", "eta", "xsph_eps",
+              "do_smooth", "nbh_h", "nbh_eps", "gp_h", "gp_rho", "contact"):
+        assert getattr(sc, f) == getattr(ref, f), f
+    assert len(sc.bodies) == len(ref.bodies)
+    for b, rb in zip(sc.bodies, ref.bodies):
+        for k in S.IN_NAMES:
+            assert np.array_equal(b.arrays[k].view(np.uint64), rb.arrays[k].view(np.uint64)), k
+        assert np.array_equal(b.hull, rb.hull)
+        assert len(b.bcs) == len(rb.bcs)
+        for bc, rbc in zip(b.bcs, rb.bcs):
+            assert bc.v == rbc.v and np.array_equal(bc.idx, rbc.idx)
+
+
+def test_workload_sizes():
+    # the two ring workloads and the plate: ~4.4k, ~1.76M and ~5.0M particles
+    assert 4300 < S.c1_rings(dx=1e-3).n_total < 4500
+    assert S.c3_plate.__doc__
+    n2 = 2 * len(S._ring_lattice_np(1601, 0.08 / 1600, 0.04, 0.03)[0])
+    assert 1.74e6 < n2 < 1.78e6
+
+
+def test_case_roundtrip(tmp_path):
+    sc = S.c1_rings(dx=4e-3, two_bodies=True)
+    p = str(tmp_path / "c.case")
+    S.write_case(p, sc, 7, 2)
+    back = S.read_case(p)
+    assert back.method == sc.method and back.contact == 1
+    for b, rb in zip(sc.bodies, back.bodies):
+        for k in S.IN_NAMES:
+            assert np.array_equal(b.arrays[k], rb.arrays[k])
+        assert np.array_equal(b.hull, rb.hull)
