@@ -48,6 +48,6 @@ def test_oracle_reports_neighbour_overflow(oracle_bin, tmp_path):
     """A neighbour list reaching MAX_NBH = 200 is the reference's assert (grid.h:167)."""
     import oracle
     sc = S.rings_monaghan(40)
-    sc.nbh_eps = 1e-3  # radius ~3 cm: every particle sees hundreds of others
+    sc.bodies[0].arrays["h"] *= 3.0  # h = 5.1 dx: ~300 particles inside 2h
     res = oracle.run(sc, 1)
     assert not res.ok
