@@ -48,6 +48,6 @@ def test_oracle_reports_neighbour_overflow(oracle_bin, tmp_path):
     """A neighbour list reaching MAX_NBH = 200 is the reference's assert (grid.h:167)."""
     import oracle
     sc = S.rings_monaghan(40)
-    sc.bodies[0].arrays["h"] *= 3.0  # h = 5.1 dx: ~300 particles inside 2h
+    sc.bodies[0].arrays["h"] *= 6.0  # h = 10 dx: several hundred particles inside 2h
     res = oracle.run(sc, 1)
     assert not res.ok
