@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit meshless time step on GB300.
+
+Workload (default): two elastic rings (r_in 0.03 m, r_out 0.04 m, centres 0.09 m
+apart) on a dx = 0.05 mm lattice, ~1.76M particles, total-Lagrangian SPH with the
+Randles-Libersky correction and penalty contact (the rings_tl_contact structure),
+E 1e7 Pa, nu 0.4, rho 1200 kg/m^3, +-10 m/s, h = 1.3 dx, dt = 0.3 h / c0, mixed
+precision (FP32 pair sums, FP64 position/velocity RK4 state and 2x2 inversions).
+Synthetic, seeded data of the workload's shapes (there is no external dataset).
+
+Metric: particle-steps/s = particles x RK4 steps / time, the whole step included
+(4 stages, contact, boundary update).  One JSON line on rank 0.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c2|c1|c4] [--precision mixed|fp64|fp64_strict]
+
+With --impl reference it times the CPU implementation of the same path (the oracle
+restatement of the reference, which is single-threaded) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s on 1 GB300: plain FP64 vs mixed/batched at <=1e-4 rel err"
+UNIT = "particle-steps/s"
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload(name: str, dx: float | None):
+    from mfree_iwf_gb300 import scenarios as S
+    if name == "c2":
+        dx = dx or 5e-5
+        return S.c2_rings_tl(dx=dx), {"workload": f"ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx={dx*1e3:g} mm"}
+    if name == "c1":
+        dx = dx or 1e-3
+        return S.c1_rings(dx=dx), {"workload": f"ring impact, Gray-Monaghan SPH, dx={dx*1e3:g} mm"}
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_sample(workload_name: str, steps: int, warmup: int, procs: int):
+    """The oracle (CPU restatement of the reference, single-threaded) on a bounded
+    sample of the workload: the same set-up at a coarser lattice.  `procs` copies run
+    concurrently (one per host core); returns particle-steps/s over all of them."""
+    import oracle
+    from mfree_iwf_gb300 import scenarios as S
+    binary = oracle.build_oracle()
+    if workload_name == "c2":
+        sc = S.c2_rings_tl(dx=4e-4)
+        desc = "same ring-impact TL set-up at dx=0.4 mm"
+    else:
+        sc = S.c1_rings(dx=1e-3)
+        desc = "the ring workload at dx=1 mm"
+    n = sc.n_total
+    with tempfile.TemporaryDirectory() as d:
+        case = os.path.join(d, "c.case")
+        S.write_case(case, sc, warmup + steps)
+        t0 = time.time()
+        ps = [subprocess.Popen([binary, case, os.path.join(d, f"o{k}.out"), str(warmup)],
+                               stdout=subprocess.DEVNULL, stderr=subprocess.PIPE) for k in range(procs)]
+        rcs = [p.wait() for p in ps]
+        wall = time.time() - t0
+        secs = []
+        for k in range(procs):
+            r = S.read_result(os.path.join(d, f"o{k}.out"))
+            secs.append(r.seconds)
+    if any(rcs):
+        raise RuntimeError("oracle failed")
+    span = max(secs)
+    value = procs * n * steps / span
+    return value, {"cores": procs, "sample": f"{desc}: {n} particles, {steps} timed steps after {warmup}, "
+                                             f"{procs} concurrent single-threaded runs ({wall:.1f} s wall)",
+                   "n": n}
+
+
+def reference_arm(args, cfg_desc):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    value, info = cpu_sample(args.workload, args.steps, args.warmup, procs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * info["n"] * procs / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": cfg_desc,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                         "sample": info["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ ours
+# Algorithmic bytes per row and launch of the timed kernels (unique data each must
+# move once; neighbour rows are assumed served on chip).  Mixed TL form:
+#   pass A: list offset 4, per pair index 4 + gradient 8, own packed u 16, rho/S 16,
+#           quad weight 4; writes P 16, rate terms 16, c 4
+#   pass B: offset 4, per pair 12, packed x, v 32, h 4, m 4, rho 4, c 4, P 16, rate 16,
+#           fc 16, m 8, the FP64 x/y/vx/vy base+acc+next (3 x 32 read/write -> 80)
+#           and float rho/S base+acc+next (3 x 16 -> 40)
+def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool) -> float:
+    if tl and mixed:
+        if kind == 1:
+            return 4 + 12 * nnz_per_row + 16 + 16 + 4 + 16 + 16 + 4
+        return 4 + 12 * nnz_per_row + 32 + 16 + 16 + 16 + 16 + 8 + 80 + 40
+    if tl:
+        if kind == 1:
+            return 4 + 20 * nnz_per_row + 32 + 32 + 32 + 32 + 8
+        return 4 + 20 * nnz_per_row + 32 + 32 + 8 + 8 + 8 + 8 + 32 + 32 + 16 + 128 + 64
+    if kind == 0:  # UL gather + pair: record write/read, perm/key/body, fc, state
+        rec = 80 if mixed else 128
+        return 2 * rec + 12 + 16 + (48 + 3 * 48 if mixed else 64 * 4)
+    return 0.0
+
+
+def ours(args, cfg_desc):
+    import torch
+    import mfree_iwf_gb300 as M
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    sc, cfg = workload(args.workload, args.dx)
+    n = sc.n_total
+    tl = sc.method == M.METHOD_TL
+    sim = M.from_scenario(sc, precision=args.precision, device=local)
+    mixed = args.precision == "mixed"
+    sim.step(args.warmup)  # includes the set-up (neighbour search, corrections)
+    sim.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream())
+    nnz = 0.0
+    if tl:
+        nnz = float(np.mean(sim.neighbor_counts(0)))
+
+    # ---- device-resident timed region
+    sim.set_timing(True)
+    l0 = sim.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        sim.synchronize()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sim.launch_count() - l0
+    clocks = clk.summary()
+    kstats = {k: sim.kernel_stats(k) for k in range(6)}
+    sim.set_timing(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers: per step the state goes
+    # host -> device (pinned), one step runs, the state comes back device -> host
+    fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy")
+    host = []
+    for b in range(len(sc.bodies)):
+        st = sim.get_state(b, fields)
+        pinned = {f: torch.from_numpy(st[f]).pin_memory().numpy() for f in fields}
+        host.append(pinned)
+    k2 = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k2):
+        for b in range(len(sc.bodies)):
+            sim.set_state(b, host[b])
+        sim.step(1)
+        for b in range(len(sc.bodies)):
+            out = sim.get_state(b, fields)
+            for f in fields:
+                host[b][f][...] = out[f]
+    wall = time.perf_counter() - t0
+    e2e_value = world * n * k2 / wall
+    bytes_io = 8 * len(fields) * n
+
+    # ---- roofline of the dominant kernel
+    peaks, peak_kind = measured_peaks()
+    dom = max(kstats, key=lambda k: kstats[k][0])
+    kms, klaunch, krows = kstats[dom]
+    names = {0: "UL stage (gather + pair + RK)", 1: "TL pass A", 2: "TL pass B", 3: "contact", 4: "grid", 5: "weak"}
+    roof = None
+    if klaunch:
+        per_launch_rows = krows / klaunch
+        abytes = algorithmic_bytes(dom, mixed, nnz, tl) * per_launch_rows
+        achieved = abytes / (kms / klaunch / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,
+                "launches": klaunch, "avg_launch_ms": kms / klaunch,
+                "algorithmic_bytes_per_launch": abytes}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cv, info = cpu_sample(args.workload, args.cpu_steps, 1, 1)
+            cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": info["sample"]}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": {"mixed": "f32+f64", "fp64": "f64", "fp64_strict": "f64"}[args.precision],
+            "data": "synthetic",
+            "config": dict(cfg, particles=n, precision=args.precision, parallelism=f"replicas x{world}",
+                           l2="inputs larger than L2 (state + neighbour lists of %d particles)" % n),
+            "clocks": clocks, "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
+                    "steps": k2},
+            "roofline": roof, "cpu_baseline": cpu,
+            "kernels_ms": {names[k]: v[0] for k, v in kstats.items() if v[1]},
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
+    ap.add_argument("--dx", type=float, default=None)
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    _, cfg = workload(args.workload, args.dx) if args.impl == "ours" and False else (None, None)
+    cfg_desc = {"workload": {"c2": "ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx=0.05 mm",
+                             "c1": "ring impact, Gray-Monaghan SPH, dx=1 mm"}[args.workload]}
+    if args.impl == "reference":
+        reference_arm(args, cfg_desc)
+        return
+    from __graft_entry__ import build
+    build()
+    ours(args, cfg_desc)
+
+
+if __name__ == "__main__":
+    main()

@@ -247,6 +247,14 @@ class Simulation:
         self._check(self._lib.mf_get_time(self._h, body, ctypes.byref(t)), "mf_get_time")
         return t.value
 
+    def neighbor_counts(self, body: int) -> np.ndarray:
+        n = self.num_particles(body)
+        counts = np.zeros(n, np.uint32)
+        tot = ctypes.c_uint64()
+        self._check(self._lib.mf_get_neighbors(self._h, body, counts.ctypes.data_as(_UP), None, 0, ctypes.byref(tot)),
+                    "mf_get_neighbors")
+        return counts
+
     def neighbors(self, body: int) -> List[np.ndarray]:
         n = self.num_particles(body)
         counts = np.zeros(n, np.uint32)

@@ -241,6 +241,7 @@ void timing_collect(mf_ctx* c) {
 }
 
 mf_status check_status(mf_ctx* c) {
+	CK(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatusH), cudaMemcpyDeviceToHost, c->stream));
 	CK(cudaStreamSynchronize(c->stream));
 	if (c->timing.on) timing_collect(c);
 	DevStatusH s = *c->h_status;
@@ -935,6 +936,7 @@ MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uin
 	CK(d_offs.alloc(n + 1));
 	std::vector<uint32_t> all_idx;
 	if (c->cfg.method == MF_METHOD_UL) {
+		if (c->mixed) return fail(c, MF_ERR_STATE, "UL neighbour lists are available in the FP64 forms");
 		ULArgs a = ul_args(c, 0);
 		cudaError_t e = mf_strict::ul_neighbors(a, d_counts.p, nullptr, nullptr, 0, c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "ul_neighbors");

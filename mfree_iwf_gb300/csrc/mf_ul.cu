@@ -433,6 +433,7 @@ __global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __re
 	uint32_t flags = a.flags;
 	int lo_i, hi_i, lo_j, hi_j;
 	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+	const uint32_t tot = *a.total_cells;
 
 	double hi = ri.h;
 	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(hi, hi), 2.), 2.);
@@ -447,8 +448,8 @@ __global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __re
 	double av_x = 0., av_y = 0., xs_x = 0., xs_y = 0.;
 	uint32_t cnt = 0;
 	for (int ni = lo_i; ni < hi_i; ni++) {
-		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
-		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
+		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
 		for (uint32_t kj = j0; kj < j1; kj++) {
 			const Rec64 rj = load_rec(rec + kj);
@@ -515,13 +516,9 @@ __global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __re
 	if (flags & A_ART_VISC) { d[2] = av_x; d[3] = av_y; }
 	if (flags & A_XSPH) { d[0] = xs_x; d[1] = xs_y; }
 	if (flags & A_JAUMANN) {
-		double Sxx = ri.sxx, Syy = ri.syy;
-		// the Jaumann rate uses the stored deviatoric-plus-pressure S (without p)
-		double p = 0.;
-		if (flags & A_EOS) p = pr.c0sq * (rhoi - pr.rho0);
-		Sxx = Sxx + p;
-		Syy = Syy + p;
-		jaumann<double>(vx_x, vx_y, vy_x, vy_y, Sxx, ri.sxy, Syy, pr.G, d[5], d[6], d[7]);
+		// the Jaumann rate uses the stage stress itself (not S - p)
+		const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
+		jaumann<double>(vx_x, vx_y, vy_x, vy_y, sv.Sxx[i], sv.Sxy[i], sv.Syy[i], pr.G, d[5], d[6], d[7]);
 	}
 	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
 	if (flags & A_MOMENTUM_UL) {
@@ -549,6 +546,7 @@ __global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __re
 	uint32_t flags = a.flags;
 	int lo_i, hi_i, lo_j, hi_j;
 	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+	const uint32_t tot = *a.total_cells;
 
 	float hi = ri.h;
 	float h1 = 1.f / hi;
@@ -564,8 +562,8 @@ __global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __re
 	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
 	float av_x = 0.f, av_y = 0.f, xs_x = 0.f, xs_y = 0.f;
 	for (int ni = lo_i; ni < hi_i; ni++) {
-		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
-		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
+		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
 		for (uint32_t kj = j0; kj < j1; kj++) {
 			const Rec32 rj = load_rec(rec + kj);
@@ -629,9 +627,8 @@ __global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __re
 	if (flags & A_XSPH) { d[0] = xs_x; d[1] = xs_y; }
 	float vxi = ri.vx.hi + ri.vx.lo, vyi = ri.vy.hi + ri.vy.lo;
 	if (flags & A_JAUMANN) {
-		float p = 0.f;
-		if (flags & A_EOS) p = (float)pr.c0sq * (rhoi - (float)pr.rho0);
-		jaumann<float>(vx_x, vx_y, vy_x, vy_y, ri.sxx + p, ri.sxy, ri.syy + p, (float)pr.G, d[5], d[6], d[7]);
+		const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
+		jaumann<float>(vx_x, vx_y, vy_x, vy_y, sv.Sxx_f[i], sv.Sxy_f[i], sv.Syy_f[i], (float)pr.G, d[5], d[6], d[7]);
 	}
 	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
 	if (flags & A_MOMENTUM_UL) {
@@ -691,13 +688,14 @@ __global__ void k_neighbors(ULArgs a, const Geom* __restrict__ G, uint32_t* coun
 	uint32_t i = a.perm[k];
 	int lo_i, hi_i, lo_j, hi_j;
 	stencil(g, a.keys_sorted[k], lo_i, hi_i, lo_j, hi_j);
+	const uint32_t tot = *a.total_cells;
 	double hi = ri.h;
 	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(hi, hi), 2.), 2.);
 	double lim = __dadd_rn(radius2, a.nbh_eps);
 	uint32_t cnt = 0;
 	for (int ni = lo_i; ni < hi_i; ni++) {
-		uint32_t c0 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j;
-		uint32_t c1 = g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j;
+		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
+		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		for (uint32_t kj = a.cell_start[c0]; kj < a.cell_start[c1]; kj++) {
 			const Rec64 rj = load_rec(rec + kj);
 			double xij = __dsub_rn(ri.x, rj.x);

@@ -14,12 +14,13 @@
 // oracle/glm_subset, the same header the compiled reference uses.  Built with
 // -ffp-contract=off so that x86-64 and aarch64 hosts round identically.
 //
-// Usage: mfo_run CASE_FILE RESULT_FILE
+// Usage: mfo_run CASE_FILE RESULT_FILE [WARMUP_STEPS]
 #include <algorithm>
 #include <cfloat>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1195,10 +1196,11 @@ int main(int argc, char** argv) {
 			}
 		};
 		double secs = 0.;
+		unsigned warm = argc > 3 ? (unsigned)atoi(argv[3]) : 0u;  // steps excluded from the timing
 		for (unsigned s = 1; s <= sim.c.nsteps; s++) {
 			auto t0 = std::chrono::steady_clock::now();
 			sim.driver_step();
-			secs += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+			if (s > warm) secs += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 			if ((sim.c.dump_every && s % sim.c.dump_every == 0) || s == sim.c.nsteps) dump(s);
 		}
 		if (sim.c.nsteps == 0) dump(0);
