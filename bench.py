@@ -248,7 +248,7 @@ def ours(args, cfg_desc):
         st = sim.get_state(b, fields)
         pinned = {f: torch.from_numpy(st[f]).pin_memory().numpy() for f in fields}
         host.append(pinned)
-    k2 = max(3, min(args.steps, 20))
+    k2 = max(3, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(k2):
@@ -256,9 +256,7 @@ def ours(args, cfg_desc):
             sim.set_state(b, host[b])
         sim.step(1)
         for b in range(len(sc.bodies)):
-            out = sim.get_state(b, fields)
-            for f in fields:
-                host[b][f][...] = out[f]
+            sim.get_state_into(b, host[b])
     wall = time.perf_counter() - t0
     e2e_value = world * n * k2 / wall
     bytes_io = 8 * len(fields) * n
@@ -315,6 +313,7 @@ def main():
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -237,6 +237,11 @@ class Simulation:
         self._check(self._lib.mf_get_state(self._h, body, ctypes.byref(s)), "mf_get_state")
         return out
 
+    def get_state_into(self, body: int, out: Dict[str, np.ndarray]) -> None:
+        """Device -> caller-owned arrays (contiguous float64, e.g. pinned host memory)."""
+        s = MfState(*[_dptr(out.get(f)) for f in _SFIELDS])
+        self._check(self._lib.mf_get_state(self._h, body, ctypes.byref(s)), "mf_get_state")
+
     def set_state(self, body: int, arrays: Dict[str, np.ndarray]) -> None:
         cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
         p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])

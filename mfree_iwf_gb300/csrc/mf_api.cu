@@ -20,6 +20,15 @@ namespace {
 
 const uint32_t REF_MAX_NBH = 200;  // particle.h:31
 
+__global__ void k_f64_to_f32(uint32_t n, const double* __restrict__ a, float* __restrict__ b) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (float)a[i];
+}
+__global__ void k_f32_to_f64(uint32_t n, const float* __restrict__ a, double* __restrict__ b) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (double)a[i];
+}
+
 struct HostBC {
 	int32_t kind;
 	double v;
@@ -98,6 +107,9 @@ struct mf_ctx {
 	DevBuf<float> wx32, wy32, P32, dA32, c32, qw32, m32, h32;
 	DevBuf<unsigned char> pack;
 	uint32_t n_bc = 0;
+
+	// host <-> device state transfers: FP64 staging for the fields stored as FP32
+	DevBuf<double> staging;
 
 	// contact
 	bool contact_on = false;
@@ -251,11 +263,12 @@ mf_status check_status(mf_ctx* c) {
 	c->h_status->first_index = 0xffffffffu;
 	CK(cudaMemcpyAsync(c->d_status, c->h_status, sizeof(DevStatusH), cudaMemcpyHostToDevice, c->stream));
 	CK(cudaStreamSynchronize(c->stream));
-	if (s.flags & 1u) return fail(c, MF_ERR_NBH_OVERFLOW, "neighbour capacity reached at row %u", s.first_index);
-	if (s.flags & 2u) return fail(c, MF_ERR_NO_NEIGHBOR, "particle without neighbours at row %u", s.first_index);
-	if (s.flags & 4u) return fail(c, MF_ERR_GRID, "cell grid invalid (num_cell >= n or particle outside) near row %u", s.first_index);
+	// the root cause first: a non-finite state also breaks the grid and the neighbour search
 	if (s.flags & 8u) return fail(c, MF_ERR_NONFINITE, "non-finite state at row %u", s.first_index);
 	if (s.flags & 16u) return fail(c, MF_ERR_SINGULAR, "singular corrector matrix at row %u", s.first_index);
+	if (s.flags & 4u) return fail(c, MF_ERR_GRID, "cell grid invalid (num_cell >= n or particle outside) near row %u", s.first_index);
+	if (s.flags & 1u) return fail(c, MF_ERR_NBH_OVERFLOW, "neighbour capacity reached at row %u", s.first_index);
+	if (s.flags & 2u) return fail(c, MF_ERR_NO_NEIGHBOR, "particle without neighbours at row %u", s.first_index);
 	if (s.flags & 32u) return fail(c, MF_ERR_TIMEOUT, "bounded device wait gave up");
 	return fail(c, MF_ERR_CUDA, "device status 0x%x", s.flags);
 }
@@ -678,7 +691,7 @@ mf_ctx::~mf_ctx() {
 	for (auto* p : f64s) p->free();
 	DevBuf<float>* f32s[] = {&wx32, &wy32, &P32, &dA32, &c32, &qw32, &m32, &h32};
 	for (auto* p : f32s) p->free();
-	pack.free(); bnd.free(); tile_bb.free();
+	pack.free(); bnd.free(); tile_bb.free(); staging.free();
 	for (auto e : timing.pool) cudaEventDestroy(e);
 	if (d_status) cudaFree(d_status);
 	if (h_status) cudaFreeHost(h_status);
@@ -865,20 +878,22 @@ MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
 			if (o[q]) std::fill(o[q], o[q] + b.n, 0.);
 		return MF_OK;
 	}
-	CK(cudaStreamSynchronize(c->stream));
+	CK(cudaSetDevice(c->cfg.device));
 	double* o[8] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy};
+	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)c->n_total));
 	for (int q = 0; q < 8; q++) {
 		if (!o[q]) continue;
 		if (c->mixed && q >= 4) {
-			std::vector<float> tmp(b.n);
-			CK(cudaMemcpy(tmp.data(), c->sf[0][q - 4].p + b.off, b.n * 4, cudaMemcpyDeviceToHost));
-			for (uint32_t i = 0; i < b.n; i++) o[q][i] = tmp[i];
+			double* st = c->staging.p + (size_t)(q - 4) * c->n_total;
+			k_f32_to_f64<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, c->sf[0][q - 4].p + b.off, st);
+			CK(cudaMemcpyAsync(o[q], st, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
 		} else {
-			CK(cudaMemcpy(o[q], c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
+			CK(cudaMemcpyAsync(o[q], c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
 		}
 	}
-	if (out->fcx) CK(cudaMemcpy(out->fcx, c->fcx.p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
-	if (out->fcy) CK(cudaMemcpy(out->fcy, c->fcy.p + b.off, b.n * 8, cudaMemcpyDeviceToHost));
+	if (out->fcx) CK(cudaMemcpyAsync(out->fcx, c->fcx.p + b.off, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
+	if (out->fcy) CK(cudaMemcpyAsync(out->fcy, c->fcy.p + b.off, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
 }
 
@@ -893,16 +908,24 @@ MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 			if (src[q]) b.in[fld[q]].assign(src[q], src[q] + b.n);
 		return MF_OK;
 	}
-	CK(cudaStreamSynchronize(c->stream));
+	CK(cudaSetDevice(c->cfg.device));
+	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)c->n_total));
+	// TL stage 0 starts from its own copy of the particles (set 2), kept in step
+	bool tl = c->cfg.method != MF_METHOD_UL;
 	for (int q = 0; q < 8; q++) {
 		if (!src[q]) continue;
 		if (c->mixed && q >= 4) {
-			std::vector<float> tmp(src[q], src[q] + b.n);
-			CK(cudaMemcpy(c->sf[0][q - 4].p + b.off, tmp.data(), b.n * 4, cudaMemcpyHostToDevice));
+			double* st = c->staging.p + (size_t)(q - 4) * c->n_total;
+			CK(cudaMemcpyAsync(st, src[q], b.n * 8, cudaMemcpyHostToDevice, c->stream));
+			k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[0][q - 4].p + b.off);
+			if (tl) k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[2][q - 4].p + b.off);
 		} else {
-			CK(cudaMemcpy(c->sd[0][q].p + b.off, src[q], b.n * 8, cudaMemcpyHostToDevice));
+			CK(cudaMemcpyAsync(c->sd[0][q].p + b.off, src[q], b.n * 8, cudaMemcpyHostToDevice, c->stream));
+			if (tl) CK(cudaMemcpyAsync(c->sd[2][q].p + b.off, c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToDevice, c->stream));
 		}
 	}
+	CK(cudaGetLastError());
+	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
 }
 

@@ -19,6 +19,16 @@ from mfree_iwf_gb300 import scenarios as S
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
+# fields compared as vectors/tensors: a component that is zero by symmetry (vy of a
+# head-on impact) carries only round-off, so its own relative error means nothing
+GROUPS = {"position": ("x", "y"), "velocity": ("vx", "vy"), "density": ("rho",),
+          "stress": ("Sxx", "Sxy", "Syy"), "contact force": ("fcx", "fcy")}
+
+
+def group_rel(g, r, fields):
+    a = np.concatenate([g[f] for f in fields])
+    b = np.concatenate([r[f] for f in fields])
+    return rel_l2(a, b)
 
 
 def rel_l2(a, b):
@@ -53,12 +63,10 @@ def test_fp64_strict_matches_reference(name, lib):
     got = run_gpu(sc, steps, "fp64_strict")
     worst = 0.0
     for g, r in zip(got, ref.dumps[-1]["bodies"]):
-        for f in FIELDS:
-            if np.linalg.norm(r[f]) == 0 and np.linalg.norm(g[f]) == 0:
-                continue
-            e = rel_l2(g[f], r[f])
+        for gname, fields in GROUPS.items():
+            e = group_rel(g, r, fields)
             worst = max(worst, e)
-            assert e < 1e-9, (name, f, e)
+            assert e < 1e-9, (name, gname, e)
     print(f"{name}: worst relative L2 {worst:.3e} after {steps} steps")
 
 
@@ -105,8 +113,8 @@ def test_fp64_fast_close_to_reference(name, lib):
     steps = ref.dumps[-1]["step"]
     got = run_gpu(sc, steps, "fp64")
     for g, r in zip(got, ref.dumps[-1]["bodies"]):
-        for f in ("x", "y", "vx", "vy", "rho"):
-            assert rel_l2(g[f], r[f]) < 1e-8, (name, f)
+        for gname in ("position", "velocity", "density", "stress"):
+            assert group_rel(g, r, GROUPS[gname]) < 1e-8, (name, gname)
 
 
 def test_ul_same_input_same_neighbor_sets_after_steps(lib, oracle_bin):
@@ -136,3 +144,29 @@ def test_ul_c1_full_size_against_oracle(lib, oracle_bin):
     got = run_gpu(sc, 60, "fp64_strict")[0]
     for f in ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy"):
         assert rel_l2(got[f], ref[f]) < 1e-9, f
+
+
+@pytest.mark.parametrize("precision", ["fp64_strict", "mixed"])
+@pytest.mark.parametrize("method", ["ul", "tl"])
+def test_set_state_resumes_exactly(lib, precision, method):
+    """A run that is given, mid-way, another run's state continues exactly as that run
+    (before the rings touch: the contact force, not part of the state, is zero)."""
+    import mfree_iwf_gb300 as M
+    sc = S.c1_rings(dx=4e-3) if method == "ul" else S.c2_rings_tl(dx=4e-3)
+    fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy")
+    a = M.from_scenario(sc, precision=precision)
+    a.step(10)
+    s10 = [a.get_state(b, fields) for b in range(len(sc.bodies))]
+    a.step(10)
+    s20 = [a.get_state(b, fields) for b in range(len(sc.bodies))]
+    b_ = M.from_scenario(sc, precision=precision)
+    b_.step(5)
+    for k in range(len(sc.bodies)):
+        b_.set_state(k, s10[k])
+    b_.step(10)
+    for k in range(len(sc.bodies)):
+        got = b_.get_state(k, fields)
+        for f in fields:
+            assert np.array_equal(got[f], s20[k][f]), (method, precision, f)
+    a.close()
+    b_.close()
