@@ -186,6 +186,34 @@ MF_API mf_status mf_launch_count(mf_ctx* ctx, uint64_t* launches);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
 MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free UL step.  No counterpart in the reference: it exists for callers
+ * that must not allocate device memory after start-up (applications that reserve all
+ * GPU memory in their own pools, plug-ins that must not trigger the implicit device
+ * synchronisation of cudaMalloc/cudaFree, code running while a stream is captured).
+ * The caller passes device pointers to one body's particle arrays, updated in place;
+ * all scratch of the step lives in one fixed array inside the library, sized for at
+ * most MF_NOALLOC_MAX_PARTICLES particles (larger n returns MF_ERR_CAPACITY).  Every
+ * call on a device shares that array: calls that overlap on the GPU race, so
+ * serialise them.  The first call on a device looks up the array's address; make it
+ * before any stream capture begins.  Form: FP64 strict, the reference predicate
+ * epsilon 1e-6 and capacity 200; no contact, no boundary conditions.
+ * ------------------------------------------------------------------------- */
+#define MF_NOALLOC_MAX_PARTICLES 16384u
+
+typedef struct mf_device_body {
+	uint32_t n;
+	uint32_t reserved;
+	double *x, *y, *vx, *vy, *rho, *Sxx, *Sxy, *Syy;   /* device arrays, read and updated */
+	const double *m, *h, *quad_weight;                  /* device arrays, read */
+} mf_device_body;
+
+/* nsteps RK4 steps of the updated-Lagrangian pipeline given by actions[0..n_actions)
+ * (an ascending subsequence of the rings_monaghan list), on `stream` (a cudaStream_t,
+ * NULL = default stream) of the current device; returns after the stream is idle. */
+MF_API mf_status mf_ul_step_noalloc(const mf_device_body* body, const mf_sim_data* sd, double dt,
+                                    const int32_t* actions, uint32_t n_actions, int32_t nsteps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

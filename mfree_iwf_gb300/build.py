@@ -46,9 +46,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
             src = os.path.join(CSRC, tu)
             obj = os.path.join(BUILD, f"{tu[:-3]}_{ns}.o")
             jobs.append((src, obj, base + [f"-DMF_NS={ns}", f"--fmad={fmad}", src, "-o", obj]))
-    src = os.path.join(CSRC, "mf_api.cu")
-    obj = os.path.join(BUILD, "mf_api.o")
-    jobs.append((src, obj, base + [src, "-o", obj]))
+    for host_tu in ("mf_api.cu", "mf_noalloc.cu"):
+        src = os.path.join(CSRC, host_tu)
+        obj = os.path.join(BUILD, host_tu[:-3] + ".o")
+        jobs.append((src, obj, base + [src, "-o", obj]))
 
     def run(job):
         s, o, cmd = job
