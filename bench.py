@@ -49,6 +49,10 @@ def measured_peaks():
 
 def workload(name: str, dx: float | None):
     from mfree_iwf_gb300 import scenarios as S
+    if name == "c4":
+        sc = S.c4_ensemble(512)
+        return sc, {"workload": "ensemble of 512 ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
+                                "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
     if name == "c2":
         dx = dx or 5e-5
         return S.c2_rings_tl(dx=dx), {"workload": f"ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx={dx*1e3:g} mm"}
@@ -182,9 +186,8 @@ def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool) -> f
         if kind == 1:
             return 4 + 20 * nnz_per_row + 32 + 32 + 32 + 32 + 8
         return 4 + 20 * nnz_per_row + 32 + 32 + 8 + 8 + 8 + 8 + 32 + 32 + 16 + 128 + 64
-    if kind == 0:  # UL gather + pair: record write/read, perm/key/body, fc, state
-        rec = 80 if mixed else 128
-        return 2 * rec + 12 + 16 + (48 + 3 * 48 if mixed else 64 * 4)
+    if kind == 0:  # UL pair: own record, perm/key/body, contact force, 4 accesses of the state vector
+        return (80 + 12 + 16 + 4 * 48) if mixed else (128 + 12 + 16 + 4 * 64)
     return 0.0
 
 
@@ -204,17 +207,16 @@ def ours(args, cfg_desc):
     sc, cfg = workload(args.workload, args.dx)
     n = sc.n_total
     tl = sc.method == M.METHOD_TL
-    sim = M.from_scenario(sc, precision=args.precision, device=local)
+    sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"
-    sim.step(args.warmup)  # includes the set-up (neighbour search, corrections)
+    sim.step(1)  # set-up (neighbour search, corrections)
+    tune = sim.autotune(args.tune_steps) if not args.no_tune else "off"
+    sim.step(args.warmup)
     sim.synchronize()
     stream = torch.cuda.ExternalStream(sim.stream())
-    nnz = 0.0
-    if tl:
-        nnz = float(np.mean(sim.neighbor_counts(0)))
+    nnz = float(np.mean(sim.neighbor_counts(0))) if tl else 0.0
 
-    # ---- device-resident timed region
-    sim.set_timing(True)
+    # ---- device-resident timed region (graph replay of whole steps)
     l0 = sim.launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -232,13 +234,19 @@ def ours(args, cfg_desc):
     ms = e0.elapsed_time(e1)
     launches = sim.launch_count() - l0
     clocks = clk.summary()
-    kstats = {k: sim.kernel_stats(k) for k in range(6)}
-    sim.set_timing(False)
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * n * args.steps / (ms / 1e3)
+
+    # ---- per-kernel CUDA-event times (eager launches: a graph replay carries no
+    # per-launch events), same workload, right after the timed region
+    sim.set_timing(True)
+    sim.step(max(2, min(args.steps, 10)))
+    sim.synchronize()
+    kstats = {k: sim.kernel_stats(k) for k in range(6)}
+    sim.set_timing(False)
 
     # ---- end to end through the C ABI with host buffers: per step the state goes
     # host -> device (pinned), one step runs, the state comes back device -> host
@@ -261,11 +269,38 @@ def ours(args, cfg_desc):
     e2e_value = world * n * k2 / wall
     bytes_io = 8 * len(fields) * n
 
+    sim.close()
+    del sim
+
+    # ---- the plain FP64 form on the same workload, same run
+    forms = None
+    if mixed and not args.no_compare:
+        sim64 = M.from_scenario(sc, precision="fp64", device=local, graph=not args.no_graph)
+        sim64.step(1)
+        if not args.no_tune:
+            sim64.autotune(1)
+        sim64.step(2)
+        sim64.synchronize()
+        k64 = max(2, min(args.steps // 5, 10))
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        st64 = torch.cuda.ExternalStream(sim64.stream())
+        torch.cuda.synchronize()
+        f0.record(st64)
+        sim64.step(k64)
+        f1.record(st64)
+        sim64.synchronize()
+        torch.cuda.synchronize()
+        v64 = n * k64 / (f0.elapsed_time(f1) / 1e3)
+        sim64.close()
+        forms = {"mixed": value / world, "fp64": v64, "mixed_over_fp64": value / world / v64, "fp64_steps": k64}
+
     # ---- roofline of the dominant kernel
     peaks, peak_kind = measured_peaks()
-    dom = max(kstats, key=lambda k: kstats[k][0])
+    dom = max((k for k in kstats if k != 4), key=lambda k: kstats[k][0])  # kind 4 is a whole UL stage
     kms, klaunch, krows = kstats[dom]
-    names = {0: "UL stage (gather + pair + RK)", 1: "TL pass A", 2: "TL pass B", 3: "contact", 4: "grid", 5: "weak"}
+    names = {0: "UL pair (+RK)", 1: "TL pass A", 2: "TL pass B", 3: "contact", 4: "UL stage (grid + gather + pair)",
+             5: "weak"}
     roof = None
     if klaunch:
         per_launch_rows = krows / klaunch
@@ -295,9 +330,9 @@ def ours(args, cfg_desc):
                     "steps": k2},
             "roofline": roof, "cpu_baseline": cpu,
             "kernels_ms": {names[k]: v[0] for k, v in kstats.items() if v[1]},
+            "forms": forms, "autotune": tune,
         }
         print(json.dumps(line), flush=True)
-    sim.close()
     if dist:
         dist.destroy_process_group()
 
@@ -308,18 +343,23 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--tune-steps", type=int, default=3)
+    ap.add_argument("--no-compare", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     _, cfg = workload(args.workload, args.dx) if args.impl == "ours" and False else (None, None)
     cfg_desc = {"workload": {"c2": "ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx=0.05 mm",
-                             "c1": "ring impact, Gray-Monaghan SPH, dx=1 mm"}[args.workload]}
+                             "c1": "ring impact, Gray-Monaghan SPH, dx=1 mm",
+                             "c4": "ensemble of 512 ring impacts, Gray-Monaghan SPH"}[args.workload]}
     if args.impl == "reference":
         reference_arm(args, cfg_desc)
         return

@@ -112,7 +112,7 @@ typedef struct mf_config {
 	double nbh_eps;      /* absolute epsilon of the predicate r^2 <= 4h^2 + eps (the reference: 1e-6) */
 	double nbh_h;        /* TL / TL_WEAK: the h given to the set-up neighbour search (neighbor_search.h:116) */
 	int32_t contact;     /* 1: after every step, penalty contact between bodies of a group (mfree_iwf.cpp:91-97) */
-	int32_t reserved;
+	int32_t graph;       /* 1: capture one step as a CUDA graph and replay it (not while timing is on) */
 } mf_config;
 
 /* simulation_data (simulation_data.h:25-99) */
@@ -183,6 +183,12 @@ MF_API mf_status mf_set_timing(mf_ctx* ctx, int32_t enable);
 MF_API mf_status mf_kernel_stats(mf_ctx* ctx, int32_t kind, double* total_ms, uint64_t* launches, uint64_t* rows);
 /* Number of kernel launches issued by this context since creation. */
 MF_API mf_status mf_launch_count(mf_ctx* ctx, uint64_t* launches);
+/* Autotuner: times the candidate launch shapes of the hot kernels (rows per block,
+ * plain or persistent pair kernel, rows per work chunk) for trial_steps steps each on
+ * a snapshot of the state, restores the state, and keeps the fastest.  Results are
+ * cached per process by (method, precision, particle-count bucket).  report (may be
+ * NULL) receives a one-line summary. */
+MF_API mf_status mf_autotune(mf_ctx* ctx, int32_t trial_steps, char* report, uint32_t report_len);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
 MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
 

@@ -40,7 +40,7 @@ _UP = ctypes.POINTER(ctypes.c_uint32)
 class MfConfig(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("max_nbh", ctypes.c_uint32), ("nbh_eps", ctypes.c_double), ("nbh_h", ctypes.c_double),
-                ("contact", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("contact", ctypes.c_int32), ("graph", ctypes.c_int32)]
 
 
 class MfSimData(ctypes.Structure):
@@ -104,6 +104,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_kernel_stats": (C.c_int32, [C.c_void_p, C.c_int32, _DP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "mf_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
         "mf_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
+        "mf_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, C.c_uint32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -154,10 +155,10 @@ class Simulation:
     """One mf_ctx: a set of bodies stepped together by the reference driver's loop."""
 
     def __init__(self, method: int = METHOD_UL, precision="fp64_strict", device: int = 0, max_nbh: int = 200,
-                 nbh_eps: float = 1e-6, nbh_h: float = 0.0, contact: bool = False):
+                 nbh_eps: float = 1e-6, nbh_h: float = 0.0, contact: bool = False, graph: bool = False):
         self._lib = load_library()
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        cfg = MfConfig(method, prec, device, max_nbh, nbh_eps, nbh_h, 1 if contact else 0, 0)
+        cfg = MfConfig(method, prec, device, max_nbh, nbh_eps, nbh_h, 1 if contact else 0, 1 if graph else 0)
         h = ctypes.c_void_p()
         st = self._lib.mf_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:
@@ -284,6 +285,11 @@ class Simulation:
                     "mf_kernel_stats")
         return ms.value, nl.value, rows.value
 
+    def autotune(self, trial_steps: int = 3) -> str:
+        buf = ctypes.create_string_buffer(2048)
+        self._check(self._lib.mf_autotune(self._h, int(trial_steps), buf, len(buf)), "mf_autotune")
+        return buf.value.decode()
+
     def launch_count(self) -> int:
         n = ctypes.c_uint64()
         self._check(self._lib.mf_launch_count(self._h, ctypes.byref(n)), "mf_launch_count")
@@ -296,15 +302,17 @@ class Simulation:
 
 
 def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 200, contact: Optional[bool] = None,
-                  groups: Optional[Sequence[int]] = None) -> Simulation:
+                  groups: Optional[Sequence[int]] = None, graph: bool = False) -> Simulation:
     """Build a :class:`Simulation` from a :class:`mfree_iwf_gb300.scenarios.Scenario` (the same
     bodies, constants, action list, boundary conditions and contact boundaries)."""
     sim = Simulation(method=sc.method, precision=precision, device=device, max_nbh=max_nbh, nbh_eps=sc.nbh_eps,
-                     nbh_h=sc.nbh_h, contact=bool(sc.contact) if contact is None else contact)
-    sd = SimData(sc.nu, sc.E, sc.rho0, sc.wdeltap, sc.corr_exp, sc.mghn_eps, sc.alpha, sc.beta, sc.eta,
-                 sc.xsph_eps, sc.do_smooth)
+                     nbh_h=sc.nbh_h, contact=bool(sc.contact) if contact is None else contact, graph=graph)
     for k, b in enumerate(sc.bodies):
-        bid = sim.add_body(b.arrays, sd, sc.dt, group=0 if groups is None else groups[k])
+        p = b.params or {}
+        sd = SimData(p.get("nu", sc.nu), p.get("E", sc.E), p.get("rho0", sc.rho0), p.get("wdeltap", sc.wdeltap),
+                     sc.corr_exp, sc.mghn_eps, sc.alpha, sc.beta, sc.eta, sc.xsph_eps, sc.do_smooth)
+        grp = (0 if not p else k) if groups is None else groups[k]
+        bid = sim.add_body(b.arrays, sd, p.get("dt", sc.dt), group=grp)
         for a in sc.actions:
             sim.add_action(bid, a)
         for bc in b.bcs:

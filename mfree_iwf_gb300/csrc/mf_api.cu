@@ -2,7 +2,10 @@
 // validation against the fused pipelines, device memory, and the step loop of the
 // reference driver (mfree_iwf.cpp:84-97) expressed as stream-ordered launches.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -69,6 +72,13 @@ struct Timing {
 	uint64_t rows[8] = {0};
 };
 
+// Launch shape of the hot kernels, chosen by mf_autotune.
+struct Tune {
+	uint32_t ul_block = 128, ul_persistent = 0, ul_chunk = 1, tl_block = 128;
+};
+std::mutex g_tune_mutex;
+std::map<std::string, Tune> g_tune_cache;
+
 }  // namespace
 
 struct mf_ctx {
@@ -101,21 +111,33 @@ struct mf_ctx {
 	DevBuf<unsigned char> rec, sort_tmp;
 	int sort_bits = 1;
 
-	// TL: fixed neighbour lists with corrected gradients, per-stage scratch
-	DevBuf<uint32_t> nbr_off, nbr, bc_rows;
+	// TL: fixed neighbour lists (CSR from the set-up, kept for mf_get_neighbors, and the
+	// sliced-ELL copy the stage kernels read) with corrected gradients, per-stage scratch
+	DevBuf<uint32_t> nbr_off, nbr, bc_rows, sl_off, snbr;
+	DevBuf<uint16_t> scnt;
 	DevBuf<double> wx64, wy64, P64, dA64, c64, bc_v;
-	DevBuf<float> wx32, wy32, P32, dA32, c32, qw32, m32, h32;
-	DevBuf<unsigned char> pack;
+	DevBuf<double2> sw64;
+	DevBuf<float2> sw32, swA32;
+	DevBuf<float> qw32, m32, h32;
+	DevBuf<float4> recA, recB, dA32;
 	uint32_t n_bc = 0;
 
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
 
+	// launch shapes, persistent-kernel work counter, captured step graph
+	Tune tune;
+	int sm_count = 0;
+	DevBuf<uint32_t> work;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t graph_exec = nullptr;
+	uint64_t graph_launches = 0;
+
 	// contact
 	bool contact_on = false;
 	DevBuf<uint32_t> bnd_rows, bnd_start, bnd_len, tile_first, tile_end, slave_rows, slave_master, m_tile_off, m_tile_n;
 	DevBuf<double4> bnd;
-	DevBuf<float4> tile_bb;
+	DevBuf<float4> tile_bb, bnd_ff;
 	DevBuf<double> slave_dt;
 	uint32_t n_bnd = 0, n_tiles = 0, n_slave = 0;
 
@@ -217,6 +239,11 @@ ULArgs ul_args(mf_ctx* c, uint32_t stage) {
 	a.sort_tmp_bytes = c->sort_tmp.n;
 	a.sort_bits = c->sort_bits;
 	a.status = c->d_status;
+	a.block = c->tune.ul_block;
+	a.persistent = c->tune.ul_persistent;
+	a.chunk = c->tune.ul_chunk;
+	a.grid = (uint32_t)std::max(1, c->sm_count) * (2048u / c->tune.ul_block);
+	a.work = c->work.p;
 	return a;
 }
 
@@ -239,6 +266,20 @@ void timing_end(mf_ctx* c, int slot, uint64_t rows) {
 	if (slot < 0) return;
 	Timing& t = c->timing;
 	cudaEventRecord(t.pool[slot + 1], c->stream);
+	int kind = t.used[slot / 2].first;
+	t.launches[kind]++;
+	t.rows[kind] += rows;
+}
+// Reserve an event pair for a launcher that records the events itself.
+int timing_reserve(mf_ctx* c, int kind) {
+	int slot;
+	if (!c->timing.on) return -1;
+	timing_begin(c, kind, slot);  // records the start event now; the launcher re-records both
+	return slot;
+}
+void timing_count(mf_ctx* c, int slot, uint64_t rows) {
+	if (slot < 0) return;
+	Timing& t = c->timing;
 	int kind = t.used[slot / 2].first;
 	t.launches[kind]++;
 	t.rows[kind] += rows;
@@ -344,11 +385,12 @@ mf_status finalize(mf_ctx* c) {
 	CK(c->params.alloc(c->h_params.size()));
 	CK(cudaMemcpy(c->params.p, c->h_params.data(), c->h_params.size() * sizeof(BodyParams), cudaMemcpyHostToDevice));
 
+	CK(c->work.alloc(1));
 	// UL grid machinery (also used for the UL neighbour dump)
 	if (c->cfg.method == MF_METHOD_UL) {
 		uint32_t nb = (uint32_t)c->bodies.size();
 		CK(c->geom.alloc(nb));
-		CK(c->bbox.alloc(5 * (size_t)nb));
+		CK(c->bbox.alloc(6 * (size_t)nb));
 		CK(c->total_cells.alloc(1));
 		CK(c->keys.alloc(n)); CK(c->keys_sorted.alloc(n)); CK(c->perm_in.alloc(n)); CK(c->perm.alloc(n));
 		CK(c->cell_start.alloc((size_t)n + 2));
@@ -374,11 +416,18 @@ mf_status finalize(mf_ctx* c) {
 mf_status ul_step(mf_ctx* c) {
 	for (uint32_t s = 0; s < 4; s++) {
 		ULArgs a = ul_args(c, s);
-		int slot;
-		timing_begin(c, 0, slot);
-		// the pair kernel is timed together with its gather; the grid build separately
+		// kind 4: the whole stage (grid build when due, gather, pair); kind 0: the pair
+		// kernel alone, between events the launcher records around it
+		int slot_all, slot_pair;
+		timing_begin(c, 4, slot_all);
+		slot_pair = timing_reserve(c, 0);
+		if (slot_pair >= 0) {
+			a.ev_pair0 = c->timing.pool[slot_pair];
+			a.ev_pair1 = c->timing.pool[slot_pair + 1];
+		}
 		cudaError_t e = c->strict ? mf_strict::ul_stage(a, c->mixed, c->stream) : mf_fast::ul_stage(a, c->mixed, c->stream);
-		timing_end(c, slot, c->n_total);
+		timing_count(c, slot_pair, c->n_total);
+		timing_end(c, slot_all, c->n_total);
 		if (e != cudaSuccess) return cuda_fail(c, e, "ul_stage");
 		c->launches += (a.strict_grid || s == 0) ? 8 + 4 : 2;
 	}
@@ -400,18 +449,22 @@ TLArgs tl_args(mf_ctx* c) {
 		for (int q = 0; q < 8; q++) *d[q] = c->sd[k][q].p;
 		s[k]->rho_f = c->sf[k][0].p; s[k]->Sxx_f = c->sf[k][1].p; s[k]->Sxy_f = c->sf[k][2].p; s[k]->Syy_f = c->sf[k][3].p;
 	}
-	a.nbr_off = c->nbr_off.p;
-	a.nbr = c->nbr.p;
-	a.wx = c->mixed ? (const void*)c->wx32.p : (const void*)c->wx64.p;
-	a.wy = c->mixed ? (const void*)c->wy32.p : (const void*)c->wy64.p;
-	a.P = c->mixed ? (void*)c->P32.p : (void*)c->P64.p;
-	a.dA = c->mixed ? (void*)c->dA32.p : (void*)c->dA64.p;
-	a.c = c->mixed ? (void*)c->c32.p : (void*)c->c64.p;
-	a.pack = c->pack.p;
+	a.sl_off = c->sl_off.p;
+	a.cnt = c->scnt.p;
+	a.snbr = c->snbr.p;
+	a.sw = c->mixed ? (const void*)c->sw32.p : (const void*)c->sw64.p;
+	a.swA = c->swA32.p;
+	a.P = c->P64.p;
+	a.dA = c->dA64.p;
+	a.c = c->c64.p;
+	a.recA = c->recA.p;
+	a.recB = c->recB.p;
+	a.dA32 = c->dA32.p;
 	a.bc_rows = c->bc_rows.p;
 	a.bc_v = c->bc_v.p;
 	a.n_bc = c->n_bc;
 	a.status = c->d_status;
+	a.block = c->tune.tl_block;
 	return a;
 }
 
@@ -550,14 +603,40 @@ mf_status tl_setup(mf_ctx* c) {
 	if (e != cudaSuccess) return cuda_fail(c, e, "tl_rl");
 	st = check_status(c);
 	if (st != MF_OK) return st;
+	// sliced ELL: slices of 32 rows, each padded to its longest list
+	uint32_t ns = (n + 31) / 32;
+	std::vector<uint32_t> sl(ns + 1, 0);
+	uint64_t ent = 0;
+	for (uint32_t s_ = 0; s_ < ns; s_++) {
+		uint32_t w = 0;
+		for (uint32_t r = 32 * s_; r < std::min(n, 32 * s_ + 32); r++) w = std::max(w, hc[r]);
+		sl[s_] = (uint32_t)ent;
+		ent += 32ull * w;
+	}
+	if (ent > 0xffffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^32 sliced-ELL entries");
+	sl[ns] = (uint32_t)ent;
+	CK(c->sl_off.alloc(ns + 1));
+	CK(cudaMemcpy(c->sl_off.p, sl.data(), (ns + 1) * 4, cudaMemcpyHostToDevice));
+	CK(c->scnt.alloc(n));
+	CK(c->snbr.alloc(ent));
 	if (c->mixed) {
-		CK(c->wx32.alloc(tot)); CK(c->wy32.alloc(tot));
-		CK(mf_fast::to_float(tot, c->wx64.p, c->wx32.p, c->stream));
-		CK(mf_fast::to_float(tot, c->wy64.p, c->wy32.p, c->stream));
-		CK(cudaStreamSynchronize(c->stream));
-		c->wx64.free(); c->wy64.free();
-		CK(c->P32.alloc(4 * (size_t)n)); CK(c->dA32.alloc(4 * (size_t)n)); CK(c->c32.alloc(n));
-		CK(c->pack.alloc(6 * (size_t)n * 8));
+		CK(c->sw32.alloc(ent));
+		CK(c->swA32.alloc(ent));
+	} else {
+		CK(c->sw64.alloc(ent));
+	}
+	e = c->strict ? mf_strict::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
+	                                      c->snbr.p, c->sw64.p, nullptr, nullptr, c->qw0.p, c->stream)
+	              : mf_fast::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
+	                                    c->snbr.p, c->mixed ? nullptr : (void*)c->sw64.p,
+	                                    c->mixed ? (void*)c->sw32.p : nullptr, c->mixed ? (void*)c->swA32.p : nullptr,
+	                                    c->qw0.p, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "tl_to_sell");
+	CK(cudaStreamSynchronize(c->stream));
+	c->wx64.free();
+	c->wy64.free();
+	if (c->mixed) {
+		CK(c->recA.alloc(n)); CK(c->recB.alloc(4 * (size_t)n)); CK(c->dA32.alloc(n));
 		auto f32 = [&](DevBuf<float>& d, int field) -> mf_status {
 			CK(d.alloc(n));
 			std::vector<float> v(n);
@@ -651,6 +730,7 @@ mf_status contact_setup(mf_ctx* c) {
 	CK(c->slave_dt.alloc(sdt.size()));
 	CK(cudaMemcpy(c->slave_dt.p, sdt.data(), sdt.size() * 8, cudaMemcpyHostToDevice));
 	CK(c->bnd.alloc(c->n_bnd));
+	CK(c->bnd_ff.alloc(c->n_bnd));
 	CK(c->tile_bb.alloc(c->n_tiles));
 	return MF_OK;
 }
@@ -659,7 +739,7 @@ mf_status contact_run(mf_ctx* c) {
 	ContactArgs a{};
 	a.n_bnd = c->n_bnd; a.n_tiles = c->n_tiles; a.n_slave = c->n_slave;
 	a.bnd_rows = c->bnd_rows.p; a.bnd_start = c->bnd_start.p; a.bnd_len = c->bnd_len.p;
-	a.bnd = c->bnd.p; a.tile_first = c->tile_first.p; a.tile_end = c->tile_end.p; a.tile_bb = c->tile_bb.p;
+	a.bnd = c->bnd.p; a.bnd_ff = c->bnd_ff.p; a.tile_first = c->tile_first.p; a.tile_end = c->tile_end.p; a.tile_bb = c->tile_bb.p;
 	a.slave_rows = c->slave_rows.p; a.slave_master = c->slave_master.p; a.dt = c->slave_dt.p;
 	a.m_tile_off = c->m_tile_off.p; a.m_tile_n = c->m_tile_n.p;
 	a.x = c->sd[0][0].p; a.y = c->sd[0][1].p; a.m = c->m.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
@@ -676,6 +756,9 @@ mf_status contact_run(mf_ctx* c) {
 
 mf_ctx::~mf_ctx() {
 	if (stream) cudaStreamSynchronize(stream);
+	if (graph_exec) cudaGraphExecDestroy(graph_exec);
+	if (graph) cudaGraphDestroy(graph);
+	work.free();
 	DevBuf<double>* d[] = {&m, &h, &qw0, &fcx, &fcy, &X, &Y};
 	for (auto* p : d) p->free();
 	for (int k = 0; k < 4; k++) {
@@ -684,14 +767,15 @@ mf_ctx::~mf_ctx() {
 	}
 	body_of.free(); params.free(); geom.free(); bbox.free(); total_cells.free(); keys.free(); keys_sorted.free();
 	perm_in.free(); perm.free(); cell_start.free(); rec_body.free(); rec.free(); sort_tmp.free();
+	sl_off.free(); snbr.free(); scnt.free(); sw64.free(); sw32.free(); swA32.free(); recA.free(); recB.free(); dA32.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
 	                            &slave_rows, &slave_master, &m_tile_off, &m_tile_n};
 	for (auto* p : u32s) p->free();
 	DevBuf<double>* f64s[] = {&wx64, &wy64, &P64, &dA64, &c64, &bc_v, &slave_dt};
 	for (auto* p : f64s) p->free();
-	DevBuf<float>* f32s[] = {&wx32, &wy32, &P32, &dA32, &c32, &qw32, &m32, &h32};
+	DevBuf<float>* f32s[] = {&qw32, &m32, &h32};
 	for (auto* p : f32s) p->free();
-	pack.free(); bnd.free(); tile_bb.free(); staging.free();
+	bnd.free(); bnd_ff.free(); tile_bb.free(); staging.free();
 	for (auto e : timing.pool) cudaEventDestroy(e);
 	if (d_status) cudaFree(d_status);
 	if (h_status) cudaFreeHost(h_status);
@@ -733,6 +817,7 @@ MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out) {
 	if (cudaSetDevice(cfg->device) != cudaSuccess) return MF_ERR_CUDA;
 	mf_ctx* c = new mf_ctx();
 	c->cfg = *cfg;
+	cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, cfg->device);
 	if (c->cfg.max_nbh == 0) c->cfg.max_nbh = REF_MAX_NBH;
 	if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
 	    cudaMalloc(&c->d_status, sizeof(DevStatusH)) != cudaSuccess ||
@@ -840,21 +925,70 @@ MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, ui
 	return MF_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The launches of one step of every body, in the driver's order (mfree_iwf.cpp:84-97):
+// the RK4 step, then the boundary refresh and contact.
+mf_status one_step(mf_ctx* c) {
+	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : tl_step_all(c);
+	if (st != MF_OK) return st;
+	if (c->contact_on) st = contact_run(c);
+	return st;
+}
+
+void drop_graph(mf_ctx* c) {
+	if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+	if (c->graph) cudaGraphDestroy(c->graph);
+	c->graph_exec = nullptr;
+	c->graph = nullptr;
+}
+
+// Capture one step on the context's stream and instantiate it for replay.
+mf_status capture_step(mf_ctx* c) {
+	drop_graph(c);
+	uint64_t l0 = c->launches;
+	CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+	mf_status st = one_step(c);
+	cudaGraph_t g = nullptr;
+	cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+	if (st != MF_OK) {
+		if (g) cudaGraphDestroy(g);
+		return st;
+	}
+	if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+	c->graph = g;
+	CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
+	c->graph_launches = c->launches - l0;
+	c->launches = l0;
+	return MF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
 	if (!c) return MF_ERR_ARG;
 	if (nsteps < 0) return fail(c, MF_ERR_ARG, "nsteps < 0");
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
 	CK(cudaSetDevice(c->cfg.device));
-	for (int32_t k = 0; k < nsteps; k++) {
-		if (c->cfg.method == MF_METHOD_UL) st = ul_step(c);
-		else st = tl_step_all(c);
+	bool use_graph = c->cfg.graph && !c->timing.on;
+	if (use_graph && !c->graph_exec && nsteps > 0) {
+		st = capture_step(c);
 		if (st != MF_OK) return st;
-		for (auto& b : c->bodies) b.time += b.dt;  // rk4.h:107 (each body's own clock)
-		if (c->contact_on) {
-			st = contact_run(c);
+	}
+	for (int32_t k = 0; k < nsteps; k++) {
+		if (use_graph) {
+			CK(cudaGraphLaunch(c->graph_exec, c->stream));
+			c->launches += c->graph_launches;
+		} else {
+			st = one_step(c);
 			if (st != MF_OK) return st;
 		}
+		for (auto& b : c->bodies) b.time += b.dt;  // rk4.h:107 (each body's own clock)
 	}
 	return check_status(c);
 }
@@ -1013,6 +1147,152 @@ MF_API mf_status mf_kernel_stats(mf_ctx* c, int32_t kind, double* total_ms, uint
 MF_API mf_status mf_launch_count(mf_ctx* c, uint64_t* launches) {
 	if (!c || !launches) return MF_ERR_ARG;
 	*launches = c->launches;
+	return MF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Device snapshot of everything a step changes (state, contact forces, TL stage-0
+// copy, body clocks), so trial steps leave no trace.
+struct Snapshot {
+	std::vector<DevBuf<unsigned char>> bufs;
+	std::vector<std::pair<void*, size_t>> src;
+	std::vector<double> times;
+	std::vector<BodyParams> params;
+};
+
+mf_status snapshot_take(mf_ctx* c, Snapshot& s) {
+	uint32_t n = c->n_total;
+	auto add = [&](void* p, size_t bytes) -> mf_status {
+		if (!p || !bytes) return MF_OK;
+		s.bufs.emplace_back();
+		CK(s.bufs.back().alloc(bytes));
+		CK(cudaMemcpyAsync(s.bufs.back().p, p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+		s.src.push_back({p, bytes});
+		return MF_OK;
+	};
+	mf_status st;
+	for (int k : {0, 2})
+		for (int q = 0; q < 8; q++)
+			if ((st = add(c->sd[k][q].p, (size_t)n * 8)) || (k == 0 && q < 4 && (st = add(c->sf[k][q].p, (size_t)n * 4))) ||
+			    (k == 2 && q < 4 && (st = add(c->sf[k][q].p, (size_t)n * 4))))
+				return st;
+	if ((st = add(c->fcx.p, (size_t)n * 8)) || (st = add(c->fcy.p, (size_t)n * 8))) return st;
+	if ((st = add(c->params.p, c->h_params.size() * sizeof(BodyParams)))) return st;
+	for (auto& b : c->bodies) s.times.push_back(b.time);
+	CK(cudaStreamSynchronize(c->stream));
+	return MF_OK;
+}
+
+mf_status snapshot_restore(mf_ctx* c, Snapshot& s) {
+	for (size_t i = 0; i < s.bufs.size(); i++)
+		CK(cudaMemcpyAsync(s.src[i].first, s.bufs[i].p, s.src[i].second, cudaMemcpyDeviceToDevice, c->stream));
+	for (size_t b = 0; b < c->bodies.size(); b++) c->bodies[b].time = s.times[b];
+	CK(cudaStreamSynchronize(c->stream));
+	return MF_OK;
+}
+
+void snapshot_free(Snapshot& s) {
+	for (auto& b : s.bufs) b.free();
+}
+
+std::string tune_key(mf_ctx* c) {
+	int bucket = 0;
+	while ((1u << bucket) < c->n_total) bucket++;
+	char k[96];
+	snprintf(k, sizeof k, "m%d p%d n2^%d", c->cfg.method, c->cfg.precision, bucket);
+	return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint32_t report_len) {
+	if (!c || trial_steps < 1) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	CK(cudaSetDevice(c->cfg.device));
+	std::string key = tune_key(c);
+	std::string rep;
+	{
+		std::lock_guard<std::mutex> lock(g_tune_mutex);
+		auto it = g_tune_cache.find(key);
+		if (it != g_tune_cache.end()) {
+			c->tune = it->second;
+			drop_graph(c);
+			rep = "cached " + key;
+			if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
+			return MF_OK;
+		}
+	}
+	std::vector<Tune> cands;
+	for (uint32_t bs : {64u, 128u, 256u}) {
+		Tune t = c->tune;
+		if (c->cfg.method == MF_METHOD_UL) {
+			t.ul_block = bs;
+			t.ul_persistent = 0;
+			t.ul_chunk = 1;
+			cands.push_back(t);
+			for (uint32_t ch : {1u, 4u}) {
+				t.ul_persistent = 1;
+				t.ul_chunk = ch;
+				cands.push_back(t);
+			}
+		} else {
+			t.tl_block = bs;
+			cands.push_back(t);
+		}
+	}
+	Snapshot snap;
+	if ((st = snapshot_take(c, snap)) != MF_OK) return st;
+	bool timing_was = c->timing.on;
+	c->timing.on = false;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	double best = 1e300;
+	Tune best_t = c->tune;
+	char line[160];
+	for (const Tune& t : cands) {
+		c->tune = t;
+		if ((st = snapshot_restore(c, snap)) != MF_OK) break;
+		if ((st = one_step(c)) != MF_OK) break;  // warm-up
+		cudaEventRecord(e0, c->stream);
+		for (int32_t k = 0; k < trial_steps && st == MF_OK; k++) st = one_step(c);
+		cudaEventRecord(e1, c->stream);
+		if (st != MF_OK) break;
+		if ((st = check_status(c)) != MF_OK) break;
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		double per = ms / trial_steps;
+		snprintf(line, sizeof line, "%s[b%u p%u c%u tl%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block, t.ul_persistent,
+		         t.ul_chunk, t.tl_block, per);
+		rep += line;
+		if (per < best) {
+			best = per;
+			best_t = t;
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	c->timing.on = timing_was;
+	c->tune = best_t;
+	mf_status rs = snapshot_restore(c, snap);
+	snapshot_free(snap);
+	if (st != MF_OK) return st;
+	if (rs != MF_OK) return rs;
+	drop_graph(c);
+	{
+		std::lock_guard<std::mutex> lock(g_tune_mutex);
+		g_tune_cache[key] = best_t;
+	}
+	snprintf(line, sizeof line, " -> b%u p%u c%u tl%u (%s)", best_t.ul_block, best_t.ul_persistent, best_t.ul_chunk,
+	         best_t.tl_block, key.c_str());
+	rep += line;
+	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
 	return MF_OK;
 }
 

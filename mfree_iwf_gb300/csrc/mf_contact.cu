@@ -4,13 +4,17 @@
 //
 // The reference finds, for every slave particle, the nearest master boundary point
 // with a kd-tree (kd_tree.cpp:61-101).  Here the master boundary (its points in tour
-// order) is cut into tiles of 32 consecutive points with a bounding box each; a
-// query first visits the tile whose box is nearest, then every other tile whose box
-// can still hold a closer point.  Box tests run in FP32 on boxes grown by an
-// absolute margin that covers FP32 rounding, so they never prune a tile that holds
-// the nearest point; point distances are FP64 with the reference's operation order,
-// so the nearest point is the kd-tree's.  Among exactly equal distances the lowest
-// boundary index wins (the kd-tree keeps the first it meets in its traversal).
+// order) is cut into tiles of 32 consecutive points with an FP32 bounding box each,
+// grown by an absolute margin that covers FP32 rounding.  A warp handles 32
+// neighbouring slave particles: from the box around its queries it keeps only the
+// tiles that can hold the nearest point of *some* query (lower bound <= the smallest
+// upper bound over all tiles).  Each query then scans those tiles with its own
+// box pruning, first in FP32 with float-float coordinate differences, then exactly in
+// FP64 -- with the reference's operation order -- over the few points whose FP32
+// distance is within 2e-5 (relative) of the FP32 minimum, a band that provably holds
+// the exact minimum.  So the nearest point is the kd-tree's; among exactly equal
+// distances the lowest boundary index wins (the kd-tree keeps the first it meets in
+// its traversal).
 #include "mf_common.cuh"
 #include "mf_kernels.h"
 
@@ -45,6 +49,8 @@ __global__ void k_boundary(ContactArgs a) {
 	double nrx = bx * ir, nry = by * ir;
 	double nx = 0.5 * (nlx + nrx), ny = 0.5 * (nly + nry);
 	a.bnd[p] = make_double4(px, py, nx, ny);
+	FF fx = ff_split(px), fy = ff_split(py);
+	a.bnd_ff[p] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 }
 
 __global__ void k_tiles(ContactArgs a) {
@@ -62,17 +68,41 @@ __global__ void k_tiles(ContactArgs a) {
 	a.tile_bb[t] = make_float4(mnx - TILE_MARGIN, mny - TILE_MARGIN, mxx + TILE_MARGIN, mxy + TILE_MARGIN);
 }
 
-__device__ __forceinline__ float box_lb(float4 bb, float qx, float qy) {
-	float dx = fmaxf(fmaxf(bb.x - qx, qx - bb.z), 0.f);
-	float dy = fmaxf(fmaxf(bb.y - qy, qy - bb.w), 0.f);
+// squared distance bounds between a query box (x0, y0, x1, y1) and a tile box
+__device__ __forceinline__ float box_lb(float4 bb, float x0, float y0, float x1, float y1) {
+	float dx = fmaxf(fmaxf(bb.x - x1, x0 - bb.z), 0.f);
+	float dy = fmaxf(fmaxf(bb.y - y1, y0 - bb.w), 0.f);
+	return dx * dx + dy * dy;
+}
+__device__ __forceinline__ float box_ub(float4 bb, float x0, float y0, float x1, float y1) {
+	float dx = fmaxf(fabsf(bb.z - x0), fabsf(x1 - bb.x));
+	float dy = fmaxf(fabsf(bb.w - y0), fabsf(y1 - bb.y));
 	return dx * dx + dy * dy;
 }
 
-__device__ __forceinline__ void scan_tile(const ContactArgs& a, uint32_t t, double qx, double qy, double& best,
-                                          uint32_t& arg) {
+struct Query {
+	float xf, yf;       // FP32 coordinates (box tests)
+	FF x, y;            // float-float (FP32 distances)
+	double xd, yd;      // FP64 (exact distances)
+};
+
+__device__ __forceinline__ float ff_dist2(const Query& q, float4 p) {
+	float dx = (q.x.hi - p.x) + (q.x.lo - p.y);
+	float dy = (q.y.hi - p.z) + (q.y.lo - p.w);
+	return dx * dx + dy * dy;
+}
+
+// FP32 pass over one tile: the smallest FP32 distance
+__device__ __forceinline__ void scan_f32(const ContactArgs& a, uint32_t t, const Query& q, float& best_f) {
+	for (uint32_t p = a.tile_first[t]; p < a.tile_end[t]; p++) best_f = fminf(best_f, ff_dist2(q, a.bnd_ff[p]));
+}
+// exact pass over one tile: FP64 distances (kd_tree.cpp:79-88 order) of the points in the band
+__device__ __forceinline__ void scan_exact(const ContactArgs& a, uint32_t t, const Query& q, float thr, double& best,
+                                           uint32_t& arg) {
 	for (uint32_t p = a.tile_first[t]; p < a.tile_end[t]; p++) {
-		double4 q = a.bnd[p];
-		double dx = qx - q.x, dy = qy - q.y;
+		if (ff_dist2(q, a.bnd_ff[p]) > thr) continue;
+		double4 c = a.bnd[p];
+		double dx = q.xd - c.x, dy = q.yd - c.y;
 		double dx2 = dx * dx, dy2 = dy * dy;
 		double dist2 = dx2 + dy2;
 		if (dist2 < best || (dist2 == best && p < arg)) {
@@ -83,33 +113,84 @@ __device__ __forceinline__ void scan_tile(const ContactArgs& a, uint32_t t, doub
 }
 
 __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
+	const unsigned FULL = 0xffffffffu;
 	uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-	if (r >= a.n_slave) return;
-	uint32_t row = a.slave_rows[r];
-	uint32_t M = a.slave_master[r];
-	uint32_t t0 = a.m_tile_off[M], t1 = t0 + a.m_tile_n[M];
-	double qx = a.x[row], qy = a.y[row];
-	float qxf = (float)qx, qyf = (float)qy;
-	// nearest box first
-	uint32_t tstar = t0;
-	float lbstar = 3.4e38f;
-	for (uint32_t t = t0; t < t1; t++) {
-		float lb = box_lb(a.tile_bb[t], qxf, qyf);
-		if (lb < lbstar) { lbstar = lb; tstar = t; }
-	}
+	bool valid = r < a.n_slave;
+	unsigned vmask = __ballot_sync(FULL, valid);
+	if (!vmask) return;  // the whole warp is past the end
+	uint32_t lane = threadIdx.x & 31;
+	uint32_t row = valid ? a.slave_rows[r] : 0u;
+	uint32_t M = valid ? a.slave_master[r] : 0u;
+	uint32_t M0 = __shfl_sync(FULL, M, __ffs(vmask) - 1);
+	if (!valid) M = M0;
+	bool uniform = __all_sync(FULL, M == M0);
+	Query q;
+	q.xd = valid ? a.x[row] : 0.;
+	q.yd = valid ? a.y[row] : 0.;
+	q.x = ff_split(q.xd);
+	q.y = ff_split(q.yd);
+	q.xf = (float)q.xd;
+	q.yf = (float)q.yd;
+	uint32_t t0 = a.m_tile_off[M], nt = a.m_tile_n[M];
+	float best_f = 3.4e38f;
 	double best = 1.7976931348623157e308;
 	uint32_t arg = 0xffffffffu;
-	if (t1 > t0) scan_tile(a, tstar, qx, qy, best, arg);
-	for (uint32_t t = t0; t < t1; t++) {
-		if (t == tstar) continue;
-		float lb = box_lb(a.tile_bb[t], qxf, qyf);
-		if (lb > __double2float_ru(best)) continue;
-		scan_tile(a, t, qx, qy, best, arg);
+	if (uniform) {
+		// the warp's query box
+		float x0 = valid ? q.xf : 3.4e38f, y0 = valid ? q.yf : 3.4e38f;
+		float x1 = valid ? q.xf : -3.4e38f, y1 = valid ? q.yf : -3.4e38f;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
+			y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
+			x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
+			y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
+		}
+		float ubmin = 3.4e38f;
+		for (uint32_t t = lane; t < nt; t += 32) ubmin = fminf(ubmin, box_ub(a.tile_bb[t0 + t], x0, y0, x1, y1));
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) ubmin = fminf(ubmin, __shfl_xor_sync(FULL, ubmin, o));
+		float cut = ubmin * (1.f + 1e-5f);
+		best_f = cut;  // an upper bound of every query's nearest squared distance
+		// FP32 pass over the warp's candidate tiles
+		for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
+			bool cand = c0 + lane < nt && box_lb(a.tile_bb[t0 + c0 + lane], x0, y0, x1, y1) <= cut;
+			unsigned m = __ballot_sync(FULL, cand);
+			while (m) {
+				uint32_t t = t0 + c0 + (__ffs(m) - 1);
+				m &= m - 1;
+				if (valid && box_lb(a.tile_bb[t], q.xf, q.yf, q.xf, q.yf) <= best_f) scan_f32(a, t, q, best_f);
+			}
+		}
+		// exact pass: every tile that can hold a point within the band of some query
+		float thr = best_f * (1.f + 2e-5f) + 1e-37f;
+		float thr_w = valid ? thr : 0.f;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) thr_w = fmaxf(thr_w, __shfl_xor_sync(FULL, thr_w, o));
+		for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
+			bool cand = c0 + lane < nt && box_lb(a.tile_bb[t0 + c0 + lane], x0, y0, x1, y1) <= thr_w;
+			unsigned m = __ballot_sync(FULL, cand);
+			while (m) {
+				uint32_t t = t0 + c0 + (__ffs(m) - 1);
+				m &= m - 1;
+				if (valid && box_lb(a.tile_bb[t], q.xf, q.yf, q.xf, q.yf) <= thr) scan_exact(a, t, q, thr, best, arg);
+			}
+		}
+	} else if (valid) {
+		// mixed masters in this warp (the seam between two slave bodies): query alone
+		for (uint32_t t = 0; t < nt; t++)
+			if (box_lb(a.tile_bb[t0 + t], q.xf, q.yf, q.xf, q.yf) <= best_f) scan_f32(a, t0 + t, q, best_f);
+		float thr = best_f * (1.f + 2e-5f) + 1e-37f;
+		for (uint32_t t = 0; t < nt; t++)
+			if (box_lb(a.tile_bb[t0 + t], q.xf, q.yf, q.xf, q.yf) <= thr) scan_exact(a, t0 + t, q, thr, best, arg);
 	}
+	if (!valid) return;
+	if (arg == 0xffffffffu)  // cannot happen with the bounds above; kept as a full exact fallback
+		for (uint32_t t = 0; t < nt; t++) scan_exact(a, t0 + t, q, 3.4e38f, best, arg);
 	double fx = 0., fy = 0.;
 	if (arg != 0xffffffffu) {
 		double4 cp = a.bnd[arg];
-		double dx = qx - cp.x, dy = qy - cp.y;
+		double dx = q.xd - cp.x, dy = q.yd - cp.y;
 		double pdotn = dx * cp.z + dy * cp.w;
 		if (pdotn <= 0.) {
 			double gN_nx = cp.z * pdotn, gN_ny = cp.w * pdotn;

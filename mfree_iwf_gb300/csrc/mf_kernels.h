@@ -27,6 +27,7 @@ struct BodyParams {
 // Per-body cell geometry of one derivative evaluation (grid.h:83-115).
 struct Geom {
 	double bbmin_x, bbmin_y, dx;
+	double slack;  // mixed form: how far a particle may move within the step (dx - 2 h_max)/2
 	uint32_t nx, ny, num_cell, cell_off;
 };
 
@@ -51,7 +52,7 @@ struct ULArgs {
 	double nbh_eps;
 	const BodyParams* params;             // device
 	Geom* geom;                           // device, per body
-	unsigned long long* bbox;             // device, 5 per body
+	unsigned long long* bbox;             // device, 6 per body
 	uint32_t* total_cells;                // device scalar
 	const uint32_t* body_of;              // device, per row
 	const double *m, *h, *qw0, *fcx, *fcy;  // constants (home order)
@@ -65,6 +66,11 @@ struct ULArgs {
 	int sort_bits;
 	mfk_host::DevStatusH* status;
 	cudaEvent_t ev_pair0, ev_pair1;       // optional timing of the pair kernel
+	// launch shape of the pair kernel (autotuned): rows per block, and, when
+	// persistent, a fixed grid whose blocks pull chunks of `chunk` blocks' worth of
+	// rows from the atomic counter `work` until all rows are done
+	uint32_t block, persistent, grid, chunk;
+	uint32_t* work;
 };
 
 // Neighbour search of the total-Lagrangian set-up (find_neighbors,
@@ -95,13 +101,21 @@ struct TLArgs {
 	const double *X, *Y, *m, *h, *qw0, *fcx, *fcy;
 	const void *qw32, *m32, *h32;       // mixed form: float copies of the constants
 	StateSoA base, acc, st, nxt;         // st: this stage's state, nxt: the next stage's
-	const uint32_t *nbr_off, *nbr;
-	const void *wx, *wy;                 // corrected kernel gradient per pair
-	void *P, *dA, *c, *pack;             // per-stage scratch
+	// neighbour lists in sliced-ELL form: rows in slices of 32, entry k of row r of
+	// slice s at sl_off[s] + 32*k + (r % 32); cnt[r] entries per row, ascending j
+	const uint32_t* sl_off;
+	const uint16_t* cnt;
+	const uint32_t* snbr;
+	const void* sw;                      // corrected gradient per pair: double2 (FP64 forms) / float2 (mixed)
+	const void* swA;                     // mixed: the gradient times the neighbour's quad weight (pass A)
+	void *P, *dA, *c;                    // per-stage scratch (FP64 forms)
+	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
+	void* dA32;                          // mixed: rate terms (float4 per row)
 	const uint32_t* bc_rows;
 	const double* bc_v;
 	uint32_t n_bc;
 	void* status;
+	uint32_t block;                      // rows per block of the pair passes (autotuned)
 };
 
 // Contact: boundary points of all bodies, their 32-point tiles, and the slave rows
@@ -110,6 +124,7 @@ struct ContactArgs {
 	uint32_t n_bnd, n_tiles, n_slave;
 	const uint32_t *bnd_rows, *bnd_start, *bnd_len;   // per boundary point
 	double4* bnd;                                       // x, y, nx, ny
+	float4* bnd_ff;                                     // x, y as float-float pairs
 	const uint32_t *tile_first, *tile_end;
 	float4* tile_bb;
 	const uint32_t *slave_rows, *slave_master;
@@ -134,6 +149,9 @@ struct ContactArgs {
 	                  const double* m, const double* rho, const float* rho_f, const double* h, double* wx,   \
 	                  double* wy, void* status, cudaStream_t s);                                             \
 	cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s);                             \
+	cudaError_t tl_to_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy, \
+	                       const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* sw64, void* sw32,     \
+	                       void* swA32, const double* qw, cudaStream_t s);                                    \
 	cudaError_t tl_stage(const mfk_host::TLArgs& a, bool mixed, int part, cudaStream_t s);                   \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
 	}

@@ -46,7 +46,7 @@ constexpr size_t OFF_STATUS = 0;
 constexpr size_t OFF_PARAMS = align_up(OFF_STATUS + sizeof(DevStatusH));
 constexpr size_t OFF_GEOM = align_up(OFF_PARAMS + sizeof(BodyParams));
 constexpr size_t OFF_BBOX = align_up(OFF_GEOM + sizeof(Geom));
-constexpr size_t OFF_TOTAL = align_up(OFF_BBOX + 5 * sizeof(unsigned long long));
+constexpr size_t OFF_TOTAL = align_up(OFF_BBOX + 6 * sizeof(unsigned long long));
 constexpr size_t OFF_KEYS = align_up(OFF_TOTAL + sizeof(uint32_t));
 constexpr size_t OFF_KEYS_SORTED = align_up(OFF_KEYS + 4ull * kMaxN);
 constexpr size_t OFF_PERM_IN = align_up(OFF_KEYS_SORTED + 4ull * kMaxN);

@@ -195,36 +195,39 @@ __device__ __forceinline__ void tl_particle(uint32_t flags, const BodyParams& pr
 	if (flags & A_C2N) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
 }
 
+// Sliced-ELL addressing: the 32 rows of a warp read entry k of their lists from 32
+// consecutive slots, so every per-pair load of the warp is one coalesced request.
+__device__ __forceinline__ uint32_t sell_base(const TLArgs& a, uint32_t i) { return a.sl_off[i >> 5] + (i & 31u); }
+
 // ---- FP64 pass A
-__global__ void __launch_bounds__(128) k_tlA64(TLArgs a) {
+__global__ void __launch_bounds__(256) k_tlA64(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	const double* wx = (const double*)a.wx;
-	const double* wy = (const double*)a.wy;
+	const double2* sw = (const double2*)a.sw;
 	uint32_t flags = a.flags;
 	double uxi = s.x[i] - a.X[i], uyi = s.y[i] - a.Y[i];
 	double vxi = s.vx[i], vyi = s.vy[i];
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
 	double Fxx = 0., Fxy = 0., Fyx = 0., Fyy = 0.;
-	uint32_t q1 = a.nbr_off[i + 1];
-	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
-		uint32_t j = a.nbr[q];
-		double wxq = wx[q], wyq = wy[q];
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		double2 w = sw[q];
 		double qwj = a.qw0[j];
 		if (flags & A_DISP) {
 			double uxj = s.x[j] - a.X[j], uyj = s.y[j] - a.Y[j];
-			Hxx += (uxj - uxi) * wxq * qwj;
-			Hxy += (uxj - uxi) * wyq * qwj;
-			Hyx += (uyj - uyi) * wxq * qwj;
-			Hyy += (uyj - uyi) * wyq * qwj;
+			Hxx += (uxj - uxi) * w.x * qwj;
+			Hxy += (uxj - uxi) * w.y * qwj;
+			Hyx += (uyj - uyi) * w.x * qwj;
+			Hyy += (uyj - uyi) * w.y * qwj;
 		}
 		if (flags & A_VEL_TL) {
 			double vxj = s.vx[j], vyj = s.vy[j];
-			Fxx += (vxj - vxi) * wxq * qwj;
-			Fxy += (vxj - vxi) * wyq * qwj;
-			Fyx += (vyj - vyi) * wxq * qwj;
-			Fyy += (vyj - vyi) * wyq * qwj;
+			Fxx += (vxj - vxi) * w.x * qwj;
+			Fxy += (vxj - vxi) * w.y * qwj;
+			Fyx += (vyj - vyi) * w.x * qwj;
+			Fyy += (vyj - vyi) * w.y * qwj;
 		}
 	}
 	const BodyParams& pr = a.params[a.body_of[i]];
@@ -241,12 +244,11 @@ __global__ void __launch_bounds__(128) k_tlA64(TLArgs a) {
 }
 
 // ---- FP64 pass B + RK update
-__global__ void __launch_bounds__(128) k_tlB64(TLArgs a) {
+__global__ void __launch_bounds__(256) k_tlB64(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	const double* wx = (const double*)a.wx;
-	const double* wy = (const double*)a.wy;
+	const double2* sw = (const double2*)a.sw;
 	const double* P = (const double*)a.P;
 	const double* cc = (const double*)a.c;
 	uint32_t n = a.n_total;
@@ -258,16 +260,16 @@ __global__ void __launch_bounds__(128) k_tlB64(TLArgs a) {
 	double xi = s.x[i], yi = s.y[i], vxi = s.vx[i], vyi = s.vy[i], hi = a.h[i], rhoi = s.rho[i], ci = cc[i];
 	double alpha = pr.alpha, beta = pr.beta, eta = pr.eta;
 	double Pxx_x = 0., Pyx_y = 0., Pxy_x = 0., Pyy_y = 0., av_x = 0., av_y = 0.;
-	uint32_t q1 = a.nbr_off[i + 1];
-	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
-		uint32_t j = a.nbr[q];
-		double wxq = wx[q], wyq = wy[q];
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		double2 w = sw[q];
 		double mj = a.m[j];
 		if (flags & A_STRESS_TL) {
-			Pxx_x += mj * (Pxxi * r21 + P[j] * r21) * wxq * rho0;
-			Pyx_y += mj * (Pyxi * r21 + P[2 * n + j] * r21) * wyq * rho0;
-			Pxy_x += mj * (Pxyi * r21 + P[n + j] * r21) * wxq * rho0;
-			Pyy_y += mj * (Pyyi * r21 + P[3 * n + j] * r21) * wyq * rho0;
+			Pxx_x += mj * (Pxxi * r21 + P[j] * r21) * w.x * rho0;
+			Pyx_y += mj * (Pyxi * r21 + P[2 * n + j] * r21) * w.y * rho0;
+			Pxy_x += mj * (Pxyi * r21 + P[n + j] * r21) * w.x * rho0;
+			Pyy_y += mj * (Pyyi * r21 + P[3 * n + j] * r21) * w.y * rho0;
 		}
 		if (flags & A_ART_VISC) {
 			double vijx = vxi - s.vx[j], vijy = vyi - s.vy[j];
@@ -280,8 +282,8 @@ __global__ void __launch_bounds__(128) k_tlB64(TLArgs a) {
 				double r2ij = xij * xij + yij * yij;
 				double muij = (hij * vijposij) / (r2ij + eta * eta * hij * hij);
 				double piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
-				av_x += -mj * piij * wxq;
-				av_y += -mj * piij * wyq;
+				av_x += -mj * piij * w.x;
+				av_y += -mj * piij * w.y;
 			}
 		}
 	}
@@ -298,80 +300,87 @@ __global__ void __launch_bounds__(128) k_tlB64(TLArgs a) {
 	d[4] = dA[i]; d[5] = dA[n + i]; d[6] = dA[2 * n + i]; d[7] = dA[3 * n + i];
 	double* bp[8] = {a.base.x, a.base.y, a.base.vx, a.base.vy, a.base.rho, a.base.Sxx, a.base.Sxy, a.base.Syy};
 	double* ap[8] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy, a.acc.rho, a.acc.Sxx, a.acc.Sxy, a.acc.Syy};
-	double* sp[8] = {a.st.x, a.st.y, a.st.vx, a.st.vy, a.st.rho, a.st.Sxx, a.st.Sxy, a.st.Syy};
+	double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
 	uint32_t stg = a.stage;
 	double dt = pr.dt;
 	if (stg < 3) {
 		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
-		// the next stage state goes to nxt (ping-pong), read by the next stage
-		double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
 #pragma unroll
-		for (int q = 0; q < 8; q++) {
-			ap[q][i] = (stg == 0) ? d[q] : ap[q][i] + 2 * d[q];
-			np[q][i] = bp[q][i] + d[q] * dts;
+		for (int q2 = 0; q2 < 8; q2++) {
+			ap[q2][i] = (stg == 0) ? d[q2] : ap[q2][i] + 2 * d[q2];
+			np[q2][i] = bp[q2][i] + d[q2] * dts;  // the next stage state (ping-pong set)
 		}
 	} else {
 		double w6 = dt * 1. / 6.;
-		double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
 #pragma unroll
-		for (int q = 0; q < 8; q++) {
-			double v = bp[q][i] + w6 * (ap[q][i] + d[q]);
-			bp[q][i] = v;
-			np[q][i] = v;  // the next step's first stage starts from a copy of the particles
+		for (int q2 = 0; q2 < 8; q2++) {
+			double v = bp[q2][i] + w6 * (ap[q2][i] + d[q2]);
+			bp[q2][i] = v;
+			np[q2][i] = v;  // the next step's first stage starts from a copy of the particles
 		}
 		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
 			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
 	}
-	(void)sp;
 }
 
-// ---- mixed form: pack the stage state into float-float / float arrays
+// ---- mixed form
+// recA[i] = displacement u = x - X as float-float (16 B).
+// recB[i] = { P (pass A output), x and y as float-float, vx and vy as float-float,
+//             h, m, rho, c = sqrt(K/rho) } (64 B): everything pass B reads of a neighbour.
+struct __align__(16) RecB {
+	float4 P, x, v, hmrc;
+};
+
 __global__ void k_tl_pack(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	double x = s.x[i], y = s.y[i];
-	FF* pk = (FF*)a.pack;
-	uint32_t n = a.n_total;
-	pk[i] = ff_split(x - a.X[i]);
-	pk[n + i] = ff_split(y - a.Y[i]);
-	pk[2 * n + i] = ff_split(x);
-	pk[3 * n + i] = ff_split(y);
-	pk[4 * n + i] = ff_split(s.vx[i]);
-	pk[5 * n + i] = ff_split(s.vy[i]);
+	double x = s.x[i], y = s.y[i], vx = s.vx[i], vy = s.vy[i];
+	FF ux = ff_split(x - a.X[i]), uy = ff_split(y - a.Y[i]);
+	((float4*)a.recA)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+	FF fx = ff_split(x), fy = ff_split(y), fvx = ff_split(vx), fvy = ff_split(vy);
+	RecB* rb = (RecB*)a.recB + i;
+	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
+	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
+	float rho = s.rho_f[i];
+	float K = (float)a.params[a.body_of[i]].K;
+	rb->hmrc = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
 }
 
-__global__ void __launch_bounds__(128) k_tlA32(TLArgs a) {
+__device__ __forceinline__ float ffd(float ahi, float alo, float bhi, float blo) { return (ahi - bhi) + (alo - blo); }
+
+__global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	const float* wx = (const float*)a.wx;
-	const float* wy = (const float*)a.wy;
-	const FF* pk = (const FF*)a.pack;
-	const float* qw = (const float*)a.qw32;
-	uint32_t n = a.n_total;
+	const float2* swA = (const float2*)a.swA;
+	const float4* recA = (const float4*)a.recA;
+	const RecB* recB = (const RecB*)a.recB;
 	uint32_t flags = a.flags;
-	FF uxi = pk[i], uyi = pk[n + i], vxi = pk[4 * n + i], vyi = pk[5 * n + i];
+	float4 ui = recA[i];
+	float4 vi = recB[i].v;
 	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
 	float Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
-	uint32_t q1 = a.nbr_off[i + 1];
-	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
-		uint32_t j = a.nbr[q];
-		float qwj = qw[j];
-		float wxq = wx[q] * qwj, wyq = wy[q] * qwj;
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+#pragma unroll 2
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		float2 w = swA[q];  // corrected gradient times the neighbour's quad weight
 		if (flags & A_DISP) {
-			float dux = ff_diff(pk[j], uxi), duy = ff_diff(pk[n + j], uyi);
-			Hxx += dux * wxq;
-			Hxy += dux * wyq;
-			Hyx += duy * wxq;
-			Hyy += duy * wyq;
+			float4 uj = __ldg(recA + j);
+			float dux = ffd(uj.x, uj.y, ui.x, ui.y), duy = ffd(uj.z, uj.w, ui.z, ui.w);
+			Hxx += dux * w.x;
+			Hxy += dux * w.y;
+			Hyx += duy * w.x;
+			Hyy += duy * w.y;
 		}
 		if (flags & A_VEL_TL) {
-			float dvx = ff_diff(pk[4 * n + j], vxi), dvy = ff_diff(pk[5 * n + j], vyi);
-			Fxx += dvx * wxq;
-			Fxy += dvx * wyq;
-			Fyx += dvy * wxq;
-			Fyy += dvy * wyq;
+			float4 vj = __ldg(&recB[j].v);
+			float dvx = ffd(vj.x, vj.y, vi.x, vi.y), dvy = ffd(vj.z, vj.w, vi.z, vi.w);
+			Fxx += dvx * w.x;
+			Fxy += dvx * w.y;
+			Fyx += dvy * w.x;
+			Fyy += dvy * w.y;
 		}
 	}
 	const BodyParams& pr = a.params[a.body_of[i]];
@@ -380,64 +389,58 @@ __global__ void __launch_bounds__(128) k_tlA32(TLArgs a) {
 	// the 2x2 inversions of the per-particle part stay FP64
 	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
 	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
-	float4* P = (float4*)a.P;
-	P[i] = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
-	float4* dA = (float4*)a.dA;
-	dA[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
-	((float*)a.c)[i] = (float)sqrt(pr.K / rho);
+	((RecB*)a.recB)[i].P = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
+	((float4*)a.dA32)[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
 }
 
-__global__ void __launch_bounds__(128) k_tlB32(TLArgs a) {
+__global__ void __launch_bounds__(256) k_tlB32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	const float* wx = (const float*)a.wx;
-	const float* wy = (const float*)a.wy;
-	const float4* P = (const float4*)a.P;
-	const float* cc = (const float*)a.c;
-	const FF* pk = (const FF*)a.pack;
-	const float* mf = (const float*)a.m32;
-	const float* hf = (const float*)a.h32;
-	uint32_t n = a.n_total;
+	const float2* sw = (const float2*)a.sw;
+	const RecB* recB = (const RecB*)a.recB;
 	uint32_t flags = a.flags;
 	const BodyParams& pr = a.params[a.body_of[i]];
 	float rho0 = (float)pr.rho0;
-	float4 Pi = P[i];
 	float r21 = 1.f / (rho0 * rho0);
-	FF xi = pk[2 * n + i], yi = pk[3 * n + i], vxi = pk[4 * n + i], vyi = pk[5 * n + i];
-	float hi = hf[i], rhoi = s.rho_f[i], ci = cc[i];
+	float sc = r21 * rho0;
+	RecB ri = recB[i];
 	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
 	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
-	uint32_t q1 = a.nbr_off[i + 1];
-	for (uint32_t q = a.nbr_off[i]; q < q1; q++) {
-		uint32_t j = a.nbr[q];
-		float wxq = wx[q], wyq = wy[q];
-		float mj = mf[j];
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+#pragma unroll 2
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		float2 w = sw[q];
+		const RecB* rj = recB + j;
+		float4 hmrc = __ldg(&rj->hmrc);
+		float mj = hmrc.y;
 		if (flags & A_STRESS_TL) {
-			float4 Pj = P[j];
-			float fx = mj * r21 * rho0 * wxq, fy = mj * r21 * rho0 * wyq;
-			Pxx_x += (Pi.x + Pj.x) * fx;
-			Pyx_y += (Pi.z + Pj.z) * fy;
-			Pxy_x += (Pi.y + Pj.y) * fx;
-			Pyy_y += (Pi.w + Pj.w) * fy;
+			float4 Pj = __ldg(&rj->P);
+			float fx = mj * sc * w.x, fy = mj * sc * w.y;
+			Pxx_x += (ri.P.x + Pj.x) * fx;
+			Pyx_y += (ri.P.z + Pj.z) * fy;
+			Pxy_x += (ri.P.y + Pj.y) * fx;
+			Pyy_y += (ri.P.w + Pj.w) * fy;
 		}
 		if (flags & A_ART_VISC) {
-			float vijx = ff_diff(vxi, pk[4 * n + j]), vijy = ff_diff(vyi, pk[5 * n + j]);
-			float xij = ff_diff(xi, pk[2 * n + j]), yij = ff_diff(yi, pk[3 * n + j]);
+			float4 xj = __ldg(&rj->x), vj = __ldg(&rj->v);
+			float xij = ffd(ri.x.x, ri.x.y, xj.x, xj.y), yij = ffd(ri.x.z, ri.x.w, xj.z, xj.w);
+			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
 			float vijposij = vijx * xij + vijy * yij;
 			if (vijposij < 0.f) {
-				float cij = 0.5f * (ci + cc[j]);
-				float hij = 0.5f * (hi + hf[j]);
-				float rhoij = 0.5f * (rhoi + s.rho_f[j]);
+				float cij = 0.5f * (ri.hmrc.w + hmrc.w);
+				float hij = 0.5f * (ri.hmrc.x + hmrc.x);
+				float rhoij = 0.5f * (ri.hmrc.z + hmrc.z);
 				float r2ij = xij * xij + yij * yij;
 				float muij = (hij * vijposij) / (r2ij + eta2 * hij * hij);
 				float piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
-				av_x += -mj * piij * wxq;
-				av_y += -mj * piij * wyq;
+				av_x += -mj * piij * w.x;
+				av_y += -mj * piij * w.y;
 			}
 		}
 	}
-	float4 dAi = ((const float4*)a.dA)[i];
+	float4 dAi = ((const float4*)a.dA32)[i];
 	double d[4];
 	d[0] = (flags & A_ADVECTION) ? s.vx[i] : 0.;
 	d[1] = (flags & A_ADVECTION) ? s.vy[i] : 0.;
@@ -459,25 +462,47 @@ __global__ void __launch_bounds__(128) k_tlB32(TLArgs a) {
 	if (stg < 3) {
 		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
 #pragma unroll
-		for (int q = 0; q < 4; q++) {
-			ap[q][i] = (stg == 0) ? d[q] : ap[q][i] + 2 * d[q];
-			np[q][i] = bp[q][i] + d[q] * dts;
-			aq[q][i] = (stg == 0) ? e[q] : aq[q][i] + 2.f * e[q];
-			nq[q][i] = bq[q][i] + e[q] * (float)dts;
+		for (int q2 = 0; q2 < 4; q2++) {
+			ap[q2][i] = (stg == 0) ? d[q2] : ap[q2][i] + 2 * d[q2];
+			np[q2][i] = bp[q2][i] + d[q2] * dts;
+			aq[q2][i] = (stg == 0) ? e[q2] : aq[q2][i] + 2.f * e[q2];
+			nq[q2][i] = bq[q2][i] + e[q2] * (float)dts;
 		}
 	} else {
 		double w6 = dt * 1. / 6.;
 #pragma unroll
-		for (int q = 0; q < 4; q++) {
-			double v = bp[q][i] + w6 * (ap[q][i] + d[q]);
-			bp[q][i] = v;
-			np[q][i] = v;
-			float f = bq[q][i] + (float)w6 * (aq[q][i] + e[q]);
-			bq[q][i] = f;
-			nq[q][i] = f;
+		for (int q2 = 0; q2 < 4; q2++) {
+			double v = bp[q2][i] + w6 * (ap[q2][i] + d[q2]);
+			bp[q2][i] = v;
+			np[q2][i] = v;
+			float f = bq[q2][i] + (float)w6 * (aq[q2][i] + e[q2]);
+			bq[q2][i] = f;
+			nq[q2][i] = f;
 		}
 		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
 			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+}
+
+// CSR (set-up order) -> sliced ELL; the mixed form also gets FP32 gradients and the
+// pass-A gradients pre-multiplied by the neighbour's quad weight (in FP64, then rounded).
+__global__ void k_to_sell(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                          const double* __restrict__ wx, const double* __restrict__ wy, const uint32_t* __restrict__ sl_off,
+                          uint16_t* cnt, uint32_t* snbr, double2* sw64, float2* sw32, float2* swA32,
+                          const double* __restrict__ qw) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t base = sl_off[i >> 5] + (i & 31u);
+	uint32_t q0 = off[i], c = off[i + 1] - q0;
+	cnt[i] = (uint16_t)c;
+	for (uint32_t k = 0; k < c; k++) {
+		uint32_t q = base + 32 * k;
+		uint32_t j = nbr[q0 + k];
+		snbr[q] = j;
+		double gx = wx[q0 + k], gy = wy[q0 + k];
+		if (sw64) sw64[q] = make_double2(gx, gy);
+		if (sw32) sw32[q] = make_float2((float)gx, (float)gy);
+		if (swA32) swA32[q] = make_float2((float)(gx * qw[j]), (float)(gy * qw[j]));
 	}
 }
 
@@ -521,6 +546,14 @@ cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s) {
 	return cudaGetLastError();
 }
 
+cudaError_t tl_to_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy,
+                       const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* sw64, void* sw32, void* swA32,
+                       const double* qw, cudaStream_t s) {
+	k_to_sell<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, wx, wy, sl_off, cnt, snbr, (double2*)sw64, (float2*)sw32,
+	                                        (float2*)swA32, qw);
+	return cudaGetLastError();
+}
+
 cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	// part 0: BCs on the stage state, 1: pack (mixed), 2: pass A, 3: pass B,
 	// 4: BCs on the particles after the combine, 5: advance the body clocks
@@ -531,14 +564,18 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	case 1:
 		if (mixed) k_tl_pack<<<grid1(a.n_total, 256), 256, 0, s>>>(a);
 		break;
-	case 2:
-		if (mixed) k_tlA32<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
-		else k_tlA64<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+	case 2: {
+		unsigned bs = a.block ? a.block : 128;
+		if (mixed) k_tlA32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else k_tlA64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
-	case 3:
-		if (mixed) k_tlB32<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
-		else k_tlB64<<<grid1(a.n_total, 128), 128, 0, s>>>(a);
+	}
+	case 3: {
+		unsigned bs = a.block ? a.block : 128;
+		if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else k_tlB64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
+	}
 	case 4:
 		if (a.n_bc) k_tl_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 1);
 		break;

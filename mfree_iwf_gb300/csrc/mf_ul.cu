@@ -88,31 +88,30 @@ __device__ __forceinline__ Rec32 load_rec(const Rec32* p) {
 __global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
 	uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
 	if (b >= nb) return;
-	bb[5 * b + 0] = ord_encode(1.7976931348623157e308);   // min x
-	bb[5 * b + 1] = ord_encode(1.7976931348623157e308);   // min y
-	bb[5 * b + 2] = ord_encode(-1.7976931348623157e308);  // max x
-	bb[5 * b + 3] = ord_encode(-1.7976931348623157e308);  // max y
-	bb[5 * b + 4] = ord_encode(-1.7976931348623157e308);  // h_max (or the mixed-form reach)
+	bb[6 * b + 0] = ord_encode(1.7976931348623157e308);   // min x
+	bb[6 * b + 1] = ord_encode(1.7976931348623157e308);   // min y
+	bb[6 * b + 2] = ord_encode(-1.7976931348623157e308);  // max x
+	bb[6 * b + 3] = ord_encode(-1.7976931348623157e308);  // max y
+	bb[6 * b + 4] = ord_encode(-1.7976931348623157e308);  // h_max
+	bb[6 * b + 5] = ord_encode(0.);                       // max |v| (mixed form)
 }
 
 // Bounding box and h_max per body (grid.h:83-104).  Rows of a body are contiguous,
 // so a warp whose rows share one body reduces in registers and issues one atomic
-// per quantity.  In the mixed form the fifth slot holds h + 4|v|dt (the reach a
-// particle can have within one step), which sizes cells valid for all four stages.
+// per quantity.  The mixed form also takes the largest speed, which sizes cells that
+// stay valid for all four stages of a step.
 __global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ h, const double* __restrict__ vx, const double* __restrict__ vy,
-                       const uint32_t* __restrict__ body_of, const BodyParams* __restrict__ P, int mixed,
-                       unsigned long long* bb) {
+                       const uint32_t* __restrict__ body_of, int mixed, unsigned long long* bb) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool valid = i < n;
 	uint32_t b = valid ? body_of[i] : 0xffffffffu;
-	unsigned long long mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull, mh = 0ull;
+	unsigned long long mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull, mh = 0ull, mv = 0ull;
 	if (valid) {
 		mnx = mxx = ord_encode(x[i]);
 		mny = mxy = ord_encode(y[i]);
-		double hh = h[i];
-		if (mixed) hh = hh + 4.0 * sqrt(vx[i] * vx[i] + vy[i] * vy[i]) * P[b].dt;
-		mh = ord_encode(hh);
+		mh = ord_encode(h[i]);
+		mv = mixed ? ord_encode(sqrt(vx[i] * vx[i] + vy[i] * vy[i])) : ord_encode(0.);
 	}
 	uint32_t lane = threadIdx.x & 31;
 	uint32_t b0 = __shfl_sync(0xffffffffu, b, 0);
@@ -125,20 +124,23 @@ __global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* _
 			mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
 			mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
 			mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+			mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
 		}
 		if (lane == 0) {
-			atomicMin(&bb[5 * b0 + 0], mnx);
-			atomicMin(&bb[5 * b0 + 1], mny);
-			atomicMax(&bb[5 * b0 + 2], mxx);
-			atomicMax(&bb[5 * b0 + 3], mxy);
-			atomicMax(&bb[5 * b0 + 4], mh);
+			atomicMin(&bb[6 * b0 + 0], mnx);
+			atomicMin(&bb[6 * b0 + 1], mny);
+			atomicMax(&bb[6 * b0 + 2], mxx);
+			atomicMax(&bb[6 * b0 + 3], mxy);
+			atomicMax(&bb[6 * b0 + 4], mh);
+			atomicMax(&bb[6 * b0 + 5], mv);
 		}
 	} else if (valid) {
-		atomicMin(&bb[5 * b + 0], mnx);
-		atomicMin(&bb[5 * b + 1], mny);
-		atomicMax(&bb[5 * b + 2], mxx);
-		atomicMax(&bb[5 * b + 3], mxy);
-		atomicMax(&bb[5 * b + 4], mh);
+		atomicMin(&bb[6 * b + 0], mnx);
+		atomicMin(&bb[6 * b + 1], mny);
+		atomicMax(&bb[6 * b + 2], mxx);
+		atomicMax(&bb[6 * b + 3], mxy);
+		atomicMax(&bb[6 * b + 4], mh);
+		atomicMax(&bb[6 * b + 5], mv);
 	}
 }
 
@@ -155,12 +157,18 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 		uint32_t cnt = 0;
 		Geom g{};
 		if (b < nb) {
-			double bminx = ord_decode(bb[5 * b + 0]), bminy = ord_decode(bb[5 * b + 1]);
-			double bmaxx = ord_decode(bb[5 * b + 2]), bmaxy = ord_decode(bb[5 * b + 3]);
-			double hmax = ord_decode(bb[5 * b + 4]);
+			double bminx = ord_decode(bb[6 * b + 0]), bminy = ord_decode(bb[6 * b + 1]);
+			double bmaxx = ord_decode(bb[6 * b + 2]), bmaxy = ord_decode(bb[6 * b + 3]);
+			double hmax = ord_decode(bb[6 * b + 4]);
 			bminx -= 1e-6; bminy -= 1e-6;
 			bmaxx += 1e-6; bmaxy += 1e-6;
 			double dx = hmax * 2.;
+			double slack = 0.;
+			if (mixed) {
+				// a particle moves at most ~ |v| dt per step; allow twice the fastest speed
+				slack = 2. * ord_decode(bb[6 * b + 5]) * P[b].dt;
+				dx = 2. * hmax + 2. * slack;
+			}
 			double lx = bmaxx - bminx, ly = bmaxy - bminy;
 			double fnx = ceil(lx / dx), fny = ceil(ly / dx);
 			uint32_t nx = (uint32_t)fnx, ny = (uint32_t)fny;
@@ -173,7 +181,7 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 				nx = ny = 1;
 				num_cell = 1;
 			}
-			g.bbmin_x = bminx; g.bbmin_y = bminy; g.dx = dx;
+			g.bbmin_x = bminx; g.bbmin_y = bminy; g.dx = dx; g.slack = slack;
 			g.nx = nx; g.ny = ny; g.num_cell = num_cell;
 			cnt = num_cell;
 		}
@@ -420,10 +428,8 @@ __device__ __forceinline__ void stencil(const Geom& g, uint32_t key, int& lo_i, 
 }
 
 // ----------------------------------------------------------- pair kernel FP64
-__global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __restrict__ P,
-                                                const Geom* __restrict__ G, DevStatus* st) {
-	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-	if (k >= a.n_total) return;
+__device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __restrict__ P,
+                                           const Geom* __restrict__ G, DevStatus* st, uint32_t k) {
 	const Rec64* rec = reinterpret_cast<const Rec64*>(a.rec);
 	const Rec64 ri = load_rec(rec + k);
 	uint32_t b = a.rec_body[k];
@@ -533,10 +539,8 @@ __global__ void __launch_bounds__(128) k_pair64(ULArgs a, const BodyParams* __re
 }
 
 // ---------------------------------------------------------- pair kernel mixed
-__global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __restrict__ P,
-                                                const Geom* __restrict__ G, DevStatus* st) {
-	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-	if (k >= a.n_total) return;
+__device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __restrict__ P,
+                                           const Geom* __restrict__ G, DevStatus* st, uint32_t k) {
 	const Rec32* rec = reinterpret_cast<const Rec32*>(a.rec);
 	const Rec32 ri = load_rec(rec + k);
 	uint32_t b = a.rec_body[k];
@@ -635,6 +639,11 @@ __global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __re
 		d[2] += 1.f / rhoi * (Sxx_x + Sxy_y) + (float)(a.fcx[i] / (double)ri.m);
 		d[3] += 1.f / rhoi * (Sxy_x + Syy_y) + (float)(a.fcy[i] / (double)ri.m);
 	}
+	if (a.stage > 0) {
+		// the cells were sized at stage 0 for moves up to g.slack; check that held
+		double mx = a.st.x[i] - a.base.x[i], my = a.st.y[i] - a.base.y[i];
+		if (mx * mx + my * my > g.slack * g.slack) raise(st, ERR_GRID, i);
+	}
 	// advection: the FP64 velocity enters the FP64 position update below
 	double dd0 = (double)d[0], dd1 = (double)d[1];
 	if (flags & A_ADVECTION) {
@@ -673,6 +682,38 @@ __global__ void __launch_bounds__(128) k_pair32(ULArgs a, const BodyParams* __re
 		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i]) &&
 		      isfinite(bq[0][i])))
 			raise(st, ERR_NONFINITE, i);
+	}
+}
+
+// The pair kernels.  Plain form: one thread per cell-ordered row.  Persistent form
+// (one launch per stage over all bodies): a fixed grid whose blocks take chunks of
+// rows -- consecutive cell-ordered rows, so a chunk is a run of cells of one body --
+// from an atomic counter until the rows run out; no block ever waits on another.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_pair(ULArgs a, const BodyParams* __restrict__ P, const Geom* __restrict__ G,
+                                              DevStatus* st) {
+	if (!a.persistent) {
+		uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+		if (k >= a.n_total) return;
+		if (MIXED) pair32_row(a, P, G, st, k);
+		else pair64_row(a, P, G, st, k);
+		return;
+	}
+	__shared__ uint32_t s_chunk;
+	const uint32_t rows = blockDim.x * a.chunk;
+	for (;;) {
+		if (threadIdx.x == 0) s_chunk = atomicAdd(a.work, 1u);
+		__syncthreads();
+		uint64_t base = (uint64_t)s_chunk * rows;
+		__syncthreads();
+		if (base >= a.n_total) break;
+		for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) {
+			uint64_t k = base + r;
+			if (k < a.n_total) {
+				if (MIXED) pair32_row(a, P, G, st, (uint32_t)k);
+				else pair64_row(a, P, G, st, (uint32_t)k);
+			}
+		}
 	}
 }
 
@@ -716,8 +757,8 @@ cudaError_t build_grid(const ULArgs& a, bool mixed, cudaStream_t s) {
 	DevStatus* st = reinterpret_cast<DevStatus*>(a.status);
 	k_bbox_init<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, a.bbox);
 	const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
-	k_bbox<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.h, sv.vx, sv.vy, a.body_of, a.params,
-	                                              mixed ? 1 : 0, a.bbox);
+	k_bbox<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.h, sv.vx, sv.vy, a.body_of, mixed ? 1 : 0,
+	                                              a.bbox);
 	k_geom<<<1, 1024, 0, s>>>(a.n_bodies, a.bbox, a.params, mixed ? 1 : 0, a.geom, a.total_cells, a.n_total + 1, st);
 	k_hash<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.body_of, a.geom, a.total_cells, a.keys,
 	                                              a.perm_in, st);
@@ -752,11 +793,17 @@ cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
 	} else {
 		k_gather64<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
 	}
+	unsigned bs = a.block ? a.block : 128;
+	unsigned grid = a.persistent ? a.grid : grid1(a.n_total, bs);
+	if (a.persistent) {
+		cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(uint32_t), s);
+		if (e != cudaSuccess) return e;
+	}
 	if (a.ev_pair0) cudaEventRecord(a.ev_pair0, s);
 	if (mixed) {
-		k_pair32<<<grid1(a.n_total, 128), 128, 0, s>>>(a, a.params, a.geom, st);
+		k_pair<true><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
 	} else {
-		k_pair64<<<grid1(a.n_total, 128), 128, 0, s>>>(a, a.params, a.geom, st);
+		k_pair<false><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
 	}
 	if (a.ev_pair1) cudaEventRecord(a.ev_pair1, s);
 	return cudaGetLastError();

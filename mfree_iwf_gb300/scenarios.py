@@ -71,6 +71,9 @@ class Body:
     bcs: List[BC] = field(default_factory=list)
     ex: int = 0
     ey: int = 0
+    # per-body constants overriding the scenario's (ensembles): keys of Scenario
+    # (E, nu, rho0, dt, wdeltap, ...)
+    params: Dict[str, float] = field(default_factory=dict)
 
     @property
     def n(self) -> int:
@@ -380,6 +383,34 @@ def c3_plate(dx: float = 2e-5, Lx: float = 0.1, Ly: float = 0.02, seed: int = 20
                   alpha=0.0, beta=0.0, eta=0.0, nbh_eps=workload_nbh_eps(dx))
     params.update(kw)
     return tensile_plate(nx, ny, Lx=Lx, method=METHOD_TL_WEAK, name=f"plate dx={dx}", **params)
+
+
+def c4_ensemble(n_instances: int = 512, seed: int = 20261203, dx_range=(2e-4, 1e-3), E_range=(5e6, 5e7),
+                nu_range=(0.3, 0.45), speed_range=(5.0, 40.0), rho0: float = 1200.0) -> Scenario:
+    """Batched ensemble of independent ring impacts, one body per instance, each with its
+    own seeded dx ~ U[0.2, 1] mm, E ~ U[5e6, 5e7] Pa, nu ~ U[0.3, 0.45] and ring speed
+    ~ U[5, 40] m/s (Gray-Monaghan SPH, the ring workload's other constants).  Instance k
+    draws from numpy's PCG64 seeded with seed + k, so any subset is reproducible alone."""
+    bodies = []
+    first = None
+    for k in range(n_instances):
+        rng = np.random.default_rng(seed + k)
+        dx = rng.uniform(*dx_range)
+        E = rng.uniform(*E_range)
+        nu = rng.uniform(*nu_range)
+        speed = rng.uniform(*speed_range)
+        sc = c1_rings(dx=dx, E=E, nu=nu, speed=speed, rho0=rho0)
+        b = sc.bodies[0]
+        b.params = {"E": sc.E, "nu": sc.nu, "rho0": sc.rho0, "dt": sc.dt, "wdeltap": sc.wdeltap, "dx": dx,
+                    "speed": speed}
+        bodies.append(b)
+        if first is None:
+            first = sc
+    ens = Scenario(method=METHOD_UL, bodies=bodies, actions=list(first.actions), dt=first.dt, nu=first.nu, E=first.E,
+                   rho0=rho0, wdeltap=first.wdeltap, corr_exp=first.corr_exp, mghn_eps=first.mghn_eps,
+                   alpha=first.alpha, beta=first.beta, eta=first.eta, xsph_eps=first.xsph_eps,
+                   nbh_eps=first.nbh_eps, name=f"ensemble of {n_instances} ring impacts")
+    return ens
 
 
 # ---------------------------------------------------------------- case files
