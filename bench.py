@@ -53,6 +53,10 @@ def workload(name: str, dx: float | None):
         sc = S.c4_ensemble(512)
         return sc, {"workload": "ensemble of 512 ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
                                 "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
+    if name == "c3":
+        dx = dx or 2e-5
+        return S.c3_plate(dx=dx), {"workload": f"plate tension 0.1 x 0.02 m, weak-form TL + RKPM, dx={dx*1e3:g} mm, "
+                                               "+-1 m/s pull, 1% seeded jitter"}
     if name == "c2":
         dx = dx or 5e-5
         return S.c2_rings_tl(dx=dx), {"workload": f"ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx={dx*1e3:g} mm"}
@@ -126,6 +130,9 @@ def cpu_sample(workload_name: str, steps: int, warmup: int, procs: int):
     if workload_name == "c2":
         sc = S.c2_rings_tl(dx=4e-4)
         desc = "same ring-impact TL set-up at dx=0.4 mm"
+    elif workload_name == "c3":
+        sc = S.c3_plate(dx=5e-4)
+        desc = "same weak-form plate set-up at dx=0.5 mm"
     else:
         sc = S.c1_rings(dx=1e-3)
         desc = "the ring workload at dx=1 mm"
@@ -206,7 +213,7 @@ def ours(args, cfg_desc):
 
     sc, cfg = workload(args.workload, args.dx)
     n = sc.n_total
-    tl = sc.method == M.METHOD_TL
+    tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"
     sim.step(1)  # set-up (neighbour search, corrections)
@@ -343,7 +350,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--cpu-steps", type=int, default=8)
@@ -359,6 +366,7 @@ def main():
     _, cfg = workload(args.workload, args.dx) if args.impl == "ours" and False else (None, None)
     cfg_desc = {"workload": {"c2": "ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx=0.05 mm",
                              "c1": "ring impact, Gray-Monaghan SPH, dx=1 mm",
+                             "c3": "plate tension, weak-form TL + RKPM, dx=0.02 mm",
                              "c4": "ensemble of 512 ring impacts, Gray-Monaghan SPH"}[args.workload]}
     if args.impl == "reference":
         reference_arm(args, cfg_desc)

@@ -153,6 +153,10 @@ MF_API mf_status mf_add_boundary_condition(mf_ctx* ctx, int32_t body, const uint
                                            double value);
 /* Contact boundary: particle indices of the body's outline, in tour order (body.h:178, boundary.h:37-48). */
 MF_API mf_status mf_set_boundary(mf_ctx* ctx, int32_t body, const uint32_t* idx, uint32_t nb);
+/* MF_METHOD_TL_WEAK: the body's particles are the nodes of element_map_rectangle(ex, ey)
+ * ((ex+1)*(ey+1) particles, ex+1 per row) with 2x2 Gauss points per element, whose h
+ * and rho are gp_h and gp_rho (gauss_int, tensile.cpp:776-795). */
+MF_API mf_status mf_set_gauss_mesh(mf_ctx* ctx, int32_t body, uint32_t ex, uint32_t ey, double gp_h, double gp_rho);
 /* Convex hull (monotone chain, collinear points kept) of n points: the reference's
  * set-up for contact boundaries (convex_hull.h:62-95).  out_idx holds n entries. */
 MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, uint32_t* out_idx, uint32_t* out_n);

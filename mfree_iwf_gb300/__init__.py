@@ -92,6 +92,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_add_action": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
         "mf_add_boundary_condition": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32, C.c_int32, C.c_double]),
         "mf_set_boundary": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32]),
+        "mf_set_gauss_mesh": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_double, C.c_double]),
         "mf_convex_hull": (C.c_int32, [_DP, _DP, C.c_uint32, _UP, _UP]),
         "mf_step": (C.c_int32, [C.c_void_p, C.c_int32]),
         "mf_synchronize": (C.c_int32, [C.c_void_p]),
@@ -218,6 +219,9 @@ class Simulation:
         a = np.ascontiguousarray(idx, np.uint32)
         self._check(self._lib.mf_set_boundary(self._h, body, a.ctypes.data_as(_UP), len(a)), "mf_set_boundary")
 
+    def set_gauss_mesh(self, body: int, ex: int, ey: int, gp_h: float, gp_rho: float) -> None:
+        self._check(self._lib.mf_set_gauss_mesh(self._h, body, ex, ey, gp_h, gp_rho), "mf_set_gauss_mesh")
+
     # -- stepping (mfree_iwf.cpp:84-97)
     def step(self, nsteps: int = 1) -> None:
         self._check(self._lib.mf_step(self._h, int(nsteps)), "mf_step")
@@ -319,4 +323,6 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
             sim.add_boundary_condition(bid, bc.idx, BC_PULL, bc.v)
         if len(b.hull):
             sim.set_boundary(bid, b.hull)
+        if sc.method == METHOD_TL_WEAK:
+            sim.set_gauss_mesh(bid, b.ex, b.ey, sc.gp_h, sc.gp_rho)
     return sim

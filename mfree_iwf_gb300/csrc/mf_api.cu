@@ -23,13 +23,15 @@ namespace {
 
 const uint32_t REF_MAX_NBH = 200;  // particle.h:31
 
-__global__ void k_f64_to_f32(uint32_t n, const double* __restrict__ a, float* __restrict__ b) {
+// FP64 <-> FP32 state fields; the mixed form keeps the density as its deviation from
+// rho0 (`off`), which resolves per-step density changes far below rho0's FP32 ulp.
+__global__ void k_f64_to_f32(uint32_t n, const double* __restrict__ a, float* __restrict__ b, double off) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) b[i] = (float)a[i];
+	if (i < n) b[i] = (float)(a[i] - off);
 }
-__global__ void k_f32_to_f64(uint32_t n, const float* __restrict__ a, double* __restrict__ b) {
+__global__ void k_f32_to_f64(uint32_t n, const float* __restrict__ a, double* __restrict__ b, double off) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) b[i] = (double)a[i];
+	if (i < n) b[i] = off + (double)a[i];
 }
 
 struct HostBC {
@@ -47,6 +49,8 @@ struct HostBody {
 	std::vector<uint32_t> hull;
 	std::vector<HostBC> bcs;
 	std::vector<double> in[13];  // x y X Y m rho h qw vx vy Sxx Sxy Syy
+	uint32_t ex = 0, ey = 0;     // TL_WEAK: element_map_rectangle(ex, ey), 2x2 Gauss points
+	double gp_h = 0., gp_rho = 0.;
 };
 
 template <class T>
@@ -122,6 +126,17 @@ struct mf_ctx {
 	DevBuf<float4> recA, recB, dA32;
 	uint32_t n_bc = 0;
 
+	// TL_WEAK: Gauss points and the three list sets (sliced ELL)
+	uint32_t n_g = 0;
+	DevBuf<uint32_t> gp_body, g_sl, g_snbr, t_sl, t_snbr, p_sl, p_snbr;
+	DevBuf<uint16_t> g_cnt, t_cnt, p_cnt;
+	DevBuf<double> gp_x, gp_y, gp_qw, gp_hh, gsd[3][4], gP64;
+	DevBuf<float> gsf[3][4];
+	DevBuf<float4> gP32, wpack;
+	DevBuf<double2> g_w64, t_w64, p_w64;
+	DevBuf<float2> g_w32, t_w32, p_w32;
+	bool do_smooth = false;
+
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
 
@@ -172,6 +187,8 @@ inline uint32_t abit(int a) { return 1u << a; }
 
 mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status tl_setup(mf_ctx* c);
+mf_status weak_setup(mf_ctx* c);
+mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status contact_setup(mf_ctx* c);
 
 // UL pipeline: any subsequence of the reference's rings_monaghan list
@@ -326,8 +343,10 @@ mf_status finalize(mf_ctx* c) {
 	mf_status st = MF_OK;
 	if (c->cfg.method == MF_METHOD_UL) {
 		st = validate_ul(c, acts, c->flags);
-	} else {
+	} else if (c->cfg.method == MF_METHOD_TL) {
 		st = validate_tl(c, acts, c->flags);
+	} else {
+		st = validate_weak(c, acts, c->flags);
 	}
 	if (st != MF_OK) return st;
 	for (auto& b : c->bodies)
@@ -372,7 +391,8 @@ mf_status finalize(mf_ctx* c) {
 				if (k == 0) {
 					std::vector<float> v(n);
 					for (auto& b : c->bodies)
-						for (uint32_t i = 0; i < b.n; i++) v[b.off + i] = (float)b.in[fld[4 + q]][i];
+						for (uint32_t i = 0; i < b.n; i++)
+							v[b.off + i] = (float)(b.in[fld[4 + q]][i] - (q == 0 ? b.sd.rho0 : 0.));
 					CK(cudaMemcpy(c->sf[0][q].p, v.data(), n * 4, cudaMemcpyHostToDevice));
 				} else {
 					CK(cudaMemset(c->sf[k][q].p, 0, n * 4));
@@ -401,8 +421,11 @@ mf_status finalize(mf_ctx* c) {
 		c->sort_bits = bits;
 		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
 		CK(c->sort_tmp.alloc(tmp));
-	} else {
+	} else if (c->cfg.method == MF_METHOD_TL) {
 		mf_status s2 = tl_setup(c);
+		if (s2 != MF_OK) return s2;
+	} else {
+		mf_status s2 = weak_setup(c);
 		if (s2 != MF_OK) return s2;
 	}
 	{
@@ -594,8 +617,15 @@ mf_status tl_setup(mf_ctx* c) {
 	dgeom.free(); keys.free(); keys_sorted.free(); vals.free(); perm.free(); cstart.free(); count.free(); tmp.free();
 	// Randles-Libersky corrected gradients, FP64
 	CK(c->wx64.alloc(tot)); CK(c->wy64.alloc(tot));
-	const double* rho64 = c->mixed ? nullptr : c->sd[0][4].p;
-	const float* rho32 = c->mixed ? c->sf[0][0].p : nullptr;
+	DevBuf<double> rho_tmp;  // the mixed form keeps no FP64 density; the set-up needs one
+	if (c->mixed) {
+		CK(rho_tmp.alloc(n));
+		std::vector<double> v(n);
+		for (auto& b : c->bodies) std::copy(b.in[5].begin(), b.in[5].end(), v.begin() + b.off);
+		CK(cudaMemcpy(rho_tmp.p, v.data(), (size_t)n * 8, cudaMemcpyHostToDevice));
+	}
+	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
+	const float* rho32 = nullptr;
 	cudaError_t e = c->strict ? mf_strict::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
 	                                             rho32, c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream)
 	                          : mf_fast::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
@@ -671,6 +701,337 @@ mf_status tl_setup(mf_ctx* c) {
 	if (!rows.empty()) {
 		CK(cudaMemcpy(c->bc_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
 		CK(cudaMemcpy(c->bc_v.p, vs.data(), vs.size() * 8, cudaMemcpyHostToDevice));
+	}
+	return MF_OK;
+}
+
+// Neighbour lists (find_neighbors semantics: every "from" point within
+// sqrt(4h^2 + eps) of a "to" point, ascending) as CSR, over a per-body cell grid of the
+// particle bounding boxes whose cell is the search radius.  `to` points must lie in
+// (or near) their body's particle box.
+mf_status build_lists(mf_ctx* c, const double* fx, const double* fy, const uint32_t* from_body, uint32_t n_from,
+                      const double* tx, const double* ty, const uint32_t* to_body, uint32_t n_to, uint32_t cap,
+                      DevBuf<uint32_t>& off_out, DevBuf<uint32_t>& nbr_out, std::vector<uint32_t>& counts) {
+	uint32_t nb = (uint32_t)c->bodies.size();
+	double h = c->cfg.nbh_h, eps = c->cfg.nbh_eps;
+	double reach = sqrt(h * h * 2 * 2 + eps) * (1. + 1e-9);
+	std::vector<Geom> g(nb);
+	uint32_t cells = 0;
+	for (uint32_t b = 0; b < nb; b++) {
+		const HostBody& B = c->bodies[b];
+		double mnx = 1e300, mny = 1e300, mxx = -1e300, mxy = -1e300;
+		for (uint32_t i = 0; i < B.n; i++) {
+			mnx = std::min(mnx, B.in[0][i]); mxx = std::max(mxx, B.in[0][i]);
+			mny = std::min(mny, B.in[1][i]); mxy = std::max(mxy, B.in[1][i]);
+		}
+		double fnx = floor((mxx - mnx) / reach) + 1, fny = floor((mxy - mny) / reach) + 1;
+		if (fnx * fny > 1.5e9) return fail(c, MF_ERR_CAPACITY, "set-up grid too large");
+		g[b].bbmin_x = mnx; g[b].bbmin_y = mny; g[b].dx = reach;
+		g[b].nx = (uint32_t)fnx; g[b].ny = (uint32_t)fny;
+		g[b].num_cell = g[b].nx * g[b].ny;
+		g[b].cell_off = cells;
+		if ((uint64_t)cells + g[b].num_cell > 0xfffffff0ull) return fail(c, MF_ERR_CAPACITY, "set-up grid too large");
+		cells += g[b].num_cell;
+	}
+	DevBuf<Geom> dgeom;
+	DevBuf<uint32_t> keys, keys_sorted, vals, perm, cstart, count;
+	DevBuf<unsigned char> tmp;
+	CK(dgeom.alloc(nb));
+	CK(cudaMemcpy(dgeom.p, g.data(), nb * sizeof(Geom), cudaMemcpyHostToDevice));
+	CK(keys.alloc(n_from)); CK(keys_sorted.alloc(n_from)); CK(vals.alloc(n_from)); CK(perm.alloc(n_from));
+	CK(cstart.alloc((size_t)cells + 2)); CK(count.alloc(n_to));
+	int bits = 1;
+	while (bits < 32 && (1ull << bits) < (uint64_t)cells + 2) bits++;
+	size_t tb = c->strict ? mf_strict::tl_sort_tmp_bytes(n_from, bits) : mf_fast::tl_sort_tmp_bytes(n_from, bits);
+	CK(tmp.alloc(tb));
+	TLSearchArgs sa{};
+	sa.n_from = n_from; sa.n_to = n_to;
+	sa.fx = fx; sa.fy = fy; sa.tx = tx; sa.ty = ty;
+	sa.from_body = from_body; sa.to_body = to_body;
+	sa.geom = dgeom.p; sa.total_cells = cells;
+	sa.h = h; sa.eps = eps; sa.max_nbh = cap;
+	sa.keys = keys.p; sa.keys_sorted = keys_sorted.p; sa.vals = vals.p; sa.perm = perm.p; sa.cell_start = cstart.p;
+	sa.sort_tmp = tmp.p; sa.sort_tmp_bytes = tb; sa.sort_bits = bits;
+	sa.count = count.p; sa.status = c->d_status;
+	auto search = [&](int pass) { return c->strict ? mf_strict::tl_search(sa, pass, c->stream) : mf_fast::tl_search(sa, pass, c->stream); };
+	CK(search(0));
+	mf_status st = check_status(c);
+	if (st != MF_OK) return st;
+	counts.assign(n_to, 0);
+	CK(cudaMemcpy(counts.data(), count.p, (size_t)n_to * 4, cudaMemcpyDeviceToHost));
+	std::vector<uint32_t> off(n_to + 1, 0);
+	uint64_t tot = 0;
+	for (uint32_t i = 0; i < n_to; i++) { off[i] = (uint32_t)tot; tot += counts[i]; }
+	if (tot > 0xffffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^32 neighbour pairs");
+	off[n_to] = (uint32_t)tot;
+	CK(off_out.alloc((size_t)n_to + 1));
+	CK(cudaMemcpy(off_out.p, off.data(), ((size_t)n_to + 1) * 4, cudaMemcpyHostToDevice));
+	CK(nbr_out.alloc(tot));
+	sa.off = off_out.p;
+	sa.nbr = nbr_out.p;
+	CK(search(1));
+	CK(cudaStreamSynchronize(c->stream));
+	dgeom.free(); keys.free(); keys_sorted.free(); vals.free(); perm.free(); cstart.free(); count.free(); tmp.free();
+	return MF_OK;
+}
+
+// Sliced-ELL offsets from per-row counts (slices of 32 rows, padded to the longest).
+mf_status sell_offsets(mf_ctx* c, const std::vector<uint32_t>& counts, DevBuf<uint32_t>& sl, uint64_t& ent) {
+	uint32_t n = (uint32_t)counts.size();
+	uint32_t ns = (n + 31) / 32;
+	std::vector<uint32_t> h(ns + 1, 0);
+	ent = 0;
+	for (uint32_t s_ = 0; s_ < ns; s_++) {
+		uint32_t w = 0;
+		for (uint32_t r = 32 * s_; r < std::min(n, 32 * s_ + 32); r++) w = std::max(w, counts[r]);
+		h[s_] = (uint32_t)ent;
+		ent += 32ull * w;
+	}
+	if (ent > 0xffffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^32 sliced-ELL entries");
+	h[ns] = (uint32_t)ent;
+	CK(sl.alloc(ns + 1));
+	CK(cudaMemcpy(sl.p, h.data(), (ns + 1) * 4, cudaMemcpyHostToDevice));
+	return MF_OK;
+}
+
+// Weak-form pipeline: a subsequence of the tensile_tl_weak list (tensile.cpp:814-823).
+mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_DERIVE_DISPLACEMENT_WEAK, MF_DERIVE_VELOCITY_TL_WEAK, MF_CONTMECH_VELOCITY_GRADIENT_TL_GP,
+	                            MF_CONTMECH_CONTINUITY_GP, MF_MATERIAL_EOS_GP, MF_MATERIAL_STRESS_RATE_JAUMANN_GP,
+	                            MF_CONTMECH_CAUCHY_TO_NOMINAL_GP, MF_DERIVE_STRESS_WEAK_TL, MF_CONTMECH_MOMENTUM_TL_WEAK,
+	                            MF_CONTMECH_ADVECTION};
+	flags = 0;
+	size_t pos = 0;
+	for (int32_t a : acts) {
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not part of the fused weak-form pipeline or out of its order", a);
+		flags |= abit(a);
+		pos++;
+	}
+	if ((flags & abit(MF_CONTMECH_MOMENTUM_TL_WEAK)) && !(flags & abit(MF_DERIVE_STRESS_WEAK_TL)))
+		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_tl_weak needs derive_stress_weak_tl before it");
+	if ((flags & abit(MF_CONTMECH_VELOCITY_GRADIENT_TL_GP)) && !(flags & abit(MF_DERIVE_VELOCITY_TL_WEAK)))
+		return fail(c, MF_ERR_PIPELINE, "the Gauss-point velocity gradient needs derive_velocity_tl_weak before it");
+	for (auto& b : c->bodies)
+		if (b.ex == 0 || b.ey == 0) return fail(c, MF_ERR_STATE, "a TL_WEAK body needs mf_set_gauss_mesh");
+	return MF_OK;
+}
+
+// Weak-form set-up (tensile.cpp:776-807): Gauss points, the lists of Gauss points and
+// particles, RKPM shape functions, the transposed Gauss-point lists, sliced ELL.
+mf_status weak_setup(mf_ctx* c) {
+	uint32_t n = c->n_total;
+	uint32_t nb = (uint32_t)c->bodies.size();
+	if (!(c->cfg.nbh_h > 0.)) return fail(c, MF_ERR_ARG, "TL_WEAK needs config.nbh_h > 0");
+	std::vector<uint32_t> elem_body, bex(nb), bpoff(nb), beoff(nb), gpb;
+	std::vector<double> gh;
+	uint64_t ne = 0;
+	for (uint32_t b = 0; b < nb; b++) {
+		const HostBody& B = c->bodies[b];
+		bex[b] = B.ex; bpoff[b] = B.off; beoff[b] = (uint32_t)ne;
+		uint64_t k = (uint64_t)B.ex * B.ey;
+		ne += k;
+		if (4 * ne > 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 Gauss points");
+		elem_body.insert(elem_body.end(), k, b);
+		gpb.insert(gpb.end(), 4 * k, b);
+		gh.insert(gh.end(), 4 * k, B.gp_h);
+	}
+	c->n_g = (uint32_t)(4 * ne);
+	uint32_t ng = c->n_g;
+	c->do_smooth = c->bodies[0].sd.do_smooth != 0;
+	DevBuf<uint32_t> d_eb, d_bex, d_bpoff, d_beoff;
+	auto up32 = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
+		CK(d.alloc(v.size()));
+		if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+		return MF_OK;
+	};
+	mf_status st;
+	if ((st = up32(d_eb, elem_body)) || (st = up32(d_bex, bex)) || (st = up32(d_bpoff, bpoff)) ||
+	    (st = up32(d_beoff, beoff)) || (st = up32(c->gp_body, gpb)))
+		return st;
+	CK(c->gp_x.alloc(ng)); CK(c->gp_y.alloc(ng)); CK(c->gp_qw.alloc(ng)); CK(c->gp_hh.alloc(ng));
+	CK(cudaMemcpy(c->gp_hh.p, gh.data(), (size_t)ng * 8, cudaMemcpyHostToDevice));
+	const double* px = c->sd[0][0].p;
+	const double* py = c->sd[0][1].p;
+	cudaError_t e = c->strict ? mf_strict::weak_gauss_points((uint32_t)ne, d_eb.p, d_bex.p, d_bpoff.p, d_beoff.p, px, py,
+	                                                         c->gp_x.p, c->gp_y.p, c->gp_qw.p, c->d_status, c->stream)
+	                          : mf_fast::weak_gauss_points((uint32_t)ne, d_eb.p, d_bex.p, d_bpoff.p, d_beoff.p, px, py,
+	                                                       c->gp_x.p, c->gp_y.p, c->gp_qw.p, c->d_status, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "weak_gauss_points");
+	if ((st = check_status(c)) != MF_OK) return st;
+	d_eb.free(); d_bex.free(); d_bpoff.free(); d_beoff.free();
+
+	// lists: Gauss points -> particles, particles -> particles, particles -> Gauss points
+	DevBuf<uint32_t> g_off, g_nbr, t_off, t_nbr;
+	std::vector<uint32_t> gc, pc, tc;
+	if ((st = build_lists(c, px, py, c->body_of.p, n, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, c->cfg.max_nbh, g_off, g_nbr, gc)))
+		return st;
+	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->nbr_off, c->nbr, pc)))
+		return st;
+	if ((st = build_lists(c, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, px, py, c->body_of.p, n, 8 * c->cfg.max_nbh, t_off,
+	                      t_nbr, tc)))
+		return st;
+	uint64_t eg = g_nbr.n, ep = c->nbr.n, et = t_nbr.n;
+	// RKPM shape functions, FP64
+	DevBuf<double> gwx, gwy, pw, twx, twy;
+	CK(gwx.alloc(eg)); CK(gwy.alloc(eg)); CK(pw.alloc(ep)); CK(twx.alloc(et)); CK(twy.alloc(et));
+	DevBuf<double> rho_tmp;  // the mixed form keeps no FP64 density; the set-up needs one
+	if (c->mixed) {
+		CK(rho_tmp.alloc(n));
+		std::vector<double> v(n);
+		for (auto& b : c->bodies) std::copy(b.in[5].begin(), b.in[5].end(), v.begin() + b.off);
+		CK(cudaMemcpy(rho_tmp.p, v.data(), (size_t)n * 8, cudaMemcpyHostToDevice));
+	}
+	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
+	const float* rho32 = nullptr;
+	auto rkpm = [&](uint32_t nt, const double* tx, const double* ty, const double* th, const uint32_t* off,
+	                const uint32_t* nbr, double* w, double* wx, double* wy) {
+		return c->strict ? mf_strict::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
+		                                        c->d_status, c->stream)
+		                 : mf_fast::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
+		                                      c->d_status, c->stream);
+	};
+	if ((e = rkpm(ng, c->gp_x.p, c->gp_y.p, c->gp_hh.p, g_off.p, g_nbr.p, nullptr, gwx.p, gwy.p)) != cudaSuccess)
+		return cuda_fail(c, e, "weak_rkpm");
+	if ((e = rkpm(n, px, py, c->h.p, c->nbr_off.p, c->nbr.p, pw.p, nullptr, nullptr)) != cudaSuccess)
+		return cuda_fail(c, e, "weak_rkpm");
+	e = c->strict ? mf_strict::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
+	                                          c->d_status, c->stream)
+	              : mf_fast::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
+	                                        c->d_status, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "weak_transpose");
+	if ((st = check_status(c)) != MF_OK) return st;
+	// sliced ELL (mixed: FP32 with the quad weights folded in)
+	uint64_t sg, sp, stt;
+	if ((st = sell_offsets(c, gc, c->g_sl, sg)) || (st = sell_offsets(c, pc, c->p_sl, sp)) ||
+	    (st = sell_offsets(c, tc, c->t_sl, stt)))
+		return st;
+	CK(c->g_cnt.alloc(ng)); CK(c->p_cnt.alloc(n)); CK(c->t_cnt.alloc(n));
+	CK(c->g_snbr.alloc(sg)); CK(c->p_snbr.alloc(sp)); CK(c->t_snbr.alloc(stt));
+	if (c->mixed) {
+		CK(c->g_w32.alloc(sg)); CK(c->p_w32.alloc(sp)); CK(c->t_w32.alloc(stt));
+	} else {
+		CK(c->g_w64.alloc(sg)); CK(c->p_w64.alloc(sp)); CK(c->t_w64.alloc(stt));
+	}
+	auto sell = [&](uint32_t nr, const uint32_t* off, const uint32_t* nbr, const double* a, const double* b,
+	                const uint32_t* sl, uint16_t* cnt, uint32_t* snbr, void* o64, void* o32, const double* mr,
+	                const double* mn) {
+		return c->strict ? mf_strict::weak_sell(nr, off, nbr, a, b, sl, cnt, snbr, o64, o32, mr, mn, c->stream)
+		                 : mf_fast::weak_sell(nr, off, nbr, a, b, sl, cnt, snbr, o64, o32, mr, mn, c->stream);
+	};
+	bool mx = c->mixed;
+	if ((e = sell(ng, g_off.p, g_nbr.p, gwx.p, gwy.p, c->g_sl.p, c->g_cnt.p, c->g_snbr.p, mx ? nullptr : c->g_w64.p,
+	              mx ? (void*)c->g_w32.p : nullptr, nullptr, c->qw0.p)) != cudaSuccess ||
+	    (e = sell(n, c->nbr_off.p, c->nbr.p, pw.p, nullptr, c->p_sl.p, c->p_cnt.p, c->p_snbr.p, mx ? nullptr : c->p_w64.p,
+	              mx ? (void*)c->p_w32.p : nullptr, nullptr, c->qw0.p)) != cudaSuccess ||
+	    (e = sell(n, t_off.p, t_nbr.p, twx.p, twy.p, c->t_sl.p, c->t_cnt.p, c->t_snbr.p, mx ? nullptr : c->t_w64.p,
+	              mx ? (void*)c->t_w32.p : nullptr, c->qw0.p, c->gp_qw.p)) != cudaSuccess)
+		return cuda_fail(c, e, "weak_sell");
+	CK(cudaStreamSynchronize(c->stream));
+	gwx.free(); gwy.free(); pw.free(); twx.free(); twy.free(); g_off.free(); g_nbr.free(); t_off.free(); t_nbr.free();
+	// Gauss-point state: rho = the set-up rho (tensile.cpp:792-795), S = 0
+	std::vector<double> grho(ng);
+	for (uint32_t g = 0; g < ng; g++) grho[g] = c->bodies[gpb[g]].gp_rho;
+	for (int k = 0; k < 3; k++)
+		for (int q = 0; q < 4; q++) {
+			if (mx) {
+				CK(c->gsf[k][q].alloc(ng));
+				if (q == 0) {
+					std::vector<float> f(ng);
+					for (uint32_t g = 0; g < ng; g++) f[g] = (float)(grho[g] - c->bodies[gpb[g]].sd.rho0);
+					CK(cudaMemcpy(c->gsf[k][q].p, f.data(), (size_t)ng * 4, cudaMemcpyHostToDevice));
+				} else {
+					CK(cudaMemset(c->gsf[k][q].p, 0, (size_t)ng * 4));
+				}
+			} else {
+				CK(c->gsd[k][q].alloc(ng));
+				if (q == 0) CK(cudaMemcpy(c->gsd[k][q].p, grho.data(), (size_t)ng * 8, cudaMemcpyHostToDevice));
+				else CK(cudaMemset(c->gsd[k][q].p, 0, (size_t)ng * 8));
+			}
+		}
+	if (mx) {
+		CK(c->gP32.alloc(ng));
+		CK(c->wpack.alloc(2 * (size_t)n));
+	} else {
+		CK(c->gP64.alloc(4 * (size_t)ng));
+	}
+	// particles: stage 0 starts from a copy of the particles (set 2)
+	for (int q = 0; q < 8; q++) {
+		if (c->mixed && q >= 4) continue;
+		CK(cudaMemcpy(c->sd[2][q].p, c->sd[0][q].p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
+	}
+	// boundary conditions
+	std::vector<uint32_t> rows;
+	std::vector<double> vs;
+	for (auto& b : c->bodies)
+		for (auto& bc : b.bcs)
+			for (uint32_t i : bc.idx) { rows.push_back(b.off + i); vs.push_back(bc.v); }
+	c->n_bc = (uint32_t)rows.size();
+	CK(c->bc_rows.alloc(rows.size())); CK(c->bc_v.alloc(vs.size()));
+	if (!rows.empty()) {
+		CK(cudaMemcpy(c->bc_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->bc_v.p, vs.data(), vs.size() * 8, cudaMemcpyHostToDevice));
+	}
+	return MF_OK;
+}
+
+WeakArgs weak_args(mf_ctx* c) {
+	WeakArgs a{};
+	a.n_p = c->n_total; a.n_g = c->n_g; a.n_bodies = (uint32_t)c->bodies.size(); a.flags = c->flags;
+	a.block = c->tune.tl_block;
+	a.params = c->params.p; a.body_of = c->body_of.p; a.gp_body = c->gp_body.p;
+	a.X = c->X.p; a.Y = c->Y.p; a.m = c->m.p; a.qw_p = c->qw0.p; a.gp_qw = c->gp_qw.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	StateSoA* s[3] = {&a.base, &a.acc, &a.st};
+	for (int k = 0; k < 3; k++) {
+		double** d[8] = {&s[k]->x, &s[k]->y, &s[k]->vx, &s[k]->vy, &s[k]->rho, &s[k]->Sxx, &s[k]->Sxy, &s[k]->Syy};
+		for (int q = 0; q < 8; q++) *d[q] = c->sd[k][q].p;
+	}
+	StateSoA* g[3] = {&a.gbase, &a.gacc, &a.gst};
+	for (int k = 0; k < 3; k++) {
+		g[k]->rho = c->gsd[k][0].p; g[k]->Sxx = c->gsd[k][1].p; g[k]->Sxy = c->gsd[k][2].p; g[k]->Syy = c->gsd[k][3].p;
+		g[k]->rho_f = c->gsf[k][0].p; g[k]->Sxx_f = c->gsf[k][1].p; g[k]->Sxy_f = c->gsf[k][2].p; g[k]->Syy_f = c->gsf[k][3].p;
+	}
+	a.g_sl = c->g_sl.p; a.g_snbr = c->g_snbr.p; a.g_cnt = c->g_cnt.p;
+	a.t_sl = c->t_sl.p; a.t_snbr = c->t_snbr.p; a.t_cnt = c->t_cnt.p;
+	a.p_sl = c->p_sl.p; a.p_snbr = c->p_snbr.p; a.p_cnt = c->p_cnt.p;
+	a.g_w = c->mixed ? (const void*)c->g_w32.p : (const void*)c->g_w64.p;
+	a.t_w = c->mixed ? (const void*)c->t_w32.p : (const void*)c->t_w64.p;
+	a.p_w = c->mixed ? (const void*)c->p_w32.p : (const void*)c->p_w64.p;
+	a.gP = c->mixed ? (void*)c->gP32.p : (void*)c->gP64.p;
+	a.pack = c->wpack.p;
+	a.bc_rows = c->bc_rows.p; a.bc_v = c->bc_v.p; a.n_bc = c->n_bc;
+	a.status = c->d_status;
+	return a;
+}
+
+// rk4::do_step_weak + step for particle_tl_weak (rk4.h:140-185, 207-218): four stages
+// of (BCs, Gauss-point pass, particle pass), then the clock, the BCs on the particles
+// and the velocity smoothing -- in the reference's order.
+mf_status weak_step(mf_ctx* c) {
+	WeakArgs a = weak_args(c);
+	auto launch = [&](int part) {
+		return c->strict ? mf_strict::weak_stage(a, c->mixed, part, c->stream)
+		                 : mf_fast::weak_stage(a, c->mixed, part, c->stream);
+	};
+	cudaError_t e;
+	for (uint32_t st = 0; st < 4; st++) {
+		a.stage = st;
+		if ((e = launch(0)) != cudaSuccess || (e = launch(1)) != cudaSuccess) return cuda_fail(c, e, "weak stage");
+		int slot;
+		timing_begin(c, 5, slot);
+		if ((e = launch(2)) != cudaSuccess) return cuda_fail(c, e, "weak Gauss-point pass");
+		timing_end(c, slot, c->n_g);
+		timing_begin(c, 2, slot);
+		if ((e = launch(3)) != cudaSuccess) return cuda_fail(c, e, "weak particle pass");
+		timing_end(c, slot, c->n_total);
+		c->launches += 2 + (c->n_bc ? 1 : 0) + (c->mixed ? 1 : 0);
+	}
+	if ((e = launch(6)) != cudaSuccess || (e = launch(4)) != cudaSuccess) return cuda_fail(c, e, "weak step end");
+	c->launches += 1 + (c->n_bc ? 1 : 0);
+	if (c->do_smooth) {
+		if ((e = launch(5)) != cudaSuccess) return cuda_fail(c, e, "weak smoothing");
+		c->launches += 2;
 	}
 	return MF_OK;
 }
@@ -767,6 +1128,15 @@ mf_ctx::~mf_ctx() {
 	}
 	body_of.free(); params.free(); geom.free(); bbox.free(); total_cells.free(); keys.free(); keys_sorted.free();
 	perm_in.free(); perm.free(); cell_start.free(); rec_body.free(); rec.free(); sort_tmp.free();
+	{
+		DevBuf<uint32_t>* w32s[] = {&gp_body, &g_sl, &g_snbr, &t_sl, &t_snbr, &p_sl, &p_snbr};
+		for (auto* p : w32s) p->free();
+		g_cnt.free(); t_cnt.free(); p_cnt.free();
+		gp_x.free(); gp_y.free(); gp_qw.free(); gp_hh.free(); gP64.free(); gP32.free(); wpack.free();
+		for (int k = 0; k < 3; k++)
+			for (int q = 0; q < 4; q++) { gsd[k][q].free(); gsf[k][q].free(); }
+		g_w64.free(); t_w64.free(); p_w64.free(); g_w32.free(); t_w32.free(); p_w32.free();
+	}
 	sl_off.free(); snbr.free(); scnt.free(); sw64.free(); sw32.free(); swA32.free(); recA.free(); recB.free(); dA32.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
 	                            &slave_rows, &slave_master, &m_tile_off, &m_tile_n};
@@ -893,6 +1263,18 @@ MF_API mf_status mf_set_boundary(mf_ctx* c, int32_t body, const uint32_t* idx, u
 	return MF_OK;
 }
 
+MF_API mf_status mf_set_gauss_mesh(mf_ctx* c, int32_t body, uint32_t ex, uint32_t ey, double gp_h, double gp_rho) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "the mesh must be set before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	HostBody& b = c->bodies[body];
+	if (ex == 0 || ey == 0 || (uint64_t)(ex + 1) * (ey + 1) != b.n)
+		return fail(c, MF_ERR_ARG, "(ex+1)*(ey+1) must equal the body's particle count");
+	if (!(gp_h > 0.) || !(gp_rho > 0.)) return fail(c, MF_ERR_ARG, "Gauss-point h and rho must be positive");
+	b.ex = ex; b.ey = ey; b.gp_h = gp_h; b.gp_rho = gp_rho;
+	return MF_OK;
+}
+
 MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, uint32_t* out_idx, uint32_t* out_n) {
 	if ((!x || !y || !out_idx || !out_n) && n) return MF_ERR_ARG;
 	if (out_n) *out_n = 0;
@@ -932,7 +1314,7 @@ namespace {
 // The launches of one step of every body, in the driver's order (mfree_iwf.cpp:84-97):
 // the RK4 step, then the boundary refresh and contact.
 mf_status one_step(mf_ctx* c) {
-	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : tl_step_all(c);
+	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (c->cfg.method == MF_METHOD_TL ? tl_step_all(c) : weak_step(c));
 	if (st != MF_OK) return st;
 	if (c->contact_on) st = contact_run(c);
 	return st;
@@ -1019,7 +1401,8 @@ MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
 		if (!o[q]) continue;
 		if (c->mixed && q >= 4) {
 			double* st = c->staging.p + (size_t)(q - 4) * c->n_total;
-			k_f32_to_f64<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, c->sf[0][q - 4].p + b.off, st);
+			k_f32_to_f64<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, c->sf[0][q - 4].p + b.off, st,
+			                                                     q == 4 ? b.sd.rho0 : 0.);
 			CK(cudaMemcpyAsync(o[q], st, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
 		} else {
 			CK(cudaMemcpyAsync(o[q], c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1051,8 +1434,9 @@ MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 		if (c->mixed && q >= 4) {
 			double* st = c->staging.p + (size_t)(q - 4) * c->n_total;
 			CK(cudaMemcpyAsync(st, src[q], b.n * 8, cudaMemcpyHostToDevice, c->stream));
-			k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[0][q - 4].p + b.off);
-			if (tl) k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[2][q - 4].p + b.off);
+			double off = q == 4 ? b.sd.rho0 : 0.;
+			k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[0][q - 4].p + b.off, off);
+			if (tl) k_f64_to_f32<<<(b.n + 255) / 256, 256, 0, c->stream>>>(b.n, st, c->sf[2][q - 4].p + b.off, off);
 		} else {
 			CK(cudaMemcpyAsync(c->sd[0][q].p + b.off, src[q], b.n * 8, cudaMemcpyHostToDevice, c->stream));
 			if (tl) CK(cudaMemcpyAsync(c->sd[2][q].p + b.off, c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToDevice, c->stream));

@@ -118,6 +118,28 @@ struct TLArgs {
 	uint32_t block;                      // rows per block of the pair passes (autotuned)
 };
 
+// One weak-form stage: particles (state x, y, vx, vy) and Gauss points (state rho,
+// Sxx, Sxy, Syy in the rho/Sxx/Sxy/Syy or *_f slots of the StateSoA).
+struct WeakArgs {
+	uint32_t n_p, n_g, n_bodies, stage, flags, block;
+	const BodyParams* params;
+	const uint32_t *body_of, *gp_body;
+	const double *X, *Y, *m, *qw_p, *gp_qw, *fcx, *fcy;
+	StateSoA base, acc, st;      // particles
+	StateSoA gbase, gacc, gst;   // Gauss points
+	// sliced-ELL lists: Gauss point -> particles (gradients), particle -> Gauss points
+	// (transposed, gradients), particle -> particles (shape-function values)
+	const uint32_t *g_sl, *g_snbr, *t_sl, *t_snbr, *p_sl, *p_snbr;
+	const uint16_t *g_cnt, *t_cnt, *p_cnt;
+	const void *g_w, *t_w, *p_w;  // double2 (FP64 forms) / float2 (mixed, pre-multiplied weights)
+	void* gP;                     // nominal stress per Gauss point
+	void* pack;                   // mixed: per particle u and v as float-float (2 x float4)
+	const uint32_t* bc_rows;
+	const double* bc_v;
+	uint32_t n_bc;
+	void* status;
+};
+
 // Contact: boundary points of all bodies, their 32-point tiles, and the slave rows
 // with the master body each one is tested against.
 struct ContactArgs {
@@ -154,6 +176,21 @@ struct ContactArgs {
 	                       void* swA32, const double* qw, cudaStream_t s);                                    \
 	cudaError_t tl_stage(const mfk_host::TLArgs& a, bool mixed, int part, cudaStream_t s);                   \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
+	cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,  \
+	                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px,     \
+	                              const double* py, double* gx, double* gy, double* gqw, void* status,        \
+	                              cudaStream_t s);                                                            \
+	cudaError_t weak_rkpm(uint32_t n_to, const double* tx, const double* ty, const double* th,                \
+	                      const uint32_t* off, const uint32_t* nbr, const double* fx, const double* fy,       \
+	                      const double* fm, const double* frho, const float* frho_f, double* w, double* wx,    \
+	                      double* wy, void* status, cudaStream_t s);                                          \
+	cudaError_t weak_transpose(uint32_t n_p, const uint32_t* toff, const uint32_t* tnbr, const uint32_t* goff, \
+	                           const uint32_t* gnbr, const double* gwx, const double* gwy, double* twx,       \
+	                           double* twy, void* status, cudaStream_t s);                                    \
+	cudaError_t weak_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* a, const double* b, \
+	                      const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* out64, void* out32,     \
+	                      const double* mul_row, const double* mul_nbr, cudaStream_t s);                      \
+	cudaError_t weak_stage(const mfk_host::WeakArgs& a, bool mixed, int part, cudaStream_t s);               \
 	}
 
 MF_DECLARE_LAUNCHERS(mf_strict)

@@ -342,8 +342,9 @@ __global__ void k_tl_pack(TLArgs a) {
 	RecB* rb = (RecB*)a.recB + i;
 	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
-	float rho = s.rho_f[i];
-	float K = (float)a.params[a.body_of[i]].K;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	float rho = s.rho_f[i] + (float)pr.rho0;  // the mixed state holds rho - rho0
+	float K = (float)pr.K;
 	rb->hmrc = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
 }
 
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 	}
 	const BodyParams& pr = a.params[a.body_of[i]];
 	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
-	double rho = (double)s.rho_f[i];
+	double rho = (double)s.rho_f[i] + pr.rho0;  // the mixed state holds rho - rho0
 	// the 2x2 inversions of the per-particle part stay FP64
 	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
 	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);

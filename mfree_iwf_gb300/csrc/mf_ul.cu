@@ -349,6 +349,7 @@ __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	float rho, Sxx, Sxy, Syy;
 	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
 	uint32_t b = a.body_of[i];
+	rho += (float)P[b].rho0;  // the mixed state holds rho - rho0
 	Rec32 r;
 	r.x = ff_split(x); r.y = ff_split(y); r.vx = ff_split(vx); r.vy = ff_split(vy);
 	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;

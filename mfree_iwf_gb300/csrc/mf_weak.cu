@@ -1,0 +1,618 @@
+// Weak-form total-Lagrangian kernels with RKPM shape functions (particle_tl_weak;
+// tensile_tl_weak, tensile.cpp:731-826; rk4::do_step_weak and step, rk4.h:140-218).
+//
+// Set-up (once): Gauss points of the quad mesh (gauss_int::update_gauss_points,
+// gauss_integration.h:47-123, 2x2 rule), the neighbour lists of Gauss points and of
+// particles among the particles (find_neighbors), and the RKPM shape functions of
+// both (precomp_rkpm, precomp_shape_functions.h:31-208) in FP64.
+//
+// Per stage (body.h:60-78 with the action list fused):
+//   k_gp_pass   per Gauss point: displacement and velocity gradients from its particle
+//               neighbours (derivatives.h:152-200,445-481; a Gauss point itself never
+//               moves and has zero velocity, so u_i = v_i = 0 exactly), then L, the
+//               continuity rate, EOS, Jaumann rate and P = J F^-1 sigma (cont_mech.h,
+//               material.h), and the Gauss point's RK4 update (rho, S).
+//   k_p_pass    per particle: the stress divergence that derive_stress_weak_tl
+//               (derivatives.h:260-294) *scatters* from Gauss points, here *gathered*
+//               over the transposed lists (the Gauss points whose list holds the
+//               particle, ascending -- the order in which the scatter adds them), then
+//               momentum (cont_mech.h:89-106), advection and the particle's RK4 update.
+//   k_smooth    velocity smoothing after the step (correctors.h:171-210).
+#include "mf_common.cuh"
+#include "mf_kernels.h"
+
+using namespace mfk;
+using mfk_host::BodyParams;
+using mfk_host::WeakArgs;
+
+namespace MF_NS {
+namespace {
+
+inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+enum : uint32_t {
+	A_ADVECTION = 1u << 11,
+	A_DISP_W = 1u << 19,
+	A_VEL_W = 1u << 20,
+	A_VGRAD_GP = 1u << 21,
+	A_CONT_GP = 1u << 22,
+	A_EOS_GP = 1u << 23,
+	A_JAUMANN_GP = 1u << 24,
+	A_C2N_GP = 1u << 25,
+	A_STRESS_W = 1u << 26,
+	A_MOMENTUM_W = 1u << 27,
+};
+
+// ---------------------------------------------------------------- set-up
+// update_gauss_points for one element (node numbering of element_map_rectangle,
+// element.cpp:23-39); Gauss point g = 4 e + k in the order of get_weight_pos_2d.
+__global__ void k_gauss_points(uint32_t n_elem_total, const uint32_t* __restrict__ elem_body,
+                               const uint32_t* __restrict__ body_ex, const uint32_t* __restrict__ body_poff,
+                               const uint32_t* __restrict__ body_eoff, const double* __restrict__ px,
+                               const double* __restrict__ py, double* gx, double* gy, double* gqw, DevStatus* st) {
+	uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= n_elem_total) return;
+	uint32_t b = elem_body[e];
+	uint32_t el = e - body_eoff[b];
+	uint32_t ex = body_ex[b];
+	uint32_t row = el / ex, col = el - row * ex;
+	uint32_t nx = ex + 1;
+	uint32_t inc = row * nx + col;
+	uint32_t nidx[4] = {inc, inc + 1, inc + nx + 1, inc + nx};
+	double mx[4], my[4];
+#pragma unroll
+	for (int I = 0; I < 4; I++) {
+		mx[I] = px[body_poff[b] + nidx[I]];
+		my[I] = py[body_poff[b] + nidx[I]];
+	}
+	const double par_x[4] = {-1, +1, +1, -1}, par_y[4] = {-1, -1, +1, +1};
+	const double p1[2] = {0.577350269189626, -0.577350269189626};
+	for (int k = 0; k < 4; k++) {
+		double xi = p1[k >> 1], eta = p1[k & 1], local_w = 1.000000000000000 * 1.000000000000000;
+		double N[4];
+		const double X1 = -1, Y1 = -1, X2 = 1, Y2 = -1, X3 = 1, Y3 = 1, X4 = -1, Y4 = 1;
+		N[0] = 0.25 * (1 + X1 * xi) * (1 + Y1 * eta);
+		N[1] = 0.25 * (1 + X2 * xi) * (1 + Y2 * eta);
+		N[2] = 0.25 * (1 + X3 * xi) * (1 + Y3 * eta);
+		N[3] = 0.25 * (1 + X4 * xi) * (1 + Y4 * eta);
+		// transpose(m_node) * N
+		double gpx = mx[0] * N[0] + mx[1] * N[1] + mx[2] * N[2] + mx[3] * N[3];
+		double gpy = my[0] * N[0] + my[1] * N[1] + my[2] * N[2] + my[3] * N[3];
+		// x_xi accumulated element by element as dmat2x2(x_xi11, x_xi21, x_xi12, x_xi22)
+		double a00 = 0., a01 = 0., a10 = 0., a11 = 0.;  // column-major [col][row]
+#pragma unroll
+		for (int I = 0; I < 4; I++) {
+			double x_xi11 = 0.25 * mx[I] * par_x[I] * (1 + par_y[I] * eta);
+			double x_xi12 = 0.25 * mx[I] * par_y[I] * (1 + par_x[I] * xi);
+			double x_xi21 = 0.25 * my[I] * par_x[I] * (1 + par_y[I] * eta);
+			double x_xi22 = 0.25 * my[I] * par_y[I] * (1 + par_x[I] * xi);
+			a00 = a00 + x_xi11;
+			a01 = a01 + x_xi21;
+			a10 = a10 + x_xi12;
+			a11 = a11 + x_xi22;
+		}
+		double J = -(a00 * a11 - a10 * a01);
+		double w = local_w * J;
+		uint32_t g = 4 * e + k;
+		if (!(w > 0.)) raise(st, ERR_GRID, g);
+		gx[g] = gpx;
+		gy[g] = gpy;
+		gqw[g] = w;
+	}
+}
+
+// compute_rkpm_correctors + compute_rkpm_shape_function (precomp_shape_functions.h:52-173)
+// for query point i over its CSR list of particles; writes w, w_x, w_y per pair.
+__global__ void k_rkpm(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
+                       const double* __restrict__ th, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                       const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
+                       const double* __restrict__ frho, const float* __restrict__ frho_f, double* w_out, double* wx_out,
+                       double* wy_out, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_to) return;
+	double xi = tx[i], yi = ty[i], hi = th[i];
+	double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
+	       My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row]
+	uint32_t q0 = off[i], q1 = off[i + 1];
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double mj = fm[j], rhoj = frho ? frho[j] : (double)frho_f[j];
+		double xj = fx[j], yj = fy[j];
+		double rx = xi - xj, ry = yi - yj;
+		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
+		KR64 w = cubic_spline(xi - xj, yi - yj, hi);
+		M[0][0] += w.w * mj / rhoj;
+		M[0][1] += w.w * rx * mj / rhoj;
+		M[0][2] += w.w * ry * mj / rhoj;
+		M[1][0] += w.w * rx * mj / rhoj;
+		M[2][0] += w.w * ry * mj / rhoj;
+		M[1][1] += rx * rx * w.w * mj / rhoj;
+		M[1][2] += rx * ry * w.w * mj / rhoj;
+		M[2][1] += ry * rx * w.w * mj / rhoj;
+		M[2][2] += ry * ry * w.w * mj / rhoj;
+
+		Mx[0][0] += w.w_x * mj / rhoj;
+		Mx[0][1] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
+		Mx[0][2] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
+		Mx[1][0] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
+		Mx[2][0] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
+		Mx[1][1] += rx * rx * w.w_x * mj / rhoj + w.w * (rx_x * rx + rx * rx_x) * mj / rhoj;
+		Mx[1][2] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_x * ry + rx * rx_y) * mj / rhoj;
+		Mx[2][1] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_y * rx + ry * rx_x) * mj / rhoj;
+		Mx[2][2] += ry * ry * w.w_x * mj / rhoj + w.w * (rx_y * ry + ry * rx_y) * mj / rhoj;
+
+		My[0][0] += w.w_y * mj / rhoj;
+		My[0][1] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
+		My[0][2] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
+		My[1][0] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
+		My[2][0] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
+		My[1][1] += rx * rx * w.w_y * mj / rhoj + w.w * (ry_x * rx + rx * ry_x) * mj / rhoj;
+		My[1][2] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_x * ry + rx * ry_y) * mj / rhoj;
+		My[2][1] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_y * rx + ry * ry_x) * mj / rhoj;
+		My[2][2] += ry * ry * w.w_y * mj / rhoj + w.w * (ry_y * ry + ry * ry_y) * mj / rhoj;
+	}
+	// solve3x3 (Cramer's rule, precomp_shape_functions.h:31-50)
+	auto solve = [&](const double r[3], double x[3]) {
+		double delta = M[0][0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * M[1][2] -
+		               M[0][2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * M[1][0];
+		double delta_x = r[0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * r[2] + M[2][0] * r[1] * M[1][2] -
+		                 r[2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * r[0] - M[2][2] * r[1] * M[1][0];
+		double delta_y = M[0][0] * r[1] * M[2][2] + r[0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * r[2] -
+		                 M[0][2] * r[1] * M[2][0] - r[2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * r[0];
+		double delta_z = M[0][0] * M[1][1] * r[2] + M[1][0] * r[1] * M[0][2] + r[0] * M[0][1] * M[1][2] -
+		                 M[0][2] * M[1][1] * r[0] - M[1][2] * r[1] * M[0][0] - r[2] * M[0][1] * M[1][0];
+		if (!(fabs(delta) > 0.)) raise(st, ERR_SINGULAR, i);
+		x[0] = delta_x / delta;
+		x[1] = delta_y / delta;
+		x[2] = delta_z / delta;
+	};
+	double P[3] = {1., 0., 0.}, C[3], Cx[3], Cy[3];
+	solve(P, C);
+	// rhs = -M_x * C  ((-M_x) * C, column-major product)
+	double rx_[3], ry_[3];
+#pragma unroll
+	for (int r = 0; r < 3; r++) {
+		rx_[r] = (-Mx[0][r]) * C[0] + (-Mx[1][r]) * C[1] + (-Mx[2][r]) * C[2];
+		ry_[r] = (-My[0][r]) * C[0] + (-My[1][r]) * C[1] + (-My[2][r]) * C[2];
+	}
+	solve(rx_, Cx);
+	solve(ry_, Cy);
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double xj = fx[j], yj = fy[j];
+		double rx = xi - xj, ry = yi - yj;
+		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
+		KR64 w = cubic_spline(xi - xj, yi - yj, hi);
+		double Corr = (rx * C[1] + ry * C[2]) + C[0];
+		double Corr_x = (rx * Cx[1] + ry * Cx[2]) + rx_x * C[1] + rx_y * C[2] + Cx[0];
+		double Corr_y = (rx * Cy[1] + ry * Cy[2]) + ry_x * C[1] + ry_y * C[2] + Cy[0];
+		if (w_out) w_out[q] = Corr * w.w;
+		if (wx_out) wx_out[q] = Corr_x * w.w + Corr * w.w_x;
+		if (wy_out) wy_out[q] = Corr_y * w.w + Corr * w.w_y;
+	}
+}
+
+// For particle j and the k-th Gauss point i of its transposed list: the position of j
+// in i's (ascending) list -- binary search -- gives the pair's gradient.
+__global__ void k_transpose_w(uint32_t n_p, const uint32_t* __restrict__ toff, const uint32_t* __restrict__ tnbr,
+                              const uint32_t* __restrict__ goff, const uint32_t* __restrict__ gnbr,
+                              const double* __restrict__ gwx, const double* __restrict__ gwy, double* twx, double* twy,
+                              DevStatus* st) {
+	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= n_p) return;
+	for (uint32_t t = toff[j]; t < toff[j + 1]; t++) {
+		uint32_t i = tnbr[t];
+		uint32_t lo = goff[i], hi = goff[i + 1];
+		while (lo < hi) {
+			uint32_t mid = (lo + hi) >> 1;
+			if (gnbr[mid] < j) lo = mid + 1;
+			else hi = mid;
+		}
+		if (lo < goff[i + 1] && gnbr[lo] == j) {
+			twx[t] = gwx[lo];
+			twy[t] = gwy[lo];
+		} else {
+			raise(st, ERR_GRID, j);  // the neighbour relation was not symmetric
+			twx[t] = 0.;
+			twy[t] = 0.;
+		}
+	}
+}
+
+// CSR -> sliced ELL for the weak lists; values optionally pre-multiplied (mixed form).
+__global__ void k_weak_sell(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                            const double* __restrict__ a, const double* __restrict__ b, const uint32_t* __restrict__ sl_off,
+                            uint16_t* cnt, uint32_t* snbr, double2* out64, float2* out32,
+                            const double* __restrict__ mul_row, const double* __restrict__ mul_nbr) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t base = sl_off[i >> 5] + (i & 31u);
+	uint32_t q0 = off[i], c = off[i + 1] - q0;
+	cnt[i] = (uint16_t)c;
+	for (uint32_t k = 0; k < c; k++) {
+		uint32_t q = base + 32 * k;
+		uint32_t j = nbr[q0 + k];
+		snbr[q] = j;
+		double va = a ? a[q0 + k] : 0., vb = b ? b[q0 + k] : 0.;
+		if (out64) out64[q] = make_double2(va, vb);
+		if (out32) {
+			double s = (mul_row ? mul_row[i] : 1.) * (mul_nbr ? mul_nbr[j] : 1.);
+			out32[q] = make_float2((float)(va * s), (float)(vb * s));
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t sbase(const uint32_t* sl, uint32_t i) { return sl[i >> 5] + (i & 31u); }
+
+// ------------------------------------------------------------- per stage
+__global__ void k_weak_bc(WeakArgs a, int on_base) {
+	uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= a.n_bc) return;
+	uint32_t i = a.bc_rows[r];
+	double v = a.bc_v[r];
+	double t = a.params[a.body_of[i]].time;
+	const mfk_host::StateSoA& s = on_base ? a.base : a.st;
+	s.x[i] = a.X[i] + v * t;
+	s.y[i] = a.Y[i];
+	s.vx[i] = v;
+	s.vy[i] = 0.;
+}
+
+// per-Gauss-point part shared by both forms
+__device__ __forceinline__ void gp_point(uint32_t flags, const BodyParams& pr, double Hxx, double Hxy, double Hyx,
+                                         double Hyy, double Fxx, double Fxy, double Fyx, double Fyy, double rho,
+                                         double Sxx, double Sxy, double Syy, double& Pxx, double& Pxy, double& Pyx,
+                                         double& Pyy, double& rho_t, double& Sxx_t, double& Sxy_t, double& Syy_t) {
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+	if (flags & A_VGRAD_GP) velocity_gradient_tl<double>(Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, vx_x, vx_y, vy_x, vy_y);
+	rho_t = 0.;
+	if (flags & A_CONT_GP) rho_t = -(rho * (vx_x + vy_y));
+	double p = 0.;
+	if (flags & A_EOS_GP) p = pr.c0sq * (rho - pr.rho0);
+	Sxx_t = Sxy_t = Syy_t = 0.;
+	if (flags & A_JAUMANN_GP) jaumann<double>(vx_x, vx_y, vy_x, vy_y, Sxx, Sxy, Syy, pr.G, Sxx_t, Sxy_t, Syy_t);
+	Pxx = Pxy = Pyx = Pyy = 0.;
+	if (flags & A_C2N_GP) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
+}
+
+// Gauss point RK4 update of rho and S (rk4.h:154-183)
+template <class T>
+__device__ __forceinline__ void gp_rk(const WeakArgs& a, uint32_t i, double dt, const double e[4], T* gb[4], T* ga[4],
+                                      T* gs[4]) {
+	uint32_t stg = a.stage;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ga[q][i] = (stg == 0) ? (T)e[q] : (T)(ga[q][i] + (T)2 * (T)e[q]);
+			gs[q][i] = (T)(gb[q][i] + (T)e[q] * (T)dts);
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			T v = (T)(gb[q][i] + (T)w6 * (ga[q][i] + (T)e[q]));
+			gb[q][i] = v;
+			gs[q][i] = v;
+		}
+	}
+}
+
+__global__ void __launch_bounds__(256) k_gp_pass64(WeakArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_g) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double2* gw = (const double2*)a.g_w;
+	uint32_t flags = a.flags;
+	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0., Fxx = 0., Fxy = 0., Fyx = 0., Fyy = 0.;
+	uint32_t q = sbase(a.g_sl, i), c = a.g_cnt[i];
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.g_snbr[q];
+		double2 w = gw[q];
+		double qwj = a.qw_p[j];
+		if (flags & A_DISP_W) {
+			double uxj = s.x[j] - a.X[j], uyj = s.y[j] - a.Y[j];
+			Hxx += (uxj - 0.) * w.x * qwj;
+			Hxy += (uxj - 0.) * w.y * qwj;
+			Hyx += (uyj - 0.) * w.x * qwj;
+			Hyy += (uyj - 0.) * w.y * qwj;
+		}
+		if (flags & A_VEL_W) {
+			double vxj = s.vx[j], vyj = s.vy[j];
+			Fxx += (vxj - 0.) * w.x * qwj;
+			Fxy += (vxj - 0.) * w.y * qwj;
+			Fyx += (vyj - 0.) * w.x * qwj;
+			Fyy += (vyj - 0.) * w.y * qwj;
+		}
+	}
+	const BodyParams& pr = a.params[a.gp_body[i]];
+	double* gs[4] = {a.gst.rho, a.gst.Sxx, a.gst.Sxy, a.gst.Syy};
+	double* gb[4] = {a.gbase.rho, a.gbase.Sxx, a.gbase.Sxy, a.gbase.Syy};
+	double* ga[4] = {a.gacc.rho, a.gacc.Sxx, a.gacc.Sxy, a.gacc.Syy};
+	double P[4], e[4];
+	gp_point(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, gs[0][i], gs[1][i], gs[2][i], gs[3][i], P[0], P[1], P[2],
+	         P[3], e[0], e[1], e[2], e[3]);
+	double* gP = (double*)a.gP;
+	uint32_t n = a.n_g;
+	gP[i] = P[0]; gP[n + i] = P[1]; gP[2 * n + i] = P[2]; gP[3 * n + i] = P[3];
+	gp_rk<double>(a, i, pr.dt, e, gb, ga, gs);
+}
+
+__global__ void __launch_bounds__(256) k_p_pass64(WeakArgs a) {
+	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= a.n_p) return;
+	const double2* tw = (const double2*)a.t_w;
+	const double* gP = (const double*)a.gP;
+	uint32_t n = a.n_g;
+	uint32_t flags = a.flags;
+	double vol_node = a.qw_p[j];
+	double Pxx_x = 0., Pyx_y = 0., Pxy_x = 0., Pyy_y = 0.;
+	if (flags & A_STRESS_W) {
+		uint32_t q = sbase(a.t_sl, j), c = a.t_cnt[j];
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t i = a.t_snbr[q];
+			double2 w = tw[q];
+			double quad_weight = a.gp_qw[i];
+			Pxx_x -= gP[i] * w.x * quad_weight * vol_node;
+			Pyx_y -= gP[2 * n + i] * w.y * quad_weight * vol_node;
+			Pxy_x -= gP[n + i] * w.x * quad_weight * vol_node;
+			Pyy_y -= gP[3 * n + i] * w.y * quad_weight * vol_node;
+		}
+	}
+	const mfk_host::StateSoA& s = a.st;
+	const BodyParams& pr = a.params[a.body_of[j]];
+	double m = a.m[j];
+	double d[4];
+	d[0] = (flags & A_ADVECTION) ? s.vx[j] : 0.;
+	d[1] = (flags & A_ADVECTION) ? s.vy[j] : 0.;
+	d[2] = 0.;
+	d[3] = 0.;
+	if (flags & A_MOMENTUM_W) {
+		d[2] += 1. / m * (Pxx_x + Pyx_y) + a.fcx[j] / a.m[j];
+		d[3] += 1. / m * (Pxy_x + Pyy_y) + a.fcy[j] / a.m[j];
+	}
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* sp[4] = {a.st.x, a.st.y, a.st.vx, a.st.vy};
+	uint32_t stg = a.stage;
+	double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ap[q][j] = (stg == 0) ? d[q] : ap[q][j] + 2 * d[q];
+			sp[q][j] = bp[q][j] + d[q] * dts;  // own row only: in place
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			double v = bp[q][j] + w6 * (ap[q][j] + d[q]);
+			bp[q][j] = v;
+			sp[q][j] = v;
+		}
+		if (!(isfinite(bp[0][j]) && isfinite(bp[1][j]) && isfinite(bp[2][j]) && isfinite(bp[3][j])))
+			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, j);
+	}
+}
+
+// ---- mixed form: particle displacement and velocity as float-float, FP32 sums
+__global__ void k_weak_pack(WeakArgs a) {
+	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= a.n_p) return;
+	const mfk_host::StateSoA& s = a.st;
+	FF ux = ff_split(s.x[j] - a.X[j]), uy = ff_split(s.y[j] - a.Y[j]);
+	FF vx = ff_split(s.vx[j]), vy = ff_split(s.vy[j]);
+	float4* pk = (float4*)a.pack;
+	pk[2 * j] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+	pk[2 * j + 1] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+}
+
+__global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_g) return;
+	const float2* gw = (const float2*)a.g_w;  // gradient times the particle's quad weight
+	const float4* pk = (const float4*)a.pack;
+	uint32_t flags = a.flags;
+	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f, Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
+	uint32_t q = sbase(a.g_sl, i), c = a.g_cnt[i];
+#pragma unroll 2
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.g_snbr[q];
+		float2 w = gw[q];
+		if (flags & A_DISP_W) {
+			float4 u = __ldg(pk + 2 * j);
+			float ux = u.x + u.y, uy = u.z + u.w;
+			Hxx += ux * w.x;
+			Hxy += ux * w.y;
+			Hyx += uy * w.x;
+			Hyy += uy * w.y;
+		}
+		if (flags & A_VEL_W) {
+			float4 v = __ldg(pk + 2 * j + 1);
+			float vx = v.x + v.y, vy = v.z + v.w;
+			Fxx += vx * w.x;
+			Fxy += vx * w.y;
+			Fyx += vy * w.x;
+			Fyy += vy * w.y;
+		}
+	}
+	const BodyParams& pr = a.params[a.gp_body[i]];
+	float* gs[4] = {a.gst.rho_f, a.gst.Sxx_f, a.gst.Sxy_f, a.gst.Syy_f};
+	float* gb[4] = {a.gbase.rho_f, a.gbase.Sxx_f, a.gbase.Sxy_f, a.gbase.Syy_f};
+	float* ga[4] = {a.gacc.rho_f, a.gacc.Sxx_f, a.gacc.Sxy_f, a.gacc.Syy_f};
+	double P[4], e[4];
+	// the mixed Gauss-point state holds rho - rho0
+	gp_point(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, (double)gs[0][i] + pr.rho0, gs[1][i], gs[2][i],
+	         gs[3][i], P[0], P[1], P[2], P[3], e[0], e[1], e[2], e[3]);
+	((float4*)a.gP)[i] = make_float4((float)P[0], (float)P[1], (float)P[2], (float)P[3]);
+	gp_rk<float>(a, i, pr.dt, e, gb, ga, gs);
+}
+
+__global__ void __launch_bounds__(256) k_p_pass32(WeakArgs a) {
+	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= a.n_p) return;
+	const float2* tw = (const float2*)a.t_w;  // gradient times both quad weights
+	const float4* gP = (const float4*)a.gP;
+	uint32_t flags = a.flags;
+	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f;
+	if (flags & A_STRESS_W) {
+		uint32_t q = sbase(a.t_sl, j), c = a.t_cnt[j];
+#pragma unroll 2
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t i = a.t_snbr[q];
+			float2 w = tw[q];
+			float4 P = __ldg(gP + i);
+			Pxx_x -= P.x * w.x;
+			Pyx_y -= P.z * w.y;
+			Pxy_x -= P.y * w.x;
+			Pyy_y -= P.w * w.y;
+		}
+	}
+	const mfk_host::StateSoA& s = a.st;
+	const BodyParams& pr = a.params[a.body_of[j]];
+	double m = a.m[j];
+	double d[4];
+	d[0] = (flags & A_ADVECTION) ? s.vx[j] : 0.;
+	d[1] = (flags & A_ADVECTION) ? s.vy[j] : 0.;
+	d[2] = 0.;
+	d[3] = 0.;
+	if (flags & A_MOMENTUM_W) {
+		d[2] += (double)(Pxx_x + Pyx_y) / m + a.fcx[j] / m;
+		d[3] += (double)(Pxy_x + Pyy_y) / m + a.fcy[j] / m;
+	}
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* sp[4] = {a.st.x, a.st.y, a.st.vx, a.st.vy};
+	uint32_t stg = a.stage;
+	double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ap[q][j] = (stg == 0) ? d[q] : ap[q][j] + 2 * d[q];
+			sp[q][j] = bp[q][j] + d[q] * dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			double v = bp[q][j] + w6 * (ap[q][j] + d[q]);
+			bp[q][j] = v;
+			sp[q][j] = v;
+		}
+		if (!(isfinite(bp[0][j]) && isfinite(bp[1][j]) && isfinite(bp[2][j]) && isfinite(bp[3][j])))
+			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, j);
+	}
+}
+
+// correctors_smooth_vel (correctors.h:171-210) on the particles: the smoothed velocity
+// goes to the stage set (the next step's first stage copy), then back to the particles.
+__global__ void k_smooth(WeakArgs a, int mixed) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_p) return;
+	uint32_t q = sbase(a.p_sl, i), c = a.p_cnt[i];
+	if (!mixed) {
+		const double2* pw = (const double2*)a.p_w;  // (w, 0)
+		double vsx = 0., vsy = 0.;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.p_snbr[q];
+			double w = pw[q].x, qwj = a.qw_p[j];
+			vsx += a.base.vx[j] * w * qwj;
+			vsy += a.base.vy[j] * w * qwj;
+		}
+		a.st.vx[i] = vsx;
+		a.st.vy[i] = vsy;
+	} else {
+		const float2* pw = (const float2*)a.p_w;  // (w * qw_j, 0)
+		float vsx = 0.f, vsy = 0.f;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.p_snbr[q];
+			float w = pw[q].x;
+			vsx += (float)a.base.vx[j] * w;
+			vsy += (float)a.base.vy[j] * w;
+		}
+		a.st.vx[i] = vsx;
+		a.st.vy[i] = vsy;
+	}
+}
+__global__ void k_smooth_copy(WeakArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_p) return;
+	a.base.vx[i] = a.st.vx[i];
+	a.base.vy[i] = a.st.vy[i];
+}
+
+__global__ void k_weak_time(uint32_t nb, BodyParams* P) {
+	uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b < nb) P[b].time += P[b].dt;
+}
+
+}  // namespace
+
+cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,
+                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px, const double* py,
+                              double* gx, double* gy, double* gqw, void* status, cudaStream_t s) {
+	k_gauss_points<<<grid1(n_elem_total, 128), 128, 0, s>>>(n_elem_total, elem_body, body_ex, body_poff, body_eoff, px,
+	                                                         py, gx, gy, gqw, reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t weak_rkpm(uint32_t n_to, const double* tx, const double* ty, const double* th, const uint32_t* off,
+                      const uint32_t* nbr, const double* fx, const double* fy, const double* fm, const double* frho,
+                      const float* frho_f, double* w, double* wx, double* wy, void* status, cudaStream_t s) {
+	k_rkpm<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, th, off, nbr, fx, fy, fm, frho, frho_f, w, wx, wy,
+	                                         reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t weak_transpose(uint32_t n_p, const uint32_t* toff, const uint32_t* tnbr, const uint32_t* goff,
+                           const uint32_t* gnbr, const double* gwx, const double* gwy, double* twx, double* twy,
+                           void* status, cudaStream_t s) {
+	k_transpose_w<<<grid1(n_p, 128), 128, 0, s>>>(n_p, toff, tnbr, goff, gnbr, gwx, gwy, twx, twy,
+	                                               reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t weak_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* a, const double* b,
+                      const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* out64, void* out32,
+                      const double* mul_row, const double* mul_nbr, cudaStream_t s) {
+	k_weak_sell<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, a, b, sl_off, cnt, snbr, (double2*)out64, (float2*)out32,
+	                                           mul_row, mul_nbr);
+	return cudaGetLastError();
+}
+
+cudaError_t weak_stage(const WeakArgs& a, bool mixed, int part, cudaStream_t s) {
+	// 0: BCs on the stage state, 1: pack (mixed), 2: Gauss-point pass, 3: particle pass,
+	// 4: BCs on the particles after the step, 5: smoothing, 6: clocks
+	unsigned bs = a.block ? a.block : 128;
+	switch (part) {
+	case 0:
+		if (a.n_bc) k_weak_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 0);
+		break;
+	case 1:
+		if (mixed) k_weak_pack<<<grid1(a.n_p, 256), 256, 0, s>>>(a);
+		break;
+	case 2:
+		if (mixed) k_gp_pass32<<<grid1(a.n_g, bs), bs, 0, s>>>(a);
+		else k_gp_pass64<<<grid1(a.n_g, bs), bs, 0, s>>>(a);
+		break;
+	case 3:
+		if (mixed) k_p_pass32<<<grid1(a.n_p, bs), bs, 0, s>>>(a);
+		else k_p_pass64<<<grid1(a.n_p, bs), bs, 0, s>>>(a);
+		break;
+	case 4:
+		if (a.n_bc) k_weak_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 1);
+		break;
+	case 5:
+		k_smooth<<<grid1(a.n_p, 128), 128, 0, s>>>(a, mixed ? 1 : 0);
+		k_smooth_copy<<<grid1(a.n_p, 256), 256, 0, s>>>(a);
+		break;
+	case 6:
+		k_weak_time<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, const_cast<BodyParams*>(a.params));
+		break;
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS

@@ -359,7 +359,10 @@ def tensile_plate(
         sc.do_smooth = do_smooth
         sc.gp_h = hdx * dx
         sc.gp_rho = rho0
-        body.ex, body.ey = nx - 1, ny - 1
+        # element_map_rectangle(ex, ey) numbers nodes row by row with ex+1 nodes per
+        # row (element.cpp:23-39); here rows run along the outer (x) index, so a row
+        # holds the ny nodes of one lattice column
+        body.ex, body.ey = ny - 1, nx - 1
     return sc
 
 

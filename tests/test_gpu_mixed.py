@@ -42,7 +42,8 @@ def errors(sc, a, b):
 # 10 mm gap); the TL rings at dx = 0.4 mm through 600 steps, well into contact.  The
 # TL contact set-up itself turns unstable near step 750 at dx = 0.4 mm -- the CPU
 # oracle of the reference's algorithm does the same -- so that case stops at 600.
-CASES = [("ul_rings_dx1mm", 1000), ("tl_rings_dx0.05mm", 1000), ("tl_rings_dx0.4mm_contact", 600)]
+CASES = [("ul_rings_dx1mm", 1000), ("tl_rings_dx0.05mm", 1000), ("tl_rings_dx0.4mm_contact", 600),
+         ("weak_plate_dx0.2mm", 1000)]
 
 
 @pytest.mark.parametrize("case,steps", CASES)
@@ -51,6 +52,8 @@ def test_mixed_error(case, steps, lib):
         sc = S.c1_rings(dx=1e-3)
     elif case == "tl_rings_dx0.05mm":
         sc = S.c2_rings_tl(dx=5e-5)
+    elif case == "weak_plate_dx0.2mm":
+        sc = S.c3_plate(dx=2e-4)
     else:
         sc = S.c2_rings_tl(dx=4e-4)
     ref = run(sc, steps, "fp64")

@@ -53,7 +53,7 @@ def golden(name):
 
 
 UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm"]
-TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm"]
+TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak"]
 
 
 @pytest.mark.parametrize("name", UL_CASES + TL_CASES)
@@ -170,3 +170,14 @@ def test_set_state_resumes_exactly(lib, precision, method):
             assert np.array_equal(got[f], s20[k][f]), (method, precision, f)
     a.close()
     b_.close()
+
+
+def test_weak_plate_against_oracle(lib, oracle_bin):
+    """The plate-tension set-up (weak form, RKPM, jittered lattice) at dx = 1 mm:
+    2121 particles, 8000 Gauss points, 20 steps; FP64 strict is bit-identical."""
+    import oracle
+    sc = S.c3_plate(dx=1e-3)
+    ref = oracle.run(sc, 20).dumps[-1]["bodies"][0]
+    got = run_gpu(sc, 20, "fp64_strict")[0]
+    for f in FIELDS:
+        assert np.array_equal(got[f], ref[f]), (f, rel_l2(got[f], ref[f]))
