@@ -193,6 +193,12 @@ MF_API mf_status mf_launch_count(mf_ctx* ctx, uint64_t* launches);
  * cached per process by (method, precision, particle-count bucket).  report (may be
  * NULL) receives a one-line summary. */
 MF_API mf_status mf_autotune(mf_ctx* ctx, int32_t trial_steps, char* report, uint32_t report_len);
+/* Per-step monitor: after every step each body's [mean vx, mean vy, max von Mises
+ * stress, sum of |contact force|] is written on the device into a ring of `capacity`
+ * rows (0 disables).  mf_get_monitor copies the min(steps, capacity) rows written,
+ * row-major [row][body][4] floats (row = step % capacity), and their count. */
+MF_API mf_status mf_set_monitor(mf_ctx* ctx, uint32_t capacity);
+MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
 MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
 

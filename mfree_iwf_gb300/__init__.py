@@ -106,6 +106,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
         "mf_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
         "mf_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, C.c_uint32]),
+        "mf_set_monitor": (C.c_int32, [C.c_void_p, C.c_uint32]),
+        "mf_get_monitor": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), _UP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -293,6 +295,18 @@ class Simulation:
         buf = ctypes.create_string_buffer(2048)
         self._check(self._lib.mf_autotune(self._h, int(trial_steps), buf, len(buf)), "mf_autotune")
         return buf.value.decode()
+
+    def set_monitor(self, capacity: int) -> None:
+        self._check(self._lib.mf_set_monitor(self._h, int(capacity)), "mf_set_monitor")
+
+    def monitor(self) -> np.ndarray:
+        """[rows, bodies, 4]: mean vx, mean vy, max von Mises stress, sum |fc| per step."""
+        rows = ctypes.c_uint32()
+        self._check(self._lib.mf_get_monitor(self._h, None, ctypes.byref(rows)), "mf_get_monitor")
+        out = np.zeros((rows.value, self.n_bodies, 4), np.float32)
+        self._check(self._lib.mf_get_monitor(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                             ctypes.byref(rows)), "mf_get_monitor")
+        return out
 
     def launch_count(self) -> int:
         n = ctypes.c_uint64()

@@ -23,6 +23,56 @@ namespace {
 
 const uint32_t REF_MAX_NBH = 200;  // particle.h:31
 
+// Per-body reductions of the current state, one row per step into a device ring of
+// `cap` rows: [mean vx, mean vy, max von Mises stress, sum |fc|] per body.  sigma =
+// S - p I with p from the EOS (material.h:37-44); plane von Mises
+// sqrt(sxx^2 - sxx syy + syy^2 + 3 sxy^2).  One block per body; the row index comes
+// from a device counter so the kernel can live inside a captured step graph.
+__global__ void k_monitor(uint32_t nb, const BodyParams* __restrict__ P, const double* __restrict__ vx,
+                          const double* __restrict__ vy, const double* __restrict__ rho, const float* __restrict__ rho_f,
+                          const double* __restrict__ Sxx, const double* __restrict__ Sxy, const double* __restrict__ Syy,
+                          const float* __restrict__ Sxx_f, const float* __restrict__ Sxy_f, const float* __restrict__ Syy_f,
+                          const double* __restrict__ fcx, const double* __restrict__ fcy, uint32_t eos, float* out,
+                          uint32_t* counter, uint32_t cap) {
+	uint32_t b = blockIdx.x;
+	if (b >= nb) return;
+	const BodyParams& pr = P[b];
+	double svx = 0., svy = 0., vm = 0., fc = 0.;
+	for (uint32_t k = threadIdx.x; k < pr.n; k += blockDim.x) {
+		uint32_t i = pr.off + k;
+		svx += vx[i];
+		svy += vy[i];
+		double r = rho ? rho[i] : (double)rho_f[i] + pr.rho0;
+		double p = eos ? pr.c0sq * (r - pr.rho0) : 0.;
+		double sxx = (Sxx ? Sxx[i] : (double)Sxx_f[i]) - p;
+		double syy = (Syy ? Syy[i] : (double)Syy_f[i]) - p;
+		double sxy = Sxy ? Sxy[i] : (double)Sxy_f[i];
+		vm = fmax(vm, sqrt(fmax(sxx * sxx - sxx * syy + syy * syy + 3. * sxy * sxy, 0.)));
+		fc += sqrt(fcx[i] * fcx[i] + fcy[i] * fcy[i]);
+	}
+	__shared__ double s0[256], s1[256], s2[256], s3[256];
+	s0[threadIdx.x] = svx; s1[threadIdx.x] = svy; s2[threadIdx.x] = vm; s3[threadIdx.x] = fc;
+	__syncthreads();
+	for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) {
+			s0[threadIdx.x] += s0[threadIdx.x + o];
+			s1[threadIdx.x] += s1[threadIdx.x + o];
+			s2[threadIdx.x] = fmax(s2[threadIdx.x], s2[threadIdx.x + o]);
+			s3[threadIdx.x] += s3[threadIdx.x + o];
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		uint32_t row = *counter % cap;
+		float* o = out + ((size_t)row * nb + b) * 4;
+		o[0] = (float)(s0[0] / pr.n);
+		o[1] = (float)(s1[0] / pr.n);
+		o[2] = (float)s2[0];
+		o[3] = (float)s3[0];
+	}
+}
+__global__ void k_monitor_tick(uint32_t* counter) { *counter += 1; }
+
 // FP64 <-> FP32 state fields; the mixed form keeps the density as its deviation from
 // rho0 (`off`), which resolves per-step density changes far below rho0's FP32 ulp.
 __global__ void k_f64_to_f32(uint32_t n, const double* __restrict__ a, float* __restrict__ b, double off) {
@@ -139,6 +189,11 @@ struct mf_ctx {
 
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
+
+	// per-step monitor (mf_set_monitor)
+	uint32_t mon_cap = 0;
+	DevBuf<float> mon;
+	DevBuf<uint32_t> mon_counter;
 
 	// launch shapes, persistent-kernel work counter, captured step graph
 	Tune tune;
@@ -1145,7 +1200,7 @@ mf_ctx::~mf_ctx() {
 	for (auto* p : f64s) p->free();
 	DevBuf<float>* f32s[] = {&qw32, &m32, &h32};
 	for (auto* p : f32s) p->free();
-	bnd.free(); bnd_ff.free(); tile_bb.free(); staging.free();
+	bnd.free(); bnd_ff.free(); tile_bb.free(); staging.free(); mon.free(); mon_counter.free();
 	for (auto e : timing.pool) cudaEventDestroy(e);
 	if (d_status) cudaFree(d_status);
 	if (h_status) cudaFreeHost(h_status);
@@ -1317,6 +1372,18 @@ mf_status one_step(mf_ctx* c) {
 	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (c->cfg.method == MF_METHOD_TL ? tl_step_all(c) : weak_step(c));
 	if (st != MF_OK) return st;
 	if (c->contact_on) st = contact_run(c);
+	if (st == MF_OK && c->mon_cap) {
+		uint32_t nb = (uint32_t)c->bodies.size();
+		bool eos = (c->flags & abit(MF_MATERIAL_EOS)) != 0;
+		k_monitor<<<nb, 256, 0, c->stream>>>(nb, c->params.p, c->sd[0][2].p, c->sd[0][3].p, c->sd[0][4].p, c->sf[0][0].p,
+		                                      c->sd[0][5].p, c->sd[0][6].p, c->sd[0][7].p, c->sf[0][1].p, c->sf[0][2].p,
+		                                      c->sf[0][3].p, c->fcx.p, c->fcy.p, eos ? 1u : 0u, c->mon.p,
+		                                      c->mon_counter.p, c->mon_cap);
+		k_monitor_tick<<<1, 1, 0, c->stream>>>(c->mon_counter.p);
+		c->launches += 2;
+		cudaError_t e = cudaGetLastError();
+		if (e != cudaSuccess) return cuda_fail(c, e, "monitor");
+	}
 	return st;
 }
 
@@ -1677,6 +1744,34 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 	         best_t.tl_block, key.c_str());
 	rep += line;
 	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_monitor(mf_ctx* c, uint32_t capacity) {
+	if (!c) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	CK(cudaSetDevice(c->cfg.device));
+	drop_graph(c);
+	c->mon.free();
+	c->mon_counter.free();
+	c->mon_cap = capacity;
+	if (!capacity) return MF_OK;
+	if ((uint64_t)capacity * c->bodies.size() * 4 > (1ull << 32)) return fail(c, MF_ERR_CAPACITY, "monitor too large");
+	CK(c->mon.alloc((size_t)capacity * c->bodies.size() * 4));
+	CK(c->mon_counter.alloc(1));
+	CK(cudaMemset(c->mon_counter.p, 0, 4));
+	return MF_OK;
+}
+
+MF_API mf_status mf_get_monitor(mf_ctx* c, float* out, uint32_t* rows) {
+	if (!c || !rows) return MF_ERR_ARG;
+	if (!c->mon_cap) return fail(c, MF_ERR_STATE, "monitor not enabled");
+	uint32_t cnt = 0;
+	CK(cudaMemcpyAsync(&cnt, c->mon_counter.p, 4, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	*rows = cnt < c->mon_cap ? cnt : c->mon_cap;
+	if (out) CK(cudaMemcpy(out, c->mon.p, (size_t)(*rows) * c->bodies.size() * 4 * 4, cudaMemcpyDeviceToHost));
 	return MF_OK;
 }
 
