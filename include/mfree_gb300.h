@@ -230,6 +230,51 @@ typedef struct mf_device_body {
 MF_API mf_status mf_ul_step_noalloc(const mf_device_body* body, const mf_sim_data* sd, double dt,
                                     const int32_t* actions, uint32_t n_actions, int32_t nsteps, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * MLP surrogate.  No counterpart in the reference: an ensemble of `members` fully
+ * connected ReLU networks (the last layer linear) with BF16 weights and activations,
+ * FP32 accumulation and FP32 Adam master weights, trained on the device on solver
+ * outputs.  Parameters of one member, as get/set_params exchange them: for each layer
+ * l, W_l [dims[l+1]][dims[l]] row-major, then b_l [dims[l+1]].  Pointers to sample
+ * arrays may be host or device memory.
+ * ------------------------------------------------------------------------- */
+#define MF_MLP_MAX_LAYERS 8
+#define MF_MLP_MAX_WIDTH 512
+
+typedef struct mf_mlp mf_mlp;
+
+typedef struct mf_mlp_config {
+	int32_t members;                      /* ensemble size, 1..64 */
+	int32_t n_layers;                     /* weight layers, 1..MF_MLP_MAX_LAYERS */
+	int32_t dims[MF_MLP_MAX_LAYERS + 1];  /* widths, input first, each 1..MF_MLP_MAX_WIDTH */
+	int32_t max_batch;                    /* rows per pass: the training minibatch and the inference chunk */
+	int32_t device;
+	uint64_t seed;                        /* weight initialisation and minibatch sampling */
+} mf_mlp_config;
+
+MF_API mf_status mf_mlp_create(const mf_mlp_config* cfg, mf_mlp** model);
+MF_API void mf_mlp_destroy(mf_mlp* model);
+MF_API const char* mf_mlp_last_error(const mf_mlp* model);
+MF_API mf_status mf_mlp_num_params(const mf_mlp* model, uint64_t* n);  /* per member */
+MF_API mf_status mf_mlp_get_params(mf_mlp* model, int32_t member, float* params);
+MF_API mf_status mf_mlp_set_params(mf_mlp* model, int32_t member, const float* params);
+/* Gradients of the mean squared error (over batch x dims[L]) of every member on its own
+ * batch x [members][batch][dims[0]] against y [members][batch][dims[L]]; loss (may be
+ * NULL) receives [members].  mf_mlp_get_grads then returns one member's gradients in
+ * the parameter layout.  batch <= max_batch. */
+MF_API mf_status mf_mlp_gradients(mf_mlp* model, const float* x, const float* y, int32_t batch, float* loss);
+MF_API mf_status mf_mlp_get_grads(mf_mlp* model, int32_t member, float* grads);
+/* Training set x [n][dims[0]], y [n][dims[L]] (copied to the device). */
+MF_API mf_status mf_mlp_set_data(mf_mlp* model, const float* x, const float* y, int32_t n);
+/* `steps` Adam steps on minibatches of max_batch rows, each member drawing its own
+ * rows with replacement; learning rate cosine-annealed from lr0 to lr1 over the call.
+ * loss_history (may be NULL) receives [steps][members] minibatch losses. */
+MF_API mf_status mf_mlp_train(mf_mlp* model, int32_t steps, float lr0, float lr1, float* loss_history);
+/* Every member's outputs y [members][n][dims[L]] for x [n][dims[0]]. */
+MF_API mf_status mf_mlp_predict(mf_mlp* model, const float* x, int32_t n, float* y);
+MF_API mf_status mf_mlp_launch_count(const mf_mlp* model, uint64_t* launches);
+MF_API mf_status mf_mlp_get_stream(const mf_mlp* model, void** stream);
+
 #ifdef __cplusplus
 }
 #endif

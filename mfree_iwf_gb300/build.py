@@ -46,7 +46,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             src = os.path.join(CSRC, tu)
             obj = os.path.join(BUILD, f"{tu[:-3]}_{ns}.o")
             jobs.append((src, obj, base + [f"-DMF_NS={ns}", f"--fmad={fmad}", src, "-o", obj]))
-    for host_tu in ("mf_api.cu", "mf_noalloc.cu"):
+    for host_tu in ("mf_api.cu", "mf_noalloc.cu", "mf_mlp.cu"):
         src = os.path.join(CSRC, host_tu)
         obj = os.path.join(BUILD, host_tu[:-3] + ".o")
         jobs.append((src, obj, base + [src, "-o", obj]))

@@ -1,0 +1,745 @@
+// MLP surrogate: an ensemble of small fully connected ReLU networks with BF16 weights
+// and activations and FP32 accumulation, trained with Adam on FP32 master weights.
+// It maps ring-impact parameters to the solver's rebound velocity, peak von Mises
+// stress and contact-force history (mfree_iwf_gb300/surrogate.py).  No counterpart in
+// the reference: this is a learned screen placed in front of the solver.
+//
+// Every matrix product goes through one tiled tensor-core GEMM (k_gemm): 64x64 output
+// tiles, K in slices of 32 staged in shared memory, four warps of 32x32 outputs each
+// issuing mma.sync m16n8k16 (BF16 inputs, FP32 accumulators), gridDim.z over the
+// ensemble members.  The bias and ReLU are fused into the epilogue, which stores FP32
+// and/or BF16.  The layers (6 -> 256 -> 256 -> 256 -> 66, a few hundred rows per
+// training batch) are too small for a TMA/tcgen05 pipeline to pay off.
+//
+// Training keeps the whole data set on the device.  One training step -- bootstrap
+// minibatch gather (each member draws its own rows), forward, MSE, backward, Adam --
+// is captured once as a CUDA graph and replayed; the step counter, learning-rate
+// schedule and loss history live in device memory, so replays need no host work.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/mfree_gb300.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+struct GemmArgs {
+	int M, N, K;
+	const bf16* A;
+	int lda;
+	long long sA;  // member strides, elements
+	const bf16* B;
+	int ldb;
+	long long sB;
+	float* C;  // FP32 output, optional
+	int ldc;
+	long long sC;
+	bf16* Cb;  // BF16 output, optional
+	int ldcb;
+	long long sCb;
+	const float* bias;  // per output column, optional
+	long long sBias;
+	int relu;
+};
+
+constexpr int BM = 64, BN = 64, BK = 32, PADK = BK + 8;  // 80-byte rows: conflict-free fragment loads
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// C[M x N] = op(A)[M x K] op(B)[K x N]
+//   TA = false: A(m, k) = A[m*lda + k]   TA = true: A(m, k) = A[k*lda + m]
+//   TB = false: B(k, n) = B[k*ldb + n]   TB = true: B(k, n) = B[n*ldb + k]
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+	__shared__ __align__(16) bf16 As[BM][PADK];  // [m][k]
+	__shared__ __align__(16) bf16 Bs[BN][PADK];  // [n][k]
+	const int z = blockIdx.z;
+	const bf16* A = g.A + z * g.sA;
+	const bf16* B = g.B + z * g.sB;
+	const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int wm = warp >> 1, wn = warp & 1;
+	const int gid = lane >> 2, tig = lane & 3;
+	float acc[2][4][4];
+#pragma unroll
+	for (int a = 0; a < 2; a++)
+#pragma unroll
+		for (int b = 0; b < 4; b++)
+#pragma unroll
+			for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
+	const bf16 zero = __float2bfloat16(0.f);
+	for (int k0 = 0; k0 < g.K; k0 += BK) {
+		// stage the tiles; consecutive threads walk the contiguous dimension
+#pragma unroll 4
+		for (int e = tid; e < BM * BK; e += 128) {
+			const int mm = TA ? (e % BM) : (e / BK), kk = TA ? (e / BM) : (e % BK);
+			const int m = m0 + mm, k = k0 + kk;
+			bf16 v = zero;
+			if (m < g.M && k < g.K) v = TA ? A[(long long)k * g.lda + m] : A[(long long)m * g.lda + k];
+			As[mm][kk] = v;
+		}
+#pragma unroll 4
+		for (int e = tid; e < BN * BK; e += 128) {
+			const int nn = TB ? (e / BK) : (e % BN), kk = TB ? (e % BK) : (e / BN);
+			const int n = n0 + nn, k = k0 + kk;
+			bf16 v = zero;
+			if (n < g.N && k < g.K) v = TB ? B[(long long)n * g.ldb + k] : B[(long long)k * g.ldb + n];
+			Bs[nn][kk] = v;
+		}
+		__syncthreads();
+#pragma unroll
+		for (int ks = 0; ks < BK; ks += 16) {
+			uint32_t af[2][4], bfr[4][2];
+			const int c = ks + tig * 2;
+#pragma unroll
+			for (int mt = 0; mt < 2; mt++) {
+				const int r = wm * 32 + mt * 16 + gid;
+				af[mt][0] = ld_pair(&As[r][c]);
+				af[mt][1] = ld_pair(&As[r + 8][c]);
+				af[mt][2] = ld_pair(&As[r][c + 8]);
+				af[mt][3] = ld_pair(&As[r + 8][c + 8]);
+			}
+#pragma unroll
+			for (int nt = 0; nt < 4; nt++) {
+				const int n = wn * 32 + nt * 8 + gid;
+				bfr[nt][0] = ld_pair(&Bs[n][c]);
+				bfr[nt][1] = ld_pair(&Bs[n][c + 8]);
+			}
+#pragma unroll
+			for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+				for (int nt = 0; nt < 4; nt++) {
+					float* d = acc[mt][nt];
+					asm volatile(
+					    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+					    "{%0,%1,%2,%3};\n"
+					    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+					    : "r"(af[mt][0]), "r"(af[mt][1]), "r"(af[mt][2]), "r"(af[mt][3]), "r"(bfr[nt][0]),
+					      "r"(bfr[nt][1]));
+				}
+		}
+		__syncthreads();
+	}
+	float* C = g.C ? g.C + z * g.sC : nullptr;
+	bf16* Cb = g.Cb ? g.Cb + z * g.sCb : nullptr;
+	const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
+#pragma unroll
+	for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+		for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+			for (int h = 0; h < 2; h++)
+#pragma unroll
+				for (int q = 0; q < 2; q++) {
+					const int m = m0 + wm * 32 + mt * 16 + gid + 8 * h;
+					const int n = n0 + wn * 32 + nt * 8 + tig * 2 + q;
+					if (m >= g.M || n >= g.N) continue;
+					float v = acc[mt][nt][2 * h + q];
+					if (bias) v += bias[n];
+					if (g.relu) v = fmaxf(v, 0.f);
+					if (C) C[(long long)m * g.ldc + n] = v;
+					if (Cb) Cb[(long long)m * g.ldcb + n] = __float2bfloat16(v);
+				}
+}
+
+// Training control block in device memory, read by the graph's kernels on every replay.
+struct TrainCtl {
+	uint32_t step;   // Adam steps taken so far (the current step's number inside a step)
+	uint32_t t0;     // step count when the current mf_mlp_train call began
+	uint32_t total;  // steps of the current call (cosine schedule length)
+	uint32_t n_data;
+	float lr0, lr1;
+	float* hist;  // [total][members] loss history of the current call
+	uint64_t seed;
+};
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+	x += 0x9E3779B97F4A7C15ull;
+	x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+	x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+	return x ^ (x >> 31);
+}
+
+// bootstrap minibatch: member z's row r takes data row splitmix(seed, step, z, r) mod n
+__global__ void k_gather(const TrainCtl* ctl, int in, int in_p, int out, long long sH0, long long sY, const float* X,
+                         const float* Y, bf16* H0, float* Yb) {
+	const int r = blockIdx.x, z = blockIdx.y;
+	const uint64_t key = ctl->seed ^ ((uint64_t)ctl->step << 20) ^ ((uint64_t)z << 52) ^ (uint64_t)r;
+	const uint32_t src = (uint32_t)(splitmix64(key) % ctl->n_data);
+	for (int c = threadIdx.x; c < in_p; c += blockDim.x)
+		H0[z * sH0 + (long long)r * in_p + c] = __float2bfloat16(c < in ? X[(long long)src * in + c] : 0.f);
+	for (int c = threadIdx.x; c < out; c += blockDim.x) Yb[z * sY + (long long)r * out + c] = Y[(long long)src * out + c];
+}
+
+// x (FP32 [batch][in] per member, member stride sx; 0 = shared) -> BF16 [batch][in_p], zero padded
+__global__ void k_input(int members, int batch, int in, int in_p, const float* x, long long sx, bf16* h, long long sh) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	const long long per = (long long)batch * in_p;
+	if (e >= per * members) return;
+	const int z = (int)(e / per);
+	const long long w = e % per;
+	const int c = (int)(w % in_p);
+	const long long r = w / in_p;
+	h[z * sh + w] = __float2bfloat16(c < in ? x[z * sx + r * in + c] : 0.f);
+}
+
+// mean squared error of member z over batch x out; dZ = 2 (y_pred - y) / (batch * out)
+__global__ void k_mse(int batch, int out, int out_p, const float* yp, long long syp, const float* y, long long sy,
+                      float* dz, bf16* dzb, long long sdz, float* loss) {
+	const int z = blockIdx.y;
+	float s = 0.f;
+	const float inv = 1.f / (float)(batch * out);
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < batch * out_p; e += gridDim.x * blockDim.x) {
+		const int c = e % out_p, r = e / out_p;
+		float d = 0.f;
+		if (c < out) {
+			const float diff = yp[z * syp + e] - y[z * sy + (long long)r * out + c];
+			s += diff * diff;
+			d = 2.f * diff * inv;
+		}
+		dz[z * sdz + e] = d;
+		dzb[z * sdz + e] = __float2bfloat16(d);
+	}
+	__shared__ float red[256];
+	red[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) atomicAdd(&loss[z], red[0] * inv);
+}
+
+// dZ = dH where the layer's ReLU output H > 0, else 0 (FP32 and BF16 copies)
+__global__ void k_relu_bwd(int members, long long per, const float* dh, long long sdh, const bf16* h, long long sh,
+                           float* dz, bf16* dzb, long long sdz) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= per * members) return;
+	const int z = (int)(e / per);
+	const long long w = e % per;
+	const float v = __bfloat162float(h[z * sh + w]) > 0.f ? dh[z * sdh + w] : 0.f;
+	dz[z * sdz + w] = v;
+	dzb[z * sdz + w] = __float2bfloat16(v);
+}
+
+// db[n] = sum over rows of dZ[r][n]
+__global__ void k_bias_grad(int batch, int out_p, const float* dz, long long sdz, float* db, long long sdb) {
+	const int n = blockIdx.x * blockDim.x + threadIdx.x, z = blockIdx.y;
+	if (n >= out_p) return;
+	const float* d = dz + z * sdz;
+	float s = 0.f;
+	for (int r = 0; r < batch; r++) s += d[(long long)r * out_p + n];
+	db[z * sdb + n] = s;
+}
+
+// Adam (Kingma & Ba 2015) on FP32 master parameters with a cosine learning-rate
+// schedule from lr0 to lr1 over the current call; refreshes the BF16 weight copy.
+__global__ void k_adam(const TrainCtl* ctl, long long n, float* w, const float* g, float* m, float* v, bf16* wb) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= n) return;
+	const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+	const uint32_t t = ctl->step;
+	const float frac = ctl->total > 1 ? (float)(t - 1 - ctl->t0) / (float)(ctl->total - 1) : 0.f;
+	const float lr = ctl->lr1 + 0.5f * (ctl->lr0 - ctl->lr1) * (1.f + cospif(fminf(fmaxf(frac, 0.f), 1.f)));
+	const float c1 = 1.f - powf(b1, (float)t), c2 = 1.f - powf(b2, (float)t);
+	const float gi = g[e];
+	const float mi = b1 * m[e] + (1.f - b1) * gi;
+	const float vi = b2 * v[e] + (1.f - b2) * gi * gi;
+	m[e] = mi;
+	v[e] = vi;
+	const float wi = w[e] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+	w[e] = wi;
+	if (wb) wb[e] = __float2bfloat16(wi);
+}
+
+__global__ void k_step_begin(TrainCtl* ctl, float* loss, int members) {
+	if (threadIdx.x == 0) ctl->step += 1;
+	for (int z = threadIdx.x; z < members; z += blockDim.x) loss[z] = 0.f;
+}
+
+__global__ void k_step_end(const TrainCtl* ctl, const float* loss, int members) {
+	const uint32_t row = ctl->step - 1 - ctl->t0;
+	if (!ctl->hist || row >= ctl->total) return;
+	for (int z = threadIdx.x; z < members; z += blockDim.x) ctl->hist[(size_t)row * members + z] = loss[z];
+}
+
+__global__ void k_to_bf16(long long n, const float* a, bf16* b) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e < n) b[e] = __float2bfloat16(a[e]);
+}
+
+// unpadded outputs [members][rows][out] from the padded last layer [members][rows][out_p]
+__global__ void k_output(int members, int rows, int out, int out_p, const float* yp, long long syp, float* y,
+                         long long sy) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	const long long per = (long long)rows * out;
+	if (e >= per * members) return;
+	const int z = (int)(e / per);
+	const long long w = e % per;
+	y[z * sy + w] = yp[z * syp + (w / out) * out_p + (w % out)];
+}
+
+inline int pad16(int v) { return (v + 15) / 16 * 16; }
+inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <class T>
+struct Buf {
+	T* p = nullptr;
+	size_t n = 0;
+	cudaError_t alloc(size_t count) {
+		free();
+		n = count;
+		return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+	}
+	void free() {
+		if (p) cudaFree(p);
+		p = nullptr;
+		n = 0;
+	}
+	~Buf() { free(); }
+};
+
+// portable seeded initialisation: splitmix64 -> uniform in [-1, 1)
+struct HostRng {
+	uint64_t s;
+	uint64_t next() {
+		uint64_t x = (s += 0x9E3779B97F4A7C15ull);
+		x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+		x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+		return x ^ (x >> 31);
+	}
+	float sym() { return (float)((double)(next() >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0); }
+};
+
+}  // namespace
+
+struct mf_mlp {
+	int members = 0, L = 0, rows = 0, device = 0;
+	std::vector<int> dims, pd;            // true and padded widths, L + 1 each
+	std::vector<long long> w_off, b_off;  // per-layer offsets inside one member's block
+	long long w_per = 0, b_per = 0;       // parameters per member (padded)
+	int widest = 0;
+	Buf<float> W, Bias, gW, gB, mW, vW, mB, vB;
+	Buf<bf16> Wb;
+	std::vector<Buf<bf16>> H;  // H[l]: BF16 [members][rows][pd[l]], l = 0..L-1
+	Buf<float> Yp;             // FP32 [members][rows][pd[L]]
+	Buf<float> dz, dh;         // FP32 [members][rows][widest]
+	Buf<bf16> dzb;
+	Buf<float> loss;           // [members]
+	Buf<float> Xin, Yin;       // batches from the host: [members][rows][in], [members][rows][out]
+	Buf<float> Xd, Yd;         // training set [n][in], [n][out]
+	Buf<float> hist;
+	Buf<TrainCtl> ctl;
+	TrainCtl h_ctl{};
+	cudaStream_t stream = nullptr;
+	cudaGraphExec_t graph = nullptr;
+	uint64_t launches = 0, step_launches = 0;
+	std::string err;
+	~mf_mlp() {
+		if (graph) cudaGraphExecDestroy(graph);
+		if (stream) cudaStreamDestroy(stream);
+	}
+};
+
+namespace {
+
+mf_status mlp_fail(mf_mlp* m, const std::string& what, cudaError_t e) {
+	m->err = what + ": " + cudaGetErrorString(e);
+	return MF_ERR_CUDA;
+}
+#define MCK(call)                                             \
+	do {                                                      \
+		cudaError_t e_ = (call);                              \
+		if (e_ != cudaSuccess) return mlp_fail(m, #call, e_); \
+	} while (0)
+
+cudaError_t gemm(mf_mlp* m, bool ta, bool tb, GemmArgs g) {
+	dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, m->members);
+	cudaStream_t s = m->stream;
+	if (!ta && tb) k_gemm<false, true><<<grid, 128, 0, s>>>(g);
+	else if (!ta && !tb) k_gemm<false, false><<<grid, 128, 0, s>>>(g);
+	else if (ta && !tb) k_gemm<true, false><<<grid, 128, 0, s>>>(g);
+	else k_gemm<true, true><<<grid, 128, 0, s>>>(g);
+	m->launches++;
+	return cudaGetLastError();
+}
+
+long long sH(const mf_mlp* m, int l) { return (long long)m->rows * m->pd[l]; }
+
+// forward pass of all members over `batch` rows already in H[0]
+cudaError_t forward_layers(mf_mlp* m, int batch) {
+	for (int l = 0; l < m->L; l++) {
+		GemmArgs g{};
+		g.M = batch; g.N = m->pd[l + 1]; g.K = m->pd[l];
+		g.A = m->H[l].p; g.lda = m->pd[l]; g.sA = sH(m, l);
+		g.B = m->Wb.p + m->w_off[l]; g.ldb = m->pd[l]; g.sB = m->w_per;
+		g.bias = m->Bias.p + m->b_off[l]; g.sBias = m->b_per;
+		if (l + 1 < m->L) {
+			g.Cb = m->H[l + 1].p; g.ldcb = m->pd[l + 1]; g.sCb = sH(m, l + 1);
+			g.relu = 1;
+		} else {
+			g.C = m->Yp.p; g.ldc = m->pd[l + 1]; g.sC = sH(m, l + 1);
+		}
+		cudaError_t e = gemm(m, false, true, g);
+		if (e != cudaSuccess) return e;
+	}
+	return cudaSuccess;
+}
+
+// gradients of the mean squared error against y (FP32 [members][rows][out]) into gW,
+// gB; the per-member losses accumulate into m->loss (zeroed beforehand)
+cudaError_t backward_layers(mf_mlp* m, const float* y, int batch) {
+	cudaStream_t s = m->stream;
+	const int L = m->L;
+	const long long sdz = (long long)m->rows * m->widest;  // member stride of dz, dh, dzb
+	k_mse<<<dim3(32, m->members), 256, 0, s>>>(batch, m->dims[L], m->pd[L], m->Yp.p, sH(m, L), y,
+	                                           (long long)m->rows * m->dims[L], m->dz.p, m->dzb.p, sdz, m->loss.p);
+	m->launches++;
+	for (int l = L - 1; l >= 0; l--) {
+		const int out_p = m->pd[l + 1], in_p = m->pd[l];
+		k_bias_grad<<<dim3(nblk(out_p, 128), m->members), 128, 0, s>>>(batch, out_p, m->dz.p, sdz, m->gB.p + m->b_off[l],
+		                                                               m->b_per);
+		m->launches++;
+		// dW [out x in] = dZ^T [out x batch] . H[l] [batch x in]
+		GemmArgs gw{};
+		gw.M = out_p; gw.N = in_p; gw.K = batch;
+		gw.A = m->dzb.p; gw.lda = out_p; gw.sA = sdz;
+		gw.B = m->H[l].p; gw.ldb = in_p; gw.sB = sH(m, l);
+		gw.C = m->gW.p + m->w_off[l]; gw.ldc = in_p; gw.sC = m->w_per;
+		cudaError_t e = gemm(m, true, false, gw);
+		if (e != cudaSuccess) return e;
+		if (l == 0) break;
+		// dH [batch x in] = dZ [batch x out] . W [out x in]
+		GemmArgs gx{};
+		gx.M = batch; gx.N = in_p; gx.K = out_p;
+		gx.A = m->dzb.p; gx.lda = out_p; gx.sA = sdz;
+		gx.B = m->Wb.p + m->w_off[l]; gx.ldb = in_p; gx.sB = m->w_per;
+		gx.C = m->dh.p; gx.ldc = in_p; gx.sC = sdz;
+		if ((e = gemm(m, false, false, gx)) != cudaSuccess) return e;
+		const long long per = (long long)batch * in_p;
+		k_relu_bwd<<<nblk(per * m->members, 256), 256, 0, s>>>(m->members, per, m->dh.p, sdz, m->H[l].p, sH(m, l), m->dz.p,
+		                                                      m->dzb.p, sdz);
+		m->launches++;
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t adam_update(mf_mlp* m) {
+	const long long nw = m->w_per * m->members, nb = m->b_per * m->members;
+	k_adam<<<nblk(nw, 256), 256, 0, m->stream>>>(m->ctl.p, nw, m->W.p, m->gW.p, m->mW.p, m->vW.p, m->Wb.p);
+	k_adam<<<nblk(nb, 256), 256, 0, m->stream>>>(m->ctl.p, nb, m->Bias.p, m->gB.p, m->mB.p, m->vB.p, nullptr);
+	m->launches += 2;
+	return cudaGetLastError();
+}
+
+// one full training step on the stream (this sequence is what the graph captures)
+cudaError_t train_step_launches(mf_mlp* m) {
+	cudaStream_t s = m->stream;
+	const int out = m->dims[m->L];
+	k_step_begin<<<1, 64, 0, s>>>(m->ctl.p, m->loss.p, m->members);
+	k_gather<<<dim3(m->rows, m->members), 32, 0, s>>>(m->ctl.p, m->dims[0], m->pd[0], out, sH(m, 0),
+	                                                  (long long)m->rows * out, m->Xd.p, m->Yd.p, m->H[0].p, m->Yin.p);
+	m->launches += 2;
+	cudaError_t e;
+	if ((e = forward_layers(m, m->rows)) != cudaSuccess) return e;
+	if ((e = backward_layers(m, m->Yin.p, m->rows)) != cudaSuccess) return e;
+	if ((e = adam_update(m)) != cudaSuccess) return e;
+	k_step_end<<<1, 64, 0, s>>>(m->ctl.p, m->loss.p, m->members);
+	m->launches++;
+	return cudaGetLastError();
+}
+
+void drop_graph(mf_mlp* m) {
+	if (m->graph) cudaGraphExecDestroy(m->graph);
+	m->graph = nullptr;
+}
+
+// parameters of one member, unpadded, layer by layer: W_l [out][in] row-major, then b_l
+enum class Walk { GetParams, GetGrads, SetParams };
+mf_status param_walk(mf_mlp* m, int member, float* host, Walk mode) {
+	size_t o = 0;
+	float* Wsrc = mode == Walk::GetGrads ? m->gW.p : m->W.p;
+	float* Bsrc = mode == Walk::GetGrads ? m->gB.p : m->Bias.p;
+	const bool get = mode != Walk::SetParams;
+	for (int l = 0; l < m->L; l++) {
+		const size_t wdev = (size_t)member * m->w_per + m->w_off[l];
+		const size_t wid = (size_t)m->dims[l] * 4, pitch = (size_t)m->pd[l] * 4;
+		if (get) MCK(cudaMemcpy2D(host + o, wid, Wsrc + wdev, pitch, wid, m->dims[l + 1], cudaMemcpyDeviceToHost));
+		else MCK(cudaMemcpy2D(Wsrc + wdev, pitch, host + o, wid, wid, m->dims[l + 1], cudaMemcpyHostToDevice));
+		o += (size_t)m->dims[l] * m->dims[l + 1];
+		const size_t bdev = (size_t)member * m->b_per + m->b_off[l];
+		if (get) MCK(cudaMemcpy(host + o, Bsrc + bdev, m->dims[l + 1] * 4, cudaMemcpyDeviceToHost));
+		else MCK(cudaMemcpy(Bsrc + bdev, host + o, m->dims[l + 1] * 4, cudaMemcpyHostToDevice));
+		o += m->dims[l + 1];
+	}
+	return MF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MF_API mf_status mf_mlp_create(const mf_mlp_config* cfg, mf_mlp** out) {
+	if (!cfg || !out) return MF_ERR_ARG;
+	*out = nullptr;
+	if (cfg->members < 1 || cfg->members > 64 || cfg->n_layers < 1 || cfg->n_layers > MF_MLP_MAX_LAYERS ||
+	    cfg->max_batch < 1)
+		return MF_ERR_ARG;
+	if (cfg->max_batch > 65535) return MF_ERR_CAPACITY;  // gridDim.y of the GEMM tiles and the gather
+	for (int l = 0; l <= cfg->n_layers; l++) {
+		if (cfg->dims[l] < 1) return MF_ERR_ARG;
+		if (cfg->dims[l] > MF_MLP_MAX_WIDTH) return MF_ERR_CAPACITY;
+	}
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MF_ERR_NO_DEVICE;
+	if (cfg->device < 0 || cfg->device >= ndev) return MF_ERR_ARG;
+	if (cudaSetDevice(cfg->device) != cudaSuccess) return MF_ERR_NO_DEVICE;
+	mf_mlp* m = new mf_mlp();
+	m->members = cfg->members;
+	m->L = cfg->n_layers;
+	m->rows = cfg->max_batch;
+	m->device = cfg->device;
+	for (int l = 0; l <= m->L; l++) {
+		m->dims.push_back(cfg->dims[l]);
+		m->pd.push_back(pad16(cfg->dims[l]));
+		m->widest = std::max(m->widest, m->pd.back());
+	}
+	for (int l = 0; l < m->L; l++) {
+		m->w_off.push_back(m->w_per);
+		m->b_off.push_back(m->b_per);
+		m->w_per += (long long)m->pd[l + 1] * m->pd[l];
+		m->b_per += m->pd[l + 1];
+	}
+	const long long nw = m->w_per * m->members, nb = m->b_per * m->members;
+	// He-uniform weights U(-sqrt(6/fan_in), sqrt(6/fan_in)), zero biases, zero padding
+	std::vector<float> hw(nw, 0.f);
+	HostRng rng{cfg->seed};
+	for (int z = 0; z < m->members; z++)
+		for (int l = 0; l < m->L; l++) {
+			const float lim = std::sqrt(6.f / (float)m->dims[l]);
+			for (int o = 0; o < m->dims[l + 1]; o++)
+				for (int i = 0; i < m->dims[l]; i++)
+					hw[z * m->w_per + m->w_off[l] + (long long)o * m->pd[l] + i] = lim * rng.sym();
+		}
+	auto setup = [&]() -> mf_status {
+		MCK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+		Buf<float>* wbufs[] = {&m->W, &m->gW, &m->mW, &m->vW};
+		for (auto* b : wbufs) {
+			MCK(b->alloc(nw));
+			MCK(cudaMemset(b->p, 0, nw * 4));
+		}
+		Buf<float>* bbufs[] = {&m->Bias, &m->gB, &m->mB, &m->vB};
+		for (auto* b : bbufs) {
+			MCK(b->alloc(nb));
+			MCK(cudaMemset(b->p, 0, nb * 4));
+		}
+		MCK(m->Wb.alloc(nw));
+		MCK(cudaMemcpy(m->W.p, hw.data(), nw * 4, cudaMemcpyHostToDevice));
+		k_to_bf16<<<nblk(nw, 256), 256, 0, m->stream>>>(nw, m->W.p, m->Wb.p);
+		m->launches++;
+		MCK(cudaGetLastError());
+		m->H.resize(m->L);
+		for (int l = 0; l < m->L; l++) MCK(m->H[l].alloc((size_t)m->members * sH(m, l)));
+		const size_t act = (size_t)m->members * m->rows * m->widest;
+		MCK(m->Yp.alloc((size_t)m->members * sH(m, m->L)));
+		MCK(m->dz.alloc(act));
+		MCK(m->dh.alloc(act));
+		MCK(m->dzb.alloc(act));
+		MCK(m->loss.alloc(m->members));
+		MCK(m->Xin.alloc((size_t)m->members * m->rows * m->dims[0]));
+		MCK(m->Yin.alloc((size_t)m->members * m->rows * m->dims[m->L]));
+		MCK(m->ctl.alloc(1));
+		m->h_ctl = TrainCtl{};
+		m->h_ctl.seed = cfg->seed * 0x2545F4914F6CDD1Dull + 1;
+		MCK(cudaMemcpy(m->ctl.p, &m->h_ctl, sizeof(TrainCtl), cudaMemcpyHostToDevice));
+		MCK(cudaStreamSynchronize(m->stream));
+		return MF_OK;
+	};
+	mf_status st = setup();
+	if (st != MF_OK) {
+		delete m;
+		return st;
+	}
+	*out = m;
+	return MF_OK;
+}
+
+MF_API void mf_mlp_destroy(mf_mlp* m) {
+	if (!m) return;
+	cudaSetDevice(m->device);
+	delete m;
+}
+
+MF_API const char* mf_mlp_last_error(const mf_mlp* m) { return m ? m->err.c_str() : "null model"; }
+
+MF_API mf_status mf_mlp_num_params(const mf_mlp* m, uint64_t* n) {
+	if (!m || !n) return MF_ERR_ARG;
+	uint64_t t = 0;
+	for (int l = 0; l < m->L; l++) t += (uint64_t)m->dims[l + 1] * m->dims[l] + m->dims[l + 1];
+	*n = t;
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_get_params(mf_mlp* m, int32_t member, float* host) {
+	if (!m || !host || member < 0 || member >= m->members) return MF_ERR_ARG;
+	MCK(cudaSetDevice(m->device));
+	MCK(cudaStreamSynchronize(m->stream));
+	return param_walk(m, member, host, Walk::GetParams);
+}
+
+MF_API mf_status mf_mlp_get_grads(mf_mlp* m, int32_t member, float* host) {
+	if (!m || !host || member < 0 || member >= m->members) return MF_ERR_ARG;
+	MCK(cudaSetDevice(m->device));
+	MCK(cudaStreamSynchronize(m->stream));
+	return param_walk(m, member, host, Walk::GetGrads);
+}
+
+MF_API mf_status mf_mlp_set_params(mf_mlp* m, int32_t member, const float* host) {
+	if (!m || !host || member < 0 || member >= m->members) return MF_ERR_ARG;
+	MCK(cudaSetDevice(m->device));
+	MCK(cudaStreamSynchronize(m->stream));
+	mf_status st = param_walk(m, member, const_cast<float*>(host), Walk::SetParams);
+	if (st != MF_OK) return st;
+	const long long nw = m->w_per * m->members;
+	k_to_bf16<<<nblk(nw, 256), 256, 0, m->stream>>>(nw, m->W.p, m->Wb.p);
+	m->launches++;
+	MCK(cudaGetLastError());
+	MCK(cudaStreamSynchronize(m->stream));
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_gradients(mf_mlp* m, const float* x, const float* y, int32_t batch, float* loss) {
+	if (!m || !x || !y || batch < 1) return MF_ERR_ARG;
+	if (batch > m->rows) return MF_ERR_CAPACITY;
+	MCK(cudaSetDevice(m->device));
+	cudaStream_t s = m->stream;
+	const int in = m->dims[0], out = m->dims[m->L];
+	// [members][batch][...] rows into the [members][rows][...] slots
+	MCK(cudaMemcpy2DAsync(m->Xin.p, (size_t)m->rows * in * 4, x, (size_t)batch * in * 4, (size_t)batch * in * 4,
+	                      m->members, cudaMemcpyDefault, s));
+	MCK(cudaMemcpy2DAsync(m->Yin.p, (size_t)m->rows * out * 4, y, (size_t)batch * out * 4, (size_t)batch * out * 4,
+	                      m->members, cudaMemcpyDefault, s));
+	MCK(cudaMemsetAsync(m->loss.p, 0, m->members * 4, s));
+	const long long per = (long long)batch * m->pd[0];
+	k_input<<<nblk(per * m->members, 256), 256, 0, s>>>(m->members, batch, in, m->pd[0], m->Xin.p,
+	                                                    (long long)m->rows * in, m->H[0].p, sH(m, 0));
+	m->launches++;
+	MCK(cudaGetLastError());
+	MCK(forward_layers(m, batch));
+	MCK(backward_layers(m, m->Yin.p, batch));
+	if (loss) MCK(cudaMemcpyAsync(loss, m->loss.p, m->members * 4, cudaMemcpyDefault, s));
+	MCK(cudaStreamSynchronize(s));
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_set_data(mf_mlp* m, const float* x, const float* y, int32_t n) {
+	if (!m || !x || !y || n < 1) return MF_ERR_ARG;
+	MCK(cudaSetDevice(m->device));
+	MCK(cudaStreamSynchronize(m->stream));
+	const int in = m->dims[0], out = m->dims[m->L];
+	if (m->Xd.n < (size_t)n * in || m->Yd.n < (size_t)n * out) {
+		drop_graph(m);  // the captured gather holds the data pointers
+		MCK(m->Xd.alloc((size_t)n * in));
+		MCK(m->Yd.alloc((size_t)n * out));
+	}
+	MCK(cudaMemcpy(m->Xd.p, x, (size_t)n * in * 4, cudaMemcpyDefault));
+	MCK(cudaMemcpy(m->Yd.p, y, (size_t)n * out * 4, cudaMemcpyDefault));
+	m->h_ctl.n_data = (uint32_t)n;
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_train(mf_mlp* m, int32_t steps, float lr0, float lr1, float* loss_history) {
+	if (!m || steps < 0 || !(lr0 >= 0.f) || !(lr1 >= 0.f)) return MF_ERR_ARG;
+	if (!m->h_ctl.n_data) {
+		m->err = "mf_mlp_train: no training data (call mf_mlp_set_data first)";
+		return MF_ERR_STATE;
+	}
+	if (!steps) return MF_OK;
+	MCK(cudaSetDevice(m->device));
+	cudaStream_t s = m->stream;
+	MCK(cudaStreamSynchronize(s));
+	if (m->hist.n < (size_t)steps * m->members) MCK(m->hist.alloc((size_t)steps * m->members));
+	// the device step counter is authoritative; rewrite the schedule fields around it
+	TrainCtl cur;
+	MCK(cudaMemcpy(&cur, m->ctl.p, sizeof(TrainCtl), cudaMemcpyDeviceToHost));
+	m->h_ctl.step = cur.step;
+	m->h_ctl.t0 = cur.step;
+	m->h_ctl.total = (uint32_t)steps;
+	m->h_ctl.lr0 = lr0;
+	m->h_ctl.lr1 = lr1;
+	m->h_ctl.hist = m->hist.p;
+	MCK(cudaMemcpy(m->ctl.p, &m->h_ctl, sizeof(TrainCtl), cudaMemcpyHostToDevice));
+	if (!m->graph) {
+		cudaGraph_t g = nullptr;
+		MCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		const uint64_t before = m->launches;
+		cudaError_t e = train_step_launches(m);
+		cudaError_t e2 = cudaStreamEndCapture(s, &g);
+		m->step_launches = m->launches - before;
+		m->launches = before;
+		if (e != cudaSuccess || e2 != cudaSuccess) {
+			if (g) cudaGraphDestroy(g);
+			return mlp_fail(m, "capturing the training step", e != cudaSuccess ? e : e2);
+		}
+		e = cudaGraphInstantiate(&m->graph, g, 0);
+		cudaGraphDestroy(g);
+		if (e != cudaSuccess) {
+			m->graph = nullptr;
+			return mlp_fail(m, "cudaGraphInstantiate", e);
+		}
+	}
+	for (int t = 0; t < steps; t++) MCK(cudaGraphLaunch(m->graph, s));
+	m->launches += m->step_launches * (uint64_t)steps;
+	if (loss_history)
+		MCK(cudaMemcpyAsync(loss_history, m->hist.p, (size_t)steps * m->members * 4, cudaMemcpyDefault, s));
+	MCK(cudaStreamSynchronize(s));
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_predict(mf_mlp* m, const float* x, int32_t n, float* y) {
+	if (!m || n < 0 || (n > 0 && (!x || !y))) return MF_ERR_ARG;
+	MCK(cudaSetDevice(m->device));
+	cudaStream_t s = m->stream;
+	const int in = m->dims[0], out = m->dims[m->L];
+	for (int r0 = 0; r0 < n; r0 += m->rows) {
+		const int b = std::min(m->rows, n - r0);
+		MCK(cudaMemcpyAsync(m->Xin.p, x + (size_t)r0 * in, (size_t)b * in * 4, cudaMemcpyDefault, s));
+		const long long per = (long long)b * m->pd[0];
+		k_input<<<nblk(per * m->members, 256), 256, 0, s>>>(m->members, b, in, m->pd[0], m->Xin.p, 0, m->H[0].p, sH(m, 0));
+		m->launches++;
+		MCK(cudaGetLastError());
+		MCK(forward_layers(m, b));
+		// unpadded outputs into Yin ([members][rows][out]), then one 2D copy per chunk
+		const long long po = (long long)b * out;
+		k_output<<<nblk(po * m->members, 256), 256, 0, s>>>(m->members, b, out, m->pd[m->L], m->Yp.p, sH(m, m->L),
+		                                                   m->Yin.p, (long long)m->rows * out);
+		m->launches++;
+		MCK(cudaGetLastError());
+		MCK(cudaMemcpy2DAsync(y + (size_t)r0 * out, (size_t)n * out * 4, m->Yin.p, (size_t)m->rows * out * 4,
+		                      (size_t)b * out * 4, m->members, cudaMemcpyDefault, s));
+	}
+	MCK(cudaStreamSynchronize(s));
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_launch_count(const mf_mlp* m, uint64_t* launches) {
+	if (!m || !launches) return MF_ERR_ARG;
+	*launches = m->launches;
+	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_get_stream(const mf_mlp* m, void** stream) {
+	if (!m || !stream) return MF_ERR_ARG;
+	*stream = (void*)m->stream;
+	return MF_OK;
+}
+
+}  // extern "C"

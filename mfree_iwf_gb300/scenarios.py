@@ -140,14 +140,20 @@ def _ring_lattice(nbox: int, dx: float, ro: float, ri: float):
     return list(zip(px.tolist(), py.tolist()))
 
 
-def _ring_lattice_np(nbox: int, dx: float, ro: float, ri: float):
+def _ring_lattice_np(nbox: int, dx: float, ro: float, ri: float, edge_tol: float = 0.0):
     """Vectorised :func:`_ring_lattice`: the same IEEE operations elementwise
-    (px = -ro + i*dx, dist = sqrt(px*px + py*py)), i-major order."""
+    (px = -ro + i*dx, dist = sqrt(px*px + py*py)), i-major order.
+
+    edge_tol > 0 leaves out the lattice points within that relative distance of either
+    circle.  The lattice always has points exactly on the outer circle ((+-ro, 0) among
+    them, the points where two rings meet first); whether their rounded distance falls
+    below ro depends on ro's last bits, so without a tolerance two nearly equal radii
+    can give rings with different outlines."""
     i = np.arange(nbox, dtype=np.float64)
     p = -ro + i * dx
     PX, PY = np.meshgrid(p, p, indexing="ij")
     dist = np.sqrt(PX * PX + PY * PY)
-    mask = (dist < ro) & (dist >= ri)
+    mask = (dist < ro * (1.0 - edge_tol)) & (dist >= ri * (1.0 + edge_tol))
     return PX[mask], PY[mask]
 
 
@@ -202,12 +208,17 @@ def rings(
     stress_exponent: float = 4.0,
     xsph_eps: float = 0.5,
     nbh_eps: float = 1e-6,
+    edge_tol: float = 0.0,
+    exact_hull: bool = False,
     name: str = "",
 ) -> Scenario:
     """Two rings on a square lattice, as rings_monaghan (rings.cpp:20-99),
     rings_monaghan_contact (:522-621) and rings_tl_contact (:338-429) build them.
 
     Defaults are the reference's constants; ``dt=None`` selects dt = cfl*h/c0.
+    ``exact_hull`` runs the hull's orientation tests on the integer lattice indices
+    instead of the rounded coordinates, so the points kept on straight hull edges do not
+    depend on rounding (the reference tests the coordinates).
     """
     if spacing is None:
         spacing = ro + 0.001
@@ -226,7 +237,7 @@ def rings(
         a["quad_weight"][:] = a["m"] / a["rho"]
         a["vx"][:] = vx
 
-    px, py = _ring_lattice_np(nbox, dx, ro, ri)
+    px, py = _ring_lattice_np(nbox, dx, ro, ri, edge_tol)
     # hull candidates: only lattice points within 3 dx of the outer circle can be hull
     # vertices or lie on hull edges, and the monotone chain visits any subset in the
     # same relative order, so the hull of the subset is the hull of the ring
@@ -244,7 +255,11 @@ def rings(
             ys = py.copy()
             a = _body_from_lists(xs, ys, xs if tl else None, ys if tl else None)
             finish(a, v)
-            hull = cand[convex_hull(xs[cand], ys[cand])].astype(np.uint32)
+            if exact_hull:
+                li, lj = np.rint((px + ro) / dx), np.rint((py + ro) / dx)
+                hull = cand[convex_hull(li[cand], lj[cand])].astype(np.uint32)
+            else:
+                hull = cand[convex_hull(xs[cand], ys[cand])].astype(np.uint32)
             sc.bodies.append(Body(a, hull=hull))
         sc.contact = 1
 
