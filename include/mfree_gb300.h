@@ -199,6 +199,16 @@ MF_API mf_status mf_autotune(mf_ctx* ctx, int32_t trial_steps, char* report, uin
  * row-major [row][body][4] floats (row = step % capacity), and their count. */
 MF_API mf_status mf_set_monitor(mf_ctx* ctx, uint32_t capacity);
 MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
+/* Tuning options (no counterpart in the reference).  Keys:
+ *   "tl_tiles"        0 (default) / 1: the mixed TL passes gather neighbours from global
+ *                     memory / stage each 128-row tile's neighbours in shared memory
+ *                     (bit-identical results; the tiles are built at set-up, so set 1
+ *                     before the first step)
+ * read-only, through mf_get_option:
+ *   "tl_tiles_built"  1 when the halo tiles exist (mixed TL, after the first step)
+ *   "tl_halo_max"     the largest tile halo, in rows */
+MF_API mf_status mf_set_option(mf_ctx* ctx, const char* key, int64_t value);
+MF_API mf_status mf_get_option(mf_ctx* ctx, const char* key, int64_t* value);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
 MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
 

@@ -107,6 +107,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
         "mf_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, C.c_uint32]),
         "mf_set_monitor": (C.c_int32, [C.c_void_p, C.c_uint32]),
+        "mf_set_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_int64]),
+        "mf_get_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),
         "mf_get_monitor": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), _UP]),
     }
     for name, (res, args) in sig.items():
@@ -295,6 +297,14 @@ class Simulation:
         buf = ctypes.create_string_buffer(2048)
         self._check(self._lib.mf_autotune(self._h, int(trial_steps), buf, len(buf)), "mf_autotune")
         return buf.value.decode()
+
+    def set_option(self, key: str, value: int) -> None:
+        self._check(self._lib.mf_set_option(self._h, key.encode(), int(value)), "mf_set_option")
+
+    def get_option(self, key: str) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.mf_get_option(self._h, key.encode(), ctypes.byref(v)), "mf_get_option")
+        return v.value
 
     def set_monitor(self, capacity: int) -> None:
         self._check(self._lib.mf_set_monitor(self._h, int(capacity)), "mf_set_monitor")

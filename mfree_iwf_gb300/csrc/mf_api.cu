@@ -2,6 +2,7 @@
 // validation against the fused pipelines, device memory, and the step loop of the
 // reference driver (mfree_iwf.cpp:84-97) expressed as stream-ordered launches.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <map>
@@ -10,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -129,6 +131,7 @@ struct Timing {
 // Launch shape of the hot kernels, chosen by mf_autotune.
 struct Tune {
 	uint32_t ul_block = 128, ul_persistent = 0, ul_chunk = 1, tl_block = 128;
+	uint32_t tl_tiled = 0;  // mixed TL: the halo-tile passes (built at set-up when requested)
 };
 std::mutex g_tune_mutex;
 std::map<std::string, Tune> g_tune_cache;
@@ -172,8 +175,16 @@ struct mf_ctx {
 	DevBuf<double> wx64, wy64, P64, dA64, c64, bc_v;
 	DevBuf<double2> sw64;
 	DevBuf<float2> sw32, swA32;
+	// mixed TL halo tiles (TLArgs::t_*)
+	DevBuf<uint32_t> tt_rows, tt_halo_off, tt_halo, tt_sl;
+	DevBuf<uint16_t> tt_cnt, tt_loc;
+	DevBuf<float2> tt_sw, tt_swA;
+	uint32_t tt_n_tiles = 0, tt_halo_max = 0, tt_ent_max = 0;
+	bool tt_ok = false;
 	DevBuf<float> qw32, m32, h32;
 	DevBuf<float4> recA, recB, dA32;
+	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
+	bool tl_recs_valid = false;       // the stage-0 records match the state (pass B keeps them current)
 	uint32_t n_bc = 0;
 
 	// TL_WEAK: Gauss points and the three list sets (sliced ELL)
@@ -512,6 +523,131 @@ mf_status ul_step(mf_ctx* c) {
 	return MF_OK;
 }
 
+// Halo tiles of the mixed TL passes.  Rows are ordered along a Z-order (Morton) curve
+// of their reference positions, quantised at half the search h, and cut into tiles
+// of TL_TILE consecutive positions: compact 2-D patches.  A tile's halo is the sorted
+// set of every row its rows' lists name; each list entry becomes the entry's slot in
+// that halo.  The lists stay in their ascending-j order, so each row sums exactly as
+// before.  Tiles whose halo would not fit the shared-memory budget leave the untiled
+// passes in use.
+uint32_t morton_spread(uint32_t v) {
+	v &= 0xffffu;
+	v = (v | (v << 8)) & 0x00ff00ffu;
+	v = (v | (v << 4)) & 0x0f0f0f0fu;
+	v = (v | (v << 2)) & 0x33333333u;
+	v = (v | (v << 1)) & 0x55555555u;
+	return v;
+}
+
+mf_status build_tl_tiles(mf_ctx* c, const std::vector<uint32_t>& off) {
+	const uint32_t n = c->n_total, T = TL_TILE;
+	const uint32_t HALO_CAP = 2048;  // 128 KB of records in pass B
+	c->tt_ok = false;
+	if (n == 0) return MF_OK;
+	std::vector<uint32_t> nbr(off[n]);
+	CK(cudaMemcpy(nbr.data(), c->nbr.p, (size_t)off[n] * 4, cudaMemcpyDeviceToHost));
+	std::vector<double> X(n), Y(n);
+	for (auto& b : c->bodies) {
+		std::copy(b.in[2].begin(), b.in[2].end(), X.begin() + b.off);
+		std::copy(b.in[3].begin(), b.in[3].end(), Y.begin() + b.off);
+	}
+	double mnx = 1e300, mny = 1e300, mxx = -1e300, mxy = -1e300;
+	for (uint32_t i = 0; i < n; i++) {
+		mnx = std::min(mnx, X[i]); mxx = std::max(mxx, X[i]);
+		mny = std::min(mny, Y[i]); mxy = std::max(mxy, Y[i]);
+	}
+	double ext = std::max(mxx - mnx, mxy - mny);
+	double qz = 0.5 * c->cfg.nbh_h;
+	if (!(qz > 0.) || ext / qz > 65535.) qz = ext > 0. ? ext / 65535. : 1.;
+	std::vector<uint64_t> key(n);
+	for (uint32_t i = 0; i < n; i++) {
+		uint32_t ix = (uint32_t)std::min(65535., (X[i] - mnx) / qz), iy = (uint32_t)std::min(65535., (Y[i] - mny) / qz);
+		key[i] = ((uint64_t)(morton_spread(ix) | (morton_spread(iy) << 1)) << 32) | i;
+	}
+	std::sort(key.begin(), key.end());
+	std::vector<uint32_t> rows(n);
+	for (uint32_t p = 0; p < n; p++) rows[p] = (uint32_t)key[p];
+	key.clear();
+	key.shrink_to_fit();
+	const uint32_t nt = (n + T - 1) / T, ns = (n + 31) / 32;
+	std::vector<uint32_t> tsl(ns + 1);
+	uint64_t ent = 0;
+	for (uint32_t s_ = 0; s_ < ns; s_++) {
+		uint32_t w = 0;
+		for (uint32_t p = 32 * s_; p < std::min(n, 32 * s_ + 32); p++) w = std::max(w, off[rows[p] + 1] - off[rows[p]]);
+		tsl[s_] = (uint32_t)ent;
+		ent += 32ull * w;
+	}
+	if (ent > 0xffffffffull) return MF_OK;
+	tsl[ns] = (uint32_t)ent;
+	std::vector<uint16_t> loc(ent, 0);
+	std::vector<std::vector<uint32_t>> halos(nt);
+	std::atomic<uint32_t> next{0};
+	std::atomic<bool> too_big{false};
+	auto work = [&]() {
+		std::vector<uint32_t> js;
+		for (uint32_t t; (t = next.fetch_add(1)) < nt;) {
+			uint32_t p0 = t * T, p1 = std::min(n, p0 + T);
+			js.clear();
+			for (uint32_t p = p0; p < p1; p++) js.insert(js.end(), nbr.begin() + off[rows[p]], nbr.begin() + off[rows[p] + 1]);
+			std::sort(js.begin(), js.end());
+			js.erase(std::unique(js.begin(), js.end()), js.end());
+			if (js.size() > HALO_CAP) {
+				too_big = true;
+				continue;
+			}
+			for (uint32_t p = p0; p < p1; p++) {
+				uint32_t i = rows[p];
+				uint64_t q = tsl[p >> 5] + (p & 31u);
+				for (uint32_t k = off[i]; k < off[i + 1]; k++, q += 32)
+					loc[q] = (uint16_t)(std::lower_bound(js.begin(), js.end(), nbr[k]) - js.begin());
+			}
+			halos[t] = js;
+		}
+	};
+	unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+	std::vector<std::thread> pool;
+	for (unsigned k = 1; k < nth; k++) pool.emplace_back(work);
+	work();
+	for (auto& th : pool) th.join();
+	if (too_big) return MF_OK;
+	std::vector<uint32_t> hoff(nt + 1, 0), halo;
+	uint32_t hmax = 1;
+	for (uint32_t t = 0; t < nt; t++) {
+		hoff[t] = (uint32_t)halo.size();
+		halo.insert(halo.end(), halos[t].begin(), halos[t].end());
+		hmax = std::max(hmax, (uint32_t)halos[t].size());
+	}
+	hoff[nt] = (uint32_t)halo.size();
+	CK(c->tt_rows.alloc(n)); CK(c->tt_halo_off.alloc(nt + 1)); CK(c->tt_halo.alloc(halo.size()));
+	CK(c->tt_sl.alloc(ns + 1)); CK(c->tt_cnt.alloc(n)); CK(c->tt_loc.alloc(ent));
+	CK(c->tt_sw.alloc(ent)); CK(c->tt_swA.alloc(ent));
+	CK(cudaMemcpy(c->tt_rows.p, rows.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->tt_halo_off.p, hoff.data(), (size_t)(nt + 1) * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->tt_halo.p, halo.data(), halo.size() * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->tt_sl.p, tsl.data(), (size_t)(ns + 1) * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->tt_loc.p, loc.data(), (size_t)ent * 2, cudaMemcpyHostToDevice));
+	cudaError_t e = c->strict ? mf_strict::tl_tile_sell(n, c->tt_rows.p, c->sl_off.p, c->scnt.p, c->sw32.p, c->swA32.p,
+	                                                    c->tt_sl.p, c->tt_cnt.p, c->tt_sw.p, c->tt_swA.p, c->stream)
+	                          : mf_fast::tl_tile_sell(n, c->tt_rows.p, c->sl_off.p, c->scnt.p, c->sw32.p, c->swA32.p,
+	                                                  c->tt_sl.p, c->tt_cnt.p, c->tt_sw.p, c->tt_swA.p, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "tl_tile_sell");
+	uint32_t emax = 32;
+	for (uint32_t t = 0; t < nt; t++) {
+		uint32_t s0 = t * (T / 32), s1 = std::min(s0 + T / 32, ns);
+		emax = std::max(emax, tsl[s1] - tsl[s0]);
+	}
+	if (64ull * hmax > 200 * 1024) return MF_OK;  // the untiled passes stay in use
+	e = c->strict ? mf_strict::tl_tile_attrs(hmax, emax) : mf_fast::tl_tile_attrs(hmax, emax);
+	if (e != cudaSuccess) return cuda_fail(c, e, "tl_tile_attrs");
+	CK(cudaStreamSynchronize(c->stream));
+	c->tt_n_tiles = nt;
+	c->tt_halo_max = hmax;
+	c->tt_ent_max = emax;
+	c->tt_ok = true;
+	return MF_OK;
+}
+
 TLArgs tl_args(mf_ctx* c) {
 	TLArgs a{};
 	a.n_total = c->n_total;
@@ -543,6 +679,19 @@ TLArgs tl_args(mf_ctx* c) {
 	a.n_bc = c->n_bc;
 	a.status = c->d_status;
 	a.block = c->tune.tl_block;
+	if (c->mixed && c->tt_ok && c->tune.tl_tiled) {
+		a.t_rows = c->tt_rows.p;
+		a.t_halo_off = c->tt_halo_off.p;
+		a.t_halo = c->tt_halo.p;
+		a.t_sl = c->tt_sl.p;
+		a.t_cnt = c->tt_cnt.p;
+		a.t_loc = c->tt_loc.p;
+		a.t_sw = c->tt_sw.p;
+		a.t_swA = c->tt_swA.p;
+		a.n_tiles = c->tt_n_tiles;
+		a.halo_max = c->tt_halo_max;
+		a.t_ent_max = c->tt_ent_max;
+	}
 	return a;
 }
 
@@ -556,13 +705,21 @@ cudaError_t tl_launch(mf_ctx* c, const TLArgs& a, int part) {
 mf_status tl_step_all(mf_ctx* c) {
 	TLArgs a = tl_args(c);
 	StateSoA S0 = a.st, S1 = a.nxt;
+	// mixed form: pass B writes the next stage's records (no pack kernel), except with
+	// boundary conditions, which change the stage state after pass B
+	const bool fused = c->mixed && c->n_bc == 0;
+	void* rb[2] = {c->recB.p, c->recB2.p};
 	for (uint32_t st = 0; st < 4; st++) {
 		a.stage = st;
 		a.st = (st % 2 == 0) ? S0 : S1;
 		a.nxt = (st % 2 == 0) ? S1 : S0;
+		a.recB = fused ? rb[st & 1] : rb[0];
+		a.recB_out = rb[(st + 1) & 1];
+		a.write_recs = fused ? 1u : 0u;
+		const bool pack = c->mixed && (!fused || (st == 0 && !c->tl_recs_valid));
 		cudaError_t e;
 		if ((e = tl_launch(c, a, 0)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
-		if ((e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
+		if (pack && (e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
 		int slot;
 		timing_begin(c, 1, slot);
 		if ((e = tl_launch(c, a, 2)) != cudaSuccess) return cuda_fail(c, e, "tl pass A");
@@ -570,12 +727,27 @@ mf_status tl_step_all(mf_ctx* c) {
 		timing_begin(c, 2, slot);
 		if ((e = tl_launch(c, a, 3)) != cudaSuccess) return cuda_fail(c, e, "tl pass B");
 		timing_end(c, slot, c->n_total);
-		c->launches += 2 + (c->n_bc ? 1 : 0) + (c->mixed ? 1 : 0);
+		c->launches += 2 + (c->n_bc ? 1 : 0) + (pack ? 1 : 0);
 	}
+	if (fused) c->tl_recs_valid = true;
 	cudaError_t e;
 	if ((e = tl_launch(c, a, 4)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
 	if ((e = tl_launch(c, a, 5)) != cudaSuccess) return cuda_fail(c, e, "tl clock");
 	c->launches += 1 + (c->n_bc ? 1 : 0);
+	return MF_OK;
+}
+
+// Mixed TL: pack the stage-0 records now (outside a graph capture), so that the
+// captured step needs no pack kernel.
+mf_status tl_prepack(mf_ctx* c) {
+	if (c->cfg.method != MF_METHOD_TL || !c->mixed || c->n_bc || c->tl_recs_valid) return MF_OK;
+	TLArgs a = tl_args(c);
+	a.stage = 0;
+	a.recB = c->recB.p;
+	cudaError_t e = tl_launch(c, a, 1);
+	if (e != cudaSuccess) return cuda_fail(c, e, "tl pack");
+	c->launches++;
+	c->tl_recs_valid = true;
 	return MF_OK;
 }
 
@@ -711,17 +883,19 @@ mf_status tl_setup(mf_ctx* c) {
 		CK(c->sw64.alloc(ent));
 	}
 	e = c->strict ? mf_strict::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
-	                                      c->snbr.p, c->sw64.p, nullptr, nullptr, c->qw0.p, c->stream)
+	                                      c->snbr.p, c->sw64.p, nullptr, nullptr, c->qw0.p, c->m.p, c->stream)
 	              : mf_fast::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
 	                                    c->snbr.p, c->mixed ? nullptr : (void*)c->sw64.p,
 	                                    c->mixed ? (void*)c->sw32.p : nullptr, c->mixed ? (void*)c->swA32.p : nullptr,
-	                                    c->qw0.p, c->stream);
+	                                    c->qw0.p, c->m.p, c->stream);
 	if (e != cudaSuccess) return cuda_fail(c, e, "tl_to_sell");
 	CK(cudaStreamSynchronize(c->stream));
 	c->wx64.free();
 	c->wy64.free();
+	if (c->mixed && c->tune.tl_tiled && (st = build_tl_tiles(c, off)) != MF_OK) return st;
 	if (c->mixed) {
-		CK(c->recA.alloc(n)); CK(c->recB.alloc(4 * (size_t)n)); CK(c->dA32.alloc(n));
+		CK(c->recA.alloc(n)); CK(c->recB.alloc(4 * (size_t)n)); CK(c->recB2.alloc(4 * (size_t)n)); CK(c->dA32.alloc(n));
+		c->tl_recs_valid = false;
 		auto f32 = [&](DevBuf<float>& d, int field) -> mf_status {
 			CK(d.alloc(n));
 			std::vector<float> v(n);
@@ -1193,6 +1367,9 @@ mf_ctx::~mf_ctx() {
 		g_w64.free(); t_w64.free(); p_w64.free(); g_w32.free(); t_w32.free(); p_w32.free();
 	}
 	sl_off.free(); snbr.free(); scnt.free(); sw64.free(); sw32.free(); swA32.free(); recA.free(); recB.free(); dA32.free();
+	recB2.free();
+	tt_rows.free(); tt_halo_off.free(); tt_halo.free(); tt_sl.free(); tt_cnt.free(); tt_loc.free(); tt_sw.free();
+	tt_swA.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
 	                            &slave_rows, &slave_master, &m_tile_off, &m_tile_n};
 	for (auto* p : u32s) p->free();
@@ -1397,6 +1574,8 @@ void drop_graph(mf_ctx* c) {
 // Capture one step on the context's stream and instantiate it for replay.
 mf_status capture_step(mf_ctx* c) {
 	drop_graph(c);
+	mf_status pst = tl_prepack(c);
+	if (pst != MF_OK) return pst;
 	uint64_t l0 = c->launches;
 	CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
 	mf_status st = one_step(c);
@@ -1510,6 +1689,9 @@ MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 		}
 	}
 	CK(cudaGetLastError());
+	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the new state
+	mf_status pst = tl_prepack(c);
+	if (pst != MF_OK) return pst;
 	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
 }
@@ -1640,6 +1822,9 @@ mf_status snapshot_take(mf_ctx* c, Snapshot& s) {
 mf_status snapshot_restore(mf_ctx* c, Snapshot& s) {
 	for (size_t i = 0; i < s.bufs.size(); i++)
 		CK(cudaMemcpyAsync(s.src[i].first, s.bufs[i].p, s.src[i].second, cudaMemcpyDeviceToDevice, c->stream));
+	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the restored state
+	mf_status pst = tl_prepack(c);
+	if (pst != MF_OK) return pst;
 	for (size_t b = 0; b < c->bodies.size(); b++) c->bodies[b].time = s.times[b];
 	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
@@ -1694,8 +1879,14 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 			}
 		} else {
 			t.tl_block = bs;
+			t.tl_tiled = 0;
 			cands.push_back(t);
 		}
+	}
+	if (c->cfg.method == MF_METHOD_TL && c->mixed && c->tt_ok) {
+		Tune t = c->tune;
+		t.tl_tiled = 1;  // the tiled passes have a fixed block (one tile)
+		cands.push_back(t);
 	}
 	Snapshot snap;
 	if ((st = snapshot_take(c, snap)) != MF_OK) return st;
@@ -1719,8 +1910,8 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		float ms = 0.f;
 		cudaEventElapsedTime(&ms, e0, e1);
 		double per = ms / trial_steps;
-		snprintf(line, sizeof line, "%s[b%u p%u c%u tl%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block, t.ul_persistent,
-		         t.ul_chunk, t.tl_block, per);
+		snprintf(line, sizeof line, "%s[b%u p%u c%u tl%u t%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block,
+		         t.ul_persistent, t.ul_chunk, t.tl_block, t.tl_tiled, per);
 		rep += line;
 		if (per < best) {
 			best = per;
@@ -1745,6 +1936,36 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 	rep += line;
 	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
 	return MF_OK;
+}
+
+MF_API mf_status mf_set_option(mf_ctx* c, const char* key, int64_t value) {
+	if (!c || !key) return MF_ERR_ARG;
+	if (!strcmp(key, "tl_tiles")) {
+		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "tl_tiles must be 0 or 1");
+		if (value == 1 && c->ready && !c->tt_ok)
+			return fail(c, MF_ERR_STATE, "tl_tiles: the halo tiles are built at set-up; set the option before the first step");
+		c->tune.tl_tiled = (uint32_t)value;
+		drop_graph(c);
+		return MF_OK;
+	}
+	return fail(c, MF_ERR_ARG, "unknown option '%s'", key);
+}
+
+MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
+	if (!c || !key || !value) return MF_ERR_ARG;
+	if (!strcmp(key, "tl_tiles")) {
+		*value = c->tune.tl_tiled;
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_tiles_built")) {
+		*value = c->tt_ok ? 1 : 0;
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_halo_max")) {
+		*value = c->tt_halo_max;
+		return MF_OK;
+	}
+	return fail(c, MF_ERR_ARG, "unknown option '%s'", key);
 }
 
 MF_API mf_status mf_set_monitor(mf_ctx* c, uint32_t capacity) {

@@ -106,17 +106,35 @@ struct TLArgs {
 	const uint32_t* sl_off;
 	const uint16_t* cnt;
 	const uint32_t* snbr;
-	const void* sw;                      // corrected gradient per pair: double2 (FP64 forms) / float2 (mixed)
+	const void* sw;                      // corrected gradient per pair: double2 (FP64 forms) / float2 times m_j (mixed)
 	const void* swA;                     // mixed: the gradient times the neighbour's quad weight (pass A)
 	void *P, *dA, *c;                    // per-stage scratch (FP64 forms)
 	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
+	void* recB_out;                      // mixed: pass B writes the next stage's records here...
+	uint32_t write_recs;                 // ...and into recA when set (no separate pack then)
 	void* dA32;                          // mixed: rate terms (float4 per row)
 	const uint32_t* bc_rows;
 	const double* bc_v;
 	uint32_t n_bc;
 	void* status;
 	uint32_t block;                      // rows per block of the pair passes (autotuned)
+	// mixed form, halo tiles: tile t holds positions [t*TL_TILE, (t+1)*TL_TILE) of a
+	// space-filling-curve order (t_rows[p] = row); its halo -- every row a list of the
+	// tile names -- is t_halo[t_halo_off[t] .. t_halo_off[t+1]) (ascending), staged in
+	// shared memory by the pass; lists are sliced ELL over positions holding the halo
+	// slot (t_loc) and the same FP32 weights as sw / swA.  t_rows == nullptr: untiled.
+	const uint32_t* t_rows;
+	const uint32_t* t_halo_off;
+	const uint32_t* t_halo;
+	const uint32_t* t_sl;
+	const uint16_t* t_cnt;
+	const uint16_t* t_loc;
+	const void* t_sw;
+	const void* t_swA;
+	uint32_t n_tiles, halo_max;
+	uint32_t t_ent_max;  // most list entries (sliced-ELL slots) of one tile
 };
+constexpr uint32_t TL_TILE = 128;
 
 // One weak-form stage: particles (state x, y, vx, vy) and Gauss points (state rho,
 // Sxx, Sxy, Syy in the rho/Sxx/Sxy/Syy or *_f slots of the StateSoA).
@@ -173,8 +191,12 @@ struct ContactArgs {
 	cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s);                             \
 	cudaError_t tl_to_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy, \
 	                       const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* sw64, void* sw32,     \
-	                       void* swA32, const double* qw, cudaStream_t s);                                    \
+	                       void* swA32, const double* qw, const double* mass, cudaStream_t s);                \
 	cudaError_t tl_stage(const mfk_host::TLArgs& a, bool mixed, int part, cudaStream_t s);                   \
+	cudaError_t tl_tile_sell(uint32_t n, const uint32_t* t_rows, const uint32_t* sl_off, const uint16_t* cnt, \
+	                         const void* sw, const void* swA, const uint32_t* t_sl, uint16_t* t_cnt, void* t_sw, \
+	                         void* t_swA, cudaStream_t s);                                                  \
+	cudaError_t tl_tile_attrs(uint32_t halo_max, uint32_t ent_max);                                          \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
 	cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,  \
 	                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px,     \

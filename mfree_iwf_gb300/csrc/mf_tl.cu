@@ -26,6 +26,7 @@ using namespace mfk;
 using mfk_host::BodyParams;
 using mfk_host::TLArgs;
 using mfk_host::TLSearchArgs;
+using mfk_host::TL_TILE;
 
 namespace MF_NS {
 namespace {
@@ -331,24 +332,120 @@ struct __align__(16) RecB {
 	float4 P, x, v, hmrc;
 };
 
-__global__ void k_tl_pack(TLArgs a) {
-	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= a.n_total) return;
-	const mfk_host::StateSoA& s = a.st;
-	double x = s.x[i], y = s.y[i], vx = s.vx[i], vy = s.vy[i];
+// The records of row i from its state (x, y, vx, vy in FP64, rho - rho0 in FP32).
+__device__ __forceinline__ void tl_pack_row(const TLArgs& a, uint32_t i, const BodyParams& pr, double x, double y,
+                                            double vx, double vy, float rho_dev, RecB* recB) {
 	FF ux = ff_split(x - a.X[i]), uy = ff_split(y - a.Y[i]);
 	((float4*)a.recA)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
 	FF fx = ff_split(x), fy = ff_split(y), fvx = ff_split(vx), fvy = ff_split(vy);
-	RecB* rb = (RecB*)a.recB + i;
+	RecB* rb = recB + i;
 	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
-	const BodyParams& pr = a.params[a.body_of[i]];
-	float rho = s.rho_f[i] + (float)pr.rho0;  // the mixed state holds rho - rho0
+	float rho = rho_dev + (float)pr.rho0;  // the mixed state holds rho - rho0
 	float K = (float)pr.K;
 	rb->hmrc = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
 }
 
+__global__ void k_tl_pack(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	tl_pack_row(a, i, a.params[a.body_of[i]], s.x[i], s.y[i], s.vx[i], s.vy[i], s.rho_f[i], (RecB*)a.recB);
+}
+
 __device__ __forceinline__ float ffd(float ahi, float alo, float bhi, float blo) { return (ahi - bhi) + (alo - blo); }
+
+// Monaghan-Gingold viscosity Pi_ij of an approaching pair (correctors.h:83-137), FP32
+// with the two divisions as reciprocal-multiply (__fdividef, 2 ulp)
+__device__ __forceinline__ float art_visc_pi(float4 hmrc_i, float4 hmrc_j, float xij, float yij, float vijposij,
+                                             float alpha, float beta, float eta2) {
+	float cij = 0.5f * (hmrc_i.w + hmrc_j.w);
+	float hij = 0.5f * (hmrc_i.x + hmrc_j.x);
+	float rhoij = 0.5f * (hmrc_i.z + hmrc_j.z);
+	float r2ij = xij * xij + yij * yij;
+	float muij = __fdividef(hij * vijposij, r2ij + eta2 * hij * hij);
+	return __fdividef(-alpha * cij * muij + beta * muij * muij, rhoij);
+}
+
+// End of pass B for row i: momentum, advection and the RK4 update (rk4.h:52-108).
+// Every load of the row is issued before the first store: the state arrays are
+// distinct, but the compiler cannot know that and would otherwise wait for each load
+// in turn behind the stores.  The loads stay after the pair loop (the empty asm is a
+// compiler barrier): hoisted above it they would hold ~40 registers through the loop.
+__device__ __forceinline__ void tlB_finish(const TLArgs& a, uint32_t i, const BodyParams& pr, float rho0, float Pxx_x,
+                                           float Pyx_y, float Pxy_x, float Pyy_y, float av_x, float av_y) {
+	asm volatile("" ::: "memory");
+	const mfk_host::StateSoA& s = a.st;
+	const uint32_t flags = a.flags, stg = a.stage;
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* np[4] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy};
+	float* bq[4] = {a.base.rho_f, a.base.Sxx_f, a.base.Sxy_f, a.base.Syy_f};
+	float* aq[4] = {a.acc.rho_f, a.acc.Sxx_f, a.acc.Sxy_f, a.acc.Syy_f};
+	float* nq[4] = {a.nxt.rho_f, a.nxt.Sxx_f, a.nxt.Sxy_f, a.nxt.Syy_f};
+	const float4 dAi = ((const float4*)a.dA32)[i];
+	const double vxs = (flags & A_ADVECTION) ? s.vx[i] : 0., vys = (flags & A_ADVECTION) ? s.vy[i] : 0.;
+	double fx = 0., fy = 0., mi = 1.;
+	if (flags & A_MOMENTUM_TL) {
+		fx = a.fcx[i];
+		fy = a.fcy[i];
+		mi = a.m[i];
+	}
+	double bv[4], av[4] = {0., 0., 0., 0.};
+	float bf[4], af[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+	for (int q2 = 0; q2 < 4; q2++) {
+		bv[q2] = bp[q2][i];
+		bf[q2] = bq[q2][i];
+		if (stg > 0) {
+			av[q2] = ap[q2][i];
+			af[q2] = aq[q2][i];
+		}
+	}
+	double d[4];
+	d[0] = vxs;
+	d[1] = vys;
+	d[2] = av_x;
+	d[3] = av_y;
+	if (flags & A_MOMENTUM_TL) {
+		d[2] += (double)(1.f / rho0 * (Pxx_x + Pyx_y)) + fx / mi;
+		d[3] += (double)(1.f / rho0 * (Pxy_x + Pyy_y)) + fy / mi;
+	}
+	const float e[4] = {dAi.x, dAi.y, dAi.z, dAi.w};
+	const double dt = pr.dt;
+	double nv[4];  // the next stage's x, y, vx, vy
+	float nrho;    // and its rho - rho0
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q2 = 0; q2 < 4; q2++) {
+			ap[q2][i] = (stg == 0) ? d[q2] : av[q2] + 2 * d[q2];
+			nv[q2] = bv[q2] + d[q2] * dts;
+			np[q2][i] = nv[q2];
+			aq[q2][i] = (stg == 0) ? e[q2] : af[q2] + 2.f * e[q2];
+			float f = bf[q2] + e[q2] * (float)dts;
+			nq[q2][i] = f;
+			if (q2 == 0) nrho = f;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+		bool ok = true;
+#pragma unroll
+		for (int q2 = 0; q2 < 4; q2++) {
+			double v = bv[q2] + w6 * (av[q2] + d[q2]);
+			bp[q2][i] = v;
+			np[q2][i] = v;
+			nv[q2] = v;
+			ok = ok && isfinite(v);
+			float f = bf[q2] + (float)w6 * (af[q2] + e[q2]);
+			bq[q2][i] = f;
+			nq[q2][i] = f;
+			if (q2 == 0) nrho = f;
+		}
+		if (!ok) raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+	if (a.write_recs) tl_pack_row(a, i, pr, nv[0], nv[1], nv[2], nv[3], nrho, (RecB*)a.recB_out);
+}
 
 __global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -394,10 +491,9 @@ __global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 	((float4*)a.dA32)[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
 }
 
-__global__ void __launch_bounds__(256) k_tlB32(TLArgs a) {
+__global__ void __launch_bounds__(256, 4) k_tlB32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
-	const mfk_host::StateSoA& s = a.st;
 	const float2* sw = (const float2*)a.sw;
 	const RecB* recB = (const RecB*)a.recB;
 	uint32_t flags = a.flags;
@@ -412,13 +508,11 @@ __global__ void __launch_bounds__(256) k_tlB32(TLArgs a) {
 #pragma unroll 2
 	for (uint32_t k = 0; k < c; k++, q += 32) {
 		uint32_t j = a.snbr[q];
-		float2 w = sw[q];
+		float2 w = sw[q];  // the neighbour's mass times its corrected gradient
 		const RecB* rj = recB + j;
-		float4 hmrc = __ldg(&rj->hmrc);
-		float mj = hmrc.y;
 		if (flags & A_STRESS_TL) {
 			float4 Pj = __ldg(&rj->P);
-			float fx = mj * sc * w.x, fy = mj * sc * w.y;
+			float fx = sc * w.x, fy = sc * w.y;
 			Pxx_x += (ri.P.x + Pj.x) * fx;
 			Pyx_y += (ri.P.z + Pj.z) * fy;
 			Pxy_x += (ri.P.y + Pj.y) * fx;
@@ -430,67 +524,166 @@ __global__ void __launch_bounds__(256) k_tlB32(TLArgs a) {
 			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
 			float vijposij = vijx * xij + vijy * yij;
 			if (vijposij < 0.f) {
-				float cij = 0.5f * (ri.hmrc.w + hmrc.w);
-				float hij = 0.5f * (ri.hmrc.x + hmrc.x);
-				float rhoij = 0.5f * (ri.hmrc.z + hmrc.z);
-				float r2ij = xij * xij + yij * yij;
-				float muij = (hij * vijposij) / (r2ij + eta2 * hij * hij);
-				float piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
-				av_x += -mj * piij * w.x;
-				av_y += -mj * piij * w.y;
+				float4 hmrc = __ldg(&rj->hmrc);
+				float piij = art_visc_pi(ri.hmrc, hmrc, xij, yij, vijposij, alpha, beta, eta2);
+				av_x += -piij * w.x;
+				av_y += -piij * w.y;
 			}
 		}
 	}
-	float4 dAi = ((const float4*)a.dA32)[i];
-	double d[4];
-	d[0] = (flags & A_ADVECTION) ? s.vx[i] : 0.;
-	d[1] = (flags & A_ADVECTION) ? s.vy[i] : 0.;
-	d[2] = av_x;
-	d[3] = av_y;
-	if (flags & A_MOMENTUM_TL) {
-		d[2] += (double)(1.f / rho0 * (Pxx_x + Pyx_y)) + a.fcx[i] / a.m[i];
-		d[3] += (double)(1.f / rho0 * (Pxy_x + Pyy_y)) + a.fcy[i] / a.m[i];
+	tlB_finish(a, i, pr, rho0, Pxx_x, Pyx_y, Pxy_x, Pyy_y, av_x, av_y);
+}
+
+// ---- mixed form over halo tiles.  The same per-row arithmetic, in the same order, as
+// k_tlA32 / k_tlB32 (so the results are bit-identical); the neighbours' records come
+// from shared memory, where the block first copies its tile's halo (a compact 2-D
+// patch of 128 rows names ~250 distinct rows, against ~2,700 list entries) with
+// 16-byte cp.async copies, all in flight at once, instead of one scattered global
+// load per list entry.  The lists (halo slot + weights) stream from global memory.
+__device__ __forceinline__ void cp16(void* smem, const void* gmem) {
+	uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_wait_all() {
+	asm volatile("cp.async.commit_group;\n" ::: "memory");
+	asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(TL_TILE) k_tlA32t(TLArgs a) {
+	extern __shared__ float4 smA[];  // [halo_max] u, then [halo_max] v
+	const uint32_t t = blockIdx.x, HM = a.halo_max;
+	const uint32_t h0 = a.t_halo_off[t], hn = a.t_halo_off[t + 1] - h0;
+	const float4* recA = (const float4*)a.recA;
+	const float4* rec4 = (const float4*)a.recB;
+	for (uint32_t e = threadIdx.x; e < 2 * hn; e += TL_TILE) {
+		uint32_t s_ = e >> 1, j = a.t_halo[h0 + s_];
+		cp16(smA + (e & 1u) * HM + s_, (e & 1u) ? rec4 + 4 * (size_t)j + 2 : recA + j);  // u, or RecB::v
 	}
-	float e[4] = {dAi.x, dAi.y, dAi.z, dAi.w};
-	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
-	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
-	double* np[4] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy};
-	float* bq[4] = {a.base.rho_f, a.base.Sxx_f, a.base.Sxy_f, a.base.Syy_f};
-	float* aq[4] = {a.acc.rho_f, a.acc.Sxx_f, a.acc.Sxy_f, a.acc.Syy_f};
-	float* nq[4] = {a.nxt.rho_f, a.nxt.Sxx_f, a.nxt.Sxy_f, a.nxt.Syy_f};
-	uint32_t stg = a.stage;
-	double dt = pr.dt;
-	if (stg < 3) {
-		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
-#pragma unroll
-		for (int q2 = 0; q2 < 4; q2++) {
-			ap[q2][i] = (stg == 0) ? d[q2] : ap[q2][i] + 2 * d[q2];
-			np[q2][i] = bp[q2][i] + d[q2] * dts;
-			aq[q2][i] = (stg == 0) ? e[q2] : aq[q2][i] + 2.f * e[q2];
-			nq[q2][i] = bq[q2][i] + e[q2] * (float)dts;
+	const uint32_t p = t * TL_TILE + threadIdx.x;
+	const bool live = p < a.n_total;
+	const uint32_t i = live ? a.t_rows[p] : 0u;
+	const float4 ui = recA[i];
+	const float4 vi = rec4[4 * (size_t)i + 2];
+	const uint32_t c = live ? a.t_cnt[p] : 0u;
+	cp_wait_all();
+	__syncthreads();
+	if (!live) return;
+	const mfk_host::StateSoA& s = a.st;
+	const float2* swA = (const float2*)a.t_swA;
+	const uint32_t flags = a.flags;
+	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
+	float Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
+	uint32_t q = a.t_sl[p >> 5] + (p & 31u);
+#pragma unroll 4
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t l = __ldg(a.t_loc + q);
+		float2 w = __ldg(swA + q);
+		if (flags & A_DISP) {
+			float4 uj = smA[l];
+			float dux = ffd(uj.x, uj.y, ui.x, ui.y), duy = ffd(uj.z, uj.w, ui.z, ui.w);
+			Hxx += dux * w.x;
+			Hxy += dux * w.y;
+			Hyx += duy * w.x;
+			Hyy += duy * w.y;
 		}
-	} else {
-		double w6 = dt * 1. / 6.;
-#pragma unroll
-		for (int q2 = 0; q2 < 4; q2++) {
-			double v = bp[q2][i] + w6 * (ap[q2][i] + d[q2]);
-			bp[q2][i] = v;
-			np[q2][i] = v;
-			float f = bq[q2][i] + (float)w6 * (aq[q2][i] + e[q2]);
-			bq[q2][i] = f;
-			nq[q2][i] = f;
+		if (flags & A_VEL_TL) {
+			float4 vj = smA[HM + l];
+			float dvx = ffd(vj.x, vj.y, vi.x, vi.y), dvy = ffd(vj.z, vj.w, vi.z, vi.w);
+			Fxx += dvx * w.x;
+			Fxy += dvx * w.y;
+			Fyx += dvy * w.x;
+			Fyy += dvy * w.y;
 		}
-		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
-			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
+	double rho = (double)s.rho_f[i] + pr.rho0;
+	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
+	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
+	((RecB*)a.recB)[i].P = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
+	((float4*)a.dA32)[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
+}
+
+__global__ void __launch_bounds__(TL_TILE, 8) k_tlB32t(TLArgs a) {
+	extern __shared__ float4 smB[];  // RecB fields as four arrays of halo_max: P, x, v, hmrc
+	const uint32_t t = blockIdx.x, HM = a.halo_max;
+	const uint32_t h0 = a.t_halo_off[t], hn = a.t_halo_off[t + 1] - h0;
+	const float4* rec4 = (const float4*)a.recB;
+	for (uint32_t e = threadIdx.x; e < 4 * hn; e += TL_TILE) {
+		uint32_t s_ = e >> 2, f = e & 3u;  // four threads copy one 64-byte record
+		cp16(smB + f * HM + s_, rec4 + 4 * (size_t)a.t_halo[h0 + s_] + f);
+	}
+	// this row's own data, requested while the copies are in flight
+	const uint32_t p = t * TL_TILE + threadIdx.x;
+	const bool live = p < a.n_total;
+	const uint32_t i = live ? a.t_rows[p] : 0u;
+	const RecB ri = ((const RecB*)a.recB)[i];
+	const uint32_t c = live ? a.t_cnt[p] : 0u;
+	const uint32_t bi = a.body_of[i];
+	cp_wait_all();
+	__syncthreads();
+	if (!live) return;
+	const mfk_host::StateSoA& s = a.st;
+	const float2* sw = (const float2*)a.t_sw;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[bi];
+	float rho0 = (float)pr.rho0;
+	float r21 = 1.f / (rho0 * rho0);
+	float sc = r21 * rho0;
+	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
+	uint32_t q = a.t_sl[p >> 5] + (p & 31u);
+#pragma unroll 4
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t l = __ldg(a.t_loc + q);
+		float2 w = __ldg(sw + q);  // the neighbour's mass times its corrected gradient
+		if (flags & A_STRESS_TL) {
+			float4 Pj = smB[l];
+			float fx = sc * w.x, fy = sc * w.y;
+			Pxx_x += (ri.P.x + Pj.x) * fx;
+			Pyx_y += (ri.P.z + Pj.z) * fy;
+			Pxy_x += (ri.P.y + Pj.y) * fx;
+			Pyy_y += (ri.P.w + Pj.w) * fy;
+		}
+		if (flags & A_ART_VISC) {
+			float4 xj = smB[HM + l], vj = smB[2 * HM + l];
+			float xij = ffd(ri.x.x, ri.x.y, xj.x, xj.y), yij = ffd(ri.x.z, ri.x.w, xj.z, xj.w);
+			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
+			float vijposij = vijx * xij + vijy * yij;
+			if (vijposij < 0.f) {
+				float4 hmrc = smB[3 * HM + l];
+				float piij = art_visc_pi(ri.hmrc, hmrc, xij, yij, vijposij, alpha, beta, eta2);
+				av_x += -piij * w.x;
+				av_y += -piij * w.y;
+			}
+		}
+	}
+	tlB_finish(a, i, pr, rho0, Pxx_x, Pyx_y, Pxy_x, Pyy_y, av_x, av_y);
+}
+
+// Sliced ELL over tile positions: the weights of row t_rows[p] copied from the row-order
+// sliced ELL (the halo slots, t_loc, come from the host).
+__global__ void k_tile_sell(uint32_t n, const uint32_t* __restrict__ t_rows, const uint32_t* __restrict__ sl_off,
+                            const uint16_t* __restrict__ cnt, const float2* __restrict__ sw, const float2* __restrict__ swA,
+                            const uint32_t* __restrict__ t_sl, uint16_t* t_cnt, float2* t_sw, float2* t_swA) {
+	uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= n) return;
+	uint32_t i = t_rows[p];
+	uint32_t c = cnt[i];
+	t_cnt[p] = (uint16_t)c;
+	uint32_t qo = sl_off[i >> 5] + (i & 31u), qn = t_sl[p >> 5] + (p & 31u);
+	for (uint32_t k = 0; k < c; k++, qo += 32, qn += 32) {
+		t_sw[qn] = sw[qo];
+		t_swA[qn] = swA[qo];
 	}
 }
 
-// CSR (set-up order) -> sliced ELL; the mixed form also gets FP32 gradients and the
-// pass-A gradients pre-multiplied by the neighbour's quad weight (in FP64, then rounded).
+// CSR (set-up order) -> sliced ELL; the mixed form gets FP32 gradients pre-multiplied
+// by the neighbour's mass (pass B) and by its quad weight (pass A), in FP64 then rounded.
 __global__ void k_to_sell(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
                           const double* __restrict__ wx, const double* __restrict__ wy, const uint32_t* __restrict__ sl_off,
                           uint16_t* cnt, uint32_t* snbr, double2* sw64, float2* sw32, float2* swA32,
-                          const double* __restrict__ qw) {
+                          const double* __restrict__ qw, const double* __restrict__ mass) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	uint32_t base = sl_off[i >> 5] + (i & 31u);
@@ -502,7 +695,7 @@ __global__ void k_to_sell(uint32_t n, const uint32_t* __restrict__ off, const ui
 		snbr[q] = j;
 		double gx = wx[q0 + k], gy = wy[q0 + k];
 		if (sw64) sw64[q] = make_double2(gx, gy);
-		if (sw32) sw32[q] = make_float2((float)gx, (float)gy);
+		if (sw32) sw32[q] = make_float2((float)(gx * mass[j]), (float)(gy * mass[j]));
 		if (swA32) swA32[q] = make_float2((float)(gx * qw[j]), (float)(gy * qw[j]));
 	}
 }
@@ -549,10 +742,31 @@ cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s) {
 
 cudaError_t tl_to_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy,
                        const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* sw64, void* sw32, void* swA32,
-                       const double* qw, cudaStream_t s) {
+                       const double* qw, const double* mass, cudaStream_t s) {
 	k_to_sell<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, wx, wy, sl_off, cnt, snbr, (double2*)sw64, (float2*)sw32,
-	                                        (float2*)swA32, qw);
+	                                        (float2*)swA32, qw, mass);
 	return cudaGetLastError();
+}
+
+cudaError_t tl_tile_sell(uint32_t n, const uint32_t* t_rows, const uint32_t* sl_off, const uint16_t* cnt, const void* sw,
+                         const void* swA, const uint32_t* t_sl, uint16_t* t_cnt, void* t_sw, void* t_swA, cudaStream_t s) {
+	k_tile_sell<<<grid1(n, 256), 256, 0, s>>>(n, t_rows, sl_off, cnt, (const float2*)sw, (const float2*)swA, t_sl, t_cnt,
+	                                          (float2*)t_sw, (float2*)t_swA);
+	return cudaGetLastError();
+}
+
+// dynamic shared memory of the tiled passes: the halo records, 32 B (pass A) / 64 B
+// (pass B) per halo row
+size_t tl_tile_smem(int pass, uint32_t halo_max, uint32_t /*ent_max*/) {
+	return (pass == 0 ? 2 : 4) * (size_t)halo_max * sizeof(float4);
+}
+
+cudaError_t tl_tile_attrs(uint32_t halo_max, uint32_t ent_max) {
+	cudaError_t e = cudaFuncSetAttribute(k_tlA32t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int)tl_tile_smem(0, halo_max, ent_max));
+	if (e != cudaSuccess) return e;
+	return cudaFuncSetAttribute(k_tlB32t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                            (int)tl_tile_smem(1, halo_max, ent_max));
 }
 
 cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
@@ -567,13 +781,15 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 		break;
 	case 2: {
 		unsigned bs = a.block ? a.block : 128;
-		if (mixed) k_tlA32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		if (mixed && a.t_rows) k_tlA32t<<<a.n_tiles, TL_TILE, tl_tile_smem(0, a.halo_max, a.t_ent_max), s>>>(a);
+		else if (mixed) k_tlA32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlA64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
 	}
 	case 3: {
 		unsigned bs = a.block ? a.block : 128;
-		if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		if (mixed && a.t_rows) k_tlB32t<<<a.n_tiles, TL_TILE, tl_tile_smem(1, a.halo_max, a.t_ent_max), s>>>(a);
+		else if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlB64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
 	}

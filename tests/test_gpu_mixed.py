@@ -62,3 +62,49 @@ def test_mixed_error(case, steps, lib):
     print(case, {k: f"{v:.2e}" for k, v in e.items()})
     assert e["velocity"] <= 1e-4, e
     assert e["displacement"] <= 1e-4, e
+
+
+@pytest.mark.parametrize("case", ["rings_contact_dx0.4mm", "tensile_tl_pull"])
+def test_halo_tiles_match_untiled(case, lib):
+    """The mixed TL passes over shared-memory halo tiles do per row exactly what the
+    untiled passes do, in the same order: bit-identical states."""
+    import mfree_iwf_gb300 as M
+    sc = S.c2_rings_tl(dx=4e-4) if case == "rings_contact_dx0.4mm" else S.tensile_tl(11)
+    out = {}
+    for tiles in (1, 0):
+        sim = M.from_scenario(sc, precision="mixed")
+        sim.set_option("tl_tiles", tiles)
+        sim.step(40)
+        assert sim.get_option("tl_tiles_built") == tiles
+        if tiles:
+            assert 0 < sim.get_option("tl_halo_max") <= 2048
+        out[tiles] = [sim.get_state(b) for b in range(len(sc.bodies))]
+        sim.close()
+    for a, b in zip(out[1], out[0]):
+        for f in ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy"):
+            np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_mixed_tl_resume_through_set_state(graph, lib):
+    """Mixed TL keeps its packed neighbour records current from pass B; writing the
+    state back through set_state (or replaying a captured step graph) re-packs them, so
+    a run interrupted by get_state/set_state equals the uninterrupted run bit for bit."""
+    import mfree_iwf_gb300 as M
+    sc = S.c2_rings_tl(dx=4e-4)
+    fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy")
+    sim = M.from_scenario(sc, precision="mixed", graph=graph)
+    sim.step(10)
+    want = [sim.get_state(b, fields) for b in range(2)]
+    sim.close()
+    sim = M.from_scenario(sc, precision="mixed", graph=graph)
+    sim.step(5)
+    mid = [sim.get_state(b, fields) for b in range(2)]
+    for b in range(2):
+        sim.set_state(b, mid[b])
+    sim.step(5)
+    got = [sim.get_state(b, fields) for b in range(2)]
+    sim.close()
+    for g, w in zip(got, want):
+        for f in fields:
+            np.testing.assert_array_equal(g[f], w[f], err_msg=f)
