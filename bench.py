@@ -184,11 +184,29 @@ def reference_arm(args, cfg_desc):
 #   pass B: offset 4, per pair 12, packed x, v 32, h 4, m 4, rho 4, c 4, P 16, rate 16,
 #           fc 16, m 8, the FP64 x/y/vx/vy base+acc+next (3 x 32 read/write -> 80)
 #           and float rho/S base+acc+next (3 x 16 -> 40)
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture:
+# (bytes, rows of the captured launch, where); scaled to the bench's rows per launch.
+MEASURED_TRAFFIC = {
+    ("c2", "mixed", "TL pass B"): (1203.7e6, 1759324, "profiles/tl_mixed_ring_impact_dx0.05mm.md: ncu "
+                                   "dram__bytes_read.sum + dram__bytes_write.sum, mean of 104 launches"),
+}
+
+
 def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool) -> float:
+    """Unique bytes per row of one launch: each row's own data once, the lists once, and
+    neighbour records assumed served on chip (their unique bytes are the rows' own)."""
     if tl and mixed:
-        if kind == 1:
-            return 4 + 12 * nnz_per_row + 16 + 16 + 4 + 16 + 16 + 4
-        return 4 + 12 * nnz_per_row + 32 + 16 + 16 + 16 + 16 + 8 + 80 + 40
+        if kind == 1:  # pass A
+            return (2 + 12 * nnz_per_row  # count; per pair: index 4 + premultiplied gradient 8
+                    + 16 + 16             # own displacement and velocity records
+                    + 16 + 4              # rho - rho0, S (FP32), body id
+                    + 16 + 16)            # writes: nominal stress P, rate terms
+        if kind == 2:  # pass B (also writes the next stage's records)
+            return (2 + 12 * nnz_per_row  # count; per pair: index 4 + mass-premultiplied gradient 8
+                    + 64 + 16 + 16 + 24   # own record, rate terms, stage vx vy, fc and m
+                    + 32 + 24 + 32 + 32 + 8   # RK4 FP64 x y vx vy: base, acc (stages 1-3), acc, next, base (stage 3)
+                    + 16 + 12 + 16 + 16 + 4   # RK4 FP32 rho S: same pattern
+                    + 24 + 64)            # next-stage records: reads X Y h m, writes displacement, x v hmrc
     if tl:
         if kind == 1:
             return 4 + 20 * nnz_per_row + 32 + 32 + 32 + 32 + 8
@@ -216,6 +234,8 @@ def ours(args, cfg_desc):
     tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"
+    if args.tl_tiles:
+        sim.set_option("tl_tiles", 1)
     sim.step(1)  # set-up (neighbour search, corrections)
     tune = sim.autotune(args.tune_steps) if not args.no_tune else "off"
     sim.step(args.warmup)
@@ -317,6 +337,10 @@ def ours(args, cfg_desc):
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,
                 "launches": klaunch, "avg_launch_ms": kms / klaunch,
                 "algorithmic_bytes_per_launch": abytes}
+        t = MEASURED_TRAFFIC.get((args.workload, args.precision, names[dom]))
+        if t is not None:
+            roof["traffic"] = t[0] * per_launch_rows / t[1]
+            roof["traffic_source"] = t[2]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -360,6 +384,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tune-steps", type=int, default=3)
     ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--tl-tiles", action="store_true", help="mixed TL: the shared-memory halo-tile passes")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
