@@ -47,11 +47,11 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def workload(name: str, dx: float | None):
+def workload(name: str, dx: float | None, instances: int = 512):
     from mfree_iwf_gb300 import scenarios as S
     if name == "c4":
-        sc = S.c4_ensemble(512)
-        return sc, {"workload": "ensemble of 512 ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
+        sc = S.c4_ensemble(instances)
+        return sc, {"workload": f"ensemble of {instances} ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
                                 "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
     if name == "c3":
         dx = dx or 2e-5
@@ -229,7 +229,7 @@ def ours(args, cfg_desc):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    sc, cfg = workload(args.workload, args.dx)
+    sc, cfg = workload(args.workload, args.dx, args.instances)
     n = sc.n_total
     tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
@@ -385,6 +385,7 @@ def main():
     ap.add_argument("--tune-steps", type=int, default=3)
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--tl-tiles", action="store_true", help="mixed TL: the shared-memory halo-tile passes")
+    ap.add_argument("--instances", type=int, default=512, help="c4: ring impacts in the ensemble")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

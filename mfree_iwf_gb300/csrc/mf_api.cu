@@ -167,6 +167,7 @@ struct mf_ctx {
 	DevBuf<uint32_t> total_cells, keys, keys_sorted, perm_in, perm, cell_start, rec_body;
 	DevBuf<unsigned char> rec, sort_tmp;
 	int sort_bits = 1;
+	uint32_t cell_cap = 0;
 
 	// TL: fixed neighbour lists (CSR from the set-up, kept for mf_get_neighbors, and the
 	// sliced-ELL copy the stage kernels read) with corrected gradients, per-stage scratch
@@ -321,6 +322,7 @@ ULArgs ul_args(mf_ctx* c, uint32_t stage) {
 	a.sort_tmp = c->sort_tmp.p;
 	a.sort_tmp_bytes = c->sort_tmp.n;
 	a.sort_bits = c->sort_bits;
+	a.cell_cap = c->cell_cap;
 	a.status = c->d_status;
 	a.block = c->tune.ul_block;
 	a.persistent = c->tune.ul_persistent;
@@ -479,11 +481,13 @@ mf_status finalize(mf_ctx* c) {
 		CK(c->bbox.alloc(6 * (size_t)nb));
 		CK(c->total_cells.alloc(1));
 		CK(c->keys.alloc(n)); CK(c->keys_sorted.alloc(n)); CK(c->perm_in.alloc(n)); CK(c->perm.alloc(n));
-		CK(c->cell_start.alloc((size_t)n + 2));
+		// the mixed grid may use half-size cells: up to twice as many cells as particles
+		c->cell_cap = c->mixed ? 3 * n + 7 : n + 1;
+		CK(c->cell_start.alloc((size_t)c->cell_cap + 1));
 		CK(c->rec_body.alloc(n));
 		CK(c->rec.alloc((size_t)n * 128));
 		int bits = 1;
-		while (bits < 32 && (1ull << bits) < (uint64_t)n + 2) bits++;
+		while (bits < 32 && (1ull << bits) < (uint64_t)c->cell_cap + 1) bits++;
 		c->sort_bits = bits;
 		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
 		CK(c->sort_tmp.alloc(tmp));

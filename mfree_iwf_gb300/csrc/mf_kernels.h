@@ -27,8 +27,10 @@ struct BodyParams {
 // Per-body cell geometry of one derivative evaluation (grid.h:83-115).
 struct Geom {
 	double bbmin_x, bbmin_y, dx;
-	double slack;  // mixed form: how far a particle may move within the step (dx - 2 h_max)/2
+	double slack;  // mixed form: how far a particle may move within the step
 	uint32_t nx, ny, num_cell, cell_off;
+	uint32_t span;  // stencil half-width in cells: 1 (cells of 2 h_max [+ 2 slack]) or 2 (mixed: half-size cells)
+	uint32_t pad;
 };
 
 struct DevStatusH {
@@ -58,7 +60,8 @@ struct ULArgs {
 	const double *m, *h, *qw0, *fcx, *fcy;  // constants (home order)
 	StateSoA base, acc, st;               // RK4 arrays (home order)
 	uint32_t *keys, *keys_sorted, *perm_in, *perm;  // sort buffers
-	uint32_t* cell_start;                 // capacity n_total + 2
+	uint32_t* cell_start;                 // capacity cell_cap + 1
+	uint32_t cell_cap;                    // most cells over all bodies (0: n_total + 1)
 	void* rec;                            // cell-ordered gathered records
 	uint32_t* rec_body;                   // body of each cell-ordered row
 	void* sort_tmp;
