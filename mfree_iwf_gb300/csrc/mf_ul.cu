@@ -83,6 +83,16 @@ __device__ __forceinline__ Rec32 load_rec(const Rec32* p) {
 	for (int i = 0; i < 5; i++) d[i] = __ldg(s + i);
 	return r;
 }
+// the rest of a record whose first 16 bytes (x, y) are already loaded
+__device__ __forceinline__ Rec32 load_rec_tail(const Rec32* p, float4 head) {
+	Rec32 r;
+	const float4* s = reinterpret_cast<const float4*>(p);
+	float4* d = reinterpret_cast<float4*>(&r);
+	d[0] = head;
+#pragma unroll
+	for (int i = 1; i < 5; i++) d[i] = __ldg(s + i);
+	return r;
+}
 
 // --------------------------------------------------------------- grid build
 __global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
@@ -581,11 +591,13 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
 		for (uint32_t kj = j0; kj < j1; kj++) {
-			const Rec32 rj = load_rec(rec + kj);
-			float xij = ff_diff(ri.x, rj.x);
-			float yij = ff_diff(ri.y, rj.y);
+			// positions first: most candidates of the stencil lie beyond the reach
+			const float4 head = __ldg(reinterpret_cast<const float4*>(rec + kj));
+			float xij = (ri.x.hi - head.x) + (ri.x.lo - head.y);
+			float yij = (ri.y.hi - head.z) + (ri.y.lo - head.w);
 			float r2 = xij * xij + yij * yij;
 			if (r2 > reach2) continue;
+			const Rec32 rj = load_rec_tail(rec + kj, head);
 			KR32 w = cubic_spline_f(xij, yij, h1, fac);
 			if (flags & A_STRESS_MGHN) {
 				float Rxx = 0.f, Rxy = 0.f, Ryy = 0.f;
