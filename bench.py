@@ -47,23 +47,43 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def workload_desc(name: str, dx: float | None, instances: int = 512) -> dict:
+    if name == "c4":
+        return {"workload": f"ensemble of {instances} ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
+                            "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
+    if name == "c3":
+        return {"workload": f"plate tension 0.1 x 0.02 m, weak-form TL + RKPM, dx={(dx or 2e-5)*1e3:g} mm, "
+                            "+-1 m/s pull, 1% seeded jitter"}
+    if name == "c2":
+        return {"workload": f"ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx={(dx or 5e-5)*1e3:g} mm"}
+    if name == "c1":
+        return {"workload": f"ring impact, Gray-Monaghan SPH, dx={(dx or 1e-3)*1e3:g} mm"}
+    raise SystemExit(f"unknown workload {name}")
+
+
 def workload(name: str, dx: float | None, instances: int = 512):
     from mfree_iwf_gb300 import scenarios as S
+    desc = workload_desc(name, dx, instances)
     if name == "c4":
-        sc = S.c4_ensemble(instances)
-        return sc, {"workload": f"ensemble of {instances} ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
-                                "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
+        return S.c4_ensemble(instances), desc
     if name == "c3":
-        dx = dx or 2e-5
-        return S.c3_plate(dx=dx), {"workload": f"plate tension 0.1 x 0.02 m, weak-form TL + RKPM, dx={dx*1e3:g} mm, "
-                                               "+-1 m/s pull, 1% seeded jitter"}
+        return S.c3_plate(dx=dx or 2e-5), desc
     if name == "c2":
-        dx = dx or 5e-5
-        return S.c2_rings_tl(dx=dx), {"workload": f"ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx={dx*1e3:g} mm"}
-    if name == "c1":
-        dx = dx or 1e-3
-        return S.c1_rings(dx=dx), {"workload": f"ring impact, Gray-Monaghan SPH, dx={dx*1e3:g} mm"}
-    raise SystemExit(f"unknown workload {name}")
+        return S.c2_rings_tl(dx=dx or 5e-5), desc
+    return S.c1_rings(dx=dx or 1e-3), desc
+
+
+def job_throughput(dist, seconds: float, units: float, device: str = "cuda"):
+    """Whole-job throughput of replicas: the units all ranks processed over the slowest
+    rank's time.  Returns (max seconds over ranks, units per second)."""
+    if dist is None:
+        return seconds, units / seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item()) / float(t.item())
 
 
 # ---------------------------------------------------------------- clocks
@@ -177,13 +197,6 @@ def reference_arm(args, cfg_desc):
 
 
 # ------------------------------------------------------------------ ours
-# Algorithmic bytes per row and launch of the timed kernels (unique data each must
-# move once; neighbour rows are assumed served on chip).  Mixed TL form:
-#   pass A: list offset 4, per pair index 4 + gradient 8, own packed u 16, rho/S 16,
-#           quad weight 4; writes P 16, rate terms 16, c 4
-#   pass B: offset 4, per pair 12, packed x, v 32, h 4, m 4, rho 4, c 4, P 16, rate 16,
-#           fc 16, m 8, the FP64 x/y/vx/vy base+acc+next (3 x 32 read/write -> 80)
-#           and float rho/S base+acc+next (3 x 16 -> 40)
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture:
 # (bytes, rows of the captured launch, where); scaled to the bench's rows per launch.
 MEASURED_TRAFFIC = {
@@ -258,14 +271,10 @@ def ours(args, cfg_desc):
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = e0.elapsed_time(e1)
     launches = sim.launch_count() - l0
     clocks = clk.summary()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n * args.steps / (ms / 1e3)
+    secs, value = job_throughput(dist, e0.elapsed_time(e1) / 1e3, n * args.steps)
+    ms = secs * 1e3
 
     # ---- per-kernel CUDA-event times (eager launches: a graph replay carries no
     # per-launch events), same workload, right after the timed region
@@ -293,7 +302,7 @@ def ours(args, cfg_desc):
         for b in range(len(sc.bodies)):
             sim.get_state_into(b, host[b])
     wall = time.perf_counter() - t0
-    e2e_value = world * n * k2 / wall
+    _, e2e_value = job_throughput(dist, wall, n * k2)
     bytes_io = 8 * len(fields) * n
 
     sim.close()
@@ -389,11 +398,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    _, cfg = workload(args.workload, args.dx) if args.impl == "ours" and False else (None, None)
-    cfg_desc = {"workload": {"c2": "ring impact, total-Lagrangian SPH + Randles-Libersky, contact, dx=0.05 mm",
-                             "c1": "ring impact, Gray-Monaghan SPH, dx=1 mm",
-                             "c3": "plate tension, weak-form TL + RKPM, dx=0.02 mm",
-                             "c4": "ensemble of 512 ring impacts, Gray-Monaghan SPH"}[args.workload]}
+    cfg_desc = workload_desc(args.workload, args.dx, args.instances)
     if args.impl == "reference":
         reference_arm(args, cfg_desc)
         return
