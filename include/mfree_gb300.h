@@ -190,7 +190,7 @@ MF_API mf_status mf_launch_count(mf_ctx* ctx, uint64_t* launches);
 /* Autotuner: times the candidate launch shapes of the hot kernels (rows per block,
  * plain or persistent pair kernel, rows per work chunk) for trial_steps steps each on
  * a snapshot of the state, restores the state, and keeps the fastest.  Results are
- * cached per process by (method, precision, particle-count bucket).  report (may be
+ * cached per process by (method, precision, particle-count bucket, h bucket).  report (may be
  * NULL) receives a one-line summary. */
 MF_API mf_status mf_autotune(mf_ctx* ctx, int32_t trial_steps, char* report, uint32_t report_len);
 /* Per-step monitor: after every step each body's [mean vx, mean vy, max von Mises

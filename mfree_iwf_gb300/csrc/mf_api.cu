@@ -1839,10 +1839,21 @@ void snapshot_free(Snapshot& s) {
 }
 
 std::string tune_key(mf_ctx* c) {
+	// (method, precision, particle-count bucket, smoothing-length bucket): the launch
+	// shapes that win depend on the rows per launch and on the neighbours per row,
+	// which the lattice spacing (through h) and the body sizes set
 	int bucket = 0;
 	while ((1u << bucket) < c->n_total) bucket++;
-	char k[96];
-	snprintf(k, sizeof k, "m%d p%d n2^%d", c->cfg.method, c->cfg.precision, bucket);
+	double hsum = 0.;
+	uint64_t hn = 0;
+	for (auto& b : c->bodies)
+		for (double h : b.in[6]) {
+			hsum += h;
+			hn++;
+		}
+	int hb = hn ? (int)std::floor(std::log2(std::max(hsum / (double)hn, 1e-12))) : 0;
+	char k[128];
+	snprintf(k, sizeof k, "m%d p%d n2^%d h2^%d", c->cfg.method, c->cfg.precision, bucket, hb);
 	return k;
 }
 
