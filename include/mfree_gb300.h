@@ -209,6 +209,30 @@ MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
  *   "tl_halo_max"     the largest tile halo, in rows */
 MF_API mf_status mf_set_option(mf_ctx* ctx, const char* key, int64_t value);
 MF_API mf_status mf_get_option(mf_ctx* ctx, const char* key, int64_t* value);
+/* ---------------------------------------------------------------------------
+ * State output.  VTK files in the reference's legacy ASCII layout (vtk_writer_write,
+ * vtk_writer.h:27-127: points, vertex cells, h, density, Sxx, Sxy, Syy, velocity;
+ * "%f" text), and binary checkpoints that restore a context's state exactly (UL and TL
+ * bodies: positions, velocities, density, stress, contact forces and clocks, in the
+ * context's own precision).  mf_dump_async snapshots the state on the device behind
+ * the steps already issued and writes the file from a host thread, so stepping can go
+ * on; one dump is in flight at a time, mf_dump_wait returns its status.
+ * ------------------------------------------------------------------------- */
+enum { MF_DUMP_VTK = 0, MF_DUMP_CHECKPOINT = 1 };
+
+typedef struct mf_vtk_body {
+	uint32_t n;
+	uint32_t reserved;
+	const double *x, *y, *h, *rho, *Sxx, *Sxy, *Syy, *vx, *vy;
+} mf_vtk_body;
+
+/* Host-only writer: the bodies' particles in order into one file. */
+MF_API mf_status mf_vtk_write(const char* path, const mf_vtk_body* bodies, uint32_t n_bodies);
+MF_API mf_status mf_dump_async(mf_ctx* ctx, const char* path, int32_t kind);
+MF_API mf_status mf_dump_wait(mf_ctx* ctx);
+MF_API mf_status mf_write_vtk(mf_ctx* ctx, const char* path);         /* dump + wait */
+MF_API mf_status mf_checkpoint_save(mf_ctx* ctx, const char* path);   /* dump + wait */
+MF_API mf_status mf_checkpoint_load(mf_ctx* ctx, const char* path);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work on it. */
 MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
 

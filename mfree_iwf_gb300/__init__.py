@@ -63,6 +63,14 @@ class MfState(ctypes.Structure):
     _fields_ = [(f, _DP) for f in _SFIELDS]
 
 
+class MfVtkBody(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("reserved", ctypes.c_uint32)] + [
+        (f, _DP) for f in ("x", "y", "h", "rho", "Sxx", "Sxy", "Syy", "vx", "vy")]
+
+
+DUMP_VTK, DUMP_CHECKPOINT = 0, 1
+
+
 class MfError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
@@ -108,6 +116,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, C.c_uint32]),
         "mf_set_monitor": (C.c_int32, [C.c_void_p, C.c_uint32]),
         "mf_set_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_int64]),
+        "mf_vtk_write": (C.c_int32, [C.c_char_p, C.POINTER(MfVtkBody), C.c_uint32]),
+        "mf_dump_async": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_int32]),
+        "mf_dump_wait": (C.c_int32, [C.c_void_p]),
+        "mf_write_vtk": (C.c_int32, [C.c_void_p, C.c_char_p]),
+        "mf_checkpoint_save": (C.c_int32, [C.c_void_p, C.c_char_p]),
+        "mf_checkpoint_load": (C.c_int32, [C.c_void_p, C.c_char_p]),
         "mf_get_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),
         "mf_get_monitor": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), _UP]),
     }
@@ -121,6 +135,20 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 
 def _dptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(_DP)
+
+
+def write_vtk_arrays(path: str, bodies: Sequence[Dict[str, np.ndarray]]) -> None:
+    """The reference's VTK layout (vtk_writer.h:27-127) from host arrays, one dict per
+    body with x, y, h, rho, Sxx, Sxy, Syy, vx, vy (runs on the host only)."""
+    lib = load_library()
+    keep, arr = [], (MfVtkBody * max(1, len(bodies)))()
+    for k, b in enumerate(bodies):
+        cols = {f: np.ascontiguousarray(b[f], np.float64) for f in ("x", "y", "h", "rho", "Sxx", "Sxy", "Syy", "vx", "vy")}
+        keep.append(cols)
+        arr[k] = MfVtkBody(len(cols["x"]), 0, *[_dptr(cols[f]) for f in ("x", "y", "h", "rho", "Sxx", "Sxy", "Syy", "vx", "vy")])
+    st = lib.mf_vtk_write(path.encode(), arr, len(bodies))
+    if st != 0:
+        raise MfError(st, f"mf_vtk_write {path}")
 
 
 def convex_hull(x: np.ndarray, y: np.ndarray) -> np.ndarray:
@@ -305,6 +333,22 @@ class Simulation:
         v = ctypes.c_int64()
         self._check(self._lib.mf_get_option(self._h, key.encode(), ctypes.byref(v)), "mf_get_option")
         return v.value
+
+    # -- state output (vtk_writer.h) and checkpoints
+    def write_vtk(self, path: str) -> None:
+        self._check(self._lib.mf_write_vtk(self._h, path.encode()), "mf_write_vtk")
+
+    def dump_async(self, path: str, kind: int = DUMP_VTK) -> None:
+        self._check(self._lib.mf_dump_async(self._h, path.encode(), int(kind)), "mf_dump_async")
+
+    def dump_wait(self) -> None:
+        self._check(self._lib.mf_dump_wait(self._h), "mf_dump_wait")
+
+    def checkpoint_save(self, path: str) -> None:
+        self._check(self._lib.mf_checkpoint_save(self._h, path.encode()), "mf_checkpoint_save")
+
+    def checkpoint_load(self, path: str) -> None:
+        self._check(self._lib.mf_checkpoint_load(self._h, path.encode()), "mf_checkpoint_load")
 
     def set_monitor(self, capacity: int) -> None:
         self._check(self._lib.mf_set_monitor(self._h, int(capacity)), "mf_set_monitor")

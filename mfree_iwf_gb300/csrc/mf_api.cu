@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -201,6 +202,17 @@ struct mf_ctx {
 
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
+
+	// state dumps (VTK, checkpoints): device snapshot, then copy-out and file write on a
+	// host thread with its own stream while the simulation goes on
+	DevBuf<unsigned char> io_dev;
+	unsigned char* io_host = nullptr;
+	size_t io_host_bytes = 0;
+	cudaStream_t io_stream = nullptr;
+	cudaEvent_t io_ready = nullptr;
+	std::thread io_thread;
+	mf_status io_status = MF_OK;
+	std::string io_err;
 
 	// per-step monitor (mf_set_monitor)
 	uint32_t mon_cap = 0;
@@ -1349,6 +1361,11 @@ mf_status contact_run(mf_ctx* c) {
 }  // namespace
 
 mf_ctx::~mf_ctx() {
+	if (io_thread.joinable()) io_thread.join();
+	if (io_stream) cudaStreamDestroy(io_stream);
+	if (io_ready) cudaEventDestroy(io_ready);
+	if (io_host) cudaFreeHost(io_host);
+	io_dev.free();
 	if (stream) cudaStreamSynchronize(stream);
 	if (graph_exec) cudaGraphExecDestroy(graph_exec);
 	if (graph) cudaGraphDestroy(graph);
@@ -2014,6 +2031,288 @@ MF_API mf_status mf_get_monitor(mf_ctx* c, float* out, uint32_t* rows) {
 MF_API mf_status mf_get_stream(mf_ctx* c, void** stream) {
 	if (!c || !stream) return MF_ERR_ARG;
 	*stream = (void*)c->stream;
+	return MF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ state I/O
+// VTK files in the reference's legacy ASCII layout (vtk_writer.h:27-127) and exact
+// binary checkpoints.  A dump first copies the state device-to-device into a snapshot
+// (stream-ordered after the steps already issued, ~64 B per particle), then a host
+// thread copies the snapshot out on its own stream and writes the file, so the caller
+// can keep stepping.
+namespace {
+
+const char CKPT_MAGIC[8] = {'M', 'F', 'C', 'K', 'P', 'T', '1', 0};
+
+// bytes per row of the snapshot: x y vx vy fcx fcy FP64; rho S FP64 or (mixed) FP32
+size_t io_row_bytes(const mf_ctx* c) { return 6 * 8 + 4 * (c->mixed ? 4 : 8); }
+
+mf_status io_join(mf_ctx* c) {
+	if (c->io_thread.joinable()) c->io_thread.join();
+	mf_status st = c->io_status;
+	if (st != MF_OK) {
+		c->err = c->io_err;
+		c->io_status = MF_OK;
+	}
+	return st;
+}
+
+struct IoBody {
+	uint32_t n;
+	double time, rho0;
+	const std::vector<double>* h;
+};
+
+// Writes the snapshot copied to host memory `hb` (layout: per field, all rows).
+mf_status io_write(const char* path, int kind, int method, int precision, bool mixed, uint32_t n_total,
+                   const std::vector<IoBody>& bodies, const std::vector<uint32_t>& offs, const unsigned char* hb,
+                   std::string& err) {
+	const double* f64[6];  // x y vx vy fcx fcy
+	for (int q = 0; q < 6; q++) f64[q] = reinterpret_cast<const double*>(hb) + (size_t)q * n_total;
+	const unsigned char* rest = hb + 6 * 8 * (size_t)n_total;  // rho Sxx Sxy Syy
+	auto rs = [&](int q, uint32_t i, double rho0) -> double {
+		if (mixed) return (double)reinterpret_cast<const float*>(rest)[(size_t)q * n_total + i] + (q == 0 ? rho0 : 0.);
+		return reinterpret_cast<const double*>(rest)[(size_t)q * n_total + i];
+	};
+	if (kind == MF_DUMP_VTK) {
+		// the host writer takes FP64 arrays per body
+		std::vector<std::vector<double>> rho(bodies.size()), sxx(bodies.size()), sxy(bodies.size()), syy(bodies.size());
+		std::vector<mf_vtk_body> vbs(bodies.size());
+		for (size_t b = 0; b < bodies.size(); b++) {
+			uint32_t o = offs[b], n = bodies[b].n;
+			rho[b].resize(n); sxx[b].resize(n); sxy[b].resize(n); syy[b].resize(n);
+			for (uint32_t i = 0; i < n; i++) {
+				rho[b][i] = rs(0, o + i, bodies[b].rho0);
+				sxx[b][i] = rs(1, o + i, 0.);
+				sxy[b][i] = rs(2, o + i, 0.);
+				syy[b][i] = rs(3, o + i, 0.);
+			}
+			vbs[b] = mf_vtk_body{n, 0, f64[0] + o, f64[1] + o, bodies[b].h->data(), rho[b].data(), sxx[b].data(),
+			                     sxy[b].data(), syy[b].data(), f64[2] + o, f64[3] + o};
+		}
+		mf_status st = mf_vtk_write(path, vbs.data(), (uint32_t)vbs.size());
+		if (st != MF_OK) err = std::string("cannot write ") + path;
+		return st;
+	}
+	FILE* fp = fopen(path, "wb");
+	if (!fp) {
+		err = std::string("cannot open ") + path;
+		return MF_ERR_ARG;
+	}
+	// checkpoint: magic, method, precision, bodies; per body n, time, then its rows of
+	// x y vx vy (FP64), rho Sxx Sxy Syy (FP64, or the mixed form's FP32 with rho - rho0),
+	// fcx fcy (FP64)
+	bool ok = fwrite(CKPT_MAGIC, 1, 8, fp) == 8;
+	uint32_t hdr[3] = {(uint32_t)method, (uint32_t)precision, (uint32_t)bodies.size()};
+	ok = ok && fwrite(hdr, 4, 3, fp) == 3;
+	const size_t es = mixed ? 4 : 8;
+	for (size_t b = 0; b < bodies.size() && ok; b++) {
+		uint32_t o = offs[b], n = bodies[b].n;
+		ok = ok && fwrite(&n, 4, 1, fp) == 1 && fwrite(&bodies[b].time, 8, 1, fp) == 1;
+		for (int q = 0; q < 4 && ok; q++) ok = fwrite(f64[q] + o, 8, n, fp) == n;
+		for (int q = 0; q < 4 && ok; q++) ok = fwrite(rest + ((size_t)q * n_total + o) * es, es, n, fp) == n;
+		for (int q = 4; q < 6 && ok; q++) ok = fwrite(f64[q] + o, 8, n, fp) == n;
+	}
+	ok = (fclose(fp) == 0) && ok;
+	if (!ok) {
+		err = std::string("cannot write ") + path;
+		return MF_ERR_ARG;
+	}
+	return MF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MF_API mf_status mf_vtk_write(const char* path, const mf_vtk_body* bodies, uint32_t n_bodies) {
+	if (!path || (n_bodies && !bodies)) return MF_ERR_ARG;
+	uint64_t tot = 0;
+	for (uint32_t b = 0; b < n_bodies; b++) {
+		const mf_vtk_body& v = bodies[b];
+		if (v.n && !(v.x && v.y && v.h && v.rho && v.Sxx && v.Sxy && v.Syy && v.vx && v.vy)) return MF_ERR_ARG;
+		tot += v.n;
+	}
+	if (tot > 0x7fffffffull) return MF_ERR_CAPACITY;
+	FILE* fp = fopen(path, "w+");
+	if (!fp) return MF_ERR_ARG;
+	const unsigned nt = (unsigned)tot;
+	fprintf(fp, "# vtk DataFile Version 2.0\n");
+	fprintf(fp, "mfree iwf\n");
+	fprintf(fp, "ASCII\n");
+	fprintf(fp, "\n");
+	fprintf(fp, "DATASET UNSTRUCTURED_GRID\n");
+	fprintf(fp, "POINTS %d float\n", nt);
+	for (uint32_t b = 0; b < n_bodies; b++)
+		for (uint32_t i = 0; i < bodies[b].n; i++) fprintf(fp, "%f %f %f\n", bodies[b].x[i], bodies[b].y[i], 0.);
+	fprintf(fp, "\n");
+	fprintf(fp, "CELLS %d %d\n", nt, 2 * nt);
+	for (unsigned i = 0; i < nt; i++) fprintf(fp, "%d %d\n", 1, i);
+	fprintf(fp, "\n");
+	fprintf(fp, "CELL_TYPES %d\n", nt);
+	for (unsigned i = 0; i < nt; i++) fprintf(fp, "%d\n", 1);
+	fprintf(fp, "\n");
+	fprintf(fp, "POINT_DATA %d\n", nt);
+	const char* names[5] = {"h", "density", "Sxx", "Sxy", "Syy"};
+	for (int k = 0; k < 5; k++) {
+		fprintf(fp, "SCALARS %s float 1\n", names[k]);
+		fprintf(fp, "LOOKUP_TABLE default\n");
+		for (uint32_t b = 0; b < n_bodies; b++) {
+			const double* a[5] = {bodies[b].h, bodies[b].rho, bodies[b].Sxx, bodies[b].Sxy, bodies[b].Syy};
+			for (uint32_t i = 0; i < bodies[b].n; i++) fprintf(fp, "%f\n", a[k][i]);
+		}
+		fprintf(fp, "\n");
+	}
+	fprintf(fp, "VECTORS velocity float\n");
+	for (uint32_t b = 0; b < n_bodies; b++)
+		for (uint32_t i = 0; i < bodies[b].n; i++) fprintf(fp, "%f %f %f\n", bodies[b].vx[i], bodies[b].vy[i], 0.);
+	fprintf(fp, "\n");
+	return fclose(fp) == 0 ? MF_OK : MF_ERR_ARG;
+}
+
+MF_API mf_status mf_dump_async(mf_ctx* c, const char* path, int32_t kind) {
+	if (!c || !path || (kind != MF_DUMP_VTK && kind != MF_DUMP_CHECKPOINT)) return MF_ERR_ARG;
+	if (kind == MF_DUMP_CHECKPOINT && c->cfg.method == MF_METHOD_TL_WEAK)
+		return fail(c, MF_ERR_STATE, "checkpoints cover updated- and total-Lagrangian bodies (not the weak form's Gauss points)");
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if ((st = io_join(c)) != MF_OK) return st;  // one dump in flight at a time
+	CK(cudaSetDevice(c->cfg.device));
+	const uint32_t n = c->n_total;
+	const size_t bytes = io_row_bytes(c) * (size_t)n;
+	if (c->io_dev.n < bytes) {
+		c->io_dev.free();
+		CK(c->io_dev.alloc(bytes));
+	}
+	if (c->io_host_bytes < bytes) {
+		if (c->io_host) cudaFreeHost(c->io_host);
+		c->io_host = nullptr;
+		c->io_host_bytes = 0;
+		CK(cudaMallocHost(&c->io_host, bytes));
+		c->io_host_bytes = bytes;
+	}
+	if (!c->io_stream) CK(cudaStreamCreateWithFlags(&c->io_stream, cudaStreamNonBlocking));
+	if (!c->io_ready) CK(cudaEventCreateWithFlags(&c->io_ready, cudaEventDisableTiming));
+	// snapshot on the simulation stream, after every step already issued
+	unsigned char* d = c->io_dev.p;
+	const double* src64[6] = {c->sd[0][0].p, c->sd[0][1].p, c->sd[0][2].p, c->sd[0][3].p, c->fcx.p, c->fcy.p};
+	for (int q = 0; q < 6; q++) CK(cudaMemcpyAsync(d + (size_t)q * 8 * n, src64[q], 8 * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+	unsigned char* rest = d + 6 * 8 * (size_t)n;
+	for (int q = 0; q < 4; q++) {
+		if (c->mixed)
+			CK(cudaMemcpyAsync(rest + (size_t)q * 4 * n, c->sf[0][q].p, 4 * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+		else
+			CK(cudaMemcpyAsync(rest + (size_t)q * 8 * n, c->sd[0][4 + q].p, 8 * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+	}
+	CK(cudaEventRecord(c->io_ready, c->stream));
+	// what the writer needs from the host side, captured now
+	std::vector<IoBody> bodies;
+	std::vector<uint32_t> offs;
+	for (auto& b : c->bodies) {
+		bodies.push_back(IoBody{b.n, b.time, b.sd.rho0, &b.in[6]});
+		offs.push_back(b.off);
+	}
+	std::string p(path);
+	int method = c->cfg.method, prec = c->cfg.precision, dev = c->cfg.device;
+	bool mixed = c->mixed;
+	c->io_status = MF_OK;
+	c->io_thread = std::thread([c, p, kind, method, prec, dev, mixed, n, bytes, bodies, offs]() {
+		cudaError_t e = cudaSetDevice(dev);
+		if (e == cudaSuccess) e = cudaStreamWaitEvent(c->io_stream, c->io_ready, 0);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(c->io_host, c->io_dev.p, bytes, cudaMemcpyDeviceToHost, c->io_stream);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(c->io_stream);
+		if (e != cudaSuccess) {
+			c->io_err = std::string("state dump: ") + cudaGetErrorString(e);
+			c->io_status = MF_ERR_CUDA;
+			return;
+		}
+		std::string err;
+		mf_status s2 = io_write(p.c_str(), kind, method, prec, mixed, n, bodies, offs, c->io_host, err);
+		if (s2 != MF_OK) {
+			c->io_err = err;
+			c->io_status = s2;
+		}
+	});
+	return MF_OK;
+}
+
+MF_API mf_status mf_dump_wait(mf_ctx* c) {
+	if (!c) return MF_ERR_ARG;
+	return io_join(c);
+}
+
+MF_API mf_status mf_write_vtk(mf_ctx* c, const char* path) {
+	mf_status st = mf_dump_async(c, path, MF_DUMP_VTK);
+	return st != MF_OK ? st : mf_dump_wait(c);
+}
+
+MF_API mf_status mf_checkpoint_save(mf_ctx* c, const char* path) {
+	mf_status st = mf_dump_async(c, path, MF_DUMP_CHECKPOINT);
+	return st != MF_OK ? st : mf_dump_wait(c);
+}
+
+MF_API mf_status mf_checkpoint_load(mf_ctx* c, const char* path) {
+	if (!c || !path) return MF_ERR_ARG;
+	if (c->cfg.method == MF_METHOD_TL_WEAK)
+		return fail(c, MF_ERR_STATE, "checkpoints cover updated- and total-Lagrangian bodies (not the weak form's Gauss points)");
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if ((st = io_join(c)) != MF_OK) return st;
+	FILE* fp = fopen(path, "rb");
+	if (!fp) return fail(c, MF_ERR_ARG, "cannot open %s", path);
+	char magic[8];
+	uint32_t hdr[3];
+	bool ok = fread(magic, 1, 8, fp) == 8 && !memcmp(magic, CKPT_MAGIC, 8) && fread(hdr, 4, 3, fp) == 3;
+	if (!ok || hdr[0] != (uint32_t)c->cfg.method || hdr[1] != (uint32_t)c->cfg.precision || hdr[2] != c->bodies.size()) {
+		fclose(fp);
+		return fail(c, MF_ERR_ARG, "%s is not a checkpoint of this context's method, precision and bodies", path);
+	}
+	CK(cudaSetDevice(c->cfg.device));
+	const bool tl = c->cfg.method == MF_METHOD_TL;
+	const size_t es = c->mixed ? 4 : 8;
+	std::vector<double> times(c->bodies.size());
+	std::vector<unsigned char> buf;
+	for (size_t b = 0; b < c->bodies.size(); b++) {
+		HostBody& B = c->bodies[b];
+		uint32_t n = 0;
+		ok = fread(&n, 4, 1, fp) == 1 && n == B.n && fread(&times[b], 8, 1, fp) == 1;
+		buf.resize((size_t)n * (6 * 8 + 4 * es));
+		ok = ok && fread(buf.data(), 1, buf.size(), fp) == buf.size();
+		if (!ok) {
+			fclose(fp);
+			return fail(c, MF_ERR_ARG, "%s: body %zu does not match (particle count or truncated file)", path, b);
+		}
+		const unsigned char* q0 = buf.data();
+		for (int q = 0; q < 4; q++) {  // x y vx vy
+			CK(cudaMemcpy(c->sd[0][q].p + B.off, q0 + (size_t)q * 8 * n, 8 * (size_t)n, cudaMemcpyHostToDevice));
+			if (tl) CK(cudaMemcpy(c->sd[2][q].p + B.off, q0 + (size_t)q * 8 * n, 8 * (size_t)n, cudaMemcpyHostToDevice));
+		}
+		const unsigned char* r0 = q0 + 4 * 8 * (size_t)n;
+		for (int q = 0; q < 4; q++) {  // rho Sxx Sxy Syy, in the context's own representation
+			const unsigned char* src = r0 + (size_t)q * es * n;
+			if (c->mixed) {
+				CK(cudaMemcpy(c->sf[0][q].p + B.off, src, 4 * (size_t)n, cudaMemcpyHostToDevice));
+				if (tl) CK(cudaMemcpy(c->sf[2][q].p + B.off, src, 4 * (size_t)n, cudaMemcpyHostToDevice));
+			} else {
+				CK(cudaMemcpy(c->sd[0][4 + q].p + B.off, src, 8 * (size_t)n, cudaMemcpyHostToDevice));
+				if (tl) CK(cudaMemcpy(c->sd[2][4 + q].p + B.off, src, 8 * (size_t)n, cudaMemcpyHostToDevice));
+			}
+		}
+		const unsigned char* f0 = r0 + 4 * es * (size_t)n;
+		CK(cudaMemcpy(c->fcx.p + B.off, f0, 8 * (size_t)n, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->fcy.p + B.off, f0 + 8 * (size_t)n, 8 * (size_t)n, cudaMemcpyHostToDevice));
+	}
+	fclose(fp);
+	for (size_t b = 0; b < c->bodies.size(); b++) {
+		c->bodies[b].time = times[b];
+		CK(cudaMemcpy(reinterpret_cast<unsigned char*>(c->params.p) + b * sizeof(BodyParams) + offsetof(BodyParams, time),
+		              &times[b], 8, cudaMemcpyHostToDevice));
+	}
+	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the loaded state
+	if ((st = tl_prepack(c)) != MF_OK) return st;
+	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
 }
 

@@ -24,6 +24,10 @@
 #include "benchmarks/rings.h"
 #include "benchmarks/tensile.h"
 
+#include "vtk_writer.h"
+
+#include <unistd.h>
+
 #include "mfcase.h"
 
 using namespace mfcase;
@@ -205,6 +209,9 @@ void dump(Writer& w, unsigned step, std::vector<body<T>>& bodies) {
 	}
 }
 
+// set by `run CASE RESULT VTKDIR`: also write the final state with vtk_writer_write
+const char* g_vtk_dir = nullptr;
+
 template <typename T>
 void run_loop(Writer& w, const Case& c, std::vector<body<T>>& bodies) {
 	double secs = 0.;
@@ -223,6 +230,14 @@ void run_loop(Writer& w, const Case& c, std::vector<body<T>>& bodies) {
 		if ((c.dump_every && s % c.dump_every == 0) || s == c.nsteps) dump(w, s, bodies);
 	}
 	if (c.nsteps == 0) dump(w, 0, bodies);
+	if (g_vtk_dir) {
+		// the reference's own writer: results/out_%06d.vtk below the given directory
+		char cwd[4096];
+		if (getcwd(cwd, sizeof cwd) && chdir(g_vtk_dir) == 0) {
+			vtk_writer_write(bodies, c.nsteps);
+			if (chdir(cwd) != 0) fprintf(stderr, "cannot return to %s\n", cwd);
+		}
+	}
 	w.u32(2);
 	for (unsigned b = 0; b < bodies.size(); b++) {
 		auto& L = g_nbh[b];
@@ -482,10 +497,11 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 int main(int argc, char** argv) {
 	if (argc >= 4 && std::string(argv[1]) == "run") {
 		Case c = read_case(argv[2]);
+		if (argc >= 5) g_vtk_dir = argv[4];
 		return run_case(c, argv[3]);
 	}
 	if (argc >= 7 && std::string(argv[1]) == "scenario")
 		return run_scenario(argv[2], (unsigned)atoi(argv[3]), (unsigned)atoi(argv[4]), argv[5], argv[6]);
-	fprintf(stderr, "usage: %s run CASE RESULT | scenario NAME NBOX NSTEPS CASE_OUT RESULT\n", argv[0]);
+	fprintf(stderr, "usage: %s run CASE RESULT [VTKDIR] | scenario NAME NBOX NSTEPS CASE_OUT RESULT\n", argv[0]);
 	return 2;
 }

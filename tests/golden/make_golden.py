@@ -4,13 +4,17 @@ Runs the reference's own scenario builders and step loop -- compiled out of tree
 from its unmodified sources by oracle/build_ref.sh -- and stores, per case, the
 initial state it built (NAME.case) and the state it reached (NAME.ref.out).  Also
 runs workload-constant cases built by mfree_iwf_gb300.scenarios through the
-reference's body/action machinery.  Needs the reference sources (not on GPU machines).
+reference's body/action machinery, and writes the final state of the VTK cases with
+the reference's own vtk_writer_write (NAME.vtk).  Needs the reference sources (not on
+GPU machines).
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--vtk-only]
 """
 import os
+import shutil
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
@@ -30,10 +34,27 @@ REFERENCE_CASES = [
 ]
 
 
+# cases whose final state is also stored as the reference's VTK output
+VTK_CASES = ["tensile_tl", "rings_tl_contact"]
+
+
+def write_vtk_goldens(ref):
+    for name in VTK_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            os.makedirs(os.path.join(d, "results"))
+            subprocess.run([ref, "run", os.path.join(HERE, f"{name}.case"), os.path.join(d, "o.out"), d], check=True)
+            (vtk,) = os.listdir(os.path.join(d, "results"))
+            shutil.copy(os.path.join(d, "results", vtk), os.path.join(HERE, f"{name}.vtk"))
+            print("wrote", name + ".vtk", "from", vtk)
+
+
 def main():
     ref = oracle.build_ref(force=True)
     if ref is None:
         raise SystemExit("reference sources not present")
+    if "--vtk-only" in sys.argv:
+        write_vtk_goldens(ref)
+        return
     for name, nbox, steps in REFERENCE_CASES:
         case = os.path.join(HERE, f"{name}.case")
         out = os.path.join(HERE, f"{name}.ref.out")
@@ -48,6 +69,7 @@ def main():
     case = os.path.join(HERE, "c2_rings_tl_dx4mm.case")
     S.write_case(case, sc, 30)
     subprocess.run([ref, "run", case, os.path.join(HERE, "c2_rings_tl_dx4mm.ref.out")], check=True)
+    write_vtk_goldens(ref)
     print("done")
 
 
