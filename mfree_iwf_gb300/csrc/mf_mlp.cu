@@ -4,11 +4,12 @@
 // stress and contact-force history (mfree_iwf_gb300/surrogate.py).  No counterpart in
 // the reference: this is a learned screen placed in front of the solver.
 //
-// Every matrix product goes through one tiled tensor-core GEMM (k_gemm): 64x64 output
-// tiles, K in slices of 32 staged in shared memory, four warps of 32x32 outputs each
-// issuing mma.sync m16n8k16 (BF16 inputs, FP32 accumulators), gridDim.z over the
-// ensemble members.  The bias and ReLU are fused into the epilogue, which stores FP32
-// and/or BF16.  The layers (6 -> 256 -> 256 -> 256 -> 66, a few hundred rows per
+// The forward products go through a pipelined tensor-core GEMM (k_gemm_nt: 128x64
+// tiles, cp.async double buffering, ldmatrix fragments); the backward products, whose
+// operands are transposed, through a simpler tiled one (k_gemm: 64x64 tiles staged
+// element-wise).  Both issue mma.sync m16n8k16 (BF16 inputs, FP32 accumulators) with
+// gridDim.z over the ensemble members, and fuse the bias and ReLU into the epilogue,
+// which stores FP32 and/or BF16.  The layers (6 -> 256 -> 256 -> 256 -> 66, a few hundred rows per
 // training batch) are too small for a TMA/tcgen05 pipeline to pay off.
 //
 // Training keeps the whole data set on the device.  One training step -- bootstrap
@@ -148,6 +149,126 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
 					if (C) C[(long long)m * g.ldc + n] = v;
 					if (Cb) Cb[(long long)m * g.ldcb + n] = __float2bfloat16(v);
 				}
+}
+
+
+// The forward product Z = H W^T (A row-major [M][K], B = W row-major [N][K], both
+// contiguous in k) as a pipelined kernel: 128x64 output tiles, 8 warps of 32x32,
+// K in slices of 32 double-buffered in shared memory by 16-byte cp.async (zero-filled
+// past M and K), fragments by ldmatrix, mma.sync m16n8k16 BF16 -> FP32.  Needs K, lda
+// and ldb multiples of 8 (the padded widths are multiples of 16).
+constexpr int NT_BM = 128, NT_BN = 64, NT_BK = 32, NT_LD = NT_BK + 8;  // 80-byte rows: ldmatrix conflict-free
+
+__device__ __forceinline__ void cp16z(void* smem, const void* gmem, uint32_t bytes) {
+	uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+	uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+	asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+	             : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+	             : "r"(a));
+}
+
+__global__ void __launch_bounds__(256) k_gemm_nt(GemmArgs g) {
+	__shared__ __align__(128) bf16 As[2][NT_BM][NT_LD];
+	__shared__ __align__(128) bf16 Bs[2][NT_BN][NT_LD];
+	const int z = blockIdx.z;
+	const bf16* A = g.A + z * g.sA;
+	const bf16* B = g.B + z * g.sB;
+	const int m0 = blockIdx.y * NT_BM, n0 = blockIdx.x * NT_BN;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int wm = warp >> 1, wn = warp & 1;  // 4 x 2 warps
+	const int gid = lane >> 2, tig = lane & 3;
+	auto load = [&](int st, int k0) {
+		// A: 128 rows x 4 chunks of 8 elements; B: 64 rows x 4 chunks
+#pragma unroll
+		for (int r = 0; r < 2; r++) {
+			const int e = tid + 256 * r, row = e >> 2, ch = e & 3;
+			const int m = m0 + row, k = k0 + ch * 8;
+			const bool ok = m < g.M && k < g.K;
+			cp16z(&As[st][row][ch * 8], ok ? (const void*)(A + (long long)m * g.lda + k) : (const void*)A, ok ? 16u : 0u);
+		}
+		{
+			const int row = tid >> 2, ch = tid & 3;
+			const int n = n0 + row, k = k0 + ch * 8;
+			const bool ok = n < g.N && k < g.K;
+			cp16z(&Bs[st][row][ch * 8], ok ? (const void*)(B + (long long)n * g.ldb + k) : (const void*)B, ok ? 16u : 0u);
+		}
+		asm volatile("cp.async.commit_group;\n" ::: "memory");
+	};
+	float acc[2][4][4];
+#pragma unroll
+	for (int a = 0; a < 2; a++)
+#pragma unroll
+		for (int b = 0; b < 4; b++)
+#pragma unroll
+			for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
+	const int nk = (g.K + NT_BK - 1) / NT_BK;
+	load(0, 0);
+	for (int kt = 0; kt < nk; kt++) {
+		if (kt + 1 < nk) {
+			load((kt + 1) & 1, (kt + 1) * NT_BK);
+			asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+		} else {
+			asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+		}
+		__syncthreads();
+		const int st = kt & 1;
+#pragma unroll
+		for (int ks = 0; ks < NT_BK; ks += 16) {
+			uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+			for (int mt = 0; mt < 2; mt++) {
+				const int r = wm * 32 + mt * 16 + (lane & 15), c = ks + (lane >> 4) * 8;
+				ldsm_x4(af[mt][0], af[mt][1], af[mt][2], af[mt][3], &As[st][r][c]);
+			}
+#pragma unroll
+			for (int np = 0; np < 2; np++) {  // two n-tiles of 8 per ldmatrix.x4
+				const int r = wn * 32 + np * 16 + (lane & 7) + ((lane >> 4) << 3), c = ks + ((lane >> 3) & 1) * 8;
+				ldsm_x4(bfr[2 * np][0], bfr[2 * np][1], bfr[2 * np + 1][0], bfr[2 * np + 1][1], &Bs[st][r][c]);
+			}
+#pragma unroll
+			for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+				for (int nt = 0; nt < 4; nt++) {
+					float* d = acc[mt][nt];
+					asm volatile(
+					    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+					    "{%0,%1,%2,%3};\n"
+					    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+					    : "r"(af[mt][0]), "r"(af[mt][1]), "r"(af[mt][2]), "r"(af[mt][3]), "r"(bfr[nt][0]),
+					      "r"(bfr[nt][1]));
+				}
+		}
+		__syncthreads();
+	}
+	// epilogue: each thread holds column pairs (n, n+1) -- stored as one float2 / bf16x2
+	// (N, ldc and ldcb are even: the padded widths are multiples of 16)
+	float* C = g.C ? g.C + z * g.sC : nullptr;
+	bf16* Cb = g.Cb ? g.Cb + z * g.sCb : nullptr;
+	const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
+#pragma unroll
+	for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+		for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				const int m = m0 + wm * 32 + mt * 16 + gid + 8 * h;
+				const int n = n0 + wn * 32 + nt * 8 + tig * 2;
+				if (m >= g.M || n >= g.N) continue;
+				float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
+				if (bias) {
+					v0 += bias[n];
+					v1 += bias[n + 1];
+				}
+				if (g.relu) {
+					v0 = fmaxf(v0, 0.f);
+					v1 = fmaxf(v1, 0.f);
+				}
+				if (C) *reinterpret_cast<float2*>(C + (long long)m * g.ldc + n) = make_float2(v0, v1);
+				if (Cb) *reinterpret_cast<__nv_bfloat162*>(Cb + (long long)m * g.ldcb + n) = __floats2bfloat162_rn(v0, v1);
+			}
 }
 
 // Training control block in device memory, read by the graph's kernels on every replay.
@@ -364,7 +485,11 @@ mf_status mlp_fail(mf_mlp* m, const std::string& what, cudaError_t e) {
 cudaError_t gemm(mf_mlp* m, bool ta, bool tb, GemmArgs g) {
 	dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, m->members);
 	cudaStream_t s = m->stream;
-	if (!ta && tb) k_gemm<false, true><<<grid, 128, 0, s>>>(g);
+	if (!ta && tb && g.K % 8 == 0 && g.lda % 8 == 0 && g.ldb % 8 == 0 && g.N % 2 == 0 && (!g.C || g.ldc % 2 == 0) &&
+	    (!g.Cb || g.ldcb % 2 == 0)) {
+		dim3 gnt((g.N + NT_BN - 1) / NT_BN, (g.M + NT_BM - 1) / NT_BM, m->members);
+		k_gemm_nt<<<gnt, 256, 0, s>>>(g);
+	} else if (!ta && tb) k_gemm<false, true><<<grid, 128, 0, s>>>(g);
 	else if (!ta && !tb) k_gemm<false, false><<<grid, 128, 0, s>>>(g);
 	else if (ta && !tb) k_gemm<true, false><<<grid, 128, 0, s>>>(g);
 	else k_gemm<true, true><<<grid, 128, 0, s>>>(g);

@@ -543,6 +543,41 @@ def run_experiment(n_train: int = 20000, n_test: int = 1000, val_frac: float = 0
     }
 
 
+
+def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device: int = 0) -> dict:
+    """Inference throughput of the ensemble on device-resident inputs: `chunks` passes of
+    `rows` rows through 6 -> 256 -> 256 -> 256 -> 66, timed with CUDA events on the
+    library's stream; FLOPs counted on the true (unpadded) layer sizes."""
+    import torch
+
+    dims = [len(FEATURE_LIMITS), 256, 256, 256, N_OUT]
+    mlp = Mlp(dims, members=members, max_batch=rows, seed=1, device=device)
+    n = rows * chunks
+    x = torch.rand(n, dims[0], device=f"cuda:{device}", dtype=torch.float32) * 2 - 1
+    y = torch.empty(members, n, dims[-1], device=f"cuda:{device}", dtype=torch.float32)
+    fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+    lib = mlp._lib
+    s = ctypes.c_void_p()
+    lib.mf_mlp_get_stream(mlp._h, ctypes.byref(s))
+    stream = torch.cuda.ExternalStream(s.value)
+    for _ in range(3):  # warm-up
+        mlp._check(lib.mf_mlp_predict(mlp._h, fp(x), n, fp(y)), "mf_mlp_predict")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = 5
+    for _ in range(reps):
+        mlp._check(lib.mf_mlp_predict(mlp._h, fp(x), n, fp(y)), "mf_mlp_predict")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3 / reps
+    flop_row = 2 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+    flops = flop_row * members * n
+    mlp.close()
+    return {"rows_per_pass": rows, "instances": n, "members": members, "seconds": secs,
+            "instances_per_s": n / secs, "tflops": flops / secs / 1e12, "flop_per_instance_member": flop_row}
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -553,8 +588,9 @@ if __name__ == "__main__":
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--data", default=None, help=".npz cache of the training set's solver outputs")
     ap.add_argument("--out", default=None, help="write the JSON result here too")
+    ap.add_argument("--gemm-bench", action="store_true", help="only time the ensemble's inference GEMMs")
     a = ap.parse_args()
-    r = run_experiment(a.train, a.test, train_steps=a.steps, data=a.data)
+    r = gemm_benchmark() if a.gemm_bench else run_experiment(a.train, a.test, train_steps=a.steps, data=a.data)
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:
