@@ -284,23 +284,18 @@ def ours(args, cfg_desc):
     kstats = {k: sim.kernel_stats(k) for k in range(6)}
     sim.set_timing(False)
 
-    # ---- end to end through the C ABI with host buffers: per step the state goes
-    # host -> device (pinned), one step runs, the state comes back device -> host
+    # ---- end to end through the C ABI with host buffers: per step the state of all
+    # bodies goes host -> device (pinned), one step runs, the state comes back
     fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy")
-    host = []
-    for b in range(len(sc.bodies)):
-        st = sim.get_state(b, fields)
-        pinned = {f: torch.from_numpy(st[f]).pin_memory().numpy() for f in fields}
-        host.append(pinned)
+    host = {f: torch.empty(n, dtype=torch.float64).pin_memory().numpy() for f in fields}
+    sim.get_state_all_into(host)
     k2 = max(3, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(k2):
-        for b in range(len(sc.bodies)):
-            sim.set_state(b, host[b])
+        sim.set_state_all(host)
         sim.step(1)
-        for b in range(len(sc.bodies)):
-            sim.get_state_into(b, host[b])
+        sim.get_state_all_into(host)
     wall = time.perf_counter() - t0
     _, e2e_value = job_throughput(dist, wall, n * k2)
     bytes_io = 8 * len(fields) * n

@@ -171,6 +171,11 @@ MF_API mf_status mf_synchronize(mf_ctx* ctx);
 MF_API mf_status mf_get_state(mf_ctx* ctx, int32_t body, const mf_state* out);
 /* Overwrite a body's state (x, y, vx, vy, rho, Sxx, Sxy, Syy; NULL fields kept). */
 MF_API mf_status mf_set_state(mf_ctx* ctx, int32_t body, const mf_particles* p);
+/* All bodies at once: one row per particle of the context, the bodies' rows
+ * concatenated in id order (one transfer per field instead of one per body and field;
+ * for ensembles of hundreds of bodies). */
+MF_API mf_status mf_get_state_all(mf_ctx* ctx, const mf_state* out);
+MF_API mf_status mf_set_state_all(mf_ctx* ctx, const mf_particles* p);
 MF_API mf_status mf_get_time(mf_ctx* ctx, int32_t body, double* t);
 MF_API mf_status mf_num_particles(mf_ctx* ctx, int32_t body, uint32_t* n);
 

@@ -106,6 +106,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_synchronize": (C.c_int32, [C.c_void_p]),
         "mf_get_state": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(MfState)]),
         "mf_set_state": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(MfParticles)]),
+        "mf_get_state_all": (C.c_int32, [C.c_void_p, C.POINTER(MfState)]),
+        "mf_set_state_all": (C.c_int32, [C.c_void_p, C.POINTER(MfParticles)]),
         "mf_get_time": (C.c_int32, [C.c_void_p, C.c_int32, _DP]),
         "mf_num_particles": (C.c_int32, [C.c_void_p, C.c_int32, _UP]),
         "mf_get_neighbors": (C.c_int32, [C.c_void_p, C.c_int32, _UP, _UP, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -283,6 +285,16 @@ class Simulation:
         cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
         p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
         self._check(self._lib.mf_set_state(self._h, body, ctypes.byref(p)), "mf_set_state")
+
+    def get_state_all_into(self, out: Dict[str, np.ndarray]) -> None:
+        """Every body's rows (concatenated in body order) -> caller-owned float64 arrays."""
+        s = MfState(*[_dptr(out.get(f)) for f in _SFIELDS])
+        self._check(self._lib.mf_get_state_all(self._h, ctypes.byref(s)), "mf_get_state_all")
+
+    def set_state_all(self, arrays: Dict[str, np.ndarray]) -> None:
+        cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
+        p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
+        self._check(self._lib.mf_set_state_all(self._h, ctypes.byref(p)), "mf_set_state_all")
 
     def time(self, body: int = 0) -> float:
         t = ctypes.c_double()

@@ -86,6 +86,17 @@ __global__ void k_f32_to_f64(uint32_t n, const float* __restrict__ a, double* __
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < n) b[i] = off + (double)a[i];
 }
+// the same over all bodies' rows, the density offset being each row's body's rho0
+__global__ void k_f64_to_f32_rows(uint32_t n, const double* __restrict__ a, float* __restrict__ b,
+                                  const uint32_t* __restrict__ body_of, const BodyParams* __restrict__ P, int rho) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (float)(a[i] - (rho ? P[body_of[i]].rho0 : 0.));
+}
+__global__ void k_f32_to_f64_rows(uint32_t n, const float* __restrict__ a, double* __restrict__ b,
+                                  const uint32_t* __restrict__ body_of, const BodyParams* __restrict__ P, int rho) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (rho ? P[body_of[i]].rho0 : 0.) + (double)a[i];
+}
 
 struct HostBC {
 	int32_t kind;
@@ -1707,6 +1718,79 @@ MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 		} else {
 			CK(cudaMemcpyAsync(c->sd[0][q].p + b.off, src[q], b.n * 8, cudaMemcpyHostToDevice, c->stream));
 			if (tl) CK(cudaMemcpyAsync(c->sd[2][q].p + b.off, c->sd[0][q].p + b.off, b.n * 8, cudaMemcpyDeviceToDevice, c->stream));
+		}
+	}
+	CK(cudaGetLastError());
+	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the new state
+	mf_status pst = tl_prepack(c);
+	if (pst != MF_OK) return pst;
+	CK(cudaStreamSynchronize(c->stream));
+	return MF_OK;
+}
+
+MF_API mf_status mf_get_state_all(mf_ctx* c, const mf_state* out) {
+	if (!c || !out) return MF_ERR_ARG;
+	if (!c->ready) {
+		for (int32_t b = 0; b < (int32_t)c->bodies.size(); b++) {
+			const uint32_t o = c->bodies[b].off;
+			auto at = [o](double* p) { return p ? p + o : nullptr; };
+			mf_state ob = {at(out->x), at(out->y), at(out->vx), at(out->vy), at(out->rho),
+			               at(out->Sxx), at(out->Sxy), at(out->Syy), at(out->fcx), at(out->fcy)};
+			mf_status st = mf_get_state(c, b, &ob);
+			if (st != MF_OK) return st;
+		}
+		return MF_OK;
+	}
+	CK(cudaSetDevice(c->cfg.device));
+	const uint32_t n = c->n_total;
+	double* o[8] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy};
+	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)n));
+	for (int q = 0; q < 8; q++) {
+		if (!o[q]) continue;
+		if (c->mixed && q >= 4) {
+			double* st = c->staging.p + (size_t)(q - 4) * n;
+			k_f32_to_f64_rows<<<(n + 255) / 256, 256, 0, c->stream>>>(n, c->sf[0][q - 4].p, st, c->body_of.p, c->params.p,
+			                                                        q == 4);
+			CK(cudaMemcpyAsync(o[q], st, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+		} else {
+			CK(cudaMemcpyAsync(o[q], c->sd[0][q].p, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+		}
+	}
+	if (out->fcx) CK(cudaMemcpyAsync(out->fcx, c->fcx.p, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+	if (out->fcy) CK(cudaMemcpyAsync(out->fcy, c->fcy.p, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_state_all(mf_ctx* c, const mf_particles* p) {
+	if (!c || !p) return MF_ERR_ARG;
+	if (!c->ready) {
+		for (int32_t b = 0; b < (int32_t)c->bodies.size(); b++) {
+			const uint32_t o = c->bodies[b].off;
+			auto at = [o](const double* q) { return q ? q + o : nullptr; };
+			mf_particles pb = {at(p->x), at(p->y), nullptr, nullptr, nullptr, at(p->rho), nullptr, nullptr,
+			                   at(p->vx), at(p->vy), at(p->Sxx), at(p->Sxy), at(p->Syy)};
+			mf_status st = mf_set_state(c, b, &pb);
+			if (st != MF_OK) return st;
+		}
+		return MF_OK;
+	}
+	CK(cudaSetDevice(c->cfg.device));
+	const uint32_t n = c->n_total;
+	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
+	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)n));
+	const bool tl = c->cfg.method != MF_METHOD_UL;  // TL stage 0 starts from its own copy (set 2)
+	for (int q = 0; q < 8; q++) {
+		if (!src[q]) continue;
+		if (c->mixed && q >= 4) {
+			double* st = c->staging.p + (size_t)(q - 4) * n;
+			CK(cudaMemcpyAsync(st, src[q], (size_t)n * 8, cudaMemcpyHostToDevice, c->stream));
+			k_f64_to_f32_rows<<<(n + 255) / 256, 256, 0, c->stream>>>(n, st, c->sf[0][q - 4].p, c->body_of.p, c->params.p,
+			                                                        q == 4);
+			if (tl) CK(cudaMemcpyAsync(c->sf[2][q - 4].p, c->sf[0][q - 4].p, (size_t)n * 4, cudaMemcpyDeviceToDevice, c->stream));
+		} else {
+			CK(cudaMemcpyAsync(c->sd[0][q].p, src[q], (size_t)n * 8, cudaMemcpyHostToDevice, c->stream));
+			if (tl) CK(cudaMemcpyAsync(c->sd[2][q].p, c->sd[0][q].p, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->stream));
 		}
 	}
 	CK(cudaGetLastError());

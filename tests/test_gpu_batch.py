@@ -66,3 +66,36 @@ def test_graph_and_autotune_do_not_change_results(lib, kind):
     for k in range(nb):
         for f in FIELDS:
             assert np.array_equal(got[k][f], want[k][f]), (kind, k, f)
+
+
+@pytest.mark.parametrize("precision", ["fp64_strict", "mixed"])
+def test_all_bodies_state_io_equals_per_body(lib, precision):
+    """get_state_all / set_state_all move every body's rows in one call per field; they
+    read and write exactly what the per-body calls do (densities of bodies with
+    different rho0 included)."""
+    import mfree_iwf_gb300 as M
+    ens = small_ensemble()
+    sims = [M.from_scenario(ens, precision=precision) for _ in range(2)]
+    for s in sims:
+        s.step(7)
+    n = sum(b.n for b in ens.bodies)
+    allst = {f: np.empty(n) for f in FIELDS}
+    sims[0].get_state_all_into(allst)
+    per = states(sims[0], len(ens.bodies))
+    offs = np.cumsum([0] + [b.n for b in ens.bodies])
+    for k in range(len(ens.bodies)):
+        for f in FIELDS:
+            np.testing.assert_array_equal(allst[f][offs[k]:offs[k + 1]], per[k][f])
+    # write back: all at once into one context, per body into the other, then step on
+    perturbed = {f: v * (1 + 1e-9) if f in ("vx", "vy") else v for f, v in allst.items()}
+    sims[0].set_state_all(perturbed)
+    for k in range(len(ens.bodies)):
+        sims[1].set_state(k, {f: perturbed[f][offs[k]:offs[k + 1]] for f in FIELDS})
+    for s in sims:
+        s.step(3)
+    a, b = states(sims[0], len(ens.bodies)), states(sims[1], len(ens.bodies))
+    for k in range(len(ens.bodies)):
+        for f in FIELDS:
+            np.testing.assert_array_equal(a[k][f], b[k][f])
+    for s in sims:
+        s.close()
