@@ -58,7 +58,8 @@ enum {
 typedef enum {
 	MF_METHOD_UL = 1,      /* particle_monaghan: updated-Lagrangian Gray-Monaghan SPH, grid rebuilt per stage */
 	MF_METHOD_TL = 2,      /* particle_tl: total-Lagrangian SPH, fixed neighbours, Randles-Libersky correction */
-	MF_METHOD_TL_WEAK = 3  /* particle_tl_weak: weak-form TL with RKPM shape functions and Gauss points */
+	MF_METHOD_TL_WEAK = 3, /* particle_tl_weak: weak-form TL with RKPM shape functions and Gauss points */
+	MF_METHOD_COROT = 4    /* particle_corotational: TL neighbours, plain SPH weights, per-particle rotation (FP64 forms) */
 } mf_method;
 
 /* Arithmetic forms. */
@@ -96,7 +97,11 @@ typedef enum {
 	MF_MATERIAL_STRESS_RATE_JAUMANN_GP = 24,       /* material.h:86-93 */
 	MF_CONTMECH_CAUCHY_TO_NOMINAL_GP = 25,         /* cont_mech.h:206-211 */
 	MF_DERIVE_STRESS_WEAK_TL = 26,                 /* derivatives.h:260-294 */
-	MF_CONTMECH_MOMENTUM_TL_WEAK = 27              /* cont_mech.h:89-106 */
+	MF_CONTMECH_MOMENTUM_TL_WEAK = 27,             /* cont_mech.h:89-106 */
+	MF_COROTATIONAL_ANISOTROPY_TENSOR = 28,        /* corotational.h:32-84 */
+	MF_DERIVE_DISPLACEMENT_COROTATIONAL = 29,      /* derivatives.h:202-258 */
+	MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN = 30,  /* material.h:102-130 */
+	MF_DERIVE_STRESS_COROTATIONAL = 31             /* derivatives.h:521-588 */
 } mf_action;
 
 /* Boundary-condition kinds (boundary_conditions<T> functors). */

@@ -54,7 +54,11 @@ enum action : int32_t {
 	material_stress_rate_jaumann_gp = MF_MATERIAL_STRESS_RATE_JAUMANN_GP,
 	contmech_cauchy_to_nominal_gp = MF_CONTMECH_CAUCHY_TO_NOMINAL_GP,
 	derive_stress_weak_tl = MF_DERIVE_STRESS_WEAK_TL,
-	contmech_momentum_tl_weak = MF_CONTMECH_MOMENTUM_TL_WEAK
+	contmech_momentum_tl_weak = MF_CONTMECH_MOMENTUM_TL_WEAK,
+	corotational_anisotropy_tensor = MF_COROTATIONAL_ANISOTROPY_TENSOR,
+	derive_displacement_corotational = MF_DERIVE_DISPLACEMENT_COROTATIONAL,
+	material_compute_stress_cauchy_green = MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN,
+	derive_stress_corotational = MF_DERIVE_STRESS_COROTATIONAL
 };
 
 class error : public std::runtime_error {

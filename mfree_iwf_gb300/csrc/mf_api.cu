@@ -197,6 +197,7 @@ struct mf_ctx {
 	DevBuf<float> qw32, m32, h32;
 	DevBuf<float4> recA, recB, dA32;
 	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
+	DevBuf<double> sW64, R64;         // corotational: W per pair (sliced ELL), rotation per row
 	bool tl_recs_valid = false;       // the stage-0 records match the state (pass B keeps them current)
 	uint32_t n_bc = 0;
 
@@ -276,6 +277,7 @@ mf_status cuda_fail(mf_ctx* c, cudaError_t e, const char* where) {
 inline uint32_t abit(int a) { return 1u << a; }
 
 mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
+mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status tl_setup(mf_ctx* c);
 mf_status weak_setup(mf_ctx* c);
 mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
@@ -436,6 +438,8 @@ mf_status finalize(mf_ctx* c) {
 		st = validate_ul(c, acts, c->flags);
 	} else if (c->cfg.method == MF_METHOD_TL) {
 		st = validate_tl(c, acts, c->flags);
+	} else if (c->cfg.method == MF_METHOD_COROT) {
+		st = validate_corot(c, acts, c->flags);
 	} else {
 		st = validate_weak(c, acts, c->flags);
 	}
@@ -514,7 +518,7 @@ mf_status finalize(mf_ctx* c) {
 		c->sort_bits = bits;
 		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
 		CK(c->sort_tmp.alloc(tmp));
-	} else if (c->cfg.method == MF_METHOD_TL) {
+	} else if (c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT) {
 		mf_status s2 = tl_setup(c);
 		if (s2 != MF_OK) return s2;
 	} else {
@@ -698,6 +702,8 @@ TLArgs tl_args(mf_ctx* c) {
 	a.P = c->P64.p;
 	a.dA = c->dA64.p;
 	a.c = c->c64.p;
+	a.sW = c->sW64.p;
+	a.R = c->R64.p;
 	a.recA = c->recA.p;
 	a.recB = c->recB.p;
 	a.dA32 = c->dA32.p;
@@ -736,6 +742,7 @@ mf_status tl_step_all(mf_ctx* c) {
 	// boundary conditions, which change the stage state after pass B
 	const bool fused = c->mixed && c->n_bc == 0;
 	void* rb[2] = {c->recB.p, c->recB2.p};
+	const bool corot = c->cfg.method == MF_METHOD_COROT;
 	for (uint32_t st = 0; st < 4; st++) {
 		a.stage = st;
 		a.st = (st % 2 == 0) ? S0 : S1;
@@ -748,6 +755,20 @@ mf_status tl_step_all(mf_ctx* c) {
 		if ((e = tl_launch(c, a, 0)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
 		if (pack && (e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
 		int slot;
+		if (corot) {
+			auto cr = [&](int part) {
+				return c->strict ? mf_strict::cr_stage(a, part, c->stream) : mf_fast::cr_stage(a, part, c->stream);
+			};
+			if ((e = cr(0)) != cudaSuccess) return cuda_fail(c, e, "corotational rotation");
+			timing_begin(c, 1, slot);
+			if ((e = cr(1)) != cudaSuccess) return cuda_fail(c, e, "corotational pass A");
+			timing_end(c, slot, c->n_total);
+			timing_begin(c, 2, slot);
+			if ((e = cr(2)) != cudaSuccess) return cuda_fail(c, e, "corotational pass B");
+			timing_end(c, slot, c->n_total);
+			c->launches += 3 + (c->n_bc ? 1 : 0);
+			continue;
+		}
 		timing_begin(c, 1, slot);
 		if ((e = tl_launch(c, a, 2)) != cudaSuccess) return cuda_fail(c, e, "tl pass A");
 		timing_end(c, slot, c->n_total);
@@ -775,6 +796,31 @@ mf_status tl_prepack(mf_ctx* c) {
 	if (e != cudaSuccess) return cuda_fail(c, e, "tl pack");
 	c->launches++;
 	c->tl_recs_valid = true;
+	return MF_OK;
+}
+
+// Corotational pipeline (rings.cpp:325-331, tensile.cpp:202-208, rotation.cpp:132-137):
+// the rotation, displacement, Cauchy-Green stress, nominal stress and stress actions
+// in this order, then optionally the artificial viscosity and advection.
+mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_COROTATIONAL_ANISOTROPY_TENSOR, MF_DERIVE_DISPLACEMENT_COROTATIONAL,
+	                            MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN, MF_CONTMECH_CAUCHY_TO_NOMINAL,
+	                            MF_DERIVE_STRESS_COROTATIONAL, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
+	                            MF_CONTMECH_ADVECTION};
+	if (c->cfg.precision == MF_PREC_MIXED)
+		return fail(c, MF_ERR_PIPELINE, "the corotational method runs in the FP64 forms");
+	flags = 0;
+	size_t pos = 0;
+	for (int32_t a : acts) {
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not part of the corotational pipeline or out of its order", a);
+		flags |= abit(a);
+		pos++;
+	}
+	for (int k = 0; k < 5; k++)
+		if (!(flags & abit(order[k])))
+			return fail(c, MF_ERR_PIPELINE, "the corotational pipeline needs action %d", order[k]);
 	return MF_OK;
 }
 
@@ -880,11 +926,23 @@ mf_status tl_setup(mf_ctx* c) {
 	}
 	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
 	const float* rho32 = nullptr;
-	cudaError_t e = c->strict ? mf_strict::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
-	                                             rho32, c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream)
-	                          : mf_fast::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64,
-	                                           rho32, c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream);
-	if (e != cudaSuccess) return cuda_fail(c, e, "tl_rl");
+	const bool corot = c->cfg.method == MF_METHOD_COROT;
+	DevBuf<double> w64;  // corotational: the kernel values of the pairs (precomp_sph)
+	cudaError_t e;
+	if (corot) {
+		CK(w64.alloc(tot));
+		e = c->strict ? mf_strict::cr_sph(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->h.p, w64.p,
+		                                  c->wx64.p, c->wy64.p, c->stream)
+		              : mf_fast::cr_sph(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->h.p, w64.p,
+		                                c->wx64.p, c->wy64.p, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "precomp_sph");
+	} else {
+		e = c->strict ? mf_strict::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64, rho32,
+		                                 c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream)
+		              : mf_fast::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64, rho32,
+		                               c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "tl_rl");
+	}
 	st = check_status(c);
 	if (st != MF_OK) return st;
 	// sliced ELL: slices of 32 rows, each padded to its longest list
@@ -916,6 +974,13 @@ mf_status tl_setup(mf_ctx* c) {
 	                                    c->mixed ? (void*)c->sw32.p : nullptr, c->mixed ? (void*)c->swA32.p : nullptr,
 	                                    c->qw0.p, c->m.p, c->stream);
 	if (e != cudaSuccess) return cuda_fail(c, e, "tl_to_sell");
+	if (corot) {
+		CK(c->sW64.alloc(ent));
+		CK(c->R64.alloc(4 * (size_t)n));
+		e = c->strict ? mf_strict::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream)
+		              : mf_fast::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "corotational weights");
+	}
 	CK(cudaStreamSynchronize(c->stream));
 	c->wx64.free();
 	c->wy64.free();
@@ -1399,7 +1464,7 @@ mf_ctx::~mf_ctx() {
 		g_w64.free(); t_w64.free(); p_w64.free(); g_w32.free(); t_w32.free(); p_w32.free();
 	}
 	sl_off.free(); snbr.free(); scnt.free(); sw64.free(); sw32.free(); swA32.free(); recA.free(); recB.free(); dA32.free();
-	recB2.free();
+	recB2.free(); sW64.free(); R64.free();
 	tt_rows.free(); tt_halo_off.free(); tt_halo.free(); tt_sl.free(); tt_cnt.free(); tt_loc.free(); tt_sw.free();
 	tt_swA.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
@@ -1443,7 +1508,7 @@ MF_API const char* mf_last_error(const mf_ctx* c) { return c ? c->err.c_str() : 
 MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out) {
 	if (!cfg || !out) return MF_ERR_ARG;
 	*out = nullptr;
-	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_TL_WEAK) return MF_ERR_ARG;
+	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_COROT) return MF_ERR_ARG;
 	if (cfg->precision < MF_PREC_FP64_STRICT || cfg->precision > MF_PREC_MIXED) return MF_ERR_ARG;
 	int ndev = 0;
 	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MF_ERR_NO_DEVICE;
@@ -1498,7 +1563,7 @@ MF_API mf_status mf_add_action(mf_ctx* c, int32_t body, int32_t action) {
 	if (!c) return MF_ERR_ARG;
 	if (c->ready) return fail(c, MF_ERR_STATE, "actions must be added before the first step");
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
-	if (action < 1 || action > MF_CONTMECH_MOMENTUM_TL_WEAK) return fail(c, MF_ERR_ARG, "bad action id %d", action);
+	if (action < 1 || action > MF_DERIVE_STRESS_COROTATIONAL) return fail(c, MF_ERR_ARG, "bad action id %d", action);
 	c->bodies[body].actions.push_back(action);
 	return MF_OK;
 }
@@ -1578,7 +1643,8 @@ namespace {
 // The launches of one step of every body, in the driver's order (mfree_iwf.cpp:84-97):
 // the RK4 step, then the boundary refresh and contact.
 mf_status one_step(mf_ctx* c) {
-	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (c->cfg.method == MF_METHOD_TL ? tl_step_all(c) : weak_step(c));
+	const bool tl_lists = c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT;
+	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (tl_lists ? tl_step_all(c) : weak_step(c));
 	if (st != MF_OK) return st;
 	if (c->contact_on) st = contact_run(c);
 	if (st == MF_OK && c->mon_cap) {
@@ -2354,7 +2420,7 @@ MF_API mf_status mf_checkpoint_load(mf_ctx* c, const char* path) {
 		return fail(c, MF_ERR_ARG, "%s is not a checkpoint of this context's method, precision and bodies", path);
 	}
 	CK(cudaSetDevice(c->cfg.device));
-	const bool tl = c->cfg.method == MF_METHOD_TL;
+	const bool tl = c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT;
 	const size_t es = c->mixed ? 4 : 8;
 	std::vector<double> times(c->bodies.size());
 	std::vector<unsigned char> buf;

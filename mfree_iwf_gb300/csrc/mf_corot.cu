@@ -1,0 +1,269 @@
+// Corotational SPH (particle_corotational; rings_corot_contact rings.cpp:245-336,
+// tensile_corot tensile.cpp:137-211): total-Lagrangian neighbour lists with plain SPH
+// weights, and a per-particle rotation that takes the neighbourhood's rigid rotation
+// out of the displacement gradient.
+//
+// Set-up (once): find_neighbors (shared with the TL path), then precomp_sph
+// (precomp_shape_functions.h:210-229): W and grad W of every listed pair from the
+// set-up positions, stored per pair in the sliced-ELL layout.
+//
+// Per RK4 stage (body.h:110-123, the action list fused):
+//   k_crR   corotational_anisotropy_tensor (corotational.h:32-84): the rotation R_i
+//           from the angle of sum_j (x_j - x_i)(X_j - X_i)^T m_j W_ij
+//   k_crA   derive_displacement_corotational (derivatives.h:202-258), then per particle
+//           material_compute_stress_cauchy_green (material.h:102-130) and
+//           contmech_cauchy_to_nominal (cont_mech.h:154-169)
+//   k_crB   derive_stress_corotational (derivatives.h:521-588) with the contact force,
+//           correctors_mghn_artificial_viscosity (correctors.h:83-137) added pair by
+//           pair onto that velocity rate as the reference does, contmech_advection,
+//           and the RK4 update (rk4.h:52-108)
+// FP64 only; the strict namespace keeps the reference's operation order without FMA
+// contraction (atan2, sin and cos are CUDA's, within an ulp or two of the C library's).
+#include "mf_common.cuh"
+#include "mf_kernels.h"
+
+using namespace mfk;
+using mfk_host::BodyParams;
+using mfk_host::TLArgs;
+
+namespace MF_NS {
+namespace {
+
+enum : uint32_t {
+	A_ART_VISC = 1u << 6,
+	A_ADVECTION = 1u << 11,
+	A_C2N = 1u << 14,
+	A_CR_ANISO = 1u << 28,
+	A_CR_DISP = 1u << 29,
+	A_CR_CAUCHY_GREEN = 1u << 30,
+	A_CR_STRESS = 1u << 31,
+};
+
+inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+__device__ __forceinline__ uint32_t sell_base(const TLArgs& a, uint32_t i) { return a.sl_off[i >> 5] + (i & 31u); }
+
+// precomp_sph: W and grad W per listed pair, with the h of particle i
+__global__ void k_sph(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                      const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ h, double* w,
+                      double* wx, double* wy) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	double xi = x[i], yi = y[i], hi = h[i];
+	for (uint32_t q = off[i]; q < off[i + 1]; q++) {
+		uint32_t j = nbr[q];
+		KR64 k = cubic_spline(xi - x[j], yi - y[j], hi);
+		w[q] = k.w;
+		wx[q] = k.w_x;
+		wy[q] = k.w_y;
+	}
+}
+
+// the kernel values into the sliced-ELL layout of the gradients
+__global__ void k_sell_w(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ sl_off,
+                         const double* __restrict__ w, double* sW) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t base = sl_off[i >> 5] + (i & 31u);
+	for (uint32_t k = 0; k < off[i + 1] - off[i]; k++) sW[base + 32 * k] = w[off[i] + k];
+}
+
+// rotation per row: R = [[cos, -sin], [sin, cos]] stored as Rxx, Rxy, Ryx, Ryy
+__global__ void __launch_bounds__(256) k_crR(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double* sW = (const double*)a.sW;
+	double Xi = a.X[i], Yi = a.Y[i], xi = s.x[i], yi = s.y[i];
+	double Axx = 0., Axy = 0., Ayx = 0., Ayy = 0.;
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		double w = sW[q];
+		double mj = a.m[j];
+		double xji = s.x[j] - xi, yji = s.y[j] - yi;
+		double Xji = a.X[j] - Xi, Yji = a.Y[j] - Yi;
+		Axx += xji * Xji * mj * w;
+		Axy += xji * Yji * mj * w;
+		Ayx += yji * Xji * mj * w;
+		Ayy += yji * Yji * mj * w;
+	}
+	double x = Axx + Ayy;
+	double y = Ayx - Axy;
+	double theta = atan2(y, x);
+	double* R = (double*)a.R;
+	const uint32_t n = a.n_total;
+	R[i] = cos(theta);
+	R[n + i] = -sin(theta);
+	R[2 * n + i] = sin(theta);
+	R[3 * n + i] = cos(theta);
+}
+
+// displacement gradient in the rotated frame, Cauchy-Green stress, nominal stress
+__global__ void __launch_bounds__(256) k_crA(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double2* sw = (const double2*)a.sw;
+	const double* R = (const double*)a.R;
+	const uint32_t n = a.n_total;
+	double xi = s.x[i], yi = s.y[i], Xi = a.X[i], Yi = a.Y[i];
+	// R^-1 = R^T (derivatives.h:219-222)
+	double Rixx_inv = R[i], Rixy_inv = R[2 * n + i], Riyx_inv = R[n + i], Riyy_inv = R[3 * n + i];
+	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		double2 w = sw[q];
+		double quad_weight = a.qw0[j];
+		double xji = s.x[j] - xi, yji = s.y[j] - yi;
+		double Xji = a.X[j] - Xi, Yji = a.Y[j] - Yi;
+		double uxji = Rixx_inv * xji + Rixy_inv * yji - Xji;
+		double uyji = Riyx_inv * xji + Riyy_inv * yji - Yji;
+		Hxx += uxji * w.x * quad_weight;
+		Hxy += uxji * w.y * quad_weight;
+		Hyx += uyji * w.x * quad_weight;
+		Hyy += uyji * w.y * quad_weight;
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	// Cauchy-Green: F = I + H (columns (Hxx+1, Hyx), (Hxy, Hyy+1)), E = (F + F^T)/2 - I
+	double Sxx = 0., Sxy = 0., Syy = 0.;
+	if (a.flags & A_CR_CAUCHY_GREEN) {
+		double F00 = Hxx + 1., F01 = Hyx, F10 = Hxy, F11 = Hyy + 1.;
+		double E00 = 0.5 * (F00 + F00) - 1.;
+		double E01 = 0.5 * (F01 + F10) - 0.;
+		double E11 = 0.5 * (F11 + F11) - 1.;
+		double D = pr.D, nu = pr.nu;
+		Sxx = D * (E00 + nu * E11);
+		Syy = D * (E00 * nu + E11);
+		Sxy = D * (1 - nu) * E01;
+	}
+	double Pxx = 0., Pxy = 0., Pyx = 0., Pyy = 0.;
+	if (a.flags & A_C2N) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - 0., Sxy, Syy - 0., Pxx, Pxy, Pyx, Pyy);
+	double* P = (double*)a.P;
+	P[i] = Pxx; P[n + i] = Pxy; P[2 * n + i] = Pyx; P[3 * n + i] = Pyy;
+	((double*)a.c)[i] = sqrt(pr.K / s.rho[i]);
+}
+
+// rotated pair forces, contact force, viscosity, advection and the RK4 update
+__global__ void __launch_bounds__(256) k_crB(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double2* sw = (const double2*)a.sw;
+	const double* P = (const double*)a.P;
+	const double* R = (const double*)a.R;
+	const double* cc = (const double*)a.c;
+	const uint32_t n = a.n_total;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	const double rho0 = pr.rho0;
+	double vx_t = 0., vy_t = 0.;
+	const uint32_t q0 = sell_base(a, i), c = a.cnt[i];
+	if (flags & A_CR_STRESS) {
+		double Pxxi = P[i], Pxyi = P[n + i], Pyxi = P[2 * n + i], Pyyi = P[3 * n + i];
+		double Rxxi = R[i], Rxyi = R[n + i], Ryxi = R[2 * n + i], Ryyi = R[3 * n + i];
+		double rhoi21 = 1. / (rho0 * rho0);
+		uint32_t q = q0;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			double2 w = sw[q];
+			double Pxxj = P[j], Pxyj = P[n + j], Pyxj = P[2 * n + j], Pyyj = P[3 * n + j];
+			double Rxxj = R[j], Rxyj = R[n + j], Ryxj = R[2 * n + j], Ryyj = R[3 * n + j];
+			double mj = a.m[j];
+			double rhoj21 = 1. / (rho0 * rho0);
+			double aijx = mj * ((Pxxi * rhoi21 + Pxxj * rhoj21) * w.x + (Pxyi * rhoi21 + Pxyj * rhoj21) * w.y);
+			double aijy = mj * ((Pyxi * rhoi21 + Pyxj * rhoj21) * w.x + (Pyyi * rhoi21 + Pyyj * rhoj21) * w.y);
+			double ajix = -aijx;
+			double ajiy = -aijy;
+			double aijxprime = aijx * Rxxi + aijy * Rxyi;
+			double aijyprime = aijx * Ryxi + aijy * Ryyi;
+			double ajixprime = ajix * Rxxj + ajiy * Rxyj;
+			double ajiyprime = ajix * Ryxj + ajiy * Ryyj;
+			vx_t += 0.5 * (aijxprime - ajixprime);
+			vy_t += 0.5 * (aijyprime - ajiyprime);
+		}
+		vx_t += a.fcx[i] / a.m[i];
+		vy_t += a.fcy[i] / a.m[i];
+	}
+	double xi = s.x[i], yi = s.y[i], vxi = s.vx[i], vyi = s.vy[i];
+	if (flags & A_ART_VISC) {
+		double hi = a.h[i], rhoi = s.rho[i], ci = cc[i];
+		double alpha = pr.alpha, beta = pr.beta, eta = pr.eta;
+		uint32_t q = q0;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			double vijx = vxi - s.vx[j], vijy = vyi - s.vy[j];
+			double xij = xi - s.x[j], yij = yi - s.y[j];
+			double vijposij = vijx * xij + vijy * yij;
+			if (vijposij < 0.) {
+				double2 w = sw[q];
+				double mj = a.m[j];
+				double cij = 0.5 * (ci + cc[j]);
+				double hij = 0.5 * (hi + a.h[j]);
+				double rhoij = 0.5 * (rhoi + s.rho[j]);
+				double r2ij = xij * xij + yij * yij;
+				double muij = (hij * vijposij) / (r2ij + eta * eta * hij * hij);
+				double piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;
+				vx_t += -mj * piij * w.x;
+				vy_t += -mj * piij * w.y;
+			}
+		}
+	}
+	double d[8];
+	d[0] = (flags & A_ADVECTION) ? vxi : 0.;
+	d[1] = (flags & A_ADVECTION) ? vyi : 0.;
+	d[2] = vx_t;
+	d[3] = vy_t;
+	d[4] = d[5] = d[6] = d[7] = 0.;  // no density or stress rate in this pipeline
+	double* bp[8] = {a.base.x, a.base.y, a.base.vx, a.base.vy, a.base.rho, a.base.Sxx, a.base.Sxy, a.base.Syy};
+	double* ap[8] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy, a.acc.rho, a.acc.Sxx, a.acc.Sxy, a.acc.Syy};
+	double* np[8] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy, a.nxt.rho, a.nxt.Sxx, a.nxt.Sxy, a.nxt.Syy};
+	uint32_t stg = a.stage;
+	double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q2 = 0; q2 < 8; q2++) {
+			ap[q2][i] = (stg == 0) ? d[q2] : ap[q2][i] + 2 * d[q2];
+			np[q2][i] = bp[q2][i] + d[q2] * dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+#pragma unroll
+		for (int q2 = 0; q2 < 8; q2++) {
+			double v = bp[q2][i] + w6 * (ap[q2][i] + d[q2]);
+			bp[q2][i] = v;
+			np[q2][i] = v;
+		}
+		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i])))
+			raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+}
+
+}  // namespace
+
+cudaError_t cr_sph(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y,
+                   const double* h, double* w, double* wx, double* wy, cudaStream_t s) {
+	k_sph<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, x, y, h, w, wx, wy);
+	return cudaGetLastError();
+}
+
+cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, const double* w, double* sW,
+                      cudaStream_t s) {
+	k_sell_w<<<grid1(n, 128), 128, 0, s>>>(n, off, sl_off, w, sW);
+	return cudaGetLastError();
+}
+
+// part 0: rotation, 1: pass A, 2: pass B
+cudaError_t cr_stage(const TLArgs& a, int part, cudaStream_t s) {
+	unsigned bs = a.block ? a.block : 128;
+	switch (part) {
+	case 0: k_crR<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	case 1: k_crA<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	case 2: k_crB<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS

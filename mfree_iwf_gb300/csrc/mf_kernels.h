@@ -112,6 +112,8 @@ struct TLArgs {
 	const void* sw;                      // corrected gradient per pair: double2 (FP64 forms) / float2 times m_j (mixed)
 	const void* swA;                     // mixed: the gradient times the neighbour's quad weight (pass A)
 	void *P, *dA, *c;                    // per-stage scratch (FP64 forms)
+	const void* sW;                      // corotational: kernel value W per pair (double, sliced ELL)
+	void* R;                             // corotational: rotation per row, 4 x n doubles (Rxx, Rxy, Ryx, Ryy)
 	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
 	void* recB_out;                      // mixed: pass B writes the next stage's records here...
 	uint32_t write_recs;                 // ...and into recA when set (no separate pack then)
@@ -200,6 +202,11 @@ struct ContactArgs {
 	                         const void* sw, const void* swA, const uint32_t* t_sl, uint16_t* t_cnt, void* t_sw, \
 	                         void* t_swA, cudaStream_t s);                                                  \
 	cudaError_t tl_tile_attrs(uint32_t halo_max, uint32_t ent_max);                                          \
+	cudaError_t cr_sph(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y, \
+	                   const double* h, double* w, double* wx, double* wy, cudaStream_t s);                 \
+	cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, const double* w, double* sW, \
+	                      cudaStream_t s);                                                                   \
+	cudaError_t cr_stage(const mfk_host::TLArgs& a, int part, cudaStream_t s);                               \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
 	cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,  \
 	                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px,     \

@@ -19,7 +19,10 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 
 from .actions import (
+    RINGS_COROT_ACTIONS,
     RINGS_MONAGHAN_ACTIONS,
+    ROTATION_COROT_ACTIONS,
+    TENSILE_COROT_ACTIONS,
     RINGS_TL_ACTIONS,
     TENSILE_TL_ACTIONS,
     TENSILE_TL_WEAK_ACTIONS,
@@ -30,7 +33,7 @@ M_1_PI = 0.31830988618379067154  # the C library's M_1_PI
 IN_NAMES = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx", "Sxy", "Syy")
 OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
 
-METHOD_UL, METHOD_TL, METHOD_TL_WEAK = 1, 2, 3
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT = 1, 2, 3, 4
 BC_PULL_TL = 1
 
 
@@ -224,7 +227,7 @@ def rings(
         spacing = ro + 0.001
     dx = 2 * ro / (nbox - 1)
     pts = _ring_lattice(nbox, dx, ro, ri)
-    tl = method == METHOD_TL
+    tl = method in (METHOD_TL, METHOD_COROT)
     sc = Scenario(method=method, bodies=[], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
     if dt is None:
         dt = cfl * (hdx * dx) / sc.c0
@@ -271,7 +274,7 @@ def rings(
         sc.mghn_eps = art_stress_eps
         sc.xsph_eps = xsph_eps
     else:
-        sc.actions = list(RINGS_TL_ACTIONS)
+        sc.actions = list(RINGS_TL_ACTIONS if method == METHOD_TL else RINGS_COROT_ACTIONS)
         sc.alpha, sc.beta, sc.eta = alpha, beta, eta
         sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
@@ -292,6 +295,32 @@ def rings_tl_contact(nbox: int) -> Scenario:
     """The reference's rings_tl_contact(nbox), rings.cpp:338-429."""
     return rings(nbox, method=METHOD_TL, two_bodies=True, dt=1e-7, alpha=3.0, beta=3.0, eta=0.1,
                  name=f"rings_tl_contact({nbox})")
+
+
+def rings_corot_contact(nbox: int) -> Scenario:
+    """The reference's rings_corot_contact(nbox), rings.cpp:245-336."""
+    return rings(nbox, method=METHOD_COROT, two_bodies=True, dt=1e-7, alpha=1.0, beta=1.0, eta=0.1,
+                 name=f"rings_corot_contact({nbox})")
+
+
+def rotation_corot(nbox: int, *, ro: float = 1.0, rho0: float = 1.0, E: float = 1e7, nu: float = 0.4,
+                   hdx: float = 1.3, omega_r: float = 50.0, dt: float = 2.5e-6) -> Scenario:
+    """A disc spinning as a rigid body (v = omega x r, |v| = omega_r at r = ro), corotational
+    SPH without artificial viscosity: the reference's rotation_corot(nbox),
+    rotation.cpp:78-140 (lattice px = -ro + i*dx, disc dist < ro)."""
+    dx = 2 * ro / (nbox - 1)
+    px, py = _ring_lattice_np(nbox, dx, ro, 0.0)
+    a = _body_from_lists(px, py, px, py)
+    a["rho"][:] = rho0
+    a["h"][:] = hdx * dx
+    a["m"][:] = dx * dx * rho0
+    a["quad_weight"][:] = a["m"] / a["rho"]
+    a["vx"][:] = -a["y"] / ro * omega_r
+    a["vy"][:] = +a["x"] / ro * omega_r
+    sc = Scenario(method=METHOD_COROT, bodies=[Body(a)], actions=list(ROTATION_COROT_ACTIONS), dt=dt, nu=nu, E=E,
+                  rho0=rho0, alpha=1.0, beta=1.0, eta=0.1, name=f"rotation_corot({nbox})")
+    sc.nbh_h = hdx * dx
+    return sc
 
 
 def workload_nbh_eps(dx: float) -> float:
@@ -366,8 +395,8 @@ def tensile_plate(
     sc.dt = dt if dt is not None else cfl * (hdx * dx) / sc.c0
     sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
-    if method == METHOD_TL:
-        sc.actions = list(TENSILE_TL_ACTIONS)
+    if method in (METHOD_TL, METHOD_COROT):
+        sc.actions = list(TENSILE_TL_ACTIONS if method == METHOD_TL else TENSILE_COROT_ACTIONS)
         sc.alpha, sc.beta, sc.eta = alpha, beta, eta
     else:
         sc.actions = list(TENSILE_TL_WEAK_ACTIONS)
@@ -384,6 +413,11 @@ def tensile_plate(
 def tensile_tl(nbox: int) -> Scenario:
     """The reference's tensile_tl(nbox), tensile.cpp:213-289."""
     return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_TL, hdx=1.0, dt=1e-6, name=f"tensile_tl({nbox})")
+
+
+def tensile_corot(nbox: int) -> Scenario:
+    """The reference's tensile_corot(nbox), tensile.cpp:137-211."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_COROT, hdx=1.0, dt=1e-6, name=f"tensile_corot({nbox})")
 
 
 def tensile_tl_weak(nbox: int) -> Scenario:

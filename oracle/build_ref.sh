@@ -16,7 +16,7 @@ pids=""
 for f in kernel particle kd_tree element simulation_data simulation_time gauss_integration; do
   g++ $FLAGS -c "$SRC/$f.cpp" -o "$OUT/$f.o" & pids="$pids $!"
 done
-for f in rings tensile; do
+for f in rings tensile rotation; do
   g++ $FLAGS -c "$SRC/benchmarks/$f.cpp" -o "$OUT/$f.o" & pids="$pids $!"
 done
 g++ $FLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" & pids="$pids $!"

@@ -20,7 +20,7 @@
 
 namespace mfcase {
 
-enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3 };
+enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3, COROT = 4 };
 
 // Action identifiers; the numbering is the C ABI's mf_action (include/mfree_gb300.h).
 enum Action : uint32_t {
@@ -51,7 +51,11 @@ enum Action : uint32_t {
 	CONTMECH_CAUCHY_TO_NOMINAL_GP = 25,
 	DERIVE_STRESS_WEAK_TL = 26,
 	CONTMECH_MOMENTUM_TL_WEAK = 27,
-	ACTION_MAX = 28
+	COROTATIONAL_ANISOTROPY_TENSOR = 28,
+	DERIVE_DISPLACEMENT_COROTATIONAL = 29,
+	MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN = 30,
+	DERIVE_STRESS_COROTATIONAL = 31,
+	ACTION_MAX = 32
 };
 
 // Boundary-condition kinds.  PULL_TL is the position-prescribed pull of

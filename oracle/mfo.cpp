@@ -44,7 +44,8 @@ struct PSet {
 	std::vector<double> x_t, y_t, rho_t, vx_t, vy_t, Sxx_t, Sxy_t, Syy_t;
 	std::vector<double> fcx, fcy;
 	std::vector<double> Sxx_x, Sxy_y, Sxy_x, Syy_y;  // particle_ul
-	std::vector<double> Rxx, Rxy, Ryy;               // particle_monaghan
+	std::vector<double> Rxx, Rxy, Ryy;               // particle_monaghan (particle_corotational: rotation R)
+	std::vector<double> Ryx;                         // particle_corotational
 	std::vector<double> Hxx, Hxy, Hyx, Hyy, Fdxx, Fdxy, Fdyx, Fdyy;  // particle_tl
 	std::vector<double> Pxx, Pxy, Pyx, Pyy, Pxx_x, Pxy_x, Pyx_y, Pyy_y;
 	std::vector<unsigned> num_nbh, nbh;  // nbh[slot*MAX_NBH + k]
@@ -55,7 +56,7 @@ struct PSet {
 		for (auto* v : {&idx, &hash, &num_nbh}) v->assign(n, 0u);
 		for (auto* v : {&x, &y, &X, &Y, &m, &rho, &h, &qw, &p, &vx, &vy, &Sxx, &Sxy, &Syy, &vx_x, &vx_y, &vy_x, &vy_y,
 		                &x_t, &y_t, &rho_t, &vx_t, &vy_t, &Sxx_t, &Sxy_t, &Syy_t, &fcx, &fcy, &Sxx_x, &Sxy_y, &Sxy_x,
-		                &Syy_y, &Rxx, &Rxy, &Ryy, &Hxx, &Hxy, &Hyx, &Hyy, &Fdxx, &Fdxy, &Fdyx, &Fdyy, &Pxx, &Pxy, &Pyx,
+		                &Syy_y, &Rxx, &Rxy, &Ryy, &Ryx, &Hxx, &Hxy, &Hyx, &Hyy, &Fdxx, &Fdxy, &Fdyx, &Fdyy, &Pxx, &Pxy, &Pyx,
 		                &Pyy, &Pxx_x, &Pxy_x, &Pyx_y, &Pyy_y})
 			v->assign(n, 0.);
 		nbh.assign((size_t)n * MAX_NBH, 0u);
@@ -89,7 +90,7 @@ void copy_into(const PSet& a, unsigned s, PSet& b, unsigned d) {
 		b.w[dof + k] = a.w[so + k]; b.w_x[dof + k] = a.w_x[so + k]; b.w_y[dof + k] = a.w_y[so + k];
 	}
 	b.Pxx[d] = a.Pxx[s]; b.Pxy[d] = a.Pxy[s]; b.Pyx[d] = a.Pyx[s]; b.Pyy[d] = a.Pyy[s];
-	b.Rxx[d] = a.Rxx[s]; b.Rxy[d] = a.Rxy[s]; b.Ryy[d] = a.Ryy[s];
+	b.Rxx[d] = a.Rxx[s]; b.Rxy[d] = a.Rxy[s]; b.Ryy[d] = a.Ryy[s]; b.Ryx[d] = a.Ryx[s];
 }
 
 struct Fail {
@@ -743,6 +744,103 @@ void a_momentum_tl_weak(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
 	}
 }
 
+// --- particle_corotational (corotational.h, derivatives.h:202-258,521-588, material.h:103-130)
+// corotational_anisotropy_tensor, corotational.h:31-82: the rotation of the neighbourhood
+void a_corot_aniso(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
+	for (unsigned i = 0; i < P.n; i++) {
+		double Xi = P.X[i], Yi = P.Y[i], xi = P.x[i], yi = P.y[i];
+		double Axx = 0., Axy = 0., Ayx = 0., Ayy = 0.;
+		for (unsigned j = 0; j < P.num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = P.nbh[o];
+			double w = P.w[o];
+			double mj = P.m[jdx];
+			double xji = P.x[jdx] - xi, yji = P.y[jdx] - yi;
+			double Xji = P.X[jdx] - Xi, Yji = P.Y[jdx] - Yi;
+			Axx += xji * Xji * mj * w;
+			Axy += xji * Yji * mj * w;
+			Ayx += yji * Xji * mj * w;
+			Ayy += yji * Yji * mj * w;
+		}
+		double x = Axx + Ayy;
+		double y = Ayx - Axy;
+		double theta = atan2(y, x);
+		P.Rxx[i] = cos(theta);
+		P.Rxy[i] = -sin(theta);
+		P.Ryx[i] = sin(theta);
+		P.Ryy[i] = cos(theta);
+	}
+}
+// derive_displacement_corotational, derivatives.h:202-258: displacement in the rotated frame
+void a_disp_corot(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
+	for (unsigned i = 0; i < P.n; i++) {
+		double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
+		double xi = P.x[i], yi = P.y[i], Xi = P.X[i], Yi = P.Y[i];
+		double Rixx_inv = P.Rxx[i], Rixy_inv = P.Ryx[i], Riyx_inv = P.Rxy[i], Riyy_inv = P.Ryy[i];
+		for (unsigned j = 0; j < P.num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = P.nbh[o];
+			double quad_weight = P.qw[jdx];
+			double xji = P.x[jdx] - xi, yji = P.y[jdx] - yi;
+			double Xji = P.X[jdx] - Xi, Yji = P.Y[jdx] - Yi;
+			double uxji = Rixx_inv * xji + Rixy_inv * yji - Xji;
+			double uyji = Riyx_inv * xji + Riyy_inv * yji - Yji;
+			Hxx += uxji * P.w_x[o] * quad_weight;
+			Hxy += uxji * P.w_y[o] * quad_weight;
+			Hyx += uyji * P.w_x[o] * quad_weight;
+			Hyy += uyji * P.w_y[o] * quad_weight;
+		}
+		P.Hxx[i] = Hxx; P.Hxy[i] = Hxy; P.Hyx[i] = Hyx; P.Hyy[i] = Hyy;
+	}
+}
+// do_material_compute_stress_cauchy_green, material.h:103-114 (small-strain Cauchy-Green)
+void a_cauchy_green(Ctx& c, PSet& P, const std::vector<unsigned>&, PSet*) {
+	double E = c.c->E, nu = c.c->nu;
+	double D = E / (1 - nu * nu);
+	for (unsigned i = 0; i < P.n; i++) {
+		glm::dmat2x2 F(P.Hxx[i] + 1., P.Hyx[i], P.Hxy[i], P.Hyy[i] + 1.);
+		glm::dmat2x2 Ecg = 0.5 * (F + glm::transpose(F)) - glm::dmat2x2(1.);
+		P.Sxx[i] = D * (Ecg[0][0] + nu * Ecg[1][1]);
+		P.Syy[i] = D * (Ecg[0][0] * nu + Ecg[1][1]);
+		P.Sxy[i] = D * (1 - nu) * Ecg[0][1];
+	}
+}
+// derive_stress_corotational, derivatives.h:521-588: pair forces rotated back, then fc/m
+void a_stress_corot(Ctx& c, PSet& P, const std::vector<unsigned>&, PSet*) {
+	double rho0 = c.k.rho0;
+	for (unsigned i = 0; i < P.n; i++) {
+		double Pxxi = P.Pxx[i], Pxyi = P.Pxy[i], Pyxi = P.Pyx[i], Pyyi = P.Pyy[i];
+		double Rxxi = P.Rxx[i], Rxyi = P.Rxy[i], Ryxi = P.Ryx[i], Ryyi = P.Ryy[i];
+		double rhoi21 = 1. / (rho0 * rho0);
+		double vx_t = 0., vy_t = 0.;
+		for (unsigned j = 0; j < P.num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = P.nbh[o];
+			double Pxxj = P.Pxx[jdx], Pxyj = P.Pxy[jdx], Pyxj = P.Pyx[jdx], Pyyj = P.Pyy[jdx];
+			double Rxxj = P.Rxx[jdx], Rxyj = P.Rxy[jdx], Ryxj = P.Ryx[jdx], Ryyj = P.Ryy[jdx];
+			double mj = P.m[jdx];
+			double rhoj21 = 1. / (rho0 * rho0);
+			double wx = P.w_x[o], wy = P.w_y[o];
+			double aijx = mj * ((Pxxi * rhoi21 + Pxxj * rhoj21) * wx + (Pxyi * rhoi21 + Pxyj * rhoj21) * wy);
+			double aijy = mj * ((Pyxi * rhoi21 + Pyxj * rhoj21) * wx + (Pyyi * rhoi21 + Pyyj * rhoj21) * wy);
+			double ajix = -aijx;
+			double ajiy = -aijy;
+			double aijxprime = aijx * Rxxi + aijy * Rxyi;
+			double aijyprime = aijx * Ryxi + aijy * Ryyi;
+			double ajixprime = ajix * Rxxj + ajiy * Rxyj;
+			double ajiyprime = ajix * Ryxj + ajiy * Ryyj;
+			vx_t += 0.5 * (aijxprime - ajixprime);
+			vy_t += 0.5 * (aijyprime - ajiyprime);
+		}
+		P.vx_t[i] = vx_t;
+		P.vy_t[i] = vy_t;
+	}
+	for (unsigned i = 0; i < P.n; i++) {
+		P.vx_t[i] += P.fcx[i] / P.m[i];
+		P.vy_t[i] += P.fcy[i] / P.m[i];
+	}
+}
+
 ActFn action_fn(uint32_t a) {
 	switch (a) {
 	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return a_riemann;
@@ -772,6 +870,10 @@ ActFn action_fn(uint32_t a) {
 	case CONTMECH_CAUCHY_TO_NOMINAL_GP: return a_c2n_gp;
 	case DERIVE_STRESS_WEAK_TL: return a_stress_weak_tl;
 	case CONTMECH_MOMENTUM_TL_WEAK: return a_momentum_tl_weak;
+	case COROTATIONAL_ANISOTROPY_TENSOR: return a_corot_aniso;
+	case DERIVE_DISPLACEMENT_COROTATIONAL: return a_disp_corot;
+	case MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN: return a_cauchy_green;
+	case DERIVE_STRESS_COROTATIONAL: return a_stress_corot;
 	}
 	throw Fail{"unknown action id"};
 }
@@ -909,7 +1011,7 @@ struct Sim {
 			if (!recorded && s == 0) record_nbh(P, perm, b);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, nullptr);
 			std::sort(perm.begin(), perm.end(), [&P](unsigned a, unsigned bb) { return P.idx[a] < P.idx[bb]; });
-		} else if (c.method == TL) {
+		} else if (c.method == TL || c.method == COROT) {
 			carry_out_bc(B, P, ctx.time);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, nullptr);
 		} else {
@@ -1068,6 +1170,11 @@ struct Sim {
 				// rings.cpp:404-408 / tensile.cpp:268-269
 				find_neighbors(B.P, B.P, c.nbh_h, c.nbh_eps);
 				precomp_randles_libersky(B.P);
+				record_nbh(B.P, ident(B.n), b);
+			} else if (c.method == COROT) {
+				// rings.cpp:311-315 / tensile.cpp:197-198: plain SPH weights on the set-up lists
+				find_neighbors(B.P, B.P, c.nbh_h, c.nbh_eps);
+				precomp_sph(B.P, ident(B.n));
 				record_nbh(B.P, ident(B.n), b);
 			} else if (c.method == TL_WEAK) {
 				setup_weak(B, in);

@@ -23,6 +23,7 @@
 #include "particle.h"
 #include "benchmarks/rings.h"
 #include "benchmarks/tensile.h"
+#include "benchmarks/rotation.h"
 
 #include "vtk_writer.h"
 
@@ -63,6 +64,7 @@ void record_fixed_nbh(T** p, unsigned n, int b) {
 typedef void (*UlAct)(body<particle_monaghan>&);
 typedef void (*TlAct)(body<particle_tl>&);
 typedef void (*WkAct)(body<particle_tl_weak>&);
+typedef void (*CrAct)(body<particle_corotational>&);
 
 UlAct ul_action(uint32_t a) {
 	typedef particle_monaghan T;
@@ -99,6 +101,19 @@ TlAct tl_action(uint32_t a) {
 	case CONTMECH_MOMENTUM_TL: return &contmech_momentum_tl<T>;
 	case DERIVE_VELOCITY_TL: return &derive_velocity_tl<T>;
 	case CONTMECH_VELOCITY_GRADIENT_TL: return &contmech_velocity_gradient_tl<T>;
+	}
+	return nullptr;
+}
+CrAct cr_action(uint32_t a) {
+	typedef particle_corotational T;
+	switch (a) {
+	case CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY: return &correctors_mghn_artificial_viscosity<T>;
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case CONTMECH_CAUCHY_TO_NOMINAL: return &contmech_cauchy_to_nominal<T>;
+	case COROTATIONAL_ANISOTROPY_TENSOR: return &corotational_anisotropy_tensor<T>;
+	case DERIVE_DISPLACEMENT_COROTATIONAL: return &derive_displacement_corotational<T>;
+	case MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN: return &material_compute_stress_cauchy_green<T>;
+	case DERIVE_STRESS_COROTATIONAL: return &derive_stress_corotational<T>;
 	}
 	return nullptr;
 }
@@ -307,6 +322,26 @@ int run_case(const Case& c, const char* out) {
 			}
 		}
 		run_loop(w, c, bodies);
+	} else if (c.method == COROT) {
+		typedef particle_corotational T;
+		std::vector<body<T>> bodies;
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			const BodyIn& in = c.bodies[b];
+			T** p = make_particles<T>(in);
+			find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
+			precomp_sph<T>(p, in.n);
+			record_fixed_nbh(p, in.n, (int)b);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot)));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
+			for (uint32_t a : c.actions) {
+				CrAct f = cr_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for the corotational method\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+		}
+		run_loop(w, c, bodies);
 	} else if (c.method == TL_WEAK) {
 		typedef particle_tl_weak T;
 		std::vector<body<T>> bodies;
@@ -457,6 +492,38 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 		c.bodies.push_back(in);
 		record_fixed_nbh(bodies[0].get_particles(), bodies[0].get_num_part(), 0);
 		c.nbodies = 1;
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "rings_corot_contact" || name == "tensile_corot" || name == "rotation_corot") {
+		const bool rings = name == "rings_corot_contact", disc = name == "rotation_corot";
+		std::vector<body<particle_corotational>> bodies =
+		    rings ? rings_corot_contact(nbox) : (disc ? rotation_corot(nbox) : tensile_corot(nbox));
+		c.method = COROT;
+		c.contact = rings ? 1 : 0;
+		c.actions = {COROTATIONAL_ANISOTROPY_TENSOR, DERIVE_DISPLACEMENT_COROTATIONAL, MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN,
+		             CONTMECH_CAUCHY_TO_NOMINAL, DERIVE_STRESS_COROTATIONAL, CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
+		             CONTMECH_ADVECTION};  // rings.cpp:325-331, tensile.cpp:202-208
+		if (disc)  // rotation.cpp:132-137: no artificial viscosity
+			c.actions = {COROTATIONAL_ANISOTROPY_TENSOR, DERIVE_DISPLACEMENT_COROTATIONAL,
+			             MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN, CONTMECH_CAUCHY_TO_NOMINAL, DERIVE_STRESS_COROTATIONAL,
+			             CONTMECH_ADVECTION};
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			BodyIn in = capture(bodies[b]);
+			if (!rings && !disc) {
+				BC l, r;  // tensile.cpp:170-176,188-190
+				l.kind = r.kind = BC_PULL_TL;
+				l.v = -10.; r.v = 10.;
+				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+				in.bcs = {l, r};
+			}
+			c.bodies.push_back(in);
+			record_fixed_nbh(bodies[b].get_particles(), bodies[b].get_num_part(), (int)b);
+		}
+		c.nbodies = (uint32_t)bodies.size();
 		write_case(case_out, c);
 		Writer w(out);
 		write_header(w, c);

@@ -8,7 +8,8 @@ reference's body/action machinery, and writes the final state of the VTK cases w
 the reference's own vtk_writer_write (NAME.vtk).  Needs the reference sources (not on
 GPU machines).
 
-Usage: python tests/golden/make_golden.py [--vtk-only]
+Usage: python tests/golden/make_golden.py [--vtk-only] [NAME ...]
+(with names: only those reference cases)
 """
 import os
 import shutil
@@ -31,6 +32,9 @@ REFERENCE_CASES = [
     ("rings_tl_contact", 20, 375),
     ("tensile_tl", 11, 25),
     ("tensile_tl_weak", 7, 6),
+    ("rings_corot_contact", 20, 480),
+    ("tensile_corot", 11, 25),
+    ("rotation_corot", 15, 400),
 ]
 
 
@@ -55,11 +59,16 @@ def main():
     if "--vtk-only" in sys.argv:
         write_vtk_goldens(ref)
         return
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]
     for name, nbox, steps in REFERENCE_CASES:
+        if only and name not in only:
+            continue
         case = os.path.join(HERE, f"{name}.case")
         out = os.path.join(HERE, f"{name}.ref.out")
         subprocess.run([ref, "scenario", name, str(nbox), str(steps), case, out], check=True)
         print("wrote", case, out)
+    if only:
+        return
     # workload constants (rho 1200, +-10 m/s, h = 1.3 dx, CFL dt) at dx = 4 mm
     sc = S.c1_rings(dx=4e-3, nbh_eps=1e-6)  # the reference predicate has a fixed 1e-6
     case = os.path.join(HERE, "c1_rings_dx4mm.case")

@@ -6,7 +6,10 @@ Tolerances (relative L2 per field over all particles):
     updated-Lagrangian path differs from the reference only in summation order within
     cells and in the last bit of atan2/sin/cos; the total-Lagrangian path sums in the
     reference's order and is expected to agree to the last bit.
-  * neighbour sets: bit-exact as sets (UL) / as ordered lists (TL).
+  * corotational: the TL lists and the reference's order, but the rotation angle goes
+    through atan2/sin/cos, which may differ in the last bit from the C library's, so
+    the same 1e-9 bound instead of bit equality.
+  * neighbour sets: bit-exact as sets (UL) / as ordered lists (TL, corotational).
 """
 import os
 
@@ -54,9 +57,10 @@ def golden(name):
 
 UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm"]
 TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak"]
+COROT_CASES = ["rings_corot_contact", "tensile_corot", "rotation_corot"]
 
 
-@pytest.mark.parametrize("name", UL_CASES + TL_CASES)
+@pytest.mark.parametrize("name", UL_CASES + TL_CASES + COROT_CASES)
 def test_fp64_strict_matches_reference(name, lib):
     sc, ref = golden(name)
     steps = ref.dumps[-1]["step"]
@@ -95,7 +99,7 @@ def test_ul_neighbor_sets_bitexact(name, lib):
     sim.close()
 
 
-@pytest.mark.parametrize("name", TL_CASES)
+@pytest.mark.parametrize("name", TL_CASES + COROT_CASES)
 def test_tl_neighbor_lists_bitexact(name, lib):
     import mfree_iwf_gb300 as M
     sc, ref = golden(name)
@@ -107,7 +111,7 @@ def test_tl_neighbor_lists_bitexact(name, lib):
     sim.close()
 
 
-@pytest.mark.parametrize("name", UL_CASES + TL_CASES)
+@pytest.mark.parametrize("name", UL_CASES + TL_CASES + COROT_CASES)
 def test_fp64_fast_close_to_reference(name, lib):
     sc, ref = golden(name)
     steps = ref.dumps[-1]["step"]

@@ -14,6 +14,9 @@ BUILDERS = {
     "rings_tl_contact": lambda: S.rings_tl_contact(20),
     "tensile_tl": lambda: S.tensile_tl(11),
     "tensile_tl_weak": lambda: S.tensile_tl_weak(7),
+    "rings_corot_contact": lambda: S.rings_corot_contact(20),
+    "tensile_corot": lambda: S.tensile_corot(11),
+    "rotation_corot": lambda: S.rotation_corot(15),
 }
 
 
