@@ -58,7 +58,10 @@ enum action : int32_t {
 	corotational_anisotropy_tensor = MF_COROTATIONAL_ANISOTROPY_TENSOR,
 	derive_displacement_corotational = MF_DERIVE_DISPLACEMENT_COROTATIONAL,
 	material_compute_stress_cauchy_green = MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN,
-	derive_stress_corotational = MF_DERIVE_STRESS_COROTATIONAL
+	derive_stress_corotational = MF_DERIVE_STRESS_COROTATIONAL,
+	godunov_continuity = MF_GODUNOV_CONTINUITY,
+	godunov_momentum = MF_GODUNOV_MOMENTUM,
+	potential_comp_elastic_potential = MF_POTENTIAL_COMP_ELASTIC_POTENTIAL
 };
 
 class error : public std::runtime_error {

@@ -22,7 +22,7 @@ from .actions import *  # noqa: F401,F403  (action ids)
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmfree_gb300.so")
 
-METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT = 1, 2, 3, 4
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
 PREC_FP64_STRICT, PREC_FP64, PREC_MIXED = 0, 1, 2
 PRECISIONS = {"fp64_strict": PREC_FP64_STRICT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
 BC_PULL = 1

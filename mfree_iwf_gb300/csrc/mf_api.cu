@@ -278,28 +278,48 @@ inline uint32_t abit(int a) { return 1u << a; }
 
 mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
+mf_status validate_potential(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status tl_setup(mf_ctx* c);
 mf_status weak_setup(mf_ctx* c);
 mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status contact_setup(mf_ctx* c);
 
-// UL pipeline: any subsequence of the reference's rings_monaghan list
-// (rings.cpp:86-96), whose ids ascend, with the data dependencies present.
+// UL pipeline: a subsequence, in this order, of the union of the reference's
+// rings_monaghan list (rings.cpp:86-96) and rings_godunov list (rings.cpp:154-160),
+// with the data dependencies present.  The Godunov actions take the flag bits
+// FLAG_GODUNOV_* and run in the FP64 forms.
 mf_status validate_ul(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS, MF_MATERIAL_EOS, MF_CORRECTORS_MGHN_ARTIFICIAL_STRESS,
+	                            MF_DERIVE_STRESS_MONAGHAN, MF_DERIVE_VELOCITY, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
+	                            MF_CORRECTORS_XSPH, MF_MATERIAL_STRESS_RATE_JAUMANN, MF_CONTMECH_CONTINUITY,
+	                            MF_GODUNOV_CONTINUITY, MF_GODUNOV_MOMENTUM, MF_CONTMECH_MOMENTUM_UL, MF_CONTMECH_ADVECTION};
 	flags = 0;
-	int prev = 0;
+	size_t pos = 0;
 	for (int32_t a : acts) {
-		if (a < MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS || a > MF_CONTMECH_ADVECTION)
-			return fail(c, MF_ERR_PIPELINE, "action %d is not an updated-Lagrangian action", a);
-		if (a <= prev) return fail(c, MF_ERR_PIPELINE, "action %d out of the order of the fused UL pipeline", a);
-		prev = a;
-		flags |= abit(a);
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not an updated-Lagrangian action or out of the fused UL order", a);
+		pos++;
+		flags |= a == MF_GODUNOV_CONTINUITY ? FLAG_GODUNOV_CONTINUITY
+		         : a == MF_GODUNOV_MOMENTUM ? FLAG_GODUNOV_MOMENTUM
+		                                    : abit(a);
 	}
 	if ((flags & abit(MF_CONTMECH_MOMENTUM_UL)) && !(flags & abit(MF_DERIVE_STRESS_MONAGHAN)))
 		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_ul needs derive_stress_monaghan before it");
 	if ((flags & (abit(MF_MATERIAL_STRESS_RATE_JAUMANN) | abit(MF_CONTMECH_CONTINUITY))) &&
 	    !(flags & abit(MF_DERIVE_VELOCITY)))
 		return fail(c, MF_ERR_PIPELINE, "Jaumann rate / continuity need derive_velocity before them");
+	const uint32_t god = FLAG_GODUNOV_CONTINUITY | FLAG_GODUNOV_MOMENTUM;
+	if (flags & god) {
+		if (c->cfg.precision == MF_PREC_MIXED)
+			return fail(c, MF_ERR_PIPELINE, "the Godunov actions run in the FP64 forms");
+		if ((flags & FLAG_GODUNOV_CONTINUITY) && (flags & abit(MF_CONTMECH_CONTINUITY)))
+			return fail(c, MF_ERR_PIPELINE, "godunov_continuity and contmech_continuity both set the density rate");
+		if ((flags & FLAG_GODUNOV_MOMENTUM) && (flags & abit(MF_CONTMECH_MOMENTUM_UL)))
+			return fail(c, MF_ERR_PIPELINE, "godunov_momentum and contmech_momentum_ul both add the stress forces");
+		if (flags & abit(MF_CORRECTORS_MGHN_ARTIFICIAL_STRESS))
+			return fail(c, MF_ERR_PIPELINE, "the Godunov actions do not combine with the artificial stress");
+	}
 	return MF_OK;
 }
 
@@ -440,6 +460,8 @@ mf_status finalize(mf_ctx* c) {
 		st = validate_tl(c, acts, c->flags);
 	} else if (c->cfg.method == MF_METHOD_COROT) {
 		st = validate_corot(c, acts, c->flags);
+	} else if (c->cfg.method == MF_METHOD_POTENTIAL) {
+		st = validate_potential(c, acts, c->flags);
 	} else {
 		st = validate_weak(c, acts, c->flags);
 	}
@@ -518,7 +540,7 @@ mf_status finalize(mf_ctx* c) {
 		c->sort_bits = bits;
 		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
 		CK(c->sort_tmp.alloc(tmp));
-	} else if (c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT) {
+	} else if (c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL) {
 		mf_status s2 = tl_setup(c);
 		if (s2 != MF_OK) return s2;
 	} else {
@@ -742,7 +764,7 @@ mf_status tl_step_all(mf_ctx* c) {
 	// boundary conditions, which change the stage state after pass B
 	const bool fused = c->mixed && c->n_bc == 0;
 	void* rb[2] = {c->recB.p, c->recB2.p};
-	const bool corot = c->cfg.method == MF_METHOD_COROT;
+	const bool corot = c->cfg.method == MF_METHOD_COROT, potential = c->cfg.method == MF_METHOD_POTENTIAL;
 	for (uint32_t st = 0; st < 4; st++) {
 		a.stage = st;
 		a.st = (st % 2 == 0) ? S0 : S1;
@@ -755,18 +777,18 @@ mf_status tl_step_all(mf_ctx* c) {
 		if ((e = tl_launch(c, a, 0)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
 		if (pack && (e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
 		int slot;
-		if (corot) {
+		if (corot || potential) {
 			auto cr = [&](int part) {
 				return c->strict ? mf_strict::cr_stage(a, part, c->stream) : mf_fast::cr_stage(a, part, c->stream);
 			};
-			if ((e = cr(0)) != cudaSuccess) return cuda_fail(c, e, "corotational rotation");
+			if (corot && (e = cr(0)) != cudaSuccess) return cuda_fail(c, e, "corotational rotation");
 			timing_begin(c, 1, slot);
-			if ((e = cr(1)) != cudaSuccess) return cuda_fail(c, e, "corotational pass A");
+			if ((e = cr(1)) != cudaSuccess) return cuda_fail(c, e, "pass A");
 			timing_end(c, slot, c->n_total);
 			timing_begin(c, 2, slot);
-			if ((e = cr(2)) != cudaSuccess) return cuda_fail(c, e, "corotational pass B");
+			if ((e = cr(2)) != cudaSuccess) return cuda_fail(c, e, "pass B");
 			timing_end(c, slot, c->n_total);
-			c->launches += 3 + (c->n_bc ? 1 : 0);
+			c->launches += (corot ? 3 : 2) + (c->n_bc ? 1 : 0);
 			continue;
 		}
 		timing_begin(c, 1, slot);
@@ -821,6 +843,29 @@ mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& 
 	for (int k = 0; k < 5; k++)
 		if (!(flags & abit(order[k])))
 			return fail(c, MF_ERR_PIPELINE, "the corotational pipeline needs action %d", order[k]);
+	return MF_OK;
+}
+
+// Elastic-potential pipeline (rings.cpp:512-516, tensile.cpp:354-358,
+// rotation.cpp:266-269): displacement, Green-St Venant stress, the potential forces,
+// then optionally the artificial viscosity and advection.
+mf_status validate_potential(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_DERIVE_DISPLACEMENT, MF_MATERIAL_COMPUTE_STRESS_GREEN_STVENANT,
+	                            MF_POTENTIAL_COMP_ELASTIC_POTENTIAL, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
+	                            MF_CONTMECH_ADVECTION};
+	if (c->cfg.precision == MF_PREC_MIXED)
+		return fail(c, MF_ERR_PIPELINE, "the elastic-potential method runs in the FP64 forms");
+	flags = 0;
+	size_t pos = 0;
+	for (int32_t a : acts) {
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not part of the elastic-potential pipeline or out of its order", a);
+		flags |= a == MF_POTENTIAL_COMP_ELASTIC_POTENTIAL ? FLAG_POTENTIAL : abit(a);
+		pos++;
+	}
+	if (!(flags & FLAG_POTENTIAL))
+		return fail(c, MF_ERR_PIPELINE, "the elastic-potential pipeline needs potential_comp_elastic_potential");
 	return MF_OK;
 }
 
@@ -926,7 +971,7 @@ mf_status tl_setup(mf_ctx* c) {
 	}
 	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
 	const float* rho32 = nullptr;
-	const bool corot = c->cfg.method == MF_METHOD_COROT;
+	const bool corot = c->cfg.method == MF_METHOD_COROT, potential = c->cfg.method == MF_METHOD_POTENTIAL;
 	DevBuf<double> w64;  // corotational: the kernel values of the pairs (precomp_sph)
 	cudaError_t e;
 	if (corot) {
@@ -980,6 +1025,14 @@ mf_status tl_setup(mf_ctx* c) {
 		e = c->strict ? mf_strict::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream)
 		              : mf_fast::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "corotational weights");
+	}
+	if (potential) {  // precomp_randles_libersky_symmetric: the reverse pairs' gradients
+		CK(c->sW64.alloc(2 * ent));
+		e = c->strict ? mf_strict::cr_sell_wji(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->sW64.p,
+		                                       c->stream)
+		              : mf_fast::cr_sell_wji(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->sW64.p,
+		                                     c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "reverse-pair weights");
 	}
 	CK(cudaStreamSynchronize(c->stream));
 	c->wx64.free();
@@ -1508,7 +1561,7 @@ MF_API const char* mf_last_error(const mf_ctx* c) { return c ? c->err.c_str() : 
 MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out) {
 	if (!cfg || !out) return MF_ERR_ARG;
 	*out = nullptr;
-	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_COROT) return MF_ERR_ARG;
+	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_POTENTIAL) return MF_ERR_ARG;
 	if (cfg->precision < MF_PREC_FP64_STRICT || cfg->precision > MF_PREC_MIXED) return MF_ERR_ARG;
 	int ndev = 0;
 	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MF_ERR_NO_DEVICE;
@@ -1563,7 +1616,7 @@ MF_API mf_status mf_add_action(mf_ctx* c, int32_t body, int32_t action) {
 	if (!c) return MF_ERR_ARG;
 	if (c->ready) return fail(c, MF_ERR_STATE, "actions must be added before the first step");
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
-	if (action < 1 || action > MF_DERIVE_STRESS_COROTATIONAL) return fail(c, MF_ERR_ARG, "bad action id %d", action);
+	if (action < 1 || action > MF_POTENTIAL_COMP_ELASTIC_POTENTIAL) return fail(c, MF_ERR_ARG, "bad action id %d", action);
 	c->bodies[body].actions.push_back(action);
 	return MF_OK;
 }
@@ -1643,7 +1696,8 @@ namespace {
 // The launches of one step of every body, in the driver's order (mfree_iwf.cpp:84-97):
 // the RK4 step, then the boundary refresh and contact.
 mf_status one_step(mf_ctx* c) {
-	const bool tl_lists = c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT;
+	const bool tl_lists =
+	    c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL;
 	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (tl_lists ? tl_step_all(c) : weak_step(c));
 	if (st != MF_OK) return st;
 	if (c->contact_on) st = contact_run(c);
@@ -2420,7 +2474,8 @@ MF_API mf_status mf_checkpoint_load(mf_ctx* c, const char* path) {
 		return fail(c, MF_ERR_ARG, "%s is not a checkpoint of this context's method, precision and bodies", path);
 	}
 	CK(cudaSetDevice(c->cfg.device));
-	const bool tl = c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT;
+	const bool tl = c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT ||
+	                c->cfg.method == MF_METHOD_POTENTIAL;
 	const size_t es = c->mixed ? 4 : 8;
 	std::vector<double> times(c->bodies.size());
 	std::vector<unsigned char> buf;

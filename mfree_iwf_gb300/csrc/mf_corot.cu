@@ -17,6 +17,17 @@
 //           correctors_mghn_artificial_viscosity (correctors.h:83-137) added pair by
 //           pair onto that velocity rate as the reference does, contmech_advection,
 //           and the RK4 update (rk4.h:52-108)
+//
+// Elastic-potential SPH (particle_potential; rings_potential_contact rings.cpp:431-520,
+// tensile_potential tensile.cpp:291-361, rotation_potential rotation.cpp:212-272) runs
+// on the same lists with the symmetric Randles-Libersky weights
+// (precomp_shape_functions.h:292-315: per pair also the gradient that j's list holds
+// for i, found once at set-up by k_sell_wji):
+//   k_ptA   derive_displacement (derivatives.h:101-149), Green-St Venant stress
+//           (material.h:132-161) and per particle F_e = -2 V F S (potential.h:43-48)
+//   k_crB   (potential form) f_ij = F_e,i grad W_ij, f_ji = F_e,j grad W_ji summed as
+//           0.5 (f_ji - f_ij) / m_i (potential.h:50-76), the contact force, then the
+//           artificial viscosity, advection and RK4 update as above
 // FP64 only; the strict namespace keeps the reference's operation order without FMA
 // contraction (atan2, sin and cos are CUDA's, within an ulp or two of the C library's).
 #include "mf_common.cuh"
@@ -32,6 +43,8 @@ namespace {
 enum : uint32_t {
 	A_ART_VISC = 1u << 6,
 	A_ADVECTION = 1u << 11,
+	A_DISP = 1u << 12,
+	A_GREEN = 1u << 13,
 	A_C2N = 1u << 14,
 	A_CR_ANISO = 1u << 28,
 	A_CR_DISP = 1u << 29,
@@ -66,6 +79,26 @@ __global__ void k_sell_w(uint32_t n, const uint32_t* __restrict__ off, const uin
 	if (i >= n) return;
 	uint32_t base = sl_off[i >> 5] + (i & 31u);
 	for (uint32_t k = 0; k < off[i + 1] - off[i]; k++) sW[base + 32 * k] = w[off[i] + k];
+}
+
+// the reverse pair's gradient per listed pair: entry k of row i (neighbour j) gets the
+// gradient at i's place in j's list, zero if j's list does not hold i
+__global__ void k_sell_wji(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                           const double* __restrict__ wx, const double* __restrict__ wy,
+                           const uint32_t* __restrict__ sl_off, double2* sWji) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t base = sl_off[i >> 5] + (i & 31u);
+	for (uint32_t k = 0; k < off[i + 1] - off[i]; k++) {
+		uint32_t j = nbr[off[i] + k];
+		double2 g = make_double2(0., 0.);
+		for (uint32_t q = off[j]; q < off[j + 1]; q++)
+			if (nbr[q] == i) {
+				g = make_double2(wx[q], wy[q]);
+				break;
+			}
+		sWji[base + 32 * k] = g;
+	}
 }
 
 // rotation per row: R = [[cos, -sin], [sin, cos]] stored as Rxx, Rxy, Ryx, Ryy
@@ -145,7 +178,46 @@ __global__ void __launch_bounds__(256) k_crA(TLArgs a) {
 	((double*)a.c)[i] = sqrt(pr.K / s.rho[i]);
 }
 
-// rotated pair forces, contact force, viscosity, advection and the RK4 update
+// displacement gradient, Green-St Venant stress and F_e = -2 V (I + H) S per row;
+// F_e is stored column-major (F[0][0], F[0][1], F[1][0], F[1][1]) in the P buffer
+__global__ void __launch_bounds__(256) k_ptA(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const double2* sw = (const double2*)a.sw;
+	const uint32_t n = a.n_total, flags = a.flags;
+	double uxi = s.x[i] - a.X[i], uyi = s.y[i] - a.Y[i];
+	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
+	if (flags & A_DISP) {
+		uint32_t q = sell_base(a, i), c = a.cnt[i];
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			double2 w = sw[q];
+			double qwj = a.qw0[j];
+			double uxj = s.x[j] - a.X[j], uyj = s.y[j] - a.Y[j];
+			Hxx += (uxj - uxi) * w.x * qwj;
+			Hxy += (uxj - uxi) * w.y * qwj;
+			Hyx += (uyj - uyi) * w.x * qwj;
+			Hyy += (uyj - uyi) * w.y * qwj;
+		}
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double Sxx = s.Sxx[i], Sxy = s.Sxy[i], Syy = s.Syy[i];
+	if (flags & A_GREEN) green_stvenant<double>(Hxx, Hxy, Hyx, Hyy, pr.D, pr.nu, Sxx, Sxy, Syy);
+	// -2*voli*Ji*Si: the scalar scales J, then the matrix product, k ascending
+	double sc = -2 * a.qw0[i];
+	double J00 = sc * (Hxx + 1.), J01 = sc * Hyx, J10 = sc * Hxy, J11 = sc * (Hyy + 1.);
+	double* P = (double*)a.P;
+	P[i] = J00 * Sxx + J10 * Sxy;
+	P[n + i] = J01 * Sxx + J11 * Sxy;
+	P[2 * n + i] = J00 * Sxy + J10 * Syy;
+	P[3 * n + i] = J01 * Sxy + J11 * Syy;
+	((double*)a.c)[i] = sqrt(pr.K / s.rho[i]);
+}
+
+// pair forces (rotated stresses or elastic potential), contact force, viscosity,
+// advection and the RK4 update
+template <bool POT>
 __global__ void __launch_bounds__(256) k_crB(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
@@ -160,7 +232,25 @@ __global__ void __launch_bounds__(256) k_crB(TLArgs a) {
 	const double rho0 = pr.rho0;
 	double vx_t = 0., vy_t = 0.;
 	const uint32_t q0 = sell_base(a, i), c = a.cnt[i];
-	if (flags & A_CR_STRESS) {
+	if (POT && (flags & mfk_host::FLAG_POTENTIAL)) {
+		const double2* swji = (const double2*)a.sW;
+		double F00i = P[i], F01i = P[n + i], F10i = P[2 * n + i], F11i = P[3 * n + i];
+		double mi = a.m[i];
+		uint32_t q = q0;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			double2 w = sw[q], wji = swji[q];
+			double fij0 = F00i * w.x + F10i * w.y;
+			double fij1 = F01i * w.x + F11i * w.y;
+			double fji0 = P[j] * wji.x + P[2 * n + j] * wji.y;
+			double fji1 = P[n + j] * wji.x + P[3 * n + j] * wji.y;
+			vx_t += 0.5 * (fji0 - fij0) / mi;
+			vy_t += 0.5 * (fji1 - fij1) / mi;
+		}
+		vx_t += a.fcx[i] / a.m[i];
+		vy_t += a.fcy[i] / a.m[i];
+	}
+	if (!POT && (flags & A_CR_STRESS)) {
 		double Pxxi = P[i], Pxyi = P[n + i], Pyxi = P[2 * n + i], Pyyi = P[3 * n + i];
 		double Rxxi = R[i], Rxyi = R[n + i], Ryxi = R[2 * n + i], Ryyi = R[3 * n + i];
 		double rhoi21 = 1. / (rho0 * rho0);
@@ -249,19 +339,32 @@ cudaError_t cr_sph(uint32_t n, const uint32_t* off, const uint32_t* nbr, const d
 	return cudaGetLastError();
 }
 
+cudaError_t cr_sell_wji(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy,
+                        const uint32_t* sl_off, void* sWji, cudaStream_t s) {
+	k_sell_wji<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, wx, wy, sl_off, (double2*)sWji);
+	return cudaGetLastError();
+}
+
 cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, const double* w, double* sW,
                       cudaStream_t s) {
 	k_sell_w<<<grid1(n, 128), 128, 0, s>>>(n, off, sl_off, w, sW);
 	return cudaGetLastError();
 }
 
-// part 0: rotation, 1: pass A, 2: pass B
+// part 0: rotation (corotational only), 1: pass A, 2: pass B
 cudaError_t cr_stage(const TLArgs& a, int part, cudaStream_t s) {
 	unsigned bs = a.block ? a.block : 128;
+	const bool pot = (a.flags & mfk_host::FLAG_POTENTIAL) != 0;
 	switch (part) {
 	case 0: k_crR<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
-	case 1: k_crA<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
-	case 2: k_crB<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	case 1:
+		if (pot) k_ptA<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else k_crA<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		break;
+	case 2:
+		if (pot) k_crB<true><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else k_crB<false><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		break;
 	}
 	return cudaGetLastError();
 }

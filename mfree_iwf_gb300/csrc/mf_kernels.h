@@ -12,6 +12,12 @@ namespace mfk_host {
 
 // Action flags of a fused pipeline (bit i = action id i of mf_action).
 inline uint32_t bit(int a) { return 1u << a; }
+// Actions with ids of 32 and above take flag bits that their method's pipeline leaves
+// free: the Godunov pair actions (updated-Lagrangian only) the bits of two
+// total-Lagrangian actions, the elastic-potential forces bit 0.
+constexpr uint32_t FLAG_GODUNOV_CONTINUITY = 1u << 12;
+constexpr uint32_t FLAG_GODUNOV_MOMENTUM = 1u << 13;
+constexpr uint32_t FLAG_POTENTIAL = 1u << 0;
 
 // Per-body constants (simulation_data.h:25-99 plus the body's dt), device copy.
 struct BodyParams {
@@ -112,7 +118,8 @@ struct TLArgs {
 	const void* sw;                      // corrected gradient per pair: double2 (FP64 forms) / float2 times m_j (mixed)
 	const void* swA;                     // mixed: the gradient times the neighbour's quad weight (pass A)
 	void *P, *dA, *c;                    // per-stage scratch (FP64 forms)
-	const void* sW;                      // corotational: kernel value W per pair (double, sliced ELL)
+	const void* sW;                      // corotational: kernel value W per pair (double, sliced ELL);
+	                                     // potential: grad W of the reverse pair (double2, sliced ELL)
 	void* R;                             // corotational: rotation per row, 4 x n doubles (Rxx, Rxy, Ryx, Ryy)
 	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
 	void* recB_out;                      // mixed: pass B writes the next stage's records here...
@@ -204,6 +211,8 @@ struct ContactArgs {
 	cudaError_t tl_tile_attrs(uint32_t halo_max, uint32_t ent_max);                                          \
 	cudaError_t cr_sph(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y, \
 	                   const double* h, double* w, double* wx, double* wy, cudaStream_t s);                 \
+	cudaError_t cr_sell_wji(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy,  \
+	                        const uint32_t* sl_off, void* sWji, cudaStream_t s);                                   \
 	cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, const double* w, double* sW, \
 	                      cudaStream_t s);                                                                   \
 	cudaError_t cr_stage(const mfk_host::TLArgs& a, int part, cudaStream_t s);                               \

@@ -49,10 +49,14 @@ enum : uint32_t {
 	A_CONTINUITY = 1u << 9,
 	A_MOMENTUM_UL = 1u << 10,
 	A_ADVECTION = 1u << 11,
+	A_GOD_CONT = mfk_host::FLAG_GODUNOV_CONTINUITY,
+	A_GOD_MOM = mfk_host::FLAG_GODUNOV_MOMENTUM,
 };
 
 // Cell-ordered record of one particle's stage state plus per-particle derived
-// quantities.  FP64 form: 16 doubles = 128 bytes, loaded as 8 x 16 B.
+// quantities.  FP64 form: 16 doubles = 128 bytes, loaded as 8 x 16 B.  With the
+// Godunov actions (which exclude the artificial stress) Rxx holds the pressure p and
+// Rxy the stress Syy itself.
 struct __align__(16) Rec64 {
 	double x, y, vx, vy;
 	double m, h, rho, sxx;   // sxx = Sxx - p
@@ -351,6 +355,10 @@ __global__ void k_gather64(ULArgs a, const BodyParams* __restrict__ P) {
 	per_particle<double>(a.flags, P[b], r.m, rho, a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c, r.qw,
 	                     r.rho21);
 	r.sxy = Sxy;
+	if (a.flags & (A_GOD_CONT | A_GOD_MOM)) {
+		r.Rxx = (a.flags & A_EOS) ? P[b].c0sq * (rho - P[b].rho0) : 0.;
+		r.Rxy = Syy;
+	}
 	Rec64* out = reinterpret_cast<Rec64*>(a.rec) + k;
 	const double2* s = reinterpret_cast<const double2*>(&r);
 	double2* d = reinterpret_cast<double2*>(out);
@@ -473,6 +481,7 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 	double Sxx_x = 0., Sxy_y = 0., Sxy_x = 0., Syy_y = 0.;
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
 	double av_x = 0., av_y = 0., xs_x = 0., xs_y = 0.;
+	double god_rho = 0., god_vx = 0., god_vy = 0.;
 	uint32_t cnt = 0;
 	for (int ni = lo_i; ni < hi_i; ni++) {
 		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
@@ -531,6 +540,43 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 				xs_x += fac * vijx;
 				xs_y += fac * vijy;
 			}
+			if ((flags & (A_GOD_CONT | A_GOD_MOM)) && kj != k) {
+				// |x_j - x_i| from the predicate's own sum (the same value as the
+				// reference's sqrt(dx*dx + dy*dy) and sqrt(dot(R, R)))
+				double mag_r = sqrt(r2);
+				if (flags & A_GOD_CONT) {  // godunov_continuity, godunov.h:144-187
+					double nx = xij / mag_r, ny = yij / mag_r;
+					double vir = ri.vx * nx + ri.vy * ny;
+					double vjr = rj.vx * nx + rj.vy * ny;
+					// riemann_solver_acoustic (godunov.h:41-54); Rxx = p
+					double frac = 1. / (ri.rho * ri.c + rj.rho * rj.c);
+					double ustar = frac * (vir * ri.rho * ri.c + vjr * rj.rho * rj.c - ri.Rxx + rj.Rxx);
+					god_rho += 2 * ri.rho * (vir - ustar) * (w.w_x * nx + w.w_y * ny) * rj.qw;
+				}
+				if (flags & A_GOD_MOM) {  // godunov_get_trafo + godunov_momentum, godunov.h:56-142
+					double rx = rj.x - ri.x, ry = rj.y - ri.y;
+					double inv = 1. / mag_r;  // glm::normalize: v * (1 / sqrt(dot(v, v)))
+					double Rx = rx * inv, Ry = ry * inv, Sx = ry * inv, Sy = -rx * inv;
+					// the frame matrix is single precision (a glm::mat2x2 of the unit vectors)
+					double lRx = (double)__double2float_rn(Rx), lRy = (double)__double2float_rn(Ry);
+					double lSx = (double)__double2float_rn(Sx), lSy = (double)__double2float_rn(Sy);
+					// stress times R: (Sxx - p, Sxy; Sxy, Syy), Rxy = Syy
+					double siR0 = ri.sxx * Rx + ri.sxy * Ry, siR1 = ri.sxy * Rx + ri.Rxy * Ry;
+					double sjR0 = rj.sxx * Rx + rj.sxy * Ry, sjR1 = rj.sxy * Rx + rj.Rxy * Ry;
+					double si0 = lRx * siR0 + lSx * siR1, si1 = lRy * siR0 + lSy * siR1;
+					double sj0 = lRx * sjR0 + lSx * sjR1, sj1 = lRy * sjR0 + lSy * sjR1;
+					double vi0 = lRx * ri.vx + lSx * ri.vy, vi1 = lRy * ri.vx + lSy * ri.vy;
+					double vj0 = lRx * rj.vx + lSx * rj.vy, vj1 = lRy * rj.vx + lSy * rj.vy;
+					double rci = ri.rho * ri.c, rcj = rj.rho * rj.c;
+					double frac = 1. / (rci + rcj);
+					// the second component takes sigma_j twice (godunov.h:116), as the reference does
+					double S0 = frac * (sj0 * ri.rho * ri.c + si0 * rj.rho * rj.c + ri.rho * ri.c * rj.rho * rj.c * (vj0 - vi0));
+					double S1 = frac * (sj1 * ri.rho * ri.c + sj1 * rj.rho * rj.c + ri.rho * ri.c * rj.rho * rj.c * (vj1 - vi1));
+					double SR0 = lRx * S0 + lRy * S1, SR1 = lSx * S0 + lSy * S1;
+					if (fabs(rx) > 0.) god_vx += 2. / ri.rho * w.w_x * mag_r / rx * SR0 * rj.qw;
+					if (fabs(ry) > 0.) god_vy += 2. / ri.rho * w.w_y * mag_r / ry * SR1 * rj.qw;
+				}
+			}
 		}
 	}
 	if (a.max_nbh && cnt >= a.max_nbh) raise(st, ERR_NBH_OVERFLOW, i);
@@ -548,6 +594,11 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 		jaumann<double>(vx_x, vx_y, vy_x, vy_y, sv.Sxx[i], sv.Sxy[i], sv.Syy[i], pr.G, d[5], d[6], d[7]);
 	}
 	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
+	if (flags & A_GOD_CONT) d[4] = god_rho;
+	if (flags & A_GOD_MOM) {
+		d[2] += god_vx + a.fcx[i] / ri.m;
+		d[3] += god_vy + a.fcy[i] / ri.m;
+	}
 	if (flags & A_MOMENTUM_UL) {
 		d[2] += 1. / rhoi * (Sxx_x + Sxy_y) + a.fcx[i] / ri.m;
 		d[3] += 1. / rhoi * (Sxy_x + Syy_y) + a.fcy[i] / ri.m;

@@ -20,8 +20,11 @@ import numpy as np
 
 from .actions import (
     RINGS_COROT_ACTIONS,
+    RINGS_GODUNOV_ACTIONS,
     RINGS_MONAGHAN_ACTIONS,
+    RINGS_POTENTIAL_ACTIONS,
     ROTATION_COROT_ACTIONS,
+    ROTATION_POTENTIAL_ACTIONS,
     TENSILE_COROT_ACTIONS,
     RINGS_TL_ACTIONS,
     TENSILE_TL_ACTIONS,
@@ -33,7 +36,7 @@ M_1_PI = 0.31830988618379067154  # the C library's M_1_PI
 IN_NAMES = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx", "Sxy", "Syy")
 OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
 
-METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT = 1, 2, 3, 4
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
 BC_PULL_TL = 1
 
 
@@ -213,12 +216,15 @@ def rings(
     nbh_eps: float = 1e-6,
     edge_tol: float = 0.0,
     exact_hull: bool = False,
+    godunov: bool = False,
     name: str = "",
 ) -> Scenario:
     """Two rings on a square lattice, as rings_monaghan (rings.cpp:20-99),
-    rings_monaghan_contact (:522-621) and rings_tl_contact (:338-429) build them.
+    rings_monaghan_contact (:522-621), rings_tl_contact (:338-429) and the other
+    families' ring set-ups build them.
 
     Defaults are the reference's constants; ``dt=None`` selects dt = cfl*h/c0.
+    ``godunov`` selects the Godunov action list for UL (all correction constants zero).
     ``exact_hull`` runs the hull's orientation tests on the integer lattice indices
     instead of the rounded coordinates, so the points kept on straight hull edges do not
     depend on rounding (the reference tests the coordinates).
@@ -227,7 +233,7 @@ def rings(
         spacing = ro + 0.001
     dx = 2 * ro / (nbox - 1)
     pts = _ring_lattice(nbox, dx, ro, ri)
-    tl = method in (METHOD_TL, METHOD_COROT)
+    tl = method in (METHOD_TL, METHOD_COROT, METHOD_POTENTIAL)
     sc = Scenario(method=method, bodies=[], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
     if dt is None:
         dt = cfl * (hdx * dx) / sc.c0
@@ -266,7 +272,9 @@ def rings(
             sc.bodies.append(Body(a, hull=hull))
         sc.contact = 1
 
-    if method == METHOD_UL:
+    if method == METHOD_UL and godunov:
+        sc.actions = list(RINGS_GODUNOV_ACTIONS)
+    elif method == METHOD_UL:
         sc.actions = list(RINGS_MONAGHAN_ACTIONS)
         sc.alpha, sc.beta, sc.eta = alpha, beta, eta
         sc.wdeltap = cubic_spline(0, 0, dx, 0, hdx * dx)[0]
@@ -274,7 +282,8 @@ def rings(
         sc.mghn_eps = art_stress_eps
         sc.xsph_eps = xsph_eps
     else:
-        sc.actions = list(RINGS_TL_ACTIONS if method == METHOD_TL else RINGS_COROT_ACTIONS)
+        sc.actions = list({METHOD_TL: RINGS_TL_ACTIONS, METHOD_COROT: RINGS_COROT_ACTIONS,
+                           METHOD_POTENTIAL: RINGS_POTENTIAL_ACTIONS}[method])
         sc.alpha, sc.beta, sc.eta = alpha, beta, eta
         sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
@@ -303,24 +312,61 @@ def rings_corot_contact(nbox: int) -> Scenario:
                  name=f"rings_corot_contact({nbox})")
 
 
-def rotation_corot(nbox: int, *, ro: float = 1.0, rho0: float = 1.0, E: float = 1e7, nu: float = 0.4,
-                   hdx: float = 1.3, omega_r: float = 50.0, dt: float = 2.5e-6) -> Scenario:
-    """A disc spinning as a rigid body (v = omega x r, |v| = omega_r at r = ro), corotational
-    SPH without artificial viscosity: the reference's rotation_corot(nbox),
-    rotation.cpp:78-140 (lattice px = -ro + i*dx, disc dist < ro)."""
+def rings_godunov(nbox: int) -> Scenario:
+    """The reference's rings_godunov(nbox), rings.cpp:101-162: both rings in one body."""
+    return rings(nbox, godunov=True, dt=1e-7, name=f"rings_godunov({nbox})")
+
+
+def rings_godunov_contact(nbox: int) -> Scenario:
+    """The reference's rings_godunov_contact(nbox), rings.cpp:164-243."""
+    return rings(nbox, godunov=True, two_bodies=True, dt=1e-7, name=f"rings_godunov_contact({nbox})")
+
+
+def rings_potential_contact(nbox: int) -> Scenario:
+    """The reference's rings_potential_contact(nbox), rings.cpp:431-520: rings of radius
+    1 m and 0.75 m, h = 1.3 dx."""
+    return rings(nbox, ro=1.0, ri=0.75, hdx=1.3, method=METHOD_POTENTIAL, two_bodies=True, dt=1e-7, alpha=1.0,
+                 beta=1.0, eta=0.1, name=f"rings_potential_contact({nbox})")
+
+
+def disc(nbox: int, *, method: int, actions: Sequence[int], hdx: float, dt: float, ro: float = 1.0,
+         rho0: float = 1.0, E: float = 1e7, nu: float = 0.4, omega_r: float = 50.0, alpha: float = 0.0,
+         beta: float = 0.0, eta: float = 0.0, name: str = "") -> Scenario:
+    """A disc spinning as a rigid body (v = omega x r, |v| = omega_r at r = ro), the
+    rotation set-ups of rotation.cpp (lattice px = -ro + i*dx, disc dist < ro)."""
     dx = 2 * ro / (nbox - 1)
     px, py = _ring_lattice_np(nbox, dx, ro, 0.0)
-    a = _body_from_lists(px, py, px, py)
+    tl = method != METHOD_UL
+    a = _body_from_lists(px, py, px if tl else None, py if tl else None)
     a["rho"][:] = rho0
     a["h"][:] = hdx * dx
     a["m"][:] = dx * dx * rho0
     a["quad_weight"][:] = a["m"] / a["rho"]
     a["vx"][:] = -a["y"] / ro * omega_r
     a["vy"][:] = +a["x"] / ro * omega_r
-    sc = Scenario(method=METHOD_COROT, bodies=[Body(a)], actions=list(ROTATION_COROT_ACTIONS), dt=dt, nu=nu, E=E,
-                  rho0=rho0, alpha=1.0, beta=1.0, eta=0.1, name=f"rotation_corot({nbox})")
-    sc.nbh_h = hdx * dx
+    sc = Scenario(method=method, bodies=[Body(a)], actions=list(actions), dt=dt, nu=nu, E=E, rho0=rho0, alpha=alpha,
+                  beta=beta, eta=eta, name=name)
+    if tl:
+        sc.nbh_h = hdx * dx
     return sc
+
+
+def rotation_godunov(nbox: int) -> Scenario:
+    """The reference's rotation_godunov(nbox), rotation.cpp:20-76."""
+    return disc(nbox, method=METHOD_UL, actions=RINGS_GODUNOV_ACTIONS, hdx=1.7, dt=1e-6,
+                name=f"rotation_godunov({nbox})")
+
+
+def rotation_corot(nbox: int) -> Scenario:
+    """The reference's rotation_corot(nbox), rotation.cpp:78-140 (no artificial viscosity)."""
+    return disc(nbox, method=METHOD_COROT, actions=ROTATION_COROT_ACTIONS, hdx=1.3, dt=2.5e-6, alpha=1.0, beta=1.0,
+                eta=0.1, name=f"rotation_corot({nbox})")
+
+
+def rotation_potential(nbox: int) -> Scenario:
+    """The reference's rotation_potential(nbox), rotation.cpp:212-272 (no artificial viscosity)."""
+    return disc(nbox, method=METHOD_POTENTIAL, actions=ROTATION_POTENTIAL_ACTIONS, hdx=1.7, dt=1e-6, alpha=1.0,
+                beta=1.0, eta=0.1, name=f"rotation_potential({nbox})")
 
 
 def workload_nbh_eps(dx: float) -> float:
@@ -395,8 +441,9 @@ def tensile_plate(
     sc.dt = dt if dt is not None else cfl * (hdx * dx) / sc.c0
     sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
-    if method in (METHOD_TL, METHOD_COROT):
-        sc.actions = list(TENSILE_TL_ACTIONS if method == METHOD_TL else TENSILE_COROT_ACTIONS)
+    if method in (METHOD_TL, METHOD_COROT, METHOD_POTENTIAL):
+        sc.actions = list({METHOD_TL: TENSILE_TL_ACTIONS, METHOD_COROT: TENSILE_COROT_ACTIONS,
+                           METHOD_POTENTIAL: RINGS_POTENTIAL_ACTIONS}[method])
         sc.alpha, sc.beta, sc.eta = alpha, beta, eta
     else:
         sc.actions = list(TENSILE_TL_WEAK_ACTIONS)
@@ -418,6 +465,12 @@ def tensile_tl(nbox: int) -> Scenario:
 def tensile_corot(nbox: int) -> Scenario:
     """The reference's tensile_corot(nbox), tensile.cpp:137-211."""
     return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_COROT, hdx=1.0, dt=1e-6, name=f"tensile_corot({nbox})")
+
+
+def tensile_potential(nbox: int) -> Scenario:
+    """The reference's tensile_potential(nbox), tensile.cpp:291-361."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_POTENTIAL, hdx=1.0, dt=1e-6,
+                         name=f"tensile_potential({nbox})")
 
 
 def tensile_tl_weak(nbox: int) -> Scenario:

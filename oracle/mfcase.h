@@ -20,7 +20,7 @@
 
 namespace mfcase {
 
-enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3, COROT = 4 };
+enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3, COROT = 4, POTENTIAL = 5 };
 
 // Action identifiers; the numbering is the C ABI's mf_action (include/mfree_gb300.h).
 enum Action : uint32_t {
@@ -55,7 +55,10 @@ enum Action : uint32_t {
 	DERIVE_DISPLACEMENT_COROTATIONAL = 29,
 	MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN = 30,
 	DERIVE_STRESS_COROTATIONAL = 31,
-	ACTION_MAX = 32
+	GODUNOV_CONTINUITY = 32,
+	GODUNOV_MOMENTUM = 33,
+	POTENTIAL_COMP_ELASTIC_POTENTIAL = 34,
+	ACTION_MAX = 35
 };
 
 // Boundary-condition kinds.  PULL_TL is the position-prescribed pull of

@@ -50,6 +50,7 @@ struct PSet {
 	std::vector<double> Pxx, Pxy, Pyx, Pyy, Pxx_x, Pxy_x, Pyx_y, Pyy_y;
 	std::vector<unsigned> num_nbh, nbh;  // nbh[slot*MAX_NBH + k]
 	std::vector<double> w, w_x, w_y;
+	std::vector<double> wji_x, wji_y;  // particle_potential: grad W of the reverse pair (particle.h:101)
 
 	void resize(unsigned nn) {
 		n = nn;
@@ -63,6 +64,8 @@ struct PSet {
 		w.assign((size_t)n * MAX_NBH, 0.);
 		w_x.assign((size_t)n * MAX_NBH, 0.);
 		w_y.assign((size_t)n * MAX_NBH, 0.);
+		wji_x.assign((size_t)n * MAX_NBH, 0.);
+		wji_y.assign((size_t)n * MAX_NBH, 0.);
 		for (unsigned i = 0; i < n; i++) idx[i] = i;
 	}
 
@@ -73,8 +76,9 @@ struct PSet {
 	}
 };
 
-// particle::copy_into (particle.cpp:45-74) plus the particle_tl (:106-116) and
-// particle_monaghan (:219-228) overrides: the union of the fields they copy.
+// particle::copy_into (particle.cpp:45-74) plus the particle_tl (:106-116),
+// particle_potential (:156-163) and particle_monaghan (:219-228) overrides: the union
+// of the fields they copy.
 void copy_into(const PSet& a, unsigned s, PSet& b, unsigned d) {
 	b.idx[d] = a.idx[s]; b.hash[d] = a.hash[s];
 	b.m[d] = a.m[s]; b.rho[d] = a.rho[s]; b.h[d] = a.h[s]; b.qw[d] = a.qw[s]; b.p[d] = a.p[s];
@@ -88,6 +92,7 @@ void copy_into(const PSet& a, unsigned s, PSet& b, unsigned d) {
 	for (unsigned k = 0; k < nn; k++) {
 		b.nbh[dof + k] = a.nbh[so + k];
 		b.w[dof + k] = a.w[so + k]; b.w_x[dof + k] = a.w_x[so + k]; b.w_y[dof + k] = a.w_y[so + k];
+		b.wji_x[dof + k] = a.wji_x[so + k]; b.wji_y[dof + k] = a.wji_y[so + k];
 	}
 	b.Pxx[d] = a.Pxx[s]; b.Pxy[d] = a.Pxy[s]; b.Pyx[d] = a.Pyx[s]; b.Pyy[d] = a.Pyy[s];
 	b.Rxx[d] = a.Rxx[s]; b.Rxy[d] = a.Rxy[s]; b.Ryy[d] = a.Ryy[s]; b.Ryx[d] = a.Ryx[s];
@@ -281,6 +286,26 @@ void precomp_randles_libersky(PSet& P) {
 			P.w_y[o] = (w.w_x * invB[0][1] + w.w_y * invB[1][1]) * 1. / C;
 		}
 	}
+}
+
+// precomp_randles_libersky_symmetric, precomp_shape_functions.h:292-315: for every
+// listed pair (i, j), the weight gradient that j's list holds for i (the first
+// match; a pair missing from j's list keeps zero)
+void precomp_randles_libersky_symmetric(PSet& P) {
+	precomp_randles_libersky(P);
+	for (unsigned i = 0; i < P.n; i++)
+		for (unsigned j = 0; j < P.num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = P.nbh[o];
+			for (unsigned k = 0; k < P.num_nbh[jdx]; k++) {
+				size_t q = (size_t)jdx * MAX_NBH + k;
+				if (P.nbh[q] == i) {
+					P.wji_x[o] = P.w_x[q];
+					P.wji_y[o] = P.w_y[q];
+					break;
+				}
+			}
+		}
 }
 
 // solve3x3, precomp_shape_functions.h:31-50
@@ -841,6 +866,120 @@ void a_stress_corot(Ctx& c, PSet& P, const std::vector<unsigned>&, PSet*) {
 	}
 }
 
+// godunov_get_trafo, godunov.h:56-84: the pair's unit direction R = (x_j - x_i)/|.|
+// and its normal S, the stresses projected on R and the velocities, all turned into
+// the (R, S) frame.  The frame matrix is built as a single-precision glm::mat2x2
+// (godunov.h:73), so it holds the float roundings of R and S.  The stress matrix
+// subtracts the pressure from Sxx only (godunov.h:68-69).
+struct GTrafo {
+	glm::dmat2x2 l;
+	glm::dvec2 siR, sjR, vi, vj;
+};
+GTrafo godunov_trafo(const PSet& P, unsigned si, unsigned sj) {
+	double Rx = P.x[sj] - P.x[si];
+	double Ry = P.y[sj] - P.y[si];
+	double Sx = Ry, Sy = -Rx;
+	glm::dvec2 R = glm::normalize(glm::dvec2(Rx, Ry));
+	glm::dvec2 S = glm::normalize(glm::dvec2(Sx, Sy));
+	glm::dmat2x2 sig_i(P.Sxx[si] - P.p[si], P.Sxy[si], P.Sxy[si], P.Syy[si]);
+	glm::dmat2x2 sig_j(P.Sxx[sj] - P.p[sj], P.Sxy[sj], P.Sxy[sj], P.Syy[sj]);
+	GTrafo t;
+	t.l = glm::mat2x2(R, S);
+	glm::dvec2 siR = sig_i * R, sjR = sig_j * R;
+	t.siR = t.l * siR;
+	t.sjR = t.l * sjR;
+	t.vi = t.l * glm::dvec2(P.vx[si], P.vy[si]);
+	t.vj = t.l * glm::dvec2(P.vx[sj], P.vy[sj]);
+	return t;
+}
+// godunov_momentum, godunov.h:86-142 (Parshikov-Medin acoustic Riemann solution per
+// pair; the second component uses sigma_j twice, godunov.h:116, as written)
+void a_godunov_momentum(Ctx& c, PSet& P, const std::vector<unsigned>& perm, PSet*) {
+	double K = c.k.K();
+	for (unsigned i = 0; i < P.n; i++) {
+		unsigned si = perm[i];
+		double ci = sqrt(K / P.rho[si]);
+		double rhoi = P.rho[si];
+		for (unsigned j = 0; j < P.num_nbh[si]; j++) {
+			size_t o = (size_t)si * MAX_NBH + j;
+			unsigned sj = perm[P.nbh[o]];
+			if (P.idx[si] == P.idx[sj]) continue;
+			GTrafo t = godunov_trafo(P, si, sj);
+			double cj = sqrt(K / P.rho[sj]);
+			double rhoj = P.rho[sj];
+			double qw = P.qw[sj];
+			glm::dvec2 SRs;
+			double frac = 1. / (rhoi * ci + rhoj * cj);
+			SRs[0] = frac * (t.sjR[0] * rhoi * ci + t.siR[0] * rhoj * cj + rhoi * ci * rhoj * cj * (t.vj[0] - t.vi[0]));
+			SRs[1] = frac * (t.sjR[1] * rhoi * ci + t.sjR[1] * rhoj * cj + rhoi * ci * rhoj * cj * (t.vj[1] - t.vi[1]));
+			glm::dvec2 SR = glm::transpose(t.l) * SRs;
+			double rx = P.x[sj] - P.x[si];
+			double ry = P.y[sj] - P.y[si];
+			double mag_r = sqrt(rx * rx + ry * ry);
+			if (fabs(rx) > 0.) P.vx_t[si] += 2. / rhoi * P.w_x[o] * mag_r / rx * SR[0] * qw;
+			if (fabs(ry) > 0.) P.vy_t[si] += 2. / rhoi * P.w_y[o] * mag_r / ry * SR[1] * qw;
+		}
+	}
+	for (unsigned i = 0; i < P.n; i++) {
+		P.vx_t[i] += P.fcx[i] / P.m[i];
+		P.vy_t[i] += P.fcy[i] / P.m[i];
+	}
+}
+// godunov_continuity, godunov.h:144-187, with riemann_solver_acoustic (:41-54) inline
+void a_godunov_continuity(Ctx& c, PSet& P, const std::vector<unsigned>& perm, PSet*) {
+	double K = c.k.K();
+	for (unsigned i = 0; i < P.n; i++) {
+		unsigned si = perm[i];
+		double xi = P.x[si], yi = P.y[si], rhoi = P.rho[si];
+		double rho_t = 0.;
+		for (unsigned j = 0; j < P.num_nbh[si]; j++) {
+			size_t o = (size_t)si * MAX_NBH + j;
+			unsigned sj = perm[P.nbh[o]];
+			if (P.idx[si] == P.idx[sj]) continue;
+			double dx = xi - P.x[sj], dy = yi - P.y[sj];
+			double mag_r = sqrt(dx * dx + dy * dy);
+			double nx = dx / mag_r, ny = dy / mag_r;
+			double vir = P.vx[si] * nx + P.vy[si] * ny;
+			double vjr = P.vx[sj] * nx + P.vy[sj] * ny;
+			double rhol = P.rho[si], rhor = P.rho[sj], pl = P.p[si], pr = P.p[sj];
+			double csl = sqrt(K / rhol), csr = sqrt(K / rhor);
+			double frac = 1. / (rhol * csl + rhor * csr);
+			double ustar = frac * (vir * rhol * csl + vjr * rhor * csr - pl + pr);
+			rho_t += 2 * rhoi * (vir - ustar) * (P.w_x[o] * nx + P.w_y[o] * ny) * P.qw[sj];
+		}
+		P.rho_t[si] = rho_t;
+	}
+}
+// potential_comp_elastic_potential, potential.h:33-83: pair forces from the elastic
+// potential, f_ij = -2 V_i F_i S_i grad W_ij, with the reverse pair's gradient for f_ji
+void a_potential(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
+	for (unsigned i = 0; i < P.n; i++) {
+		glm::dmat2x2 Ji(P.Hxx[i] + 1., P.Hyx[i], P.Hxy[i], P.Hyy[i] + 1.);
+		glm::dmat2x2 Si(P.Sxx[i], P.Sxy[i], P.Sxy[i], P.Syy[i]);
+		double voli = P.qw[i];
+		glm::dmat2x2 Fei = -2 * voli * Ji * Si;
+		double vx_t = 0., vy_t = 0.;
+		for (unsigned j = 0; j < P.num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = P.nbh[o];
+			glm::dvec2 fij = Fei * glm::dvec2(P.w_x[o], P.w_y[o]);
+			glm::dmat2x2 Jj(P.Hxx[jdx] + 1., P.Hyx[jdx], P.Hxy[jdx], P.Hyy[jdx] + 1.);
+			glm::dmat2x2 Sj(P.Sxx[jdx], P.Sxy[jdx], P.Sxy[jdx], P.Syy[jdx]);
+			double volj = P.qw[jdx];
+			glm::dmat2x2 Fej = -2 * volj * Jj * Sj;
+			glm::dvec2 fji = Fej * glm::dvec2(P.wji_x[o], P.wji_y[o]);
+			vx_t += 0.5 * (fji[0] - fij[0]) / P.m[i];
+			vy_t += 0.5 * (fji[1] - fij[1]) / P.m[i];
+		}
+		P.vx_t[i] = vx_t;
+		P.vy_t[i] = vy_t;
+	}
+	for (unsigned i = 0; i < P.n; i++) {
+		P.vx_t[i] += P.fcx[i] / P.m[i];
+		P.vy_t[i] += P.fcy[i] / P.m[i];
+	}
+}
+
 ActFn action_fn(uint32_t a) {
 	switch (a) {
 	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return a_riemann;
@@ -874,6 +1013,9 @@ ActFn action_fn(uint32_t a) {
 	case DERIVE_DISPLACEMENT_COROTATIONAL: return a_disp_corot;
 	case MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN: return a_cauchy_green;
 	case DERIVE_STRESS_COROTATIONAL: return a_stress_corot;
+	case GODUNOV_CONTINUITY: return a_godunov_continuity;
+	case GODUNOV_MOMENTUM: return a_godunov_momentum;
+	case POTENTIAL_COMP_ELASTIC_POTENTIAL: return a_potential;
 	}
 	throw Fail{"unknown action id"};
 }
@@ -1011,7 +1153,7 @@ struct Sim {
 			if (!recorded && s == 0) record_nbh(P, perm, b);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, nullptr);
 			std::sort(perm.begin(), perm.end(), [&P](unsigned a, unsigned bb) { return P.idx[a] < P.idx[bb]; });
-		} else if (c.method == TL || c.method == COROT) {
+		} else if (c.method == TL || c.method == COROT || c.method == POTENTIAL) {
 			carry_out_bc(B, P, ctx.time);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, nullptr);
 		} else {
@@ -1175,6 +1317,11 @@ struct Sim {
 				// rings.cpp:311-315 / tensile.cpp:197-198: plain SPH weights on the set-up lists
 				find_neighbors(B.P, B.P, c.nbh_h, c.nbh_eps);
 				precomp_sph(B.P, ident(B.n));
+				record_nbh(B.P, ident(B.n), b);
+			} else if (c.method == POTENTIAL) {
+				// rings.cpp:497-501 / tensile.cpp:345-346: symmetric Randles-Libersky weights
+				find_neighbors(B.P, B.P, c.nbh_h, c.nbh_eps);
+				precomp_randles_libersky_symmetric(B.P);
 				record_nbh(B.P, ident(B.n), b);
 			} else if (c.method == TL_WEAK) {
 				setup_weak(B, in);

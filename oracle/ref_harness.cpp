@@ -65,6 +65,7 @@ typedef void (*UlAct)(body<particle_monaghan>&);
 typedef void (*TlAct)(body<particle_tl>&);
 typedef void (*WkAct)(body<particle_tl_weak>&);
 typedef void (*CrAct)(body<particle_corotational>&);
+typedef void (*PtAct)(body<particle_potential>&);
 
 UlAct ul_action(uint32_t a) {
 	typedef particle_monaghan T;
@@ -80,6 +81,19 @@ UlAct ul_action(uint32_t a) {
 	case CONTMECH_CONTINUITY: return &contmech_continuity<T>;
 	case CONTMECH_MOMENTUM_UL: return &contmech_momentum_ul<T>;
 	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case GODUNOV_CONTINUITY: return &godunov_continuity<T>;
+	case GODUNOV_MOMENTUM: return &godunov_momentum<T>;
+	}
+	return nullptr;
+}
+PtAct pt_action(uint32_t a) {
+	typedef particle_potential T;
+	switch (a) {
+	case CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY: return &correctors_mghn_artificial_viscosity<T>;
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case DERIVE_DISPLACEMENT: return &derive_displacement<T>;
+	case MATERIAL_COMPUTE_STRESS_GREEN_STVENANT: return &material_compute_stress_green_stvenant<T>;
+	case POTENTIAL_COMP_ELASTIC_POTENTIAL: return &potential_comp_elastic_potential<T>;
 	}
 	return nullptr;
 }
@@ -342,6 +356,26 @@ int run_case(const Case& c, const char* out) {
 			}
 		}
 		run_loop(w, c, bodies);
+	} else if (c.method == POTENTIAL) {
+		typedef particle_potential T;
+		std::vector<body<T>> bodies;
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			const BodyIn& in = c.bodies[b];
+			T** p = make_particles<T>(in);
+			find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
+			precomp_randles_libersky_symmetric<T>(p, in.n);
+			record_fixed_nbh(p, in.n, (int)b);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot)));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
+			for (uint32_t a : c.actions) {
+				PtAct f = pt_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for the potential method\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+		}
+		run_loop(w, c, bodies);
 	} else if (c.method == TL_WEAK) {
 		typedef particle_tl_weak T;
 		std::vector<body<T>> bodies;
@@ -515,6 +549,51 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 			BodyIn in = capture(bodies[b]);
 			if (!rings && !disc) {
 				BC l, r;  // tensile.cpp:170-176,188-190
+				l.kind = r.kind = BC_PULL_TL;
+				l.v = -10.; r.v = 10.;
+				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+				in.bcs = {l, r};
+			}
+			c.bodies.push_back(in);
+			record_fixed_nbh(bodies[b].get_particles(), bodies[b].get_num_part(), (int)b);
+		}
+		c.nbodies = (uint32_t)bodies.size();
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "rings_godunov" || name == "rings_godunov_contact" || name == "rotation_godunov") {
+		std::vector<body<particle_ul>> bodies = name == "rings_godunov" ? rings_godunov(nbox)
+		                                        : (name == "rotation_godunov" ? rotation_godunov(nbox)
+		                                                                      : rings_godunov_contact(nbox));
+		c.method = UL;
+		c.contact = name == "rings_godunov_contact";
+		c.actions = {RIEMANN_UPDATE_INTEGRATION_WEIGHTS, MATERIAL_EOS, DERIVE_VELOCITY, MATERIAL_STRESS_RATE_JAUMANN,
+		             GODUNOV_CONTINUITY, GODUNOV_MOMENTUM, CONTMECH_ADVECTION};  // rings.cpp:154-160,233-239
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		for (auto& b : bodies) { c.bodies.push_back(capture(b)); b.add_action(&record_first_nbh<particle_ul>); }
+		c.nbodies = (uint32_t)bodies.size();
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "rings_potential_contact" || name == "tensile_potential" || name == "rotation_potential") {
+		const bool rings = name == "rings_potential_contact", disc = name == "rotation_potential";
+		std::vector<body<particle_potential>> bodies =
+		    rings ? rings_potential_contact(nbox) : (disc ? rotation_potential(nbox) : tensile_potential(nbox));
+		c.method = POTENTIAL;
+		c.contact = rings ? 1 : 0;
+		c.actions = {DERIVE_DISPLACEMENT, MATERIAL_COMPUTE_STRESS_GREEN_STVENANT, POTENTIAL_COMP_ELASTIC_POTENTIAL,
+		             CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY, CONTMECH_ADVECTION};  // rings.cpp:512-516, tensile.cpp:354-358
+		if (disc)  // rotation.cpp:266-269: no artificial viscosity
+			c.actions = {DERIVE_DISPLACEMENT, MATERIAL_COMPUTE_STRESS_GREEN_STVENANT, POTENTIAL_COMP_ELASTIC_POTENTIAL,
+			             CONTMECH_ADVECTION};
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			BodyIn in = capture(bodies[b]);
+			if (!rings && !disc) {
+				BC l, r;  // tensile.cpp:349-350
 				l.kind = r.kind = BC_PULL_TL;
 				l.v = -10.; r.v = 10.;
 				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }

@@ -35,6 +35,12 @@ REFERENCE_CASES = [
     ("rings_corot_contact", 20, 480),
     ("tensile_corot", 11, 25),
     ("rotation_corot", 15, 400),
+    ("rings_godunov", 20, 30),
+    ("rings_godunov_contact", 20, 560),
+    ("rotation_godunov", 15, 100),
+    ("rings_potential_contact", 20, 5975),
+    ("tensile_potential", 11, 25),
+    ("rotation_potential", 15, 200),
 ]
 
 

@@ -2,10 +2,11 @@
 written by the compiled reference) and against the CPU oracle.
 
 Tolerances (relative L2 per field over all particles):
-  * FP64 strict (no FMA contraction): 1e-9 after the golden runs (12-375 steps).  The
-    updated-Lagrangian path differs from the reference only in summation order within
-    cells and in the last bit of atan2/sin/cos; the total-Lagrangian path sums in the
-    reference's order and is expected to agree to the last bit.
+  * FP64 strict (no FMA contraction): 1e-9 after the golden runs (6-5975 steps).  The
+    updated-Lagrangian paths (Gray-Monaghan, Godunov) differ from the reference only in
+    summation order within cells and in the last bit of atan2/sin/cos; the
+    total-Lagrangian paths (TL, weak TL, elastic potential) sum in the reference's order
+    and are expected to agree to the last bit.
   * corotational: the TL lists and the reference's order, but the rotation angle goes
     through atan2/sin/cos, which may differ in the last bit from the C library's, so
     the same 1e-9 bound instead of bit equality.
@@ -55,8 +56,11 @@ def golden(name):
     return sc, ref
 
 
-UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm"]
-TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak"]
+UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm", "rings_godunov", "rotation_godunov"]
+# rings_godunov_contact is checked against the reference's own conditioning in
+# test_gpu_families.py: its result moves by 1e-5..1e-2 under 1-ulp input noise
+TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak", "rings_potential_contact",
+            "tensile_potential", "rotation_potential"]
 COROT_CASES = ["rings_corot_contact", "tensile_corot", "rotation_corot"]
 
 
@@ -111,7 +115,7 @@ def test_tl_neighbor_lists_bitexact(name, lib):
     sim.close()
 
 
-@pytest.mark.parametrize("name", UL_CASES + TL_CASES + COROT_CASES)
+@pytest.mark.parametrize("name", [c for c in UL_CASES if "godunov" not in c] + TL_CASES + COROT_CASES)
 def test_fp64_fast_close_to_reference(name, lib):
     sc, ref = golden(name)
     steps = ref.dumps[-1]["step"]

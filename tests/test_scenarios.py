@@ -17,6 +17,12 @@ BUILDERS = {
     "rings_corot_contact": lambda: S.rings_corot_contact(20),
     "tensile_corot": lambda: S.tensile_corot(11),
     "rotation_corot": lambda: S.rotation_corot(15),
+    "rings_godunov": lambda: S.rings_godunov(20),
+    "rings_godunov_contact": lambda: S.rings_godunov_contact(20),
+    "rotation_godunov": lambda: S.rotation_godunov(15),
+    "rings_potential_contact": lambda: S.rings_potential_contact(20),
+    "tensile_potential": lambda: S.tensile_potential(11),
+    "rotation_potential": lambda: S.rotation_potential(15),
 }
 
 
