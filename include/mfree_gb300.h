@@ -111,7 +111,10 @@ typedef enum {
 
 /* Boundary-condition kinds (boundary_conditions<T> functors). */
 typedef enum {
-	MF_BC_PULL = 1  /* x = X + v*t, y = Y, vx = v, vy = 0, vx_t = vy_t = 0 (tensile.cpp:20-42) */
+	MF_BC_PULL = 1,    /* x = X + v*t, y = Y, vx = v, vy = 0, vx_t = vy_t = 0 (tensile.cpp:20-42); TL-type bodies,
+	                      at the start of every derivative evaluation */
+	MF_BC_VELOCITY = 2 /* x_t = v, y_t = 0, vx = v, vy = 0, vx_t = vy_t = 0 (tensile.cpp:44-66); UL bodies, after
+	                      every step (rk4.h:105) */
 } mf_bc_kind;
 
 typedef struct mf_config {

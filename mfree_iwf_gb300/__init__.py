@@ -25,7 +25,8 @@ LIB_PATH = os.path.join(HERE, "libmfree_gb300.so")
 METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
 PREC_FP64_STRICT, PREC_FP64, PREC_MIXED = 0, 1, 2
 PRECISIONS = {"fp64_strict": PREC_FP64_STRICT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
-BC_PULL = 1
+BC_PULL = 1       # tensile.cpp:20-42, TL-type bodies
+BC_VELOCITY = 2   # tensile.cpp:44-66, UL bodies
 
 STATUS = {
     0: "MF_OK", -1: "MF_ERR_ARG", -2: "MF_ERR_CUDA", -3: "MF_ERR_NBH_OVERFLOW", -4: "MF_ERR_NONFINITE",
@@ -400,7 +401,7 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
         for a in sc.actions:
             sim.add_action(bid, a)
         for bc in b.bcs:
-            sim.add_boundary_condition(bid, bc.idx, BC_PULL, bc.v)
+            sim.add_boundary_condition(bid, bc.idx, bc.kind, bc.v)
         if len(b.hull):
             sim.set_boundary(bid, b.hull)
         if sc.method == METHOD_TL_WEAK:

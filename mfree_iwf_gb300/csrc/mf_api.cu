@@ -283,6 +283,7 @@ mf_status tl_setup(mf_ctx* c);
 mf_status weak_setup(mf_ctx* c);
 mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status contact_setup(mf_ctx* c);
+mf_status upload_bcs(mf_ctx* c);
 
 // UL pipeline: a subsequence, in this order, of the union of the reference's
 // rings_monaghan list (rings.cpp:86-96) and rings_godunov list (rings.cpp:154-160),
@@ -466,9 +467,15 @@ mf_status finalize(mf_ctx* c) {
 		st = validate_weak(c, acts, c->flags);
 	}
 	if (st != MF_OK) return st;
+	// the reference's UL set-ups use the velocity form (tensile.cpp:44-66), applied after
+	// each step; the TL set-ups the pull form (tensile.cpp:20-42), applied per stage
 	for (auto& b : c->bodies)
-		for (auto& bc : b.bcs)
-			if (c->cfg.method == MF_METHOD_UL) return fail(c, MF_ERR_PIPELINE, "boundary conditions are not supported for UL bodies");
+		for (auto& bc : b.bcs) {
+			if (c->cfg.method == MF_METHOD_UL && bc.kind != MF_BC_VELOCITY)
+				return fail(c, MF_ERR_PIPELINE, "updated-Lagrangian bodies take MF_BC_VELOCITY conditions");
+			if (c->cfg.method != MF_METHOD_UL && bc.kind != MF_BC_PULL)
+				return fail(c, MF_ERR_PIPELINE, "total-Lagrangian bodies take MF_BC_PULL conditions");
+		}
 
 	uint32_t n = c->n_total;
 	CK(c->body_of.alloc(n));
@@ -540,6 +547,7 @@ mf_status finalize(mf_ctx* c) {
 		c->sort_bits = bits;
 		size_t tmp = c->strict ? mf_strict::ul_sort_tmp_bytes(n, bits) : mf_fast::ul_sort_tmp_bytes(n, bits);
 		CK(c->sort_tmp.alloc(tmp));
+		if ((st = upload_bcs(c)) != MF_OK) return st;
 	} else if (c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL) {
 		mf_status s2 = tl_setup(c);
 		if (s2 != MF_OK) return s2;
@@ -572,6 +580,12 @@ mf_status ul_step(mf_ctx* c) {
 		timing_end(c, slot_all, c->n_total);
 		if (e != cudaSuccess) return cuda_fail(c, e, "ul_stage");
 		c->launches += (a.strict_grid || s == 0) ? 8 + 4 : 2;
+	}
+	if (c->n_bc) {  // rk4.h:105: the conditions act on the particles after the combine
+		cudaError_t e = c->strict ? mf_strict::ul_bc(c->n_bc, c->bc_rows.p, c->bc_v.p, c->sd[0][2].p, c->sd[0][3].p, c->stream)
+		                          : mf_fast::ul_bc(c->n_bc, c->bc_rows.p, c->bc_v.p, c->sd[0][2].p, c->sd[0][3].p, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "ul_bc");
+		c->launches++;
 	}
 	return MF_OK;
 }
@@ -1064,7 +1078,11 @@ mf_status tl_setup(mf_ctx* c) {
 			CK(c->sf[3][q].alloc(n));
 			CK(cudaMemcpy(c->sf[2][q].p, c->sf[0][q].p, n * 4, cudaMemcpyDeviceToDevice));
 		}
-	// boundary conditions
+	return upload_bcs(c);
+}
+
+// The rows and speeds of every body's boundary conditions, concatenated.
+mf_status upload_bcs(mf_ctx* c) {
 	std::vector<uint32_t> rows;
 	std::vector<double> vs;
 	for (auto& b : c->bodies)
@@ -1335,20 +1353,9 @@ mf_status weak_setup(mf_ctx* c) {
 		if (c->mixed && q >= 4) continue;
 		CK(cudaMemcpy(c->sd[2][q].p, c->sd[0][q].p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
 	}
-	// boundary conditions
-	std::vector<uint32_t> rows;
-	std::vector<double> vs;
-	for (auto& b : c->bodies)
-		for (auto& bc : b.bcs)
-			for (uint32_t i : bc.idx) { rows.push_back(b.off + i); vs.push_back(bc.v); }
-	c->n_bc = (uint32_t)rows.size();
-	CK(c->bc_rows.alloc(rows.size())); CK(c->bc_v.alloc(vs.size()));
-	if (!rows.empty()) {
-		CK(cudaMemcpy(c->bc_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
-		CK(cudaMemcpy(c->bc_v.p, vs.data(), vs.size() * 8, cudaMemcpyHostToDevice));
-	}
-	return MF_OK;
+	return upload_bcs(c);
 }
+
 
 WeakArgs weak_args(mf_ctx* c) {
 	WeakArgs a{};
@@ -1626,7 +1633,8 @@ MF_API mf_status mf_add_boundary_condition(mf_ctx* c, int32_t body, const uint32
 	if (!c) return MF_ERR_ARG;
 	if (c->ready) return fail(c, MF_ERR_STATE, "boundary conditions must be added before the first step");
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
-	if (kind != MF_BC_PULL) return fail(c, MF_ERR_ARG, "unknown boundary-condition kind %d", kind);
+	if (kind != MF_BC_PULL && kind != MF_BC_VELOCITY)
+		return fail(c, MF_ERR_ARG, "unknown boundary-condition kind %d", kind);
 	if (k && !idx) return fail(c, MF_ERR_ARG, "null index list");
 	for (uint32_t i = 0; i < k; i++)
 		if (idx[i] >= c->bodies[body].n) return fail(c, MF_ERR_ARG, "boundary index %u out of range", idx[i]);

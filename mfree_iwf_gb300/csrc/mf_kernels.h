@@ -193,6 +193,7 @@ struct ContactArgs {
 	size_t ul_sort_tmp_bytes(uint32_t n, int bits);                                                          \
 	size_t ul_rec_bytes(bool mixed);                                                                         \
 	cudaError_t ul_stage(const mfk_host::ULArgs& a, bool mixed, cudaStream_t s);                             \
+	cudaError_t ul_bc(uint32_t n_bc, const uint32_t* rows, const double* v, double* vx, double* vy, cudaStream_t s); \
 	cudaError_t ul_neighbors(const mfk_host::ULArgs& a, uint32_t* counts, uint32_t* idx, const uint64_t* offs, \
 	                         int pass, cudaStream_t s);                                                      \
 	size_t tl_sort_tmp_bytes(uint32_t n, int bits);                                                          \

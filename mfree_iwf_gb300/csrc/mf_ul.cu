@@ -884,6 +884,23 @@ cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
 	return cudaGetLastError();
 }
 
+// left/right_bndry_fun_ul (tensile.cpp:44-66) on the particles after the RK4 combine
+// (rk4.h:105): of what they set only the velocity outlives the step, since every
+// derivative evaluation starts from zeroed rates
+__global__ void k_ul_bc(uint32_t n_bc, const uint32_t* __restrict__ rows, const double* __restrict__ v, double* vx,
+                        double* vy) {
+	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n_bc) return;
+	uint32_t i = rows[k];
+	vx[i] = v[k];
+	vy[i] = 0.;
+}
+
+cudaError_t ul_bc(uint32_t n_bc, const uint32_t* rows, const double* v, double* vx, double* vy, cudaStream_t s) {
+	k_ul_bc<<<grid1(n_bc, 128), 128, 0, s>>>(n_bc, rows, v, vx, vy);
+	return cudaGetLastError();
+}
+
 cudaError_t ul_neighbors(const ULArgs& a, uint32_t* counts, uint32_t* idx, const uint64_t* offs, int pass,
                          cudaStream_t s) {
 	if (a.n_total == 0) return cudaSuccess;

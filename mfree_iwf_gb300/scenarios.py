@@ -37,7 +37,8 @@ IN_NAMES = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx
 OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
 
 METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
-BC_PULL_TL = 1
+BC_PULL_TL = 1       # tensile.cpp:20-42 (total-Lagrangian bodies)
+BC_VELOCITY_UL = 2   # tensile.cpp:44-66 (updated-Lagrangian bodies)
 
 
 def cubic_spline(xi: float, yi: float, xj: float, yj: float, h: float):
@@ -275,12 +276,7 @@ def rings(
     if method == METHOD_UL and godunov:
         sc.actions = list(RINGS_GODUNOV_ACTIONS)
     elif method == METHOD_UL:
-        sc.actions = list(RINGS_MONAGHAN_ACTIONS)
-        sc.alpha, sc.beta, sc.eta = alpha, beta, eta
-        sc.wdeltap = cubic_spline(0, 0, dx, 0, hdx * dx)[0]
-        sc.corr_exp = stress_exponent
-        sc.mghn_eps = art_stress_eps
-        sc.xsph_eps = xsph_eps
+        _monaghan_constants(sc, dx, hdx, alpha, beta, eta, art_stress_eps, stress_exponent, xsph_eps)
     else:
         sc.actions = list({METHOD_TL: RINGS_TL_ACTIONS, METHOD_COROT: RINGS_COROT_ACTIONS,
                            METHOD_POTENTIAL: RINGS_POTENTIAL_ACTIONS}[method])
@@ -288,6 +284,20 @@ def rings(
         sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
     return sc
+
+
+def _monaghan_constants(sc: Scenario, dx: float, hdx: float, alpha: float = 1.0, beta: float = 1.0,
+                        eta: float = 0.1, art_stress_eps: float = 0.3, stress_exponent: float = 4.0,
+                        xsph_eps: float = 0.5) -> None:
+    """The Gray-Monaghan action list and correction constants of the reference's UL
+    set-ups (rings.cpp:58-96): W(dx) for the artificial stress, exponent 4, eps 0.3,
+    XSPH 0.5."""
+    sc.actions = list(RINGS_MONAGHAN_ACTIONS)
+    sc.alpha, sc.beta, sc.eta = alpha, beta, eta
+    sc.wdeltap = cubic_spline(0, 0, dx, 0, hdx * dx)[0]
+    sc.corr_exp = stress_exponent
+    sc.mghn_eps = art_stress_eps
+    sc.xsph_eps = xsph_eps
 
 
 def rings_monaghan(nbox: int) -> Scenario:
@@ -349,6 +359,21 @@ def disc(nbox: int, *, method: int, actions: Sequence[int], hdx: float, dt: floa
     if tl:
         sc.nbh_h = hdx * dx
     return sc
+
+
+def rotation_monaghan(nbox: int) -> Scenario:
+    """The reference's rotation_monaghan(nbox), rotation.cpp:274-351."""
+    sc = disc(nbox, method=METHOD_UL, actions=RINGS_MONAGHAN_ACTIONS, hdx=1.7, dt=1e-5,
+              name=f"rotation_monaghan({nbox})")
+    _monaghan_constants(sc, 2.0 / (nbox - 1), 1.7)
+    return sc
+
+
+def rotation_tl(nbox: int) -> Scenario:
+    """The reference's rotation_tl(nbox), rotation.cpp:142-210 (the reference notes that
+    the total-Lagrangian disc fails as rotations grow)."""
+    return disc(nbox, method=METHOD_TL, actions=TENSILE_TL_ACTIONS, hdx=1.7, dt=1e-6, alpha=3.0, beta=3.0, eta=0.1,
+                name=f"rotation_tl({nbox})")
 
 
 def rotation_godunov(nbox: int) -> Scenario:
@@ -416,31 +441,45 @@ def tensile_plate(
     eta: float = 0.1,
     do_smooth: int = 1,
     nbh_eps: float = 1e-6,
+    godunov: bool = False,
+    bc_cols: int = 1,
     name: str = "",
 ) -> Scenario:
     """A rectangular plate pulled at both ends: tensile_tl (tensile.cpp:213-289) and
     tensile_tl_weak (:731-826) lattices (px = i*dx, py = j*dx; column i = 0 and
-    i = nx-1 carry the pull), generalised to nx != ny and optional seeded jitter."""
+    i = nx-1 carry the pull), generalised to nx != ny and optional seeded jitter.
+    Updated-Lagrangian plates (tensile_monaghan :363-450, tensile_godunov :68-135 with
+    ``godunov``) carry the velocity conditions of tensile.cpp:44-66 and no reference
+    coordinates; ``bc_cols`` lattice columns at each end are pulled (tensile_monaghan
+    pulls three, tensile.cpp:392-398)."""
     dx = Lx / (nx - 1)
     I, J = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64), indexing="ij")
     xs = (I * dx).ravel()
     ys = (J * dx).ravel()
-    left = np.arange(ny, dtype=np.uint32)
-    right = (np.uint32(nx - 1) * np.uint32(ny) + np.arange(ny, dtype=np.uint32)).astype(np.uint32)
+    left = np.arange(bc_cols * ny, dtype=np.uint32)
+    right = (np.uint32(nx - bc_cols) * np.uint32(ny) + np.arange(bc_cols * ny, dtype=np.uint32)).astype(np.uint32)
     if jitter > 0.0:
         rng = np.random.default_rng(seed)
         xs = xs + rng.uniform(-jitter, jitter, xs.shape) * dx
         ys = ys + rng.uniform(-jitter, jitter, ys.shape) * dx
-    a = _body_from_lists(xs, ys, xs, ys)
+    ul = method == METHOD_UL
+    a = _body_from_lists(xs, ys, None if ul else xs, None if ul else ys)
     a["rho"][:] = rho0
     a["h"][:] = hdx * dx
     a["m"][:] = dx * dx * rho0
     a["quad_weight"][:] = a["m"] / a["rho"]
-    body = Body(a, bcs=[BC(BC_PULL_TL, -pull, left), BC(BC_PULL_TL, pull, right)])
+    kind = BC_VELOCITY_UL if ul else BC_PULL_TL
+    body = Body(a, bcs=[BC(kind, -pull, left), BC(kind, pull, right)])
     sc = Scenario(method=method, bodies=[body], actions=[], dt=0.0, nu=nu, E=E, rho0=rho0, name=name)
     sc.dt = dt if dt is not None else cfl * (hdx * dx) / sc.c0
-    sc.nbh_h = hdx * dx
     sc.nbh_eps = nbh_eps
+    if ul:
+        if godunov:
+            sc.actions = list(RINGS_GODUNOV_ACTIONS)
+        else:
+            _monaghan_constants(sc, dx, hdx, alpha, beta, eta)
+        return sc
+    sc.nbh_h = hdx * dx
     if method in (METHOD_TL, METHOD_COROT, METHOD_POTENTIAL):
         sc.actions = list({METHOD_TL: TENSILE_TL_ACTIONS, METHOD_COROT: TENSILE_COROT_ACTIONS,
                            METHOD_POTENTIAL: RINGS_POTENTIAL_ACTIONS}[method])
@@ -465,6 +504,18 @@ def tensile_tl(nbox: int) -> Scenario:
 def tensile_corot(nbox: int) -> Scenario:
     """The reference's tensile_corot(nbox), tensile.cpp:137-211."""
     return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_COROT, hdx=1.0, dt=1e-6, name=f"tensile_corot({nbox})")
+
+
+def tensile_monaghan(nbox: int) -> Scenario:
+    """The reference's tensile_monaghan(nbox), tensile.cpp:363-450."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_UL, hdx=1.3, dt=1e-6, bc_cols=3,
+                         name=f"tensile_monaghan({nbox})")
+
+
+def tensile_godunov(nbox: int) -> Scenario:
+    """The reference's tensile_godunov(nbox), tensile.cpp:68-135."""
+    return tensile_plate(nbox, nbox, Lx=1.0, method=METHOD_UL, hdx=1.7, dt=1e-6, godunov=True,
+                         name=f"tensile_godunov({nbox})")
 
 
 def tensile_potential(nbox: int) -> Scenario:

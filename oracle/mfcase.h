@@ -63,7 +63,9 @@ enum Action : uint32_t {
 
 // Boundary-condition kinds.  PULL_TL is the position-prescribed pull of
 // tensile.cpp:20-42: x = X + v*t, y = Y, vx = v, vy = 0, vx_t = vy_t = 0.
-enum BCKind : uint32_t { BC_PULL_TL = 1 };
+// VELOCITY_UL is the updated-Lagrangian form of tensile.cpp:44-66: x_t = v, y_t = 0,
+// vx = v, vy = 0, vx_t = vy_t = 0.
+enum BCKind : uint32_t { BC_PULL_TL = 1, BC_VELOCITY_UL = 2 };
 
 struct BC {
 	uint32_t kind = 0;

@@ -1110,9 +1110,16 @@ struct Body {
 void carry_out_bc(const Body& B, PSet& P, double t) {
 	for (const BC& bc : B.bcs) {
 		for (unsigned i : bc.idx) {
-			if (bc.kind == BC_PULL_TL) {
+			if (bc.kind == BC_PULL_TL) {  // left/right_bndry_fun_tl, tensile.cpp:20-42
 				P.x[i] = P.X[i] + bc.v * t;
 				P.y[i] = P.Y[i];
+				P.vx[i] = bc.v;
+				P.vy[i] = 0.;
+				P.vx_t[i] = 0.;
+				P.vy_t[i] = 0.;
+			} else if (bc.kind == BC_VELOCITY_UL) {  // left/right_bndry_fun_ul, tensile.cpp:44-66
+				P.x_t[i] = bc.v;
+				P.y_t[i] = 0.;
 				P.vx[i] = bc.v;
 				P.vy[i] = 0.;
 				P.vx_t[i] = 0.;

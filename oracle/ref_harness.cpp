@@ -162,6 +162,27 @@ void pull_bc(T* p) {
 	p->vx_t = 0.;
 	p->vy_t = 0.;
 }
+// the updated-Lagrangian form (tensile.cpp:44-66)
+template <typename T, int K>
+void vel_bc(T* p) {
+	double v = g_bc_speed[K];
+	p->x_t = v;
+	p->y_t = 0.;
+	p->vx = v;
+	p->vy = 0.;
+	p->vx_t = 0.;
+	p->vy_t = 0.;
+}
+template <typename T>
+void (*vel_fn(int k))(T*) {
+	switch (k) {
+	case 0: return &vel_bc<T, 0>;
+	case 1: return &vel_bc<T, 1>;
+	case 2: return &vel_bc<T, 2>;
+	case 3: return &vel_bc<T, 3>;
+	}
+	return nullptr;
+}
 template <typename T>
 void (*pull_fn(int k))(T*) {
 	switch (k) {
@@ -196,9 +217,12 @@ template <typename T>
 boundary_conditions<T> make_bcs(const BodyIn& in, int& slot) {
 	boundary_conditions<T> bc;
 	for (const BC& b : in.bcs) {
-		if (b.kind != BC_PULL_TL || slot >= 4) { fprintf(stderr, "unsupported boundary condition\n"); exit(2); }
+		if ((b.kind != BC_PULL_TL && b.kind != BC_VELOCITY_UL) || slot >= 4) {
+			fprintf(stderr, "unsupported boundary condition\n");
+			exit(2);
+		}
 		g_bc_speed[slot] = b.v;
-		bc.add_boundary_condition(b.idx, pull_fn<T>(slot));
+		bc.add_boundary_condition(b.idx, b.kind == BC_PULL_TL ? pull_fn<T>(slot) : vel_fn<T>(slot));
 		slot++;
 	}
 	return bc;
@@ -573,6 +597,62 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
 		for (auto& b : bodies) { c.bodies.push_back(capture(b)); b.add_action(&record_first_nbh<particle_ul>); }
 		c.nbodies = (uint32_t)bodies.size();
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+	} else if (name == "tensile_godunov" || name == "tensile_monaghan" || name == "rotation_monaghan") {
+		// UL plates pulled by the velocity conditions of tensile.cpp:44-66, and the
+		// spinning UL disc; both run as particle_monaghan bodies here (the Godunov
+		// actions take any particle_ul)
+		std::vector<body<particle_monaghan>> bm;
+		std::vector<body<particle_ul>> bu;
+		c.method = UL;
+		if (name == "tensile_godunov") {
+			bu = tensile_godunov(nbox);
+			c.actions = {RIEMANN_UPDATE_INTEGRATION_WEIGHTS, MATERIAL_EOS, DERIVE_VELOCITY, MATERIAL_STRESS_RATE_JAUMANN,
+			             GODUNOV_CONTINUITY, GODUNOV_MOMENTUM, CONTMECH_ADVECTION};  // tensile.cpp:126-132
+			fill_consts(c, bu[0].get_sim_data(), simulation_time::getInstance().get_dt());
+			c.bodies.push_back(capture(bu[0]));
+			bu[0].add_action(&record_first_nbh<particle_ul>);
+		} else {
+			bm = name == "tensile_monaghan" ? tensile_monaghan(nbox) : rotation_monaghan(nbox);
+			c.actions = ul_actions;  // tensile.cpp:437-447, rotation.cpp:338-348
+			fill_consts(c, bm[0].get_sim_data(), simulation_time::getInstance().get_dt());
+			c.bodies.push_back(capture(bm[0]));
+			bm[0].add_action(&record_first_nbh<particle_monaghan>);
+		}
+		if (name != "rotation_monaghan") {
+			// tensile.cpp:119-120 / :431-432; the Monaghan plate pulls three columns at
+			// each end (tensile.cpp:392-398), the Godunov plate one (:97-103)
+			const unsigned cols = name == "tensile_monaghan" ? 3 : 1;
+			BC l, r;
+			l.kind = r.kind = BC_VELOCITY_UL;
+			l.v = -10.; r.v = 10.;
+			for (unsigned i = 0; i < cols; i++)
+				for (unsigned j = 0; j < nbox; j++) {
+					l.idx.push_back(i * nbox + j);
+					r.idx.push_back((nbox - cols + i) * nbox + j);
+				}
+			c.bodies[0].bcs = {l, r};
+		}
+		c.nbodies = 1;
+		write_case(case_out, c);
+		Writer w(out);
+		write_header(w, c);
+		if (bu.empty()) run_loop(w, c, bm);
+		else run_loop(w, c, bu);
+	} else if (name == "rotation_tl") {
+		std::vector<body<particle_tl>> bodies = rotation_tl(nbox);
+		c.method = TL;
+		c.actions = {DERIVE_DISPLACEMENT, DERIVE_VELOCITY_TL, CONTMECH_VELOCITY_GRADIENT_TL, CONTMECH_CONTINUITY, MATERIAL_EOS,
+		             MATERIAL_STRESS_RATE_JAUMANN, CONTMECH_CAUCHY_TO_NOMINAL, DERIVE_STRESS_TL,
+		             CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY, CONTMECH_MOMENTUM_TL, CONTMECH_ADVECTION};  // rotation.cpp:196-206
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = bodies[0].get_particles()[0]->h;
+		c.bodies.push_back(capture(bodies[0]));
+		record_fixed_nbh(bodies[0].get_particles(), bodies[0].get_num_part(), 0);
+		c.nbodies = 1;
 		write_case(case_out, c);
 		Writer w(out);
 		write_header(w, c);

@@ -41,6 +41,10 @@ REFERENCE_CASES = [
     ("rings_potential_contact", 20, 5975),
     ("tensile_potential", 11, 25),
     ("rotation_potential", 15, 200),
+    ("tensile_godunov", 11, 25),
+    ("tensile_monaghan", 11, 25),
+    ("rotation_monaghan", 15, 20),
+    ("rotation_tl", 15, 100),
 ]
 
 

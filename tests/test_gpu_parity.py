@@ -56,11 +56,13 @@ def golden(name):
     return sc, ref
 
 
-UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm", "rings_godunov", "rotation_godunov"]
-# rings_godunov_contact is checked against the reference's own conditioning in
-# test_gpu_families.py: its result moves by 1e-5..1e-2 under 1-ulp input noise
+UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm", "rings_godunov", "rotation_godunov",
+            "tensile_monaghan", "rotation_monaghan"]
+# rings_godunov_contact and tensile_godunov are checked against the reference's own
+# conditioning in test_gpu_families.py: their results move by 1e-6..1e-2 under 1-ulp
+# input noise
 TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak", "rings_potential_contact",
-            "tensile_potential", "rotation_potential"]
+            "tensile_potential", "rotation_potential", "rotation_tl"]
 COROT_CASES = ["rings_corot_contact", "tensile_corot", "rotation_corot"]
 
 

@@ -12,7 +12,7 @@ from mfree_iwf_gb300 import scenarios as S
 CASES = ["rings_monaghan", "rings_monaghan_contact", "rings_tl_contact", "tensile_tl", "tensile_tl_weak",
          "c1_rings_dx4mm", "c2_rings_tl_dx4mm", "rings_corot_contact", "tensile_corot", "rotation_corot",
          "rings_godunov", "rings_godunov_contact", "rotation_godunov", "rings_potential_contact", "tensile_potential",
-         "rotation_potential"]
+         "rotation_potential", "tensile_godunov", "tensile_monaghan", "rotation_monaghan", "rotation_tl"]
 
 
 @pytest.mark.parametrize("name", CASES)

@@ -23,6 +23,10 @@ BUILDERS = {
     "rings_potential_contact": lambda: S.rings_potential_contact(20),
     "tensile_potential": lambda: S.tensile_potential(11),
     "rotation_potential": lambda: S.rotation_potential(15),
+    "tensile_godunov": lambda: S.tensile_godunov(11),
+    "tensile_monaghan": lambda: S.tensile_monaghan(11),
+    "rotation_monaghan": lambda: S.rotation_monaghan(15),
+    "rotation_tl": lambda: S.rotation_tl(15),
 }
 
 
