@@ -19,6 +19,8 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 
 from .actions import (
+    RINGS_UL_WEAK_ACTIONS,
+    TENSILE_UL_WEAK_ACTIONS,
     RINGS_COROT_ACTIONS,
     RINGS_GODUNOV_ACTIONS,
     RINGS_MONAGHAN_ACTIONS,
@@ -36,7 +38,7 @@ M_1_PI = 0.31830988618379067154  # the C library's M_1_PI
 IN_NAMES = ("x", "y", "X", "Y", "m", "rho", "h", "quad_weight", "vx", "vy", "Sxx", "Sxy", "Syy")
 OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
 
-METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL, METHOD_UL_WEAK = 1, 2, 3, 4, 5, 6
 BC_PULL_TL = 1       # tensile.cpp:20-42 (total-Lagrangian bodies)
 BC_VELOCITY_UL = 2   # tensile.cpp:44-66 (updated-Lagrangian bodies)
 
@@ -81,6 +83,8 @@ class Body:
     # per-body constants overriding the scenario's (ensembles): keys of Scenario
     # (E, nu, rho0, dt, wdeltap, ...)
     params: Dict[str, float] = field(default_factory=dict)
+    # METHOD_UL_WEAK: the stress points, the same 13 arrays as the particles
+    gp: Optional[Dict[str, np.ndarray]] = None
 
     @property
     def n(self) -> int:
@@ -569,6 +573,119 @@ def c4_ensemble(n_instances: int = 512, seed: int = 20261203, dx_range=(2e-4, 1e
     return ens
 
 
+# ------------------------------------------------------------ UL weak form
+def element_map_rectangle(ex: int, ey: int) -> np.ndarray:
+    """element_map_rectangle (element.cpp:23-39): rows of (ll, lr, tr, tl) node
+    indices, ex elements per row, nodes numbered row by row with ex+1 per row."""
+    out = []
+    nx = ex + 1
+    inc = 0
+    for i in range(ey):
+        for _ in range(ex):
+            out.append((inc, inc + 1, inc + nx + 1, inc + nx))
+            inc += 1
+        inc = (i + 1) * nx
+    return np.array(out, dtype=np.int64).reshape(-1, 4)
+
+
+def mesh_ring(nbox: int, rin: float, rout: float):
+    """mesh_ring (benchmarks/utils.h:20-109): the lattice x = i dx - rout, y = j dx - rout
+    reduced to the quads whose four corners all lie strictly inside the annulus
+    (rin^2 < r^2 < rout^2), and to the nodes those quads use, renumbered in lattice
+    order.  Returns the nodes' x, y and the remapped (ll, lr, tr, tl) elements."""
+    dx = 2.0 * rout / (nbox - 1)
+    I, J = np.meshgrid(np.arange(nbox, dtype=np.float64), np.arange(nbox, dtype=np.float64), indexing="ij")
+    px = (I * dx - rout).ravel()
+    py = (J * dx - rout).ravel()
+    el = element_map_rectangle(nbox - 1, nbox - 1)
+    r = px * px + py * py
+    inside = (r < rout * rout) & (r > rin * rin)
+    el = el[inside[el].all(axis=1)]
+    used = np.zeros(len(px), bool)
+    used[el.ravel()] = True
+    new = np.cumsum(used) - 1
+    return px[used], py[used], new[el]
+
+
+def _gauss_centres(x: np.ndarray, y: np.ndarray, el: np.ndarray):
+    """The one-point Gauss rule of gauss_int(elements, 1) (gauss_integration.h:47-123):
+    the shape functions at the element centre are all 0.25 exactly, so each stress point
+    is 0.25 x_ll + 0.25 x_lr + 0.25 x_tr + 0.25 x_tl, summed in that order."""
+    gx = ((x[el[:, 0]] * 0.25 + x[el[:, 1]] * 0.25) + x[el[:, 2]] * 0.25) + x[el[:, 3]] * 0.25
+    gy = ((y[el[:, 0]] * 0.25 + y[el[:, 1]] * 0.25) + y[el[:, 2]] * 0.25) + y[el[:, 3]] * 0.25
+    return gx, gy
+
+
+def _ul_weak_body(x, y, X, Y, gx, gy, GX, GY, dx, hdx, rho0, vx=0.0, vy=0.0) -> Body:
+    a = _body_from_lists(x, y, X, Y)
+    g = _body_from_lists(gx, gy, GX, GY)
+    for d in (a, g):
+        d["rho"][:] = rho0
+        d["h"][:] = hdx * dx
+        d["m"][:] = dx * dx * rho0
+        d["quad_weight"][:] = d["m"] / d["rho"]
+    a["vx"][:] = vx
+    a["vy"][:] = vy
+    b = Body(a)
+    b.gp = g
+    return b
+
+
+def _ul_weak_scenario(bodies, actions, dt, dx, name, contact=0) -> Scenario:
+    # correction_constants(.., 0, true): velocity smoothing on, the rest zero;
+    # candidates by find_neighbors(.., 1.5*dx, distance_manhattan)
+    sc = Scenario(method=METHOD_UL_WEAK, bodies=bodies, actions=list(actions), dt=dt, nu=0.4, E=1e7, rho0=1.0,
+                  do_smooth=1, contact=contact, name=name)
+    sc.nbh_h = 1.5 * dx
+    return sc
+
+
+def tensile_ul_weak(nbox: int) -> Scenario:
+    """The reference's tensile_ul_weak(nbox), tensile.cpp:626-729: the plate lattice with
+    one stress point per cell centre, velocity conditions on the end columns."""
+    dx = 1.0 / (nbox - 1)
+    I, J = np.meshgrid(np.arange(nbox, dtype=np.float64), np.arange(nbox, dtype=np.float64), indexing="ij")
+    x, y = (I * dx).ravel(), (J * dx).ravel()
+    I, J = np.meshgrid(np.arange(nbox - 1, dtype=np.float64), np.arange(nbox - 1, dtype=np.float64), indexing="ij")
+    gx, gy = (I * dx + dx / 2).ravel(), (J * dx + dx / 2).ravel()
+    b = _ul_weak_body(x, y, None, None, gx, gy, None, None, dx, 1.0, 1.0)
+    left = np.arange(nbox, dtype=np.uint32)
+    right = (np.uint32(nbox - 1) * np.uint32(nbox) + left).astype(np.uint32)
+    b.bcs = [BC(BC_VELOCITY_UL, -10.0, left), BC(BC_VELOCITY_UL, 10.0, right)]
+    return _ul_weak_scenario([b], TENSILE_UL_WEAK_ACTIONS, 1e-6, dx, f"tensile_ul_weak({nbox})")
+
+
+def rotation_ul_weak(nbox: int) -> Scenario:
+    """The reference's rotation_ul_weak(nbox), rotation.cpp:466-535: mesh_ring(nbox, 0, 1)
+    with one stress point per quad, spinning at 50 m/s rim speed."""
+    ro = 1.0
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, 0.0, ro)
+    gx, gy = _gauss_centres(x, y, el)
+    b = _ul_weak_body(x, y, x, y, gx, gy, gx, gy, dx, 1.0, 1.0, vx=-y / ro * 50, vy=+x / ro * 50)
+    return _ul_weak_scenario([b], RINGS_UL_WEAK_ACTIONS, 1e-6, dx, f"rotation_ul_weak({nbox})")
+
+
+def rings_ul_weak_contact(nbox: int) -> Scenario:
+    """The reference's rings_ul_weak_contact(nbox), rings.cpp:817-934: two meshed rings
+    (mesh_ring, r 0.03-0.04 m) at +-(ro + 1 mm), one stress point per quad, 180 m/s
+    each, penalty contact on their hulls.  The shift applies to x only: X keeps the
+    unshifted positions, as the reference's does."""
+    ri, ro = 0.03, 0.04
+    spacing = ro + 0.001
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, ri, ro)
+    gx, gy = _gauss_centres(x, y, el)
+    bodies = []
+    for sgn, v in ((-1.0, 180.0), (1.0, -180.0)):
+        xs = x - spacing if sgn < 0 else x + spacing
+        gxs = gx - spacing if sgn < 0 else gx + spacing
+        b = _ul_weak_body(xs, y, x, y, gxs, gy, gx, gy, dx, 1.0, 1.0, vx=v)
+        b.hull = convex_hull(xs, y)
+        bodies.append(b)
+    return _ul_weak_scenario(bodies, RINGS_UL_WEAK_ACTIONS, 1e-7, dx, f"rings_ul_weak_contact({nbox})", contact=1)
+
+
 # ---------------------------------------------------------------- case files
 def write_case(path: str, sc: Scenario, nsteps: int, dump_every: int = 0) -> None:
     """Write the binary case file read by the oracle (oracle/mfcase.h)."""
@@ -596,6 +713,11 @@ def write_case(path: str, sc: Scenario, nsteps: int, dump_every: int = 0) -> Non
             u32(bc.kind); f64(bc.v); u32(len(bc.idx))
             out.extend(np.ascontiguousarray(bc.idx, np.uint32).tobytes())
         u32(b.ex); u32(b.ey)
+        if sc.method == METHOD_UL_WEAK:
+            ng = len(b.gp["x"])
+            u32(ng)
+            for k in IN_NAMES:
+                out.extend(np.ascontiguousarray(b.gp[k], np.float64).tobytes())
     with open(path, "wb") as f:
         f.write(bytes(out))
 
@@ -640,7 +762,11 @@ def read_case(path: str) -> Scenario:
             kind = u32(); v = f64(); idx = arr(np.uint32, u32())
             bcs.append(BC(kind, v, idx))
         ex, ey = u32(), u32()
-        bodies.append(Body(a, hull, bcs, ex, ey))
+        body = Body(a, hull, bcs, ex, ey)
+        if method == METHOD_UL_WEAK:
+            ng = u32()
+            body.gp = {k: arr(np.float64, ng) for k in IN_NAMES}
+        bodies.append(body)
     sc = Scenario(method=method, bodies=bodies, actions=[int(a) for a in actions], dt=dt, nu=vals[0], E=vals[1],
                   rho0=vals[2], wdeltap=vals[3], corr_exp=vals[4], mghn_eps=vals[5], alpha=vals[6], beta=vals[7],
                   eta=vals[8], xsph_eps=vals[9], do_smooth=do_smooth, nbh_h=nbh_h, nbh_eps=nbh_eps, gp_h=gp_h,

@@ -20,7 +20,7 @@
 
 namespace mfcase {
 
-enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3, COROT = 4, POTENTIAL = 5 };
+enum Method : uint32_t { UL = 1, TL = 2, TL_WEAK = 3, COROT = 4, POTENTIAL = 5, UL_WEAK = 6 };
 
 // Action identifiers; the numbering is the C ABI's mf_action (include/mfree_gb300.h).
 enum Action : uint32_t {
@@ -58,7 +58,13 @@ enum Action : uint32_t {
 	GODUNOV_CONTINUITY = 32,
 	GODUNOV_MOMENTUM = 33,
 	POTENTIAL_COMP_ELASTIC_POTENTIAL = 34,
-	ACTION_MAX = 35
+	RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP = 35,
+	DERIVE_STRESS_WEAK_UL = 36,
+	DERIVE_VELOCITY_WEAK = 37,
+	CONTMECH_MOMENTUM_UL_WEAK = 38,
+	INTERPOLATION_INTERPOLATE_VELOCITY = 39,
+	CONTMECH_ADVECTION_GP = 40,
+	ACTION_MAX = 41
 };
 
 // Boundary-condition kinds.  PULL_TL is the position-prescribed pull of
@@ -86,6 +92,9 @@ struct BodyIn {
 	std::vector<uint32_t> hull;
 	std::vector<BC> bcs;
 	uint32_t ex = 0, ey = 0;  // TL_WEAK: element_map_rectangle(ex, ey), 2x2 Gauss points
+	// UL_WEAK: the stress points (their NIN arrays), present in the file for that method only
+	uint32_t ngp = 0;
+	std::vector<double> g[NIN];
 };
 
 struct Case {
@@ -100,6 +109,7 @@ struct Case {
 	double nbh_h = 0.;     // TL/TL_WEAK: the h given to find_neighbors (neighbor_search.h:116)
 	double nbh_eps = 1e-6; // absolute epsilon of the neighbour predicate (grid.h:157, neighbor_search.h:41)
 	double gp_h = 0., gp_rho = 0.;  // TL_WEAK: h and rho given to the Gauss points (tensile.cpp:792-795)
+	                                // (UL_WEAK: nbh_h is the h of the Manhattan candidate search)
 	std::vector<BodyIn> bodies;
 };
 
@@ -150,6 +160,10 @@ inline Case read_case(const char* path) {
 			r.vu32(bc.idx, k);
 		}
 		b.ex = r.u32(); b.ey = r.u32();
+		if (c.method == UL_WEAK) {
+			b.ngp = r.u32();
+			for (int k = 0; k < NIN; k++) r.vf64(b.g[k], b.ngp);
+		}
 	}
 	return c;
 }

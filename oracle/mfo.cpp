@@ -51,10 +51,12 @@ struct PSet {
 	std::vector<unsigned> num_nbh, nbh;  // nbh[slot*MAX_NBH + k]
 	std::vector<double> w, w_x, w_y;
 	std::vector<double> wji_x, wji_y;  // particle_potential: grad W of the reverse pair (particle.h:101)
+	std::vector<unsigned> num_cand, cand;  // particle_ul_weak: candidate neighbours (particle.h:135-136)
 
 	void resize(unsigned nn) {
 		n = nn;
-		for (auto* v : {&idx, &hash, &num_nbh}) v->assign(n, 0u);
+		for (auto* v : {&idx, &hash, &num_nbh, &num_cand}) v->assign(n, 0u);
+		cand.assign((size_t)n * MAX_NBH, 0u);
 		for (auto* v : {&x, &y, &X, &Y, &m, &rho, &h, &qw, &p, &vx, &vy, &Sxx, &Sxy, &Syy, &vx_x, &vx_y, &vy_x, &vy_y,
 		                &x_t, &y_t, &rho_t, &vx_t, &vy_t, &Sxx_t, &Sxy_t, &Syy_t, &fcx, &fcy, &Sxx_x, &Sxy_y, &Sxy_x,
 		                &Syy_y, &Rxx, &Rxy, &Ryy, &Ryx, &Hxx, &Hxy, &Hyx, &Hyy, &Fdxx, &Fdxy, &Fdyx, &Fdyy, &Pxx, &Pxy, &Pyx,
@@ -77,8 +79,8 @@ struct PSet {
 };
 
 // particle::copy_into (particle.cpp:45-74) plus the particle_tl (:106-116),
-// particle_potential (:156-163) and particle_monaghan (:219-228) overrides: the union
-// of the fields they copy.
+// particle_potential (:156-163), particle_ul_weak (:195-203) and particle_monaghan
+// (:219-228) overrides: the union of the fields they copy.
 void copy_into(const PSet& a, unsigned s, PSet& b, unsigned d) {
 	b.idx[d] = a.idx[s]; b.hash[d] = a.hash[s];
 	b.m[d] = a.m[s]; b.rho[d] = a.rho[s]; b.h[d] = a.h[s]; b.qw[d] = a.qw[s]; b.p[d] = a.p[s];
@@ -96,6 +98,9 @@ void copy_into(const PSet& a, unsigned s, PSet& b, unsigned d) {
 	}
 	b.Pxx[d] = a.Pxx[s]; b.Pxy[d] = a.Pxy[s]; b.Pyx[d] = a.Pyx[s]; b.Pyy[d] = a.Pyy[s];
 	b.Rxx[d] = a.Rxx[s]; b.Rxy[d] = a.Rxy[s]; b.Ryy[d] = a.Ryy[s]; b.Ryx[d] = a.Ryx[s];
+	unsigned nc = a.num_cand[s];
+	b.num_cand[d] = nc;
+	for (unsigned k = 0; k < nc; k++) b.cand[dof + k] = a.cand[so + k];
 }
 
 struct Fail {
@@ -437,6 +442,93 @@ void find_neighbors(PSet& to, const PSet& from, double h, double eps) {
 		}
 		if (!(nbh_iter < MAX_NBH)) throw Fail{"find_neighbors: overflow (neighbor_search.h:142)"};
 		if (!(nbh_iter > 0)) throw Fail{"find_neighbors: no neighbours (neighbor_search.h:143)"};
+		to.num_nbh[i] = nbh_iter;
+	}
+}
+
+// find_neighbors with distance_manhattan into the candidate lists of particle_ul_weak
+// (neighbor_search.h:43-48, 84-113, 150-180): every "from" point with
+// |dx| < 2h + 1e-6 and |dy| < 2h + 1e-6, ascending
+void find_candidates(PSet& to, const PSet& from, double h) {
+	for (unsigned i = 0; i < to.n; i++) {
+		double xi = to.x[i], yi = to.y[i];
+		unsigned nbh_iter = 0;
+		for (unsigned j = 0; j < from.n; j++) {
+			double xij = xi - from.x[j];
+			double yij = yi - from.y[j];
+			if (fabs(xij) < 2. * h + 1e-6 && fabs(yij) < 2. * h + 1e-6) {
+				if (nbh_iter >= MAX_NBH) throw Fail{"find_neighbors: overflow (neighbor_search.h:176)"};
+				to.cand[(size_t)i * MAX_NBH + nbh_iter] = j;
+				nbh_iter++;
+			}
+		}
+		if (!(nbh_iter < MAX_NBH)) throw Fail{"find_neighbors: overflow (neighbor_search.h:176)"};
+		if (!(nbh_iter > 0)) throw Fail{"find_neighbors: no neighbours (neighbor_search.h:177)"};
+		to.num_cand[i] = nbh_iter;
+	}
+}
+
+// eigen, neighbor_ellipse.h:29-60: eigenvalues of the symmetric 2x2 A, ascending, and
+// unit eigenvectors as the columns of V (only D[0][0], D[1][1] are set)
+void eigen2(const glm::dmat2x2& A, glm::dmat2x2& V, glm::dmat2x2& D) {
+	if (fabs(A[1][0]) < 1e-9 && fabs(A[0][1]) < 1e-9) {
+		V = glm::dmat2x2(1.);
+		D = glm::dmat2x2(A[0][0], 0., 0., A[1][1]);
+		return;
+	}
+	double T = A[0][0] + A[1][1];
+	double det = glm::determinant(A);
+	double L1 = T / 2 + sqrt(T * T / 4 - det);
+	double L2 = T / 2 - sqrt(T * T / 4 - det);
+	double lambda1 = fmin(L1, L2);
+	double lambda2 = fmax(L1, L2);
+	D[0][0] = lambda1;
+	D[1][1] = lambda2;
+	if (fabs(A[1][0]) > 1e-12) {
+		glm::dvec2 v1 = glm::normalize(glm::dvec2(lambda1 - A[1][1], A[0][1]));
+		glm::dvec2 v2 = glm::normalize(glm::dvec2(lambda2 - A[1][1], A[0][1]));
+		V = glm::dmat2x2(v1, v2);
+	} else {
+		glm::dvec2 v1 = glm::normalize(glm::dvec2(A[1][0], lambda1 - A[0][0]));
+		glm::dvec2 v2 = glm::normalize(glm::dvec2(A[1][0], lambda2 - A[0][0]));
+		V = glm::dmat2x2(v1, v2);
+	}
+}
+
+// nbh_ellipse, neighbor_ellipse.h:62-127: h = half the largest candidate distance; the
+// neighbours are the candidates inside the ellipse of semi-axes 1.6651 sqrt(lambda)
+// along the eigenvectors of the candidates' mean offset product
+void nbh_ellipse(PSet& to, const PSet& from) {
+	for (unsigned i = 0; i < to.n; i++) {
+		double px = to.x[i], py = to.y[i];
+		double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
+		double h = 0.;
+		unsigned nc = to.num_cand[i];
+		for (unsigned j = 0; j < nc; j++) {
+			unsigned jdx = to.cand[(size_t)i * MAX_NBH + j];
+			double dx = px - from.x[jdx], dy = py - from.y[jdx];
+			double r2 = dx * dx + dy * dy;
+			h = fmax(h, r2);
+			Hxx += dx * dx; Hxy += dx * dy;
+			Hyx += dy * dx; Hyy += dy * dy;
+		}
+		h = sqrt(h);
+		h /= 2;
+		to.h[i] = h;
+		glm::dmat2x2 V, D;
+		eigen2(glm::dmat2x2(Hxx / nc, Hyx / nc, Hxy / nc, Hyy / nc), V, D);
+		double a = 1.6651 * sqrt(D[0][0]);
+		double b = 1.6651 * sqrt(D[1][1]);
+		double phi = atan2(V[0][1], V[0][0]);
+		unsigned nbh_iter = 0;
+		for (unsigned j = 0; j < nc; j++) {
+			unsigned jdx = to.cand[(size_t)i * MAX_NBH + j];
+			double xc = from.x[jdx] - px, yc = from.y[jdx] - py;
+			double left = ((cos(phi) * xc + sin(phi) * yc) / a);
+			double right = ((sin(phi) * xc - cos(phi) * yc) / b);
+			if (left * left + right * right <= 1) to.nbh[(size_t)i * MAX_NBH + nbh_iter++] = jdx;
+		}
+		if (!(nbh_iter > 0)) throw Fail{"nbh_ellipse: no neighbours (neighbor_ellipse.h:125)"};
 		to.num_nbh[i] = nbh_iter;
 	}
 }
@@ -980,6 +1072,71 @@ void a_potential(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
 	}
 }
 
+// riemann_update_integration_weights_gp, riemann_integration.h:21-26
+void a_riemann_gp(Ctx&, PSet&, const std::vector<unsigned>&, PSet* Q) {
+	for (unsigned i = 0; i < Q->n; i++) Q->qw[i] = Q->m[i] / Q->rho[i];
+}
+// derive_stress_weak_ul, derivatives.h:296-329: each stress point scatters its stress
+// times the shape-function gradient onto its particle neighbours, ascending
+void a_stress_weak_ul(Ctx&, PSet& P, const std::vector<unsigned>&, PSet* Q) {
+	for (unsigned i = 0; i < P.n; i++) { P.Sxx_x[i] = 0.; P.Sxy_y[i] = 0.; P.Sxy_x[i] = 0.; P.Syy_y[i] = 0.; }
+	for (unsigned i = 0; i < Q->n; i++) {
+		double Sxxi = Q->Sxx[i] - Q->p[i], Sxyi = Q->Sxy[i], Syyi = Q->Syy[i] - Q->p[i];
+		double qw = Q->qw[i];
+		for (unsigned j = 0; j < Q->num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = Q->nbh[o];
+			double vol_node = P.qw[jdx];
+			P.Sxx_x[jdx] -= Sxxi * Q->w_x[o] * qw * vol_node;
+			P.Sxy_y[jdx] -= Sxyi * Q->w_y[o] * qw * vol_node;
+			P.Sxy_x[jdx] -= Sxyi * Q->w_x[o] * qw * vol_node;
+			P.Syy_y[jdx] -= Syyi * Q->w_y[o] * qw * vol_node;
+		}
+	}
+}
+// derive_velocity_weak, derivatives.h:68-99: stress-point velocity gradients
+void a_vel_weak(Ctx&, PSet& P, const std::vector<unsigned>&, PSet* Q) {
+	for (unsigned i = 0; i < Q->n; i++) {
+		double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+		for (unsigned j = 0; j < Q->num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = Q->nbh[o];
+			double vxj = P.vx[jdx], vyj = P.vy[jdx], qw = P.qw[jdx];
+			vx_x += vxj * Q->w_x[o] * qw;
+			vx_y += vxj * Q->w_y[o] * qw;
+			vy_x += vyj * Q->w_x[o] * qw;
+			vy_y += vyj * Q->w_y[o] * qw;
+		}
+		Q->vx_x[i] = vx_x; Q->vx_y[i] = vx_y; Q->vy_x[i] = vy_x; Q->vy_y[i] = vy_y;
+	}
+}
+// contmech_momentum_ul_weak, cont_mech.h:51-68
+void a_momentum_ul_weak(Ctx&, PSet& P, const std::vector<unsigned>&, PSet*) {
+	for (unsigned i = 0; i < P.n; i++) {
+		double m = P.m[i];
+		P.vx_t[i] += 1. / m * (P.Sxx_x[i] + P.Sxy_y[i]) + P.fcx[i] / P.m[i];
+		P.vy_t[i] += 1. / m * (P.Sxy_x[i] + P.Syy_y[i]) + P.fcy[i] / P.m[i];
+	}
+}
+// interpolation_interpolate_velocity, interpolation.h:32-59
+void a_interp_vel(Ctx&, PSet& P, const std::vector<unsigned>&, PSet* Q) {
+	for (unsigned i = 0; i < Q->n; i++) {
+		double vxi = 0., vyi = 0.;
+		for (unsigned j = 0; j < Q->num_nbh[i]; j++) {
+			size_t o = (size_t)i * MAX_NBH + j;
+			unsigned jdx = Q->nbh[o];
+			vxi += P.vx[jdx] * Q->w[o] * P.qw[jdx];
+			vyi += P.vy[jdx] * Q->w[o] * P.qw[jdx];
+		}
+		Q->vx[i] = vxi;
+		Q->vy[i] = vyi;
+	}
+}
+// contmech_advection_gp, cont_mech.h:144-152
+void a_advection_gp(Ctx&, PSet&, const std::vector<unsigned>&, PSet* Q) {
+	for (unsigned i = 0; i < Q->n; i++) { Q->x_t[i] += Q->vx[i]; Q->y_t[i] += Q->vy[i]; }
+}
+
 ActFn action_fn(uint32_t a) {
 	switch (a) {
 	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return a_riemann;
@@ -1016,6 +1173,12 @@ ActFn action_fn(uint32_t a) {
 	case GODUNOV_CONTINUITY: return a_godunov_continuity;
 	case GODUNOV_MOMENTUM: return a_godunov_momentum;
 	case POTENTIAL_COMP_ELASTIC_POTENTIAL: return a_potential;
+	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP: return a_riemann_gp;
+	case DERIVE_STRESS_WEAK_UL: return a_stress_weak_ul;
+	case DERIVE_VELOCITY_WEAK: return a_vel_weak;
+	case CONTMECH_MOMENTUM_UL_WEAK: return a_momentum_ul_weak;
+	case INTERPOLATION_INTERPOLATE_VELOCITY: return a_interp_vel;
+	case CONTMECH_ADVECTION_GP: return a_advection_gp;
 	}
 	throw Fail{"unknown action id"};
 }
@@ -1163,6 +1326,18 @@ struct Sim {
 		} else if (c.method == TL || c.method == COROT || c.method == POTENTIAL) {
 			carry_out_bc(B, P, ctx.time);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, nullptr);
+		} else if (c.method == UL_WEAK) {
+			// body.h:80-108: this stage's neighbourhoods and shape functions, the
+			// actions, then the boundary conditions
+			PSet& Q = B.kq[s];
+			for (unsigned i = 0; i < Q.n; i++) Q.reset(i);
+			nbh_ellipse(P, P);
+			nbh_ellipse(Q, P);
+			precomp_rkpm(Q, P);
+			precomp_rkpm(P, P);
+			if (!recorded && s == 0) record_nbh(P, perm, b);
+			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, &Q);
+			carry_out_bc(B, P, ctx.time);
 		} else {
 			PSet& Q = B.kq[s];
 			for (unsigned i = 0; i < Q.n; i++) Q.reset(i);
@@ -1190,7 +1365,7 @@ struct Sim {
 	void step_body(unsigned b) {
 		Body& B = bodies[b];
 		double m_dt = c.dt;
-		bool weak = c.method == TL_WEAK;
+		bool weak = c.method == TL_WEAK || c.method == UL_WEAK;
 		for (unsigned i = 0; i < B.n; i++) copy_into(B.P, i, B.k[0], i);
 		if (weak) for (unsigned i = 0; i < B.Q.n; i++) copy_into(B.Q, i, B.kq[0], i);
 		const double fr[3] = {0.5, 0.5, 1.0};
@@ -1227,9 +1402,18 @@ struct Sim {
 				Q.Sxy[i] += m_dt * 1. / 6. * (q1->Sxy_t[i] + 2 * q2->Sxy_t[i] + 2 * q3->Sxy_t[i] + q4->Sxy_t[i]);
 				Q.Syy[i] += m_dt * 1. / 6. * (q1->Syy_t[i] + 2 * q2->Syy_t[i] + 2 * q3->Syy_t[i] + q4->Syy_t[i]);
 			}
-			ctx.time += m_dt;  // rk4.h:214
+			ctx.time += m_dt;  // rk4.h:194 / :214
 			carry_out_bc(B, P, ctx.time);
-			if (c.do_smooth) smooth_vel(B);
+			if (c.method == UL_WEAK) {
+				if (c.do_smooth) {  // rk4.h:198-204: fresh neighbourhoods and weights first
+					nbh_ellipse(P, P);
+					for (unsigned i = 0; i < P.n; i++) P.qw[i] = P.m[i] / P.rho[i];
+					precomp_rkpm(P, P);
+					smooth_vel(B);
+				}
+			} else if (c.do_smooth) {
+				smooth_vel(B);
+			}
 		} else {
 			carry_out_bc(B, P, ctx.time);  // rk4.h:105
 			ctx.time += m_dt;              // rk4.h:107
@@ -1333,9 +1517,19 @@ struct Sim {
 			} else if (c.method == TL_WEAK) {
 				setup_weak(B, in);
 				record_nbh(B.P, ident(B.n), b);
+			} else if (c.method == UL_WEAK) {
+				// the stress points as given; candidates by the Manhattan search
+				// (tensile.cpp:706-707, rings.cpp:900-904)
+				B.Q.resize(in.ngp);
+				for (int s = 0; s < 4; s++) B.kq[s].resize(in.ngp);
+				std::vector<double>* gd[NIN] = {&B.Q.x, &B.Q.y, &B.Q.X, &B.Q.Y, &B.Q.m, &B.Q.rho, &B.Q.h, &B.Q.qw,
+				                                &B.Q.vx, &B.Q.vy, &B.Q.Sxx, &B.Q.Sxy, &B.Q.Syy};
+				for (int a = 0; a < NIN; a++) *gd[a] = in.g[a];
+				find_candidates(B.P, B.P, c.nbh_h);
+				find_candidates(B.Q, B.P, c.nbh_h);
 			}
 		}
-		if (c.method != UL) recorded = true;
+		if (c.method != UL && c.method != UL_WEAK) recorded = true;
 	}
 
 	// tensile.cpp:776-807: element map, 2x2 Gauss points, neighbours, RKPM

@@ -24,6 +24,7 @@
 #include "benchmarks/rings.h"
 #include "benchmarks/tensile.h"
 #include "benchmarks/rotation.h"
+#include "interpolation.h"
 
 #include "vtk_writer.h"
 
@@ -52,6 +53,29 @@ void record_first_nbh(body<T>& b) {
 		for (unsigned j = 0; j < p[i]->num_nbh; j++) L[p[i]->idx].push_back(p[p[i]->nbh[j]]->idx);
 }
 
+// The stress points of a particle_ul_weak body as its builder made them: the body
+// keeps them private, so this action (run after the others) copies them at the first
+// derivative evaluation, where the stage copies still hold the built values except
+// h (set by the neighbour search) and the velocity (set by
+// interpolation_interpolate_velocity); neither is an input of the method, both are
+// written as zero.
+std::vector<BodyIn> g_gp;
+std::vector<bool> g_gp_done;
+template <typename T>
+void capture_gp(body<T>& b) {
+	if (g_gp_done[g_cur_body]) return;
+	g_gp_done[g_cur_body] = true;
+	BodyIn& g = g_gp[g_cur_body];
+	T** q = b.get_cur_quad_points();
+	g.n = b.get_num_quad_points();
+	for (int k = 0; k < NIN; k++) g.a[k].resize(g.n);
+	for (unsigned i = 0; i < g.n; i++) {
+		double f[NIN] = {q[i]->x, q[i]->y, q[i]->X, q[i]->Y, q[i]->m, q[i]->rho, 0., q[i]->quad_weight,
+		                 0., 0., q[i]->Sxx, q[i]->Sxy, q[i]->Syy};
+		for (int k = 0; k < NIN; k++) g.a[k][i] = f[k];
+	}
+}
+
 template <typename T>
 void record_fixed_nbh(T** p, unsigned n, int b) {
 	auto& L = g_nbh[b];
@@ -66,6 +90,7 @@ typedef void (*TlAct)(body<particle_tl>&);
 typedef void (*WkAct)(body<particle_tl_weak>&);
 typedef void (*CrAct)(body<particle_corotational>&);
 typedef void (*PtAct)(body<particle_potential>&);
+typedef void (*UwAct)(body<particle_ul_weak>&);
 
 UlAct ul_action(uint32_t a) {
 	typedef particle_monaghan T;
@@ -94,6 +119,26 @@ PtAct pt_action(uint32_t a) {
 	case DERIVE_DISPLACEMENT: return &derive_displacement<T>;
 	case MATERIAL_COMPUTE_STRESS_GREEN_STVENANT: return &material_compute_stress_green_stvenant<T>;
 	case POTENTIAL_COMP_ELASTIC_POTENTIAL: return &potential_comp_elastic_potential<T>;
+	}
+	return nullptr;
+}
+UwAct uw_action(uint32_t a) {
+	typedef particle_ul_weak T;
+	switch (a) {
+	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS: return &riemann_update_integration_weights<T>;
+	case RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP: return &riemann_update_integration_weights_gp<T>;
+	case MATERIAL_EOS_GP: return &material_eos_gp<T>;
+	case DERIVE_STRESS_WEAK_UL: return &derive_stress_weak_ul<T>;
+	case DERIVE_VELOCITY_WEAK: return &derive_velocity_weak<T>;
+	case DERIVE_VELOCITY: return &derive_velocity<T>;
+	case MATERIAL_STRESS_RATE_JAUMANN_GP: return &material_stress_rate_jaumann_gp<T>;
+	case CONTMECH_MOMENTUM_UL: return &contmech_momentum_ul<T>;
+	case CONTMECH_MOMENTUM_UL_WEAK: return &contmech_momentum_ul_weak<T>;
+	case CONTMECH_CONTINUITY: return &contmech_continuity<T>;
+	case CONTMECH_CONTINUITY_GP: return &contmech_continuity_gp<T>;
+	case CONTMECH_ADVECTION: return &contmech_advection<T>;
+	case INTERPOLATION_INTERPOLATE_VELOCITY: return &interpolation_interpolate_velocity<T>;
+	case CONTMECH_ADVECTION_GP: return &contmech_advection_gp<T>;
 	}
 	return nullptr;
 }
@@ -400,6 +445,30 @@ int run_case(const Case& c, const char* out) {
 			}
 		}
 		run_loop(w, c, bodies);
+	} else if (c.method == UL_WEAK) {
+		typedef particle_ul_weak T;
+		std::vector<body<T>> bodies;
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			const BodyIn& in = c.bodies[b];
+			T** p = make_particles<T>(in);
+			BodyIn gin;
+			gin.n = in.ngp;
+			for (int k = 0; k < NIN; k++) gin.a[k] = in.g[k];
+			T** q = make_particles<T>(gin);
+			find_neighbors(p, in.n, c.nbh_h, distance_manhattan);
+			find_neighbors(p, in.n, q, in.ngp, c.nbh_h, distance_manhattan);
+			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot), q, in.ngp));
+		}
+		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
+			for (uint32_t a : c.actions) {
+				UwAct f = uw_action(a);
+				if (!f) { fprintf(stderr, "action %u not valid for UL_WEAK\n", a); return 2; }
+				bodies[b].add_action(f);
+			}
+			bodies[b].add_action(&record_first_nbh<T>);
+		}
+		run_loop(w, c, bodies);
 	} else if (c.method == TL_WEAK) {
 		typedef particle_tl_weak T;
 		std::vector<body<T>> bodies;
@@ -458,6 +527,10 @@ void write_case(const char* path, const Case& c) {
 			w.raw(bc.idx.data(), bc.idx.size() * 4);
 		}
 		w.u32(b.ex); w.u32(b.ey);
+		if (c.method == UL_WEAK) {
+			w.u32(b.ngp);
+			for (int k = 0; k < NIN; k++) w.raw(b.g[k].data(), b.ngp * 8);
+		}
 	}
 }
 
@@ -687,6 +760,46 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 		Writer w(out);
 		write_header(w, c);
 		run_loop(w, c, bodies);
+	} else if (name == "tensile_ul_weak" || name == "rotation_ul_weak" || name == "rings_ul_weak_contact") {
+		typedef particle_ul_weak T;
+		std::vector<body<T>> bodies = name == "tensile_ul_weak" ? tensile_ul_weak(nbox)
+		                              : (name == "rotation_ul_weak" ? rotation_ul_weak(nbox) : rings_ul_weak_contact(nbox));
+		c.method = UL_WEAK;
+		c.contact = name == "rings_ul_weak_contact";
+		// tensile.cpp:713-726; rotation.cpp:511-525 and rings.cpp:917-930 take the
+		// momentum of cont_mech.h:51-68
+		const uint32_t momentum = name == "tensile_ul_weak" ? CONTMECH_MOMENTUM_UL : CONTMECH_MOMENTUM_UL_WEAK;
+		c.actions = {RIEMANN_UPDATE_INTEGRATION_WEIGHTS, RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP, MATERIAL_EOS_GP,
+		             DERIVE_STRESS_WEAK_UL, DERIVE_VELOCITY_WEAK, DERIVE_VELOCITY, MATERIAL_STRESS_RATE_JAUMANN_GP,
+		             momentum, CONTMECH_CONTINUITY, CONTMECH_CONTINUITY_GP, CONTMECH_ADVECTION,
+		             INTERPOLATION_INTERPOLATE_VELOCITY, CONTMECH_ADVECTION_GP};
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = 1.5 * bodies[0].get_particles()[0]->h;  // find_neighbors(.., 1.5*dx, ..) with h = dx
+		g_gp.assign(bodies.size(), BodyIn());
+		g_gp_done.assign(bodies.size(), false);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			BodyIn in = capture(bodies[b]);
+			if (name == "tensile_ul_weak") {
+				BC l, r;  // tensile.cpp:688-690
+				l.kind = r.kind = BC_VELOCITY_UL;
+				l.v = -10.; r.v = 10.;
+				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+				in.bcs = {l, r};
+			}
+			c.bodies.push_back(in);
+			std::vector<void (*)(body<T>&)> acts;
+			bodies[b].add_action(&record_first_nbh<T>);
+			bodies[b].add_action(&capture_gp<T>);
+		}
+		c.nbodies = (uint32_t)bodies.size();
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			c.bodies[b].ngp = g_gp[b].n;
+			for (int k = 0; k < NIN; k++) c.bodies[b].g[k] = g_gp[b].a[k];
+		}
+		write_case(case_out, c);
 	} else if (name == "tensile_tl_weak") {
 		std::vector<body<particle_tl_weak>> bodies = tensile_tl_weak(nbox);
 		c.method = TL_WEAK;

@@ -45,6 +45,9 @@ REFERENCE_CASES = [
     ("tensile_monaghan", 11, 25),
     ("rotation_monaghan", 15, 20),
     ("rotation_tl", 15, 100),
+    ("tensile_ul_weak", 11, 25),
+    ("rotation_ul_weak", 21, 50),
+    ("rings_ul_weak_contact", 20, 450),
 ]
 
 

@@ -12,7 +12,8 @@ from mfree_iwf_gb300 import scenarios as S
 CASES = ["rings_monaghan", "rings_monaghan_contact", "rings_tl_contact", "tensile_tl", "tensile_tl_weak",
          "c1_rings_dx4mm", "c2_rings_tl_dx4mm", "rings_corot_contact", "tensile_corot", "rotation_corot",
          "rings_godunov", "rings_godunov_contact", "rotation_godunov", "rings_potential_contact", "tensile_potential",
-         "rotation_potential", "tensile_godunov", "tensile_monaghan", "rotation_monaghan", "rotation_tl"]
+         "rotation_potential", "tensile_godunov", "tensile_monaghan", "rotation_monaghan", "rotation_tl",
+         "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact"]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -38,7 +39,8 @@ def test_oracle_matches_reference_bitwise(name, oracle_bin, tmp_path):
 def test_golden_cases_exercise_contact_and_pull():
     r = S.read_result(os.path.join(GOLDEN, "rings_monaghan_contact.ref.out"))
     assert any(np.count_nonzero(b["fcx"]) > 0 for b in r.dumps[-1]["bodies"])
-    for name in ("rings_tl_contact", "rings_corot_contact", "rings_godunov_contact", "rings_potential_contact"):
+    for name in ("rings_tl_contact", "rings_corot_contact", "rings_godunov_contact", "rings_potential_contact",
+                 "rings_ul_weak_contact"):
         r = S.read_result(os.path.join(GOLDEN, f"{name}.ref.out"))
         assert any(np.count_nonzero(b["fcx"]) > 0 for b in r.dumps[-1]["bodies"]), name
     c = S.read_case(os.path.join(GOLDEN, "tensile_tl.case"))
