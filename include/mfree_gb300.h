@@ -60,8 +60,10 @@ typedef enum {
 	MF_METHOD_TL = 2,      /* particle_tl: total-Lagrangian SPH, fixed neighbours, Randles-Libersky correction */
 	MF_METHOD_TL_WEAK = 3, /* particle_tl_weak: weak-form TL with RKPM shape functions and Gauss points */
 	MF_METHOD_COROT = 4,   /* particle_corotational: TL neighbours, plain SPH weights, per-particle rotation (FP64 forms) */
-	MF_METHOD_POTENTIAL = 5 /* particle_potential: TL neighbours, symmetric Randles-Libersky weights, elastic-potential
+	MF_METHOD_POTENTIAL = 5, /* particle_potential: TL neighbours, symmetric Randles-Libersky weights, elastic-potential
 	                           pair forces (FP64 forms) */
+	MF_METHOD_UL_WEAK = 6   /* particle_ul_weak: weak-form UL with stress points (mf_set_stress_points), per-stage
+	                           neighbour ellipses from Manhattan candidates and RKPM shape functions (FP64 forms) */
 } mf_method;
 
 /* Arithmetic forms. */
@@ -106,7 +108,13 @@ typedef enum {
 	MF_DERIVE_STRESS_COROTATIONAL = 31,            /* derivatives.h:521-588 */
 	MF_GODUNOV_CONTINUITY = 32,                    /* godunov.h:144-187 (MF_METHOD_UL, FP64 forms) */
 	MF_GODUNOV_MOMENTUM = 33,                      /* godunov.h:86-142 (MF_METHOD_UL, FP64 forms) */
-	MF_POTENTIAL_COMP_ELASTIC_POTENTIAL = 34       /* potential.h:32-83 (MF_METHOD_POTENTIAL) */
+	MF_POTENTIAL_COMP_ELASTIC_POTENTIAL = 34,      /* potential.h:32-83 (MF_METHOD_POTENTIAL) */
+	MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP = 35, /* riemann_integration.h:21-26 (MF_METHOD_UL_WEAK) */
+	MF_DERIVE_STRESS_WEAK_UL = 36,                 /* derivatives.h:296-329 */
+	MF_DERIVE_VELOCITY_WEAK = 37,                  /* derivatives.h:68-99 */
+	MF_CONTMECH_MOMENTUM_UL_WEAK = 38,             /* cont_mech.h:51-68 */
+	MF_INTERPOLATION_INTERPOLATE_VELOCITY = 39,    /* interpolation.h:32-59 */
+	MF_CONTMECH_ADVECTION_GP = 40                  /* cont_mech.h:144-152 */
 } mf_action;
 
 /* Boundary-condition kinds (boundary_conditions<T> functors). */
@@ -170,6 +178,14 @@ MF_API mf_status mf_set_boundary(mf_ctx* ctx, int32_t body, const uint32_t* idx,
  * ((ex+1)*(ey+1) particles, ex+1 per row) with 2x2 Gauss points per element, whose h
  * and rho are gp_h and gp_rho (gauss_int, tensile.cpp:776-795). */
 MF_API mf_status mf_set_gauss_mesh(mf_ctx* ctx, int32_t body, uint32_t ex, uint32_t ey, double gp_h, double gp_rho);
+
+/* MF_METHOD_UL_WEAK: the body's stress points (the quad_points of body<particle_ul_weak>,
+ * body.h:216-217), n of them, with the particles' field layout (X, Y may be NULL).  Their
+ * candidate particles are found at the first step, as find_neighbors(particles, np,
+ * stress_points, ns, config.nbh_h, distance_manhattan) does (neighbor_search.h:84-113);
+ * the particles' own candidates likewise (:150-180).  Replaces body<T>(..., stress_points,
+ * ns) (tensile.cpp:711). */
+MF_API mf_status mf_set_stress_points(mf_ctx* ctx, int32_t body, const mf_particles* stress_points, uint32_t n);
 /* Convex hull (monotone chain, collinear points kept) of n points: the reference's
  * set-up for contact boundaries (convex_hull.h:62-95).  out_idx holds n entries. */
 MF_API mf_status mf_convex_hull(const double* x, const double* y, uint32_t n, uint32_t* out_idx, uint32_t* out_n);

@@ -22,7 +22,7 @@ from .actions import *  # noqa: F401,F403  (action ids)
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmfree_gb300.so")
 
-METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL = 1, 2, 3, 4, 5
+METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL, METHOD_UL_WEAK = 1, 2, 3, 4, 5, 6
 PREC_FP64_STRICT, PREC_FP64, PREC_MIXED = 0, 1, 2
 PRECISIONS = {"fp64_strict": PREC_FP64_STRICT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
 BC_PULL = 1       # tensile.cpp:20-42, TL-type bodies
@@ -102,6 +102,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_add_boundary_condition": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32, C.c_int32, C.c_double]),
         "mf_set_boundary": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32]),
         "mf_set_gauss_mesh": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_double, C.c_double]),
+        "mf_set_stress_points": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint32]),
         "mf_convex_hull": (C.c_int32, [_DP, _DP, C.c_uint32, _UP, _UP]),
         "mf_step": (C.c_int32, [C.c_void_p, C.c_int32]),
         "mf_synchronize": (C.c_int32, [C.c_void_p]),
@@ -257,6 +258,13 @@ class Simulation:
     def set_gauss_mesh(self, body: int, ex: int, ey: int, gp_h: float, gp_rho: float) -> None:
         self._check(self._lib.mf_set_gauss_mesh(self._h, body, ex, ey, gp_h, gp_rho), "mf_set_gauss_mesh")
 
+    def set_stress_points(self, body: int, arrays: Dict[str, np.ndarray]) -> None:
+        """The stress points of a METHOD_UL_WEAK body (the particles' 13 fields)."""
+        n = len(arrays["x"])
+        cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
+        p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
+        self._check(self._lib.mf_set_stress_points(self._h, body, ctypes.byref(p), n), "mf_set_stress_points")
+
     # -- stepping (mfree_iwf.cpp:84-97)
     def step(self, nsteps: int = 1) -> None:
         self._check(self._lib.mf_step(self._h, int(nsteps)), "mf_step")
@@ -406,4 +414,6 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
             sim.set_boundary(bid, b.hull)
         if sc.method == METHOD_TL_WEAK:
             sim.set_gauss_mesh(bid, b.ex, b.ey, sc.gp_h, sc.gp_rho)
+        if sc.method == METHOD_UL_WEAK:
+            sim.set_stress_points(bid, b.gp)
     return sim

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmfree_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-KERNEL_TUS = ["mf_ul.cu", "mf_tl.cu", "mf_contact.cu", "mf_weak.cu", "mf_corot.cu"]
+KERNEL_TUS = ["mf_ul.cu", "mf_tl.cu", "mf_contact.cu", "mf_weak.cu", "mf_corot.cu", "mf_ulweak.cu"]
 
 
 def nvcc() -> str:

@@ -115,6 +115,8 @@ struct HostBody {
 	std::vector<double> in[13];  // x y X Y m rho h qw vx vy Sxx Sxy Syy
 	uint32_t ex = 0, ey = 0;     // TL_WEAK: element_map_rectangle(ex, ey), 2x2 Gauss points
 	double gp_h = 0., gp_rho = 0.;
+	uint32_t n_sp = 0;           // UL_WEAK: stress points (mf_set_stress_points), same fields as `in`
+	std::vector<double> sp[13];
 };
 
 template <class T>
@@ -212,6 +214,13 @@ struct mf_ctx {
 	DevBuf<float2> g_w32, t_w32, p_w32;
 	bool do_smooth = false;
 
+	// UL_WEAK: stress points (state sets as the particles: base, accumulator, two stage
+	// sets), fixed candidate lists, per-evaluation ellipse masks and shape functions
+	DevBuf<uint32_t> uw_gbody, uw_pc_off, uw_pc_nbr, uw_gc_off, uw_gc_nbr, uw_tp_off, uw_tp_gp, uw_tp_slot, uw_bc_of;
+	DevBuf<uint8_t> uw_pmask, uw_gmask;
+	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_gm, uw_gqw;
+	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
+
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
 
@@ -279,6 +288,9 @@ inline uint32_t abit(int a) { return 1u << a; }
 mf_status validate_tl(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
 mf_status validate_potential(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
+mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
+mf_status uw_setup(mf_ctx* c);
+mf_status uw_step(mf_ctx* c);
 mf_status tl_setup(mf_ctx* c);
 mf_status weak_setup(mf_ctx* c);
 mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags);
@@ -463,6 +475,8 @@ mf_status finalize(mf_ctx* c) {
 		st = validate_corot(c, acts, c->flags);
 	} else if (c->cfg.method == MF_METHOD_POTENTIAL) {
 		st = validate_potential(c, acts, c->flags);
+	} else if (c->cfg.method == MF_METHOD_UL_WEAK) {
+		st = validate_ulweak(c, acts, c->flags);
 	} else {
 		st = validate_weak(c, acts, c->flags);
 	}
@@ -471,9 +485,10 @@ mf_status finalize(mf_ctx* c) {
 	// each step; the TL set-ups the pull form (tensile.cpp:20-42), applied per stage
 	for (auto& b : c->bodies)
 		for (auto& bc : b.bcs) {
-			if (c->cfg.method == MF_METHOD_UL && bc.kind != MF_BC_VELOCITY)
+			const bool ul = c->cfg.method == MF_METHOD_UL || c->cfg.method == MF_METHOD_UL_WEAK;
+			if (ul && bc.kind != MF_BC_VELOCITY)
 				return fail(c, MF_ERR_PIPELINE, "updated-Lagrangian bodies take MF_BC_VELOCITY conditions");
-			if (c->cfg.method != MF_METHOD_UL && bc.kind != MF_BC_PULL)
+			if (!ul && bc.kind != MF_BC_PULL)
 				return fail(c, MF_ERR_PIPELINE, "total-Lagrangian bodies take MF_BC_PULL conditions");
 		}
 
@@ -550,6 +565,9 @@ mf_status finalize(mf_ctx* c) {
 		if ((st = upload_bcs(c)) != MF_OK) return st;
 	} else if (c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL) {
 		mf_status s2 = tl_setup(c);
+		if (s2 != MF_OK) return s2;
+	} else if (c->cfg.method == MF_METHOD_UL_WEAK) {
+		mf_status s2 = uw_setup(c);
 		if (s2 != MF_OK) return s2;
 	} else {
 		mf_status s2 = weak_setup(c);
@@ -1103,10 +1121,12 @@ mf_status upload_bcs(mf_ctx* c) {
 // (or near) their body's particle box.
 mf_status build_lists(mf_ctx* c, const double* fx, const double* fy, const uint32_t* from_body, uint32_t n_from,
                       const double* tx, const double* ty, const uint32_t* to_body, uint32_t n_to, uint32_t cap,
-                      DevBuf<uint32_t>& off_out, DevBuf<uint32_t>& nbr_out, std::vector<uint32_t>& counts) {
+                      DevBuf<uint32_t>& off_out, DevBuf<uint32_t>& nbr_out, std::vector<uint32_t>& counts,
+                      bool manhattan) {
 	uint32_t nb = (uint32_t)c->bodies.size();
 	double h = c->cfg.nbh_h, eps = c->cfg.nbh_eps;
-	double reach = sqrt(h * h * 2 * 2 + eps) * (1. + 1e-9);
+	// the cell covers the predicate's reach: the radius, or the Manhattan half-width
+	double reach = (manhattan ? 2. * h + 1e-6 : sqrt(h * h * 2 * 2 + eps)) * (1. + 1e-9);
 	std::vector<Geom> g(nb);
 	uint32_t cells = 0;
 	for (uint32_t b = 0; b < nb; b++) {
@@ -1145,6 +1165,7 @@ mf_status build_lists(mf_ctx* c, const double* fx, const double* fy, const uint3
 	sa.keys = keys.p; sa.keys_sorted = keys_sorted.p; sa.vals = vals.p; sa.perm = perm.p; sa.cell_start = cstart.p;
 	sa.sort_tmp = tmp.p; sa.sort_tmp_bytes = tb; sa.sort_bits = bits;
 	sa.count = count.p; sa.status = c->d_status;
+	sa.manhattan = manhattan ? 1u : 0u;
 	auto search = [&](int pass) { return c->strict ? mf_strict::tl_search(sa, pass, c->stream) : mf_fast::tl_search(sa, pass, c->stream); };
 	CK(search(0));
 	mf_status st = check_status(c);
@@ -1257,12 +1278,12 @@ mf_status weak_setup(mf_ctx* c) {
 	// lists: Gauss points -> particles, particles -> particles, particles -> Gauss points
 	DevBuf<uint32_t> g_off, g_nbr, t_off, t_nbr;
 	std::vector<uint32_t> gc, pc, tc;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, c->cfg.max_nbh, g_off, g_nbr, gc)))
+	if ((st = build_lists(c, px, py, c->body_of.p, n, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, c->cfg.max_nbh, g_off, g_nbr, gc, false)))
 		return st;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->nbr_off, c->nbr, pc)))
+	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->nbr_off, c->nbr, pc, false)))
 		return st;
 	if ((st = build_lists(c, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, px, py, c->body_of.p, n, 8 * c->cfg.max_nbh, t_off,
-	                      t_nbr, tc)))
+	                      t_nbr, tc, false)))
 		return st;
 	uint64_t eg = g_nbr.n, ep = c->nbr.n, et = t_nbr.n;
 	// RKPM shape functions, FP64
@@ -1413,6 +1434,218 @@ mf_status weak_step(mf_ctx* c) {
 	if (c->do_smooth) {
 		if ((e = launch(5)) != cudaSuccess) return cuda_fail(c, e, "weak smoothing");
 		c->launches += 2;
+	}
+	return MF_OK;
+}
+
+// Weak updated-Lagrangian pipeline: a subsequence, in this order, of the reference's
+// list (tensile.cpp:713-726; rings.cpp:917-930 with the mass-divided momentum), with
+// the data dependencies present.  Ids 35-40 take the FLAG_UW_* bits.
+mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& flags) {
+	static const int order[] = {MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS, MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP,
+	                            MF_MATERIAL_EOS_GP, MF_DERIVE_STRESS_WEAK_UL, MF_DERIVE_VELOCITY_WEAK, MF_DERIVE_VELOCITY,
+	                            MF_MATERIAL_STRESS_RATE_JAUMANN_GP, MF_CONTMECH_MOMENTUM_UL, MF_CONTMECH_MOMENTUM_UL_WEAK,
+	                            MF_CONTMECH_CONTINUITY, MF_CONTMECH_CONTINUITY_GP, MF_CONTMECH_ADVECTION,
+	                            MF_INTERPOLATION_INTERPOLATE_VELOCITY, MF_CONTMECH_ADVECTION_GP};
+	if (c->cfg.precision == MF_PREC_MIXED) return fail(c, MF_ERR_PIPELINE, "the weak UL form runs in the FP64 forms");
+	flags = 0;
+	size_t pos = 0;
+	for (int32_t a : acts) {
+		while (pos < sizeof(order) / sizeof(order[0]) && order[pos] != a) pos++;
+		if (pos == sizeof(order) / sizeof(order[0]))
+			return fail(c, MF_ERR_PIPELINE, "action %d is not part of the weak UL pipeline or out of its order", a);
+		pos++;
+		switch (a) {
+		case MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP: flags |= FLAG_UW_RIEMANN_GP; break;
+		case MF_DERIVE_STRESS_WEAK_UL: flags |= FLAG_UW_STRESS; break;
+		case MF_DERIVE_VELOCITY_WEAK: flags |= FLAG_UW_VEL_WEAK; break;
+		case MF_CONTMECH_MOMENTUM_UL_WEAK: flags |= FLAG_UW_MOMENTUM_W; break;
+		case MF_INTERPOLATION_INTERPOLATE_VELOCITY: flags |= FLAG_UW_INTERP; break;
+		case MF_CONTMECH_ADVECTION_GP: flags |= FLAG_UW_ADVECTION_GP; break;
+		default: flags |= abit(a);
+		}
+	}
+	const bool mom = (flags & abit(MF_CONTMECH_MOMENTUM_UL)) || (flags & FLAG_UW_MOMENTUM_W);
+	if ((flags & abit(MF_CONTMECH_MOMENTUM_UL)) && (flags & FLAG_UW_MOMENTUM_W))
+		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_ul and contmech_momentum_ul_weak both add the stress forces");
+	if (mom && !(flags & FLAG_UW_STRESS))
+		return fail(c, MF_ERR_PIPELINE, "the momentum needs derive_stress_weak_ul before it");
+	if ((flags & (abit(MF_MATERIAL_STRESS_RATE_JAUMANN_GP) | abit(MF_CONTMECH_CONTINUITY_GP))) &&
+	    !(flags & FLAG_UW_VEL_WEAK))
+		return fail(c, MF_ERR_PIPELINE, "the stress points' Jaumann rate / continuity need derive_velocity_weak");
+	if ((flags & abit(MF_CONTMECH_CONTINUITY)) && !(flags & abit(MF_DERIVE_VELOCITY)))
+		return fail(c, MF_ERR_PIPELINE, "contmech_continuity needs derive_velocity before it");
+	if ((flags & FLAG_UW_ADVECTION_GP) && !(flags & FLAG_UW_INTERP))
+		return fail(c, MF_ERR_PIPELINE, "contmech_advection_gp needs interpolation_interpolate_velocity before it");
+	return MF_OK;
+}
+
+// Weak UL set-up: stress points, candidate lists by the Manhattan search
+// (tensile.cpp:706-707), the transposed stress-point candidates, per-candidate scratch.
+mf_status uw_setup(mf_ctx* c) {
+	const uint32_t n = c->n_total;
+	if (!(c->cfg.nbh_h > 0.)) return fail(c, MF_ERR_ARG, "the weak UL form needs config.nbh_h > 0 (the candidate search h)");
+	uint32_t ng = 0;
+	for (auto& b : c->bodies) {
+		if (b.n_sp == 0) return fail(c, MF_ERR_STATE, "a UL_WEAK body needs mf_set_stress_points");
+		ng += b.n_sp;
+	}
+	c->n_g = ng;
+	c->do_smooth = c->bodies[0].sd.do_smooth != 0;
+	std::vector<uint32_t> gb(ng);
+	std::vector<double> gv[13];
+	for (int k = 0; k < 13; k++) gv[k].reserve(ng);
+	for (size_t b = 0, o = 0; b < c->bodies.size(); b++) {
+		const HostBody& B = c->bodies[b];
+		for (uint32_t i = 0; i < B.n_sp; i++) gb[o++] = (uint32_t)b;
+		for (int k = 0; k < 13; k++) gv[k].insert(gv[k].end(), B.sp[k].begin(), B.sp[k].end());
+	}
+	auto up = [&](DevBuf<double>& d, const std::vector<double>& v) -> mf_status {
+		CK(d.alloc(v.size()));
+		CK(cudaMemcpy(d.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+		return MF_OK;
+	};
+	mf_status st;
+	CK(c->uw_gbody.alloc(ng));
+	CK(cudaMemcpy(c->uw_gbody.p, gb.data(), (size_t)ng * 4, cudaMemcpyHostToDevice));
+	// stress-point state: x y rho Sxx Sxy Syy (input fields 0 1 5 10 11 12)
+	const int gf[6] = {0, 1, 5, 10, 11, 12};
+	for (int q = 0; q < 6; q++) {
+		if ((st = up(c->uw_g[0][q], gv[gf[q]]))) return st;
+		for (int k = 1; k < 4; k++) CK(c->uw_g[k][q].alloc(ng));
+	}
+	if ((st = up(c->uw_gm, gv[4])) || (st = up(c->uw_gqw, gv[7]))) return st;
+	CK(c->uw_gh.alloc(ng)); CK(c->uw_gsig.alloc(4 * (size_t)ng));
+	// particles: the weights of the last riemann update (the input weights at first)
+	CK(c->uw_qwp.alloc(n));
+	CK(cudaMemcpy(c->uw_qwp.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
+	CK(c->uw_ph.alloc(n));
+	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
+	// candidate lists (CSR, ascending)
+	std::vector<uint32_t> pc, gc;
+	const double *px = c->sd[0][0].p, *py = c->sd[0][1].p;
+	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->uw_pc_off,
+	                      c->uw_pc_nbr, pc, true)))
+		return st;
+	if ((st = build_lists(c, px, py, c->body_of.p, n, c->uw_g[0][0].p, c->uw_g[0][1].p, c->uw_gbody.p, ng,
+	                      c->cfg.max_nbh, c->uw_gc_off, c->uw_gc_nbr, gc, true)))
+		return st;
+	const uint64_t ep = c->uw_pc_nbr.n, eg = c->uw_gc_nbr.n;
+	CK(c->uw_pmask.alloc(ep)); CK(c->uw_pw.alloc(ep)); CK(c->uw_pwx.alloc(ep)); CK(c->uw_pwy.alloc(ep));
+	CK(c->uw_gmask.alloc(eg)); CK(c->uw_gw.alloc(eg)); CK(c->uw_gwx.alloc(eg)); CK(c->uw_gwy.alloc(eg));
+	// per particle, the stress points whose candidates hold it (ascending) and the slot
+	std::vector<uint32_t> goff(ng + 1), gnbr(eg);
+	CK(cudaMemcpy(goff.data(), c->uw_gc_off.p, ((size_t)ng + 1) * 4, cudaMemcpyDeviceToHost));
+	if (eg) CK(cudaMemcpy(gnbr.data(), c->uw_gc_nbr.p, eg * 4, cudaMemcpyDeviceToHost));
+	std::vector<uint32_t> toff(n + 1, 0), tgp(eg), tslot(eg);
+	for (uint64_t q = 0; q < eg; q++) toff[gnbr[q] + 1]++;
+	for (uint32_t j = 0; j < n; j++) toff[j + 1] += toff[j];
+	std::vector<uint32_t> fill(toff.begin(), toff.end() - 1);
+	for (uint32_t i = 0; i < ng; i++)
+		for (uint32_t q = goff[i]; q < goff[i + 1]; q++) {
+			uint32_t t = fill[gnbr[q]]++;
+			tgp[t] = i;
+			tslot[t] = q;
+		}
+	CK(c->uw_tp_off.alloc(n + 1)); CK(c->uw_tp_gp.alloc(eg)); CK(c->uw_tp_slot.alloc(eg));
+	CK(cudaMemcpy(c->uw_tp_off.p, toff.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+	if (eg) {
+		CK(cudaMemcpy(c->uw_tp_gp.p, tgp.data(), eg * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_tp_slot.p, tslot.data(), eg * 4, cudaMemcpyHostToDevice));
+	}
+	// boundary conditions: the rows' index into the value list
+	if ((st = upload_bcs(c))) return st;
+	std::vector<uint32_t> bc_of(n, ~0u);
+	uint32_t k = 0;
+	for (auto& b : c->bodies)
+		for (auto& bc : b.bcs)
+			for (uint32_t i : bc.idx) bc_of[b.off + i] = k++;
+	CK(c->uw_bc_of.alloc(n));
+	CK(cudaMemcpy(c->uw_bc_of.p, bc_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+	return MF_OK;
+}
+
+UWArgs uw_args(mf_ctx* c, uint32_t stage) {
+	UWArgs a{};
+	a.n_p = c->n_total; a.n_g = c->n_g; a.stage = stage; a.flags = c->flags;
+	a.params = c->params.p; a.body_of = c->body_of.p; a.gbody_of = c->uw_gbody.p;
+	a.m = c->m.p; a.gm = c->uw_gm.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	a.qw_base = c->uw_qwp.p; a.gqw_base = c->uw_gqw.p;
+	auto soa = [&](int k) {
+		StateSoA s{};
+		s.x = c->sd[k][0].p; s.y = c->sd[k][1].p; s.vx = c->sd[k][2].p; s.vy = c->sd[k][3].p;
+		s.rho = c->sd[k][4].p; s.Sxx = c->sd[k][5].p; s.Sxy = c->sd[k][6].p; s.Syy = c->sd[k][7].p;
+		return s;
+	};
+	auto gsoa = [&](int k) {
+		GSoA g{c->uw_g[k][0].p, c->uw_g[k][1].p, c->uw_g[k][2].p, c->uw_g[k][3].p, c->uw_g[k][4].p, c->uw_g[k][5].p};
+		return g;
+	};
+	// stage 0 reads the particles themselves (rk4.h:144-150), then sets 2 and 3 alternate
+	const int rd = stage == 0 ? 0 : (stage % 2 == 1 ? 2 : 3);
+	const int wr = stage % 2 == 0 ? 2 : 3;
+	a.base = soa(0); a.acc = soa(1); a.rd = soa(rd); a.wr = soa(wr);
+	a.gbase = gsoa(0); a.gacc = gsoa(1); a.grd = gsoa(rd); a.gwr = gsoa(wr);
+	a.pc_off = c->uw_pc_off.p; a.pc_nbr = c->uw_pc_nbr.p; a.gc_off = c->uw_gc_off.p; a.gc_nbr = c->uw_gc_nbr.p;
+	a.pmask = c->uw_pmask.p; a.gmask = c->uw_gmask.p;
+	a.pw = c->uw_pw.p; a.pwx = c->uw_pwx.p; a.pwy = c->uw_pwy.p;
+	a.gw = c->uw_gw.p; a.gwx = c->uw_gwx.p; a.gwy = c->uw_gwy.p;
+	a.tp_off = c->uw_tp_off.p; a.tp_gp = c->uw_tp_gp.p; a.tp_slot = c->uw_tp_slot.p;
+	a.gsig = c->uw_gsig.p; a.bc_of = c->uw_bc_of.p; a.bc_v = c->bc_v.p;
+	a.status = c->d_status;
+	return a;
+}
+
+// The ellipse neighbourhoods and shape functions of the particles (and, when
+// `points`, of the stress points) at the state `a.rd`; `refresh_qw` also stores m / rho
+// as the particles' weights (the smoothing's riemann update, rk4.h:201).
+cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refresh_qw) {
+	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
+	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qm, double* qw) {
+		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
+		                                     qm, qw, c->d_status, c->stream)
+		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qm,
+		                                   qw, c->d_status, c->stream);
+	};
+	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc_off, a.pc_nbr, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy,
+	                    refresh_qw ? a.m : nullptr, refresh_qw ? a.qw_base : nullptr);
+	if (e == cudaSuccess && points)
+		e = nbh(a.n_g, a.grd.x, a.grd.y, a.gc_off, a.gc_nbr, c->uw_gh.p, a.gmask, a.gw, a.gwx, a.gwy, nullptr, nullptr);
+	return e;
+}
+
+// rk4::do_step_weak + step for particle_ul_weak (rk4.h:140-205): per stage the
+// neighbourhoods and shape functions, the stress-point pass, the particle pass; then
+// the velocity conditions and the smoothing with fresh neighbourhoods.
+mf_status uw_step(mf_ctx* c) {
+	cudaError_t e;
+	auto launch = [&](const UWArgs& a, int part) {
+		return c->strict ? mf_strict::uw_stage(a, part, c->stream) : mf_fast::uw_stage(a, part, c->stream);
+	};
+	for (uint32_t st = 0; st < 4; st++) {
+		UWArgs a = uw_args(c, st);
+		if ((e = uw_neighbourhoods(c, a, true, false)) != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+		int slot;
+		timing_begin(c, 5, slot);
+		if ((e = launch(a, 0)) != cudaSuccess) return cuda_fail(c, e, "weak UL stress-point pass");
+		timing_end(c, slot, c->n_g);
+		timing_begin(c, 2, slot);
+		if ((e = launch(a, 1)) != cudaSuccess) return cuda_fail(c, e, "weak UL particle pass");
+		timing_end(c, slot, c->n_total);
+		c->launches += 4;
+	}
+	if (c->n_bc) {  // rk4.h:196
+		e = c->strict ? mf_strict::ul_bc(c->n_bc, c->bc_rows.p, c->bc_v.p, c->sd[0][2].p, c->sd[0][3].p, c->stream)
+		              : mf_fast::ul_bc(c->n_bc, c->bc_rows.p, c->bc_v.p, c->sd[0][2].p, c->sd[0][3].p, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "weak UL conditions");
+		c->launches++;
+	}
+	if (c->do_smooth) {  // rk4.h:198-204
+		UWArgs a = uw_args(c, 0);  // reads the particles themselves
+		if ((e = uw_neighbourhoods(c, a, false, true)) != cudaSuccess) return cuda_fail(c, e, "weak UL smoothing");
+		if ((e = launch(a, 2)) != cudaSuccess || (e = launch(a, 3)) != cudaSuccess)
+			return cuda_fail(c, e, "weak UL smoothing");
+		c->launches += 3;
 	}
 	return MF_OK;
 }
@@ -1568,7 +1801,7 @@ MF_API const char* mf_last_error(const mf_ctx* c) { return c ? c->err.c_str() : 
 MF_API mf_status mf_create(const mf_config* cfg, mf_ctx** out) {
 	if (!cfg || !out) return MF_ERR_ARG;
 	*out = nullptr;
-	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_POTENTIAL) return MF_ERR_ARG;
+	if (cfg->method < MF_METHOD_UL || cfg->method > MF_METHOD_UL_WEAK) return MF_ERR_ARG;
 	if (cfg->precision < MF_PREC_FP64_STRICT || cfg->precision > MF_PREC_MIXED) return MF_ERR_ARG;
 	int ndev = 0;
 	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MF_ERR_NO_DEVICE;
@@ -1623,7 +1856,7 @@ MF_API mf_status mf_add_action(mf_ctx* c, int32_t body, int32_t action) {
 	if (!c) return MF_ERR_ARG;
 	if (c->ready) return fail(c, MF_ERR_STATE, "actions must be added before the first step");
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
-	if (action < 1 || action > MF_POTENTIAL_COMP_ELASTIC_POTENTIAL) return fail(c, MF_ERR_ARG, "bad action id %d", action);
+	if (action < 1 || action > MF_CONTMECH_ADVECTION_GP) return fail(c, MF_ERR_ARG, "bad action id %d", action);
 	c->bodies[body].actions.push_back(action);
 	return MF_OK;
 }
@@ -1662,6 +1895,24 @@ MF_API mf_status mf_set_gauss_mesh(mf_ctx* c, int32_t body, uint32_t ex, uint32_
 		return fail(c, MF_ERR_ARG, "(ex+1)*(ey+1) must equal the body's particle count");
 	if (!(gp_h > 0.) || !(gp_rho > 0.)) return fail(c, MF_ERR_ARG, "Gauss-point h and rho must be positive");
 	b.ex = ex; b.ey = ey; b.gp_h = gp_h; b.gp_rho = gp_rho;
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_stress_points(mf_ctx* c, int32_t body, const mf_particles* sp, uint32_t n) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "stress points must be set before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	if (!sp || n == 0) return fail(c, MF_ERR_ARG, "null stress points or n == 0");
+	const double* src[13] = {sp->x, sp->y, sp->X, sp->Y, sp->m, sp->rho, sp->h, sp->quad_weight, sp->vx, sp->vy,
+	                         sp->Sxx, sp->Sxy, sp->Syy};
+	for (int k = 0; k < 13; k++)
+		if (!src[k] && k != 2 && k != 3) return fail(c, MF_ERR_ARG, "stress-point field %d is null", k);
+	HostBody& b = c->bodies[body];
+	b.n_sp = n;
+	for (int k = 0; k < 13; k++) {
+		const double* s = src[k] ? src[k] : (k == 2 ? sp->x : sp->y);
+		b.sp[k].assign(s, s + n);
+	}
 	return MF_OK;
 }
 
@@ -1706,7 +1957,10 @@ namespace {
 mf_status one_step(mf_ctx* c) {
 	const bool tl_lists =
 	    c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL;
-	mf_status st = c->cfg.method == MF_METHOD_UL ? ul_step(c) : (tl_lists ? tl_step_all(c) : weak_step(c));
+	mf_status st = c->cfg.method == MF_METHOD_UL        ? ul_step(c)
+	               : tl_lists                            ? tl_step_all(c)
+	               : c->cfg.method == MF_METHOD_UL_WEAK ? uw_step(c)
+	                                                     : weak_step(c);
 	if (st != MF_OK) return st;
 	if (c->contact_on) st = contact_run(c);
 	if (st == MF_OK && c->mon_cap) {
@@ -1974,6 +2228,29 @@ MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uin
 		CK(cudaMemcpyAsync(all_idx.data(), d_idx.p, offs[n] * 4, cudaMemcpyDeviceToHost, c->stream));
 		st = check_status(c);
 		if (st != MF_OK && st != MF_ERR_NBH_OVERFLOW) return st;
+	} else if (c->cfg.method == MF_METHOD_UL_WEAK) {
+		// the ellipse neighbourhoods of the particles' current state: those of the next
+		// step's first derivative evaluation
+		UWArgs a = uw_args(c, 0);
+		cudaError_t e = uw_neighbourhoods(c, a, false, false);
+		if (e != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+		CK(cudaStreamSynchronize(c->stream));
+		uint64_t ec = c->uw_pc_nbr.n;
+		std::vector<uint32_t> off(n + 1), cand(ec);
+		std::vector<uint8_t> mask(ec);
+		CK(cudaMemcpy(off.data(), c->uw_pc_off.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+		if (ec) {
+			CK(cudaMemcpy(cand.data(), c->uw_pc_nbr.p, ec * 4, cudaMemcpyDeviceToHost));
+			CK(cudaMemcpy(mask.data(), c->uw_pmask.p, ec, cudaMemcpyDeviceToHost));
+		}
+		st = check_status(c);
+		if (st != MF_OK) return st;
+		for (uint32_t i = 0; i < n; i++) {
+			for (uint32_t q = off[i]; q < off[i + 1]; q++)
+				if (mask[q]) all_idx.push_back(cand[q]);
+			all_counts[i] = (uint32_t)(all_idx.size() - offs[i]);
+			offs[i + 1] = all_idx.size();
+		}
 	} else {
 		std::vector<uint32_t> off(n + 1);
 		CK(cudaMemcpy(off.data(), c->nbr_off.p, (n + 1) * 4, cudaMemcpyDeviceToHost));
@@ -2094,6 +2371,10 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 	if (!c || trial_steps < 1) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if (c->cfg.method == MF_METHOD_UL_WEAK) {  // fixed launch shapes: nothing to try
+		if (report && report_len) snprintf(report, report_len, "fixed launch shapes");
+		return MF_OK;
+	}
 	CK(cudaSetDevice(c->cfg.device));
 	std::string key = tune_key(c);
 	std::string rep;
@@ -2386,7 +2667,7 @@ MF_API mf_status mf_vtk_write(const char* path, const mf_vtk_body* bodies, uint3
 
 MF_API mf_status mf_dump_async(mf_ctx* c, const char* path, int32_t kind) {
 	if (!c || !path || (kind != MF_DUMP_VTK && kind != MF_DUMP_CHECKPOINT)) return MF_ERR_ARG;
-	if (kind == MF_DUMP_CHECKPOINT && c->cfg.method == MF_METHOD_TL_WEAK)
+	if (kind == MF_DUMP_CHECKPOINT && (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK))
 		return fail(c, MF_ERR_STATE, "checkpoints cover updated- and total-Lagrangian bodies (not the weak form's Gauss points)");
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
@@ -2467,7 +2748,7 @@ MF_API mf_status mf_checkpoint_save(mf_ctx* c, const char* path) {
 
 MF_API mf_status mf_checkpoint_load(mf_ctx* c, const char* path) {
 	if (!c || !path) return MF_ERR_ARG;
-	if (c->cfg.method == MF_METHOD_TL_WEAK)
+	if (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK)
 		return fail(c, MF_ERR_STATE, "checkpoints cover updated- and total-Lagrangian bodies (not the weak form's Gauss points)");
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;

@@ -18,6 +18,14 @@ inline uint32_t bit(int a) { return 1u << a; }
 constexpr uint32_t FLAG_GODUNOV_CONTINUITY = 1u << 12;
 constexpr uint32_t FLAG_GODUNOV_MOMENTUM = 1u << 13;
 constexpr uint32_t FLAG_POTENTIAL = 1u << 0;
+// The weak updated-Lagrangian form's own actions (ids 35-40) take the bits of the
+// total-Lagrangian actions 12-17, which its pipeline never holds.
+constexpr uint32_t FLAG_UW_RIEMANN_GP = 1u << 12;
+constexpr uint32_t FLAG_UW_STRESS = 1u << 13;
+constexpr uint32_t FLAG_UW_VEL_WEAK = 1u << 14;
+constexpr uint32_t FLAG_UW_MOMENTUM_W = 1u << 15;
+constexpr uint32_t FLAG_UW_INTERP = 1u << 16;
+constexpr uint32_t FLAG_UW_ADVECTION_GP = 1u << 17;
 
 // Per-body constants (simulation_data.h:25-99 plus the body's dt), device copy.
 struct BodyParams {
@@ -99,6 +107,7 @@ struct TLSearchArgs {
 	uint32_t* count;           // pass 0 output
 	const uint32_t* off;       // pass 1 input (exclusive scan of count)
 	uint32_t* nbr;             // pass 1 output
+	uint32_t manhattan;        // 1: |dx| < 2h + 1e-6 and |dy| < 2h + 1e-6 (neighbor_search.h:43-48)
 	void* status;
 };
 
@@ -170,6 +179,30 @@ struct WeakArgs {
 	void* status;
 };
 
+// Weak updated-Lagrangian form (particle_ul_weak): particles and stress points, both
+// with fixed candidate lists (CSR, ascending) and, per derivative evaluation, the
+// candidates inside the neighbour ellipse (mask) with their RKPM shape functions.
+struct GSoA {
+	double *x, *y, *rho, *Sxx, *Sxy, *Syy;
+};
+struct UWArgs {
+	uint32_t n_p, n_g, stage, flags, block;
+	const BodyParams* params;
+	const uint32_t *body_of, *gbody_of;
+	const double *m, *gm, *fcx, *fcy;
+	double *qw_base, *gqw_base;          // quad weights of the particles / stress points
+	StateSoA base, acc, rd, wr;          // particles: this stage reads rd, writes wr
+	GSoA gbase, gacc, grd, gwr;          // stress points
+	const uint32_t *pc_off, *pc_nbr, *gc_off, *gc_nbr;  // candidate lists
+	uint8_t *pmask, *gmask;              // per candidate: inside this evaluation's ellipse
+	double *pw, *pwx, *pwy, *gw, *gwx, *gwy;  // per candidate: shape function and gradient
+	const uint32_t *tp_off, *tp_gp, *tp_slot;  // per particle: the stress points listing it, ascending
+	double* gsig;                        // per stress point: Sxx - p, Sxy, Syy - p, quad weight
+	const uint32_t* bc_of;               // per particle: index into bc_v, or ~0u
+	const double* bc_v;
+	void* status;
+};
+
 // Contact: boundary points of all bodies, their 32-point tiles, and the slave rows
 // with the master body each one is tested against.
 struct ContactArgs {
@@ -233,6 +266,11 @@ struct ContactArgs {
 	                      const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* out64, void* out32,     \
 	                      const double* mul_row, const double* mul_nbr, cudaStream_t s);                      \
 	cudaError_t weak_stage(const mfk_host::WeakArgs& a, bool mixed, int part, cudaStream_t s);               \
+	cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr, \
+	                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,  \
+	                   uint8_t* mask, double* w, double* wx, double* wy, const double* set_qw_m, double* set_qw, \
+	                   void* status, cudaStream_t s);                                                       \
+	cudaError_t uw_stage(const mfk_host::UWArgs& a, int part, cudaStream_t s);                                \
 	}
 
 MF_DECLARE_LAUNCHERS(mf_strict)

@@ -1,0 +1,105 @@
+// RKPM shape functions with a linear basis: compute_rkpm_correctors and
+// compute_rkpm_shape_function (precomp_shape_functions.h:31-173), in the reference's
+// operation order, for one query point over the entries q0..q1 of its neighbour list.
+// Shared by the weak total-Lagrangian set-up and the per-stage shape functions of the
+// weak updated-Lagrangian form.
+#pragma once
+
+#include "mf_common.cuh"
+
+namespace MF_NS {
+namespace {
+
+// use(q): whether list entry q takes part; rho(j): the neighbour's density;
+// out(q, w, w_x, w_y): the shape function and its gradient of entry q.  Returns false
+// when the moment matrix is singular (the reference's assert, precomp_shape_functions.h:45).
+template <class Rho, class Use, class Out>
+__device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32_t q0, uint32_t q1,
+                                         const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
+                                         const double* __restrict__ fy, const double* __restrict__ fm, Rho rho, Use use,
+                                         Out out) {
+	bool ok = true;
+	double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
+	       My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row]
+	for (uint32_t q = q0; q < q1; q++) {
+		if (!use(q)) continue;
+		uint32_t j = nbr[q];
+		double mj = fm[j], rhoj = rho(j);
+		double xj = fx[j], yj = fy[j];
+		double rx = xi - xj, ry = yi - yj;
+		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
+		mfk::KR64 w = mfk::cubic_spline(xi - xj, yi - yj, hi);
+		M[0][0] += w.w * mj / rhoj;
+		M[0][1] += w.w * rx * mj / rhoj;
+		M[0][2] += w.w * ry * mj / rhoj;
+		M[1][0] += w.w * rx * mj / rhoj;
+		M[2][0] += w.w * ry * mj / rhoj;
+		M[1][1] += rx * rx * w.w * mj / rhoj;
+		M[1][2] += rx * ry * w.w * mj / rhoj;
+		M[2][1] += ry * rx * w.w * mj / rhoj;
+		M[2][2] += ry * ry * w.w * mj / rhoj;
+
+		Mx[0][0] += w.w_x * mj / rhoj;
+		Mx[0][1] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
+		Mx[0][2] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
+		Mx[1][0] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
+		Mx[2][0] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
+		Mx[1][1] += rx * rx * w.w_x * mj / rhoj + w.w * (rx_x * rx + rx * rx_x) * mj / rhoj;
+		Mx[1][2] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_x * ry + rx * rx_y) * mj / rhoj;
+		Mx[2][1] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_y * rx + ry * rx_x) * mj / rhoj;
+		Mx[2][2] += ry * ry * w.w_x * mj / rhoj + w.w * (rx_y * ry + ry * rx_y) * mj / rhoj;
+
+		My[0][0] += w.w_y * mj / rhoj;
+		My[0][1] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
+		My[0][2] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
+		My[1][0] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
+		My[2][0] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
+		My[1][1] += rx * rx * w.w_y * mj / rhoj + w.w * (ry_x * rx + rx * ry_x) * mj / rhoj;
+		My[1][2] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_x * ry + rx * ry_y) * mj / rhoj;
+		My[2][1] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_y * rx + ry * ry_x) * mj / rhoj;
+		My[2][2] += ry * ry * w.w_y * mj / rhoj + w.w * (ry_y * ry + ry * ry_y) * mj / rhoj;
+	}
+	// solve3x3 (Cramer's rule, precomp_shape_functions.h:31-50)
+	auto solve = [&](const double r[3], double x[3]) {
+		double delta = M[0][0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * M[1][2] -
+		               M[0][2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * M[1][0];
+		double delta_x = r[0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * r[2] + M[2][0] * r[1] * M[1][2] -
+		                 r[2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * r[0] - M[2][2] * r[1] * M[1][0];
+		double delta_y = M[0][0] * r[1] * M[2][2] + r[0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * r[2] -
+		                 M[0][2] * r[1] * M[2][0] - r[2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * r[0];
+		double delta_z = M[0][0] * M[1][1] * r[2] + M[1][0] * r[1] * M[0][2] + r[0] * M[0][1] * M[1][2] -
+		                 M[0][2] * M[1][1] * r[0] - M[1][2] * r[1] * M[0][0] - r[2] * M[0][1] * M[1][0];
+		if (!(fabs(delta) > 0.)) ok = false;
+		x[0] = delta_x / delta;
+		x[1] = delta_y / delta;
+		x[2] = delta_z / delta;
+	};
+	double P[3] = {1., 0., 0.}, C[3], Cx[3], Cy[3];
+	solve(P, C);
+	// rhs = -M_x * C  ((-M_x) * C, column-major product)
+	double rx_[3], ry_[3];
+#pragma unroll
+	for (int r = 0; r < 3; r++) {
+		rx_[r] = (-Mx[0][r]) * C[0] + (-Mx[1][r]) * C[1] + (-Mx[2][r]) * C[2];
+		ry_[r] = (-My[0][r]) * C[0] + (-My[1][r]) * C[1] + (-My[2][r]) * C[2];
+	}
+	solve(rx_, Cx);
+	solve(ry_, Cy);
+	for (uint32_t q = q0; q < q1; q++) {
+		if (!use(q)) continue;
+		uint32_t j = nbr[q];
+		double xj = fx[j], yj = fy[j];
+		double rx = xi - xj, ry = yi - yj;
+		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
+		mfk::KR64 w = mfk::cubic_spline(xi - xj, yi - yj, hi);
+		double Corr = (rx * C[1] + ry * C[2]) + C[0];
+		double Corr_x = (rx * Cx[1] + ry * Cx[2]) + rx_x * C[1] + rx_y * C[2] + Cx[0];
+		double Corr_y = (rx * Cy[1] + ry * Cy[2]) + ry_x * C[1] + ry_y * C[2] + Cy[0];
+		out(q, Corr * w.w, Corr_x * w.w + Corr * w.w_x, Corr_y * w.w + Corr * w.w_y);
+	}
+	return ok;
+}
+
+
+}  // namespace
+}  // namespace MF_NS

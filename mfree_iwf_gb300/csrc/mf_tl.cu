@@ -84,6 +84,7 @@ __global__ void k_search(TLSearchArgs a, int pass, DevStatus* st) {
 	double h = a.h;
 	double radius2 = __dmul_rn(__dmul_rn(__dmul_rn(h, h), 2.), 2.);
 	double lim = __dadd_rn(radius2, a.eps);
+	double box = __dadd_rn(__dmul_rn(2., h), 1e-6);  // the Manhattan predicate's half-width
 	long cx = (long)floor((xi - g.bbmin_x) / g.dx), cy = (long)floor((yi - g.bbmin_y) / g.dx);
 	uint32_t cnt = 0;
 	uint32_t base = pass ? a.off[i] : 0u;
@@ -98,7 +99,8 @@ __global__ void k_search(TLSearchArgs a, int pass, DevStatus* st) {
 			double xij = __dsub_rn(xi, a.fx[j]);
 			double yij = __dsub_rn(yi, a.fy[j]);
 			double r2 = __dadd_rn(__dmul_rn(xij, xij), __dmul_rn(yij, yij));
-			if (r2 <= lim) {
+			bool in = a.manhattan ? (fabs(xij) < box && fabs(yij) < box) : (r2 <= lim);
+			if (in) {
 				if (pass && cnt < a.max_nbh) {
 					// insertion into the ascending list
 					uint32_t pos = base + cnt;

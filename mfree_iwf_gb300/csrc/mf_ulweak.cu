@@ -1,0 +1,283 @@
+// Weak-form updated-Lagrangian SPH with RKPM shape functions and stress points
+// (particle_ul_weak; tensile_ul_weak tensile.cpp:626-729, rotation_ul_weak
+// rotation.cpp:466-535, rings_ul_weak_contact rings.cpp:817-934; body.h:80-108,
+// rk4.h:140-205).
+//
+// Set-up (host side): candidate lists of the particles and of the stress points among
+// the particles (find_neighbors with distance_manhattan, neighbor_search.h:84-180), and
+// per particle the stress points whose candidates hold it, ascending.
+//
+// Per derivative evaluation:
+//   k_uw_nbh  (particles, then stress points)  nbh_ellipse (neighbor_ellipse.h:62-127):
+//             h and the candidates inside the ellipse, then precomp_rkpm over those
+//             (precomp_shape_functions.h:143-208)
+//   k_uw_gp   per stress point: integration weight, EOS, velocity gradient
+//             (derivatives.h:68-99), Jaumann rate, continuity, interpolated velocity
+//             (interpolation.h:32-59) and advection, its stress for the particles,
+//             and its RK4 update
+//   k_uw_p    per particle: integration weight; the stress divergence that
+//             derive_stress_weak_ul (derivatives.h:296-329) scatters from the stress
+//             points, gathered over the stress points listing the particle in
+//             ascending order (the order the scatter adds them); velocity gradient
+//             (derivatives.h:32-66), momentum (cont_mech.h:32-68), continuity,
+//             advection, the boundary conditions (body.h:106) and the RK4 update
+// After the step: the velocity conditions, then the smoothing of rk4.h:198-204
+// (ellipse, weights and shape functions of the particles, correctors.h:171-210).
+#include "mf_common.cuh"
+#include "mf_kernels.h"
+#include "mf_rkpm.cuh"
+
+using namespace mfk;
+using mfk_host::BodyParams;
+using mfk_host::UWArgs;
+
+namespace MF_NS {
+namespace {
+
+inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
+
+enum : uint32_t {
+	A_RIEMANN = 1u << 1,
+	A_DERIVE_VEL = 1u << 5,
+	A_CONTINUITY = 1u << 9,
+	A_MOMENTUM_UL = 1u << 10,
+	A_ADVECTION = 1u << 11,
+	A_CONT_GP = 1u << 22,
+	A_EOS_GP = 1u << 23,
+	A_JAUMANN_GP = 1u << 24,
+};
+
+// nbh_ellipse for query point i over its candidates, then the RKPM shape functions of
+// the candidates inside the ellipse.  set_qw (the smoothing's
+// riemann_update_integration_weights) also refreshes the row's weight m / rho.
+__global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
+                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                         const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
+                         const double* __restrict__ frho, double* h_out, uint8_t* mask, double* w, double* wx,
+                         double* wy, const double* __restrict__ set_qw_m, double* set_qw, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_to) return;
+	const double px = tx[i], py = ty[i];
+	const uint32_t q0 = off[i], q1 = off[i + 1];
+	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0., h = 0.;
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double dx = px - fx[j], dy = py - fy[j];
+		double r2 = dx * dx + dy * dy;
+		h = fmax(h, r2);
+		Hxx += dx * dx; Hxy += dx * dy;
+		Hyx += dy * dx; Hyy += dy * dy;
+	}
+	h = sqrt(h);
+	h /= 2;
+	h_out[i] = h;
+	// eigen (neighbor_ellipse.h:29-60) of A = (Hxx, Hyx; Hxy, Hyy) / n, columns first
+	const double nc = (double)(q1 - q0);
+	const double A00 = Hxx / nc, A01 = Hyx / nc, A10 = Hxy / nc, A11 = Hyy / nc;
+	double D0, D1, rax, ray;
+	if (fabs(A10) < 1e-9 && fabs(A01) < 1e-9) {
+		D0 = A00; D1 = A11; rax = 1.; ray = 0.;
+	} else {
+		double T = A00 + A11;
+		double det = A00 * A11 - A10 * A01;
+		double L1 = T / 2 + sqrt(T * T / 4 - det);
+		double L2 = T / 2 - sqrt(T * T / 4 - det);
+		double l1 = fmin(L1, L2), l2 = fmax(L1, L2);
+		D0 = l1; D1 = l2;
+		double vx, vy;
+		if (fabs(A10) > 1e-12) { vx = l1 - A11; vy = A01; }
+		else { vx = A10; vy = l1 - A00; }
+		double inv = 1. / sqrt(vx * vx + vy * vy);  // glm::normalize
+		rax = vx * inv; ray = vy * inv;
+	}
+	const double a = 1.6651 * sqrt(D0), b = 1.6651 * sqrt(D1);
+	const double phi = atan2(ray, rax);
+	const double cs = cos(phi), sn = sin(phi);
+	uint32_t cnt = 0;
+	for (uint32_t q = q0; q < q1; q++) {
+		uint32_t j = nbr[q];
+		double xc = fx[j] - px, yc = fy[j] - py;
+		double left = ((cs * xc + sn * yc) / a);
+		double right = ((sn * xc - cs * yc) / b);
+		bool in = left * left + right * right <= 1;
+		mask[q] = in ? 1 : 0;
+		cnt += in ? 1u : 0u;
+	}
+	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
+	if (set_qw) set_qw[i] = set_qw_m[i] / frho[i];
+	auto rho = [&](uint32_t j) { return frho[j]; };
+	auto use = [&](uint32_t q) { return mask[q] != 0; };
+	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
+	if (!rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)) raise(st, ERR_SINGULAR, i);
+}
+
+// the particles' integration weight of this evaluation (riemann_update_integration_weights)
+__device__ __forceinline__ double p_qw(const UWArgs& a, uint32_t j) {
+	return (a.flags & A_RIEMANN) ? a.m[j] / a.rd.rho[j] : a.qw_base[j];
+}
+
+// rk_add (rk4.h:52-69) for stages 0-2, the 1-2-2-1 combine (rk4.h:168-182) at stage 3
+__device__ __forceinline__ void uw_rk(uint32_t stg, double dt, uint32_t i, int nf, double* const* bp,
+                                      double* const* ap, double* const* wp, const double* d) {
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+		for (int q = 0; q < nf; q++) {
+			ap[q][i] = (stg == 0) ? d[q] : ap[q][i] + 2 * d[q];
+			wp[q][i] = bp[q][i] + d[q] * dts;
+		}
+	} else {
+		double w6 = dt * 1. / 6.;
+		for (int q = 0; q < nf; q++) bp[q][i] = bp[q][i] + w6 * (ap[q][i] + d[q]);
+	}
+}
+
+__global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_g) return;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.gbody_of[i]];
+	const mfk_host::GSoA& g = a.grd;
+	const double rho = g.rho[i];
+	const double qw = (flags & mfk_host::FLAG_UW_RIEMANN_GP) ? a.gm[i] / rho : a.gqw_base[i];
+	const double p = (flags & A_EOS_GP) ? pr.c0sq * (rho - pr.rho0) : 0.;
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0., vxi = 0., vyi = 0.;
+	for (uint32_t q = a.gc_off[i]; q < a.gc_off[i + 1]; q++) {
+		if (!a.gmask[q]) continue;
+		uint32_t j = a.gc_nbr[q];
+		double vxj = a.rd.vx[j], vyj = a.rd.vy[j], qwj = p_qw(a, j);
+		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
+			vx_x += vxj * a.gwx[q] * qwj;
+			vx_y += vxj * a.gwy[q] * qwj;
+			vy_x += vyj * a.gwx[q] * qwj;
+			vy_y += vyj * a.gwy[q] * qwj;
+		}
+		if (flags & mfk_host::FLAG_UW_INTERP) {
+			vxi += vxj * a.gw[q] * qwj;
+			vyi += vyj * a.gw[q] * qwj;
+		}
+	}
+	const double Sxx = g.Sxx[i], Sxy = g.Sxy[i], Syy = g.Syy[i];
+	double d[6] = {0., 0., 0., 0., 0., 0.};  // x_t y_t rho_t Sxx_t Sxy_t Syy_t
+	if (flags & A_JAUMANN_GP) jaumann<double>(vx_x, vx_y, vy_x, vy_y, Sxx, Sxy, Syy, pr.G, d[3], d[4], d[5]);
+	if (flags & A_CONT_GP) d[2] = 0. - rho * (vx_x + vy_y);
+	if (flags & mfk_host::FLAG_UW_ADVECTION_GP) { d[0] = 0. + vxi; d[1] = 0. + vyi; }
+	const uint32_t n = a.n_g;
+	a.gsig[i] = Sxx - p;
+	a.gsig[n + i] = Sxy;
+	a.gsig[2 * n + i] = Syy - p;
+	a.gsig[3 * n + i] = qw;
+	double* bp[6] = {a.gbase.x, a.gbase.y, a.gbase.rho, a.gbase.Sxx, a.gbase.Sxy, a.gbase.Syy};
+	double* ap[6] = {a.gacc.x, a.gacc.y, a.gacc.rho, a.gacc.Sxx, a.gacc.Sxy, a.gacc.Syy};
+	double* wp[6] = {a.gwr.x, a.gwr.y, a.gwr.rho, a.gwr.Sxx, a.gwr.Sxy, a.gwr.Syy};
+	uw_rk(a.stage, pr.dt, i, 6, bp, ap, wp, d);
+}
+
+__global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
+	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= a.n_p) return;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[j]];
+	const mfk_host::StateSoA& s = a.rd;
+	const double rho = s.rho[j], m = a.m[j], vxj = s.vx[j], vyj = s.vy[j];
+	const double qwj = p_qw(a, j);
+	double Sxx_x = 0., Sxy_y = 0., Sxy_x = 0., Syy_y = 0.;
+	if (flags & mfk_host::FLAG_UW_STRESS) {
+		const uint32_t ng = a.n_g;
+		for (uint32_t t = a.tp_off[j]; t < a.tp_off[j + 1]; t++) {
+			uint32_t q = a.tp_slot[t];
+			if (!a.gmask[q]) continue;
+			uint32_t gi = a.tp_gp[t];
+			double Sxxi = a.gsig[gi], Sxyi = a.gsig[ng + gi], Syyi = a.gsig[2 * ng + gi], qwi = a.gsig[3 * ng + gi];
+			Sxx_x -= Sxxi * a.gwx[q] * qwi * qwj;
+			Sxy_y -= Sxyi * a.gwy[q] * qwi * qwj;
+			Sxy_x -= Sxyi * a.gwx[q] * qwi * qwj;
+			Syy_y -= Syyi * a.gwy[q] * qwi * qwj;
+		}
+	}
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+	if (flags & A_DERIVE_VEL) {
+		for (uint32_t q = a.pc_off[j]; q < a.pc_off[j + 1]; q++) {
+			if (!a.pmask[q]) continue;
+			uint32_t k = a.pc_nbr[q];
+			double qwk = p_qw(a, k);
+			vx_x += (s.vx[k] - vxj) * a.pwx[q] * qwk;
+			vx_y += (s.vx[k] - vxj) * a.pwy[q] * qwk;
+			vy_x += (s.vy[k] - vyj) * a.pwx[q] * qwk;
+			vy_y += (s.vy[k] - vyj) * a.pwy[q] * qwk;
+		}
+	}
+	double d[5] = {0., 0., 0., 0., 0.};  // x_t y_t vx_t vy_t rho_t
+	if (flags & A_MOMENTUM_UL) {
+		d[2] = 0. + (1. / rho * (Sxx_x + Sxy_y) + a.fcx[j] / m);
+		d[3] = 0. + (1. / rho * (Sxy_x + Syy_y) + a.fcy[j] / m);
+	}
+	if (flags & mfk_host::FLAG_UW_MOMENTUM_W) {
+		d[2] = d[2] + (1. / m * (Sxx_x + Sxy_y) + a.fcx[j] / m);
+		d[3] = d[3] + (1. / m * (Sxy_x + Syy_y) + a.fcy[j] / m);
+	}
+	if (flags & A_CONTINUITY) d[4] = 0. - rho * (vx_x + vy_y);
+	if (flags & A_ADVECTION) { d[0] = 0. + vxj; d[1] = 0. + vyj; }
+	uint32_t bc = a.bc_of[j];
+	if (bc != ~0u) {  // left/right_bndry_fun_ul after the actions (body.h:106)
+		d[0] = a.bc_v[bc];
+		d[1] = 0.;
+		d[2] = 0.;
+		d[3] = 0.;
+	}
+	double* bp[5] = {a.base.x, a.base.y, a.base.vx, a.base.vy, a.base.rho};
+	double* ap[5] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy, a.acc.rho};
+	double* wp[5] = {a.wr.x, a.wr.y, a.wr.vx, a.wr.vy, a.wr.rho};
+	uw_rk(a.stage, pr.dt, j, 5, bp, ap, wp, d);
+	if (a.stage == 3 && !(isfinite(bp[0][j]) && isfinite(bp[1][j]) && isfinite(bp[2][j]) && isfinite(bp[3][j])))
+		raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, j);
+}
+
+// correctors_smooth_vel (correctors.h:171-210) over the particles' fresh ellipse lists;
+// the smoothed velocities go to the accumulator arrays first (every row reads the
+// unsmoothed ones), then k_uw_smooth_copy moves them into the state
+__global__ void k_uw_smooth(UWArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_p) return;
+	double vsx = 0., vsy = 0.;
+	for (uint32_t q = a.pc_off[i]; q < a.pc_off[i + 1]; q++) {
+		if (!a.pmask[q]) continue;
+		uint32_t k = a.pc_nbr[q];
+		vsx += a.base.vx[k] * a.pw[q] * a.qw_base[k];
+		vsy += a.base.vy[k] * a.pw[q] * a.qw_base[k];
+	}
+	a.acc.x[i] = vsx;
+	a.acc.y[i] = vsy;
+}
+
+__global__ void k_uw_smooth_copy(UWArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_p) return;
+	a.base.vx[i] = a.acc.x[i];
+	a.base.vy[i] = a.acc.y[i];
+}
+
+}  // namespace
+
+cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
+                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,
+                   uint8_t* mask, double* w, double* wx, double* wy, const double* set_qw_m, double* set_qw,
+                   void* status, cudaStream_t s) {
+	if (n_to == 0) return cudaSuccess;
+	k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx, wy,
+	                                          set_qw_m, set_qw, reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+// part 0: stress points, 1: particles, 2: smoothing sums, 3: smoothing copy
+cudaError_t uw_stage(const UWArgs& a, int part, cudaStream_t s) {
+	const unsigned bs = 128;  // the passes' launch bounds
+	switch (part) {
+	case 0: if (a.n_g) k_uw_gp<<<grid1(a.n_g, bs), bs, 0, s>>>(a); break;
+	case 1: if (a.n_p) k_uw_p<<<grid1(a.n_p, bs), bs, 0, s>>>(a); break;
+	case 2: if (a.n_p) k_uw_smooth<<<grid1(a.n_p, 128), 128, 0, s>>>(a); break;
+	case 3: if (a.n_p) k_uw_smooth_copy<<<grid1(a.n_p, 128), 128, 0, s>>>(a); break;
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS

@@ -20,6 +20,7 @@
 //   k_smooth    velocity smoothing after the step (correctors.h:171-210).
 #include "mf_common.cuh"
 #include "mf_kernels.h"
+#include "mf_rkpm.cuh"
 
 using namespace mfk;
 using mfk_host::BodyParams;
@@ -110,86 +111,14 @@ __global__ void k_rkpm(uint32_t n_to, const double* __restrict__ tx, const doubl
                        double* wy_out, DevStatus* st) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n_to) return;
-	double xi = tx[i], yi = ty[i], hi = th[i];
-	double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
-	       My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row]
-	uint32_t q0 = off[i], q1 = off[i + 1];
-	for (uint32_t q = q0; q < q1; q++) {
-		uint32_t j = nbr[q];
-		double mj = fm[j], rhoj = frho ? frho[j] : (double)frho_f[j];
-		double xj = fx[j], yj = fy[j];
-		double rx = xi - xj, ry = yi - yj;
-		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
-		KR64 w = cubic_spline(xi - xj, yi - yj, hi);
-		M[0][0] += w.w * mj / rhoj;
-		M[0][1] += w.w * rx * mj / rhoj;
-		M[0][2] += w.w * ry * mj / rhoj;
-		M[1][0] += w.w * rx * mj / rhoj;
-		M[2][0] += w.w * ry * mj / rhoj;
-		M[1][1] += rx * rx * w.w * mj / rhoj;
-		M[1][2] += rx * ry * w.w * mj / rhoj;
-		M[2][1] += ry * rx * w.w * mj / rhoj;
-		M[2][2] += ry * ry * w.w * mj / rhoj;
-
-		Mx[0][0] += w.w_x * mj / rhoj;
-		Mx[0][1] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
-		Mx[0][2] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
-		Mx[1][0] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
-		Mx[2][0] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
-		Mx[1][1] += rx * rx * w.w_x * mj / rhoj + w.w * (rx_x * rx + rx * rx_x) * mj / rhoj;
-		Mx[1][2] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_x * ry + rx * rx_y) * mj / rhoj;
-		Mx[2][1] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_y * rx + ry * rx_x) * mj / rhoj;
-		Mx[2][2] += ry * ry * w.w_x * mj / rhoj + w.w * (rx_y * ry + ry * rx_y) * mj / rhoj;
-
-		My[0][0] += w.w_y * mj / rhoj;
-		My[0][1] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
-		My[0][2] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
-		My[1][0] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
-		My[2][0] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
-		My[1][1] += rx * rx * w.w_y * mj / rhoj + w.w * (ry_x * rx + rx * ry_x) * mj / rhoj;
-		My[1][2] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_x * ry + rx * ry_y) * mj / rhoj;
-		My[2][1] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_y * rx + ry * ry_x) * mj / rhoj;
-		My[2][2] += ry * ry * w.w_y * mj / rhoj + w.w * (ry_y * ry + ry * ry_y) * mj / rhoj;
-	}
-	// solve3x3 (Cramer's rule, precomp_shape_functions.h:31-50)
-	auto solve = [&](const double r[3], double x[3]) {
-		double delta = M[0][0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * M[1][2] -
-		               M[0][2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * M[1][0];
-		double delta_x = r[0] * M[1][1] * M[2][2] + M[1][0] * M[2][1] * r[2] + M[2][0] * r[1] * M[1][2] -
-		                 r[2] * M[1][1] * M[2][0] - M[1][2] * M[2][1] * r[0] - M[2][2] * r[1] * M[1][0];
-		double delta_y = M[0][0] * r[1] * M[2][2] + r[0] * M[2][1] * M[0][2] + M[2][0] * M[0][1] * r[2] -
-		                 M[0][2] * r[1] * M[2][0] - r[2] * M[2][1] * M[0][0] - M[2][2] * M[0][1] * r[0];
-		double delta_z = M[0][0] * M[1][1] * r[2] + M[1][0] * r[1] * M[0][2] + r[0] * M[0][1] * M[1][2] -
-		                 M[0][2] * M[1][1] * r[0] - M[1][2] * r[1] * M[0][0] - r[2] * M[0][1] * M[1][0];
-		if (!(fabs(delta) > 0.)) raise(st, ERR_SINGULAR, i);
-		x[0] = delta_x / delta;
-		x[1] = delta_y / delta;
-		x[2] = delta_z / delta;
+	auto rho = [&](uint32_t j) { return frho ? frho[j] : (double)frho_f[j]; };
+	auto all = [](uint32_t) { return true; };
+	auto out = [&](uint32_t q, double w, double wx, double wy) {
+		if (w_out) w_out[q] = w;
+		if (wx_out) wx_out[q] = wx;
+		if (wy_out) wy_out[q] = wy;
 	};
-	double P[3] = {1., 0., 0.}, C[3], Cx[3], Cy[3];
-	solve(P, C);
-	// rhs = -M_x * C  ((-M_x) * C, column-major product)
-	double rx_[3], ry_[3];
-#pragma unroll
-	for (int r = 0; r < 3; r++) {
-		rx_[r] = (-Mx[0][r]) * C[0] + (-Mx[1][r]) * C[1] + (-Mx[2][r]) * C[2];
-		ry_[r] = (-My[0][r]) * C[0] + (-My[1][r]) * C[1] + (-My[2][r]) * C[2];
-	}
-	solve(rx_, Cx);
-	solve(ry_, Cy);
-	for (uint32_t q = q0; q < q1; q++) {
-		uint32_t j = nbr[q];
-		double xj = fx[j], yj = fy[j];
-		double rx = xi - xj, ry = yi - yj;
-		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
-		KR64 w = cubic_spline(xi - xj, yi - yj, hi);
-		double Corr = (rx * C[1] + ry * C[2]) + C[0];
-		double Corr_x = (rx * Cx[1] + ry * Cx[2]) + rx_x * C[1] + rx_y * C[2] + Cx[0];
-		double Corr_y = (rx * Cy[1] + ry * Cy[2]) + ry_x * C[1] + ry_y * C[2] + Cy[0];
-		if (w_out) w_out[q] = Corr * w.w;
-		if (wx_out) wx_out[q] = Corr_x * w.w + Corr * w.w_x;
-		if (wy_out) wy_out[q] = Corr_y * w.w + Corr * w.w_y;
-	}
+	if (!rkpm_row(tx[i], ty[i], th[i], off[i], off[i + 1], nbr, fx, fy, fm, rho, all, out)) raise(st, ERR_SINGULAR, i);
 }
 
 // For particle j and the k-th Gauss point i of its transposed list: the position of j

@@ -196,3 +196,36 @@ def test_ul_plate_velocity_conditions(lib, oracle_bin, precision):
     again = run(sc, 60, precision, graph=True)[0]
     for f in FIELDS:
         assert np.array_equal(again[f], got[f]), f
+
+
+@pytest.mark.parametrize("build,steps", [
+    (lambda: S.tensile_ul_weak(21), 60),
+    (lambda: S.rings_ul_weak_contact(30), 500),
+])
+def test_ul_weak_against_oracle(lib, oracle_bin, build, steps):
+    """The weak UL form (ellipse neighbourhoods and RKPM per derivative evaluation,
+    stress points, smoothing) on larger lattices against the oracle, FP64 strict."""
+    import oracle
+    sc = build()
+    ref = oracle.run(sc, steps).dumps[-1]["bodies"]
+    got = run(sc, steps)
+    for g, r in zip(got, ref):
+        for name, fields in GODUNOV_GROUPS.items():
+            assert rel(g, r, fields) < 1e-9, (sc.name, name, rel(g, r, fields))
+
+
+def test_ul_weak_graph_and_pipeline_checks(lib):
+    import mfree_iwf_gb300 as M
+    sc = S.tensile_ul_weak(11)
+    a = run(sc, 20)
+    b = run(sc, 20, graph=True)
+    for ga, gb in zip(a, b):
+        for f in FIELDS:
+            assert np.array_equal(ga[f], gb[f]), f
+    with pytest.raises(M.MfError) as e:
+        run(sc, 1, precision="mixed")
+    assert "MF_ERR_PIPELINE" in str(e.value)
+    sc.actions = [x for x in sc.actions if x != M.DERIVE_STRESS_WEAK_UL]
+    with pytest.raises(M.MfError) as e:
+        run(sc, 1)
+    assert "MF_ERR_PIPELINE" in str(e.value)
