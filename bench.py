@@ -12,7 +12,11 @@ Metric: particle-steps/s = particles x RK4 steps / time, the whole step included
 (4 stages, contact, boundary update).  One JSON line on rank 0.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c4] [--precision mixed|fp64|fp64_strict]
+                  [--workload c2|c1|c3|c4|corot|godunov|potential|ulweak]
+                  [--precision mixed|fp64|fp64_strict]
+
+The family workloads (corot, godunov, potential, ulweak) are ensembles of the
+reference's own two-ring set-up of that SPH family (FP64 forms only).
 
 With --impl reference it times the CPU implementation of the same path (the oracle
 restatement of the reference, which is single-threaded) on all host cores.
@@ -47,7 +51,14 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+FAMILIES = ("corot", "godunov", "potential", "ulweak")
+
+
 def workload_desc(name: str, dx: float | None, instances: int = 512) -> dict:
+    if name in FAMILIES:
+        from mfree_iwf_gb300 import scenarios as S
+        return {"workload": f"ensemble of {instances} two-ring impacts, {S.FAMILY_RING_SETUPS[name]}(81) each "
+                            "(the reference's set-up), per-instance E~U[8e6,1.2e7] Pa, seeded"}
     if name == "c4":
         return {"workload": f"ensemble of {instances} ring impacts, Gray-Monaghan SPH, per-instance dx~U[0.2,1] mm, "
                             "E~U[5e6,5e7] Pa, nu~U[0.3,0.45], speed~U[5,40] m/s, seeded"}
@@ -64,6 +75,8 @@ def workload_desc(name: str, dx: float | None, instances: int = 512) -> dict:
 def workload(name: str, dx: float | None, instances: int = 512):
     from mfree_iwf_gb300 import scenarios as S
     desc = workload_desc(name, dx, instances)
+    if name in FAMILIES:
+        return S.family_ensemble(name, instances), desc
     if name == "c4":
         return S.c4_ensemble(instances), desc
     if name == "c3":
@@ -147,7 +160,10 @@ def cpu_sample(workload_name: str, steps: int, warmup: int, procs: int):
     import oracle
     from mfree_iwf_gb300 import scenarios as S
     binary = oracle.build_oracle()
-    if workload_name == "c2":
+    if workload_name in FAMILIES:
+        sc = S.family_ensemble(workload_name, 1)
+        desc = f"one instance of the ensemble ({S.FAMILY_RING_SETUPS[workload_name]}(81))"
+    elif workload_name == "c2":
         sc = S.c2_rings_tl(dx=4e-4)
         desc = "same ring-impact TL set-up at dx=0.4 mm"
     elif workload_name == "c3":
@@ -244,7 +260,9 @@ def ours(args, cfg_desc):
 
     sc, cfg = workload(args.workload, args.dx, args.instances)
     n = sc.n_total
-    tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK)
+    if args.workload in FAMILIES and args.precision == "mixed":
+        args.precision = "fp64"  # these families run in the FP64 forms only
+    tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK, M.METHOD_COROT, M.METHOD_POTENTIAL)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"
     if args.tl_tiles:
@@ -332,8 +350,12 @@ def ours(args, cfg_desc):
     kms, klaunch, krows = kstats[dom]
     names = {0: "UL pair (+RK)", 1: "TL pass A", 2: "TL pass B", 3: "contact", 4: "UL stage (grid + gather + pair)",
              5: "weak"}
+    if sc.method == M.METHOD_UL_WEAK:
+        names.update({2: "weak UL particle pass", 5: "weak UL stress-point pass"})
+    elif sc.method in (M.METHOD_COROT, M.METHOD_POTENTIAL):
+        names.update({1: "pass A", 2: "pass B"})
     roof = None
-    if klaunch:
+    if klaunch and sc.method != M.METHOD_UL_WEAK:  # (no byte model for the weak UL passes)
         per_launch_rows = krows / klaunch
         abytes = algorithmic_bytes(dom, mixed, nnz, tl) * per_launch_rows
         achieved = abytes / (kms / klaunch / 1e3) / 1e9
@@ -378,7 +400,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "corot", "godunov", "potential", "ulweak"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--cpu-steps", type=int, default=8)

@@ -404,7 +404,12 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
         p = b.params or {}
         sd = SimData(p.get("nu", sc.nu), p.get("E", sc.E), p.get("rho0", sc.rho0), p.get("wdeltap", sc.wdeltap),
                      sc.corr_exp, sc.mghn_eps, sc.alpha, sc.beta, sc.eta, sc.xsph_eps, sc.do_smooth)
-        grp = (0 if not p else k) if groups is None else groups[k]
+        if groups is not None:
+            grp = groups[k]
+        elif sc.groups is not None:
+            grp = sc.groups[k]
+        else:
+            grp = 0 if not p else k
         bid = sim.add_body(b.arrays, sd, p.get("dt", sc.dt), group=grp)
         for a in sc.actions:
             sim.add_action(bid, a)

@@ -45,7 +45,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for ns, fmad in (("mf_strict", "false"), ("mf_fast", "true")):
             src = os.path.join(CSRC, tu)
             obj = os.path.join(BUILD, f"{tu[:-3]}_{ns}.o")
-            jobs.append((src, obj, base + [f"-DMF_NS={ns}", f"--fmad={fmad}", src, "-o", obj]))
+            strict = "1" if ns == "mf_strict" else "0"
+            jobs.append((src, obj, base + [f"-DMF_NS={ns}", f"-DMF_STRICT_FORM={strict}", f"--fmad={fmad}", src, "-o", obj]))
     for host_tu in ("mf_api.cu", "mf_noalloc.cu", "mf_mlp.cu"):
         src = os.path.join(CSRC, host_tu)
         obj = os.path.join(BUILD, host_tu[:-3] + ".o")

@@ -199,7 +199,8 @@ struct mf_ctx {
 	DevBuf<float> qw32, m32, h32;
 	DevBuf<float4> recA, recB, dA32;
 	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
-	DevBuf<double> sW64, R64;         // corotational: W per pair (sliced ELL), rotation per row
+	DevBuf<double> sW64, R64, av64;   // corotational: W per pair (sliced ELL), rotation per row;
+	                                  // corotational / potential: the viscosity records
 	bool tl_recs_valid = false;       // the stage-0 records match the state (pass B keeps them current)
 	uint32_t n_bc = 0;
 
@@ -218,7 +219,7 @@ struct mf_ctx {
 	// sets), fixed candidate lists, per-evaluation ellipse masks and shape functions
 	DevBuf<uint32_t> uw_gbody, uw_pc_off, uw_pc_nbr, uw_gc_off, uw_gc_nbr, uw_tp_off, uw_tp_gp, uw_tp_slot, uw_bc_of;
 	DevBuf<uint8_t> uw_pmask, uw_gmask;
-	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_gm, uw_gqw;
+	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
 	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
 
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
@@ -758,6 +759,7 @@ TLArgs tl_args(mf_ctx* c) {
 	a.c = c->c64.p;
 	a.sW = c->sW64.p;
 	a.R = c->R64.p;
+	a.av = c->av64.p;
 	a.recA = c->recA.p;
 	a.recB = c->recB.p;
 	a.dA32 = c->dA32.p;
@@ -1054,12 +1056,14 @@ mf_status tl_setup(mf_ctx* c) {
 	if (corot) {
 		CK(c->sW64.alloc(ent));
 		CK(c->R64.alloc(4 * (size_t)n));
+		CK(c->av64.alloc(8 * (size_t)n));
 		e = c->strict ? mf_strict::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream)
 		              : mf_fast::cr_sell_w(n, c->nbr_off.p, c->sl_off.p, w64.p, c->sW64.p, c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "corotational weights");
 	}
 	if (potential) {  // precomp_randles_libersky_symmetric: the reverse pairs' gradients
 		CK(c->sW64.alloc(2 * ent));
+		CK(c->av64.alloc(8 * (size_t)n));
 		e = c->strict ? mf_strict::cr_sell_wji(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->sW64.p,
 		                                       c->stream)
 		              : mf_fast::cr_sell_wji(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->sW64.p,
@@ -1519,7 +1523,7 @@ mf_status uw_setup(mf_ctx* c) {
 	// particles: the weights of the last riemann update (the input weights at first)
 	CK(c->uw_qwp.alloc(n));
 	CK(cudaMemcpy(c->uw_qwp.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
-	CK(c->uw_ph.alloc(n));
+	CK(c->uw_ph.alloc(n)); CK(c->uw_qws.alloc(n));
 	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
 	// candidate lists (CSR, ascending)
 	std::vector<uint32_t> pc, gc;
@@ -1570,7 +1574,7 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 	a.n_p = c->n_total; a.n_g = c->n_g; a.stage = stage; a.flags = c->flags;
 	a.params = c->params.p; a.body_of = c->body_of.p; a.gbody_of = c->uw_gbody.p;
 	a.m = c->m.p; a.gm = c->uw_gm.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
-	a.qw_base = c->uw_qwp.p; a.gqw_base = c->uw_gqw.p;
+	a.qw_base = c->uw_qwp.p; a.gqw_base = c->uw_gqw.p; a.qw_stage = c->uw_qws.p;
 	auto soa = [&](int k) {
 		StateSoA s{};
 		s.x = c->sd[k][0].p; s.y = c->sd[k][1].p; s.vx = c->sd[k][2].p; s.vy = c->sd[k][3].p;
@@ -1597,18 +1601,22 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 }
 
 // The ellipse neighbourhoods and shape functions of the particles (and, when
-// `points`, of the stress points) at the state `a.rd`; `refresh_qw` also stores m / rho
-// as the particles' weights (the smoothing's riemann update, rk4.h:201).
+// `points`, of the stress points) at the state `a.rd`.  The particles' weights: with
+// `refresh_qw` m / rho into the stored weights (the smoothing's riemann update,
+// rk4.h:201), else this evaluation's weights into qw_stage (m / rho when the pipeline
+// updates them, the stored ones otherwise).
 cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refresh_qw) {
 	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
-	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qm, double* qw) {
+	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qs, double* qd) {
 		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
-		                                     qm, qw, c->d_status, c->stream)
-		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qm,
-		                                   qw, c->d_status, c->stream);
+		                                     qs, qd, c->d_status, c->stream)
+		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qs,
+		                                   qd, c->d_status, c->stream);
 	};
-	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc_off, a.pc_nbr, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy,
-	                    refresh_qw ? a.m : nullptr, refresh_qw ? a.qw_base : nullptr);
+	const bool riemann = (c->flags & abit(MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS)) != 0;
+	const double* qs = refresh_qw ? nullptr : (riemann ? nullptr : a.qw_base);
+	double* qd = refresh_qw ? a.qw_base : a.qw_stage;
+	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc_off, a.pc_nbr, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy, qs, qd);
 	if (e == cudaSuccess && points)
 		e = nbh(a.n_g, a.grd.x, a.grd.y, a.gc_off, a.gc_nbr, c->uw_gh.p, a.gmask, a.gw, a.gwx, a.gwy, nullptr, nullptr);
 	return e;

@@ -11,6 +11,9 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#ifndef MF_STRICT_FORM
+#error "MF_STRICT_FORM must be 1 (the FP64 parity form) or 0"
+#endif
 #ifndef MF_NS
 #error "MF_NS must name the kernel namespace (mf_strict or mf_fast)"
 #endif

@@ -56,6 +56,13 @@ inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) 
 
 __device__ __forceinline__ uint32_t sell_base(const TLArgs& a, uint32_t i) { return a.sl_off[i >> 5] + (i & 31u); }
 
+// a 32-byte per-row record through the read-only path, as two 16-byte loads
+__device__ __forceinline__ double4 ld4(const double4* p) {
+	const double2* q = reinterpret_cast<const double2*>(p);
+	double2 u = __ldg(q), v = __ldg(q + 1);
+	return make_double4(u.x, u.y, v.x, v.y);
+}
+
 // precomp_sph: W and grad W per listed pair, with the h of particle i
 __global__ void k_sph(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
                       const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ h, double* w,
@@ -124,12 +131,17 @@ __global__ void __launch_bounds__(256) k_crR(TLArgs a) {
 	double x = Axx + Ayy;
 	double y = Ayx - Axy;
 	double theta = atan2(y, x);
-	double* R = (double*)a.R;
-	const uint32_t n = a.n_total;
-	R[i] = cos(theta);
-	R[n + i] = -sin(theta);
-	R[2 * n + i] = sin(theta);
-	R[3 * n + i] = cos(theta);
+	// R = (cos, -sin; sin, cos) kept as {cos, sin} (Rxy = -sin exactly), with the mass
+	// that the pair forces read alongside
+	((double4*)a.R)[i] = make_double4(cos(theta), sin(theta), a.m[i], 0.);
+}
+
+// the viscosity loop's view of row i: {x, y, vx, vy} and {h, rho, c, m}
+__device__ __forceinline__ void write_av(const TLArgs& a, uint32_t i, double c) {
+	const mfk_host::StateSoA& s = a.st;
+	double4* av = (double4*)a.av;
+	av[2 * i] = make_double4(s.x[i], s.y[i], s.vx[i], s.vy[i]);
+	av[2 * i + 1] = make_double4(a.h[i], s.rho[i], c, a.m[i]);
 }
 
 // displacement gradient in the rotated frame, Cauchy-Green stress, nominal stress
@@ -138,11 +150,10 @@ __global__ void __launch_bounds__(256) k_crA(TLArgs a) {
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
 	const double2* sw = (const double2*)a.sw;
-	const double* R = (const double*)a.R;
-	const uint32_t n = a.n_total;
+	const double4 Ri = ((const double4*)a.R)[i];
 	double xi = s.x[i], yi = s.y[i], Xi = a.X[i], Yi = a.Y[i];
-	// R^-1 = R^T (derivatives.h:219-222)
-	double Rixx_inv = R[i], Rixy_inv = R[2 * n + i], Riyx_inv = R[n + i], Riyy_inv = R[3 * n + i];
+	// R^-1 = R^T (derivatives.h:219-222): (cos, sin; -sin, cos)
+	double Rixx_inv = Ri.x, Rixy_inv = Ri.y, Riyx_inv = -Ri.y, Riyy_inv = Ri.x;
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
 	uint32_t q = sell_base(a, i), c = a.cnt[i];
 	for (uint32_t k = 0; k < c; k++, q += 32) {
@@ -173,9 +184,8 @@ __global__ void __launch_bounds__(256) k_crA(TLArgs a) {
 	}
 	double Pxx = 0., Pxy = 0., Pyx = 0., Pyy = 0.;
 	if (a.flags & A_C2N) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - 0., Sxy, Syy - 0., Pxx, Pxy, Pyx, Pyy);
-	double* P = (double*)a.P;
-	P[i] = Pxx; P[n + i] = Pxy; P[2 * n + i] = Pyx; P[3 * n + i] = Pyy;
-	((double*)a.c)[i] = sqrt(pr.K / s.rho[i]);
+	((double4*)a.P)[i] = make_double4(Pxx, Pxy, Pyx, Pyy);
+	write_av(a, i, sqrt(pr.K / s.rho[i]));
 }
 
 // displacement gradient, Green-St Venant stress and F_e = -2 V (I + H) S per row;
@@ -185,7 +195,7 @@ __global__ void __launch_bounds__(256) k_ptA(TLArgs a) {
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
 	const double2* sw = (const double2*)a.sw;
-	const uint32_t n = a.n_total, flags = a.flags;
+	const uint32_t flags = a.flags;
 	double uxi = s.x[i] - a.X[i], uyi = s.y[i] - a.Y[i];
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0.;
 	if (flags & A_DISP) {
@@ -207,12 +217,9 @@ __global__ void __launch_bounds__(256) k_ptA(TLArgs a) {
 	// -2*voli*Ji*Si: the scalar scales J, then the matrix product, k ascending
 	double sc = -2 * a.qw0[i];
 	double J00 = sc * (Hxx + 1.), J01 = sc * Hyx, J10 = sc * Hxy, J11 = sc * (Hyy + 1.);
-	double* P = (double*)a.P;
-	P[i] = J00 * Sxx + J10 * Sxy;
-	P[n + i] = J01 * Sxx + J11 * Sxy;
-	P[2 * n + i] = J00 * Sxy + J10 * Syy;
-	P[3 * n + i] = J01 * Sxy + J11 * Syy;
-	((double*)a.c)[i] = sqrt(pr.K / s.rho[i]);
+	((double4*)a.P)[i] = make_double4(J00 * Sxx + J10 * Sxy, J01 * Sxx + J11 * Sxy, J00 * Sxy + J10 * Syy,
+	                                  J01 * Sxy + J11 * Syy);
+	write_av(a, i, sqrt(pr.K / s.rho[i]));
 }
 
 // pair forces (rotated stresses or elastic potential), contact force, viscosity,
@@ -223,47 +230,57 @@ __global__ void __launch_bounds__(256) k_crB(TLArgs a) {
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
 	const double2* sw = (const double2*)a.sw;
-	const double* P = (const double*)a.P;
-	const double* R = (const double*)a.R;
-	const double* cc = (const double*)a.c;
-	const uint32_t n = a.n_total;
+	const double4* P = (const double4*)a.P;
+	const double4* R = (const double4*)a.R;
+	const double4* av = (const double4*)a.av;
 	const uint32_t flags = a.flags;
 	const BodyParams& pr = a.params[a.body_of[i]];
 	const double rho0 = pr.rho0;
 	double vx_t = 0., vy_t = 0.;
 	const uint32_t q0 = sell_base(a, i), c = a.cnt[i];
+	const double4 Pi = P[i];
 	if (POT && (flags & mfk_host::FLAG_POTENTIAL)) {
 		const double2* swji = (const double2*)a.sW;
-		double F00i = P[i], F01i = P[n + i], F10i = P[2 * n + i], F11i = P[3 * n + i];
 		double mi = a.m[i];
+#if !MF_STRICT_FORM
+		const double inv_mi = 1. / mi;
+#endif
 		uint32_t q = q0;
 		for (uint32_t k = 0; k < c; k++, q += 32) {
 			uint32_t j = a.snbr[q];
 			double2 w = sw[q], wji = swji[q];
-			double fij0 = F00i * w.x + F10i * w.y;
-			double fij1 = F01i * w.x + F11i * w.y;
-			double fji0 = P[j] * wji.x + P[2 * n + j] * wji.y;
-			double fji1 = P[n + j] * wji.x + P[3 * n + j] * wji.y;
+			double4 Fj = ld4(P + j);  // F_e column-major: F[0][0], F[0][1], F[1][0], F[1][1]
+			double fij0 = Pi.x * w.x + Pi.z * w.y;
+			double fij1 = Pi.y * w.x + Pi.w * w.y;
+			double fji0 = Fj.x * wji.x + Fj.z * wji.y;
+			double fji1 = Fj.y * wji.x + Fj.w * wji.y;
+#if MF_STRICT_FORM
 			vx_t += 0.5 * (fji0 - fij0) / mi;
 			vy_t += 0.5 * (fji1 - fij1) / mi;
+#else
+			vx_t += 0.5 * (fji0 - fij0) * inv_mi;
+			vy_t += 0.5 * (fji1 - fij1) * inv_mi;
+#endif
 		}
 		vx_t += a.fcx[i] / a.m[i];
 		vy_t += a.fcy[i] / a.m[i];
 	}
 	if (!POT && (flags & A_CR_STRESS)) {
-		double Pxxi = P[i], Pxyi = P[n + i], Pyxi = P[2 * n + i], Pyyi = P[3 * n + i];
-		double Rxxi = R[i], Rxyi = R[n + i], Ryxi = R[2 * n + i], Ryyi = R[3 * n + i];
+		double Pxxi = Pi.x, Pxyi = Pi.y, Pyxi = Pi.z, Pyyi = Pi.w;
+		const double4 Ri = R[i];
+		double Rxxi = Ri.x, Rxyi = -Ri.y, Ryxi = Ri.y, Ryyi = Ri.x;
 		double rhoi21 = 1. / (rho0 * rho0);
 		uint32_t q = q0;
 		for (uint32_t k = 0; k < c; k++, q += 32) {
 			uint32_t j = a.snbr[q];
 			double2 w = sw[q];
-			double Pxxj = P[j], Pxyj = P[n + j], Pyxj = P[2 * n + j], Pyyj = P[3 * n + j];
-			double Rxxj = R[j], Rxyj = R[n + j], Ryxj = R[2 * n + j], Ryyj = R[3 * n + j];
-			double mj = a.m[j];
-			double rhoj21 = 1. / (rho0 * rho0);
-			double aijx = mj * ((Pxxi * rhoi21 + Pxxj * rhoj21) * w.x + (Pxyi * rhoi21 + Pxyj * rhoj21) * w.y);
-			double aijy = mj * ((Pyxi * rhoi21 + Pyxj * rhoj21) * w.x + (Pyyi * rhoi21 + Pyyj * rhoj21) * w.y);
+			double4 Pj = ld4(P + j);
+			double4 Rj = ld4(R + j);  // {cos, sin, m, 0}
+			double Rxxj = Rj.x, Rxyj = -Rj.y, Ryxj = Rj.y, Ryyj = Rj.x;
+			double mj = Rj.z;
+			double rhoj21 = rhoi21;  // 1. / (rho0 * rho0), the same expression per pair
+			double aijx = mj * ((Pxxi * rhoi21 + Pj.x * rhoj21) * w.x + (Pxyi * rhoi21 + Pj.y * rhoj21) * w.y);
+			double aijy = mj * ((Pyxi * rhoi21 + Pj.z * rhoj21) * w.x + (Pyyi * rhoi21 + Pj.w * rhoj21) * w.y);
 			double ajix = -aijx;
 			double ajiy = -aijy;
 			double aijxprime = aijx * Rxxi + aijy * Rxyi;
@@ -276,22 +293,25 @@ __global__ void __launch_bounds__(256) k_crB(TLArgs a) {
 		vx_t += a.fcx[i] / a.m[i];
 		vy_t += a.fcy[i] / a.m[i];
 	}
-	double xi = s.x[i], yi = s.y[i], vxi = s.vx[i], vyi = s.vy[i];
+	const double4 ai0 = av[2 * i], ai1 = av[2 * i + 1];
+	double xi = ai0.x, yi = ai0.y, vxi = ai0.z, vyi = ai0.w;
 	if (flags & A_ART_VISC) {
-		double hi = a.h[i], rhoi = s.rho[i], ci = cc[i];
+		double hi = ai1.x, rhoi = ai1.y, ci = ai1.z;
 		double alpha = pr.alpha, beta = pr.beta, eta = pr.eta;
 		uint32_t q = q0;
 		for (uint32_t k = 0; k < c; k++, q += 32) {
 			uint32_t j = a.snbr[q];
-			double vijx = vxi - s.vx[j], vijy = vyi - s.vy[j];
-			double xij = xi - s.x[j], yij = yi - s.y[j];
+			double4 aj0 = ld4(av + 2 * j);
+			double vijx = vxi - aj0.z, vijy = vyi - aj0.w;
+			double xij = xi - aj0.x, yij = yi - aj0.y;
 			double vijposij = vijx * xij + vijy * yij;
 			if (vijposij < 0.) {
+				double4 aj1 = ld4(av + 2 * j + 1);  // {h, rho, c, m}
 				double2 w = sw[q];
-				double mj = a.m[j];
-				double cij = 0.5 * (ci + cc[j]);
-				double hij = 0.5 * (hi + a.h[j]);
-				double rhoij = 0.5 * (rhoi + s.rho[j]);
+				double mj = aj1.w;
+				double cij = 0.5 * (ci + aj1.z);
+				double hij = 0.5 * (hi + aj1.x);
+				double rhoij = 0.5 * (rhoi + aj1.y);
 				double r2ij = xij * xij + yij * yij;
 				double muij = (hij * vijposij) / (r2ij + eta * eta * hij * hij);
 				double piij = (-alpha * cij * muij + beta * muij * muij) / rhoij;

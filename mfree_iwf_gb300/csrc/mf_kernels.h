@@ -129,7 +129,9 @@ struct TLArgs {
 	void *P, *dA, *c;                    // per-stage scratch (FP64 forms)
 	const void* sW;                      // corotational: kernel value W per pair (double, sliced ELL);
 	                                     // potential: grad W of the reverse pair (double2, sliced ELL)
-	void* R;                             // corotational: rotation per row, 4 x n doubles (Rxx, Rxy, Ryx, Ryy)
+	void* R;                             // corotational: per row double4 {cos, sin, m, 0} of the rotation
+	void* av;                            // corotational / potential: per row two double4 records
+	                                     // {x, y, vx, vy} and {h, rho, c, m} for the viscosity loop
 	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
 	void* recB_out;                      // mixed: pass B writes the next stage's records here...
 	uint32_t write_recs;                 // ...and into recA when set (no separate pack then)
@@ -191,6 +193,7 @@ struct UWArgs {
 	const uint32_t *body_of, *gbody_of;
 	const double *m, *gm, *fcx, *fcy;
 	double *qw_base, *gqw_base;          // quad weights of the particles / stress points
+	double* qw_stage;                    // the particles' weights of this evaluation
 	StateSoA base, acc, rd, wr;          // particles: this stage reads rd, writes wr
 	GSoA gbase, gacc, grd, gwr;          // stress points
 	const uint32_t *pc_off, *pc_nbr, *gc_off, *gc_nbr;  // candidate lists
@@ -268,7 +271,7 @@ struct ContactArgs {
 	cudaError_t weak_stage(const mfk_host::WeakArgs& a, bool mixed, int part, cudaStream_t s);               \
 	cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr, \
 	                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,  \
-	                   uint8_t* mask, double* w, double* wx, double* wy, const double* set_qw_m, double* set_qw, \
+	                   uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,   \
 	                   void* status, cudaStream_t s);                                                       \
 	cudaError_t uw_stage(const mfk_host::UWArgs& a, int part, cudaStream_t s);                                \
 	}

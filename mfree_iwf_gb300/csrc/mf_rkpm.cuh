@@ -7,6 +7,15 @@
 
 #include "mf_common.cuh"
 
+// The neighbour volume factor m_j / rho_j of every moment term: the parity form keeps
+// the reference's (term * m_j) / rho_j; the fast form multiplies by v_j = m_j / rho_j,
+// formed once per neighbour (one FP64 division instead of 27).
+#if MF_STRICT_FORM
+#define MF_RKPM_VOL * mj / rhoj
+#else
+#define MF_RKPM_VOL * vj
+#endif
+
 namespace MF_NS {
 namespace {
 
@@ -25,39 +34,42 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 		if (!use(q)) continue;
 		uint32_t j = nbr[q];
 		double mj = fm[j], rhoj = rho(j);
+#if !MF_STRICT_FORM
+		const double vj = mj / rhoj;
+#endif
 		double xj = fx[j], yj = fy[j];
 		double rx = xi - xj, ry = yi - yj;
 		const double rx_x = 1., rx_y = 0., ry_x = 0., ry_y = 1.;
 		mfk::KR64 w = mfk::cubic_spline(xi - xj, yi - yj, hi);
-		M[0][0] += w.w * mj / rhoj;
-		M[0][1] += w.w * rx * mj / rhoj;
-		M[0][2] += w.w * ry * mj / rhoj;
-		M[1][0] += w.w * rx * mj / rhoj;
-		M[2][0] += w.w * ry * mj / rhoj;
-		M[1][1] += rx * rx * w.w * mj / rhoj;
-		M[1][2] += rx * ry * w.w * mj / rhoj;
-		M[2][1] += ry * rx * w.w * mj / rhoj;
-		M[2][2] += ry * ry * w.w * mj / rhoj;
+		M[0][0] += w.w MF_RKPM_VOL;
+		M[0][1] += w.w * rx MF_RKPM_VOL;
+		M[0][2] += w.w * ry MF_RKPM_VOL;
+		M[1][0] += w.w * rx MF_RKPM_VOL;
+		M[2][0] += w.w * ry MF_RKPM_VOL;
+		M[1][1] += rx * rx * w.w MF_RKPM_VOL;
+		M[1][2] += rx * ry * w.w MF_RKPM_VOL;
+		M[2][1] += ry * rx * w.w MF_RKPM_VOL;
+		M[2][2] += ry * ry * w.w MF_RKPM_VOL;
 
-		Mx[0][0] += w.w_x * mj / rhoj;
-		Mx[0][1] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
-		Mx[0][2] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
-		Mx[1][0] += w.w_x * rx * mj / rhoj + w.w * rx_x * mj / rhoj;
-		Mx[2][0] += w.w_x * ry * mj / rhoj + w.w * rx_y * mj / rhoj;
-		Mx[1][1] += rx * rx * w.w_x * mj / rhoj + w.w * (rx_x * rx + rx * rx_x) * mj / rhoj;
-		Mx[1][2] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_x * ry + rx * rx_y) * mj / rhoj;
-		Mx[2][1] += rx * ry * w.w_x * mj / rhoj + w.w * (rx_y * rx + ry * rx_x) * mj / rhoj;
-		Mx[2][2] += ry * ry * w.w_x * mj / rhoj + w.w * (rx_y * ry + ry * rx_y) * mj / rhoj;
+		Mx[0][0] += w.w_x MF_RKPM_VOL;
+		Mx[0][1] += w.w_x * rx MF_RKPM_VOL + w.w * rx_x MF_RKPM_VOL;
+		Mx[0][2] += w.w_x * ry MF_RKPM_VOL + w.w * rx_y MF_RKPM_VOL;
+		Mx[1][0] += w.w_x * rx MF_RKPM_VOL + w.w * rx_x MF_RKPM_VOL;
+		Mx[2][0] += w.w_x * ry MF_RKPM_VOL + w.w * rx_y MF_RKPM_VOL;
+		Mx[1][1] += rx * rx * w.w_x MF_RKPM_VOL + w.w * (rx_x * rx + rx * rx_x) MF_RKPM_VOL;
+		Mx[1][2] += rx * ry * w.w_x MF_RKPM_VOL + w.w * (rx_x * ry + rx * rx_y) MF_RKPM_VOL;
+		Mx[2][1] += rx * ry * w.w_x MF_RKPM_VOL + w.w * (rx_y * rx + ry * rx_x) MF_RKPM_VOL;
+		Mx[2][2] += ry * ry * w.w_x MF_RKPM_VOL + w.w * (rx_y * ry + ry * rx_y) MF_RKPM_VOL;
 
-		My[0][0] += w.w_y * mj / rhoj;
-		My[0][1] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
-		My[0][2] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
-		My[1][0] += w.w_y * rx * mj / rhoj + w.w * ry_x * mj / rhoj;
-		My[2][0] += w.w_y * ry * mj / rhoj + w.w * ry_y * mj / rhoj;
-		My[1][1] += rx * rx * w.w_y * mj / rhoj + w.w * (ry_x * rx + rx * ry_x) * mj / rhoj;
-		My[1][2] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_x * ry + rx * ry_y) * mj / rhoj;
-		My[2][1] += rx * ry * w.w_y * mj / rhoj + w.w * (ry_y * rx + ry * ry_x) * mj / rhoj;
-		My[2][2] += ry * ry * w.w_y * mj / rhoj + w.w * (ry_y * ry + ry * ry_y) * mj / rhoj;
+		My[0][0] += w.w_y MF_RKPM_VOL;
+		My[0][1] += w.w_y * rx MF_RKPM_VOL + w.w * ry_x MF_RKPM_VOL;
+		My[0][2] += w.w_y * ry MF_RKPM_VOL + w.w * ry_y MF_RKPM_VOL;
+		My[1][0] += w.w_y * rx MF_RKPM_VOL + w.w * ry_x MF_RKPM_VOL;
+		My[2][0] += w.w_y * ry MF_RKPM_VOL + w.w * ry_y MF_RKPM_VOL;
+		My[1][1] += rx * rx * w.w_y MF_RKPM_VOL + w.w * (ry_x * rx + rx * ry_x) MF_RKPM_VOL;
+		My[1][2] += rx * ry * w.w_y MF_RKPM_VOL + w.w * (ry_x * ry + rx * ry_y) MF_RKPM_VOL;
+		My[2][1] += rx * ry * w.w_y MF_RKPM_VOL + w.w * (ry_y * rx + ry * ry_x) MF_RKPM_VOL;
+		My[2][2] += ry * ry * w.w_y MF_RKPM_VOL + w.w * (ry_y * ry + ry * ry_y) MF_RKPM_VOL;
 	}
 	// solve3x3 (Cramer's rule, precomp_shape_functions.h:31-50)
 	auto solve = [&](const double r[3], double x[3]) {

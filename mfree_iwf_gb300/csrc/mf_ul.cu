@@ -482,6 +482,7 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
 	double av_x = 0., av_y = 0., xs_x = 0., xs_y = 0.;
 	double god_rho = 0., god_vx = 0., god_vy = 0.;
+	const double two_rhoi = 2. / ri.rho;  // godunov.h:127-133's 2./rhoi, the same per pair
 	uint32_t cnt = 0;
 	for (int ni = lo_i; ni < hi_i; ni++) {
 		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
@@ -543,19 +544,31 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 			if ((flags & (A_GOD_CONT | A_GOD_MOM)) && kj != k) {
 				// |x_j - x_i| from the predicate's own sum (the same value as the
 				// reference's sqrt(dx*dx + dy*dy) and sqrt(dot(R, R)))
-				double mag_r = sqrt(r2);
+				const double mag_r = sqrt(r2);
+				// the acoustic Riemann denominator, the same expression in both actions
+				const double frac = 1. / (ri.rho * ri.c + rj.rho * rj.c);
+#if !MF_STRICT_FORM
+				const double inv_r = 1. / mag_r;
+#endif
 				if (flags & A_GOD_CONT) {  // godunov_continuity, godunov.h:144-187
+#if MF_STRICT_FORM
 					double nx = xij / mag_r, ny = yij / mag_r;
+#else
+					double nx = xij * inv_r, ny = yij * inv_r;
+#endif
 					double vir = ri.vx * nx + ri.vy * ny;
 					double vjr = rj.vx * nx + rj.vy * ny;
 					// riemann_solver_acoustic (godunov.h:41-54); Rxx = p
-					double frac = 1. / (ri.rho * ri.c + rj.rho * rj.c);
 					double ustar = frac * (vir * ri.rho * ri.c + vjr * rj.rho * rj.c - ri.Rxx + rj.Rxx);
 					god_rho += 2 * ri.rho * (vir - ustar) * (w.w_x * nx + w.w_y * ny) * rj.qw;
 				}
 				if (flags & A_GOD_MOM) {  // godunov_get_trafo + godunov_momentum, godunov.h:56-142
 					double rx = rj.x - ri.x, ry = rj.y - ri.y;
+#if MF_STRICT_FORM
 					double inv = 1. / mag_r;  // glm::normalize: v * (1 / sqrt(dot(v, v)))
+#else
+					double inv = inv_r;
+#endif
 					double Rx = rx * inv, Ry = ry * inv, Sx = ry * inv, Sy = -rx * inv;
 					// the frame matrix is single precision (a glm::mat2x2 of the unit vectors)
 					double lRx = (double)__double2float_rn(Rx), lRy = (double)__double2float_rn(Ry);
@@ -563,18 +576,16 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 					// stress times R: (Sxx - p, Sxy; Sxy, Syy), Rxy = Syy
 					double siR0 = ri.sxx * Rx + ri.sxy * Ry, siR1 = ri.sxy * Rx + ri.Rxy * Ry;
 					double sjR0 = rj.sxx * Rx + rj.sxy * Ry, sjR1 = rj.sxy * Rx + rj.Rxy * Ry;
-					double si0 = lRx * siR0 + lSx * siR1, si1 = lRy * siR0 + lSy * siR1;
+					double si0 = lRx * siR0 + lSx * siR1;
 					double sj0 = lRx * sjR0 + lSx * sjR1, sj1 = lRy * sjR0 + lSy * sjR1;
 					double vi0 = lRx * ri.vx + lSx * ri.vy, vi1 = lRy * ri.vx + lSy * ri.vy;
 					double vj0 = lRx * rj.vx + lSx * rj.vy, vj1 = lRy * rj.vx + lSy * rj.vy;
-					double rci = ri.rho * ri.c, rcj = rj.rho * rj.c;
-					double frac = 1. / (rci + rcj);
 					// the second component takes sigma_j twice (godunov.h:116), as the reference does
 					double S0 = frac * (sj0 * ri.rho * ri.c + si0 * rj.rho * rj.c + ri.rho * ri.c * rj.rho * rj.c * (vj0 - vi0));
 					double S1 = frac * (sj1 * ri.rho * ri.c + sj1 * rj.rho * rj.c + ri.rho * ri.c * rj.rho * rj.c * (vj1 - vi1));
 					double SR0 = lRx * S0 + lRy * S1, SR1 = lSx * S0 + lSy * S1;
-					if (fabs(rx) > 0.) god_vx += 2. / ri.rho * w.w_x * mag_r / rx * SR0 * rj.qw;
-					if (fabs(ry) > 0.) god_vy += 2. / ri.rho * w.w_y * mag_r / ry * SR1 * rj.qw;
+					if (fabs(rx) > 0.) god_vx += two_rhoi * w.w_x * mag_r / rx * SR0 * rj.qw;
+					if (fabs(ry) > 0.) god_vy += two_rhoi * w.w_y * mag_r / ry * SR1 * rj.qw;
 				}
 			}
 		}

@@ -48,13 +48,14 @@ enum : uint32_t {
 };
 
 // nbh_ellipse for query point i over its candidates, then the RKPM shape functions of
-// the candidates inside the ellipse.  set_qw (the smoothing's
-// riemann_update_integration_weights) also refreshes the row's weight m / rho.
+// the candidates inside the ellipse.  With qw_dst the row also stores its integration
+// weight for the passes: m / rho (riemann_update_integration_weights) when qw_src is
+// null, else qw_src (the weights of the last update).
 __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
                          const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
                          const double* __restrict__ frho, double* h_out, uint8_t* mask, double* w, double* wx,
-                         double* wy, const double* __restrict__ set_qw_m, double* set_qw, DevStatus* st) {
+                         double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n_to) return;
 	const double px = tx[i], py = ty[i];
@@ -104,17 +105,16 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 		cnt += in ? 1u : 0u;
 	}
 	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
-	if (set_qw) set_qw[i] = set_qw_m[i] / frho[i];
+	if (qw_dst) qw_dst[i] = qw_src ? qw_src[i] : fm[i] / frho[i];
 	auto rho = [&](uint32_t j) { return frho[j]; };
 	auto use = [&](uint32_t q) { return mask[q] != 0; };
 	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
 	if (!rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)) raise(st, ERR_SINGULAR, i);
 }
 
-// the particles' integration weight of this evaluation (riemann_update_integration_weights)
-__device__ __forceinline__ double p_qw(const UWArgs& a, uint32_t j) {
-	return (a.flags & A_RIEMANN) ? a.m[j] / a.rd.rho[j] : a.qw_base[j];
-}
+// the particles' integration weight of this evaluation (riemann_update_integration_weights),
+// stored by k_uw_nbh
+__device__ __forceinline__ double p_qw(const UWArgs& a, uint32_t j) { return a.qw_stage[j]; }
 
 // rk_add (rk4.h:52-69) for stages 0-2, the 1-2-2-1 combine (rk4.h:168-182) at stage 3
 __device__ __forceinline__ void uw_rk(uint32_t stg, double dt, uint32_t i, int nf, double* const* bp,
@@ -260,11 +260,11 @@ __global__ void k_uw_smooth_copy(UWArgs a) {
 
 cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
                    const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,
-                   uint8_t* mask, double* w, double* wx, double* wy, const double* set_qw_m, double* set_qw,
+                   uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,
                    void* status, cudaStream_t s) {
 	if (n_to == 0) return cudaSuccess;
 	k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx, wy,
-	                                          set_qw_m, set_qw, reinterpret_cast<DevStatus*>(status));
+	                                          qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
 	return cudaGetLastError();
 }
 

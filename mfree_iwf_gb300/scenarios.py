@@ -114,6 +114,9 @@ class Scenario:
     gp_rho: float = 0.0
     contact: int = 0
     name: str = ""
+    # contact groups per body (bodies touch only within their group); None: all in group 0,
+    # or one group per body when bodies carry their own constants (ensembles of one body)
+    groups: Optional[List[int]] = None
 
     @property
     def n_total(self) -> int:
@@ -631,10 +634,10 @@ def _ul_weak_body(x, y, X, Y, gx, gy, GX, GY, dx, hdx, rho0, vx=0.0, vy=0.0) -> 
     return b
 
 
-def _ul_weak_scenario(bodies, actions, dt, dx, name, contact=0) -> Scenario:
+def _ul_weak_scenario(bodies, actions, dt, dx, name, contact=0, nu=0.4, E=1e7, rho0=1.0) -> Scenario:
     # correction_constants(.., 0, true): velocity smoothing on, the rest zero;
     # candidates by find_neighbors(.., 1.5*dx, distance_manhattan)
-    sc = Scenario(method=METHOD_UL_WEAK, bodies=bodies, actions=list(actions), dt=dt, nu=0.4, E=1e7, rho0=1.0,
+    sc = Scenario(method=METHOD_UL_WEAK, bodies=bodies, actions=list(actions), dt=dt, nu=nu, E=E, rho0=rho0,
                   do_smooth=1, contact=contact, name=name)
     sc.nbh_h = 1.5 * dx
     return sc
@@ -684,6 +687,79 @@ def rings_ul_weak_contact(nbox: int) -> Scenario:
         b.hull = convex_hull(xs, y)
         bodies.append(b)
     return _ul_weak_scenario(bodies, RINGS_UL_WEAK_ACTIONS, 1e-7, dx, f"rings_ul_weak_contact({nbox})", contact=1)
+
+
+# ------------------------------------------------- workloads of the other families
+def family_rings(family: str, dx: float = 5e-5) -> Scenario:
+    """The ring-impact workload (two bodies with penalty contact, the constants of
+    :func:`c1_rings`) run by another SPH family: "corot" (corotational, viscosity
+    1/1/0.1 as rings_corot_contact), "potential" (elastic potential, the same
+    viscosity) or "godunov" (Godunov UL, no correction terms)."""
+    if family == "corot":
+        return c1_rings(dx=dx, two_bodies=True, method=METHOD_COROT, alpha=1.0, beta=1.0, eta=0.1)
+    if family == "potential":
+        return c1_rings(dx=dx, two_bodies=True, method=METHOD_POTENTIAL, alpha=1.0, beta=1.0, eta=0.1)
+    if family == "godunov":
+        return c1_rings(dx=dx, two_bodies=True, method=METHOD_UL, godunov=True)
+    raise ValueError(family)
+
+
+def plate_ul_weak(dx: float = 5e-5, Lx: float = 0.1, Ly: float = 0.02, seed: int = 20261203,
+                  jitter: float = 0.01) -> Scenario:
+    """Uniaxial tension of the steel plate of :func:`c3_plate` with the weak UL form
+    (tensile_ul_weak structure): particles on the jittered lattice, one stress point per
+    cell centre, velocity conditions +-1 m/s on the end columns, h = dx, candidates by
+    the 1.5 dx Manhattan search, dt = 0.3 dx / c0, smoothing on."""
+    nx = int(round(Lx / dx)) + 1
+    ny = int(round(Ly / dx)) + 1
+    I, J = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64), indexing="ij")
+    x, y = (I * dx).ravel(), (J * dx).ravel()
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        x = x + rng.uniform(-jitter, jitter, x.shape) * dx
+        y = y + rng.uniform(-jitter, jitter, y.shape) * dx
+    I, J = np.meshgrid(np.arange(nx - 1, dtype=np.float64), np.arange(ny - 1, dtype=np.float64), indexing="ij")
+    gx, gy = (I * dx + dx / 2).ravel(), (J * dx + dx / 2).ravel()
+    rho0, E, nu = 7850.0, 2e11, 0.3
+    b = _ul_weak_body(x, y, None, None, gx, gy, None, None, dx, 1.0, rho0)
+    left = np.arange(ny, dtype=np.uint32)
+    right = (np.uint32(nx - 1) * np.uint32(ny) + left).astype(np.uint32)
+    b.bcs = [BC(BC_VELOCITY_UL, -1.0, left), BC(BC_VELOCITY_UL, 1.0, right)]
+    sc = _ul_weak_scenario([b], TENSILE_UL_WEAK_ACTIONS, 0.0, dx, f"plate dx={dx} (weak UL)", nu=nu, E=E, rho0=rho0)
+    sc.dt = 0.3 * dx / sc.c0
+    return sc
+
+
+FAMILY_RING_SETUPS = {"corot": "rings_corot_contact", "godunov": "rings_godunov_contact",
+                      "potential": "rings_potential_contact", "ulweak": "rings_ul_weak_contact"}
+
+
+def family_ensemble(family: str, instances: int = 256, nbox: int = 81, seed: int = 20261203,
+                    E_range=(0.8e7, 1.2e7)) -> Scenario:
+    """An ensemble of independent two-ring impacts of one SPH family, each the
+    reference's own set-up (rings_corot_contact, rings_godunov_contact,
+    rings_potential_contact or rings_ul_weak_contact at nbox) with its own seeded
+    Young's modulus E ~ U[E_range]; the two rings of an instance form one contact group.
+    (The reference's potential and Godunov rings do not stay finite at much finer
+    lattices, so the ensemble, not one large lattice, gives the size.)"""
+    make = globals()[FAMILY_RING_SETUPS[family]]
+    base = make(nbox)
+    bodies, groups = [], []
+    for k in range(instances):
+        E = float(np.random.default_rng(seed + k).uniform(*E_range))
+        for b in base.bodies:
+            nb = Body({f: a.copy() for f, a in b.arrays.items()}, hull=b.hull.copy(), bcs=list(b.bcs), ex=b.ex,
+                      ey=b.ey, params={"E": E})
+            if b.gp is not None:
+                nb.gp = {f: a.copy() for f, a in b.gp.items()}
+            bodies.append(nb)
+            groups.append(k)
+    sc = Scenario(method=base.method, bodies=bodies, actions=list(base.actions), dt=base.dt, nu=base.nu, E=base.E,
+                  rho0=base.rho0, wdeltap=base.wdeltap, corr_exp=base.corr_exp, mghn_eps=base.mghn_eps,
+                  alpha=base.alpha, beta=base.beta, eta=base.eta, xsph_eps=base.xsph_eps, do_smooth=base.do_smooth,
+                  nbh_h=base.nbh_h, nbh_eps=base.nbh_eps, contact=base.contact, groups=groups,
+                  name=f"ensemble of {instances} x {base.name}")
+    return sc
 
 
 # ---------------------------------------------------------------- case files
