@@ -98,6 +98,52 @@ __global__ void k_f32_to_f64_rows(uint32_t n, const float* __restrict__ a, doubl
 	if (i < n) b[i] = (rho ? P[body_of[i]].rho0 : 0.) + (double)a[i];
 }
 
+// All-body state transfers in one pass when the host arrays are device-accessible
+// (pinned and mapped, or system memory the GPU reaches through the CPU's page tables,
+// as on a C2C-coupled Grace host): each row's fields cross the link once, coalesced,
+// with the FP32 conversion of the mixed form and the copy into the TL stage set fused.
+// Same values as the copy-and-convert path.
+struct StateIO {
+	const double* src[8];  // set: host x y vx vy rho Sxx Sxy Syy (null: field untouched)
+	double* dst[10];       // get: host x y vx vy rho Sxx Sxy Syy fcx fcy (null: not read)
+	double* sd0[8];        // device FP64 state (null where the mixed form keeps FP32)
+	double* sd2[8];        // device TL stage-0 copy (null: none)
+	float* sf0[4];         // mixed: rho - rho0, Sxx, Sxy, Syy
+	float* sf2[4];
+	const double *fcx, *fcy;
+};
+__global__ void k_set_state_io(uint32_t n, StateIO io, const uint32_t* __restrict__ body_of,
+                               const BodyParams* __restrict__ P) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		if (!io.src[q]) continue;
+		double v = io.src[q][i];
+		if (q >= 4 && io.sf0[q - 4]) {
+			float f = (float)(v - (q == 4 ? P[body_of[i]].rho0 : 0.));
+			io.sf0[q - 4][i] = f;
+			if (io.sf2[q - 4]) io.sf2[q - 4][i] = f;
+		} else {
+			io.sd0[q][i] = v;
+			if (io.sd2[q]) io.sd2[q][i] = v;
+		}
+	}
+}
+__global__ void k_get_state_io(uint32_t n, StateIO io, const uint32_t* __restrict__ body_of,
+                               const BodyParams* __restrict__ P) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		if (!io.dst[q]) continue;
+		if (q >= 4 && io.sf0[q - 4]) io.dst[q][i] = (q == 4 ? P[body_of[i]].rho0 : 0.) + (double)io.sf0[q - 4][i];
+		else io.dst[q][i] = io.sd0[q][i];
+	}
+	if (io.dst[8]) io.dst[8][i] = io.fcx[i];
+	if (io.dst[9]) io.dst[9][i] = io.fcy[i];
+}
+
 struct HostBC {
 	int32_t kind;
 	double v;
@@ -2118,6 +2164,40 @@ MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 	return MF_OK;
 }
 
+// The device address of host memory the GPU can read and write directly, or null:
+// pinned (registered) memory through its mapping, other system memory when the device
+// reaches pageable memory through the host's page tables.
+const void* device_view(mf_ctx* c, const void* h) {
+	if (!h) return nullptr;
+	cudaPointerAttributes at{};
+	if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+	if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return h;
+	int pageable = 0;
+	cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->cfg.device);
+	return pageable ? h : nullptr;
+}
+
+// The fused transfer's device view of the state (set 2 for TL stage 0 when `stage_copy`).
+StateIO state_io(mf_ctx* c, bool stage_copy) {
+	StateIO io{};
+	for (int q = 0; q < 8; q++) {
+		const bool f32 = c->mixed && q >= 4;
+		io.sd0[q] = f32 ? nullptr : c->sd[0][q].p;
+		io.sd2[q] = (f32 || !stage_copy) ? nullptr : c->sd[2][q].p;
+		if (f32) {
+			io.sf0[q - 4] = c->sf[0][q - 4].p;
+			io.sf2[q - 4] = stage_copy ? c->sf[2][q - 4].p : nullptr;
+		}
+	}
+	io.fcx = c->fcx.p;
+	io.fcy = c->fcy.p;
+	return io;
+}
+
 MF_API mf_status mf_get_state_all(mf_ctx* c, const mf_state* out) {
 	if (!c || !out) return MF_ERR_ARG;
 	if (!c->ready) {
@@ -2134,6 +2214,22 @@ MF_API mf_status mf_get_state_all(mf_ctx* c, const mf_state* out) {
 	CK(cudaSetDevice(c->cfg.device));
 	const uint32_t n = c->n_total;
 	double* o[8] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy};
+	{
+		StateIO io = state_io(c, false);
+		double* all[10] = {o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], out->fcx, out->fcy};
+		bool direct = c->cfg.method != MF_METHOD_TL_WEAK && c->cfg.method != MF_METHOD_UL_WEAK;
+		for (int q = 0; q < 10 && direct; q++) {
+			if (!all[q]) continue;
+			io.dst[q] = (double*)device_view(c, all[q]);
+			direct = io.dst[q] != nullptr;
+		}
+		if (direct) {
+			if (n) k_get_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
+			CK(cudaGetLastError());
+			CK(cudaStreamSynchronize(c->stream));
+			return MF_OK;
+		}
+	}
 	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)n));
 	for (int q = 0; q < 8; q++) {
 		if (!o[q]) continue;
@@ -2168,8 +2264,26 @@ MF_API mf_status mf_set_state_all(mf_ctx* c, const mf_particles* p) {
 	CK(cudaSetDevice(c->cfg.device));
 	const uint32_t n = c->n_total;
 	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
-	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)n));
 	const bool tl = c->cfg.method != MF_METHOD_UL;  // TL stage 0 starts from its own copy (set 2)
+	{
+		StateIO io = state_io(c, tl);
+		bool direct = c->cfg.method != MF_METHOD_TL_WEAK && c->cfg.method != MF_METHOD_UL_WEAK;
+		for (int q = 0; q < 8 && direct; q++) {
+			if (!src[q]) continue;
+			io.src[q] = (const double*)device_view(c, src[q]);
+			direct = io.src[q] != nullptr;
+		}
+		if (direct) {
+			if (n) k_set_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
+			CK(cudaGetLastError());
+			c->tl_recs_valid = false;  // mixed TL: re-pack the records from the new state
+			mf_status pst = tl_prepack(c);
+			if (pst != MF_OK) return pst;
+			CK(cudaStreamSynchronize(c->stream));
+			return MF_OK;
+		}
+	}
+	if (c->mixed && !c->staging.p) CK(c->staging.alloc(4 * (size_t)n));
 	for (int q = 0; q < 8; q++) {
 		if (!src[q]) continue;
 		if (c->mixed && q >= 4) {
