@@ -247,6 +247,10 @@ struct mf_ctx {
 	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
 	DevBuf<double> sW64, R64, av64;   // corotational: W per pair (sliced ELL), rotation per row;
 	                                  // corotational / potential: the viscosity records
+	// corotational / potential, mixed form (TLArgs::cm_*)
+	DevBuf<float2> cm_sw, cm_swA, cm_sX, cm_swji;
+	DevBuf<float> cm_sW;
+	DevBuf<float4> cm_U, cm_X, cm_V, cm_P, cm_R, cm_H;
 	bool tl_recs_valid = false;       // the stage-0 records match the state (pass B keeps them current)
 	uint32_t n_bc = 0;
 
@@ -806,6 +810,9 @@ TLArgs tl_args(mf_ctx* c) {
 	a.sW = c->sW64.p;
 	a.R = c->R64.p;
 	a.av = c->av64.p;
+	a.cm_sw = c->cm_sw.p; a.cm_swA = c->cm_swA.p; a.cm_sX = c->cm_sX.p; a.cm_sW = c->cm_sW.p; a.cm_swji = c->cm_swji.p;
+	a.cm_U = c->cm_U.p; a.cm_X = c->cm_X.p; a.cm_V = c->cm_V.p; a.cm_P = c->cm_P.p; a.cm_R = c->cm_R.p;
+	a.cm_H = c->cm_H.p;
 	a.recA = c->recA.p;
 	a.recB = c->recB.p;
 	a.dA32 = c->dA32.p;
@@ -842,9 +849,9 @@ mf_status tl_step_all(mf_ctx* c) {
 	StateSoA S0 = a.st, S1 = a.nxt;
 	// mixed form: pass B writes the next stage's records (no pack kernel), except with
 	// boundary conditions, which change the stage state after pass B
-	const bool fused = c->mixed && c->n_bc == 0;
-	void* rb[2] = {c->recB.p, c->recB2.p};
 	const bool corot = c->cfg.method == MF_METHOD_COROT, potential = c->cfg.method == MF_METHOD_POTENTIAL;
+	const bool fused = c->mixed && c->n_bc == 0 && !corot && !potential;
+	void* rb[2] = {c->recB.p, c->recB2.p};
 	for (uint32_t st = 0; st < 4; st++) {
 		a.stage = st;
 		a.st = (st % 2 == 0) ? S0 : S1;
@@ -852,7 +859,7 @@ mf_status tl_step_all(mf_ctx* c) {
 		a.recB = fused ? rb[st & 1] : rb[0];
 		a.recB_out = rb[(st + 1) & 1];
 		a.write_recs = fused ? 1u : 0u;
-		const bool pack = c->mixed && (!fused || (st == 0 && !c->tl_recs_valid));
+		const bool pack = c->mixed && !corot && !potential && (!fused || (st == 0 && !c->tl_recs_valid));
 		cudaError_t e;
 		if ((e = tl_launch(c, a, 0)) != cudaSuccess) return cuda_fail(c, e, "tl bc");
 		if (pack && (e = tl_launch(c, a, 1)) != cudaSuccess) return cuda_fail(c, e, "tl pack");
@@ -861,14 +868,16 @@ mf_status tl_step_all(mf_ctx* c) {
 			auto cr = [&](int part) {
 				return c->strict ? mf_strict::cr_stage(a, part, c->stream) : mf_fast::cr_stage(a, part, c->stream);
 			};
-			if (corot && (e = cr(0)) != cudaSuccess) return cuda_fail(c, e, "corotational rotation");
+			const int base = c->mixed ? 10 : 0;  // the mixed form's records, then its passes
+			if (c->mixed && (e = cr(10)) != cudaSuccess) return cuda_fail(c, e, "records");
+			if (corot && (e = cr(base + (c->mixed ? 1 : 0))) != cudaSuccess) return cuda_fail(c, e, "corotational rotation");
 			timing_begin(c, 1, slot);
-			if ((e = cr(1)) != cudaSuccess) return cuda_fail(c, e, "pass A");
+			if ((e = cr(base + (c->mixed ? 2 : 1))) != cudaSuccess) return cuda_fail(c, e, "pass A");
 			timing_end(c, slot, c->n_total);
 			timing_begin(c, 2, slot);
-			if ((e = cr(2)) != cudaSuccess) return cuda_fail(c, e, "pass B");
+			if ((e = cr(base + (c->mixed ? 3 : 2))) != cudaSuccess) return cuda_fail(c, e, "pass B");
 			timing_end(c, slot, c->n_total);
-			c->launches += (corot ? 3 : 2) + (c->n_bc ? 1 : 0);
+			c->launches += (corot ? 3 : 2) + (c->mixed ? 1 : 0) + (c->n_bc ? 1 : 0);
 			continue;
 		}
 		timing_begin(c, 1, slot);
@@ -909,8 +918,6 @@ mf_status validate_corot(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& 
 	                            MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN, MF_CONTMECH_CAUCHY_TO_NOMINAL,
 	                            MF_DERIVE_STRESS_COROTATIONAL, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
 	                            MF_CONTMECH_ADVECTION};
-	if (c->cfg.precision == MF_PREC_MIXED)
-		return fail(c, MF_ERR_PIPELINE, "the corotational method runs in the FP64 forms");
 	flags = 0;
 	size_t pos = 0;
 	for (int32_t a : acts) {
@@ -933,8 +940,6 @@ mf_status validate_potential(mf_ctx* c, const std::vector<int32_t>& acts, uint32
 	static const int order[] = {MF_DERIVE_DISPLACEMENT, MF_MATERIAL_COMPUTE_STRESS_GREEN_STVENANT,
 	                            MF_POTENTIAL_COMP_ELASTIC_POTENTIAL, MF_CORRECTORS_MGHN_ARTIFICIAL_VISCOSITY,
 	                            MF_CONTMECH_ADVECTION};
-	if (c->cfg.precision == MF_PREC_MIXED)
-		return fail(c, MF_ERR_PIPELINE, "the elastic-potential method runs in the FP64 forms");
 	flags = 0;
 	size_t pos = 0;
 	for (int32_t a : acts) {
@@ -1086,7 +1091,9 @@ mf_status tl_setup(mf_ctx* c) {
 	CK(cudaMemcpy(c->sl_off.p, sl.data(), (ns + 1) * 4, cudaMemcpyHostToDevice));
 	CK(c->scnt.alloc(n));
 	CK(c->snbr.alloc(ent));
-	if (c->mixed) {
+	const bool fam = corot || potential;       // their mixed lists come from the FP64 ones
+	const bool tl_mixed_lists = c->mixed && !fam;
+	if (tl_mixed_lists) {
 		CK(c->sw32.alloc(ent));
 		CK(c->swA32.alloc(ent));
 	} else {
@@ -1095,9 +1102,9 @@ mf_status tl_setup(mf_ctx* c) {
 	e = c->strict ? mf_strict::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
 	                                      c->snbr.p, c->sw64.p, nullptr, nullptr, c->qw0.p, c->m.p, c->stream)
 	              : mf_fast::tl_to_sell(n, c->nbr_off.p, c->nbr.p, c->wx64.p, c->wy64.p, c->sl_off.p, c->scnt.p,
-	                                    c->snbr.p, c->mixed ? nullptr : (void*)c->sw64.p,
-	                                    c->mixed ? (void*)c->sw32.p : nullptr, c->mixed ? (void*)c->swA32.p : nullptr,
-	                                    c->qw0.p, c->m.p, c->stream);
+	                                    c->snbr.p, tl_mixed_lists ? nullptr : (void*)c->sw64.p,
+	                                    tl_mixed_lists ? (void*)c->sw32.p : nullptr,
+	                                    tl_mixed_lists ? (void*)c->swA32.p : nullptr, c->qw0.p, c->m.p, c->stream);
 	if (e != cudaSuccess) return cuda_fail(c, e, "tl_to_sell");
 	if (corot) {
 		CK(c->sW64.alloc(ent));
@@ -1116,10 +1123,21 @@ mf_status tl_setup(mf_ctx* c) {
 		                                     c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "reverse-pair weights");
 	}
+	if (fam && c->mixed) {  // FP32 per-pair arrays and per-row records of the mixed passes
+		CK(c->cm_sw.alloc(ent)); CK(c->cm_swA.alloc(ent));
+		if (corot) { CK(c->cm_sX.alloc(ent)); CK(c->cm_sW.alloc(ent)); CK(c->cm_R.alloc(n)); }
+		else CK(c->cm_swji.alloc(ent));
+		CK(c->cm_U.alloc(n)); CK(c->cm_X.alloc(n)); CK(c->cm_V.alloc(n)); CK(c->cm_P.alloc(n)); CK(c->cm_H.alloc(n));
+		e = mf_fast::cr_mixed_lists(n, c->sl_off.p, c->scnt.p, c->snbr.p, c->sw64.p, c->sW64.p, potential ? 1 : 0,
+		                            c->X.p, c->Y.p, c->m.p, c->qw0.p, c->cm_sw.p, c->cm_swA.p, c->cm_sX.p, c->cm_sW.p,
+		                            c->cm_swji.p, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "mixed lists");
+	}
 	CK(cudaStreamSynchronize(c->stream));
+	if (fam && c->mixed) { c->sw64.free(); c->sW64.free(); }
 	c->wx64.free();
 	c->wy64.free();
-	if (c->mixed && c->tune.tl_tiled && (st = build_tl_tiles(c, off)) != MF_OK) return st;
+	if (c->mixed && !fam && c->tune.tl_tiled && (st = build_tl_tiles(c, off)) != MF_OK) return st;
 	if (c->mixed) {
 		CK(c->recA.alloc(n)); CK(c->recB.alloc(4 * (size_t)n)); CK(c->recB2.alloc(4 * (size_t)n)); CK(c->dA32.alloc(n));
 		c->tl_recs_valid = false;

@@ -371,11 +371,27 @@ cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, c
 	return cudaGetLastError();
 }
 
-// part 0: rotation (corotational only), 1: pass A, 2: pass B
+namespace {
+__global__ void k_cm_pack(TLArgs a);
+__global__ void k_cm_R(TLArgs a);
+__global__ void k_cm_A(TLArgs a);
+template <bool POT>
+__global__ void k_cm_B(TLArgs a);
+}  // namespace
+
+// part 0: rotation (corotational only), 1: pass A, 2: pass B; mixed form: 10 records,
+// 11 rotation, 12 pass A, 13 pass B
 cudaError_t cr_stage(const TLArgs& a, int part, cudaStream_t s) {
 	unsigned bs = a.block ? a.block : 128;
 	const bool pot = (a.flags & mfk_host::FLAG_POTENTIAL) != 0;
 	switch (part) {
+	case 10: k_cm_pack<<<grid1(a.n_total, 256), 256, 0, s>>>(a); break;
+	case 11: k_cm_R<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	case 12: k_cm_A<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
+	case 13:
+		if (pot) k_cm_B<true><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else k_cm_B<false><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		break;
 	case 0: k_crR<<<grid1(a.n_total, bs), bs, 0, s>>>(a); break;
 	case 1:
 		if (pot) k_ptA<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
@@ -386,6 +402,283 @@ cudaError_t cr_stage(const TLArgs& a, int part, cudaStream_t s) {
 		else k_crB<false><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
 	}
+	return cudaGetLastError();
+}
+
+}  // namespace MF_NS
+
+// ---------------------------------------------------------------------------------
+// Mixed form of the corotational and elastic-potential methods: the pair arithmetic in
+// FP32, position differences from float-float records, the per-row stress (2x2
+// inversion, Cauchy-Green / Green-St Venant) and the RK4 state of x, y, vx, vy in FP64.
+// The rotated displacement difference is formed as (R^T - I) X_ji + R^T u_ji, with
+// cos - 1 kept as -2 sin^2(theta/2), so that no term cancels in FP32.
+namespace MF_NS {
+namespace {
+
+__device__ __forceinline__ float ffdiff(float ahi, float alo, float bhi, float blo) {
+	return (ahi - bhi) + (alo - blo);
+}
+
+// FP64 lists of the set-up -> the mixed form's FP32 per-pair arrays
+__global__ void k_cm_lists(uint32_t n, const uint32_t* __restrict__ sl_off, const uint16_t* __restrict__ cnt,
+                           const uint32_t* __restrict__ snbr, const double2* __restrict__ sw64,
+                           const double* __restrict__ sW64, int potential, const double* __restrict__ X,
+                           const double* __restrict__ Y, const double* __restrict__ m, const double* __restrict__ qw,
+                           float2* sw, float2* swA, float2* sX, float* sW, float2* swji) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t q = sl_off[i >> 5] + (i & 31u);
+	for (uint32_t k = 0; k < cnt[i]; k++, q += 32) {
+		uint32_t j = snbr[q];
+		double2 w = sw64[q];
+		double s = potential ? 1. : m[j];
+		sw[q] = make_float2((float)(w.x * s), (float)(w.y * s));
+		swA[q] = make_float2((float)(w.x * qw[j]), (float)(w.y * qw[j]));
+		if (potential) {
+			double2 wr = reinterpret_cast<const double2*>(sW64)[q];
+			swji[q] = make_float2((float)wr.x, (float)wr.y);
+		} else {
+			sX[q] = make_float2((float)(X[j] - X[i]), (float)(Y[j] - Y[i]));
+			sW[q] = (float)(m[j] * sW64[q]);
+		}
+	}
+}
+
+// the stage's per-row records from the state (x, y, vx, vy in FP64, rho - rho0 in FP32)
+__global__ void k_cm_pack(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	double x = s.x[i], y = s.y[i];
+	FF ux = ff_split(x - a.X[i]), uy = ff_split(y - a.Y[i]);
+	FF fx = ff_split(x), fy = ff_split(y), fvx = ff_split(s.vx[i]), fvy = ff_split(s.vy[i]);
+	((float4*)a.cm_U)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+	((float4*)a.cm_X)[i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
+	((float4*)a.cm_V)[i] = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
+	float rho = s.rho_f[i] + (float)pr.rho0;  // the mixed state holds rho - rho0
+	((float4*)a.cm_H)[i] = make_float4(((const float*)a.h32)[i], rho, sqrtf((float)pr.K / rho), ((const float*)a.m32)[i]);
+}
+
+// rotation from the anisotropy tensor, x_ji = X_ji + u_ji
+__global__ void __launch_bounds__(256) k_cm_R(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const float4* U = (const float4*)a.cm_U;
+	const float2* sX = (const float2*)a.cm_sX;
+	const float* sW = (const float*)a.cm_sW;
+	const float4 ui = U[i];
+	float Axx = 0.f, Axy = 0.f, Ayx = 0.f, Ayy = 0.f;
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+#pragma unroll 2
+	for (uint32_t k = 0; k < c; k++, q += 32) {
+		uint32_t j = a.snbr[q];
+		float2 X2 = sX[q];
+		float mW = sW[q];
+		float4 uj = __ldg(U + j);
+		float xji = X2.x + ffdiff(uj.x, uj.y, ui.x, ui.y);
+		float yji = X2.y + ffdiff(uj.z, uj.w, ui.z, ui.w);
+		Axx += xji * X2.x * mW;
+		Axy += xji * X2.y * mW;
+		Ayx += yji * X2.x * mW;
+		Ayy += yji * X2.y * mW;
+	}
+	float th = atan2f(Ayx - Axy, Axx + Ayy);
+	float sn, cs;
+	sincosf(th, &sn, &cs);
+	float h = sinf(0.5f * th);
+	((float4*)a.cm_R)[i] = make_float4(cs, sn, -2.f * h * h, ((const float*)a.m32)[i]);
+}
+
+// pass A: displacement gradient (rotated, corotational; plain, potential), then per row
+// in FP64 the stress, nominal stress (corotational) or F_e (potential)
+__global__ void __launch_bounds__(256) k_cm_A(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const bool pot = (a.flags & mfk_host::FLAG_POTENTIAL) != 0;
+	const float4* U = (const float4*)a.cm_U;
+	const float2* swA = (const float2*)a.cm_swA;
+	const float2* sX = (const float2*)a.cm_sX;
+	const float4 ui = U[i];
+	float cs = 1.f, sn = 0.f, c1 = 0.f;
+	if (!pot) {
+		float4 Ri = ((const float4*)a.cm_R)[i];
+		cs = Ri.x; sn = Ri.y; c1 = Ri.z;
+	}
+	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
+	uint32_t q = sell_base(a, i), c = a.cnt[i];
+	if (pot ? (a.flags & A_DISP) : (a.flags & A_CR_DISP)) {
+#pragma unroll 2
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			float2 w = swA[q];  // gradient times the neighbour's quad weight
+			float4 uj = __ldg(U + j);
+			float dux = ffdiff(uj.x, uj.y, ui.x, ui.y), duy = ffdiff(uj.z, uj.w, ui.z, ui.w);
+			float ux = dux, uy = duy;
+			if (!pot) {  // (R^T - I) X_ji + R^T u_ji, R^T = (cos, sin; -sin, cos)
+				float2 X2 = sX[q];
+				ux = (c1 * X2.x + sn * X2.y) + (cs * dux + sn * duy);
+				uy = (-sn * X2.x + c1 * X2.y) + (-sn * dux + cs * duy);
+			}
+			Hxx += ux * w.x;
+			Hxy += ux * w.y;
+			Hyx += uy * w.x;
+			Hyy += uy * w.y;
+		}
+	}
+	const BodyParams& pr = a.params[a.body_of[i]];
+	const mfk_host::StateSoA& s = a.st;
+	double H00 = Hxx, H01 = Hxy, H10 = Hyx, H11 = Hyy;
+	double P0 = 0., P1 = 0., P2 = 0., P3 = 0.;
+	if (pot) {
+		double Sxx = s.Sxx_f[i], Sxy = s.Sxy_f[i], Syy = s.Syy_f[i];
+		if (a.flags & A_GREEN) green_stvenant<double>(H00, H01, H10, H11, pr.D, pr.nu, Sxx, Sxy, Syy);
+		double sc = -2 * a.qw0[i];
+		double J00 = sc * (H00 + 1.), J01 = sc * H10, J10 = sc * H01, J11 = sc * (H11 + 1.);
+		P0 = J00 * Sxx + J10 * Sxy; P1 = J01 * Sxx + J11 * Sxy;
+		P2 = J00 * Sxy + J10 * Syy; P3 = J01 * Sxy + J11 * Syy;
+	} else {
+		double Sxx = 0., Sxy = 0., Syy = 0.;
+		if (a.flags & A_CR_CAUCHY_GREEN) {
+			double E00 = H00, E01 = 0.5 * (H10 + H01), E11 = H11;  // (F + F^T)/2 - I
+			Sxx = pr.D * (E00 + pr.nu * E11);
+			Syy = pr.D * (E00 * pr.nu + E11);
+			Sxy = pr.D * (1 - pr.nu) * E01;
+		}
+		if (a.flags & A_C2N) cauchy_to_nominal<double>(H00, H01, H10, H11, Sxx, Sxy, Syy, P0, P1, P2, P3);
+	}
+	((float4*)a.cm_P)[i] = make_float4((float)P0, (float)P1, (float)P2, (float)P3);
+}
+
+// pass B: pair forces, contact, viscosity, advection, RK4 (x, y, vx, vy; rho and the
+// stresses have no rate in these pipelines)
+template <bool POT>
+__global__ void __launch_bounds__(256) k_cm_B(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const float2* sw = (const float2*)a.cm_sw;
+	const float4* P = (const float4*)a.cm_P;
+	const float4* R = (const float4*)a.cm_R;
+	const float4* Xr = (const float4*)a.cm_X;
+	const float4* Vr = (const float4*)a.cm_V;
+	const float4* Hr = (const float4*)a.cm_H;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	const float4 Pi = P[i];
+	float fx = 0.f, fy = 0.f;
+	const uint32_t q0 = sell_base(a, i), c = a.cnt[i];
+	bool forces = false;
+	if (POT && (flags & mfk_host::FLAG_POTENTIAL)) {
+		forces = true;
+		const float2* swji = (const float2*)a.cm_swji;
+		uint32_t q = q0;
+#pragma unroll 2
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			float2 w = sw[q], wr = swji[q];
+			float4 Fj = __ldg(P + j);
+			fx += (Fj.x * wr.x + Fj.z * wr.y) - (Pi.x * w.x + Pi.z * w.y);
+			fy += (Fj.y * wr.x + Fj.w * wr.y) - (Pi.y * w.x + Pi.w * w.y);
+		}
+		const float half_mi = 0.5f / ((const float*)a.m32)[i];
+		fx *= half_mi;
+		fy *= half_mi;
+	}
+	if (!POT && (flags & A_CR_STRESS)) {
+		forces = true;
+		const float r21 = (float)(1. / (pr.rho0 * pr.rho0));
+		const float4 Ri = R[i];
+		uint32_t q = q0;
+#pragma unroll 2
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			float2 w = sw[q];  // m_j grad W
+			float4 Pj = __ldg(P + j), Rj = __ldg(R + j);
+			float ax = ((Pi.x + Pj.x) * w.x + (Pi.y + Pj.y) * w.y) * r21;
+			float ay = ((Pi.z + Pj.z) * w.x + (Pi.w + Pj.w) * w.y) * r21;
+			// R_i a_ij - R_j a_ji with a_ji = -a_ij, R = (cos, -sin; sin, cos)
+			fx += 0.5f * ((ax * Ri.x - ay * Ri.y) + (ax * Rj.x - ay * Rj.y));
+			fy += 0.5f * ((ax * Ri.y + ay * Ri.x) + (ax * Rj.y + ay * Rj.x));
+		}
+	}
+	const float4 xi = Xr[i], vi = Vr[i], hi = Hr[i];
+	float avx = 0.f, avy = 0.f;
+	if (flags & A_ART_VISC) {
+		const float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+		uint32_t q = q0;
+		for (uint32_t k = 0; k < c; k++, q += 32) {
+			uint32_t j = a.snbr[q];
+			float4 xj = __ldg(Xr + j), vj = __ldg(Vr + j);
+			float xij = ffdiff(xi.x, xi.y, xj.x, xj.y), yij = ffdiff(xi.z, xi.w, xj.z, xj.w);
+			float vijx = ffdiff(vi.x, vi.y, vj.x, vj.y), vijy = ffdiff(vi.z, vi.w, vj.z, vj.w);
+			float vijposij = vijx * xij + vijy * yij;
+			if (vijposij < 0.f) {
+				float4 hj = __ldg(Hr + j);  // {h, rho, c, m}
+				float2 w = sw[q];
+				float mj_w_x = POT ? hj.w * w.x : w.x, mj_w_y = POT ? hj.w * w.y : w.y;  // m_j grad W
+				float cij = 0.5f * (hi.z + hj.z), hij = 0.5f * (hi.x + hj.x), rhoij = 0.5f * (hi.y + hj.y);
+				float r2ij = xij * xij + yij * yij;
+				float muij = __fdividef(hij * vijposij, r2ij + eta2 * hij * hij);
+				float piij = __fdividef(-alpha * cij * muij + beta * muij * muij, rhoij);
+				avx += -piij * mj_w_x;
+				avy += -piij * mj_w_y;
+			}
+		}
+	}
+	const mfk_host::StateSoA& s = a.st;
+	double d[4];
+	d[0] = (flags & A_ADVECTION) ? s.vx[i] : 0.;
+	d[1] = (flags & A_ADVECTION) ? s.vy[i] : 0.;
+	d[2] = (double)avx;
+	d[3] = (double)avy;
+	if (forces) {
+		d[2] += (double)fx + a.fcx[i] / a.m[i];
+		d[3] += (double)fy + a.fcy[i] / a.m[i];
+	}
+	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
+	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
+	double* np[4] = {a.nxt.x, a.nxt.y, a.nxt.vx, a.nxt.vy};
+	const uint32_t stg = a.stage;
+	const double dt = pr.dt;
+	if (stg < 3) {
+		double dts = (stg == 2 ? 1.0 : 0.5) * dt;
+#pragma unroll
+		for (int q2 = 0; q2 < 4; q2++) {
+			ap[q2][i] = (stg == 0) ? d[q2] : ap[q2][i] + 2 * d[q2];
+			np[q2][i] = bp[q2][i] + d[q2] * dts;
+		}
+		// rho and the stresses carry over unchanged into the next stage's set
+		a.nxt.rho_f[i] = a.base.rho_f[i];
+		a.nxt.Sxx_f[i] = a.base.Sxx_f[i];
+		a.nxt.Sxy_f[i] = a.base.Sxy_f[i];
+		a.nxt.Syy_f[i] = a.base.Syy_f[i];
+	} else {
+		double w6 = dt * 1. / 6.;
+		bool ok = true;
+#pragma unroll
+		for (int q2 = 0; q2 < 4; q2++) {
+			double v = bp[q2][i] + w6 * (ap[q2][i] + d[q2]);
+			bp[q2][i] = v;
+			np[q2][i] = v;
+			ok = ok && isfinite(v);
+		}
+		a.nxt.rho_f[i] = a.base.rho_f[i];
+		a.nxt.Sxx_f[i] = a.base.Sxx_f[i];
+		a.nxt.Sxy_f[i] = a.base.Sxy_f[i];
+		a.nxt.Syy_f[i] = a.base.Syy_f[i];
+		if (!ok) raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
+	}
+}
+
+}  // namespace
+
+cudaError_t cr_mixed_lists(uint32_t n, const uint32_t* sl_off, const uint16_t* cnt, const uint32_t* snbr,
+                           const void* sw64, const double* sW64, int potential, const double* X, const double* Y,
+                           const double* m, const double* qw, void* sw, void* swA, void* sX, void* sW, void* swji,
+                           cudaStream_t s) {
+	k_cm_lists<<<(n + 127) / 128, 128, 0, s>>>(n, sl_off, cnt, snbr, (const double2*)sw64, sW64, potential, X, Y, m, qw,
+	                                           (float2*)sw, (float2*)swA, (float2*)sX, (float*)sW, (float2*)swji);
 	return cudaGetLastError();
 }
 

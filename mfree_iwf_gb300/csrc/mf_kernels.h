@@ -132,6 +132,13 @@ struct TLArgs {
 	void* R;                             // corotational: per row double4 {cos, sin, m, 0} of the rotation
 	void* av;                            // corotational / potential: per row two double4 records
 	                                     // {x, y, vx, vy} and {h, rho, c, m} for the viscosity loop
+	// corotational / potential, mixed form: per pair (sliced ELL) float2 gradients times
+	// m_j (corotational) or plain (potential), times qw_j (pass A), X_j - X_i and m_j W_ij
+	// (corotational), the reverse gradient (potential); per row float4 records:
+	// displacement, position and velocity as float-float pairs, stress, rotation
+	// {cos, sin, cos - 1, m}, {h, rho, c, m}
+	const void *cm_sw, *cm_swA, *cm_sX, *cm_sW, *cm_swji;
+	void *cm_U, *cm_X, *cm_V, *cm_P, *cm_R, *cm_H;
 	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
 	void* recB_out;                      // mixed: pass B writes the next stage's records here...
 	uint32_t write_recs;                 // ...and into recA when set (no separate pack then)
@@ -253,6 +260,10 @@ struct ContactArgs {
 	cudaError_t cr_sell_w(uint32_t n, const uint32_t* off, const uint32_t* sl_off, const double* w, double* sW, \
 	                      cudaStream_t s);                                                                   \
 	cudaError_t cr_stage(const mfk_host::TLArgs& a, int part, cudaStream_t s);                               \
+	cudaError_t cr_mixed_lists(uint32_t n, const uint32_t* sl_off, const uint16_t* cnt, const uint32_t* snbr,   \
+	                           const void* sw64, const double* sW64, int potential, const double* X,        \
+	                           const double* Y, const double* m, const double* qw, void* sw, void* swA,      \
+	                           void* sX, void* sW, void* swji, cudaStream_t s);                              \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
 	cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,  \
 	                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px,     \

@@ -153,16 +153,34 @@ def test_corot_checkpoint_roundtrip(lib, tmp_path):
     (lambda: S.tensile_corot(11), "DERIVE_STRESS_COROTATIONAL"),
     (lambda: S.tensile_potential(11), "POTENTIAL_COMP_ELASTIC_POTENTIAL"),
 ])
-def test_families_reject_mixed_and_incomplete_pipelines(lib, build, drop):
+def test_families_reject_incomplete_pipelines(lib, build, drop):
     import mfree_iwf_gb300 as M
     sc = build()
-    with pytest.raises(M.MfError) as e:
-        run(sc, 1, precision="mixed")
-    assert "MF_ERR_PIPELINE" in str(e.value)
     sc.actions = [a for a in sc.actions if a != getattr(M, drop)]
     with pytest.raises(M.MfError) as e:
         run(sc, 1)
     assert "MF_ERR_PIPELINE" in str(e.value)
+
+
+@pytest.mark.parametrize("build,steps,tol", [
+    (lambda: S.rings_corot_contact(40), 600, 1e-5),
+    (lambda: S.tensile_corot(21), 200, 1e-5),
+    (lambda: S.rotation_corot(41), 200, 1e-5),
+    (lambda: S.rings_potential_contact(40), 600, 1e-5),
+    (lambda: S.tensile_potential(21), 100, 1e-5),
+])
+def test_families_mixed_close_to_fp64(lib, build, steps, tol):
+    """The mixed form (FP32 pair arithmetic, float-float position differences, FP64
+    per-row stress and RK4 state) against the FP64 form: relative L2 of positions and
+    velocities below `tol`."""
+    sc = build()
+    ref = run(sc, steps, "fp64")
+    got = run(sc, steps, "mixed")
+    for g, r in zip(got, ref):
+        for name in ("position", "velocity"):
+            e = rel(g, r, GROUPS[name])
+            print(sc.name, name, f"{e:.3e}")
+            assert e < tol, (sc.name, name, e)
 
 
 def test_godunov_pipeline_checks(lib):
