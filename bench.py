@@ -222,9 +222,17 @@ MEASURED_TRAFFIC = {
 }
 
 
-def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool) -> float:
+def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool, family: str = "") -> float:
     """Unique bytes per row of one launch: each row's own data once, the lists once, and
     neighbour records assumed served on chip (their unique bytes are the rows' own)."""
+    if family in ("corot", "potential") and mixed:
+        if kind == 1:  # pass A: index + qw-weighted gradient (+ X_j - X_i, corotational) per pair
+            per_pair = 20 if family == "corot" else 12
+            return 2 + per_pair * nnz_per_row + 16 + 16 + 12 + 8 + 4 + 16  # u, rotation, S, qw, body; writes P
+        if kind == 2:  # pass B: index + gradient per pair (+ reverse gradient, potential)
+            per_pair = 12 if family == "corot" else 20
+            return (2 + per_pair * nnz_per_row + 80 + 24  # own records P R X V H, fc and m
+                    + 112 + 32)                           # RK4 FP64 x y vx vy, rho/S carried to the next set
     if tl and mixed:
         if kind == 1:  # pass A
             return (2 + 12 * nnz_per_row  # count; per pair: index 4 + premultiplied gradient 8
@@ -358,7 +366,7 @@ def ours(args, cfg_desc):
     roof = None
     if klaunch and sc.method != M.METHOD_UL_WEAK:  # (no byte model for the weak UL passes)
         per_launch_rows = krows / klaunch
-        abytes = algorithmic_bytes(dom, mixed, nnz, tl) * per_launch_rows
+        abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload) * per_launch_rows
         achieved = abytes / (kms / klaunch / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,
