@@ -16,8 +16,7 @@ Metric: particle-steps/s = particles x RK4 steps / time, the whole step included
                   [--precision mixed|fp64|fp64_strict]
 
 The family workloads (corot, godunov, potential, ulweak) are ensembles of the
-reference's own two-ring set-up of that SPH family (godunov and ulweak: FP64 forms
-only).
+reference's own two-ring set-up of that SPH family (ulweak: FP64 forms only).
 
 With --impl reference it times the CPU implementation of the same path (the oracle
 restatement of the reference, which is single-threaded) on all host cores.
@@ -269,8 +268,8 @@ def ours(args, cfg_desc):
 
     sc, cfg = workload(args.workload, args.dx, args.instances)
     n = sc.n_total
-    if args.workload in ("godunov", "ulweak") and args.precision == "mixed":
-        args.precision = "fp64"  # these families run in the FP64 forms only
+    if args.workload == "ulweak" and args.precision == "mixed":
+        args.precision = "fp64"  # the weak UL form runs in the FP64 forms only
     tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK, M.METHOD_COROT, M.METHOD_POTENTIAL)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"

@@ -375,8 +375,6 @@ mf_status validate_ul(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& fla
 		return fail(c, MF_ERR_PIPELINE, "Jaumann rate / continuity need derive_velocity before them");
 	const uint32_t god = FLAG_GODUNOV_CONTINUITY | FLAG_GODUNOV_MOMENTUM;
 	if (flags & god) {
-		if (c->cfg.precision == MF_PREC_MIXED)
-			return fail(c, MF_ERR_PIPELINE, "the Godunov actions run in the FP64 forms");
 		if ((flags & FLAG_GODUNOV_CONTINUITY) && (flags & abit(MF_CONTMECH_CONTINUITY)))
 			return fail(c, MF_ERR_PIPELINE, "godunov_continuity and contmech_continuity both set the density rate");
 		if ((flags & FLAG_GODUNOV_MOMENTUM) && (flags & abit(MF_CONTMECH_MOMENTUM_UL)))

@@ -376,13 +376,18 @@ __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	float rho, Sxx, Sxy, Syy;
 	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
 	uint32_t b = a.body_of[i];
-	rho += (float)P[b].rho0;  // the mixed state holds rho - rho0
+	const float rho_dev = rho;  // the mixed state holds rho - rho0
+	rho += (float)P[b].rho0;
 	Rec32 r;
 	r.x = ff_split(x); r.y = ff_split(y); r.vx = ff_split(vx); r.vy = ff_split(vy);
 	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
 	per_particle<float>(a.flags, P[b], r.m, rho, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c,
 	                    r.qw, r.rho21);
 	r.sxy = Sxy;
+	if (a.flags & (A_GOD_CONT | A_GOD_MOM)) {  // p from the stored deviation, the stress Syy itself
+		r.Rxx = (a.flags & A_EOS) ? (float)P[b].c0sq * rho_dev : 0.f;
+		r.Rxy = Syy;
+	}
 	Rec32* out = reinterpret_cast<Rec32*>(a.rec) + k;
 	const float4* s = reinterpret_cast<const float4*>(&r);
 	float4* d = reinterpret_cast<float4*>(out);
@@ -622,6 +627,7 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 }
 
 // ---------------------------------------------------------- pair kernel mixed
+template <bool GOD>
 __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __restrict__ P,
                                            const Geom* __restrict__ G, DevStatus* st, uint32_t k) {
 	const Rec32* rec = reinterpret_cast<const Rec32*>(a.rec);
@@ -648,6 +654,8 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	float Sxx_x = 0.f, Sxy_y = 0.f, Sxy_x = 0.f, Syy_y = 0.f;
 	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
 	float av_x = 0.f, av_y = 0.f, xs_x = 0.f, xs_y = 0.f;
+	float god_rho = 0.f, god_vx = 0.f, god_vy = 0.f;
+	const float two_rhoi = 2.f / ri.rho;
 	for (int ni = lo_i; ni < hi_i; ni++) {
 		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
 		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
@@ -707,6 +715,36 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 				xs_x -= f * dvx;
 				xs_y -= f * dvy;
 			}
+			if (GOD && kj != k) {
+				// godunov_continuity / godunov_momentum (godunov.h:86-187) in FP32: velocity
+				// differences from the float-float records, the Riemann state in the form
+				// v_i - u* = (Z_j (v_i - v_j).n + p_i - p_j) / (Z_i + Z_j), Z = rho c;
+				// Rxx holds p, Rxy the stress Syy itself
+				const float mag_r = sqrtf(r2), inv = 1.f / mag_r;
+				const float Zi = ri.rho * ri.c, Zj = rj.rho * rj.c;
+				const float frac = 1.f / (Zi + Zj);
+				if (flags & A_GOD_CONT) {
+					float nx = xij * inv, ny = yij * inv;
+					float dvn = -(dvx * nx + dvy * ny);  // (v_i - v_j).n
+					float vi_us = frac * (Zj * dvn + (ri.Rxx - rj.Rxx));
+					god_rho += 2.f * ri.rho * vi_us * (w.w_x * nx + w.w_y * ny) * rj.qw;
+				}
+				if (flags & A_GOD_MOM) {
+					float rx = -xij, ry = -yij;
+					float Rx = rx * inv, Ry = ry * inv, Sx = ry * inv, Sy = -rx * inv;  // the float frame
+					float siR0 = ri.sxx * Rx + ri.sxy * Ry;
+					float sjR0 = rj.sxx * Rx + rj.sxy * Ry, sjR1 = rj.sxy * Rx + rj.Rxy * Ry;
+					float si0 = Rx * siR0 + Sx * (ri.sxy * Rx + ri.Rxy * Ry);
+					float sj0 = Rx * sjR0 + Sx * sjR1, sj1 = Ry * sjR0 + Sy * sjR1;
+					float dv0 = Rx * dvx + Sx * dvy, dv1 = Ry * dvx + Sy * dvy;  // frame (v_j - v_i)
+					// the second component takes sigma_j twice (godunov.h:116), as the reference does
+					float S0 = frac * (sj0 * Zi + si0 * Zj + Zi * Zj * dv0);
+					float S1 = frac * (sj1 * Zi + sj1 * Zj + Zi * Zj * dv1);
+					float SR0 = Rx * S0 + Ry * S1, SR1 = Sx * S0 + Sy * S1;
+					if (fabsf(rx) > 0.f) god_vx += two_rhoi * __fdividef(w.w_x * mag_r, rx) * SR0 * rj.qw;
+					if (fabsf(ry) > 0.f) god_vy += two_rhoi * __fdividef(w.w_y * mag_r, ry) * SR1 * rj.qw;
+				}
+			}
 		}
 	}
 	float d[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -720,6 +758,11 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 		jaumann<float>(vx_x, vx_y, vy_x, vy_y, sv.Sxx_f[i], sv.Sxy_f[i], sv.Syy_f[i], (float)pr.G, d[5], d[6], d[7]);
 	}
 	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
+	if (GOD && (flags & A_GOD_CONT)) d[4] = god_rho;
+	if (GOD && (flags & A_GOD_MOM)) {
+		d[2] += god_vx + (float)(a.fcx[i] / (double)ri.m);
+		d[3] += god_vy + (float)(a.fcy[i] / (double)ri.m);
+	}
 	if (flags & A_MOMENTUM_UL) {
 		d[2] += 1.f / rhoi * (Sxx_x + Sxy_y) + (float)(a.fcx[i] / (double)ri.m);
 		d[3] += 1.f / rhoi * (Sxy_x + Syy_y) + (float)(a.fcy[i] / (double)ri.m);
@@ -774,13 +817,13 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 // (one launch per stage over all bodies): a fixed grid whose blocks take chunks of
 // rows -- consecutive cell-ordered rows, so a chunk is a run of cells of one body --
 // from an atomic counter until the rows run out; no block ever waits on another.
-template <bool MIXED>
+template <bool MIXED, bool GOD = false>
 __global__ void __launch_bounds__(256, MIXED ? 3 : 1) k_pair(ULArgs a, const BodyParams* __restrict__ P, const Geom* __restrict__ G,
                                               DevStatus* st) {
 	if (!a.persistent) {
 		uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 		if (k >= a.n_total) return;
-		if (MIXED) pair32_row(a, P, G, st, k);
+		if (MIXED) pair32_row<GOD>(a, P, G, st, k);
 		else pair64_row(a, P, G, st, k);
 		return;
 	}
@@ -795,7 +838,7 @@ __global__ void __launch_bounds__(256, MIXED ? 3 : 1) k_pair(ULArgs a, const Bod
 		for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) {
 			uint64_t k = base + r;
 			if (k < a.n_total) {
-				if (MIXED) pair32_row(a, P, G, st, (uint32_t)k);
+				if (MIXED) pair32_row<GOD>(a, P, G, st, (uint32_t)k);
 				else pair64_row(a, P, G, st, (uint32_t)k);
 			}
 		}
@@ -886,7 +929,9 @@ cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
 		if (e != cudaSuccess) return e;
 	}
 	if (a.ev_pair0) cudaEventRecord(a.ev_pair0, s);
-	if (mixed) {
+	if (mixed && (a.flags & (A_GOD_CONT | A_GOD_MOM))) {
+		k_pair<true, true><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
+	} else if (mixed) {
 		k_pair<true><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
 	} else {
 		k_pair<false><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
