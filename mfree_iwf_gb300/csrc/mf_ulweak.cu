@@ -92,14 +92,26 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 		rax = vx * inv; ray = vy * inv;
 	}
 	const double a = 1.6651 * sqrt(D0), b = 1.6651 * sqrt(D1);
+#if MF_STRICT_FORM
 	const double phi = atan2(ray, rax);
 	const double cs = cos(phi), sn = sin(phi);
+#else
+	// the fast form takes the unit eigenvector itself as (cos phi, sin phi), which the
+	// reference's cos(atan2(ray, rax)), sin(...) reproduce to an ulp or two, and
+	// multiplies by the reciprocal semi-axes
+	const double cs = rax, sn = ray, ia = 1. / a, ib = 1. / b;
+#endif
 	uint32_t cnt = 0;
 	for (uint32_t q = q0; q < q1; q++) {
 		uint32_t j = nbr[q];
 		double xc = fx[j] - px, yc = fy[j] - py;
+#if MF_STRICT_FORM
 		double left = ((cs * xc + sn * yc) / a);
 		double right = ((sn * xc - cs * yc) / b);
+#else
+		double left = (cs * xc + sn * yc) * ia;
+		double right = (sn * xc - cs * yc) * ib;
+#endif
 		bool in = left * left + right * right <= 1;
 		mask[q] = in ? 1 : 0;
 		cnt += in ? 1u : 0u;
