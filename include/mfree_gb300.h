@@ -59,9 +59,9 @@ typedef enum {
 	MF_METHOD_UL = 1,      /* particle_monaghan: updated-Lagrangian Gray-Monaghan SPH, grid rebuilt per stage */
 	MF_METHOD_TL = 2,      /* particle_tl: total-Lagrangian SPH, fixed neighbours, Randles-Libersky correction */
 	MF_METHOD_TL_WEAK = 3, /* particle_tl_weak: weak-form TL with RKPM shape functions and Gauss points */
-	MF_METHOD_COROT = 4,   /* particle_corotational: TL neighbours, plain SPH weights, per-particle rotation (FP64 forms) */
+	MF_METHOD_COROT = 4,   /* particle_corotational: TL neighbours, plain SPH weights, per-particle rotation */
 	MF_METHOD_POTENTIAL = 5, /* particle_potential: TL neighbours, symmetric Randles-Libersky weights, elastic-potential
-	                           pair forces (FP64 forms) */
+	                           pair forces */
 	MF_METHOD_UL_WEAK = 6   /* particle_ul_weak: weak-form UL with stress points (mf_set_stress_points), per-stage
 	                           neighbour ellipses from Manhattan candidates and RKPM shape functions (FP64 forms) */
 } mf_method;
@@ -106,8 +106,8 @@ typedef enum {
 	MF_DERIVE_DISPLACEMENT_COROTATIONAL = 29,      /* derivatives.h:202-258 */
 	MF_MATERIAL_COMPUTE_STRESS_CAUCHY_GREEN = 30,  /* material.h:102-130 */
 	MF_DERIVE_STRESS_COROTATIONAL = 31,            /* derivatives.h:521-588 */
-	MF_GODUNOV_CONTINUITY = 32,                    /* godunov.h:144-187 (MF_METHOD_UL, FP64 forms) */
-	MF_GODUNOV_MOMENTUM = 33,                      /* godunov.h:86-142 (MF_METHOD_UL, FP64 forms) */
+	MF_GODUNOV_CONTINUITY = 32,                    /* godunov.h:144-187 (MF_METHOD_UL) */
+	MF_GODUNOV_MOMENTUM = 33,                      /* godunov.h:86-142 (MF_METHOD_UL) */
 	MF_POTENTIAL_COMP_ELASTIC_POTENTIAL = 34,      /* potential.h:32-83 (MF_METHOD_POTENTIAL) */
 	MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS_GP = 35, /* riemann_integration.h:21-26 (MF_METHOD_UL_WEAK) */
 	MF_DERIVE_STRESS_WEAK_UL = 36,                 /* derivatives.h:296-329 */
