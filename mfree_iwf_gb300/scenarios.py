@@ -41,6 +41,7 @@ OUT_NAMES = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
 METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL, METHOD_UL_WEAK = 1, 2, 3, 4, 5, 6
 BC_PULL_TL = 1       # tensile.cpp:20-42 (total-Lagrangian bodies)
 BC_VELOCITY_UL = 2   # tensile.cpp:44-66 (updated-Lagrangian bodies)
+SHAPE_RKPM, SHAPE_ELEMENT = 0, 1
 
 
 def cubic_spline(xi: float, yi: float, xj: float, yj: float, h: float):
@@ -83,8 +84,14 @@ class Body:
     # per-body constants overriding the scenario's (ensembles): keys of Scenario
     # (E, nu, rho0, dt, wdeltap, ...)
     params: Dict[str, float] = field(default_factory=dict)
-    # METHOD_UL_WEAK: the stress points, the same 13 arrays as the particles
+    # METHOD_UL_WEAK: the stress points, the same 13 arrays as the particles;
+    # METHOD_TL_WEAK with an explicit element map: the Gauss points as the set-up left them
     gp: Optional[Dict[str, np.ndarray]] = None
+    # METHOD_TL_WEAK with ex = ey = 0: element map (n_elem x 4: ll, lr, tr, tl), Gauss order,
+    # shape functions (SHAPE_RKPM or SHAPE_ELEMENT)
+    quads: Optional[np.ndarray] = None
+    order: int = 2
+    shape: int = 0
 
     @property
     def n(self) -> int:
@@ -789,7 +796,12 @@ def write_case(path: str, sc: Scenario, nsteps: int, dump_every: int = 0) -> Non
             u32(bc.kind); f64(bc.v); u32(len(bc.idx))
             out.extend(np.ascontiguousarray(bc.idx, np.uint32).tobytes())
         u32(b.ex); u32(b.ey)
-        if sc.method == METHOD_UL_WEAK:
+        explicit = sc.method == METHOD_TL_WEAK and b.ex == 0
+        if explicit:
+            q = np.ascontiguousarray(b.quads, np.uint32).reshape(-1, 4)
+            u32(len(q)); u32(b.order); u32(b.shape)
+            out.extend(q.tobytes())
+        if sc.method == METHOD_UL_WEAK or explicit:
             ng = len(b.gp["x"])
             u32(ng)
             for k in IN_NAMES:
@@ -839,7 +851,12 @@ def read_case(path: str) -> Scenario:
             bcs.append(BC(kind, v, idx))
         ex, ey = u32(), u32()
         body = Body(a, hull, bcs, ex, ey)
-        if method == METHOD_UL_WEAK:
+        explicit = method == METHOD_TL_WEAK and ex == 0
+        if explicit:
+            ne = u32()
+            body.order, body.shape = u32(), u32()
+            body.quads = arr(np.uint32, 4 * ne).reshape(-1, 4)
+        if method == METHOD_UL_WEAK or explicit:
             ng = u32()
             body.gp = {k: arr(np.float64, ng) for k in IN_NAMES}
         bodies.append(body)

@@ -73,6 +73,8 @@ enum Action : uint32_t {
 // vx = v, vy = 0, vx_t = vy_t = 0.
 enum BCKind : uint32_t { BC_PULL_TL = 1, BC_VELOCITY_UL = 2 };
 
+enum Shape : uint32_t { SHAPE_RKPM = 0, SHAPE_ELEMENT = 1 };
+
 struct BC {
 	uint32_t kind = 0;
 	double v = 0.;
@@ -92,7 +94,14 @@ struct BodyIn {
 	std::vector<uint32_t> hull;
 	std::vector<BC> bcs;
 	uint32_t ex = 0, ey = 0;  // TL_WEAK: element_map_rectangle(ex, ey), 2x2 Gauss points
-	// UL_WEAK: the stress points (their NIN arrays), present in the file for that method only
+	// TL_WEAK with ex = ey = 0: an explicit element map (ll, lr, tr, tl per element), the
+	// Gauss order per direction, and the shape functions of the Gauss points
+	// (SHAPE_RKPM: neighbour search + RKPM as tensile_tl_weak; SHAPE_ELEMENT: the
+	// elements' own bilinear functions, as the *_fem set-ups)
+	std::vector<uint32_t> quads;
+	uint32_t order = 2, shape = 0;
+	// UL_WEAK: the stress points; TL_WEAK with an explicit map: the Gauss points as the
+	// set-up left them (x, y, X, Y, h, rho are read) -- their NIN arrays
 	uint32_t ngp = 0;
 	std::vector<double> g[NIN];
 };
@@ -160,7 +169,13 @@ inline Case read_case(const char* path) {
 			r.vu32(bc.idx, k);
 		}
 		b.ex = r.u32(); b.ey = r.u32();
-		if (c.method == UL_WEAK) {
+		if (c.method == TL_WEAK && b.ex == 0) {
+			uint32_t ne = r.u32();
+			b.order = r.u32();
+			b.shape = r.u32();
+			r.vu32(b.quads, 4 * (size_t)ne);
+		}
+		if (c.method == UL_WEAK || (c.method == TL_WEAK && b.ex == 0)) {
 			b.ngp = r.u32();
 			for (int k = 0; k < NIN; k++) r.vf64(b.g[k], b.ngp);
 		}

@@ -1555,16 +1555,33 @@ std::vector<Elem> element_map_rectangle(unsigned ex, unsigned ey) {
 	return map;
 }
 
-// gauss_int::update_gauss_points (gauss_integration.h:47-123) with order 2
-// (gauss_integration.cpp:20-34 shape functions, :44-52 abscissae, :127-141 tensor rule)
+// gauss_int::update_gauss_points (gauss_integration.h:47-123): per element the Gauss
+// points of the tensor rule of `order` (gauss_integration.cpp:20-34 shape functions,
+// :38-64 abscissae, :127-141 tensor rule), their weights J w and the elements' own
+// shape functions.  The element geometry is the particles' reference position X: the
+// set-ups call it before they move any body.  With an explicit element map the Gauss
+// points' x, y, h and rho come from the case (as the set-up left them, e.g. shifted
+// with their body); otherwise x = X, h = gp_h, rho = gp_rho.  SHAPE_RKPM then replaces
+// the element functions by neighbour search + RKPM (tensile.cpp:797-801, rings.cpp:1015-1025);
+// SHAPE_ELEMENT keeps them (the *_fem set-ups) and gives the particles no lists.
 void Sim::setup_weak(Body& B, const BodyIn& in) {
-	std::vector<Elem> elems = element_map_rectangle(in.ex, in.ey);
-	const double p1[2] = {0.577350269189626, -0.577350269189626};
-	const double w1[2] = {1.000000000000000, 1.000000000000000};
+	std::vector<Elem> elems;
+	if (in.ex) {
+		elems = element_map_rectangle(in.ex, in.ey);
+	} else {
+		for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
+			elems.push_back(Elem{in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]});
+	}
+	const unsigned order = in.ex ? 2 : in.order;
+	double p1[2], w1[2];
+	if (order == 1) { p1[0] = 0.; w1[0] = 2.; }
+	else if (order == 2) { p1[0] = 0.577350269189626; p1[1] = -0.577350269189626; w1[0] = w1[1] = 1.000000000000000; }
+	else throw Fail{"gauss: orders 1 and 2 only"};
+	const unsigned npe = order * order;
 	double lx[4], ly[4], lw[4];
-	for (unsigned i = 0, k = 0; i < 2; i++)
-		for (unsigned j = 0; j < 2; j++, k++) { lx[k] = p1[i]; ly[k] = p1[j]; lw[k] = w1[i] * w1[j]; }
-	unsigned ngp = 4 * (unsigned)elems.size();
+	for (unsigned i = 0, k = 0; i < order; i++)
+		for (unsigned j = 0; j < order; j++, k++) { lx[k] = p1[i]; ly[k] = p1[j]; lw[k] = w1[i] * w1[j]; }
+	unsigned ngp = npe * (unsigned)elems.size();
 	B.Q.resize(ngp);
 	for (int s = 0; s < 4; s++) B.kq[s].resize(ngp);
 	PSet& Q = B.Q;
@@ -1572,12 +1589,12 @@ void Sim::setup_weak(Body& B, const BodyIn& in) {
 	for (const Elem& e : elems) {
 		unsigned node_idx[4] = {e.ll, e.lr, e.tr, e.tl};
 		glm::dmat2x4 m_node, m_node_par;
-		for (int I = 0; I < 4; I++) { m_node[0][I] = B.P.x[node_idx[I]]; m_node[1][I] = B.P.y[node_idx[I]]; }
+		for (int I = 0; I < 4; I++) { m_node[0][I] = B.P.X[node_idx[I]]; m_node[1][I] = B.P.Y[node_idx[I]]; }
 		m_node_par[0][0] = -1; m_node_par[1][0] = -1;
 		m_node_par[0][1] = +1; m_node_par[1][1] = -1;
 		m_node_par[0][2] = +1; m_node_par[1][2] = +1;
 		m_node_par[0][3] = -1; m_node_par[1][3] = +1;
-		for (unsigned i = 0; i < 4; i++) {
+		for (unsigned i = 0; i < npe; i++) {
 			double xi = lx[i], eta = ly[i], local_w = lw[i];
 			const double X1 = -1, Y1 = -1, X2 = 1, Y2 = -1, X3 = 1, Y3 = 1, X4 = -1, Y4 = 1;
 			glm::dvec4 N;
@@ -1618,8 +1635,13 @@ void Sim::setup_weak(Body& B, const BodyIn& in) {
 			g++;
 		}
 	}
-	for (unsigned i = 0; i < ngp; i++) { Q.h[i] = c.gp_h; Q.rho[i] = c.gp_rho; }
-	// tensile.cpp:797-801
+	const bool given = !in.ex && in.ngp == ngp;
+	for (unsigned i = 0; i < ngp; i++) {
+		Q.h[i] = given ? in.g[6][i] : c.gp_h;
+		Q.rho[i] = given ? in.g[5][i] : c.gp_rho;
+		if (given) { Q.x[i] = in.g[0][i]; Q.y[i] = in.g[1][i]; }
+	}
+	if (!in.ex && in.shape == SHAPE_ELEMENT) return;
 	find_neighbors(B.P, B.P, c.nbh_h, c.nbh_eps);
 	find_neighbors(Q, B.P, c.nbh_h, c.nbh_eps);
 	precomp_rkpm(Q, B.P);

@@ -24,6 +24,7 @@
 #include "benchmarks/rings.h"
 #include "benchmarks/tensile.h"
 #include "benchmarks/rotation.h"
+#include "benchmarks/utils.h"
 #include "interpolation.h"
 
 #include "vtk_writer.h"
@@ -72,6 +73,24 @@ void capture_gp(body<T>& b) {
 	for (unsigned i = 0; i < g.n; i++) {
 		double f[NIN] = {q[i]->x, q[i]->y, q[i]->X, q[i]->Y, q[i]->m, q[i]->rho, 0., q[i]->quad_weight,
 		                 0., 0., q[i]->Sxx, q[i]->Sxy, q[i]->Syy};
+		for (int k = 0; k < NIN; k++) g.a[k][i] = f[k];
+	}
+}
+
+// The Gauss points of a particle_tl_weak body as its set-up left them (the body keeps
+// them private): copied at the first derivative evaluation, where nothing has changed
+// their position, h or density yet.
+template <typename T>
+void capture_gp_tl(body<T>& b) {
+	if (g_gp_done[g_cur_body]) return;
+	g_gp_done[g_cur_body] = true;
+	BodyIn& g = g_gp[g_cur_body];
+	T** q = b.get_cur_quad_points();
+	g.n = b.get_num_quad_points();
+	for (int k = 0; k < NIN; k++) g.a[k].resize(g.n);
+	for (unsigned i = 0; i < g.n; i++) {
+		double f[NIN] = {q[i]->x, q[i]->y, q[i]->X, q[i]->Y, q[i]->m, q[i]->rho, q[i]->h, q[i]->quad_weight,
+		                 q[i]->vx, q[i]->vy, q[i]->Sxx, q[i]->Sxy, q[i]->Syy};
 		for (int k = 0; k < NIN; k++) g.a[k][i] = f[k];
 	}
 }
@@ -475,21 +494,40 @@ int run_case(const Case& c, const char* out) {
 		for (unsigned b = 0; b < c.nbodies; b++) {
 			const BodyIn& in = c.bodies[b];
 			T** p = make_particles<T>(in);
-			std::vector<element> elements = element_map_rectangle(in.ex, in.ey);
-			unsigned num_gp = 2 * 2 * elements.size();
+			std::vector<element> elements;
+			if (in.ex) {
+				elements = element_map_rectangle(in.ex, in.ey);
+			} else {
+				for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
+					elements.push_back(element(in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]));
+			}
+			const unsigned order = in.ex ? 2 : in.order;
+			unsigned num_gp = order * order * elements.size();
 			T** gp = new T*[num_gp];
 			for (unsigned i = 0; i < num_gp; i++) gp[i] = new T(i);
-			gauss_int gi(elements, 2);
+			gauss_int gi(elements, order);
+			// the set-ups place the Gauss points before they move any body: from X
+			std::vector<double> sx(in.n), sy(in.n);
+			for (unsigned i = 0; i < in.n; i++) { sx[i] = p[i]->x; sy[i] = p[i]->y; p[i]->x = p[i]->X; p[i]->y = p[i]->Y; }
 			gi.update_gauss_points(p, gp);
-			for (unsigned i = 0; i < num_gp; i++) { gp[i]->h = c.gp_h; gp[i]->rho = c.gp_rho; }
-			find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
-			find_neighbors(p, in.n, gp, num_gp, c.nbh_h, distance_euclidian);
-			precomp_rkpm<T>(p, gp, num_gp);
-			precomp_rkpm<T>(p, in.n);
+			for (unsigned i = 0; i < in.n; i++) { p[i]->x = sx[i]; p[i]->y = sy[i]; }
+			const bool given = !in.ex && in.ngp == num_gp;
+			for (unsigned i = 0; i < num_gp; i++) {
+				gp[i]->h = given ? in.g[6][i] : c.gp_h;
+				gp[i]->rho = given ? in.g[5][i] : c.gp_rho;
+				if (given) { gp[i]->x = in.g[0][i]; gp[i]->y = in.g[1][i]; }
+			}
+			if (in.ex || in.shape == SHAPE_RKPM) {
+				find_neighbors(p, in.n, c.nbh_h, distance_euclidian);
+				find_neighbors(p, in.n, gp, num_gp, c.nbh_h, distance_euclidian);
+				precomp_rkpm<T>(p, gp, num_gp);
+				precomp_rkpm<T>(p, in.n);
+			}
 			record_fixed_nbh(p, in.n, (int)b);
 			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot), gp, num_gp));
 		}
 		for (unsigned b = 0; b < c.nbodies; b++) {
+			attach_hull(bodies[b], c.bodies[b].hull);
 			for (uint32_t a : c.actions) {
 				WkAct f = wk_action(a);
 				if (!f) { fprintf(stderr, "action %u not valid for TL_WEAK\n", a); return 2; }
@@ -527,7 +565,11 @@ void write_case(const char* path, const Case& c) {
 			w.raw(bc.idx.data(), bc.idx.size() * 4);
 		}
 		w.u32(b.ex); w.u32(b.ey);
-		if (c.method == UL_WEAK) {
+		if (c.method == TL_WEAK && b.ex == 0) {
+			w.u32((uint32_t)(b.quads.size() / 4)); w.u32(b.order); w.u32(b.shape);
+			w.raw(b.quads.data(), b.quads.size() * 4);
+		}
+		if (c.method == UL_WEAK || (c.method == TL_WEAK && b.ex == 0)) {
 			w.u32(b.ngp);
 			for (int k = 0; k < NIN; k++) w.raw(b.g[k].data(), b.ngp * 8);
 		}
@@ -790,6 +832,66 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 			std::vector<void (*)(body<T>&)> acts;
 			bodies[b].add_action(&record_first_nbh<T>);
 			bodies[b].add_action(&capture_gp<T>);
+		}
+		c.nbodies = (uint32_t)bodies.size();
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			c.bodies[b].ngp = g_gp[b].n;
+			for (int k = 0; k < NIN; k++) c.bodies[b].g[k] = g_gp[b].a[k];
+		}
+		write_case(case_out, c);
+	} else if (name == "tensile_tl_fem" || name == "rotation_tl_fem" || name == "rings_tl_fem_contact" ||
+	           name == "rotation_tl_weak" || name == "rings_tl_weak_contact") {
+		// weak TL bodies on explicit element maps: the rectangle (tensile.cpp:581) or
+		// mesh_ring (rings.cpp:742-743, rotation.cpp:425,555), 2x2 Gauss points; the
+		// *_fem set-ups keep the elements' shape functions, the *_weak ones use RKPM
+		typedef particle_tl_weak T;
+		const bool rings = name.compare(0, 6, "rings_") == 0, disc = name.compare(0, 9, "rotation_") == 0;
+		const bool fem = name.find("_fem") != std::string::npos;
+		std::vector<body<T>> bodies = name == "tensile_tl_fem"   ? tensile_tl_fem(nbox)
+		                              : name == "rotation_tl_fem" ? rotation_tl_fem(nbox)
+		                              : name == "rings_tl_fem_contact" ? rings_tl_fem_contact(nbox)
+		                              : name == "rotation_tl_weak" ? rotation_tl_weak(nbox)
+		                                                             : rings_tl_weak_contact(nbox);
+		std::vector<element> elems;
+		if (rings || disc) {
+			unsigned nn = 0;
+			T** tmp = mesh_ring<T>(nbox, nn, elems, rings ? 0.03 : 0., rings ? 0.04 : 1.);
+			for (unsigned i = 0; i < nn; i++) delete tmp[i];
+			delete[] tmp;
+		} else {
+			elems = element_map_rectangle(nbox - 1, nbox - 1);
+		}
+		c.method = TL_WEAK;
+		c.contact = rings ? 1 : 0;
+		c.actions = {DERIVE_DISPLACEMENT_WEAK, DERIVE_VELOCITY_TL_WEAK, CONTMECH_VELOCITY_GRADIENT_TL_GP, CONTMECH_CONTINUITY_GP,
+		             MATERIAL_EOS_GP, MATERIAL_STRESS_RATE_JAUMANN_GP, CONTMECH_CAUCHY_TO_NOMINAL_GP, DERIVE_STRESS_WEAK_TL,
+		             CONTMECH_MOMENTUM_TL_WEAK, CONTMECH_ADVECTION};  // rings.cpp:802-811 and the same lists
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = fem ? 0. : bodies[0].get_particles()[0]->h;  // find_neighbors(.., hdx*dx, ..)
+		g_gp.assign(bodies.size(), BodyIn());
+		g_gp_done.assign(bodies.size(), false);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			BodyIn in = capture(bodies[b]);
+			in.ex = in.ey = 0;
+			in.order = 2;
+			in.shape = fem ? SHAPE_ELEMENT : SHAPE_RKPM;
+			for (const element& e : elems) {
+				in.quads.push_back(e.ll_idx); in.quads.push_back(e.lr_idx);
+				in.quads.push_back(e.tr_idx); in.quads.push_back(e.tl_idx);
+			}
+			if (name == "tensile_tl_fem") {
+				BC l, r;  // tensile.cpp:595-596
+				l.kind = r.kind = BC_PULL_TL;
+				l.v = -10.; r.v = 10.;
+				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+				in.bcs = {l, r};
+			}
+			c.bodies.push_back(in);
+			record_fixed_nbh(bodies[b].get_particles(), bodies[b].get_num_part(), (int)b);
+			bodies[b].add_action(&capture_gp_tl<T>);
 		}
 		c.nbodies = (uint32_t)bodies.size();
 		Writer w(out);

@@ -48,6 +48,11 @@ REFERENCE_CASES = [
     ("tensile_ul_weak", 11, 25),
     ("rotation_ul_weak", 21, 50),
     ("rings_ul_weak_contact", 20, 450),
+    ("tensile_tl_fem", 11, 25),
+    ("rotation_tl_fem", 15, 50),
+    ("rotation_tl_weak", 15, 50),
+    ("rings_tl_fem_contact", 20, 450),
+    ("rings_tl_weak_contact", 20, 450),
 ]
 
 
