@@ -178,6 +178,25 @@ MF_API mf_status mf_set_boundary(mf_ctx* ctx, int32_t body, const uint32_t* idx,
  * ((ex+1)*(ey+1) particles, ex+1 per row) with 2x2 Gauss points per element, whose h
  * and rho are gp_h and gp_rho (gauss_int, tensile.cpp:776-795). */
 MF_API mf_status mf_set_gauss_mesh(mf_ctx* ctx, int32_t body, uint32_t ex, uint32_t ey, double gp_h, double gp_rho);
+/* Weak-form shape functions of a MF_METHOD_TL_WEAK body (mf_set_elements). */
+enum {
+	MF_SHAPE_RKPM = 0,   /* RKPM on neighbourhoods of radius config.nbh_h (tensile.cpp:797-801) */
+	MF_SHAPE_ELEMENT = 1 /* the elements' own bilinear functions: each Gauss point sees its element's four
+	                        nodes (the *_fem set-ups: tensile.cpp:585-601, rotation.cpp:425-440, rings.cpp:742-790) */
+};
+/* MF_METHOD_TL_WEAK on an explicit element map (element.h: ll, lr, tr, tl particle indices of
+ * the body per element, quads[4 e + k]): order x order Gauss points per element (order 1 or
+ * 2; gauss_int::update_gauss_points, gauss_integration.h:47-123) placed on the particles'
+ * reference positions X, with h = gp_h and rho = gp_rho (both positive) unless
+ * mf_set_gauss_points gives them; `shape` is MF_SHAPE_RKPM or MF_SHAPE_ELEMENT.  Replaces mf_set_gauss_mesh. */
+MF_API mf_status mf_set_elements(mf_ctx* ctx, int32_t body, const uint32_t* quads, uint32_t n_elem, uint32_t order,
+                                 int32_t shape, double gp_h, double gp_rho);
+/* The Gauss points' current position, h and rho as the set-up left them (e.g. moved with
+ * their body after update_gauss_points, rings.cpp:1003-1013), n = order^2 * n_elem, point
+ * order^2 e + (i order + j) for abscissae i (xi) and j (eta).  A point's displacement from
+ * its place on X enters the displacement gradient (derivatives.h:296-345). */
+MF_API mf_status mf_set_gauss_points(mf_ctx* ctx, int32_t body, const double* x, const double* y, const double* h,
+                                     const double* rho, uint32_t n);
 
 /* MF_METHOD_UL_WEAK: the body's stress points (the quad_points of body<particle_ul_weak>,
  * body.h:216-217), n of them, with the particles' field layout (X, Y may be NULL).  Their

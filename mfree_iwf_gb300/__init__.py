@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmfree_gb300.so")
 
 METHOD_UL, METHOD_TL, METHOD_TL_WEAK, METHOD_COROT, METHOD_POTENTIAL, METHOD_UL_WEAK = 1, 2, 3, 4, 5, 6
+SHAPE_RKPM, SHAPE_ELEMENT = 0, 1  # weak TL shape functions (mf_set_elements)
 PREC_FP64_STRICT, PREC_FP64, PREC_MIXED = 0, 1, 2
 PRECISIONS = {"fp64_strict": PREC_FP64_STRICT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
 BC_PULL = 1       # tensile.cpp:20-42, TL-type bodies
@@ -103,6 +104,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_set_boundary": (C.c_int32, [C.c_void_p, C.c_int32, _UP, C.c_uint32]),
         "mf_set_gauss_mesh": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_double, C.c_double]),
         "mf_set_stress_points": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint32]),
+        "mf_set_elements": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32,
+                                        C.c_double, C.c_double]),
+        "mf_set_gauss_points": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_uint32]),
         "mf_convex_hull": (C.c_int32, [_DP, _DP, C.c_uint32, _UP, _UP]),
         "mf_step": (C.c_int32, [C.c_void_p, C.c_int32]),
         "mf_synchronize": (C.c_int32, [C.c_void_p]),
@@ -257,6 +262,20 @@ class Simulation:
 
     def set_gauss_mesh(self, body: int, ex: int, ey: int, gp_h: float, gp_rho: float) -> None:
         self._check(self._lib.mf_set_gauss_mesh(self._h, body, ex, ey, gp_h, gp_rho), "mf_set_gauss_mesh")
+
+    def set_elements(self, body: int, quads: np.ndarray, order: int, shape: int, gp_h: float, gp_rho: float) -> None:
+        """A METHOD_TL_WEAK body's explicit element map (n_elem x 4 body-local particle indices
+        ll, lr, tr, tl), Gauss order (1 or 2) and shape kind (SHAPE_RKPM or SHAPE_ELEMENT)."""
+        q = np.ascontiguousarray(quads, np.uint32).reshape(-1)
+        self._check(self._lib.mf_set_elements(self._h, body, q.ctypes.data_as(_UP), len(q) // 4, int(order), int(shape),
+                                              gp_h, gp_rho), "mf_set_elements")
+
+    def set_gauss_points(self, body: int, x, y, h, rho) -> None:
+        """The Gauss points' current x, y, h and rho of a METHOD_TL_WEAK body on an explicit
+        element map, as the set-up left them."""
+        cols = [np.ascontiguousarray(a, np.float64) for a in (x, y, h, rho)]
+        self._check(self._lib.mf_set_gauss_points(self._h, body, *[_dptr(a) for a in cols], len(cols[0])),
+                    "mf_set_gauss_points")
 
     def set_stress_points(self, body: int, arrays: Dict[str, np.ndarray]) -> None:
         """The stress points of a METHOD_UL_WEAK body (the particles' 13 fields)."""
@@ -418,7 +437,12 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
         if len(b.hull):
             sim.set_boundary(bid, b.hull)
         if sc.method == METHOD_TL_WEAK:
-            sim.set_gauss_mesh(bid, b.ex, b.ey, sc.gp_h, sc.gp_rho)
+            if b.quads is not None and len(b.quads):
+                sim.set_elements(bid, b.quads, b.order, b.shape, sc.gp_h, sc.gp_rho)
+                if b.gp is not None:
+                    sim.set_gauss_points(bid, b.gp["x"], b.gp["y"], b.gp["h"], b.gp["rho"])
+            else:
+                sim.set_gauss_mesh(bid, b.ex, b.ey, sc.gp_h, sc.gp_rho)
         if sc.method == METHOD_UL_WEAK:
             sim.set_stress_points(bid, b.gp)
     return sim

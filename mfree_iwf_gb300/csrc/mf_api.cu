@@ -160,7 +160,11 @@ struct HostBody {
 	std::vector<HostBC> bcs;
 	std::vector<double> in[13];  // x y X Y m rho h qw vx vy Sxx Sxy Syy
 	uint32_t ex = 0, ey = 0;     // TL_WEAK: element_map_rectangle(ex, ey), 2x2 Gauss points
+	std::vector<uint32_t> quads;  // TL_WEAK: explicit element map (ll lr tr tl, body-local), mf_set_elements
+	uint32_t order = 2;
+	int32_t shape = MF_SHAPE_RKPM;
 	double gp_h = 0., gp_rho = 0.;
+	std::vector<double> gpt[4];  // TL_WEAK: given Gauss-point x, y, h, rho (mf_set_gauss_points)
 	uint32_t n_sp = 0;           // UL_WEAK: stress points (mf_set_stress_points), same fields as `in`
 	std::vector<double> sp[13];
 };
@@ -258,7 +262,7 @@ struct mf_ctx {
 	uint32_t n_g = 0;
 	DevBuf<uint32_t> gp_body, g_sl, g_snbr, t_sl, t_snbr, p_sl, p_snbr;
 	DevBuf<uint16_t> g_cnt, t_cnt, p_cnt;
-	DevBuf<double> gp_x, gp_y, gp_qw, gp_hh, gsd[3][4], gP64;
+	DevBuf<double> gp_x, gp_y, gp_qw, gp_hh, gp_ux, gp_uy, gsd[3][4], gP64;
 	DevBuf<float> gsf[3][4];
 	DevBuf<float4> gP32, wpack;
 	DevBuf<double2> g_w64, t_w64, p_w64;
@@ -1292,95 +1296,207 @@ mf_status validate_weak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t& f
 		return fail(c, MF_ERR_PIPELINE, "contmech_momentum_tl_weak needs derive_stress_weak_tl before it");
 	if ((flags & abit(MF_CONTMECH_VELOCITY_GRADIENT_TL_GP)) && !(flags & abit(MF_DERIVE_VELOCITY_TL_WEAK)))
 		return fail(c, MF_ERR_PIPELINE, "the Gauss-point velocity gradient needs derive_velocity_tl_weak before it");
-	for (auto& b : c->bodies)
-		if (b.ex == 0 || b.ey == 0) return fail(c, MF_ERR_STATE, "a TL_WEAK body needs mf_set_gauss_mesh");
+	for (auto& b : c->bodies) {
+		if ((b.ex == 0 || b.ey == 0) && b.quads.empty())
+			return fail(c, MF_ERR_STATE, "a TL_WEAK body needs mf_set_gauss_mesh or mf_set_elements");
+		if (b.shape != c->bodies[0].shape)
+			return fail(c, MF_ERR_PIPELINE, "all TL_WEAK bodies take the same shape-function kind");
+		const uint64_t ne = b.quads.empty() ? (uint64_t)b.ex * b.ey : b.quads.size() / 4;
+		const uint64_t ngp = ne * (b.quads.empty() ? 4u : b.order * b.order);
+		if (!b.gpt[0].empty() && (b.quads.empty() || b.gpt[0].size() != ngp))
+			return fail(c, MF_ERR_ARG, "mf_set_gauss_points gave %zu points; the element map has %llu", b.gpt[0].size(),
+			            (unsigned long long)ngp);
+		if (b.gpt[0].empty() && (!(b.gp_h > 0.) || !(b.gp_rho > 0.)))
+			return fail(c, MF_ERR_ARG, "Gauss-point h and rho must be positive (or given by mf_set_gauss_points)");
+	}
 	return MF_OK;
 }
 
-// Weak-form set-up (tensile.cpp:776-807): Gauss points, the lists of Gauss points and
-// particles, RKPM shape functions, the transposed Gauss-point lists, sliced ELL.
+// Element map of a weak TL body: the explicit one, or element_map_rectangle(ex, ey)
+// (element.cpp:23-39: row-major elements, nodes ll lr tr tl), in global particle indices.
+static void body_quads(const HostBody& B, std::vector<uint32_t>& q) {
+	if (!B.quads.empty()) {
+		for (uint32_t k : B.quads) q.push_back(B.off + k);
+		return;
+	}
+	const uint32_t nx = B.ex + 1;
+	for (uint32_t i = 0; i < B.ey; i++)
+		for (uint32_t j = 0; j < B.ex; j++) {
+			uint32_t ll = B.off + i * nx + j;
+			q.push_back(ll); q.push_back(ll + 1); q.push_back(ll + nx + 1); q.push_back(ll + nx);
+		}
+}
+
+// Weak-form set-up (tensile.cpp:776-807, rings.cpp:742-790, rotation.cpp:425-440): Gauss
+// points on the element maps, the lists of Gauss points and particles (RKPM on
+// neighbourhoods, or the elements' own functions), the transposed Gauss-point lists,
+// sliced ELL.
 mf_status weak_setup(mf_ctx* c) {
 	uint32_t n = c->n_total;
 	uint32_t nb = (uint32_t)c->bodies.size();
-	if (!(c->cfg.nbh_h > 0.)) return fail(c, MF_ERR_ARG, "TL_WEAK needs config.nbh_h > 0");
-	std::vector<uint32_t> elem_body, bex(nb), bpoff(nb), beoff(nb), gpb;
-	std::vector<double> gh;
-	uint64_t ne = 0;
+	const bool fem = c->bodies[0].shape == MF_SHAPE_ELEMENT;
+	if (!fem && !(c->cfg.nbh_h > 0.)) return fail(c, MF_ERR_ARG, "TL_WEAK with RKPM needs config.nbh_h > 0");
+	std::vector<uint32_t> quads, gpb, b_order(nb), b_eoff(nb + 1), b_goff(nb + 1);
+	std::vector<double> gh, grho;
+	uint64_t ng64 = 0;
 	for (uint32_t b = 0; b < nb; b++) {
 		const HostBody& B = c->bodies[b];
-		bex[b] = B.ex; bpoff[b] = B.off; beoff[b] = (uint32_t)ne;
-		uint64_t k = (uint64_t)B.ex * B.ey;
-		ne += k;
-		if (4 * ne > 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 Gauss points");
-		elem_body.insert(elem_body.end(), k, b);
-		gpb.insert(gpb.end(), 4 * k, b);
-		gh.insert(gh.end(), 4 * k, B.gp_h);
+		b_eoff[b] = (uint32_t)(quads.size() / 4);
+		b_goff[b] = (uint32_t)ng64;
+		body_quads(B, quads);
+		b_order[b] = B.quads.empty() ? 2u : B.order;
+		uint64_t k = (uint64_t)(quads.size() / 4 - b_eoff[b]) * b_order[b] * b_order[b];
+		ng64 += k;
+		if (ng64 > 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 Gauss points");
+		gpb.insert(gpb.end(), k, b);
+		if (B.gpt[0].empty()) {
+			gh.insert(gh.end(), k, B.gp_h);
+			grho.insert(grho.end(), k, B.gp_rho);
+		} else {
+			gh.insert(gh.end(), B.gpt[2].begin(), B.gpt[2].end());
+			grho.insert(grho.end(), B.gpt[3].begin(), B.gpt[3].end());
+		}
 	}
-	c->n_g = (uint32_t)(4 * ne);
+	b_eoff[nb] = (uint32_t)(quads.size() / 4);
+	b_goff[nb] = (uint32_t)ng64;
+	c->n_g = (uint32_t)ng64;
 	uint32_t ng = c->n_g;
 	c->do_smooth = c->bodies[0].sd.do_smooth != 0;
-	DevBuf<uint32_t> d_eb, d_bex, d_bpoff, d_beoff;
-	auto up32 = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
-		CK(d.alloc(v.size()));
-		if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
-		return MF_OK;
-	};
+	DevBuf<uint32_t> d_quads;
 	mf_status st;
-	if ((st = up32(d_eb, elem_body)) || (st = up32(d_bex, bex)) || (st = up32(d_bpoff, bpoff)) ||
-	    (st = up32(d_beoff, beoff)) || (st = up32(c->gp_body, gpb)))
-		return st;
+	CK(d_quads.alloc(quads.size()));
+	CK(cudaMemcpy(d_quads.p, quads.data(), quads.size() * 4, cudaMemcpyHostToDevice));
+	CK(c->gp_body.alloc(ng));
+	CK(cudaMemcpy(c->gp_body.p, gpb.data(), (size_t)ng * 4, cudaMemcpyHostToDevice));
 	CK(c->gp_x.alloc(ng)); CK(c->gp_y.alloc(ng)); CK(c->gp_qw.alloc(ng)); CK(c->gp_hh.alloc(ng));
+	CK(c->gp_ux.alloc(ng)); CK(c->gp_uy.alloc(ng));
 	CK(cudaMemcpy(c->gp_hh.p, gh.data(), (size_t)ng * 8, cudaMemcpyHostToDevice));
+	// update_gauss_points on the reference positions X, body runs of one order per launch
+	DevBuf<double> gX, gY, fwx, fwy;
+	CK(gX.alloc(ng)); CK(gY.alloc(ng));
+	if (fem) { CK(fwx.alloc(4 * (size_t)ng)); CK(fwy.alloc(4 * (size_t)ng)); }
+	cudaError_t e = cudaSuccess;
+	for (uint32_t b0 = 0, b1; b0 < nb; b0 = b1) {
+		for (b1 = b0 + 1; b1 < nb && b_order[b1] == b_order[b0];) b1++;
+		const uint32_t eo = b_eoff[b0], go = b_goff[b0], ne = b_eoff[b1] - eo;
+		const uint32_t* q = d_quads.p + 4 * (size_t)eo;
+		double* w3[3] = {nullptr, fem ? fwx.p + 4 * (size_t)go : nullptr, fem ? fwy.p + 4 * (size_t)go : nullptr};
+		e = c->strict ? mf_strict::weak_gauss_points(ne, q, b_order[b0], c->X.p, c->Y.p, gX.p + go, gY.p + go,
+		                                             c->gp_qw.p + go, w3[0], w3[1], w3[2], c->d_status, c->stream)
+		              : mf_fast::weak_gauss_points(ne, q, b_order[b0], c->X.p, c->Y.p, gX.p + go, gY.p + go,
+		                                           c->gp_qw.p + go, w3[0], w3[1], w3[2], c->d_status, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "weak_gauss_points");
+	}
+	if ((st = check_status(c)) != MF_OK) return st;
+	// current Gauss-point positions: as given, else where update_gauss_points put them
+	CK(cudaMemcpyAsync(c->gp_x.p, gX.p, (size_t)ng * 8, cudaMemcpyDeviceToDevice, c->stream));
+	CK(cudaMemcpyAsync(c->gp_y.p, gY.p, (size_t)ng * 8, cudaMemcpyDeviceToDevice, c->stream));
+	for (uint32_t b = 0; b < nb; b++) {
+		const HostBody& B = c->bodies[b];
+		if (B.gpt[0].empty()) continue;
+		CK(cudaMemcpyAsync(c->gp_x.p + b_goff[b], B.gpt[0].data(), B.gpt[0].size() * 8, cudaMemcpyHostToDevice, c->stream));
+		CK(cudaMemcpyAsync(c->gp_y.p + b_goff[b], B.gpt[1].data(), B.gpt[1].size() * 8, cudaMemcpyHostToDevice, c->stream));
+	}
+	e = c->strict ? mf_strict::weak_gp_disp(ng, c->gp_x.p, c->gp_y.p, gX.p, gY.p, c->gp_ux.p, c->gp_uy.p, c->stream)
+	              : mf_fast::weak_gp_disp(ng, c->gp_x.p, c->gp_y.p, gX.p, gY.p, c->gp_ux.p, c->gp_uy.p, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "weak_gp_disp");
+	CK(cudaStreamSynchronize(c->stream));
+	gX.free(); gY.free();
 	const double* px = c->sd[0][0].p;
 	const double* py = c->sd[0][1].p;
-	cudaError_t e = c->strict ? mf_strict::weak_gauss_points((uint32_t)ne, d_eb.p, d_bex.p, d_bpoff.p, d_beoff.p, px, py,
-	                                                         c->gp_x.p, c->gp_y.p, c->gp_qw.p, c->d_status, c->stream)
-	                          : mf_fast::weak_gauss_points((uint32_t)ne, d_eb.p, d_bex.p, d_bpoff.p, d_beoff.p, px, py,
-	                                                       c->gp_x.p, c->gp_y.p, c->gp_qw.p, c->d_status, c->stream);
-	if (e != cudaSuccess) return cuda_fail(c, e, "weak_gauss_points");
-	if ((st = check_status(c)) != MF_OK) return st;
-	d_eb.free(); d_bex.free(); d_bpoff.free(); d_beoff.free();
 
 	// lists: Gauss points -> particles, particles -> particles, particles -> Gauss points
 	DevBuf<uint32_t> g_off, g_nbr, t_off, t_nbr;
 	std::vector<uint32_t> gc, pc, tc;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, c->cfg.max_nbh, g_off, g_nbr, gc, false)))
-		return st;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->nbr_off, c->nbr, pc, false)))
-		return st;
-	if ((st = build_lists(c, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, px, py, c->body_of.p, n, 8 * c->cfg.max_nbh, t_off,
-	                      t_nbr, tc, false)))
-		return st;
-	uint64_t eg = g_nbr.n, ep = c->nbr.n, et = t_nbr.n;
-	// RKPM shape functions, FP64
 	DevBuf<double> gwx, gwy, pw, twx, twy;
-	CK(gwx.alloc(eg)); CK(gwy.alloc(eg)); CK(pw.alloc(ep)); CK(twx.alloc(et)); CK(twy.alloc(et));
-	DevBuf<double> rho_tmp;  // the mixed form keeps no FP64 density; the set-up needs one
-	if (c->mixed) {
-		CK(rho_tmp.alloc(n));
-		std::vector<double> v(n);
-		for (auto& b : c->bodies) std::copy(b.in[5].begin(), b.in[5].end(), v.begin() + b.off);
-		CK(cudaMemcpy(rho_tmp.p, v.data(), (size_t)n * 8, cudaMemcpyHostToDevice));
+	if (fem) {
+		// the elements' own functions: a Gauss point sees its element's nodes in node order
+		// (gauss_integration.h:110-116); the particles have no lists (the *_fem set-ups run
+		// no neighbour search); the transposed lists keep the Gauss points ascending, the
+		// order of the scatter in derive_stress_weak_tl (derivatives.h:260-294)
+		std::vector<uint32_t> goff(ng + 1), gn(4 * (size_t)ng), toff(n + 1, 0), tn(4 * (size_t)ng), tsrc(4 * (size_t)ng);
+		for (uint32_t b = 0; b < nb; b++) {
+			const uint32_t npe = b_order[b] * b_order[b];
+			for (uint32_t g = b_goff[b]; g < b_goff[b + 1]; g++) {
+				const uint32_t el = b_eoff[b] + (g - b_goff[b]) / npe;
+				for (int k = 0; k < 4; k++) gn[4 * (size_t)g + k] = quads[4 * (size_t)el + k];
+			}
+		}
+		for (uint32_t g = 0; g <= ng; g++) goff[g] = 4 * g;
+		for (uint32_t v : gn) toff[v + 1]++;
+		tc.assign(toff.begin() + 1, toff.end());
+		for (uint32_t j = 0; j < n; j++) toff[j + 1] += toff[j];
+		std::vector<uint32_t> pos(toff.begin(), toff.end() - 1);
+		for (size_t k = 0; k < gn.size(); k++) {
+			uint32_t t = pos[gn[k]]++;
+			tn[t] = (uint32_t)(k / 4);
+			tsrc[t] = (uint32_t)k;
+		}
+		gc.assign(ng, 4);
+		pc.assign(n, 0);
+		std::vector<double> hx(4 * (size_t)ng), hy(4 * (size_t)ng), tx(4 * (size_t)ng), ty(4 * (size_t)ng);
+		CK(cudaMemcpy(hx.data(), fwx.p, hx.size() * 8, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(hy.data(), fwy.p, hy.size() * 8, cudaMemcpyDeviceToHost));
+		for (size_t t = 0; t < tn.size(); t++) { tx[t] = hx[tsrc[t]]; ty[t] = hy[tsrc[t]]; }
+		auto upu = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
+			CK(d.alloc(v.size()));
+			if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+			return MF_OK;
+		};
+		auto upd = [&](DevBuf<double>& d, const std::vector<double>& v) -> mf_status {
+			CK(d.alloc(v.size()));
+			if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+			return MF_OK;
+		};
+		std::vector<uint32_t> zoff(n + 1, 0);
+		if ((st = upu(g_off, goff)) || (st = upu(g_nbr, gn)) || (st = upu(t_off, toff)) || (st = upu(t_nbr, tn)) ||
+		    (st = upu(c->nbr_off, zoff)) || (st = upu(c->nbr, {})) || (st = upd(twx, tx)) || (st = upd(twy, ty)))
+			return st;
+		CK(pw.alloc(0));
+		gwx = fwx; gwy = fwy;
+		fwx.p = fwy.p = nullptr;
+	} else {
+		if ((st = build_lists(c, px, py, c->body_of.p, n, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, c->cfg.max_nbh, g_off,
+		                      g_nbr, gc, false)))
+			return st;
+		if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->nbr_off, c->nbr, pc,
+		                      false)))
+			return st;
+		if ((st = build_lists(c, c->gp_x.p, c->gp_y.p, c->gp_body.p, ng, px, py, c->body_of.p, n, 8 * c->cfg.max_nbh,
+		                      t_off, t_nbr, tc, false)))
+			return st;
+		uint64_t eg = g_nbr.n, ep = c->nbr.n, et = t_nbr.n;
+		// RKPM shape functions, FP64
+		CK(gwx.alloc(eg)); CK(gwy.alloc(eg)); CK(pw.alloc(ep)); CK(twx.alloc(et)); CK(twy.alloc(et));
+		DevBuf<double> rho_tmp;  // the mixed form keeps no FP64 density; the set-up needs one
+		if (c->mixed) {
+			CK(rho_tmp.alloc(n));
+			std::vector<double> v(n);
+			for (auto& b : c->bodies) std::copy(b.in[5].begin(), b.in[5].end(), v.begin() + b.off);
+			CK(cudaMemcpy(rho_tmp.p, v.data(), (size_t)n * 8, cudaMemcpyHostToDevice));
+		}
+		const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
+		const float* rho32 = nullptr;
+		auto rkpm = [&](uint32_t nt, const double* tx, const double* ty, const double* th, const uint32_t* off,
+		                const uint32_t* nbr, double* w, double* wx, double* wy) {
+			return c->strict ? mf_strict::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
+			                                        c->d_status, c->stream)
+			                 : mf_fast::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
+			                                      c->d_status, c->stream);
+		};
+		if ((e = rkpm(ng, c->gp_x.p, c->gp_y.p, c->gp_hh.p, g_off.p, g_nbr.p, nullptr, gwx.p, gwy.p)) != cudaSuccess)
+			return cuda_fail(c, e, "weak_rkpm");
+		if ((e = rkpm(n, px, py, c->h.p, c->nbr_off.p, c->nbr.p, pw.p, nullptr, nullptr)) != cudaSuccess)
+			return cuda_fail(c, e, "weak_rkpm");
+		e = c->strict ? mf_strict::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
+		                                          c->d_status, c->stream)
+		              : mf_fast::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
+		                                        c->d_status, c->stream);
+		if (e != cudaSuccess) return cuda_fail(c, e, "weak_transpose");
+		if ((st = check_status(c)) != MF_OK) return st;
+		CK(cudaStreamSynchronize(c->stream));
+		rho_tmp.free();
 	}
-	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
-	const float* rho32 = nullptr;
-	auto rkpm = [&](uint32_t nt, const double* tx, const double* ty, const double* th, const uint32_t* off,
-	                const uint32_t* nbr, double* w, double* wx, double* wy) {
-		return c->strict ? mf_strict::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
-		                                        c->d_status, c->stream)
-		                 : mf_fast::weak_rkpm(nt, tx, ty, th, off, nbr, px, py, c->m.p, rho64, rho32, w, wx, wy,
-		                                      c->d_status, c->stream);
-	};
-	if ((e = rkpm(ng, c->gp_x.p, c->gp_y.p, c->gp_hh.p, g_off.p, g_nbr.p, nullptr, gwx.p, gwy.p)) != cudaSuccess)
-		return cuda_fail(c, e, "weak_rkpm");
-	if ((e = rkpm(n, px, py, c->h.p, c->nbr_off.p, c->nbr.p, pw.p, nullptr, nullptr)) != cudaSuccess)
-		return cuda_fail(c, e, "weak_rkpm");
-	e = c->strict ? mf_strict::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
-	                                          c->d_status, c->stream)
-	              : mf_fast::weak_transpose(n, t_off.p, t_nbr.p, g_off.p, g_nbr.p, gwx.p, gwy.p, twx.p, twy.p,
-	                                        c->d_status, c->stream);
-	if (e != cudaSuccess) return cuda_fail(c, e, "weak_transpose");
-	if ((st = check_status(c)) != MF_OK) return st;
 	// sliced ELL (mixed: FP32 with the quad weights folded in)
 	uint64_t sg, sp, stt;
 	if ((st = sell_offsets(c, gc, c->g_sl, sg)) || (st = sell_offsets(c, pc, c->p_sl, sp)) ||
@@ -1410,8 +1526,7 @@ mf_status weak_setup(mf_ctx* c) {
 	CK(cudaStreamSynchronize(c->stream));
 	gwx.free(); gwy.free(); pw.free(); twx.free(); twy.free(); g_off.free(); g_nbr.free(); t_off.free(); t_nbr.free();
 	// Gauss-point state: rho = the set-up rho (tensile.cpp:792-795), S = 0
-	std::vector<double> grho(ng);
-	for (uint32_t g = 0; g < ng; g++) grho[g] = c->bodies[gpb[g]].gp_rho;
+	// (grho: gp_rho, or the given Gauss-point rho)
 	for (int k = 0; k < 3; k++)
 		for (int q = 0; q < 4; q++) {
 			if (mx) {
@@ -1450,6 +1565,7 @@ WeakArgs weak_args(mf_ctx* c) {
 	a.block = c->tune.tl_block;
 	a.params = c->params.p; a.body_of = c->body_of.p; a.gp_body = c->gp_body.p;
 	a.X = c->X.p; a.Y = c->Y.p; a.m = c->m.p; a.qw_p = c->qw0.p; a.gp_qw = c->gp_qw.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
+	a.gp_ux = c->gp_ux.p; a.gp_uy = c->gp_uy.p;
 	StateSoA* s[3] = {&a.base, &a.acc, &a.st};
 	for (int k = 0; k < 3; k++) {
 		double** d[8] = {&s[k]->x, &s[k]->y, &s[k]->vx, &s[k]->vy, &s[k]->rho, &s[k]->Sxx, &s[k]->Sxy, &s[k]->Syy};
@@ -1821,7 +1937,7 @@ mf_ctx::~mf_ctx() {
 		DevBuf<uint32_t>* w32s[] = {&gp_body, &g_sl, &g_snbr, &t_sl, &t_snbr, &p_sl, &p_snbr};
 		for (auto* p : w32s) p->free();
 		g_cnt.free(); t_cnt.free(); p_cnt.free();
-		gp_x.free(); gp_y.free(); gp_qw.free(); gp_hh.free(); gP64.free(); gP32.free(); wpack.free();
+		gp_x.free(); gp_y.free(); gp_qw.free(); gp_hh.free(); gp_ux.free(); gp_uy.free(); gP64.free(); gP32.free(); wpack.free();
 		for (int k = 0; k < 3; k++)
 			for (int q = 0; q < 4; q++) { gsd[k][q].free(); gsf[k][q].free(); }
 		g_w64.free(); t_w64.free(); p_w64.free(); g_w32.free(); t_w32.free(); p_w32.free();
@@ -1965,6 +2081,37 @@ MF_API mf_status mf_set_gauss_mesh(mf_ctx* c, int32_t body, uint32_t ex, uint32_
 		return fail(c, MF_ERR_ARG, "(ex+1)*(ey+1) must equal the body's particle count");
 	if (!(gp_h > 0.) || !(gp_rho > 0.)) return fail(c, MF_ERR_ARG, "Gauss-point h and rho must be positive");
 	b.ex = ex; b.ey = ey; b.gp_h = gp_h; b.gp_rho = gp_rho;
+	b.quads.clear(); b.order = 2; b.shape = MF_SHAPE_RKPM;
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_elements(mf_ctx* c, int32_t body, const uint32_t* quads, uint32_t n_elem, uint32_t order,
+                                 int32_t shape, double gp_h, double gp_rho) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "the elements must be set before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	HostBody& b = c->bodies[body];
+	if (!quads || n_elem == 0) return fail(c, MF_ERR_ARG, "null element map or n_elem == 0");
+	if (order != 1 && order != 2) return fail(c, MF_ERR_ARG, "Gauss orders 1 and 2 only");
+	if (shape != MF_SHAPE_RKPM && shape != MF_SHAPE_ELEMENT) return fail(c, MF_ERR_ARG, "bad shape kind %d", shape);
+	if ((uint64_t)n_elem * order * order > 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 Gauss points");
+	for (uint64_t k = 0; k < 4ull * n_elem; k++)
+		if (quads[k] >= b.n) return fail(c, MF_ERR_ARG, "element %llu names particle %u of %u", (unsigned long long)(k / 4), quads[k], b.n);
+	b.quads.assign(quads, quads + 4ull * n_elem);
+	b.ex = b.ey = 0;
+	b.order = order; b.shape = shape; b.gp_h = gp_h; b.gp_rho = gp_rho;
+	return MF_OK;
+}
+
+MF_API mf_status mf_set_gauss_points(mf_ctx* c, int32_t body, const double* x, const double* y, const double* h,
+                                     const double* rho, uint32_t n) {
+	if (!c) return MF_ERR_ARG;
+	if (c->ready) return fail(c, MF_ERR_STATE, "Gauss points must be set before the first step");
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	if (!x || !y || !h || !rho || n == 0) return fail(c, MF_ERR_ARG, "null Gauss-point field or n == 0");
+	HostBody& b = c->bodies[body];
+	const double* src[4] = {x, y, h, rho};
+	for (int k = 0; k < 4; k++) b.gpt[k].assign(src[k], src[k] + n);
 	return MF_OK;
 }
 

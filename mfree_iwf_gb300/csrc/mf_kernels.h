@@ -173,6 +173,7 @@ struct WeakArgs {
 	const BodyParams* params;
 	const uint32_t *body_of, *gp_body;
 	const double *X, *Y, *m, *qw_p, *gp_qw, *fcx, *fcy;
+	const double *gp_ux, *gp_uy;  // Gauss points' own displacement x - X
 	StateSoA base, acc, st;      // particles
 	StateSoA gbase, gacc, gst;   // Gauss points
 	// sliced-ELL lists: Gauss point -> particles (gradients), particle -> Gauss points
@@ -265,10 +266,11 @@ struct ContactArgs {
 	                           const double* Y, const double* m, const double* qw, void* sw, void* swA,      \
 	                           void* sX, void* sW, void* swji, cudaStream_t s);                              \
 	cudaError_t contact_step(const mfk_host::ContactArgs& a, cudaStream_t s);                                \
-	cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,  \
-	                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px,     \
-	                              const double* py, double* gx, double* gy, double* gqw, void* status,        \
-	                              cudaStream_t s);                                                            \
+	cudaError_t weak_gauss_points(uint32_t n_elem, const uint32_t* quads, uint32_t order, const double* px,    \
+	                              const double* py, double* gx, double* gy, double* gqw, double* fw,         \
+	                              double* fwx, double* fwy, void* status, cudaStream_t s);                    \
+	cudaError_t weak_gp_disp(uint32_t n, const double* gx, const double* gy, const double* gX, const double* gY, \
+	                         double* ux, double* uy, cudaStream_t s);                                           \
 	cudaError_t weak_rkpm(uint32_t n_to, const double* tx, const double* ty, const double* th,                \
 	                      const uint32_t* off, const uint32_t* nbr, const double* fx, const double* fy,       \
 	                      const double* fm, const double* frho, const float* frho_f, double* w, double* wx,    \

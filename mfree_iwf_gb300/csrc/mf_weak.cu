@@ -45,31 +45,34 @@ enum : uint32_t {
 };
 
 // ---------------------------------------------------------------- set-up
-// update_gauss_points for one element (node numbering of element_map_rectangle,
-// element.cpp:23-39); Gauss point g = 4 e + k in the order of get_weight_pos_2d.
-__global__ void k_gauss_points(uint32_t n_elem_total, const uint32_t* __restrict__ elem_body,
-                               const uint32_t* __restrict__ body_ex, const uint32_t* __restrict__ body_poff,
-                               const uint32_t* __restrict__ body_eoff, const double* __restrict__ px,
-                               const double* __restrict__ py, double* gx, double* gy, double* gqw, DevStatus* st) {
+// update_gauss_points (gauss_integration.h:47-123) for one element of an explicit map
+// (ll, lr, tr, tl rows): the Gauss points of the tensor rule of `order` (1 or 2;
+// gauss_integration.cpp:38-64), point g = order^2 e + k with k = i order + j in the
+// order of get_weight_pos_2d, their positions from the nodes' (x, y), the weights
+// J w, and, when fwx is given, the element's shape-function gradients (and, with fw,
+// the functions) per (point, node) in node order (gauss_integration.h:96-118).
+__global__ void k_gauss_quads(uint32_t n_elem, const uint32_t* __restrict__ quads, uint32_t order,
+                              const double* __restrict__ px, const double* __restrict__ py, double* gx, double* gy,
+                              double* gqw, double* fw, double* fwx, double* fwy, DevStatus* st) {
 	uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= n_elem_total) return;
-	uint32_t b = elem_body[e];
-	uint32_t el = e - body_eoff[b];
-	uint32_t ex = body_ex[b];
-	uint32_t row = el / ex, col = el - row * ex;
-	uint32_t nx = ex + 1;
-	uint32_t inc = row * nx + col;
-	uint32_t nidx[4] = {inc, inc + 1, inc + nx + 1, inc + nx};
+	if (e >= n_elem) return;
+	uint32_t nidx[4] = {quads[4 * e], quads[4 * e + 1], quads[4 * e + 2], quads[4 * e + 3]};
 	double mx[4], my[4];
 #pragma unroll
 	for (int I = 0; I < 4; I++) {
-		mx[I] = px[body_poff[b] + nidx[I]];
-		my[I] = py[body_poff[b] + nidx[I]];
+		mx[I] = px[nidx[I]];
+		my[I] = py[nidx[I]];
 	}
 	const double par_x[4] = {-1, +1, +1, -1}, par_y[4] = {-1, -1, +1, +1};
-	const double p1[2] = {0.577350269189626, -0.577350269189626};
-	for (int k = 0; k < 4; k++) {
-		double xi = p1[k >> 1], eta = p1[k & 1], local_w = 1.000000000000000 * 1.000000000000000;
+	const double p2[2] = {0.577350269189626, -0.577350269189626};
+	const uint32_t npe = order * order;
+	for (uint32_t k = 0; k < npe; k++) {
+		double xi, eta, local_w;
+		if (order == 1) {
+			xi = 0.; eta = 0.; local_w = 2. * 2.;
+		} else {
+			xi = p2[k / 2]; eta = p2[k % 2]; local_w = 1.000000000000000 * 1.000000000000000;
+		}
 		double N[4];
 		const double X1 = -1, Y1 = -1, X2 = 1, Y2 = -1, X3 = 1, Y3 = 1, X4 = -1, Y4 = 1;
 		N[0] = 0.25 * (1 + X1 * xi) * (1 + Y1 * eta);
@@ -94,12 +97,34 @@ __global__ void k_gauss_points(uint32_t n_elem_total, const uint32_t* __restrict
 		}
 		double J = -(a00 * a11 - a10 * a01);
 		double w = local_w * J;
-		uint32_t g = 4 * e + k;
+		uint32_t g = npe * e + k;
 		if (!(w > 0.)) raise(st, ERR_GRID, g);
 		gx[g] = gpx;
 		gy[g] = gpy;
 		gqw[g] = w;
+		if (fwx) {
+			// N_x = N_xi * inverse(x_xi): glm's 2x2 inverse (adjugate times 1/det), then
+			// the mat2x4 * mat2x2 product, k ascending
+			double inv_det = 1. / (a00 * a11 - a10 * a01);
+			double i00 = a11 * inv_det, i01 = -a01 * inv_det, i10 = -a10 * inv_det, i11 = a00 * inv_det;
+#pragma unroll
+			for (int I = 0; I < 4; I++) {
+				double nxi = 0.25 * par_x[I] * (1 + par_y[I] * eta);   // N_xi[0][I]
+				double neta = 0.25 * par_y[I] * (1 + par_x[I] * xi);  // N_xi[1][I]
+				if (fw) fw[4 * g + I] = N[I];
+				fwx[4 * g + I] = nxi * i00 + neta * i01;
+				fwy[4 * g + I] = nxi * i10 + neta * i11;
+			}
+		}
 	}
+}
+
+__global__ void k_gp_disp(uint32_t n, const double* gx, const double* gy, const double* gX, const double* gY, double* ux,
+                          double* uy) {
+	uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+	if (g >= n) return;
+	ux[g] = gx[g] - gX[g];
+	uy[g] = gy[g] - gY[g];
 }
 
 // compute_rkpm_correctors + compute_rkpm_shape_function (precomp_shape_functions.h:52-173)
@@ -233,6 +258,9 @@ __global__ void __launch_bounds__(256) k_gp_pass64(WeakArgs a) {
 	const mfk_host::StateSoA& s = a.st;
 	const double2* gw = (const double2*)a.g_w;
 	uint32_t flags = a.flags;
+	// the Gauss point's own displacement x - X (constant: the points do not move; zero
+	// unless the set-up moved its body after placing them)
+	const double uxi = a.gp_ux[i], uyi = a.gp_uy[i];
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0., Fxx = 0., Fxy = 0., Fyx = 0., Fyy = 0.;
 	uint32_t q = sbase(a.g_sl, i), c = a.g_cnt[i];
 	for (uint32_t k = 0; k < c; k++, q += 32) {
@@ -241,10 +269,10 @@ __global__ void __launch_bounds__(256) k_gp_pass64(WeakArgs a) {
 		double qwj = a.qw_p[j];
 		if (flags & A_DISP_W) {
 			double uxj = s.x[j] - a.X[j], uyj = s.y[j] - a.Y[j];
-			Hxx += (uxj - 0.) * w.x * qwj;
-			Hxy += (uxj - 0.) * w.y * qwj;
-			Hyx += (uyj - 0.) * w.x * qwj;
-			Hyy += (uyj - 0.) * w.y * qwj;
+			Hxx += (uxj - uxi) * w.x * qwj;
+			Hxy += (uxj - uxi) * w.y * qwj;
+			Hyx += (uyj - uyi) * w.x * qwj;
+			Hyy += (uyj - uyi) * w.y * qwj;
 		}
 		if (flags & A_VEL_W) {
 			double vxj = s.vx[j], vyj = s.vy[j];
@@ -343,6 +371,7 @@ __global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
 	const float2* gw = (const float2*)a.g_w;  // gradient times the particle's quad weight
 	const float4* pk = (const float4*)a.pack;
 	uint32_t flags = a.flags;
+	const FF uxi = ff_split(a.gp_ux[i]), uyi = ff_split(a.gp_uy[i]);
 	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f, Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
 	uint32_t q = sbase(a.g_sl, i), c = a.g_cnt[i];
 #pragma unroll 2
@@ -351,7 +380,7 @@ __global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
 		float2 w = gw[q];
 		if (flags & A_DISP_W) {
 			float4 u = __ldg(pk + 2 * j);
-			float ux = u.x + u.y, uy = u.z + u.w;
+			float ux = (u.x - uxi.hi) + (u.y - uxi.lo), uy = (u.z - uyi.hi) + (u.w - uyi.lo);
 			Hxx += ux * w.x;
 			Hxy += ux * w.y;
 			Hyx += uy * w.x;
@@ -479,11 +508,19 @@ __global__ void k_weak_time(uint32_t nb, BodyParams* P) {
 
 }  // namespace
 
-cudaError_t weak_gauss_points(uint32_t n_elem_total, const uint32_t* elem_body, const uint32_t* body_ex,
-                              const uint32_t* body_poff, const uint32_t* body_eoff, const double* px, const double* py,
-                              double* gx, double* gy, double* gqw, void* status, cudaStream_t s) {
-	k_gauss_points<<<grid1(n_elem_total, 128), 128, 0, s>>>(n_elem_total, elem_body, body_ex, body_poff, body_eoff, px,
-	                                                         py, gx, gy, gqw, reinterpret_cast<DevStatus*>(status));
+cudaError_t weak_gauss_points(uint32_t n_elem, const uint32_t* quads, uint32_t order, const double* px, const double* py,
+                              double* gx, double* gy, double* gqw, double* fw, double* fwx, double* fwy, void* status,
+                              cudaStream_t s) {
+	if (n_elem == 0) return cudaSuccess;
+	k_gauss_quads<<<grid1(n_elem, 128), 128, 0, s>>>(n_elem, quads, order, px, py, gx, gy, gqw, fw, fwx, fwy,
+	                                                   reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t weak_gp_disp(uint32_t n, const double* gx, const double* gy, const double* gX, const double* gY, double* ux,
+                         double* uy, cudaStream_t s) {
+	if (n == 0) return cudaSuccess;
+	k_gp_disp<<<grid1(n, 256), 256, 0, s>>>(n, gx, gy, gX, gY, ux, uy);
 	return cudaGetLastError();
 }
 

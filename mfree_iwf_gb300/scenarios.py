@@ -696,6 +696,131 @@ def rings_ul_weak_contact(nbox: int) -> Scenario:
     return _ul_weak_scenario(bodies, RINGS_UL_WEAK_ACTIONS, 1e-7, dx, f"rings_ul_weak_contact({nbox})", contact=1)
 
 
+def gauss_points(X: np.ndarray, Y: np.ndarray, el: np.ndarray, order: int = 2):
+    """update_gauss_points (gauss_integration.h:47-123) on the nodes' reference positions:
+    per element (rows of ``el``) the order x order points of the tensor rule
+    (get_weight_pos_2d, gauss_integration.cpp:144-157: abscissa i of xi, j of eta, point
+    i*order + j), placed by the bilinear functions (transpose(m_node) * N, summed over
+    the nodes in order) with weight w_i w_j J, J = -det(x_xi) accumulated node by node.
+    Returns the points' x, y and weights, element-major."""
+    p1, w1 = {1: ([0.0], [2.0]), 2: ([0.577350269189626, -0.577350269189626], [1.0, 1.0])}[order]
+    mx, my = X[el], Y[el]
+    par_x, par_y = (-1.0, 1.0, 1.0, -1.0), (-1.0, -1.0, 1.0, 1.0)
+    npe = order * order
+    gx = np.empty((len(el), npe))
+    gy = np.empty_like(gx)
+    qw = np.empty_like(gx)
+    for k in range(npe):
+        xi, eta, lw = p1[k // order], p1[k % order], w1[k // order] * w1[k % order]
+        N = [0.25 * (1 + par_x[I] * xi) * (1 + par_y[I] * eta) for I in range(4)]
+        gx[:, k] = mx[:, 0] * N[0] + mx[:, 1] * N[1] + mx[:, 2] * N[2] + mx[:, 3] * N[3]
+        gy[:, k] = my[:, 0] * N[0] + my[:, 1] * N[1] + my[:, 2] * N[2] + my[:, 3] * N[3]
+        a00 = a01 = a10 = a11 = 0.0
+        for I in range(4):
+            a00 = a00 + 0.25 * mx[:, I] * par_x[I] * (1 + par_y[I] * eta)
+            a10 = a10 + 0.25 * mx[:, I] * par_y[I] * (1 + par_x[I] * xi)
+            a01 = a01 + 0.25 * my[:, I] * par_x[I] * (1 + par_y[I] * eta)
+            a11 = a11 + 0.25 * my[:, I] * par_y[I] * (1 + par_x[I] * xi)
+        qw[:, k] = lw * -(a00 * a11 - a10 * a01)
+    return gx.ravel(), gy.ravel(), qw.ravel()
+
+
+def _tl_element_body(x, y, X, Y, el, *, dx, rho0, fem, hdx=1.0, vx=0.0, vy=0.0, gshift=0.0) -> Body:
+    """A weak TL body on an explicit element map with 2x2 Gauss points: fem nodes carry
+    unit quad weights and no density or h (the *_fem set-ups), RKPM particles
+    rho0, h = hdx dx and quad weight m / rho; the Gauss points take rho0 (and h = hdx dx
+    with RKPM) and sit where update_gauss_points put them, shifted by ``gshift``."""
+    a = _body_from_lists(x, y, X, Y)
+    a["m"][:] = dx * dx * rho0
+    if fem:
+        a["quad_weight"][:] = 1.0
+    else:
+        a["rho"][:] = rho0
+        a["h"][:] = hdx * dx
+        a["quad_weight"][:] = a["m"] / a["rho"]
+    a["vx"][:] = vx
+    a["vy"][:] = vy
+    GX, GY, qw = gauss_points(a["X"], a["Y"], el, 2)
+    g = _body_from_lists(GX + gshift if gshift else GX, GY, GX, GY)
+    g["rho"][:] = rho0
+    g["quad_weight"][:] = qw
+    if not fem:
+        g["h"][:] = hdx * dx
+    return Body(a, gp=g, quads=np.ascontiguousarray(el, np.uint32), order=2,
+                shape=SHAPE_ELEMENT if fem else SHAPE_RKPM)
+
+
+def _tl_element_scenario(bodies, dt, dx, fem, name, contact=0, hdx=1.0) -> Scenario:
+    # the *_fem set-ups take correction_constants() (all zero), the RKPM ones
+    # correction_constants(.., 0, true) (velocity smoothing) and neighbourhoods of hdx dx
+    sc = Scenario(method=METHOD_TL_WEAK, bodies=bodies, actions=list(TENSILE_TL_WEAK_ACTIONS), dt=dt, nu=0.4, E=1e7,
+                  rho0=1.0, do_smooth=0 if fem else 1, contact=contact, name=name)
+    sc.nbh_h = 0.0 if fem else hdx * dx
+    return sc
+
+
+def tensile_tl_fem(nbox: int) -> Scenario:
+    """The reference's tensile_tl_fem(nbox), tensile.cpp:539-624: the plate lattice as
+    bilinear elements (element_map_rectangle), 2x2 Gauss points, the pull conditions."""
+    dx = 1.0 / (nbox - 1)
+    I, J = np.meshgrid(np.arange(nbox, dtype=np.float64), np.arange(nbox, dtype=np.float64), indexing="ij")
+    x, y = (I * dx).ravel(), (J * dx).ravel()
+    b = _tl_element_body(x, y, x, y, element_map_rectangle(nbox - 1, nbox - 1), dx=dx, rho0=1.0, fem=True)
+    left = np.arange(nbox, dtype=np.uint32)
+    right = (np.uint32(nbox - 1) * np.uint32(nbox) + left).astype(np.uint32)
+    b.bcs = [BC(BC_PULL_TL, -10.0, left), BC(BC_PULL_TL, 10.0, right)]
+    return _tl_element_scenario([b], 1e-6, dx, True, f"tensile_tl_fem({nbox})")
+
+
+def _rotation_tl_element(nbox: int, fem: bool, name: str) -> Scenario:
+    ro = 1.0
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, 0.0, ro)
+    b = _tl_element_body(x, y, x, y, el, dx=dx, rho0=1.0, fem=fem, vx=-y / ro * 50, vy=+x / ro * 50)
+    return _tl_element_scenario([b], 1e-6, dx, fem, name)
+
+
+def rotation_tl_fem(nbox: int) -> Scenario:
+    """The reference's rotation_tl_fem(nbox), rotation.cpp:408-459: mesh_ring(nbox, 0, 1)
+    as bilinear elements with 2x2 Gauss points, spinning at 50 m/s rim speed."""
+    return _rotation_tl_element(nbox, True, f"rotation_tl_fem({nbox})")
+
+
+def rotation_tl_weak(nbox: int) -> Scenario:
+    """The reference's rotation_tl_weak(nbox), rotation.cpp:537-605: the same disc mesh
+    with RKPM on neighbourhoods of dx and velocity smoothing."""
+    return _rotation_tl_element(nbox, False, f"rotation_tl_weak({nbox})")
+
+
+def _rings_tl_element(nbox: int, fem: bool, name: str) -> Scenario:
+    ri, ro = 0.03, 0.04
+    spacing = ro + 0.001
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, ri, ro)
+    bodies = []
+    for sgn, v in ((-1.0, 180.0), (1.0, -180.0)):
+        xs = x - spacing if sgn < 0 else x + spacing
+        b = _tl_element_body(xs, y, x, y, el, dx=dx, rho0=1.0, fem=fem, vx=v, gshift=0.0 if fem else sgn * spacing)
+        b.hull = convex_hull(xs, y)
+        bodies.append(b)
+    return _tl_element_scenario(bodies, 1e-7, dx, fem, name, contact=1)
+
+
+def rings_tl_fem_contact(nbox: int) -> Scenario:
+    """The reference's rings_tl_fem_contact(nbox), rings.cpp:720-815: two meshed rings
+    (r 0.03-0.04 m) at +-(ro + 1 mm), 180 m/s each, bilinear elements with 2x2 Gauss
+    points, penalty contact on their hulls.  The particles' x is shifted, X and the
+    Gauss points are not (the set-up moves only the particles)."""
+    return _rings_tl_element(nbox, True, f"rings_tl_fem_contact({nbox})")
+
+
+def rings_tl_weak_contact(nbox: int) -> Scenario:
+    """The reference's rings_tl_weak_contact(nbox), rings.cpp:936-1051: the same rings
+    with RKPM on neighbourhoods of dx; particles and Gauss points both move with their
+    ring, their reference positions do not."""
+    return _rings_tl_element(nbox, False, f"rings_tl_weak_contact({nbox})")
+
+
 # ------------------------------------------------- workloads of the other families
 def family_rings(family: str, dx: float = 5e-5) -> Scenario:
     """The ring-impact workload (two bodies with penalty contact, the constants of

@@ -42,8 +42,10 @@ def errors(sc, a, b):
 # 10 mm gap); the TL rings at dx = 0.4 mm through 600 steps, well into contact.  The
 # TL contact set-up itself turns unstable near step 750 at dx = 0.4 mm -- the CPU
 # oracle of the reference's algorithm does the same -- so that case stops at 600.
+# The weak form on explicit element maps: the meshed rings with the elements' own
+# functions through contact, the meshed disc with RKPM.
 CASES = [("ul_rings_dx1mm", 1000), ("tl_rings_dx0.05mm", 1000), ("tl_rings_dx0.4mm_contact", 600),
-         ("weak_plate_dx0.2mm", 1000)]
+         ("weak_plate_dx0.2mm", 1000), ("weak_fem_rings_contact", 600), ("weak_rkpm_disc", 400)]
 
 
 @pytest.mark.parametrize("case,steps", CASES)
@@ -54,6 +56,10 @@ def test_mixed_error(case, steps, lib):
         sc = S.c2_rings_tl(dx=5e-5)
     elif case == "weak_plate_dx0.2mm":
         sc = S.c3_plate(dx=2e-4)
+    elif case == "weak_fem_rings_contact":
+        sc = S.rings_tl_fem_contact(81)
+    elif case == "weak_rkpm_disc":
+        sc = S.rotation_tl_weak(61)
     else:
         sc = S.c2_rings_tl(dx=4e-4)
     ref = run(sc, steps, "fp64")

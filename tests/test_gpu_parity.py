@@ -62,7 +62,8 @@ UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm", "rings
 # conditioning in test_gpu_families.py: their results move by 1e-6..1e-2 under 1-ulp
 # input noise
 TL_CASES = ["rings_tl_contact", "tensile_tl", "c2_rings_tl_dx4mm", "tensile_tl_weak", "rings_potential_contact",
-            "tensile_potential", "rotation_potential", "rotation_tl"]
+            "tensile_potential", "rotation_potential", "rotation_tl", "tensile_tl_fem", "rotation_tl_fem",
+            "rings_tl_fem_contact", "rotation_tl_weak", "rings_tl_weak_contact"]
 COROT_CASES = ["rings_corot_contact", "tensile_corot", "rotation_corot"]
 
 

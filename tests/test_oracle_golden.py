@@ -13,7 +13,8 @@ CASES = ["rings_monaghan", "rings_monaghan_contact", "rings_tl_contact", "tensil
          "c1_rings_dx4mm", "c2_rings_tl_dx4mm", "rings_corot_contact", "tensile_corot", "rotation_corot",
          "rings_godunov", "rings_godunov_contact", "rotation_godunov", "rings_potential_contact", "tensile_potential",
          "rotation_potential", "tensile_godunov", "tensile_monaghan", "rotation_monaghan", "rotation_tl",
-         "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact"]
+         "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact", "tensile_tl_fem", "rotation_tl_fem",
+         "rings_tl_fem_contact", "rotation_tl_weak", "rings_tl_weak_contact"]
 
 
 @pytest.mark.parametrize("name", CASES)

@@ -30,6 +30,11 @@ BUILDERS = {
     "tensile_ul_weak": lambda: S.tensile_ul_weak(11),
     "rotation_ul_weak": lambda: S.rotation_ul_weak(21),
     "rings_ul_weak_contact": lambda: S.rings_ul_weak_contact(20),
+    "tensile_tl_fem": lambda: S.tensile_tl_fem(11),
+    "rotation_tl_fem": lambda: S.rotation_tl_fem(15),
+    "rings_tl_fem_contact": lambda: S.rings_tl_fem_contact(20),
+    "rotation_tl_weak": lambda: S.rotation_tl_weak(15),
+    "rings_tl_weak_contact": lambda: S.rings_tl_weak_contact(20),
 }
 
 
@@ -52,6 +57,13 @@ def test_builder_matches_reference_setup(name):
             for k in S.IN_NAMES:
                 if k not in ("h", "vx", "vy"):
                     assert np.array_equal(b.gp[k].view(np.uint64), rb.gp[k].view(np.uint64)), ("gp", k)
+        if sc.method == S.METHOD_TL_WEAK and rb.quads is not None and len(rb.quads):
+            # explicit element map and the Gauss points as update_gauss_points (and the
+            # set-up's shift) left them, weights included
+            assert np.array_equal(np.asarray(b.quads).reshape(-1), np.asarray(rb.quads).reshape(-1))
+            assert (b.order, b.shape) == (rb.order, rb.shape)
+            for k in S.IN_NAMES:
+                assert np.array_equal(b.gp[k].view(np.uint64), rb.gp[k].view(np.uint64)), ("gp", k)
         assert len(b.bcs) == len(rb.bcs)
         for bc, rbc in zip(b.bcs, rb.bcs):
             assert bc.v == rbc.v and np.array_equal(bc.idx, rbc.idx)
