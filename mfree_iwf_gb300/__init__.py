@@ -444,5 +444,7 @@ def from_scenario(sc, precision="fp64_strict", device: int = 0, max_nbh: int = 2
             else:
                 sim.set_gauss_mesh(bid, b.ex, b.ey, sc.gp_h, sc.gp_rho)
         if sc.method == METHOD_UL_WEAK:
+            if b.quads is not None and len(b.quads):
+                sim.set_elements(bid, b.quads, b.order, SHAPE_ELEMENT, 0.0, 0.0)
             sim.set_stress_points(bid, b.gp)
     return sim

@@ -275,6 +275,8 @@ struct mf_ctx {
 	DevBuf<uint8_t> uw_pmask, uw_gmask;
 	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
 	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
+	DevBuf<uint32_t> uw_quads;  // element maps (global ll lr tr tl) when a gauss_int replaces the ellipse
+	uint32_t uw_order = 0, uw_nelem = 0;
 
 	// host <-> device state transfers: FP64 staging for the fields stored as FP32
 	DevBuf<double> staging;
@@ -1659,6 +1661,8 @@ mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t&
 		return fail(c, MF_ERR_PIPELINE, "contmech_continuity needs derive_velocity before it");
 	if ((flags & FLAG_UW_ADVECTION_GP) && !(flags & FLAG_UW_INTERP))
 		return fail(c, MF_ERR_PIPELINE, "contmech_advection_gp needs interpolation_interpolate_velocity before it");
+	if ((flags & abit(MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS)) && !c->bodies.empty() && !c->bodies[0].quads.empty())
+		return fail(c, MF_ERR_PIPELINE, "riemann_update_integration_weights runs with the ellipse (no element maps)");
 	return MF_OK;
 }
 
@@ -1666,12 +1670,22 @@ mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t&
 // (tensile.cpp:706-707), the transposed stress-point candidates, per-candidate scratch.
 mf_status uw_setup(mf_ctx* c) {
 	const uint32_t n = c->n_total;
-	if (!(c->cfg.nbh_h > 0.)) return fail(c, MF_ERR_ARG, "the weak UL form needs config.nbh_h > 0 (the candidate search h)");
+	// a gauss_int in place of the ellipse (body.h:91-99): every body on an element map
+	const bool fem = !c->bodies[0].quads.empty();
+	if (!fem && !(c->cfg.nbh_h > 0.))
+		return fail(c, MF_ERR_ARG, "the weak UL form needs config.nbh_h > 0 (the candidate search h)");
 	uint32_t ng = 0;
 	for (auto& b : c->bodies) {
 		if (b.n_sp == 0) return fail(c, MF_ERR_STATE, "a UL_WEAK body needs mf_set_stress_points");
+		if (b.quads.empty() == fem || (fem && b.order != c->bodies[0].order))
+			return fail(c, MF_ERR_PIPELINE, "UL_WEAK bodies take all the ellipse or all element maps of one order");
+		if (fem && (uint64_t)b.order * b.order * (b.quads.size() / 4) != b.n_sp)
+			return fail(c, MF_ERR_ARG, "a UL_WEAK element map of %zu elements needs %u stress points per element",
+			            b.quads.size() / 4, b.order * b.order);
 		ng += b.n_sp;
 	}
+	if (fem && c->bodies[0].sd.do_smooth)
+		return fail(c, MF_ERR_PIPELINE, "velocity smoothing needs the ellipse neighbourhoods (no element maps)");
 	c->n_g = ng;
 	c->do_smooth = c->bodies[0].sd.do_smooth != 0;
 	std::vector<uint32_t> gb(ng);
@@ -1703,22 +1717,52 @@ mf_status uw_setup(mf_ctx* c) {
 	CK(cudaMemcpy(c->uw_qwp.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
 	CK(c->uw_ph.alloc(n)); CK(c->uw_qws.alloc(n));
 	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
-	// candidate lists (CSR, ascending)
-	std::vector<uint32_t> pc, gc;
-	const double *px = c->sd[0][0].p, *py = c->sd[0][1].p;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->uw_pc_off,
-	                      c->uw_pc_nbr, pc, true)))
-		return st;
-	if ((st = build_lists(c, px, py, c->body_of.p, n, c->uw_g[0][0].p, c->uw_g[0][1].p, c->uw_gbody.p, ng,
-	                      c->cfg.max_nbh, c->uw_gc_off, c->uw_gc_nbr, gc, true)))
-		return st;
-	const uint64_t ep = c->uw_pc_nbr.n, eg = c->uw_gc_nbr.n;
+	std::vector<uint32_t> goff(ng + 1), gnbr;
+	uint64_t ep, eg;
+	if (fem) {
+		// the particles have no lists; a stress point's candidates are its element's
+		// nodes in node order (gauss_integration.h:110-116), all of them used; the
+		// particles' weights stay the input ones (no ellipse, no riemann update)
+		std::vector<uint32_t> quads;
+		for (auto& b : c->bodies) body_quads(b, quads);
+		c->uw_order = c->bodies[0].order;
+		c->uw_nelem = (uint32_t)(quads.size() / 4);
+		const uint32_t npe = c->uw_order * c->uw_order;
+		gnbr.resize(4 * (size_t)ng);
+		for (uint32_t g = 0; g < ng; g++)
+			for (int k = 0; k < 4; k++) gnbr[4 * (size_t)g + k] = quads[4 * (size_t)(g / npe) + k];
+		for (uint32_t g = 0; g <= ng; g++) goff[g] = 4 * g;
+		std::vector<uint32_t> zoff(n + 1, 0);
+		CK(c->uw_quads.alloc(quads.size()));
+		CK(cudaMemcpy(c->uw_quads.p, quads.data(), quads.size() * 4, cudaMemcpyHostToDevice));
+		CK(c->uw_pc_off.alloc(n + 1)); CK(c->uw_pc_nbr.alloc(0));
+		CK(cudaMemcpy(c->uw_pc_off.p, zoff.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+		CK(c->uw_gc_off.alloc(ng + 1)); CK(c->uw_gc_nbr.alloc(gnbr.size()));
+		CK(cudaMemcpy(c->uw_gc_off.p, goff.data(), ((size_t)ng + 1) * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_gc_nbr.p, gnbr.data(), gnbr.size() * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_qws.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
+		ep = 0;
+		eg = gnbr.size();
+	} else {
+		// candidate lists (CSR, ascending)
+		std::vector<uint32_t> pc, gc;
+		const double *px = c->sd[0][0].p, *py = c->sd[0][1].p;
+		if ((st = build_lists(c, px, py, c->body_of.p, n, px, py, c->body_of.p, n, c->cfg.max_nbh, c->uw_pc_off,
+		                      c->uw_pc_nbr, pc, true)))
+			return st;
+		if ((st = build_lists(c, px, py, c->body_of.p, n, c->uw_g[0][0].p, c->uw_g[0][1].p, c->uw_gbody.p, ng,
+		                      c->cfg.max_nbh, c->uw_gc_off, c->uw_gc_nbr, gc, true)))
+			return st;
+		ep = c->uw_pc_nbr.n;
+		eg = c->uw_gc_nbr.n;
+		gnbr.resize(eg);
+		CK(cudaMemcpy(goff.data(), c->uw_gc_off.p, ((size_t)ng + 1) * 4, cudaMemcpyDeviceToHost));
+		if (eg) CK(cudaMemcpy(gnbr.data(), c->uw_gc_nbr.p, eg * 4, cudaMemcpyDeviceToHost));
+	}
 	CK(c->uw_pmask.alloc(ep)); CK(c->uw_pw.alloc(ep)); CK(c->uw_pwx.alloc(ep)); CK(c->uw_pwy.alloc(ep));
 	CK(c->uw_gmask.alloc(eg)); CK(c->uw_gw.alloc(eg)); CK(c->uw_gwx.alloc(eg)); CK(c->uw_gwy.alloc(eg));
+	if (fem) CK(cudaMemset(c->uw_gmask.p, 1, eg));
 	// per particle, the stress points whose candidates hold it (ascending) and the slot
-	std::vector<uint32_t> goff(ng + 1), gnbr(eg);
-	CK(cudaMemcpy(goff.data(), c->uw_gc_off.p, ((size_t)ng + 1) * 4, cudaMemcpyDeviceToHost));
-	if (eg) CK(cudaMemcpy(gnbr.data(), c->uw_gc_nbr.p, eg * 4, cudaMemcpyDeviceToHost));
 	std::vector<uint32_t> toff(n + 1, 0), tgp(eg), tslot(eg);
 	for (uint64_t q = 0; q < eg; q++) toff[gnbr[q] + 1]++;
 	for (uint32_t j = 0; j < n; j++) toff[j + 1] += toff[j];
@@ -1810,7 +1854,20 @@ mf_status uw_step(mf_ctx* c) {
 	};
 	for (uint32_t st = 0; st < 4; st++) {
 		UWArgs a = uw_args(c, st);
-		if ((e = uw_neighbourhoods(c, a, true, false)) != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+		if (c->uw_order) {
+			// update_gauss_points on this stage's nodes (body.h:97): weights J w and the
+			// element functions into the stress points' candidate slots
+			e = c->strict ? mf_strict::weak_gauss_points(c->uw_nelem, c->uw_quads.p, c->uw_order, a.rd.x, a.rd.y, nullptr,
+			                                             nullptr, c->uw_gqw.p, c->uw_gw.p, c->uw_gwx.p, c->uw_gwy.p,
+			                                             c->d_status, c->stream)
+			              : mf_fast::weak_gauss_points(c->uw_nelem, c->uw_quads.p, c->uw_order, a.rd.x, a.rd.y, nullptr,
+			                                           nullptr, c->uw_gqw.p, c->uw_gw.p, c->uw_gwx.p, c->uw_gwy.p,
+			                                           c->d_status, c->stream);
+			if (e != cudaSuccess) return cuda_fail(c, e, "weak UL Gauss points");
+			c->launches++;
+		} else if ((e = uw_neighbourhoods(c, a, true, false)) != cudaSuccess) {
+			return cuda_fail(c, e, "weak UL neighbourhoods");
+		}
 		int slot;
 		timing_begin(c, 5, slot);
 		if ((e = launch(a, 0)) != cudaSuccess) return cuda_fail(c, e, "weak UL stress-point pass");
@@ -1943,7 +2000,20 @@ mf_ctx::~mf_ctx() {
 		g_w64.free(); t_w64.free(); p_w64.free(); g_w32.free(); t_w32.free(); p_w32.free();
 	}
 	sl_off.free(); snbr.free(); scnt.free(); sw64.free(); sw32.free(); swA32.free(); recA.free(); recB.free(); dA32.free();
-	recB2.free(); sW64.free(); R64.free();
+	recB2.free(); sW64.free(); R64.free(); av64.free();
+	cm_sw.free(); cm_swA.free(); cm_sX.free(); cm_swji.free(); cm_sW.free();
+	cm_U.free(); cm_X.free(); cm_V.free(); cm_P.free(); cm_R.free(); cm_H.free();
+	{
+		DevBuf<uint32_t>* uws[] = {&uw_gbody, &uw_pc_off, &uw_pc_nbr, &uw_gc_off, &uw_gc_nbr, &uw_tp_off, &uw_tp_gp,
+		                           &uw_tp_slot, &uw_bc_of, &uw_quads};
+		for (auto* p : uws) p->free();
+		uw_pmask.free(); uw_gmask.free();
+		DevBuf<double>* uwd[] = {&uw_pw, &uw_pwx, &uw_pwy, &uw_gw, &uw_gwx, &uw_gwy, &uw_gsig, &uw_ph, &uw_gh, &uw_qwp,
+		                         &uw_qws, &uw_gm, &uw_gqw};
+		for (auto* p : uwd) p->free();
+		for (int k = 0; k < 4; k++)
+			for (int q = 0; q < 6; q++) uw_g[k][q].free();
+	}
 	tt_rows.free(); tt_halo_off.free(); tt_halo.free(); tt_sl.free(); tt_cnt.free(); tt_loc.free(); tt_sw.free();
 	tt_swA.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
@@ -2094,6 +2164,10 @@ MF_API mf_status mf_set_elements(mf_ctx* c, int32_t body, const uint32_t* quads,
 	if (!quads || n_elem == 0) return fail(c, MF_ERR_ARG, "null element map or n_elem == 0");
 	if (order != 1 && order != 2) return fail(c, MF_ERR_ARG, "Gauss orders 1 and 2 only");
 	if (shape != MF_SHAPE_RKPM && shape != MF_SHAPE_ELEMENT) return fail(c, MF_ERR_ARG, "bad shape kind %d", shape);
+	if (c->cfg.method != MF_METHOD_TL_WEAK && c->cfg.method != MF_METHOD_UL_WEAK)
+		return fail(c, MF_ERR_ARG, "element maps belong to the weak forms");
+	if (c->cfg.method == MF_METHOD_UL_WEAK && shape != MF_SHAPE_ELEMENT)
+		return fail(c, MF_ERR_ARG, "a UL_WEAK element map takes MF_SHAPE_ELEMENT (RKPM there is the ellipse's)");
 	if ((uint64_t)n_elem * order * order > 0x7fffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^31 Gauss points");
 	for (uint64_t k = 0; k < 4ull * n_elem; k++)
 		if (quads[k] >= b.n) return fail(c, MF_ERR_ARG, "element %llu names particle %u of %u", (unsigned long long)(k / 4), quads[k], b.n);
@@ -2515,10 +2589,12 @@ MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uin
 		if (st != MF_OK && st != MF_ERR_NBH_OVERFLOW) return st;
 	} else if (c->cfg.method == MF_METHOD_UL_WEAK) {
 		// the ellipse neighbourhoods of the particles' current state: those of the next
-		// step's first derivative evaluation
-		UWArgs a = uw_args(c, 0);
-		cudaError_t e = uw_neighbourhoods(c, a, false, false);
-		if (e != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+		// step's first derivative evaluation (on element maps the particles have none)
+		if (!c->uw_order) {
+			UWArgs a = uw_args(c, 0);
+			cudaError_t e = uw_neighbourhoods(c, a, false, false);
+			if (e != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+		}
 		CK(cudaStreamSynchronize(c->stream));
 		uint64_t ec = c->uw_pc_nbr.n;
 		std::vector<uint32_t> off(n + 1), cand(ec);

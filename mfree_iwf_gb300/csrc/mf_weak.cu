@@ -44,13 +44,16 @@ enum : uint32_t {
 	A_MOMENTUM_W = 1u << 27,
 };
 
-// ---------------------------------------------------------------- set-up
+// ---------------------------------------------------------------- Gauss points
 // update_gauss_points (gauss_integration.h:47-123) for one element of an explicit map
 // (ll, lr, tr, tl rows): the Gauss points of the tensor rule of `order` (1 or 2;
 // gauss_integration.cpp:38-64), point g = order^2 e + k with k = i order + j in the
-// order of get_weight_pos_2d, their positions from the nodes' (x, y), the weights
-// J w, and, when fwx is given, the element's shape-function gradients (and, with fw,
-// the functions) per (point, node) in node order (gauss_integration.h:96-118).
+// order of get_weight_pos_2d, placed by the nodes' (px, py): their positions (when gx
+// is given), the weights J w, and, when fwx is given, the element's shape-function
+// gradients (and, with fw, the functions) per (point, node) in node order
+// (gauss_integration.h:96-118).  The weak TL set-up runs it once on the reference
+// positions; the weak UL form with element maps at every derivative evaluation on the
+// stage's positions (body.h:97).
 __global__ void k_gauss_quads(uint32_t n_elem, const uint32_t* __restrict__ quads, uint32_t order,
                               const double* __restrict__ px, const double* __restrict__ py, double* gx, double* gy,
                               double* gqw, double* fw, double* fwx, double* fwy, DevStatus* st) {
@@ -99,8 +102,10 @@ __global__ void k_gauss_quads(uint32_t n_elem, const uint32_t* __restrict__ quad
 		double w = local_w * J;
 		uint32_t g = npe * e + k;
 		if (!(w > 0.)) raise(st, ERR_GRID, g);
-		gx[g] = gpx;
-		gy[g] = gpy;
+		if (gx) {
+			gx[g] = gpx;
+			gy[g] = gpy;
+		}
 		gqw[g] = w;
 		if (fwx) {
 			// N_x = N_xi * inverse(x_xi): glm's 2x2 inverse (adjugate times 1/det), then

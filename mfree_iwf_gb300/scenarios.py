@@ -19,6 +19,7 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 
 from .actions import (
+    UL_FEM_ACTIONS,
     RINGS_UL_WEAK_ACTIONS,
     TENSILE_UL_WEAK_ACTIONS,
     RINGS_COROT_ACTIONS,
@@ -821,6 +822,71 @@ def rings_tl_weak_contact(nbox: int) -> Scenario:
     return _rings_tl_element(nbox, False, f"rings_tl_weak_contact({nbox})")
 
 
+def _ul_element_body(x, y, X, Y, el, *, dx, rho0, vx=0.0, vy=0.0) -> Body:
+    """A weak UL body on an explicit element map (the *_ul_fem set-ups): nodes with
+    unit quad weights and no density or h, 2x2 stress points of density rho0.  The
+    stress points are recorded as the first update_gauss_points of the step loop leaves
+    them: placed on the nodes' current positions (it places them again at every
+    derivative evaluation, so their set-up positions are no input)."""
+    a = _body_from_lists(x, y, X, Y)
+    a["m"][:] = dx * dx * rho0
+    a["quad_weight"][:] = 1.0
+    a["vx"][:] = vx
+    a["vy"][:] = vy
+    gx, gy, qw = gauss_points(a["x"], a["y"], el, 2)
+    g = _body_from_lists(gx, gy, gx, gy)
+    g["rho"][:] = rho0
+    g["quad_weight"][:] = qw
+    return Body(a, ex=1, gp=g, quads=np.ascontiguousarray(el, np.uint32), order=2, shape=SHAPE_ELEMENT)
+
+
+def _ul_element_scenario(bodies, dt, name, contact=0) -> Scenario:
+    # correction_constants() (all zero); no neighbour search
+    return Scenario(method=METHOD_UL_WEAK, bodies=bodies, actions=list(UL_FEM_ACTIONS), dt=dt, nu=0.4, E=1e7, rho0=1.0,
+                    contact=contact, name=name)
+
+
+def tensile_ul_fem(nbox: int) -> Scenario:
+    """The reference's tensile_ul_fem(nbox), tensile.cpp:452-537: the plate lattice as
+    bilinear elements, the velocity conditions on the end columns, its hull set."""
+    dx = 1.0 / (nbox - 1)
+    I, J = np.meshgrid(np.arange(nbox, dtype=np.float64), np.arange(nbox, dtype=np.float64), indexing="ij")
+    x, y = (I * dx).ravel(), (J * dx).ravel()
+    b = _ul_element_body(x, y, x, y, element_map_rectangle(nbox - 1, nbox - 1), dx=dx, rho0=1.0)
+    left = np.arange(nbox, dtype=np.uint32)
+    right = (np.uint32(nbox - 1) * np.uint32(nbox) + left).astype(np.uint32)
+    b.bcs = [BC(BC_VELOCITY_UL, -10.0, left), BC(BC_VELOCITY_UL, 10.0, right)]
+    b.hull = convex_hull(x, y)
+    return _ul_element_scenario([b], 1e-6, f"tensile_ul_fem({nbox})")
+
+
+def rotation_ul_fem(nbox: int) -> Scenario:
+    """The reference's rotation_ul_fem(nbox), rotation.cpp:353-405: mesh_ring(nbox, 0, 1)
+    as bilinear elements, spinning at 50 m/s rim speed, dt 1e-5."""
+    ro = 1.0
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, 0.0, ro)
+    b = _ul_element_body(x, y, x, y, el, dx=dx, rho0=1.0, vx=-y / ro * 50, vy=+x / ro * 50)
+    return _ul_element_scenario([b], 1e-5, f"rotation_ul_fem({nbox})")
+
+
+def rings_ul_fem_contact(nbox: int) -> Scenario:
+    """The reference's rings_ul_fem_contact(nbox), rings.cpp:623-718: two meshed rings
+    (r 0.03-0.04 m) at +-(ro + 1 mm), 180 m/s each, bilinear elements, penalty contact
+    on their hulls; X keeps the unshifted positions."""
+    ri, ro = 0.03, 0.04
+    spacing = ro + 0.001
+    dx = 2 * ro / (nbox - 1)
+    x, y, el = mesh_ring(nbox, ri, ro)
+    bodies = []
+    for sgn, v in ((-1.0, 180.0), (1.0, -180.0)):
+        xs = x - spacing if sgn < 0 else x + spacing
+        b = _ul_element_body(xs, y, x, y, el, dx=dx, rho0=1.0, vx=v)
+        b.hull = convex_hull(xs, y)
+        bodies.append(b)
+    return _ul_element_scenario(bodies, 1e-7, f"rings_ul_fem_contact({nbox})", contact=1)
+
+
 # ------------------------------------------------- workloads of the other families
 def family_rings(family: str, dx: float = 5e-5) -> Scenario:
     """The ring-impact workload (two bodies with penalty contact, the constants of
@@ -921,7 +987,9 @@ def write_case(path: str, sc: Scenario, nsteps: int, dump_every: int = 0) -> Non
             u32(bc.kind); f64(bc.v); u32(len(bc.idx))
             out.extend(np.ascontiguousarray(bc.idx, np.uint32).tobytes())
         u32(b.ex); u32(b.ey)
-        explicit = sc.method == METHOD_TL_WEAK and b.ex == 0
+        # an element map follows for TL_WEAK bodies without a rectangle and for UL_WEAK
+        # bodies with ex = 1 (a gauss_int in place of the ellipse)
+        explicit = (sc.method == METHOD_TL_WEAK and b.ex == 0) or (sc.method == METHOD_UL_WEAK and b.ex == 1)
         if explicit:
             q = np.ascontiguousarray(b.quads, np.uint32).reshape(-1, 4)
             u32(len(q)); u32(b.order); u32(b.shape)
@@ -976,7 +1044,7 @@ def read_case(path: str) -> Scenario:
             bcs.append(BC(kind, v, idx))
         ex, ey = u32(), u32()
         body = Body(a, hull, bcs, ex, ey)
-        explicit = method == METHOD_TL_WEAK and ex == 0
+        explicit = (method == METHOD_TL_WEAK and ex == 0) or (method == METHOD_UL_WEAK and ex == 1)
         if explicit:
             ne = u32()
             body.order, body.shape = u32(), u32()

@@ -169,7 +169,9 @@ inline Case read_case(const char* path) {
 			r.vu32(bc.idx, k);
 		}
 		b.ex = r.u32(); b.ey = r.u32();
-		if (c.method == TL_WEAK && b.ex == 0) {
+		// an explicit element map: TL_WEAK bodies without a rectangle, UL_WEAK bodies
+		// with ex = 1 (a gauss_int in place of the ellipse, the *_ul_fem set-ups)
+		if ((c.method == TL_WEAK && b.ex == 0) || (c.method == UL_WEAK && b.ex == 1)) {
 			uint32_t ne = r.u32();
 			b.order = r.u32();
 			b.shape = r.u32();

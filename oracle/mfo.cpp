@@ -1257,10 +1257,17 @@ void update_normals(std::vector<KdPoint>& b) {
 }
 
 // --------------------------------------------------------------------- bodies
+// element (element.h): the ll, lr, tr, tl node indices of a bilinear quadrilateral
+struct Elem {
+	unsigned ll, lr, tr, tl;
+};
+
 struct Body {
 	unsigned n = 0;
 	PSet P, k[4];
-	PSet Q, kq[4];  // Gauss points (TL_WEAK)
+	PSet Q, kq[4];  // Gauss points (TL_WEAK) / stress points (UL_WEAK)
+	std::vector<Elem> elems;  // UL_WEAK with a gauss_int (the *_ul_fem set-ups), else empty
+	unsigned gorder = 0;
 	std::vector<unsigned> perm[4];
 	std::vector<unsigned> hull;
 	std::vector<KdPoint> bnd;
@@ -1291,6 +1298,9 @@ void carry_out_bc(const Body& B, PSet& P, double t) {
 		}
 	}
 }
+
+void update_gauss_points(PSet& Q, const std::vector<double>& nx, const std::vector<double>& ny,
+                         const std::vector<Elem>& elems, unsigned order);
 
 struct Sim {
 	Case c;
@@ -1331,10 +1341,14 @@ struct Sim {
 			// actions, then the boundary conditions
 			PSet& Q = B.kq[s];
 			for (unsigned i = 0; i < Q.n; i++) Q.reset(i);
-			nbh_ellipse(P, P);
-			nbh_ellipse(Q, P);
-			precomp_rkpm(Q, P);
-			precomp_rkpm(P, P);
+			if (B.gorder) {
+				update_gauss_points(Q, P.x, P.y, B.elems, B.gorder);
+			} else {
+				nbh_ellipse(P, P);
+				nbh_ellipse(Q, P);
+				precomp_rkpm(Q, P);
+				precomp_rkpm(P, P);
+			}
 			if (!recorded && s == 0) record_nbh(P, perm, b);
 			for (uint32_t a : c.actions) action_fn(a)(ctx, P, perm, &Q);
 			carry_out_bc(B, P, ctx.time);
@@ -1525,8 +1539,16 @@ struct Sim {
 				std::vector<double>* gd[NIN] = {&B.Q.x, &B.Q.y, &B.Q.X, &B.Q.Y, &B.Q.m, &B.Q.rho, &B.Q.h, &B.Q.qw,
 				                                &B.Q.vx, &B.Q.vy, &B.Q.Sxx, &B.Q.Sxy, &B.Q.Syy};
 				for (int a = 0; a < NIN; a++) *gd[a] = in.g[a];
-				find_candidates(B.P, B.P, c.nbh_h);
-				find_candidates(B.Q, B.P, c.nbh_h);
+				if (in.ex == 1) {
+					// a gauss_int replaces the ellipse (body.h:91-99): no candidates
+					for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
+						B.elems.push_back(Elem{in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]});
+					B.gorder = in.order;
+					if ((size_t)B.gorder * B.gorder * B.elems.size() != in.ngp) throw Fail{"element map and stress points differ"};
+				} else {
+					find_candidates(B.P, B.P, c.nbh_h);
+					find_candidates(B.Q, B.P, c.nbh_h);
+				}
 			}
 		}
 		if (c.method != UL && c.method != UL_WEAK) recorded = true;
@@ -1537,9 +1559,6 @@ struct Sim {
 };
 
 // element_map_rectangle, element.cpp:23-39
-struct Elem {
-	unsigned ll, lr, tr, tl;
-};
 std::vector<Elem> element_map_rectangle(unsigned ex, unsigned ey) {
 	std::vector<Elem> map;
 	unsigned nx = ex + 1;
@@ -1557,22 +1576,11 @@ std::vector<Elem> element_map_rectangle(unsigned ex, unsigned ey) {
 
 // gauss_int::update_gauss_points (gauss_integration.h:47-123): per element the Gauss
 // points of the tensor rule of `order` (gauss_integration.cpp:20-34 shape functions,
-// :38-64 abscissae, :127-141 tensor rule), their weights J w and the elements' own
-// shape functions.  The element geometry is the particles' reference position X: the
-// set-ups call it before they move any body.  With an explicit element map the Gauss
-// points' x, y, h and rho come from the case (as the set-up left them, e.g. shifted
-// with their body); otherwise x = X, h = gp_h, rho = gp_rho.  SHAPE_RKPM then replaces
-// the element functions by neighbour search + RKPM (tensile.cpp:797-801, rings.cpp:1015-1025);
-// SHAPE_ELEMENT keeps them (the *_fem set-ups) and gives the particles no lists.
-void Sim::setup_weak(Body& B, const BodyIn& in) {
-	std::vector<Elem> elems;
-	if (in.ex) {
-		elems = element_map_rectangle(in.ex, in.ey);
-	} else {
-		for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
-			elems.push_back(Elem{in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]});
-	}
-	const unsigned order = in.ex ? 2 : in.order;
+// :38-64 abscissae, :127-141 tensor rule) placed by the nodes' positions (nx, ny):
+// the points' x = X, their weights J w, and as their neighbours the element's nodes in
+// node order with the element's shape functions and gradients.
+void update_gauss_points(PSet& Q, const std::vector<double>& nx, const std::vector<double>& ny,
+                         const std::vector<Elem>& elems, unsigned order) {
 	double p1[2], w1[2];
 	if (order == 1) { p1[0] = 0.; w1[0] = 2.; }
 	else if (order == 2) { p1[0] = 0.577350269189626; p1[1] = -0.577350269189626; w1[0] = w1[1] = 1.000000000000000; }
@@ -1581,15 +1589,11 @@ void Sim::setup_weak(Body& B, const BodyIn& in) {
 	double lx[4], ly[4], lw[4];
 	for (unsigned i = 0, k = 0; i < order; i++)
 		for (unsigned j = 0; j < order; j++, k++) { lx[k] = p1[i]; ly[k] = p1[j]; lw[k] = w1[i] * w1[j]; }
-	unsigned ngp = npe * (unsigned)elems.size();
-	B.Q.resize(ngp);
-	for (int s = 0; s < 4; s++) B.kq[s].resize(ngp);
-	PSet& Q = B.Q;
 	unsigned g = 0;
 	for (const Elem& e : elems) {
 		unsigned node_idx[4] = {e.ll, e.lr, e.tr, e.tl};
 		glm::dmat2x4 m_node, m_node_par;
-		for (int I = 0; I < 4; I++) { m_node[0][I] = B.P.X[node_idx[I]]; m_node[1][I] = B.P.Y[node_idx[I]]; }
+		for (int I = 0; I < 4; I++) { m_node[0][I] = nx[node_idx[I]]; m_node[1][I] = ny[node_idx[I]]; }
 		m_node_par[0][0] = -1; m_node_par[1][0] = -1;
 		m_node_par[0][1] = +1; m_node_par[1][1] = -1;
 		m_node_par[0][2] = +1; m_node_par[1][2] = +1;
@@ -1635,6 +1639,29 @@ void Sim::setup_weak(Body& B, const BodyIn& in) {
 			g++;
 		}
 	}
+}
+
+// Weak TL set-up: update_gauss_points on the element map, their weights J w and the
+// elements' own shape functions.  The element geometry is the particles' reference position X: the
+// set-ups call it before they move any body.  With an explicit element map the Gauss
+// points' x, y, h and rho come from the case (as the set-up left them, e.g. shifted
+// with their body); otherwise x = X, h = gp_h, rho = gp_rho.  SHAPE_RKPM then replaces
+// the element functions by neighbour search + RKPM (tensile.cpp:797-801, rings.cpp:1015-1025);
+// SHAPE_ELEMENT keeps them (the *_fem set-ups) and gives the particles no lists.
+void Sim::setup_weak(Body& B, const BodyIn& in) {
+	std::vector<Elem> elems;
+	if (in.ex) {
+		elems = element_map_rectangle(in.ex, in.ey);
+	} else {
+		for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
+			elems.push_back(Elem{in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]});
+	}
+	const unsigned order = in.ex ? 2 : in.order;
+	unsigned ngp = order * order * (unsigned)elems.size();
+	B.Q.resize(ngp);
+	for (int s = 0; s < 4; s++) B.kq[s].resize(ngp);
+	PSet& Q = B.Q;
+	update_gauss_points(Q, B.P.X, B.P.Y, elems, order);
 	const bool given = !in.ex && in.ngp == ngp;
 	for (unsigned i = 0; i < ngp; i++) {
 		Q.h[i] = given ? in.g[6][i] : c.gp_h;

@@ -474,6 +474,15 @@ int run_case(const Case& c, const char* out) {
 			gin.n = in.ngp;
 			for (int k = 0; k < NIN; k++) gin.a[k] = in.g[k];
 			T** q = make_particles<T>(gin);
+			if (in.ex == 1) {
+				// a gauss_int in place of the ellipse (body.h:91-99, the *_ul_fem set-ups)
+				std::vector<element> elements;
+				for (size_t e = 0; e + 3 < in.quads.size(); e += 4)
+					elements.push_back(element(in.quads[e], in.quads[e + 1], in.quads[e + 2], in.quads[e + 3]));
+				gauss_int* gi = new gauss_int(elements, in.order);
+				bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot), q, in.ngp, gi));
+				continue;
+			}
 			find_neighbors(p, in.n, c.nbh_h, distance_manhattan);
 			find_neighbors(p, in.n, q, in.ngp, c.nbh_h, distance_manhattan);
 			bodies.push_back(body<T>(p, in.n, sd, c.dt, make_bcs<T>(in, slot), q, in.ngp));
@@ -565,7 +574,7 @@ void write_case(const char* path, const Case& c) {
 			w.raw(bc.idx.data(), bc.idx.size() * 4);
 		}
 		w.u32(b.ex); w.u32(b.ey);
-		if (c.method == TL_WEAK && b.ex == 0) {
+		if ((c.method == TL_WEAK && b.ex == 0) || (c.method == UL_WEAK && b.ex == 1)) {
 			w.u32((uint32_t)(b.quads.size() / 4)); w.u32(b.order); w.u32(b.shape);
 			w.raw(b.quads.data(), b.quads.size() * 4);
 		}
@@ -830,6 +839,61 @@ int run_scenario(const std::string& name, unsigned nbox, unsigned nsteps, const 
 			}
 			c.bodies.push_back(in);
 			std::vector<void (*)(body<T>&)> acts;
+			bodies[b].add_action(&record_first_nbh<T>);
+			bodies[b].add_action(&capture_gp<T>);
+		}
+		c.nbodies = (uint32_t)bodies.size();
+		Writer w(out);
+		write_header(w, c);
+		run_loop(w, c, bodies);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			c.bodies[b].ngp = g_gp[b].n;
+			for (int k = 0; k < NIN; k++) c.bodies[b].g[k] = g_gp[b].a[k];
+		}
+		write_case(case_out, c);
+	} else if (name == "tensile_ul_fem" || name == "rotation_ul_fem" || name == "rings_ul_fem_contact") {
+		// weak UL bodies with a gauss_int: bilinear elements on the rectangle
+		// (tensile.cpp:452-537) or mesh_ring (rotation.cpp:353-405, rings.cpp:623-718),
+		// 2x2 Gauss points placed again on the current nodes at every evaluation
+		typedef particle_ul_weak T;
+		const bool rings = name == "rings_ul_fem_contact", disc = name == "rotation_ul_fem";
+		std::vector<body<T>> bodies = name == "tensile_ul_fem"   ? tensile_ul_fem(nbox)
+		                              : disc ? rotation_ul_fem(nbox) : rings_ul_fem_contact(nbox);
+		std::vector<element> elems;
+		if (rings || disc) {
+			unsigned nn = 0;
+			T** tmp = mesh_ring<T>(nbox, nn, elems, rings ? 0.03 : 0., rings ? 0.04 : 1.);
+			for (unsigned i = 0; i < nn; i++) delete tmp[i];
+			delete[] tmp;
+		} else {
+			elems = element_map_rectangle(nbox - 1, nbox - 1);
+		}
+		c.method = UL_WEAK;
+		c.contact = rings ? 1 : 0;
+		c.actions = {MATERIAL_EOS_GP, DERIVE_STRESS_WEAK_UL, DERIVE_VELOCITY_WEAK, MATERIAL_STRESS_RATE_JAUMANN_GP,
+		             CONTMECH_MOMENTUM_UL_WEAK, CONTMECH_CONTINUITY_GP, CONTMECH_ADVECTION};  // tensile.cpp:526-532
+		fill_consts(c, bodies[0].get_sim_data(), simulation_time::getInstance().get_dt());
+		c.nbh_h = 0.;
+		g_gp.assign(bodies.size(), BodyIn());
+		g_gp_done.assign(bodies.size(), false);
+		for (unsigned b = 0; b < bodies.size(); b++) {
+			BodyIn in = capture(bodies[b]);
+			in.ex = 1;
+			in.ey = 0;
+			in.order = 2;
+			in.shape = SHAPE_ELEMENT;
+			for (const element& e : elems) {
+				in.quads.push_back(e.ll_idx); in.quads.push_back(e.lr_idx);
+				in.quads.push_back(e.tr_idx); in.quads.push_back(e.tl_idx);
+			}
+			if (name == "tensile_ul_fem") {
+				BC l, r;  // tensile.cpp:507-509
+				l.kind = r.kind = BC_VELOCITY_UL;
+				l.v = -10.; r.v = 10.;
+				for (unsigned i = 0; i < nbox; i++) { l.idx.push_back(i); r.idx.push_back((nbox - 1) * nbox + i); }
+				in.bcs = {l, r};
+			}
+			c.bodies.push_back(in);
 			bodies[b].add_action(&record_first_nbh<T>);
 			bodies[b].add_action(&capture_gp<T>);
 		}

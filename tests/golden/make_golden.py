@@ -53,6 +53,9 @@ REFERENCE_CASES = [
     ("rotation_tl_weak", 15, 50),
     ("rings_tl_fem_contact", 20, 450),
     ("rings_tl_weak_contact", 20, 450),
+    ("tensile_ul_fem", 11, 25),
+    ("rotation_ul_fem", 15, 50),
+    ("rings_ul_fem_contact", 20, 450),
 ]
 
 

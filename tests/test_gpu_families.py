@@ -234,10 +234,13 @@ def test_ul_plate_velocity_conditions(lib, oracle_bin, precision):
 @pytest.mark.parametrize("build,steps", [
     (lambda: S.tensile_ul_weak(21), 60),
     (lambda: S.rings_ul_weak_contact(30), 500),
+    (lambda: S.tensile_ul_fem(41), 200),
+    (lambda: S.rings_ul_fem_contact(60), 600),
 ])
 def test_ul_weak_against_oracle(lib, oracle_bin, build, steps):
     """The weak UL form (ellipse neighbourhoods and RKPM per derivative evaluation,
-    stress points, smoothing) on larger lattices against the oracle, FP64 strict."""
+    stress points, smoothing; or the element functions placed again on the moving
+    nodes at every evaluation) on larger lattices against the oracle, FP64 strict."""
     import oracle
     sc = build()
     ref = oracle.run(sc, steps).dumps[-1]["bodies"]
@@ -261,4 +264,26 @@ def test_ul_weak_graph_and_pipeline_checks(lib):
     sc.actions = [x for x in sc.actions if x != M.DERIVE_STRESS_WEAK_UL]
     with pytest.raises(M.MfError) as e:
         run(sc, 1)
+    assert "MF_ERR_PIPELINE" in str(e.value)
+
+
+def test_ul_element_maps_graph_and_checks(lib):
+    """The weak UL form on element maps: graph replay equals eager; the particle weight
+    update and the velocity smoothing, which need the ellipse, are refused."""
+    import mfree_iwf_gb300 as M
+    sc = S.rotation_ul_fem(21)
+    a = run(sc, 20)
+    b = run(sc, 20, graph=True)
+    for ga, gb in zip(a, b):
+        for f in FIELDS:
+            assert np.array_equal(ga[f], gb[f]), f
+    bad = S.rotation_ul_fem(21)
+    bad.actions = [M.RIEMANN_UPDATE_INTEGRATION_WEIGHTS] + list(bad.actions)
+    with pytest.raises(M.MfError) as e:
+        run(bad, 1)
+    assert "MF_ERR_PIPELINE" in str(e.value)
+    bad = S.rotation_ul_fem(21)
+    bad.do_smooth = 1
+    with pytest.raises(M.MfError) as e:
+        run(bad, 1)
     assert "MF_ERR_PIPELINE" in str(e.value)

@@ -57,7 +57,8 @@ def golden(name):
 
 
 UL_CASES = ["rings_monaghan", "rings_monaghan_contact", "c1_rings_dx4mm", "rings_godunov", "rotation_godunov",
-            "tensile_monaghan", "rotation_monaghan", "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact"]
+            "tensile_monaghan", "rotation_monaghan", "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact",
+            "tensile_ul_fem", "rotation_ul_fem", "rings_ul_fem_contact"]
 # rings_godunov_contact and tensile_godunov are checked against the reference's own
 # conditioning in test_gpu_families.py: their results move by 1e-6..1e-2 under 1-ulp
 # input noise

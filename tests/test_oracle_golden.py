@@ -14,7 +14,8 @@ CASES = ["rings_monaghan", "rings_monaghan_contact", "rings_tl_contact", "tensil
          "rings_godunov", "rings_godunov_contact", "rotation_godunov", "rings_potential_contact", "tensile_potential",
          "rotation_potential", "tensile_godunov", "tensile_monaghan", "rotation_monaghan", "rotation_tl",
          "tensile_ul_weak", "rotation_ul_weak", "rings_ul_weak_contact", "tensile_tl_fem", "rotation_tl_fem",
-         "rings_tl_fem_contact", "rotation_tl_weak", "rings_tl_weak_contact"]
+         "rings_tl_fem_contact", "rotation_tl_weak", "rings_tl_weak_contact", "tensile_ul_fem", "rotation_ul_fem",
+         "rings_ul_fem_contact"]
 
 
 @pytest.mark.parametrize("name", CASES)

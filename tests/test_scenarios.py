@@ -35,6 +35,9 @@ BUILDERS = {
     "rings_tl_fem_contact": lambda: S.rings_tl_fem_contact(20),
     "rotation_tl_weak": lambda: S.rotation_tl_weak(15),
     "rings_tl_weak_contact": lambda: S.rings_tl_weak_contact(20),
+    "tensile_ul_fem": lambda: S.tensile_ul_fem(11),
+    "rotation_ul_fem": lambda: S.rotation_ul_fem(15),
+    "rings_ul_fem_contact": lambda: S.rings_ul_fem_contact(20),
 }
 
 
@@ -57,11 +60,11 @@ def test_builder_matches_reference_setup(name):
             for k in S.IN_NAMES:
                 if k not in ("h", "vx", "vy"):
                     assert np.array_equal(b.gp[k].view(np.uint64), rb.gp[k].view(np.uint64)), ("gp", k)
-        if sc.method == S.METHOD_TL_WEAK and rb.quads is not None and len(rb.quads):
+        if rb.quads is not None and len(rb.quads):
             # explicit element map and the Gauss points as update_gauss_points (and the
             # set-up's shift) left them, weights included
             assert np.array_equal(np.asarray(b.quads).reshape(-1), np.asarray(rb.quads).reshape(-1))
-            assert (b.order, b.shape) == (rb.order, rb.shape)
+            assert (b.ex, b.order, b.shape) == (rb.ex, rb.order, rb.shape)
             for k in S.IN_NAMES:
                 assert np.array_equal(b.gp[k].view(np.uint64), rb.gp[k].view(np.uint64)), ("gp", k)
         assert len(b.bcs) == len(rb.bcs)
