@@ -113,6 +113,23 @@ public:
 	void set_gauss_mesh(uint32_t ex, uint32_t ey, double gp_h, double gp_rho) {
 		check(mf_set_gauss_mesh(ctx_, id_, ex, ey, gp_h, gp_rho), ctx_, "mf_set_gauss_mesh");
 	}
+	// weak bodies on an explicit element map (gauss_int(elements, order)): quads holds
+	// ll, lr, tr, tl per element; MF_SHAPE_ELEMENT for the *_fem set-ups
+	void set_elements(const std::vector<uint32_t>& quads, uint32_t order, int32_t shape, double gp_h = 0.,
+	                  double gp_rho = 0.) {
+		check(mf_set_elements(ctx_, id_, quads.data(), (uint32_t)(quads.size() / 4), order, shape, gp_h, gp_rho), ctx_,
+		      "mf_set_elements");
+	}
+	// particle_ul_weak: the stress points (the particles' 13 fields)
+	void set_stress_points(const mf_particles& sp, uint32_t n) {
+		check(mf_set_stress_points(ctx_, id_, &sp, n), ctx_, "mf_set_stress_points");
+	}
+	// particle_tl_weak: the Gauss points' position, h and rho as the set-up left them
+	void set_gauss_points(const std::vector<double>& x, const std::vector<double>& y, const std::vector<double>& h,
+	                      const std::vector<double>& rho) {
+		check(mf_set_gauss_points(ctx_, id_, x.data(), y.data(), h.data(), rho.data(), (uint32_t)x.size()), ctx_,
+		      "mf_set_gauss_points");
+	}
 	uint32_t get_num_part() const {
 		uint32_t n = 0;
 		check(mf_num_particles(ctx_, id_, &n), ctx_, "mf_num_particles");

@@ -33,7 +33,19 @@ int main(int argc, char** argv) {
 			if (!b.hull.empty()) body.set_boundary(b.hull);
 			for (auto& bc : b.bcs) body.add_boundary_condition(bc.idx, (mf_bc_kind)bc.kind, bc.v);
 			for (uint32_t act : cs.actions) body.add_action((mf::action)act);
-			if (cs.method == mfcase::TL_WEAK) body.set_gauss_mesh(b.ex, b.ey, cs.gp_h, cs.gp_rho);
+			if (cs.method == mfcase::TL_WEAK && b.ex) body.set_gauss_mesh(b.ex, b.ey, cs.gp_h, cs.gp_rho);
+			if (cs.method == mfcase::TL_WEAK && !b.ex) {
+				body.set_elements(b.quads, b.order, (int32_t)b.shape, cs.gp_h, cs.gp_rho);
+				if (b.ngp) body.set_gauss_points(b.g[0], b.g[1], b.g[6], b.g[5]);
+			}
+			if (cs.method == mfcase::UL_WEAK) {
+				if (b.ex == 1) body.set_elements(b.quads, b.order, MF_SHAPE_ELEMENT);
+				auto& g = b.g;
+				mf_particles sp = {g[0].data(), g[1].data(), g[2].data(), g[3].data(), g[4].data(),
+				                   g[5].data(), g[6].data(), g[7].data(), g[8].data(), g[9].data(),
+				                   g[10].data(), g[11].data(), g[12].data()};
+				body.set_stress_points(sp, b.ngp);
+			}
 			bodies.push_back(body);
 		}
 		ctx.step((int32_t)cs.nsteps);

@@ -39,7 +39,8 @@ def test_facade_compiles_and_reports_errors(facade_bin, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["rings_monaghan", "rings_monaghan_contact", "rings_tl_contact", "tensile_tl",
-                                  "tensile_tl_weak"])
+                                  "tensile_tl_weak", "rings_tl_fem_contact", "rotation_tl_weak", "rings_ul_weak_contact",
+                                  "tensile_ul_fem"])
 def test_facade_reproduces_the_reference(facade_bin, tmp_path, name):
     case = os.path.join(GOLDEN, f"{name}.case")
     out = str(tmp_path / "o.out")
