@@ -411,7 +411,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "corot", "godunov", "potential", "ulweak"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
-    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--cpu-steps", type=int, default=150)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-graph", action="store_true")

@@ -2817,8 +2817,8 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
 		g_tune_cache[key] = best_t;
 	}
-	snprintf(line, sizeof line, " -> b%u p%u c%u tl%u (%s)", best_t.ul_block, best_t.ul_persistent, best_t.ul_chunk,
-	         best_t.tl_block, key.c_str());
+	snprintf(line, sizeof line, " -> b%u p%u c%u tl%u t%u (%s)", best_t.ul_block, best_t.ul_persistent,
+	         best_t.ul_chunk, best_t.tl_block, best_t.tl_tiled, key.c_str());
 	rep += line;
 	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
 	return MF_OK;

@@ -357,16 +357,23 @@ __global__ void k_tl_pack(TLArgs a) {
 
 __device__ __forceinline__ float ffd(float ahi, float alo, float bhi, float blo) { return (ahi - bhi) + (alo - blo); }
 
+// v_ij . x_ij of a pair, FP32.  The FP32 pair passes (plain and halo tiles) share this
+// and art_visc_pi with every rounding spelled out, so that neither compile can contract
+// them differently: the two variants stay bit-identical.
+__device__ __forceinline__ float approach(float vijx, float vijy, float xij, float yij) {
+	return __fmaf_rn(vijy, yij, __fmul_rn(vijx, xij));
+}
+
 // Monaghan-Gingold viscosity Pi_ij of an approaching pair (correctors.h:83-137), FP32
 // with the two divisions as reciprocal-multiply (__fdividef, 2 ulp)
 __device__ __forceinline__ float art_visc_pi(float4 hmrc_i, float4 hmrc_j, float xij, float yij, float vijposij,
                                              float alpha, float beta, float eta2) {
-	float cij = 0.5f * (hmrc_i.w + hmrc_j.w);
-	float hij = 0.5f * (hmrc_i.x + hmrc_j.x);
-	float rhoij = 0.5f * (hmrc_i.z + hmrc_j.z);
-	float r2ij = xij * xij + yij * yij;
-	float muij = __fdividef(hij * vijposij, r2ij + eta2 * hij * hij);
-	return __fdividef(-alpha * cij * muij + beta * muij * muij, rhoij);
+	float cij = __fmul_rn(0.5f, __fadd_rn(hmrc_i.w, hmrc_j.w));
+	float hij = __fmul_rn(0.5f, __fadd_rn(hmrc_i.x, hmrc_j.x));
+	float rhoij = __fmul_rn(0.5f, __fadd_rn(hmrc_i.z, hmrc_j.z));
+	float r2ij = __fmaf_rn(yij, yij, __fmul_rn(xij, xij));
+	float muij = __fdividef(__fmul_rn(hij, vijposij), __fmaf_rn(__fmul_rn(eta2, hij), hij, r2ij));
+	return __fdividef(__fmaf_rn(__fmul_rn(-alpha, cij), muij, __fmul_rn(__fmul_rn(beta, muij), muij)), rhoij);
 }
 
 // End of pass B for row i: momentum, advection and the RK4 update (rk4.h:52-108).
@@ -524,7 +531,7 @@ __global__ void __launch_bounds__(256, 4) k_tlB32(TLArgs a) {
 			float4 xj = __ldg(&rj->x), vj = __ldg(&rj->v);
 			float xij = ffd(ri.x.x, ri.x.y, xj.x, xj.y), yij = ffd(ri.x.z, ri.x.w, xj.z, xj.w);
 			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
-			float vijposij = vijx * xij + vijy * yij;
+			float vijposij = approach(vijx, vijy, xij, yij);
 			if (vijposij < 0.f) {
 				float4 hmrc = __ldg(&rj->hmrc);
 				float piij = art_visc_pi(ri.hmrc, hmrc, xij, yij, vijposij, alpha, beta, eta2);
@@ -651,7 +658,7 @@ __global__ void __launch_bounds__(TL_TILE, 8) k_tlB32t(TLArgs a) {
 			float4 xj = smB[HM + l], vj = smB[2 * HM + l];
 			float xij = ffd(ri.x.x, ri.x.y, xj.x, xj.y), yij = ffd(ri.x.z, ri.x.w, xj.z, xj.w);
 			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
-			float vijposij = vijx * xij + vijy * yij;
+			float vijposij = approach(vijx, vijy, xij, yij);
 			if (vijposij < 0.f) {
 				float4 hmrc = smB[3 * HM + l];
 				float piij = art_visc_pi(ri.hmrc, hmrc, xij, yij, vijposij, alpha, beta, eta2);
