@@ -12,11 +12,12 @@ Metric: particle-steps/s = particles x RK4 steps / time, the whole step included
 (4 stages, contact, boundary update).  One JSON line on rank 0.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c3|c4|corot|godunov|potential|ulweak]
+                  [--workload c2|c1|c3|c4|corot|godunov|potential|ulweak|tlweak|tlfem|ulfem]
                   [--precision mixed|fp64|fp64_strict]
 
-The family workloads (corot, godunov, potential, ulweak) are ensembles of the
-reference's own two-ring set-up of that SPH family (ulweak: FP64 forms only).
+The family workloads (corot, godunov, potential, ulweak, tlweak, tlfem, ulfem) are
+ensembles of the reference's own two-ring set-up of that family (ulweak and ulfem: FP64
+forms only).
 
 With --impl reference it times the CPU implementation of the same path (the oracle
 restatement of the reference, which is single-threaded) on all host cores.
@@ -51,7 +52,8 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-FAMILIES = ("corot", "godunov", "potential", "ulweak")
+FAMILIES = ("corot", "godunov", "potential", "ulweak", "tlweak", "tlfem", "ulfem")
+FP64_ONLY = ("ulweak", "ulfem")  # the weak UL form runs in the FP64 forms only
 
 
 def workload_desc(name: str, dx: float | None, instances: int = 512) -> dict:
@@ -268,8 +270,8 @@ def ours(args, cfg_desc):
 
     sc, cfg = workload(args.workload, args.dx, args.instances)
     n = sc.n_total
-    if args.workload == "ulweak" and args.precision == "mixed":
-        args.precision = "fp64"  # the weak UL form runs in the FP64 forms only
+    if args.workload in FP64_ONLY and args.precision == "mixed":
+        args.precision = "fp64"
     tl = sc.method in (M.METHOD_TL, M.METHOD_TL_WEAK, M.METHOD_COROT, M.METHOD_POTENTIAL)
     sim = M.from_scenario(sc, precision=args.precision, device=local, graph=not args.no_graph)
     mixed = args.precision == "mixed"
@@ -360,10 +362,13 @@ def ours(args, cfg_desc):
              5: "weak"}
     if sc.method == M.METHOD_UL_WEAK:
         names.update({2: "weak UL particle pass", 5: "weak UL stress-point pass"})
+    elif sc.method == M.METHOD_TL_WEAK:
+        names.update({2: "weak TL particle pass", 5: "weak TL Gauss-point pass"})
     elif sc.method in (M.METHOD_COROT, M.METHOD_POTENTIAL):
         names.update({1: "pass A", 2: "pass B"})
     roof = None
-    if klaunch and sc.method != M.METHOD_UL_WEAK:  # (no byte model for the weak UL passes)
+    # (no byte model for the weak-form passes)
+    if klaunch and sc.method not in (M.METHOD_UL_WEAK, M.METHOD_TL_WEAK):
         per_launch_rows = krows / klaunch
         abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload) * per_launch_rows
         achieved = abytes / (kms / klaunch / 1e3) / 1e9
@@ -408,7 +413,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "corot", "godunov", "potential", "ulweak"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", *FAMILIES])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--cpu-steps", type=int, default=150)

@@ -404,6 +404,8 @@ BodyParams make_params(const HostBody& b) {
 	p.alpha = b.sd.artvisc_alpha; p.beta = b.sd.artvisc_beta; p.eta = b.sd.artvisc_eta; p.xsph_eps = b.sd.xsph_eps;
 	p.dt = b.dt; p.time = b.time;
 	p.off = b.off; p.n = b.n;
+	p.fK = (float)p.K; p.fG = (float)p.G; p.frho0 = (float)p.rho0; p.fc0sq = (float)p.c0sq; p.fD = (float)p.D;
+	p.fnu = (float)p.nu; p.falpha = (float)p.alpha; p.fbeta = (float)p.beta; p.feta2 = (float)(p.eta * p.eta);
 	return p;
 }
 

@@ -182,6 +182,19 @@ MF_DEV void green_stvenant(T Hxx, T Hxy, T Hyx, T Hyy, T D, T nu, T& Sxx, T& Sxy
 	Sxy = D * (T(1) - nu) * Esv.c[1][0];
 }
 
+// The same law with E = (F^T F - I) / 2 expanded as (H + H^T + H^T H) / 2 (F = I + H):
+// algebraically equal, and free of the cancellation of F^T F - I, which in FP32 would
+// leave a relative error of ~1e-7 / |H| in small strains.
+template <class T>
+MF_DEV void green_stvenant_h(T Hxx, T Hxy, T Hyx, T Hyy, T D, T nu, T& Sxx, T& Sxy, T& Syy) {
+	T E00 = Hxx + T(0.5) * (Hxx * Hxx + Hyx * Hyx);
+	T E11 = Hyy + T(0.5) * (Hxy * Hxy + Hyy * Hyy);
+	T E01 = T(0.5) * (Hxy + Hyx + Hxx * Hxy + Hyx * Hyy);
+	Sxx = D * (E00 + nu * E11);
+	Syy = D * (E00 * nu + E11);
+	Sxy = D * (T(1) - nu) * E01;
+}
+
 // L = Fdot F^-1 (cont_mech.h:188-203)
 template <class T>
 MF_DEV void velocity_gradient_tl(T Hxx, T Hxy, T Hyx, T Hyy, T Fxx, T Fxy, T Fyx, T Fyy, T& vx_x, T& vx_y, T& vy_x, T& vy_y) {

@@ -198,6 +198,28 @@ __device__ __forceinline__ void tl_particle(uint32_t flags, const BodyParams& pr
 	if (flags & A_C2N) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
 }
 
+// The per-row part of the mixed pass A in FP32.  GB300 issues FP64 at a small fraction
+// of its FP32 rate, and in FP64 this part kept the FP64 pipe ~70 % busy, the pass's
+// real bound.  FP32 suffices: F = I + H and its inverse are well conditioned, the
+// density enters as rho - rho0 (the mixed state), so the EOS takes no cancellation,
+// and Green-St Venant takes E from H without forming F^T F - I.
+__device__ __forceinline__ void tl_particle32(uint32_t flags, const BodyParams& pr, float Hxx, float Hxy, float Hyx,
+                                              float Hyy, float Fxx, float Fxy, float Fyx, float Fyy, float drho,
+                                              float Sxx, float Sxy, float Syy, float& Pxx, float& Pxy, float& Pyx,
+                                              float& Pyy, float& rho_t, float& Sxx_t, float& Sxy_t, float& Syy_t) {
+	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
+	if (flags & A_VGRAD_TL) velocity_gradient_tl<float>(Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, vx_x, vx_y, vy_x, vy_y);
+	rho_t = 0.f;
+	if (flags & A_CONTINUITY) rho_t = -((pr.frho0 + drho) * (vx_x + vy_y));
+	float p = 0.f;
+	if (flags & A_EOS) p = pr.fc0sq * drho;
+	Sxx_t = Sxy_t = Syy_t = 0.f;
+	if (flags & A_JAUMANN) jaumann<float>(vx_x, vx_y, vy_x, vy_y, Sxx, Sxy, Syy, pr.fG, Sxx_t, Sxy_t, Syy_t);
+	if (flags & A_GREEN) green_stvenant_h<float>(Hxx, Hxy, Hyx, Hyy, pr.fD, pr.fnu, Sxx, Sxy, Syy);
+	Pxx = Pxy = Pyx = Pyy = 0.f;
+	if (flags & A_C2N) cauchy_to_nominal<float>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
+}
+
 // Sliced-ELL addressing: the 32 rows of a warp read entry k of their lists from 32
 // consecutive slots, so every per-pair load of the warp is one coalesced request.
 __device__ __forceinline__ uint32_t sell_base(const TLArgs& a, uint32_t i) { return a.sl_off[i >> 5] + (i & 31u); }
@@ -334,6 +356,19 @@ struct __align__(16) RecB {
 	float4 P, x, v, hmrc;
 };
 
+// End of the mixed pass A for row i: the per-row part in FP32, then the nominal stress
+// into the row's record and the rate terms.
+__device__ __forceinline__ void tlA_finish(const TLArgs& a, uint32_t i, float Hxx, float Hxy, float Hyx, float Hyy,
+                                           float Fxx, float Fxy, float Fyx, float Fyy) {
+	const mfk_host::StateSoA& s = a.st;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	float4 P, dA;
+	tl_particle32(a.flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, s.rho_f[i], s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i],
+	              P.x, P.y, P.z, P.w, dA.x, dA.y, dA.z, dA.w);
+	((RecB*)a.recB)[i].P = P;
+	((float4*)a.dA32)[i] = dA;
+}
+
 // The records of row i from its state (x, y, vx, vy in FP64, rho - rho0 in FP32).
 __device__ __forceinline__ void tl_pack_row(const TLArgs& a, uint32_t i, const BodyParams& pr, double x, double y,
                                             double vx, double vy, float rho_dev, RecB* recB) {
@@ -343,8 +378,8 @@ __device__ __forceinline__ void tl_pack_row(const TLArgs& a, uint32_t i, const B
 	RecB* rb = recB + i;
 	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
-	float rho = rho_dev + (float)pr.rho0;  // the mixed state holds rho - rho0
-	float K = (float)pr.K;
+	float rho = rho_dev + pr.frho0;  // the mixed state holds rho - rho0
+	float K = pr.fK;
 	rb->hmrc = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
 }
 
@@ -394,11 +429,13 @@ __device__ __forceinline__ void tlB_finish(const TLArgs& a, uint32_t i, const Bo
 	float* nq[4] = {a.nxt.rho_f, a.nxt.Sxx_f, a.nxt.Sxy_f, a.nxt.Syy_f};
 	const float4 dAi = ((const float4*)a.dA32)[i];
 	const double vxs = (flags & A_ADVECTION) ? s.vx[i] : 0., vys = (flags & A_ADVECTION) ? s.vy[i] : 0.;
-	double fx = 0., fy = 0., mi = 1.;
+	// the momentum in FP32 (an FP64 division per component would keep the narrow FP64
+	// pipe busy); the RK4 accumulation below stays FP64
+	float fx = 0.f, fy = 0.f, inv_m = 0.f;
 	if (flags & A_MOMENTUM_TL) {
-		fx = a.fcx[i];
-		fy = a.fcy[i];
-		mi = a.m[i];
+		fx = (float)a.fcx[i];
+		fy = (float)a.fcy[i];
+		inv_m = 1.f / ((const float*)a.m32)[i];
 	}
 	double bv[4], av[4] = {0., 0., 0., 0.};
 	float bf[4], af[4] = {0.f, 0.f, 0.f, 0.f};
@@ -414,12 +451,13 @@ __device__ __forceinline__ void tlB_finish(const TLArgs& a, uint32_t i, const Bo
 	double d[4];
 	d[0] = vxs;
 	d[1] = vys;
-	d[2] = av_x;
-	d[3] = av_y;
+	float acc_x = av_x, acc_y = av_y;
 	if (flags & A_MOMENTUM_TL) {
-		d[2] += (double)(1.f / rho0 * (Pxx_x + Pyx_y)) + fx / mi;
-		d[3] += (double)(1.f / rho0 * (Pxy_x + Pyy_y)) + fy / mi;
+		acc_x += 1.f / rho0 * (Pxx_x + Pyx_y) + fx * inv_m;
+		acc_y += 1.f / rho0 * (Pxy_x + Pyy_y) + fy * inv_m;
 	}
+	d[2] = acc_x;
+	d[3] = acc_y;
 	const float e[4] = {dAi.x, dAi.y, dAi.z, dAi.w};
 	const double dt = pr.dt;
 	double nv[4];  // the next stage's x, y, vx, vy
@@ -490,14 +528,7 @@ __global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 			Fyy += dvy * w.y;
 		}
 	}
-	const BodyParams& pr = a.params[a.body_of[i]];
-	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
-	double rho = (double)s.rho_f[i] + pr.rho0;  // the mixed state holds rho - rho0
-	// the 2x2 inversions of the per-particle part stay FP64
-	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
-	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
-	((RecB*)a.recB)[i].P = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
-	((float4*)a.dA32)[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
+	tlA_finish(a, i, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy);
 }
 
 __global__ void __launch_bounds__(256, 4) k_tlB32(TLArgs a) {
@@ -507,11 +538,11 @@ __global__ void __launch_bounds__(256, 4) k_tlB32(TLArgs a) {
 	const RecB* recB = (const RecB*)a.recB;
 	uint32_t flags = a.flags;
 	const BodyParams& pr = a.params[a.body_of[i]];
-	float rho0 = (float)pr.rho0;
+	float rho0 = pr.frho0;
 	float r21 = 1.f / (rho0 * rho0);
 	float sc = r21 * rho0;
 	RecB ri = recB[i];
-	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+	float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2;
 	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
 	uint32_t q = sell_base(a, i), c = a.cnt[i];
 #pragma unroll 2
@@ -604,13 +635,7 @@ __global__ void __launch_bounds__(TL_TILE) k_tlA32t(TLArgs a) {
 			Fyy += dvy * w.y;
 		}
 	}
-	const BodyParams& pr = a.params[a.body_of[i]];
-	double Pxx, Pxy, Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t;
-	double rho = (double)s.rho_f[i] + pr.rho0;
-	tl_particle(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, rho, s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i], Pxx, Pxy,
-	            Pyx, Pyy, rho_t, Sxx_t, Sxy_t, Syy_t);
-	((RecB*)a.recB)[i].P = make_float4((float)Pxx, (float)Pxy, (float)Pyx, (float)Pyy);
-	((float4*)a.dA32)[i] = make_float4((float)rho_t, (float)Sxx_t, (float)Sxy_t, (float)Syy_t);
+	tlA_finish(a, i, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy);
 }
 
 __global__ void __launch_bounds__(TL_TILE, 8) k_tlB32t(TLArgs a) {
@@ -636,10 +661,10 @@ __global__ void __launch_bounds__(TL_TILE, 8) k_tlB32t(TLArgs a) {
 	const float2* sw = (const float2*)a.t_sw;
 	const uint32_t flags = a.flags;
 	const BodyParams& pr = a.params[bi];
-	float rho0 = (float)pr.rho0;
+	float rho0 = pr.frho0;
 	float r21 = 1.f / (rho0 * rho0);
 	float sc = r21 * rho0;
-	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+	float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2;
 	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
 	uint32_t q = a.t_sl[p >> 5] + (p & 31u);
 #pragma unroll 4

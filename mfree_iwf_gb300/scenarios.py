@@ -929,14 +929,17 @@ def plate_ul_weak(dx: float = 5e-5, Lx: float = 0.1, Ly: float = 0.02, seed: int
 
 
 FAMILY_RING_SETUPS = {"corot": "rings_corot_contact", "godunov": "rings_godunov_contact",
-                      "potential": "rings_potential_contact", "ulweak": "rings_ul_weak_contact"}
+                      "potential": "rings_potential_contact", "ulweak": "rings_ul_weak_contact",
+                      "tlweak": "rings_tl_weak_contact", "tlfem": "rings_tl_fem_contact",
+                      "ulfem": "rings_ul_fem_contact"}
 
 
 def family_ensemble(family: str, instances: int = 256, nbox: int = 81, seed: int = 20261203,
                     E_range=(0.8e7, 1.2e7)) -> Scenario:
     """An ensemble of independent two-ring impacts of one SPH family, each the
     reference's own set-up (rings_corot_contact, rings_godunov_contact,
-    rings_potential_contact or rings_ul_weak_contact at nbox) with its own seeded
+    rings_potential_contact, rings_ul_weak_contact, rings_tl_weak_contact,
+    rings_tl_fem_contact or rings_ul_fem_contact at nbox) with its own seeded
     Young's modulus E ~ U[E_range]; the two rings of an instance form one contact group.
     (The reference's potential and Godunov rings do not stay finite at much finer
     lattices, so the ensemble, not one large lattice, gives the size.)"""
@@ -950,6 +953,7 @@ def family_ensemble(family: str, instances: int = 256, nbox: int = 81, seed: int
                       ey=b.ey, params={"E": E})
             if b.gp is not None:
                 nb.gp = {f: a.copy() for f, a in b.gp.items()}
+            nb.quads, nb.order, nb.shape = b.quads, b.order, b.shape
             bodies.append(nb)
             groups.append(k)
     sc = Scenario(method=base.method, bodies=bodies, actions=list(base.actions), dt=base.dt, nu=base.nu, E=base.E,
