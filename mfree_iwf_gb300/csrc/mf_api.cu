@@ -406,6 +406,7 @@ BodyParams make_params(const HostBody& b) {
 	p.off = b.off; p.n = b.n;
 	p.fK = (float)p.K; p.fG = (float)p.G; p.frho0 = (float)p.rho0; p.fc0sq = (float)p.c0sq; p.fD = (float)p.D;
 	p.fnu = (float)p.nu; p.falpha = (float)p.alpha; p.fbeta = (float)p.beta; p.feta2 = (float)(p.eta * p.eta);
+	p.fdt = (float)p.dt;
 	return p;
 }
 

@@ -229,4 +229,25 @@ MF_DEV FF ff_split(double d) {
 }
 MF_DEV float ff_diff(FF a, FF b) { return (a.hi - b.hi) + (a.lo - b.lo); }
 
+// The same kind of split from the double's bit pattern, with integer operations only
+// (every conversion from FP64 runs on the FP64 pipe, which GB300 keeps narrow): hi is
+// the double's leading 24 significant bits (truncated, not rounded), lo the remaining
+// 29 bits rounded to FP32, so hi + lo carries ~48 significant bits.  Below 2^-74 lo is
+// left zero (its unit would be subnormal in FP32), below 2^-126 hi is a signed zero;
+// beyond FP32's range (and inf, nan) hi is the plain conversion.
+MF_DEV FF ff_split_bits(double d) {
+	const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+	const uint32_t h = (uint32_t)(u >> 32), l = (uint32_t)u;
+	const uint32_t sign = h & 0x80000000u;
+	const int e = (int)((h >> 20) & 0x7ffu);  // biased FP64 exponent
+	if (e < 897) return FF{__uint_as_float(sign), 0.f};
+	if (e > 1150) return FF{(float)d, 0.f};
+	const float hi = __uint_as_float(sign | ((uint32_t)(e - 896) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
+	const uint32_t rest = l & 0x1fffffffu;  // units of 2^(e - 1075)
+	const int se = e - 948;                 // biased FP32 exponent of that unit
+	float lo = 0.f;
+	if (rest != 0u && se > 0) lo = __uint2float_rn(rest) * __uint_as_float((uint32_t)se << 23);
+	return FF{hi, sign ? -lo : lo};
+}
+
 }  // namespace mfk

@@ -37,7 +37,7 @@ struct BodyParams {
 	uint32_t off, n;                // particle rows [off, off+n)
 	uint32_t pad0, pad1;
 	// FP32 copies for the mixed passes (a conversion from FP64 runs on the FP64 pipe)
-	float fK, fG, frho0, fc0sq, fD, fnu, falpha, fbeta, feta2, pad2;
+	float fK, fG, frho0, fc0sq, fD, fnu, falpha, fbeta, feta2, fdt;
 };
 
 // Per-body cell geometry of one derivative evaluation (grid.h:83-115).

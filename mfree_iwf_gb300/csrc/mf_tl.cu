@@ -372,9 +372,9 @@ __device__ __forceinline__ void tlA_finish(const TLArgs& a, uint32_t i, float Hx
 // The records of row i from its state (x, y, vx, vy in FP64, rho - rho0 in FP32).
 __device__ __forceinline__ void tl_pack_row(const TLArgs& a, uint32_t i, const BodyParams& pr, double x, double y,
                                             double vx, double vy, float rho_dev, RecB* recB) {
-	FF ux = ff_split(x - a.X[i]), uy = ff_split(y - a.Y[i]);
+	FF ux = ff_split_bits(x - a.X[i]), uy = ff_split_bits(y - a.Y[i]);
 	((float4*)a.recA)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
-	FF fx = ff_split(x), fy = ff_split(y), fvx = ff_split(vx), fvy = ff_split(vy);
+	FF fx = ff_split_bits(x), fy = ff_split_bits(y), fvx = ff_split_bits(vx), fvy = ff_split_bits(vy);
 	RecB* rb = recB + i;
 	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
 	tlA_finish(a, i, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy);
 }
 
-__global__ void __launch_bounds__(256, 4) k_tlB32(TLArgs a) {
+__global__ void __launch_bounds__(256, 5) k_tlB32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const float2* sw = (const float2*)a.sw;

@@ -234,6 +234,47 @@ __device__ __forceinline__ void gp_point(uint32_t flags, const BodyParams& pr, d
 	if (flags & A_C2N_GP) cauchy_to_nominal<double>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, Pxx, Pxy, Pyx, Pyy);
 }
 
+// The per-Gauss-point part of the mixed pass in FP32: GB300 runs FP64 (and every
+// conversion from it) on a narrow pipe, and in FP64 this part bounded the pass.  The
+// density enters as rho - rho0 (the mixed state), so the EOS takes no cancellation;
+// F = I + H and its inverse are well conditioned.
+__device__ __forceinline__ void gp_point32(uint32_t flags, const BodyParams& pr, float Hxx, float Hxy, float Hyx,
+                                           float Hyy, float Fxx, float Fxy, float Fyx, float Fyy, float drho, float Sxx,
+                                           float Sxy, float Syy, float P[4], float e[4]) {
+	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
+	if (flags & A_VGRAD_GP) velocity_gradient_tl<float>(Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, vx_x, vx_y, vy_x, vy_y);
+	e[0] = 0.f;
+	if (flags & A_CONT_GP) e[0] = -((pr.frho0 + drho) * (vx_x + vy_y));
+	float p = 0.f;
+	if (flags & A_EOS_GP) p = pr.fc0sq * drho;
+	e[1] = e[2] = e[3] = 0.f;
+	if (flags & A_JAUMANN_GP) jaumann<float>(vx_x, vx_y, vy_x, vy_y, Sxx, Sxy, Syy, pr.fG, e[1], e[2], e[3]);
+	P[0] = P[1] = P[2] = P[3] = 0.f;
+	if (flags & A_C2N_GP) cauchy_to_nominal<float>(Hxx, Hxy, Hyx, Hyy, Sxx - p, Sxy, Syy - p, P[0], P[1], P[2], P[3]);
+}
+
+// The mixed Gauss-point state's RK4 update (rk4.h:154-183) in FP32, the state's own type
+__device__ __forceinline__ void gp_rk32(const WeakArgs& a, uint32_t i, float dt, const float e[4], float* gb[4],
+                                        float* ga[4], float* gs[4]) {
+	const uint32_t stg = a.stage;
+	if (stg < 3) {
+		const float dts = (stg == 2 ? 1.f : 0.5f) * dt;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ga[q][i] = (stg == 0) ? e[q] : ga[q][i] + 2.f * e[q];
+			gs[q][i] = gb[q][i] + e[q] * dts;
+		}
+	} else {
+		const float w6 = dt * (1.f / 6.f);
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			float v = gb[q][i] + w6 * (ga[q][i] + e[q]);
+			gb[q][i] = v;
+			gs[q][i] = v;
+		}
+	}
+}
+
 // Gauss point RK4 update of rho and S (rk4.h:154-183)
 template <class T>
 __device__ __forceinline__ void gp_rk(const WeakArgs& a, uint32_t i, double dt, const double e[4], T* gb[4], T* ga[4],
@@ -363,8 +404,8 @@ __global__ void k_weak_pack(WeakArgs a) {
 	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
 	if (j >= a.n_p) return;
 	const mfk_host::StateSoA& s = a.st;
-	FF ux = ff_split(s.x[j] - a.X[j]), uy = ff_split(s.y[j] - a.Y[j]);
-	FF vx = ff_split(s.vx[j]), vy = ff_split(s.vy[j]);
+	FF ux = ff_split_bits(s.x[j] - a.X[j]), uy = ff_split_bits(s.y[j] - a.Y[j]);
+	FF vx = ff_split_bits(s.vx[j]), vy = ff_split_bits(s.vy[j]);
 	float4* pk = (float4*)a.pack;
 	pk[2 * j] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
 	pk[2 * j + 1] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
@@ -376,7 +417,7 @@ __global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
 	const float2* gw = (const float2*)a.g_w;  // gradient times the particle's quad weight
 	const float4* pk = (const float4*)a.pack;
 	uint32_t flags = a.flags;
-	const FF uxi = ff_split(a.gp_ux[i]), uyi = ff_split(a.gp_uy[i]);
+	const FF uxi = ff_split_bits(a.gp_ux[i]), uyi = ff_split_bits(a.gp_uy[i]);
 	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f, Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
 	uint32_t q = sbase(a.g_sl, i), c = a.g_cnt[i];
 #pragma unroll 2
@@ -404,12 +445,11 @@ __global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
 	float* gs[4] = {a.gst.rho_f, a.gst.Sxx_f, a.gst.Sxy_f, a.gst.Syy_f};
 	float* gb[4] = {a.gbase.rho_f, a.gbase.Sxx_f, a.gbase.Sxy_f, a.gbase.Syy_f};
 	float* ga[4] = {a.gacc.rho_f, a.gacc.Sxx_f, a.gacc.Sxy_f, a.gacc.Syy_f};
-	double P[4], e[4];
+	float P[4], e[4];
 	// the mixed Gauss-point state holds rho - rho0
-	gp_point(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, (double)gs[0][i] + pr.rho0, gs[1][i], gs[2][i],
-	         gs[3][i], P[0], P[1], P[2], P[3], e[0], e[1], e[2], e[3]);
-	((float4*)a.gP)[i] = make_float4((float)P[0], (float)P[1], (float)P[2], (float)P[3]);
-	gp_rk<float>(a, i, pr.dt, e, gb, ga, gs);
+	gp_point32(flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, gs[0][i], gs[1][i], gs[2][i], gs[3][i], P, e);
+	((float4*)a.gP)[i] = make_float4(P[0], P[1], P[2], P[3]);
+	gp_rk32(a, i, pr.fdt, e, gb, ga, gs);
 }
 
 __global__ void __launch_bounds__(256) k_p_pass32(WeakArgs a) {
@@ -440,9 +480,10 @@ __global__ void __launch_bounds__(256) k_p_pass32(WeakArgs a) {
 	d[1] = (flags & A_ADVECTION) ? s.vy[j] : 0.;
 	d[2] = 0.;
 	d[3] = 0.;
-	if (flags & A_MOMENTUM_W) {
-		d[2] += (double)(Pxx_x + Pyx_y) / m + a.fcx[j] / m;
-		d[3] += (double)(Pxy_x + Pyy_y) / m + a.fcy[j] / m;
+	if (flags & A_MOMENTUM_W) {  // in FP32: an FP64 division would occupy the narrow FP64 pipe
+		const float inv_m = 1.f / (float)m;
+		d[2] = (Pxx_x + Pyx_y) * inv_m + (float)a.fcx[j] * inv_m;
+		d[3] = (Pxy_x + Pyy_y) * inv_m + (float)a.fcy[j] * inv_m;
 	}
 	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
 	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};
