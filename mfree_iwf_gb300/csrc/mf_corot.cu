@@ -452,8 +452,8 @@ __global__ void k_cm_pack(TLArgs a) {
 	const mfk_host::StateSoA& s = a.st;
 	const BodyParams& pr = a.params[a.body_of[i]];
 	double x = s.x[i], y = s.y[i];
-	FF ux = ff_split(x - a.X[i]), uy = ff_split(y - a.Y[i]);
-	FF fx = ff_split(x), fy = ff_split(y), fvx = ff_split(s.vx[i]), fvy = ff_split(s.vy[i]);
+	FF ux = ff_split_bits(x - a.X[i]), uy = ff_split_bits(y - a.Y[i]);
+	FF fx = ff_split_bits(x), fy = ff_split_bits(y), fvx = ff_split_bits(s.vx[i]), fvy = ff_split_bits(s.vy[i]);
 	((float4*)a.cm_U)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
 	((float4*)a.cm_X)[i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	((float4*)a.cm_V)[i] = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
@@ -632,9 +632,10 @@ __global__ void __launch_bounds__(256) k_cm_B(TLArgs a) {
 	d[1] = (flags & A_ADVECTION) ? s.vy[i] : 0.;
 	d[2] = (double)avx;
 	d[3] = (double)avy;
-	if (forces) {
-		d[2] += (double)fx + a.fcx[i] / a.m[i];
-		d[3] += (double)fy + a.fcy[i] / a.m[i];
+	if (forces) {  // the contact term in FP32 (an FP64 division would occupy the narrow FP64 pipe)
+		const float inv_m = 1.f / ((const float*)a.m32)[i];
+		d[2] += (double)(fx + (float)a.fcx[i] * inv_m);
+		d[3] += (double)(fy + (float)a.fcy[i] * inv_m);
 	}
 	double* bp[4] = {a.base.x, a.base.y, a.base.vx, a.base.vy};
 	double* ap[4] = {a.acc.x, a.acc.y, a.acc.vx, a.acc.vy};

@@ -377,9 +377,9 @@ __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
 	uint32_t b = a.body_of[i];
 	const float rho_dev = rho;  // the mixed state holds rho - rho0
-	rho += (float)P[b].rho0;
+	rho += P[b].frho0;
 	Rec32 r;
-	r.x = ff_split(x); r.y = ff_split(y); r.vx = ff_split(vx); r.vy = ff_split(vy);
+	r.x = ff_split_bits(x); r.y = ff_split_bits(y); r.vx = ff_split_bits(vx); r.vy = ff_split_bits(vy);
 	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
 	per_particle<float>(a.flags, P[b], r.m, rho, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c,
 	                    r.qw, r.rho21);
@@ -755,17 +755,17 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	float vxi = ri.vx.hi + ri.vx.lo, vyi = ri.vy.hi + ri.vy.lo;
 	if (flags & A_JAUMANN) {
 		const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
-		jaumann<float>(vx_x, vx_y, vy_x, vy_y, sv.Sxx_f[i], sv.Sxy_f[i], sv.Syy_f[i], (float)pr.G, d[5], d[6], d[7]);
+		jaumann<float>(vx_x, vx_y, vy_x, vy_y, sv.Sxx_f[i], sv.Sxy_f[i], sv.Syy_f[i], pr.fG, d[5], d[6], d[7]);
 	}
 	if (flags & A_CONTINUITY) d[4] = -(rhoi * (vx_x + vy_y));
 	if (GOD && (flags & A_GOD_CONT)) d[4] = god_rho;
 	if (GOD && (flags & A_GOD_MOM)) {
-		d[2] += god_vx + (float)(a.fcx[i] / (double)ri.m);
-		d[3] += god_vy + (float)(a.fcy[i] / (double)ri.m);
+		d[2] += god_vx + (float)a.fcx[i] / ri.m;
+		d[3] += god_vy + (float)a.fcy[i] / ri.m;
 	}
 	if (flags & A_MOMENTUM_UL) {
-		d[2] += 1.f / rhoi * (Sxx_x + Sxy_y) + (float)(a.fcx[i] / (double)ri.m);
-		d[3] += 1.f / rhoi * (Sxy_x + Syy_y) + (float)(a.fcy[i] / (double)ri.m);
+		d[2] += 1.f / rhoi * (Sxx_x + Sxy_y) + (float)a.fcx[i] / ri.m;
+		d[3] += 1.f / rhoi * (Sxy_x + Syy_y) + (float)a.fcy[i] / ri.m;
 	}
 	if (a.stage > 0) {
 		// the cells were sized at stage 0 for moves up to g.slack; check that held
