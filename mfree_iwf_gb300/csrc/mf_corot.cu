@@ -408,9 +408,9 @@ cudaError_t cr_stage(const TLArgs& a, int part, cudaStream_t s) {
 }  // namespace MF_NS
 
 // ---------------------------------------------------------------------------------
-// Mixed form of the corotational and elastic-potential methods: the pair arithmetic in
-// FP32, position differences from float-float records, the per-row stress (2x2
-// inversion, Cauchy-Green / Green-St Venant) and the RK4 state of x, y, vx, vy in FP64.
+// Mixed form of the corotational and elastic-potential methods: the pair arithmetic and
+// the per-row stress (2x2 inversion, Cauchy-Green / Green-St Venant from H) in FP32,
+// position differences from float-float records, the RK4 state of x, y, vx, vy in FP64.
 // The rotated displacement difference is formed as (R^T - I) X_ji + R^T u_ji, with
 // cos - 1 kept as -2 sin^2(theta/2), so that no term cancels in FP32.
 namespace MF_NS {
@@ -457,8 +457,8 @@ __global__ void k_cm_pack(TLArgs a) {
 	((float4*)a.cm_U)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
 	((float4*)a.cm_X)[i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 	((float4*)a.cm_V)[i] = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
-	float rho = s.rho_f[i] + (float)pr.rho0;  // the mixed state holds rho - rho0
-	((float4*)a.cm_H)[i] = make_float4(((const float*)a.h32)[i], rho, sqrtf((float)pr.K / rho), ((const float*)a.m32)[i]);
+	float rho = s.rho_f[i] + pr.frho0;  // the mixed state holds rho - rho0
+	((float4*)a.cm_H)[i] = make_float4(((const float*)a.h32)[i], rho, sqrtf(pr.fK / rho), ((const float*)a.m32)[i]);
 }
 
 // rotation from the anisotropy tensor, x_ji = X_ji + u_ji
@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(256) k_cm_R(TLArgs a) {
 }
 
 // pass A: displacement gradient (rotated, corotational; plain, potential), then per row
-// in FP64 the stress, nominal stress (corotational) or F_e (potential)
+// the stress, nominal stress (corotational) or F_e (potential)
 __global__ void __launch_bounds__(256) k_cm_A(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
@@ -527,28 +527,30 @@ __global__ void __launch_bounds__(256) k_cm_A(TLArgs a) {
 			Hyy += uy * w.y;
 		}
 	}
+	// the per-row part in FP32 (GB300 runs FP64 on a narrow pipe): F = I + H is well
+	// conditioned, Green-St Venant takes E from H without forming F^T F - I, and the
+	// corotational strain (F + F^T)/2 - I is linear in H
 	const BodyParams& pr = a.params[a.body_of[i]];
 	const mfk_host::StateSoA& s = a.st;
-	double H00 = Hxx, H01 = Hxy, H10 = Hyx, H11 = Hyy;
-	double P0 = 0., P1 = 0., P2 = 0., P3 = 0.;
+	float P0 = 0.f, P1 = 0.f, P2 = 0.f, P3 = 0.f;
 	if (pot) {
-		double Sxx = s.Sxx_f[i], Sxy = s.Sxy_f[i], Syy = s.Syy_f[i];
-		if (a.flags & A_GREEN) green_stvenant<double>(H00, H01, H10, H11, pr.D, pr.nu, Sxx, Sxy, Syy);
-		double sc = -2 * a.qw0[i];
-		double J00 = sc * (H00 + 1.), J01 = sc * H10, J10 = sc * H01, J11 = sc * (H11 + 1.);
+		float Sxx = s.Sxx_f[i], Sxy = s.Sxy_f[i], Syy = s.Syy_f[i];
+		if (a.flags & A_GREEN) green_stvenant_h<float>(Hxx, Hxy, Hyx, Hyy, pr.fD, pr.fnu, Sxx, Sxy, Syy);
+		float sc = -2.f * ((const float*)a.qw32)[i];
+		float J00 = sc * (Hxx + 1.f), J01 = sc * Hyx, J10 = sc * Hxy, J11 = sc * (Hyy + 1.f);
 		P0 = J00 * Sxx + J10 * Sxy; P1 = J01 * Sxx + J11 * Sxy;
 		P2 = J00 * Sxy + J10 * Syy; P3 = J01 * Sxy + J11 * Syy;
 	} else {
-		double Sxx = 0., Sxy = 0., Syy = 0.;
+		float Sxx = 0.f, Sxy = 0.f, Syy = 0.f;
 		if (a.flags & A_CR_CAUCHY_GREEN) {
-			double E00 = H00, E01 = 0.5 * (H10 + H01), E11 = H11;  // (F + F^T)/2 - I
-			Sxx = pr.D * (E00 + pr.nu * E11);
-			Syy = pr.D * (E00 * pr.nu + E11);
-			Sxy = pr.D * (1 - pr.nu) * E01;
+			float E00 = Hxx, E01 = 0.5f * (Hyx + Hxy), E11 = Hyy;  // (F + F^T)/2 - I
+			Sxx = pr.fD * (E00 + pr.fnu * E11);
+			Syy = pr.fD * (E00 * pr.fnu + E11);
+			Sxy = pr.fD * (1.f - pr.fnu) * E01;
 		}
-		if (a.flags & A_C2N) cauchy_to_nominal<double>(H00, H01, H10, H11, Sxx, Sxy, Syy, P0, P1, P2, P3);
+		if (a.flags & A_C2N) cauchy_to_nominal<float>(Hxx, Hxy, Hyx, Hyy, Sxx, Sxy, Syy, P0, P1, P2, P3);
 	}
-	((float4*)a.cm_P)[i] = make_float4((float)P0, (float)P1, (float)P2, (float)P3);
+	((float4*)a.cm_P)[i] = make_float4(P0, P1, P2, P3);
 }
 
 // pass B: pair forces, contact, viscosity, advection, RK4 (x, y, vx, vy; rho and the
@@ -605,7 +607,7 @@ __global__ void __launch_bounds__(256) k_cm_B(TLArgs a) {
 	const float4 xi = Xr[i], vi = Vr[i], hi = Hr[i];
 	float avx = 0.f, avy = 0.f;
 	if (flags & A_ART_VISC) {
-		const float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta);
+		const float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2;
 		uint32_t q = q0;
 		for (uint32_t k = 0; k < c; k++, q += 32) {
 			uint32_t j = a.snbr[q];
