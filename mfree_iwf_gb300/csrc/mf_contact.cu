@@ -26,7 +26,7 @@ namespace {
 
 inline unsigned grid1(uint64_t n, unsigned bs) { return (unsigned)((n + bs - 1) / bs); }
 
-constexpr float TILE_MARGIN = 1e-6f;  // metres; >> FP32 rounding of |coordinates| <= ~10 m
+constexpr float TILE_MARGIN = 1e-6f;  // metres; > one FP32 ulp of |coordinates| < 16 m
 
 __global__ void k_boundary(ContactArgs a) {
 	uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,10 +127,13 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
 	Query q;
 	q.xd = valid ? a.x[row] : 0.;
 	q.yd = valid ? a.y[row] : 0.;
-	q.x = ff_split(q.xd);
-	q.y = ff_split(q.yd);
-	q.xf = (float)q.xd;
-	q.yf = (float)q.yd;
+	// integer-only splits (conversions from FP64 would occupy the narrow FP64 pipe for
+	// every query); the box tests take hi, within one FP32 ulp of the coordinate, which
+	// TILE_MARGIN covers
+	q.x = ff_split_bits(q.xd);
+	q.y = ff_split_bits(q.yd);
+	q.xf = q.x.hi;
+	q.yf = q.y.hi;
 	uint32_t t0 = a.m_tile_off[M], nt = a.m_tile_n[M];
 	float best_f = 3.4e38f;
 	double best = 1.7976931348623157e308;
