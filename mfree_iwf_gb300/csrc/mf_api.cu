@@ -407,6 +407,8 @@ BodyParams make_params(const HostBody& b) {
 	p.fK = (float)p.K; p.fG = (float)p.G; p.frho0 = (float)p.rho0; p.fc0sq = (float)p.c0sq; p.fD = (float)p.D;
 	p.fnu = (float)p.nu; p.falpha = (float)p.alpha; p.fbeta = (float)p.beta; p.feta2 = (float)(p.eta * p.eta);
 	p.fdt = (float)p.dt;
+	p.fwdp1 = p.wdeltap > 0 ? (float)(1.0 / p.wdeltap) : 0.f;
+	p.fcorr_exp = (float)p.corr_exp; p.fxsph_eps = (float)p.xsph_eps; p.fmghn_eps = (float)p.mghn_eps;
 	return p;
 }
 

@@ -38,6 +38,7 @@ struct BodyParams {
 	uint32_t pad0, pad1;
 	// FP32 copies for the mixed passes (a conversion from FP64 runs on the FP64 pipe)
 	float fK, fG, frho0, fc0sq, fD, fnu, falpha, fbeta, feta2, fdt;
+	float fwdp1, fcorr_exp, fxsph_eps, fmghn_eps;  // fwdp1 = 1 / wdeltap (0 when wdeltap <= 0)
 };
 
 // Per-body cell geometry of one derivative evaluation (grid.h:83-115).

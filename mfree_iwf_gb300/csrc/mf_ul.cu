@@ -341,6 +341,37 @@ __device__ __forceinline__ void per_particle(uint32_t flags, const BodyParams& p
 	rho21 = T(1.) / (rho * rho);
 }
 
+// The same in FP32 for the mixed gather, from the parameters' FP32 copies, the EOS from
+// the stored rho - rho0 (no cancellation of rho - rho0 in FP32)
+__device__ __forceinline__ void per_particle32(uint32_t flags, const BodyParams& pr, float m, float rho, float drho,
+                                               float qw0, float Sxx, float Sxy, float Syy, float& sxx_o, float& syy_o,
+                                               float& Rxx, float& Rxy, float& Ryy, float& c, float& qw,
+                                               float& rho21) {
+	float p = 0.f;
+	if (flags & A_EOS) p = pr.fc0sq * drho;
+	float sxx = Sxx - p, syy = Syy - p, sxy = Sxy;
+	Rxx = Rxy = Ryy = 0.f;
+	if (flags & A_ART_STRESS) {
+		float eps = pr.fmghn_eps;
+		float theta = 0.5f * atan2f(2.f * sxy, sxx - syy + 0.f);
+		float cs = cosf(theta), sn = sinf(theta);
+		float cs2 = cs * cs, sn2 = sn * sn;
+		float rot_sxx = cs2 * sxx + 2.f * cs * sn * sxy + sn2 * syy;
+		float rot_syy = sn2 * sxx - 2.f * cs * sn * sxy + cs2 * syy;
+		float rot_rxx = 0.f, rot_ryy = 0.f;
+		if (rot_sxx > 0.f) rot_rxx = -eps * rot_sxx / (rho * rho);
+		if (rot_syy > 0.f) rot_ryy = -eps * rot_syy / (rho * rho);
+		Rxx = cs2 * rot_rxx + sn2 * rot_ryy;
+		Rxy = cs * sn * (rot_rxx - rot_ryy);
+		Ryy = sn2 * rot_rxx + cs2 * rot_ryy;
+	}
+	sxx_o = sxx;
+	syy_o = syy;
+	c = sqrtf(pr.fK / rho);
+	qw = (flags & A_RIEMANN) ? m / rho : qw0;
+	rho21 = 1.f / (rho * rho);
+}
+
 __global__ void k_gather64(ULArgs a, const BodyParams* __restrict__ P) {
 	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= a.n_total) return;
@@ -381,11 +412,11 @@ __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	Rec32 r;
 	r.x = ff_split_bits(x); r.y = ff_split_bits(y); r.vx = ff_split_bits(vx); r.vy = ff_split_bits(vy);
 	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
-	per_particle<float>(a.flags, P[b], r.m, rho, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy, r.c,
-	                    r.qw, r.rho21);
+	per_particle32(a.flags, P[b], r.m, rho, rho_dev, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy,
+	               r.c, r.qw, r.rho21);
 	r.sxy = Sxy;
 	if (a.flags & (A_GOD_CONT | A_GOD_MOM)) {  // p from the stored deviation, the stress Syy itself
-		r.Rxx = (a.flags & A_EOS) ? (float)P[b].c0sq * rho_dev : 0.f;
+		r.Rxx = (a.flags & A_EOS) ? P[b].fc0sq * rho_dev : 0.f;
 		r.Rxy = Syy;
 	}
 	Rec32* out = reinterpret_cast<Rec32*>(a.rec) + k;
@@ -646,10 +677,12 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	float fac = (float)(10 * (K_1_PI) / 7.0) * h1 * h1;
 	float reach2 = 4.0001f * hi * hi;
 	float rhoi21 = ri.rho21;
-	float wdp1 = pr.wdeltap > 0 ? (float)(1.0 / pr.wdeltap) : 0.f;
-	bool exp4 = pr.corr_exp == 4.;
-	float corr_exp = (float)pr.corr_exp;
-	float alpha = (float)pr.alpha, beta = (float)pr.beta, eta2 = (float)(pr.eta * pr.eta), xeps = (float)pr.xsph_eps;
+	// the parameters' FP32 copies: a conversion (let alone a division) in FP64 would run
+	// on the narrow FP64 pipe for every row
+	float wdp1 = pr.fwdp1;
+	bool exp4 = pr.fcorr_exp == 4.f;
+	float corr_exp = pr.fcorr_exp;
+	float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2, xeps = pr.fxsph_eps;
 
 	float Sxx_x = 0.f, Sxy_y = 0.f, Sxy_x = 0.f, Syy_y = 0.f;
 	float vx_x = 0.f, vx_y = 0.f, vy_x = 0.f, vy_y = 0.f;
