@@ -220,7 +220,26 @@ def reference_arm(args, cfg_desc):
 MEASURED_TRAFFIC = {
     ("c2", "mixed", "TL pass B"): (1218.0e6, 1759324, "profiles/tl_mixed_ring_impact_dx0.05mm.md: ncu "
                                    "dram__bytes_read.sum + dram__bytes_write.sum, mean of 108 launches"),
+    ("c3", "mixed", "weak TL Gauss-point pass"): (294.24e6, 800000, "profiles/weak_tl_passes_plate.md: ncu "
+                                                  "dram__bytes_read.sum + dram__bytes_write.sum at dx = 0.1 mm "
+                                                  "(800k Gauss points), scaled by the Gauss points"),
 }
+
+
+def weak_bytes(kind: int, n_p: int, n_g: int, e_g: int, e_t: int) -> float:
+    """Unique bytes per row of the mixed weak TL passes (kind 5: per Gauss point, kind 2:
+    per particle), stage-averaged over the four RK4 stages; the gathered records counted
+    once (their unique bytes), as in algorithmic_bytes."""
+    if kind == 5:  # Gauss-point pass
+        return (2 + 12 * e_g / n_g      # count; per entry: index 4 + FP32 gradient pair 8
+                + 16 + 4                # the point's own displacement (FP64 pair), body
+                + 44 + 32               # RK4 of rho, S (FP32): reads stage, base, acc (stages 1-3); writes
+                + 16                    # nominal stress for the particles
+                + 32 * n_p / n_g)       # the particles' float-float displacement/velocity records
+    return (2 + 12 * e_t / n_p          # count; per transposed entry: index 4 + gradient pair 8
+            + 16 * n_g / n_p            # the Gauss points' nominal stress
+            + 8 + 4 + 16                # m, body, contact force
+            + 16 + 32 + 24 + 24 + 40)   # RK4 FP64 x y vx vy: stage v, base, acc (1-3), acc (0-2), stage/base
 
 
 def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool, family: str = "") -> float:
@@ -310,6 +329,10 @@ def ours(args, cfg_desc):
     sim.step(max(2, min(args.steps, 10)))
     sim.synchronize()
     kstats = {k: sim.kernel_stats(k) for k in range(6)}
+    weak_lists = None
+    if sc.method == M.METHOD_TL_WEAK:  # list sizes for the weak passes' byte model
+        weak_lists = (sim.get_option("weak_gauss_points"), sim.get_option("weak_gp_entries"),
+                      sim.get_option("weak_particle_entries"))
     sim.set_timing(False)
 
     # ---- end to end through the C ABI with host buffers: per step the state of all
@@ -367,10 +390,14 @@ def ours(args, cfg_desc):
     elif sc.method in (M.METHOD_COROT, M.METHOD_POTENTIAL):
         names.update({1: "pass A", 2: "pass B"})
     roof = None
-    # (no byte model for the weak-form passes)
-    if klaunch and sc.method not in (M.METHOD_UL_WEAK, M.METHOD_TL_WEAK):
+    # (no byte model for the weak UL passes, nor for the FP64 weak TL ones)
+    weak_model = sc.method == M.METHOD_TL_WEAK and mixed and weak_lists is not None and dom in (2, 5)
+    if klaunch and sc.method != M.METHOD_UL_WEAK and (sc.method != M.METHOD_TL_WEAK or weak_model):
         per_launch_rows = krows / klaunch
-        abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload) * per_launch_rows
+        if weak_model:
+            abytes = weak_bytes(dom, n, weak_lists[0], weak_lists[1], weak_lists[2]) * per_launch_rows
+        else:
+            abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload) * per_launch_rows
         achieved = abytes / (kms / klaunch / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,

@@ -259,7 +259,10 @@ MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
  *                     before the first step)
  * read-only, through mf_get_option:
  *   "tl_tiles_built"  1 when the halo tiles exist (mixed TL, after the first step)
- *   "tl_halo_max"     the largest tile halo, in rows */
+ *   "tl_halo_max"     the largest tile halo, in rows
+ *   "weak_gauss_points", "weak_gp_entries", "weak_particle_entries"
+ *                     MF_METHOD_TL_WEAK after the first step: the Gauss points, and the
+ *                     entries of their lists and of the particles' transposed lists */
 MF_API mf_status mf_set_option(mf_ctx* ctx, const char* key, int64_t value);
 MF_API mf_status mf_get_option(mf_ctx* ctx, const char* key, int64_t* value);
 /* ---------------------------------------------------------------------------

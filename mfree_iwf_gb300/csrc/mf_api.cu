@@ -260,6 +260,7 @@ struct mf_ctx {
 
 	// TL_WEAK: Gauss points and the three list sets (sliced ELL)
 	uint32_t n_g = 0;
+	uint64_t g_entries = 0, t_entries = 0;  // TL_WEAK: list entries of the Gauss points and of the particles' transposed lists
 	DevBuf<uint32_t> gp_body, g_sl, g_snbr, t_sl, t_snbr, p_sl, p_snbr;
 	DevBuf<uint16_t> g_cnt, t_cnt, p_cnt;
 	DevBuf<double> gp_x, gp_y, gp_qw, gp_hh, gp_ux, gp_uy, gsd[3][4], gP64;
@@ -1506,6 +1507,10 @@ mf_status weak_setup(mf_ctx* c) {
 	}
 	// sliced ELL (mixed: FP32 with the quad weights folded in)
 	uint64_t sg, sp, stt;
+	c->g_entries = 0;
+	c->t_entries = 0;
+	for (uint32_t v : gc) c->g_entries += v;
+	for (uint32_t v : tc) c->t_entries += v;
 	if ((st = sell_offsets(c, gc, c->g_sl, sg)) || (st = sell_offsets(c, pc, c->p_sl, sp)) ||
 	    (st = sell_offsets(c, tc, c->t_sl, stt)))
 		return st;
@@ -2846,6 +2851,18 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	if (!c || !key || !value) return MF_ERR_ARG;
 	if (!strcmp(key, "tl_tiles")) {
 		*value = c->tune.tl_tiled;
+		return MF_OK;
+	}
+	if (!strcmp(key, "weak_gp_entries")) {
+		*value = (int64_t)c->g_entries;
+		return MF_OK;
+	}
+	if (!strcmp(key, "weak_particle_entries")) {
+		*value = (int64_t)c->t_entries;
+		return MF_OK;
+	}
+	if (!strcmp(key, "weak_gauss_points")) {
+		*value = c->n_g;
 		return MF_OK;
 	}
 	if (!strcmp(key, "tl_tiles_built")) {
