@@ -257,6 +257,9 @@ MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
  *                     memory / stage each 128-row tile's neighbours in shared memory
  *                     (bit-identical results; the tiles are built at set-up, so set 1
  *                     before the first step)
+ *   "ul_split"        1 (default) / 4 / 8: threads per row of the mixed UL pair pass
+ *                     (plain grid; partial sums added across the row's threads, so the
+ *                     pair sums change order); mf_autotune tries all three
  * read-only, through mf_get_option:
  *   "tl_tiles_built"  1 when the halo tiles exist (mixed TL, after the first step)
  *   "tl_halo_max"     the largest tile halo, in rows

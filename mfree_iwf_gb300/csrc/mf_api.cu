@@ -195,6 +195,7 @@ struct Timing {
 // Launch shape of the hot kernels, chosen by mf_autotune.
 struct Tune {
 	uint32_t ul_block = 128, ul_persistent = 0, ul_chunk = 1, tl_block = 128;
+	uint32_t ul_split = 1;  // mixed UL, plain grid: threads per row of the pair pass
 	uint32_t tl_tiled = 0;  // mixed TL: the halo-tile passes (built at set-up when requested)
 };
 std::mutex g_tune_mutex;
@@ -446,6 +447,7 @@ ULArgs ul_args(mf_ctx* c, uint32_t stage) {
 	a.block = c->tune.ul_block;
 	a.persistent = c->tune.ul_persistent;
 	a.chunk = c->tune.ul_chunk;
+	a.split = c->tune.ul_split;
 	a.grid = (uint32_t)std::max(1, c->sm_count) * (2048u / c->tune.ul_block);
 	a.work = c->work.p;
 	return a;
@@ -2767,7 +2769,14 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 			t.ul_block = bs;
 			t.ul_persistent = 0;
 			t.ul_chunk = 1;
+			t.ul_split = 1;
 			cands.push_back(t);
+			if (c->mixed)
+				for (uint32_t sp : {4u, 8u}) {
+					t.ul_split = sp;
+					cands.push_back(t);
+				}
+			t.ul_split = 1;
 			for (uint32_t ch : {1u, 4u}) {
 				t.ul_persistent = 1;
 				t.ul_chunk = ch;
@@ -2806,8 +2815,8 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		float ms = 0.f;
 		cudaEventElapsedTime(&ms, e0, e1);
 		double per = ms / trial_steps;
-		snprintf(line, sizeof line, "%s[b%u p%u c%u tl%u t%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block,
-		         t.ul_persistent, t.ul_chunk, t.tl_block, t.tl_tiled, per);
+		snprintf(line, sizeof line, "%s[b%u p%u c%u s%u tl%u t%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block,
+		         t.ul_persistent, t.ul_chunk, t.ul_split, t.tl_block, t.tl_tiled, per);
 		rep += line;
 		if (per < best) {
 			best = per;
@@ -2827,8 +2836,8 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
 		g_tune_cache[key] = best_t;
 	}
-	snprintf(line, sizeof line, " -> b%u p%u c%u tl%u t%u (%s)", best_t.ul_block, best_t.ul_persistent,
-	         best_t.ul_chunk, best_t.tl_block, best_t.tl_tiled, key.c_str());
+	snprintf(line, sizeof line, " -> b%u p%u c%u s%u tl%u t%u (%s)", best_t.ul_block, best_t.ul_persistent,
+	         best_t.ul_chunk, best_t.ul_split, best_t.tl_block, best_t.tl_tiled, key.c_str());
 	rep += line;
 	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
 	return MF_OK;
@@ -2836,6 +2845,13 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 
 MF_API mf_status mf_set_option(mf_ctx* c, const char* key, int64_t value) {
 	if (!c || !key) return MF_ERR_ARG;
+	if (!strcmp(key, "ul_split")) {
+		if (value != 1 && value != 4 && value != 8) return fail(c, MF_ERR_ARG, "ul_split must be 1, 4 or 8");
+		c->tune.ul_split = (uint32_t)value;
+		c->tune.ul_persistent = 0;
+		drop_graph(c);
+		return MF_OK;
+	}
 	if (!strcmp(key, "tl_tiles")) {
 		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "tl_tiles must be 0 or 1");
 		if (value == 1 && c->ready && !c->tt_ok)
@@ -2851,6 +2867,10 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	if (!c || !key || !value) return MF_ERR_ARG;
 	if (!strcmp(key, "tl_tiles")) {
 		*value = c->tune.tl_tiled;
+		return MF_OK;
+	}
+	if (!strcmp(key, "ul_split")) {
+		*value = c->tune.ul_split;
 		return MF_OK;
 	}
 	if (!strcmp(key, "weak_gp_entries")) {

@@ -90,6 +90,7 @@ struct ULArgs {
 	// persistent, a fixed grid whose blocks pull chunks of `chunk` blocks' worth of
 	// rows from the atomic counter `work` until all rows are done
 	uint32_t block, persistent, grid, chunk;
+	uint32_t split;  // mixed, plain grid: threads per row of the pair pass (1, 4 or 8)
 	uint32_t* work;
 };
 

@@ -658,9 +658,15 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 }
 
 // ---------------------------------------------------------- pair kernel mixed
-template <bool GOD>
+// L threads per row (L = 1: one thread walks the row's whole stencil): lane takes every
+// L-th candidate of each stencil row, the partial sums are added across the L lanes,
+// and lane 0 finishes the row.  L > 1 puts more rows' work in flight when the rows are
+// few (the launch would otherwise cover a handful of SMs); it changes the order of the
+// pair sums, not their terms.
+template <bool GOD, int L = 1>
 __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __restrict__ P,
-                                           const Geom* __restrict__ G, DevStatus* st, uint32_t k) {
+                                           const Geom* __restrict__ G, DevStatus* st, uint32_t k,
+                                           uint32_t lane = 0) {
 	const Rec32* rec = reinterpret_cast<const Rec32*>(a.rec);
 	const Rec32 ri = load_rec(rec + k);
 	uint32_t b = a.rec_body[k];
@@ -693,7 +699,7 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
 		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
-		for (uint32_t kj = j0; kj < j1; kj++) {
+		for (uint32_t kj = j0 + lane; kj < j1; kj += L) {
 			// positions first: most candidates of the stencil lie beyond the reach
 			const float4 head = __ldg(reinterpret_cast<const float4*>(rec + kj));
 			float xij = (ri.x.hi - head.x) + (ri.x.lo - head.y);
@@ -780,6 +786,16 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 			}
 		}
 	}
+	if (L > 1) {
+		const unsigned gmask = ((1u << L) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(L - 1));
+		float* acc[15] = {&Sxx_x, &Sxy_y, &Sxy_x, &Syy_y, &vx_x, &vx_y, &vy_x, &vy_y,
+		                  &av_x, &av_y, &xs_x, &xs_y, &god_rho, &god_vx, &god_vy};
+#pragma unroll
+		for (int q = 0; q < 15; q++)
+#pragma unroll
+			for (int o = L / 2; o > 0; o >>= 1) *acc[q] += __shfl_xor_sync(gmask, *acc[q], o, L);
+		if (lane != 0) return;
+	}
 	float d[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	float rhoi = ri.rho;
 	if (flags & A_STRESS_MGHN) { Sxx_x *= rhoi; Sxy_y *= rhoi; Sxy_x *= rhoi; Syy_y *= rhoi; }
@@ -844,6 +860,16 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 		      isfinite(bq[0][i])))
 			raise(st, ERR_NONFINITE, i);
 	}
+}
+
+// The mixed pair pass with L threads per row (plain grid)
+template <bool GOD, int L>
+__global__ void __launch_bounds__(256, 3) k_pair_split(ULArgs a, const BodyParams* __restrict__ P,
+                                                       const Geom* __restrict__ G, DevStatus* st) {
+	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t k = t / L;
+	if (k >= a.n_total) return;  // a row's L lanes leave together (L divides the warp)
+	pair32_row<GOD, L>(a, P, G, st, k, t % L);
 }
 
 // The pair kernels.  Plain form: one thread per cell-ordered row.  Persistent form
@@ -962,7 +988,17 @@ cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
 		if (e != cudaSuccess) return e;
 	}
 	if (a.ev_pair0) cudaEventRecord(a.ev_pair0, s);
-	if (mixed && (a.flags & (A_GOD_CONT | A_GOD_MOM))) {
+	const bool god = a.flags & (A_GOD_CONT | A_GOD_MOM);
+	if (mixed && !a.persistent && (a.split == 4 || a.split == 8)) {
+		const unsigned g2 = grid1((uint64_t)a.n_total * a.split, bs);
+		if (a.split == 4) {
+			if (god) k_pair_split<true, 4><<<g2, bs, 0, s>>>(a, a.params, a.geom, st);
+			else k_pair_split<false, 4><<<g2, bs, 0, s>>>(a, a.params, a.geom, st);
+		} else {
+			if (god) k_pair_split<true, 8><<<g2, bs, 0, s>>>(a, a.params, a.geom, st);
+			else k_pair_split<false, 8><<<g2, bs, 0, s>>>(a, a.params, a.geom, st);
+		}
+	} else if (mixed && god) {
 		k_pair<true, true><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);
 	} else if (mixed) {
 		k_pair<true><<<grid, bs, 0, s>>>(a, a.params, a.geom, st);

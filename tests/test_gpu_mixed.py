@@ -91,6 +91,26 @@ def test_halo_tiles_match_untiled(case, lib):
             np.testing.assert_array_equal(a[f], b[f], err_msg=f)
 
 
+@pytest.mark.parametrize("split", [4, 8])
+def test_ul_split_rows_match_one_thread_per_row(split, lib):
+    """The mixed UL pair pass with 4 or 8 threads per row adds the same pair terms in
+    another order: after 200 steps through the impact it stays within 1e-6 (relative
+    L2) of one thread per row, and the options read back."""
+    import mfree_iwf_gb300 as M
+    sc = S.c1_rings(dx=1e-3)
+    out = {}
+    for sp in (split, 1):
+        sim = M.from_scenario(sc, precision="mixed")
+        sim.set_option("ul_split", sp)
+        assert sim.get_option("ul_split") == sp
+        sim.step(200)
+        out[sp] = [sim.get_state(k) for k in range(len(sc.bodies))]
+        sim.close()
+    e = errors(sc, out[split], out[1])
+    print(split, {k: f"{v:.2e}" for k, v in e.items()})
+    assert e["velocity"] < 1e-6 and e["displacement"] < 1e-6, e
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_mixed_tl_resume_through_set_state(graph, lib):
     """Mixed TL keeps its packed neighbour records current from pass B; writing the
