@@ -494,7 +494,7 @@ __device__ __forceinline__ void tlB_finish(const TLArgs& a, uint32_t i, const Bo
 	if (a.write_recs) tl_pack_row(a, i, pr, nv[0], nv[1], nv[2], nv[3], nrho, (RecB*)a.recB_out);
 }
 
-__global__ void __launch_bounds__(256) k_tlA32(TLArgs a) {
+__global__ void __launch_bounds__(256, 8) k_tlA32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
