@@ -411,7 +411,7 @@ __global__ void k_weak_pack(WeakArgs a) {
 	pk[2 * j + 1] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
 }
 
-__global__ void __launch_bounds__(256) k_gp_pass32(WeakArgs a) {
+__global__ void __launch_bounds__(256, 8) k_gp_pass32(WeakArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_g) return;
 	const float2* gw = (const float2*)a.g_w;  // gradient times the particle's quad weight
