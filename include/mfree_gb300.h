@@ -299,7 +299,7 @@ MF_API mf_status mf_get_stream(mf_ctx* ctx, void** stream);
  * Allocation-free UL step.  No counterpart in the reference: it exists for callers
  * that must not allocate device memory after start-up (applications that reserve all
  * GPU memory in their own pools, plug-ins that must not trigger the implicit device
- * synchronisation of cudaMalloc/cudaFree, code running while a stream is captured).
+ * synchronisation of cudaMalloc/cudaFree).
  * The caller passes device pointers to one body's particle arrays, updated in place;
  * all scratch of the step lives in one fixed array inside the library, sized for at
  * most MF_NOALLOC_MAX_PARTICLES particles (larger n returns MF_ERR_CAPACITY).  Every

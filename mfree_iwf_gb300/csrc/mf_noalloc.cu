@@ -3,9 +3,8 @@
 //
 // Some callers must not allocate on the device after start-up: applications that
 // reserve all GPU memory up front in their own pools and forbid allocations later,
-// plug-ins that run inside another framework's stream and must not trigger the
-// implicit device-wide synchronisation of cudaMalloc/cudaFree, and code that runs
-// while a stream is being captured, where cudaMalloc is not allowed.  A context
+// and plug-ins that run inside another framework's stream and must not trigger the
+// implicit device-wide synchronisation of cudaMalloc/cudaFree.  A context
 // (mf_create) allocates all of its buffers, so those callers use this entry point
 // instead: the caller passes the particle arrays (device pointers, updated in
 // place), and every buffer of the step -- cell grid, sort keys and radix-sort

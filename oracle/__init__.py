@@ -12,7 +12,6 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 MFO = os.path.join(HERE, "mfo_run")
 REF = os.path.join(HERE, "_ref", "ref_harness")
-REFERENCE_ROOT = "/root/reference"
 
 
 def build_oracle(force: bool = False) -> str:
@@ -26,13 +25,19 @@ def build_oracle(force: bool = False) -> str:
     return MFO
 
 
-def build_ref(force: bool = False) -> str | None:
-    """Compile the reference (only where its sources are present)."""
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
-        return None
+def build_ref(force: bool = False, root: str | None = None) -> str | None:
+    """Compile the reference (only where its sources are present).  The sources' root
+    is `root`, else the environment variable MF_REFERENCE_ROOT, else the default of
+    build_ref.sh; returns None when no sources are found there."""
     if os.path.exists(REF) and not force:
         return REF
-    subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True, capture_output=True)
+    root = root or os.environ.get("MF_REFERENCE_ROOT")
+    cmd = [os.path.join(HERE, "build_ref.sh")] + ([root] if root else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode == 3:  # no reference sources on this machine
+        return None
+    if r.returncode != 0:
+        raise RuntimeError(f"building the reference failed:\n{r.stdout}{r.stderr}")
     return REF
 
 

@@ -7,8 +7,12 @@ set -e
 REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-mkdir -p "$OUT"
 SRC="$REF/src"
+if [ ! -d "$SRC" ]; then
+  echo "no reference sources under $REF"
+  exit 3
+fi
+mkdir -p "$OUT"
 # the Release flags of the reference (Release/src/subdir.mk:41) plus
 # -ffp-contract=off so x86-64 and aarch64 round alike
 FLAGS="-std=c++14 -O3 -w -ffp-contract=off -I$HERE/glm_subset -I$SRC -I$HERE"

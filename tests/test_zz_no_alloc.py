@@ -1,8 +1,8 @@
 """The allocation-free UL step (mf_ul_step_noalloc), called through the C ABI.
 
 It serves callers that cannot allocate device memory once they are running (memory
-reserved up front in their own pools, no implicit synchronisation from cudaMalloc
-allowed, or work issued during stream capture): they hand in device arrays and the
+reserved up front in their own pools, or no implicit synchronisation from cudaMalloc
+allowed): they hand in device arrays and the
 library works in a fixed scratch array of its own.  Checked against the regular
 context-based step (mf_step) on the same body, over two calls in a row, with the
 tolerance of the other FP64-strict parity tests (relative L2 < 1e-9).  The device
@@ -50,8 +50,13 @@ def test_noalloc_step_matches_context_step(lib):
     acts = (ctypes.c_int32 * len(sc.actions))(*sc.actions)
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         st = fn(ctypes.byref(body), ctypes.byref(sd), sc.dt, acts, len(sc.actions), 5, ctypes.c_void_p(stream))
         assert st == 0, M.STATUS.get(st, st)
+        torch.cuda.synchronize()
+        if call > 0:  # the first call loads the kernels; later calls leave free memory as it was
+            assert torch.cuda.mem_get_info()[0] == free0, "the allocation-free step changed free device memory"
         sim.step(5)
         want = sim.get_state(0, FIELDS)
         for f in FIELDS:
