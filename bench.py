@@ -19,8 +19,9 @@ The family workloads (corot, godunov, potential, ulweak, tlweak, tlfem, ulfem) a
 ensembles of the reference's own two-ring set-up of that family (ulweak and ulfem: FP64
 forms only).
 
-With --impl reference it times the CPU implementation of the same path (the oracle
-restatement of the reference, which is single-threaded) on all host cores.
+With --impl reference it times the reference's CPU implementation of the same path
+(single-threaded; the reference's own build where this host has one, else the oracle
+restatement) on all host cores.
 """
 from __future__ import annotations
 
@@ -156,31 +157,42 @@ class ClockSampler:
 
 # ------------------------------------------------------------- CPU baseline
 def cpu_sample(workload_name: str, steps: int, warmup: int, procs: int):
-    """The oracle (CPU restatement of the reference, single-threaded) on a bounded
-    sample of the workload: the same set-up at a coarser lattice.  `procs` copies run
-    concurrently (one per host core); returns particle-steps/s over all of them."""
+    """The reference's CPU implementation of the step on a bounded sample of the
+    workload (the same set-up at a coarser lattice), `procs` single-threaded copies at
+    once (one per host core); returns particle-steps/s over all of them.
+
+    The reference itself (its unmodified sources compiled by oracle/build_ref.sh) runs
+    where it was built on this host; elsewhere the oracle port stands in for it.  On an
+    x86 host where both ran, the reference ran at 0.92x the port's rate on the TL ring
+    set-up and 0.73x on the Gray-Monaghan rings (same cases, one core each)."""
     import oracle
     from mfree_iwf_gb300 import scenarios as S
-    binary = oracle.build_oracle()
     if workload_name in FAMILIES:
         sc = S.family_ensemble(workload_name, 1)
         desc = f"one instance of the ensemble ({S.FAMILY_RING_SETUPS[workload_name]}(81))"
     elif workload_name == "c2":
-        sc = S.c2_rings_tl(dx=4e-4)
-        desc = "same ring-impact TL set-up at dx=0.4 mm"
+        # at dx = 1 mm the workload's neighbour epsilon equals the reference's fixed 1e-6 m^2
+        sc = S.c2_rings_tl(dx=1e-3)
+        desc = "same ring-impact TL set-up at dx=1 mm"
     elif workload_name == "c3":
         sc = S.c3_plate(dx=5e-4)
         desc = "same weak-form plate set-up at dx=0.5 mm"
     else:
         sc = S.c1_rings(dx=1e-3)
         desc = "the ring workload at dx=1 mm"
+    kind, binary = "port", oracle.build_oracle()
+    if sc.nbh_eps == 1e-6 and os.access(oracle.REF, os.X_OK):
+        kind, binary = "reference", oracle.REF
     n = sc.n_total
     with tempfile.TemporaryDirectory() as d:
         case = os.path.join(d, "c.case")
         S.write_case(case, sc, warmup + steps)
         t0 = time.time()
-        ps = [subprocess.Popen([binary, case, os.path.join(d, f"o{k}.out"), str(warmup)],
-                               stdout=subprocess.DEVNULL, stderr=subprocess.PIPE) for k in range(procs)]
+        if kind == "reference":  # the harness times every step; the warm-up steps are timed too
+            cmds = [[binary, "run", case, os.path.join(d, f"o{k}.out")] for k in range(procs)]
+        else:
+            cmds = [[binary, case, os.path.join(d, f"o{k}.out"), str(warmup)] for k in range(procs)]
+        ps = [subprocess.Popen(c, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE) for c in cmds]
         rcs = [p.wait() for p in ps]
         wall = time.time() - t0
         secs = []
@@ -188,11 +200,15 @@ def cpu_sample(workload_name: str, steps: int, warmup: int, procs: int):
             r = S.read_result(os.path.join(d, f"o{k}.out"))
             secs.append(r.seconds)
     if any(rcs):
-        raise RuntimeError("oracle failed")
+        raise RuntimeError(f"{kind} CPU run failed")
+    timed = steps + (warmup if kind == "reference" else 0)
     span = max(secs)
-    value = procs * n * steps / span
-    return value, {"cores": procs, "sample": f"{desc}: {n} particles, {steps} timed steps after {warmup}, "
-                                             f"{procs} concurrent single-threaded runs ({wall:.1f} s wall)",
+    value = procs * n * timed / span
+    what = ("the reference's own sources, compiled here" if kind == "reference" else
+            "the oracle port of the reference (the reference's sources are not on this host)")
+    return value, {"cores": procs, "kind": kind,
+                   "sample": f"{what}; {desc}: {n} particles, {timed} timed steps, "
+                             f"{procs} concurrent single-threaded runs ({wall:.1f} s wall)",
                    "n": n}
 
 
@@ -207,7 +223,7 @@ def reference_arm(args, cfg_desc):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * info["n"] * procs / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": cfg_desc,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": info["kind"],
                          "sample": info["sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -215,15 +231,106 @@ def reference_arm(args, cfg_desc):
 
 
 # ------------------------------------------------------------------ ours
-# DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture:
-# (bytes, rows of the captured launch, where); scaled to the bench's rows per launch.
+# DRAM bytes (read + write) per row of one launch of the dominant kernel, from one ncu
+# capture of that kernel alone (dram__bytes_read.sum + dram__bytes_write.sum) on a
+# smaller case of the same workload; the bench scales it by its own rows per launch.
+# (bytes per row, description of the capture)
 MEASURED_TRAFFIC = {
-    ("c2", "mixed", "TL pass B"): (1218.0e6, 1759324, "profiles/tl_mixed_ring_impact_dx0.05mm.md: ncu "
-                                   "dram__bytes_read.sum + dram__bytes_write.sum, mean of 108 launches"),
-    ("c3", "mixed", "weak TL Gauss-point pass"): (294.24e6, 800000, "profiles/weak_tl_passes_plate.md: ncu "
-                                                  "dram__bytes_read.sum + dram__bytes_write.sum at dx = 0.1 mm "
-                                                  "(800k Gauss points), scaled by the Gauss points"),
+    ("c3", "mixed", "weak TL Gauss-point pass"): (367.8, "ncu, the Gauss-point pass alone at dx = 0.1 mm "
+                                                         "(800k Gauss points), scaled by Gauss points"),
 }
+
+# The survey's idealised algorithmic bytes per particle-step (every per-particle value
+# read or written once per stage, neighbour data served on chip, per-pair weights
+# recomputed on chip): (method, mixed) -> bytes per particle-step.
+SURVEY_BYTES = {("ul", False): 1344.0, ("ul", True): 992.0, ("tl", False): 896.0, ("tl", True): 768.0}
+
+
+def rel_l2(pairs, floor=0.0):
+    """Relative L2 of the first arrays against the second, the norm of the second
+    floored at `floor`."""
+    num = sum(float(np.sum((a - b) ** 2)) for a, b in pairs)
+    den = max(sum(float(np.sum(b ** 2)) for _, b in pairs), floor ** 2)
+    return (num / den) ** 0.5 if den > 0 else num ** 0.5
+
+
+def field_errors(sc, got, want):
+    """Relative L2 error of run `got` against run `want` (each: final states, stresses)
+    per output field over all bodies: displacement (x - X0), velocity, density change
+    (rho - rho_initial, where the method evolves it) and the stress the method
+    evaluates (UL: the state's S; strong-form TL: the nominal stress P).  Density and
+    stress norms are floored at those of a uniform 1e-6 strain (1e-6 rho0, 1e-6 E)."""
+    import mfree_iwf_gb300 as M
+    initial = [b.arrays for b in sc.bodies]
+    n = sc.n_total
+    (sg, pg), (sw, pw) = got, want
+    res = {"x": rel_l2([(a[f] - b0[f], b[f] - b0[f]) for b0, a, b in zip(initial, sg, sw) for f in ("x", "y")]),
+           "v": rel_l2([(a[f], b[f]) for a, b in zip(sg, sw) for f in ("vx", "vy")])}
+    if sc.method == M.METHOD_UL:
+        res["rho"] = rel_l2([(a["rho"] - b0["rho"], b["rho"] - b0["rho"]) for b0, a, b in zip(initial, sg, sw)],
+                            1e-6 * sc.rho0 * n ** 0.5)
+    else:
+        res["rho"] = None  # not evolved by the method (constant, as in the reference)
+    res["S"] = None if pg is None else rel_l2([(a[f], b[f]) for a, b in zip(pg, pw) for f in ("Pxx", "Pxy", "Pyx", "Pyy")],
+                                              1e-6 * sc.E * (4 * n) ** 0.5)
+    return res
+
+
+def run_states(M, sc, precision, steps, device, graph, time_from=None):
+    """Run `steps` steps of a fresh context; returns (final states, stresses) and, when
+    `time_from` is given, particle-steps/s over the steps after that many (after
+    autotuning; CUDA events on the library's stream, graph replay)."""
+    import torch
+    sim = M.from_scenario(sc, precision=precision, device=device, graph=graph)
+    rate = None
+    if time_from is None:
+        sim.step(steps)
+    else:
+        sim.step(1)
+        sim.autotune(1)
+        sim.step(time_from - 1)
+        sim.synchronize()
+        st = torch.cuda.ExternalStream(sim.stream())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        sim.step(steps - time_from)
+        b.record(st)
+        sim.synchronize()
+        torch.cuda.synchronize()
+        rate = sc.n_total * (steps - time_from) / (a.elapsed_time(b) / 1e3)
+    out = [sim.get_state(k) for k in range(len(sc.bodies))]
+    stress = None  # the UL and strong-form TL methods evaluate a per-particle stress
+    if sc.method in (M.METHOD_UL, M.METHOD_TL):
+        stress = [sim.get_stress(k) for k in range(len(sc.bodies))]
+    sim.close()
+    return (out, stress), rate
+
+
+def timed_rate(M, sc, precision, steps, device, graph, tune=True):
+    """particle-steps/s of `steps` timed steps (after set-up, autotuning and 3 warm-up
+    steps) and the per-kernel CUDA-event statistics of two more eager steps."""
+    import torch
+    sim = M.from_scenario(sc, precision=precision, device=device, graph=graph)
+    sim.step(1)
+    if tune:
+        sim.autotune(1)
+    sim.step(3)
+    sim.synchronize()
+    st = torch.cuda.ExternalStream(sim.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    sim.step(steps)
+    b.record(st)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    secs = a.elapsed_time(b) / 1e3
+    sim.set_timing(True)
+    sim.step(2)
+    sim.synchronize()
+    ks = {k: sim.kernel_stats(k) for k in range(6)}
+    sim.close()
+    return sc.n_total * steps / secs, secs / steps, ks
 
 
 def weak_bytes(kind: int, n_p: int, n_g: int, e_g: int, e_t: int) -> float:
@@ -296,6 +403,8 @@ def ours(args, cfg_desc):
     mixed = args.precision == "mixed"
     if args.tl_tiles:
         sim.set_option("tl_tiles", 1)
+    if args.tl_runs is not None and sc.method == M.METHOD_TL and mixed:
+        sim.set_option("tl_runs", args.tl_runs)
     sim.step(1)  # set-up (neighbour search, corrections)
     tune = sim.autotune(args.tune_steps) if not args.no_tune else "off"
     sim.step(args.warmup)
@@ -354,28 +463,66 @@ def ours(args, cfg_desc):
     sim.close()
     del sim
 
-    # ---- the plain FP64 form on the same workload, same run
+    # ---- the plain FP64 form on the same workload, same run, and the per-field error
+    # of the mixed form against it after `err_steps` steps from the same initial state
     forms = None
+    mixed_error = None
     if mixed and not args.no_compare:
-        sim64 = M.from_scenario(sc, precision="fp64", device=local, graph=not args.no_graph)
-        sim64.step(1)
-        if not args.no_tune:
-            sim64.autotune(1)
-        sim64.step(2)
-        sim64.synchronize()
-        k64 = max(2, min(args.steps // 5, 10))
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        st64 = torch.cuda.ExternalStream(sim64.stream())
-        torch.cuda.synchronize()
-        f0.record(st64)
-        sim64.step(k64)
-        f1.record(st64)
-        sim64.synchronize()
-        torch.cuda.synchronize()
-        v64 = n * k64 / (f0.elapsed_time(f1) / 1e3)
-        sim64.close()
-        forms = {"mixed": value / world, "fp64": v64, "mixed_over_fp64": value / world / v64, "fp64_steps": k64}
+        err_steps = args.error_steps
+        want, v64 = run_states(M, sc, "fp64", err_steps, local, not args.no_graph, time_from=min(10, err_steps // 2))
+        got, _ = run_states(M, sc, "mixed", err_steps, local, not args.no_graph)
+        mixed_error = dict(field_errors(sc, got, want), steps=err_steps,
+                           fields="relative L2 over all particles, mixed against FP64 from the same initial "
+                                  "state: x = displacement, v = velocity, rho = density change (null: not evolved "
+                                  "by the method), S = the stress the method evaluates (TL: nominal stress P); "
+                                  "rho and S norms floored at a uniform 1e-6 strain")
+        forms = {"mixed": value / world, "fp64": v64, "mixed_over_fp64": value / world / v64,
+                 "fp64_steps": err_steps - min(10, err_steps // 2)}
+        del want, got
+
+    # ---- the batched ensemble (512 ring impacts, one launch per stage for all of
+    # them): mixed against FP64 on the same ensemble, and the per-field error of the
+    # mixed form after 1000 steps on its first 8 instances
+    batched = None
+    if args.workload == "c2" and not args.no_batched:
+        from mfree_iwf_gb300 import scenarios as S
+        sc4 = S.c4_ensemble(args.instances)
+        vb, sb, ksb = timed_rate(M, sc4, "mixed", args.batched_steps, local, not args.no_graph)
+        vb64, sb64, _ = timed_rate(M, sc4, "fp64", args.batched_steps, local, not args.no_graph)
+        sub = S.c4_ensemble(8)
+        pert = S.c4_ensemble(8)
+        for b in pert.bodies:  # a 1-ulp change of the initial positions: the FP64 form's own spread
+            b.arrays["x"] = np.nextafter(b.arrays["x"], np.inf)
+        want, _ = run_states(M, sub, "fp64", args.error_steps, local, not args.no_graph)
+        got, _ = run_states(M, sub, "mixed", args.error_steps, local, not args.no_graph)
+        ulp, _ = run_states(M, pert, "fp64", args.error_steps, local, not args.no_graph)
+        per_instance = []
+        for k, b in enumerate(sub.bodies):
+            per_instance.append({"particles": b.n, "dx_mm": b.params["dx"] * 1e3, "speed": b.params["speed"],
+                                 "v": rel_l2([(got[0][k][f], want[0][k][f]) for f in ("vx", "vy")]),
+                                 "fp64_1ulp_spread": rel_l2([(ulp[0][k][f], want[0][k][f]) for f in ("vx", "vy")])})
+        well = [r for r in per_instance if r["fp64_1ulp_spread"] <= 1e-12]
+        peaks, _ = measured_peaks()
+        pms, pl, prow = ksb[0]
+        pair = None
+        if pl:
+            t_launch = pms / pl / 1e3
+            pair = {"avg_launch_ms": pms / pl,
+                    "frac_survey_model": SURVEY_BYTES[("ul", True)] / 4 * (prow / pl) / t_launch / 1e9 / peaks["hbm_gbs"]}
+        batched = {"workload": workload_desc("c4", None, args.instances)["workload"], "particles": sc4.n_total,
+                   "instances": args.instances, "steps": args.batched_steps,
+                   "mixed": vb, "fp64": vb64, "mixed_over_fp64": vb / vb64,
+                   "ms_per_step": {"mixed": sb * 1e3, "fp64": sb64 * 1e3},
+                   "step_frac_survey_model": SURVEY_BYTES[("ul", True)] * vb / 1e9 / peaks["hbm_gbs"],
+                   "pair_kernel": pair,
+                   "mixed_error": dict(field_errors(sub, got, want), steps=args.error_steps,
+                                       instances=8, particles=sub.n_total, per_instance=per_instance,
+                                       well_conditioned=len(well),
+                                       v_max_well_conditioned=max((r["v"] for r in well), default=None),
+                                       within_1e4=sum(r["v"] <= 1e-4 for r in per_instance),
+                                       note="well conditioned: the FP64 velocities move by <= 1e-12 under a "
+                                            "1-ulp change of the initial positions")}
+        del want, got
 
     # ---- roofline of the dominant kernel
     peaks, peak_kind = measured_peaks()
@@ -402,16 +549,25 @@ def ours(args, cfg_desc):
         roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,
                 "launches": klaunch, "avg_launch_ms": kms / klaunch,
-                "algorithmic_bytes_per_launch": abytes}
+                "algorithmic_bytes_per_launch": abytes,
+                "byte_model": "itemised: every byte the kernel must move (lists and per-pair weights streamed)"}
+        fam = "tl" if sc.method == M.METHOD_TL else "ul" if sc.method == M.METHOD_UL else None
+        if fam is not None:
+            per_ps = SURVEY_BYTES[(fam, mixed)]
+            # the survey's bytes of one stage (a quarter of a particle-step) per launch,
+            # and of the whole step
+            roof["survey_bytes_per_particle_step"] = per_ps
+            roof["frac_survey_model"] = per_ps / 4 * per_launch_rows / (kms / klaunch / 1e3) / 1e9 / peaks["hbm_gbs"]
+            roof["step_frac_survey_model"] = per_ps * value / world / 1e9 / peaks["hbm_gbs"]
         t = MEASURED_TRAFFIC.get((args.workload, args.precision, names[dom]))
         if t is not None:
-            roof["traffic"] = t[0] * per_launch_rows / t[1]
-            roof["traffic_source"] = t[2]
+            roof["traffic"] = t[0] * per_launch_rows
+            roof["traffic_source"] = t[1]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             cv, info = cpu_sample(args.workload, args.cpu_steps, 1, 1)
-            cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": info["sample"]}
+            cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": info["kind"], "sample": info["sample"]}
         except Exception as e:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
     if rank == 0:
@@ -427,7 +583,7 @@ def ours(args, cfg_desc):
                     "steps": k2},
             "roofline": roof, "cpu_baseline": cpu,
             "kernels_ms": {names[k]: v[0] for k, v in kstats.items() if v[1]},
-            "forms": forms, "autotune": tune,
+            "forms": forms, "mixed_error": mixed_error, "batched": batched, "autotune": tune,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -443,7 +599,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", *FAMILIES])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64_strict"])
     ap.add_argument("--dx", type=float, default=None)
-    ap.add_argument("--cpu-steps", type=int, default=150)
+    ap.add_argument("--cpu-steps", type=int, default=600)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-graph", action="store_true")
@@ -451,7 +607,12 @@ def main():
     ap.add_argument("--tune-steps", type=int, default=3)
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--tl-tiles", action="store_true", help="mixed TL: the shared-memory halo-tile passes")
+    ap.add_argument("--tl-runs", type=int, choices=[0, 1], default=None,
+                    help="mixed TL: 1 = run-walk passes (gradients recomputed on chip), 0 = streamed lists")
     ap.add_argument("--instances", type=int, default=512, help="c4: ring impacts in the ensemble")
+    ap.add_argument("--error-steps", type=int, default=1000, help="steps of the mixed-against-FP64 error runs")
+    ap.add_argument("--batched-steps", type=int, default=20, help="timed steps of the batched ensemble block")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched ensemble block (c2 only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

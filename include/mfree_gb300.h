@@ -51,7 +51,9 @@ enum {
 	MF_ERR_NO_DEVICE = -9,     /* no CUDA device */
 	MF_ERR_SINGULAR = -10,     /* singular corrector matrix (precomp_shape_functions.h:45) */
 	MF_ERR_NO_NEIGHBOR = -11,  /* a particle without neighbours (grid.h:168) */
-	MF_ERR_CAPACITY = -12      /* a size beyond a documented maximum */
+	MF_ERR_CAPACITY = -12,     /* a size beyond a documented maximum */
+	MF_ERR_BODY_FAILED = -13   /* with per-body masking: some bodies failed and are frozen, the
+	                              others stepped on (which: mf_get_failed) */
 };
 
 /* Method families (the reference's particle types). */
@@ -226,6 +228,27 @@ MF_API mf_status mf_get_state_all(mf_ctx* ctx, const mf_state* out);
 MF_API mf_status mf_set_state_all(mf_ctx* ctx, const mf_particles* p);
 MF_API mf_status mf_get_time(mf_ctx* ctx, int32_t body, double* t);
 MF_API mf_status mf_num_particles(mf_ctx* ctx, int32_t body, uint32_t* n);
+/* The stress the method evaluates at a body's current state, per particle.  TL (strong
+ * form): the nominal stress P = J F^-1 sigma that derive_stress_tl consumes
+ * (cont_mech.h:154-169), evaluated on the current state -- the reference keeps TL
+ * stresses in per-stage particle copies only, and its state's Sxx, Sxy, Syy stay at
+ * their initial values; UL: the state's S (Pxy = Pyx = Sxy).  Other methods return
+ * MF_ERR_STATE. */
+MF_API mf_status mf_get_stress(mf_ctx* ctx, int32_t body, double* Pxx, double* Pxy, double* Pyx, double* Pyy);
+/* The weak TL form's Gauss-point state (rho, Sxx, Sxy, Syy; NULL fields skipped), the
+ * bodies' points concatenated in id order; *n_out = number of Gauss points (all NULL:
+ * only the count).  The particles' own rho and S are not evolved by this form. */
+/* Per-body failure words of an updated-Lagrangian context (0: running; otherwise the
+ * bits of what failed it: 1 neighbour capacity, 2 no neighbour, 4 cell grid, 8
+ * non-finite state).  Bodies fail alone only with the option "mask_failed" set
+ * (mf_set_option): then a NaN, a neighbour overflow or a grid error in one body freezes
+ * that body -- its rows leave the grid and the pair pass -- while the others step on
+ * unchanged, and mf_step returns MF_ERR_BODY_FAILED instead of failing the whole step.
+ * The reference aborts the process instead (assert, grid.h:167-168).  No counterpart
+ * in the reference. */
+MF_API mf_status mf_get_failed(mf_ctx* ctx, uint32_t* flags, uint32_t n_bodies);
+MF_API mf_status mf_get_gauss_state(mf_ctx* ctx, double* rho, double* Sxx, double* Sxy, double* Syy, uint32_t cap,
+                                    uint32_t* n_out);
 
 /* Neighbour lists of a body's current state, as particle indices within the body:
  * for MF_METHOD_UL those of the next first-stage grid (grid.h:117-177), for TL the

@@ -32,7 +32,7 @@ BC_VELOCITY = 2   # tensile.cpp:44-66, UL bodies
 STATUS = {
     0: "MF_OK", -1: "MF_ERR_ARG", -2: "MF_ERR_CUDA", -3: "MF_ERR_NBH_OVERFLOW", -4: "MF_ERR_NONFINITE",
     -5: "MF_ERR_TIMEOUT", -6: "MF_ERR_PIPELINE", -7: "MF_ERR_GRID", -8: "MF_ERR_STATE", -9: "MF_ERR_NO_DEVICE",
-    -10: "MF_ERR_SINGULAR", -11: "MF_ERR_NO_NEIGHBOR", -12: "MF_ERR_CAPACITY",
+    -10: "MF_ERR_SINGULAR", -11: "MF_ERR_NO_NEIGHBOR", -12: "MF_ERR_CAPACITY", -13: "MF_ERR_BODY_FAILED",
 }
 
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -83,6 +83,18 @@ class MfError(RuntimeError):
 _lib = None
 
 
+ERR_BODY_FAILED = -13
+
+
+class BodyFailed(MfError):
+    """mf_step with per-body masking: some bodies failed and are frozen; the others
+    stepped on.  `failed` holds every body's failure word."""
+
+    def __init__(self, status: int, msg: str, failed: np.ndarray):
+        super().__init__(status, msg)
+        self.failed = failed
+
+
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     """Load the CUDA library (raises OSError if it has not been built)."""
     global _lib
@@ -117,6 +129,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_set_state_all": (C.c_int32, [C.c_void_p, C.POINTER(MfParticles)]),
         "mf_get_time": (C.c_int32, [C.c_void_p, C.c_int32, _DP]),
         "mf_num_particles": (C.c_int32, [C.c_void_p, C.c_int32, _UP]),
+        "mf_get_stress": (C.c_int32, [C.c_void_p, C.c_int32, _DP, _DP, _DP, _DP]),
+        "mf_get_failed": (C.c_int32, [C.c_void_p, _UP, C.c_uint32]),
+        "mf_get_gauss_state": (C.c_int32, [C.c_void_p, _DP, _DP, _DP, _DP, C.c_uint32, _UP]),
         "mf_get_neighbors": (C.c_int32, [C.c_void_p, C.c_int32, _UP, _UP, C.c_uint64, C.POINTER(C.c_uint64)]),
         "mf_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
         "mf_kernel_stats": (C.c_int32, [C.c_void_p, C.c_int32, _DP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
@@ -286,7 +301,20 @@ class Simulation:
 
     # -- stepping (mfree_iwf.cpp:84-97)
     def step(self, nsteps: int = 1) -> None:
-        self._check(self._lib.mf_step(self._h, int(nsteps)), "mf_step")
+        """Advance every body by nsteps RK4 steps.  With the option "mask_failed" set, a
+        body that fails (NaN, neighbour overflow, grid error) is frozen while the others
+        step on, and BodyFailed (an MfError) is raised after the steps; failed() names
+        the bodies."""
+        st = self._lib.mf_step(self._h, int(nsteps))
+        if st == ERR_BODY_FAILED:
+            raise BodyFailed(st, self._lib.mf_last_error(self._h).decode(), self.failed())
+        self._check(st, "mf_step")
+
+    def failed(self) -> np.ndarray:
+        """Per-body failure words (0: running; else the ERR bits that failed it)."""
+        out = np.zeros(self.n_bodies, np.uint32)
+        self._check(self._lib.mf_get_failed(self._h, out.ctypes.data_as(_UP), self.n_bodies), "mf_get_failed")
+        return out
 
     def synchronize(self) -> None:
         self._check(self._lib.mf_synchronize(self._h), "mf_synchronize")
@@ -323,6 +351,25 @@ class Simulation:
         cols = {f: (None if arrays.get(f) is None else np.ascontiguousarray(arrays[f], np.float64)) for f in _PFIELDS}
         p = MfParticles(*[_dptr(cols[f]) for f in _PFIELDS])
         self._check(self._lib.mf_set_state_all(self._h, ctypes.byref(p)), "mf_set_state_all")
+
+    def get_stress(self, body: int) -> Dict[str, np.ndarray]:
+        """The stress the method evaluates at the body's current state: TL (strong form)
+        the nominal stress P = J F^-1 sigma, UL the state's S (Pxy = Pyx = Sxy)."""
+        n = self.num_particles(body)
+        out = {k: np.empty(n, np.float64) for k in ("Pxx", "Pxy", "Pyx", "Pyy")}
+        self._check(self._lib.mf_get_stress(self._h, body, *[_dptr(out[k]) for k in ("Pxx", "Pxy", "Pyx", "Pyy")]),
+                    "mf_get_stress")
+        return out
+
+    def get_gauss_state(self) -> Dict[str, np.ndarray]:
+        """The weak TL form's Gauss-point state (rho, Sxx, Sxy, Syy), all bodies."""
+        n = ctypes.c_uint32()
+        self._check(self._lib.mf_get_gauss_state(self._h, None, None, None, None, 0, ctypes.byref(n)),
+                    "mf_get_gauss_state")
+        out = {k: np.empty(n.value, np.float64) for k in ("rho", "Sxx", "Sxy", "Syy")}
+        self._check(self._lib.mf_get_gauss_state(self._h, *[_dptr(out[k]) for k in ("rho", "Sxx", "Sxy", "Syy")],
+                                                 n.value, ctypes.byref(n)), "mf_get_gauss_state")
+        return out
 
     def time(self, body: int = 0) -> float:
         t = ctypes.c_double()

@@ -197,6 +197,8 @@ struct Tune {
 	uint32_t ul_block = 128, ul_persistent = 0, ul_chunk = 1, tl_block = 128;
 	uint32_t ul_split = 1;  // mixed UL, plain grid: threads per row of the pair pass
 	uint32_t tl_tiled = 0;  // mixed TL: the halo-tile passes (built at set-up when requested)
+	uint32_t tl_runs = 1;   // mixed TL: the run-walk passes (gradients recomputed on chip)
+	uint32_t tl_unroll = 1; // run walk: pairs per loop iteration (1, 2: the same results)
 };
 std::mutex g_tune_mutex;
 std::map<std::string, Tune> g_tune_cache;
@@ -247,6 +249,11 @@ struct mf_ctx {
 	DevBuf<float2> tt_sw, tt_swA;
 	uint32_t tt_n_tiles = 0, tt_halo_max = 0, tt_ent_max = 0;
 	bool tt_ok = false;
+	// mixed TL run walk (TLArgs::r_sl, r_cnt, runs, XF, G)
+	DevBuf<uint32_t> rw_sl, rw_runs;
+	DevBuf<uint16_t> rw_cnt;
+	DevBuf<float4> rw_XF, rw_G;
+	bool rw_ok = false;
 	DevBuf<float> qw32, m32, h32;
 	DevBuf<float4> recA, recB, dA32;
 	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
@@ -257,6 +264,9 @@ struct mf_ctx {
 	DevBuf<float> cm_sW;
 	DevBuf<float4> cm_U, cm_X, cm_V, cm_P, cm_R, cm_H;
 	bool tl_recs_valid = false;       // the stage-0 records match the state (pass B keeps them current)
+	// UL: per-body failure words (ERR_* bits); used by the kernels when mask_failed is set
+	DevBuf<uint32_t> failed;
+	bool mask_failed = false;
 	uint32_t n_bc = 0;
 
 	// TL_WEAK: Gauss points and the three list sets (sliced ELL)
@@ -450,6 +460,7 @@ ULArgs ul_args(mf_ctx* c, uint32_t stage) {
 	a.split = c->tune.ul_split;
 	a.grid = (uint32_t)std::max(1, c->sm_count) * (2048u / c->tune.ul_block);
 	a.work = c->work.p;
+	a.failed = c->mask_failed ? c->failed.p : nullptr;
 	return a;
 }
 
@@ -520,6 +531,24 @@ mf_status check_status(mf_ctx* c) {
 	return fail(c, MF_ERR_CUDA, "device status 0x%x", s.flags);
 }
 
+// With per-body masking: MF_ERR_BODY_FAILED while any body has failed (the others
+// have stepped on), else MF_OK.
+mf_status failed_status(mf_ctx* c) {
+	if (!c->mask_failed || !c->ready) return MF_OK;
+	const uint32_t nb = (uint32_t)c->bodies.size();
+	std::vector<uint32_t> f(nb);
+	CK(cudaMemcpy(f.data(), c->failed.p, (size_t)nb * 4, cudaMemcpyDeviceToHost));
+	uint32_t cnt = 0, first = nb;
+	for (uint32_t b = 0; b < nb; b++)
+		if (f[b]) {
+			cnt++;
+			if (first == nb) first = b;
+		}
+	if (!cnt) return MF_OK;
+	return fail(c, MF_ERR_BODY_FAILED, "%u of %u bodies failed and are frozen (first: body %u, flags 0x%x)", cnt, nb,
+	            first, f[first]);
+}
+
 // ---------------------------------------------------------------- set-up
 mf_status finalize(mf_ctx* c) {
 	if (c->ready) return MF_OK;
@@ -561,6 +590,8 @@ mf_status finalize(mf_ctx* c) {
 	for (size_t b = 0; b < c->bodies.size(); b++)
 		for (uint32_t i = 0; i < c->bodies[b].n; i++) bof[c->bodies[b].off + i] = (uint32_t)b;
 	CK(cudaMemcpy(c->body_of.p, bof.data(), n * 4, cudaMemcpyHostToDevice));
+	CK(c->failed.alloc(c->bodies.size()));
+	CK(cudaMemset(c->failed.p, 0, c->bodies.size() * 4));
 
 	auto upload = [&](DevBuf<double>& d, int field) -> mf_status {
 		CK(d.alloc(n));
@@ -685,6 +716,62 @@ uint32_t morton_spread(uint32_t v) {
 	v = (v | (v << 2)) & 0x33333333u;
 	v = (v | (v << 1)) & 0x55555555u;
 	return v;
+}
+
+// Mixed TL run walk: every row's list (ascending j, CSR `off` / c->nbr) as runs of
+// consecutive rows, one word each (first row | (length - 1) << TL_RUN_SHIFT, at most
+// TL_RUN_MAX_LEN rows per word), in sliced ELL; the reference positions as float-float
+// pairs.  The rows' corrections (rw_G) come from the Randles-Libersky set-up.
+mf_status build_tl_runs(mf_ctx* c, const std::vector<uint32_t>& off) {
+	const uint32_t n = c->n_total;
+	std::vector<uint32_t> nb(off[n]);
+	if (off[n]) CK(cudaMemcpy(nb.data(), c->nbr.p, (size_t)off[n] * 4, cudaMemcpyDeviceToHost));
+	std::vector<uint32_t> words;
+	std::vector<uint32_t> roff(n + 1, 0);
+	words.reserve(off[n] / 2 + n);
+	for (uint32_t i = 0; i < n; i++) {
+		roff[i] = (uint32_t)words.size();
+		uint32_t q = off[i];
+		while (q < off[i + 1]) {
+			uint32_t j0 = nb[q], len = 1;
+			while (q + len < off[i + 1] && len < TL_RUN_MAX_LEN && nb[q + len] == j0 + len) len++;
+			words.push_back(j0 | ((len - 1) << TL_RUN_SHIFT));
+			q += len;
+		}
+		if (words.size() - roff[i] > 0xffffu) return fail(c, MF_ERR_CAPACITY, "more than 65535 runs in one list");
+	}
+	roff[n] = (uint32_t)words.size();
+	const uint32_t ns = (n + 31) / 32;
+	std::vector<uint32_t> sl(ns + 1, 0);
+	uint64_t ent = 0;
+	for (uint32_t s_ = 0; s_ < ns; s_++) {
+		uint32_t w = 0;
+		for (uint32_t r = 32 * s_; r < std::min(n, 32 * s_ + 32); r++) w = std::max(w, roff[r + 1] - roff[r]);
+		sl[s_] = (uint32_t)ent;
+		ent += 32ull * w;
+	}
+	if (ent > 0xffffffffull) return fail(c, MF_ERR_CAPACITY, "more than 2^32 sliced-ELL run entries");
+	sl[ns] = (uint32_t)ent;
+	std::vector<uint32_t> sell(std::max<uint64_t>(ent, 1), 0);
+	std::vector<uint16_t> cnt(n);
+	for (uint32_t i = 0; i < n; i++) {
+		cnt[i] = (uint16_t)(roff[i + 1] - roff[i]);
+		uint64_t base = sl[i >> 5] + (i & 31u);
+		for (uint32_t k = 0; k < cnt[i]; k++) sell[base + 32ull * k] = words[roff[i] + k];
+	}
+	CK(c->rw_sl.alloc(ns + 1));
+	CK(c->rw_cnt.alloc(n));
+	CK(c->rw_runs.alloc(sell.size()));
+	CK(c->rw_XF.alloc(n));
+	CK(cudaMemcpy(c->rw_sl.p, sl.data(), (ns + 1) * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->rw_cnt.p, cnt.data(), (size_t)n * 2, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->rw_runs.p, sell.data(), sell.size() * 4, cudaMemcpyHostToDevice));
+	// the positions the Randles-Libersky set-up used (the set-up state)
+	cudaError_t e = mf_fast::tl_ref_positions(n, c->sd[0][0].p, c->sd[0][1].p, c->rw_XF.p, c->stream);
+	if (e != cudaSuccess) return cuda_fail(c, e, "reference positions");
+	CK(cudaStreamSynchronize(c->stream));
+	c->rw_ok = true;
+	return MF_OK;
 }
 
 mf_status build_tl_tiles(mf_ctx* c, const std::vector<uint32_t>& off) {
@@ -833,6 +920,14 @@ TLArgs tl_args(mf_ctx* c) {
 	a.n_bc = c->n_bc;
 	a.status = c->d_status;
 	a.block = c->tune.tl_block;
+	if (c->mixed && c->rw_ok && c->tune.tl_runs) {
+		a.r_sl = c->rw_sl.p;
+		a.r_cnt = c->rw_cnt.p;
+		a.runs = c->rw_runs.p;
+		a.XF = c->rw_XF.p;
+		a.G = c->rw_G.p;
+		a.unroll = c->tune.tl_unroll;
+	}
 	if (c->mixed && c->tt_ok && c->tune.tl_tiled) {
 		a.t_rows = c->tt_rows.p;
 		a.t_halo_off = c->tt_halo_off.p;
@@ -1069,6 +1164,9 @@ mf_status tl_setup(mf_ctx* c) {
 	const double* rho64 = c->mixed ? rho_tmp.p : c->sd[0][4].p;
 	const float* rho32 = nullptr;
 	const bool corot = c->cfg.method == MF_METHOD_COROT, potential = c->cfg.method == MF_METHOD_POTENTIAL;
+	// mixed TL: the run-walk passes (their run words address rows below 2^27)
+	const bool run_walk = c->mixed && !corot && !potential && n < TL_RUN_MAX_ROWS;
+	c->rw_ok = false;
 	DevBuf<double> w64;  // corotational: the kernel values of the pairs (precomp_sph)
 	cudaError_t e;
 	if (corot) {
@@ -1079,10 +1177,12 @@ mf_status tl_setup(mf_ctx* c) {
 		                                c->wx64.p, c->wy64.p, c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "precomp_sph");
 	} else {
+		if (run_walk) CK(c->rw_G.alloc(n));
 		e = c->strict ? mf_strict::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64, rho32,
-		                                 c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream)
+		                                 c->h.p, c->wx64.p, c->wy64.p, nullptr, c->d_status, c->stream)
 		              : mf_fast::tl_rl(n, c->nbr_off.p, c->nbr.p, c->sd[0][0].p, c->sd[0][1].p, c->m.p, rho64, rho32,
-		                               c->h.p, c->wx64.p, c->wy64.p, c->d_status, c->stream);
+		                               c->h.p, c->wx64.p, c->wy64.p, run_walk ? (void*)c->rw_G.p : nullptr, c->d_status,
+		                               c->stream);
 		if (e != cudaSuccess) return cuda_fail(c, e, "tl_rl");
 	}
 	st = check_status(c);
@@ -1150,6 +1250,7 @@ mf_status tl_setup(mf_ctx* c) {
 	c->wx64.free();
 	c->wy64.free();
 	if (c->mixed && !fam && c->tune.tl_tiled && (st = build_tl_tiles(c, off)) != MF_OK) return st;
+	if (run_walk && (st = build_tl_runs(c, off)) != MF_OK) return st;
 	if (c->mixed) {
 		CK(c->recA.alloc(n)); CK(c->recB.alloc(4 * (size_t)n)); CK(c->recB2.alloc(4 * (size_t)n)); CK(c->dA32.alloc(n));
 		c->tl_recs_valid = false;
@@ -2028,6 +2129,8 @@ mf_ctx::~mf_ctx() {
 	}
 	tt_rows.free(); tt_halo_off.free(); tt_halo.free(); tt_sl.free(); tt_cnt.free(); tt_loc.free(); tt_sw.free();
 	tt_swA.free();
+	rw_sl.free(); rw_runs.free(); rw_cnt.free(); rw_XF.free(); rw_G.free();
+	failed.free();
 	DevBuf<uint32_t>* u32s[] = {&nbr_off, &nbr, &bc_rows, &bnd_rows, &bnd_start, &bnd_len, &tile_first, &tile_end,
 	                            &slave_rows, &slave_master, &m_tile_off, &m_tile_n};
 	for (auto* p : u32s) p->free();
@@ -2060,6 +2163,7 @@ MF_API const char* mf_status_string(mf_status s) {
 	case MF_ERR_SINGULAR: return "singular corrector matrix";
 	case MF_ERR_NO_NEIGHBOR: return "particle without neighbours";
 	case MF_ERR_CAPACITY: return "size beyond the documented maximum";
+	case MF_ERR_BODY_FAILED: return "some bodies failed (masked; the others stepped on)";
 	}
 	return "unknown status";
 }
@@ -2335,7 +2439,8 @@ MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
 		}
 		for (auto& b : c->bodies) b.time += b.dt;  // rk4.h:107 (each body's own clock)
 	}
-	return check_status(c);
+	if ((st = check_status(c)) != MF_OK) return st;
+	return failed_status(c);
 }
 
 MF_API mf_status mf_synchronize(mf_ctx* c) {
@@ -2554,6 +2659,95 @@ MF_API mf_status mf_set_state_all(mf_ctx* c, const mf_particles* p) {
 	return MF_OK;
 }
 
+// The stress the method evaluates at the body's current state.  TL (strong form):
+// pass A once more on the current state -- the displacement gradient, Green-St Venant
+// and the nominal stress P = J F^-1 sigma (derivatives.h:101-149, material.h:132-161,
+// cont_mech.h:154-169) -- into the per-stage scratch the next step rewrites anyway;
+// UL: the state's stress S (P_xy = P_yx = S_xy).
+MF_API mf_status mf_get_stress(mf_ctx* c, int32_t body, double* Pxx, double* Pxy, double* Pyx, double* Pyy) {
+	if (!c || !Pxx || !Pxy || !Pyx || !Pyy) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "no body %d", body);
+	const HostBody& b = c->bodies[body];
+	if (c->cfg.method == MF_METHOD_UL) {
+		mf_state o{};
+		o.Sxx = Pxx; o.Sxy = Pxy; o.Syy = Pyy;
+		if ((st = mf_get_state(c, body, &o)) != MF_OK) return st;
+		std::copy(Pxy, Pxy + b.n, Pyx);
+		return MF_OK;
+	}
+	if (c->cfg.method != MF_METHOD_TL)
+		return fail(c, MF_ERR_STATE, "the stress evaluation covers the UL and the strong-form TL methods");
+	CK(cudaSetDevice(c->cfg.device));
+	TLArgs a = tl_args(c);
+	a.stage = 0;
+	a.recB = c->recB.p;  // stage 0 reads set 2 and (mixed) the first record buffer
+	cudaError_t e;
+	if (c->mixed && (c->n_bc || !c->tl_recs_valid) && (e = tl_launch(c, a, 1)) != cudaSuccess)
+		return cuda_fail(c, e, "tl pack");
+	if ((e = tl_launch(c, a, 2)) != cudaSuccess) return cuda_fail(c, e, "tl pass A");
+	const uint32_t n = b.n, o = b.off;
+	double* out[4] = {Pxx, Pxy, Pyx, Pyy};
+	if (c->mixed) {  // P is the records' first field array (float4 per row)
+		std::vector<float> h(4 * (size_t)n);
+		CK(cudaMemcpyAsync(h.data(), c->recB.p + o, 16ull * n, cudaMemcpyDeviceToHost, c->stream));
+		CK(cudaStreamSynchronize(c->stream));
+		for (uint32_t i = 0; i < n; i++)
+			for (int k = 0; k < 4; k++) out[k][i] = h[4 * (size_t)i + k];
+	} else {
+		for (int k = 0; k < 4; k++)
+			CK(cudaMemcpyAsync(out[k], c->P64.p + (size_t)k * c->n_total + o, (size_t)n * 8, cudaMemcpyDeviceToHost,
+			                   c->stream));
+		CK(cudaStreamSynchronize(c->stream));
+	}
+	return check_status(c);
+}
+
+// The weak TL form's Gauss-point state (rho, Sxx, Sxy, Syy) of every body, the bodies'
+// points concatenated in id order.
+MF_API mf_status mf_get_gauss_state(mf_ctx* c, double* rho, double* Sxx, double* Sxy, double* Syy, uint32_t cap,
+                                    uint32_t* n_out) {
+	if (!c || !n_out) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if (c->cfg.method != MF_METHOD_TL_WEAK) return fail(c, MF_ERR_STATE, "Gauss points belong to the weak TL form");
+	const uint32_t ng = c->n_g;
+	*n_out = ng;
+	if (!rho && !Sxx && !Sxy && !Syy) return MF_OK;
+	if (cap < ng) return fail(c, MF_ERR_ARG, "capacity %u below the %u Gauss points", cap, ng);
+	CK(cudaSetDevice(c->cfg.device));
+	CK(cudaStreamSynchronize(c->stream));
+	double* out[4] = {rho, Sxx, Sxy, Syy};
+	if (c->mixed) {
+		std::vector<uint32_t> gb(ng);
+		CK(cudaMemcpy(gb.data(), c->gp_body.p, (size_t)ng * 4, cudaMemcpyDeviceToHost));
+		std::vector<float> h(ng);
+		for (int q = 0; q < 4; q++) {
+			if (!out[q]) continue;
+			CK(cudaMemcpy(h.data(), c->gsf[0][q].p, (size_t)ng * 4, cudaMemcpyDeviceToHost));
+			for (uint32_t g = 0; g < ng; g++)  // the mixed form keeps rho - rho0
+				out[q][g] = (double)h[g] + (q == 0 ? c->bodies[gb[g]].sd.rho0 : 0.);
+		}
+	} else {
+		for (int q = 0; q < 4; q++)
+			if (out[q]) CK(cudaMemcpy(out[q], c->gsd[0][q].p, (size_t)ng * 8, cudaMemcpyDeviceToHost));
+	}
+	return check_status(c);
+}
+
+MF_API mf_status mf_get_failed(mf_ctx* c, uint32_t* flags, uint32_t n_bodies) {
+	if (!c || !flags) return MF_ERR_ARG;
+	if (n_bodies < c->bodies.size()) return fail(c, MF_ERR_ARG, "room for %u of %zu bodies", n_bodies, c->bodies.size());
+	if (!c->ready) {
+		std::fill(flags, flags + c->bodies.size(), 0u);
+		return MF_OK;
+	}
+	CK(cudaStreamSynchronize(c->stream));
+	CK(cudaMemcpy(flags, c->failed.p, c->bodies.size() * 4, cudaMemcpyDeviceToHost));
+	return MF_OK;
+}
+
 MF_API mf_status mf_get_time(mf_ctx* c, int32_t body, double* t) {
 	if (!c || !t) return MF_ERR_ARG;
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
@@ -2697,6 +2891,7 @@ mf_status snapshot_take(mf_ctx* c, Snapshot& s) {
 				return st;
 	if ((st = add(c->fcx.p, (size_t)n * 8)) || (st = add(c->fcy.p, (size_t)n * 8))) return st;
 	if ((st = add(c->params.p, c->h_params.size() * sizeof(BodyParams)))) return st;
+	if ((st = add(c->failed.p, c->bodies.size() * 4))) return st;  // trial steps may fail a body
 	for (auto& b : c->bodies) s.times.push_back(b.time);
 	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
@@ -2732,7 +2927,8 @@ std::string tune_key(mf_ctx* c) {
 		}
 	int hb = hn ? (int)std::floor(std::log2(std::max(hsum / (double)hn, 1e-12))) : 0;
 	char k[128];
-	snprintf(k, sizeof k, "m%d p%d n2^%d h2^%d", c->cfg.method, c->cfg.precision, bucket, hb);
+	// (the mixed TL form also by its pass family: the run walk or the streamed lists)
+	snprintf(k, sizeof k, "m%d p%d n2^%d h2^%d r%u", c->cfg.method, c->cfg.precision, bucket, hb, c->tune.tl_runs);
 	return k;
 }
 
@@ -2785,7 +2981,12 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		} else {
 			t.tl_block = bs;
 			t.tl_tiled = 0;
-			cands.push_back(t);
+			// (tl_runs stays as set: it changes results in the last FP32 bits; the
+			// unroll factor of the run walk does not)
+			for (uint32_t u : {1u, 2u}) {
+				t.tl_unroll = u;
+				if (u == 1 || (c->cfg.method == MF_METHOD_TL && c->mixed && c->rw_ok && t.tl_runs)) cands.push_back(t);
+			}
 		}
 	}
 	if (c->cfg.method == MF_METHOD_TL && c->mixed && c->tt_ok) {
@@ -2815,8 +3016,8 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		float ms = 0.f;
 		cudaEventElapsedTime(&ms, e0, e1);
 		double per = ms / trial_steps;
-		snprintf(line, sizeof line, "%s[b%u p%u c%u s%u tl%u t%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block,
-		         t.ul_persistent, t.ul_chunk, t.ul_split, t.tl_block, t.tl_tiled, per);
+		snprintf(line, sizeof line, "%s[b%u p%u c%u s%u tl%u t%u r%u u%u]=%.4fms", rep.empty() ? "" : " ", t.ul_block,
+		         t.ul_persistent, t.ul_chunk, t.ul_split, t.tl_block, t.tl_tiled, t.tl_runs, t.tl_unroll, per);
 		rep += line;
 		if (per < best) {
 			best = per;
@@ -2836,8 +3037,9 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
 		g_tune_cache[key] = best_t;
 	}
-	snprintf(line, sizeof line, " -> b%u p%u c%u s%u tl%u t%u (%s)", best_t.ul_block, best_t.ul_persistent,
-	         best_t.ul_chunk, best_t.ul_split, best_t.tl_block, best_t.tl_tiled, key.c_str());
+	snprintf(line, sizeof line, " -> b%u p%u c%u s%u tl%u t%u r%u u%u (%s)", best_t.ul_block, best_t.ul_persistent,
+	         best_t.ul_chunk, best_t.ul_split, best_t.tl_block, best_t.tl_tiled, best_t.tl_runs, best_t.tl_unroll,
+	         key.c_str());
 	rep += line;
 	if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
 	return MF_OK;
@@ -2857,6 +3059,20 @@ MF_API mf_status mf_set_option(mf_ctx* c, const char* key, int64_t value) {
 		if (value == 1 && c->ready && !c->tt_ok)
 			return fail(c, MF_ERR_STATE, "tl_tiles: the halo tiles are built at set-up; set the option before the first step");
 		c->tune.tl_tiled = (uint32_t)value;
+		drop_graph(c);
+		return MF_OK;
+	}
+	if (!strcmp(key, "mask_failed")) {
+		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "mask_failed must be 0 or 1");
+		if (value && c->cfg.method != MF_METHOD_UL)
+			return fail(c, MF_ERR_PIPELINE, "per-body failure masking covers the updated-Lagrangian method");
+		c->mask_failed = value != 0;
+		drop_graph(c);
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_runs")) {
+		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "tl_runs must be 0 or 1");
+		c->tune.tl_runs = (uint32_t)value;
 		drop_graph(c);
 		return MF_OK;
 	}
@@ -2883,6 +3099,18 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	}
 	if (!strcmp(key, "weak_gauss_points")) {
 		*value = c->n_g;
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_runs")) {
+		*value = c->tune.tl_runs;
+		return MF_OK;
+	}
+	if (!strcmp(key, "mask_failed")) {
+		*value = c->mask_failed ? 1 : 0;
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_runs_built")) {
+		*value = c->rw_ok ? 1 : 0;
 		return MF_OK;
 	}
 	if (!strcmp(key, "tl_tiles_built")) {

@@ -92,6 +92,10 @@ struct ULArgs {
 	uint32_t block, persistent, grid, chunk;
 	uint32_t split;  // mixed, plain grid: threads per row of the pair pass (1, 4 or 8)
 	uint32_t* work;
+	// per-body failure words (ERR_* bits), device; nullptr: an error of any row fails the
+	// whole step.  When set, a row's error marks its body failed instead, and a failed
+	// body's rows are left out of the grid and the pair pass from then on (frozen).
+	uint32_t* failed;
 };
 
 // Neighbour search of the total-Lagrangian set-up (find_neighbors,
@@ -143,10 +147,22 @@ struct TLArgs {
 	// {cos, sin, cos - 1, m}, {h, rho, c, m}
 	const void *cm_sw, *cm_swA, *cm_sX, *cm_sW, *cm_swji;
 	void *cm_U, *cm_X, *cm_V, *cm_P, *cm_R, *cm_H;
-	void *recA, *recB;                   // mixed: packed per-row records (16 B and 64 B)
+	void *recA, *recB;                   // mixed: per-row records: recA float4 per row; recB four float4
+	                                     // field arrays of n_total (P, x, v, {h, m, rho, c})
 	void* recB_out;                      // mixed: pass B writes the next stage's records here...
 	uint32_t write_recs;                 // ...and into recA when set (no separate pack then)
 	void* dA32;                          // mixed: rate terms (float4 per row)
+	// mixed form, run walk: each row's ascending neighbour list as runs of consecutive
+	// rows, one word per run (first row | (length - 1) << TL_RUN_SHIFT), in sliced ELL
+	// (r_sl per slice of 32 rows, r_cnt runs per row); the passes recompute every pair's
+	// corrected gradient from the reference positions as float-float pairs (XF: float4
+	// {X hi, X lo, Y hi, Y lo} per row) and the row's Randles-Libersky correction
+	// (G: float4 {invB00, invB10, invB01, invB11} / C).  runs == nullptr: the lists.
+	const uint32_t* r_sl;
+	const uint16_t* r_cnt;
+	const uint32_t* runs;
+	const void *XF, *G;
+	uint32_t unroll;                     // run walk: pairs per loop iteration (1 or 2; same results)
 	const uint32_t* bc_rows;
 	const double* bc_v;
 	uint32_t n_bc;
@@ -169,6 +185,9 @@ struct TLArgs {
 	uint32_t t_ent_max;  // most list entries (sliced-ELL slots) of one tile
 };
 constexpr uint32_t TL_TILE = 128;
+constexpr uint32_t TL_RUN_SHIFT = 27;  // runs: start rows below 2^27, lengths 1..32
+constexpr uint32_t TL_RUN_MAX_ROWS = 1u << TL_RUN_SHIFT;
+constexpr uint32_t TL_RUN_MAX_LEN = 32;
 
 // One weak-form stage: particles (state x, y, vx, vy) and Gauss points (state rho,
 // Sxx, Sxy, Syy in the rho/Sxx/Sxy/Syy or *_f slots of the StateSoA).
@@ -248,7 +267,8 @@ struct ContactArgs {
 	cudaError_t tl_search(const mfk_host::TLSearchArgs& a, int pass, cudaStream_t s);                        \
 	cudaError_t tl_rl(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y, \
 	                  const double* m, const double* rho, const float* rho_f, const double* h, double* wx,   \
-	                  double* wy, void* status, cudaStream_t s);                                             \
+	                  double* wy, void* g32, void* status, cudaStream_t s);                                  \
+	cudaError_t tl_ref_positions(uint32_t n, const double* X, const double* Y, void* XF, cudaStream_t s);     \
 	cudaError_t to_float(uint64_t n, const double* a, float* b, cudaStream_t s);                             \
 	cudaError_t tl_to_sell(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* wx, const double* wy, \
 	                       const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* sw64, void* sw32,     \

@@ -27,6 +27,8 @@ using mfk_host::BodyParams;
 using mfk_host::TLArgs;
 using mfk_host::TLSearchArgs;
 using mfk_host::TL_TILE;
+using mfk_host::TL_RUN_MAX_ROWS;
+using mfk_host::TL_RUN_SHIFT;
 
 namespace MF_NS {
 namespace {
@@ -126,7 +128,7 @@ __global__ void k_search(TLSearchArgs a, int pass, DevStatus* st) {
 __global__ void k_rl(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
                      const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ m,
                      const double* __restrict__ rho, const float* __restrict__ rho_f, const double* __restrict__ h,
-                     double* wx, double* wy, DevStatus* st) {
+                     double* wx, double* wy, float4* g32, DevStatus* st) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	double xi = x[i], yi = y[i], hi = h[i];
@@ -159,6 +161,19 @@ __global__ void k_rl(uint32_t n, const uint32_t* __restrict__ off, const uint32_
 		wx[q] = (w.w_x * invB.c[0][0] + w.w_y * invB.c[1][0]) * 1. / C;
 		wy[q] = (w.w_x * invB.c[0][1] + w.w_y * invB.c[1][1]) * 1. / C;
 	}
+	// the mixed run-walk passes recompute the gradients on chip from this row's
+	// correction, rounded once to FP32
+	if (g32)
+		g32[i] = make_float4((float)(invB.c[0][0] / C), (float)(invB.c[1][0] / C), (float)(invB.c[0][1] / C),
+		                     (float)(invB.c[1][1] / C));
+}
+
+// Reference positions as float-float pairs for the run-walk passes.
+__global__ void k_xf(uint32_t n, const double* __restrict__ X, const double* __restrict__ Y, float4* XF) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	FF fx = ff_split_bits(X[i]), fy = ff_split_bits(Y[i]);
+	XF[i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
 }
 
 __global__ void k_to_float(uint64_t n, const double* a, float* b) {
@@ -350,11 +365,22 @@ __global__ void __launch_bounds__(256) k_tlB64(TLArgs a) {
 
 // ---- mixed form
 // recA[i] = displacement u = x - X as float-float (16 B).
-// recB[i] = { P (pass A output), x and y as float-float, vx and vy as float-float,
-//             h, m, rho, c = sqrt(K/rho) } (64 B): everything pass B reads of a neighbour.
-struct __align__(16) RecB {
+// The mixed form's per-row records for pass B (and pass A's velocities): four float4
+// fields -- the nominal stress P, position and velocity as float-float pairs, and
+// {h, m, rho, c} -- stored as four arrays of n_total (field f of row i at
+// rec[f * n + i]).  A warp that gathers one field of 32 neighbouring rows then reads
+// 512 contiguous bytes (4 cache lines) where 64-byte records would spread it over 16.
+struct RecB {
 	float4 P, x, v, hmrc;
 };
+enum { RB_P = 0, RB_X = 1, RB_V = 2, RB_H = 3 };
+__device__ __forceinline__ const float4* rb_field(const void* rec, uint32_t n, int f) {
+	return (const float4*)rec + (size_t)f * n;
+}
+__device__ __forceinline__ RecB rb_load(const void* rec, uint32_t n, uint32_t i) {
+	const float4* r = (const float4*)rec;
+	return RecB{r[i], r[(size_t)n + i], r[2 * (size_t)n + i], r[3 * (size_t)n + i]};
+}
 
 // End of the mixed pass A for row i: the per-row part in FP32, then the nominal stress
 // into the row's record and the rate terms.
@@ -365,29 +391,30 @@ __device__ __forceinline__ void tlA_finish(const TLArgs& a, uint32_t i, float Hx
 	float4 P, dA;
 	tl_particle32(a.flags, pr, Hxx, Hxy, Hyx, Hyy, Fxx, Fxy, Fyx, Fyy, s.rho_f[i], s.Sxx_f[i], s.Sxy_f[i], s.Syy_f[i],
 	              P.x, P.y, P.z, P.w, dA.x, dA.y, dA.z, dA.w);
-	((RecB*)a.recB)[i].P = P;
+	((float4*)a.recB)[i] = P;  // field RB_P
 	((float4*)a.dA32)[i] = dA;
 }
 
 // The records of row i from its state (x, y, vx, vy in FP64, rho - rho0 in FP32).
 __device__ __forceinline__ void tl_pack_row(const TLArgs& a, uint32_t i, const BodyParams& pr, double x, double y,
-                                            double vx, double vy, float rho_dev, RecB* recB) {
+                                            double vx, double vy, float rho_dev, void* rec) {
 	FF ux = ff_split_bits(x - a.X[i]), uy = ff_split_bits(y - a.Y[i]);
 	((float4*)a.recA)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
 	FF fx = ff_split_bits(x), fy = ff_split_bits(y), fvx = ff_split_bits(vx), fvy = ff_split_bits(vy);
-	RecB* rb = recB + i;
-	rb->x = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
-	rb->v = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
+	float4* r = (float4*)rec;
+	const size_t n = a.n_total;
+	r[RB_X * n + i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
+	r[RB_V * n + i] = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
 	float rho = rho_dev + pr.frho0;  // the mixed state holds rho - rho0
 	float K = pr.fK;
-	rb->hmrc = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
+	r[RB_H * n + i] = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(K / rho));
 }
 
 __global__ void k_tl_pack(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const mfk_host::StateSoA& s = a.st;
-	tl_pack_row(a, i, a.params[a.body_of[i]], s.x[i], s.y[i], s.vx[i], s.vy[i], s.rho_f[i], (RecB*)a.recB);
+	tl_pack_row(a, i, a.params[a.body_of[i]], s.x[i], s.y[i], s.vx[i], s.vy[i], s.rho_f[i], a.recB);
 }
 
 __device__ __forceinline__ float ffd(float ahi, float alo, float bhi, float blo) { return (ahi - bhi) + (alo - blo); }
@@ -491,7 +518,7 @@ __device__ __forceinline__ void tlB_finish(const TLArgs& a, uint32_t i, const Bo
 		}
 		if (!ok) raise(reinterpret_cast<DevStatus*>(a.status), ERR_NONFINITE, i);
 	}
-	if (a.write_recs) tl_pack_row(a, i, pr, nv[0], nv[1], nv[2], nv[3], nrho, (RecB*)a.recB_out);
+	if (a.write_recs) tl_pack_row(a, i, pr, nv[0], nv[1], nv[2], nv[3], nrho, a.recB_out);
 }
 
 __global__ void __launch_bounds__(256, 8) k_tlA32(TLArgs a) {
@@ -500,10 +527,10 @@ __global__ void __launch_bounds__(256, 8) k_tlA32(TLArgs a) {
 	const mfk_host::StateSoA& s = a.st;
 	const float2* swA = (const float2*)a.swA;
 	const float4* recA = (const float4*)a.recA;
-	const RecB* recB = (const RecB*)a.recB;
+	const float4* recV = rb_field(a.recB, a.n_total, RB_V);
 	uint32_t flags = a.flags;
 	float4 ui = recA[i];
-	float4 vi = recB[i].v;
+	float4 vi = recV[i];
 	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
 	float Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
 	uint32_t q = sell_base(a, i), c = a.cnt[i];
@@ -520,7 +547,7 @@ __global__ void __launch_bounds__(256, 8) k_tlA32(TLArgs a) {
 			Hyy += duy * w.y;
 		}
 		if (flags & A_VEL_TL) {
-			float4 vj = __ldg(&recB[j].v);
+			float4 vj = __ldg(recV + j);
 			float dvx = ffd(vj.x, vj.y, vi.x, vi.y), dvy = ffd(vj.z, vj.w, vi.z, vi.w);
 			Fxx += dvx * w.x;
 			Fxy += dvx * w.y;
@@ -535,13 +562,15 @@ __global__ void __launch_bounds__(256, 5) k_tlB32(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const float2* sw = (const float2*)a.sw;
-	const RecB* recB = (const RecB*)a.recB;
+	const uint32_t n = a.n_total;
+	const float4 *recP = rb_field(a.recB, n, RB_P), *recX = rb_field(a.recB, n, RB_X);
+	const float4 *recV = rb_field(a.recB, n, RB_V), *recH = rb_field(a.recB, n, RB_H);
 	uint32_t flags = a.flags;
 	const BodyParams& pr = a.params[a.body_of[i]];
 	float rho0 = pr.frho0;
 	float r21 = 1.f / (rho0 * rho0);
 	float sc = r21 * rho0;
-	RecB ri = recB[i];
+	RecB ri = rb_load(a.recB, n, i);
 	float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2;
 	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
 	uint32_t q = sell_base(a, i), c = a.cnt[i];
@@ -549,9 +578,8 @@ __global__ void __launch_bounds__(256, 5) k_tlB32(TLArgs a) {
 	for (uint32_t k = 0; k < c; k++, q += 32) {
 		uint32_t j = a.snbr[q];
 		float2 w = sw[q];  // the neighbour's mass times its corrected gradient
-		const RecB* rj = recB + j;
 		if (flags & A_STRESS_TL) {
-			float4 Pj = __ldg(&rj->P);
+			float4 Pj = __ldg(recP + j);
 			float fx = sc * w.x, fy = sc * w.y;
 			Pxx_x += (ri.P.x + Pj.x) * fx;
 			Pyx_y += (ri.P.z + Pj.z) * fy;
@@ -559,12 +587,12 @@ __global__ void __launch_bounds__(256, 5) k_tlB32(TLArgs a) {
 			Pyy_y += (ri.P.w + Pj.w) * fy;
 		}
 		if (flags & A_ART_VISC) {
-			float4 xj = __ldg(&rj->x), vj = __ldg(&rj->v);
+			float4 xj = __ldg(recX + j), vj = __ldg(recV + j);
 			float xij = ffd(ri.x.x, ri.x.y, xj.x, xj.y), yij = ffd(ri.x.z, ri.x.w, xj.z, xj.w);
 			float vijx = ffd(ri.v.x, ri.v.y, vj.x, vj.y), vijy = ffd(ri.v.z, ri.v.w, vj.z, vj.w);
 			float vijposij = approach(vijx, vijy, xij, yij);
 			if (vijposij < 0.f) {
-				float4 hmrc = __ldg(&rj->hmrc);
+				float4 hmrc = __ldg(recH + j);
 				float piij = art_visc_pi(ri.hmrc, hmrc, xij, yij, vijposij, alpha, beta, eta2);
 				av_x += -piij * w.x;
 				av_y += -piij * w.y;
@@ -572,6 +600,184 @@ __global__ void __launch_bounds__(256, 5) k_tlB32(TLArgs a) {
 		}
 	}
 	tlB_finish(a, i, pr, rho0, Pxx_x, Pyx_y, Pxy_x, Pyy_y, av_x, av_y);
+}
+
+// ---- mixed form, run walk.  The same per-row arithmetic as k_tlA32 / k_tlB32 and the
+// same pair order (ascending j), but with no per-pair data streamed: the neighbour
+// list comes as runs of consecutive rows (one word per run, so no list entry has to
+// be loaded before its neighbour's record), and each pair's corrected gradient
+//     grad w_ij = invB_i grad W(X_i - X_j, h_i) / C_i      (precomp_shape_functions.h:285-287)
+// is recomputed in FP32 from the float-float reference positions and the row's
+// correction invB_i / C_i (rounded once from the FP64 set-up).  The weights then
+// differ from the streamed FP32 ones by a few FP32 ulps.
+
+// 10 / (7 pi) of the 2-D cubic spline (kernel.cpp:24)
+constexpr float K_SPLINE_2D = 0.45472840883398667f;
+
+// Corrected gradient of pair (i, j): the cubic spline's gradient at X_i - X_j (zero
+// at r >= 2h and for r <= 1e-12, kernel.cpp:20-55) times the row's invB / C.
+__device__ __forceinline__ float2 rl_grad32(float4 Xi, float4 Xj, float4 Gi, float h1, float fac) {
+	float xij = ffd(Xi.x, Xi.y, Xj.x, Xj.y), yij = ffd(Xi.z, Xi.w, Xj.z, Xj.w);
+	float r2 = xij * xij + yij * yij;
+	float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+	float q = r2 * rinv * h1;
+	float der = 0.f;
+	if (q < 2.f && r2 > 1e-24f) {
+		float t = 2.f - q;
+		der = (q >= 1.f ? -0.75f * t * t : -3.0f * q * (1.f - 0.75f * q)) * h1 * rinv * fac;
+	}
+	float gx = xij * der, gy = yij * der;
+	return make_float2(gx * Gi.x + gy * Gi.y, gx * Gi.z + gy * Gi.w);
+}
+
+// Pass A's gathers of one pair: reference position, quad weight, displacement and
+// velocity records of row j.
+struct PairA {
+	float4 X, u, v;
+	float qw;
+};
+__device__ __forceinline__ PairA tlA_load(const TLArgs& a, uint32_t j) {
+	PairA p;
+	p.X = __ldg((const float4*)a.XF + j);
+	p.qw = __ldg((const float*)a.qw32 + j);
+	p.u = (a.flags & A_DISP) ? __ldg((const float4*)a.recA + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+	p.v = (a.flags & A_VEL_TL) ? __ldg(rb_field(a.recB, a.n_total, RB_V) + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+	return p;
+}
+
+struct AccA {
+	float Hxx = 0.f, Hxy = 0.f, Hyx = 0.f, Hyy = 0.f;
+	float Fxx = 0.f, Fxy = 0.f, Fyx = 0.f, Fyy = 0.f;
+};
+__device__ __forceinline__ void tlA_add(uint32_t flags, const PairA& p, float4 Xi, float4 Gi, float h1, float fac,
+                                        float4 ui, float4 vi, AccA& s) {
+	float2 w = rl_grad32(Xi, p.X, Gi, h1, fac);
+	w.x *= p.qw;  // times the neighbour's quad weight
+	w.y *= p.qw;
+	if (flags & A_DISP) {
+		float dux = ffd(p.u.x, p.u.y, ui.x, ui.y), duy = ffd(p.u.z, p.u.w, ui.z, ui.w);
+		s.Hxx += dux * w.x;
+		s.Hxy += dux * w.y;
+		s.Hyx += duy * w.x;
+		s.Hyy += duy * w.y;
+	}
+	if (flags & A_VEL_TL) {
+		float dvx = ffd(p.v.x, p.v.y, vi.x, vi.y), dvy = ffd(p.v.z, p.v.w, vi.z, vi.w);
+		s.Fxx += dvx * w.x;
+		s.Fxy += dvx * w.y;
+		s.Fyx += dvy * w.x;
+		s.Fyy += dvy * w.y;
+	}
+}
+
+// U pairs per iteration: the gathers of both pairs are issued before either pair's
+// arithmetic, and the pairs are added in list order, so U = 1 and U = 2 give the same
+// bits; U = 2 keeps twice the loads in flight at the cost of registers.
+template <int U>
+__global__ void __launch_bounds__(256, U == 1 ? 4 : 3) k_tlA32r(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const uint32_t flags = a.flags;
+	const float4 Xi = ((const float4*)a.XF)[i], Gi = ((const float4*)a.G)[i];
+	const float h1 = 1.f / ((const float*)a.h32)[i], fac = K_SPLINE_2D * h1 * h1;
+	const float4 ui = ((const float4*)a.recA)[i];
+	const float4 vi = rb_field(a.recB, a.n_total, RB_V)[i];
+	AccA s;
+	uint32_t q = a.r_sl[i >> 5] + (i & 31u), nr = a.r_cnt[i];
+	for (uint32_t r = 0; r < nr; r++, q += 32) {
+		const uint32_t run = a.runs[q];
+		const uint32_t j0 = run & (TL_RUN_MAX_ROWS - 1u), j1 = j0 + (run >> TL_RUN_SHIFT) + 1u;
+		if (U == 1) {
+			for (uint32_t j = j0; j < j1; j++) tlA_add(flags, tlA_load(a, j), Xi, Gi, h1, fac, ui, vi, s);
+		} else {
+			for (uint32_t j = j0; j < j1; j += 2) {
+				const bool two = j + 1 < j1;
+				const PairA p0 = tlA_load(a, j), p1 = tlA_load(a, two ? j + 1 : j);
+				tlA_add(flags, p0, Xi, Gi, h1, fac, ui, vi, s);
+				if (two) tlA_add(flags, p1, Xi, Gi, h1, fac, ui, vi, s);
+			}
+		}
+	}
+	tlA_finish(a, i, s.Hxx, s.Hxy, s.Hyx, s.Hyy, s.Fxx, s.Fxy, s.Fyx, s.Fyy);
+}
+
+// Pass B's gathers of one pair: row j's record and reference position.
+struct PairB {
+	float4 P, x, v, hmrc, X;
+};
+__device__ __forceinline__ PairB tlB_load(const TLArgs& a, uint32_t j) {
+	const uint32_t n = a.n_total;
+	PairB p;
+	p.hmrc = __ldg(rb_field(a.recB, n, RB_H) + j);
+	p.X = __ldg((const float4*)a.XF + j);
+	p.P = (a.flags & A_STRESS_TL) ? __ldg(rb_field(a.recB, n, RB_P) + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+	if (a.flags & A_ART_VISC) {
+		p.x = __ldg(rb_field(a.recB, n, RB_X) + j);
+		p.v = __ldg(rb_field(a.recB, n, RB_V) + j);
+	} else {
+		p.x = p.v = make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	return p;
+}
+
+struct AccB {
+	float Pxx_x = 0.f, Pyx_y = 0.f, Pxy_x = 0.f, Pyy_y = 0.f, av_x = 0.f, av_y = 0.f;
+};
+__device__ __forceinline__ void tlB_add(uint32_t flags, const PairB& p, const RecB& ri, float4 Xi, float4 Gi, float h1,
+                                        float fac, float sc, float alpha, float beta, float eta2, AccB& s) {
+	float2 w = rl_grad32(Xi, p.X, Gi, h1, fac);
+	w.x *= p.hmrc.y;  // times the neighbour's mass
+	w.y *= p.hmrc.y;
+	if (flags & A_STRESS_TL) {
+		float fx = sc * w.x, fy = sc * w.y;
+		s.Pxx_x += (ri.P.x + p.P.x) * fx;
+		s.Pyx_y += (ri.P.z + p.P.z) * fy;
+		s.Pxy_x += (ri.P.y + p.P.y) * fx;
+		s.Pyy_y += (ri.P.w + p.P.w) * fy;
+	}
+	if (flags & A_ART_VISC) {
+		float xij = ffd(ri.x.x, ri.x.y, p.x.x, p.x.y), yij = ffd(ri.x.z, ri.x.w, p.x.z, p.x.w);
+		float vijx = ffd(ri.v.x, ri.v.y, p.v.x, p.v.y), vijy = ffd(ri.v.z, ri.v.w, p.v.z, p.v.w);
+		float vijposij = approach(vijx, vijy, xij, yij);
+		if (vijposij < 0.f) {
+			float piij = art_visc_pi(ri.hmrc, p.hmrc, xij, yij, vijposij, alpha, beta, eta2);
+			s.av_x += -piij * w.x;
+			s.av_y += -piij * w.y;
+		}
+	}
+}
+
+template <int U>
+__global__ void __launch_bounds__(256, U == 1 ? 3 : 2) k_tlB32r(TLArgs a) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const uint32_t flags = a.flags;
+	const BodyParams& pr = a.params[a.body_of[i]];
+	const float rho0 = pr.frho0;
+	const float r21 = 1.f / (rho0 * rho0);
+	const float sc = r21 * rho0;
+	const RecB ri = rb_load(a.recB, a.n_total, i);
+	const float4 Xi = ((const float4*)a.XF)[i], Gi = ((const float4*)a.G)[i];
+	const float h1 = 1.f / ri.hmrc.x, fac = K_SPLINE_2D * h1 * h1;
+	const float alpha = pr.falpha, beta = pr.fbeta, eta2 = pr.feta2;
+	AccB s;
+	uint32_t q = a.r_sl[i >> 5] + (i & 31u), nr = a.r_cnt[i];
+	for (uint32_t r = 0; r < nr; r++, q += 32) {
+		const uint32_t run = a.runs[q];
+		const uint32_t j0 = run & (TL_RUN_MAX_ROWS - 1u), j1 = j0 + (run >> TL_RUN_SHIFT) + 1u;
+		if (U == 1) {
+			for (uint32_t j = j0; j < j1; j++)
+				tlB_add(flags, tlB_load(a, j), ri, Xi, Gi, h1, fac, sc, alpha, beta, eta2, s);
+		} else {
+			for (uint32_t j = j0; j < j1; j += 2) {
+				const bool two = j + 1 < j1;
+				const PairB p0 = tlB_load(a, j), p1 = tlB_load(a, two ? j + 1 : j);
+				tlB_add(flags, p0, ri, Xi, Gi, h1, fac, sc, alpha, beta, eta2, s);
+				if (two) tlB_add(flags, p1, ri, Xi, Gi, h1, fac, sc, alpha, beta, eta2, s);
+			}
+		}
+	}
+	tlB_finish(a, i, pr, rho0, s.Pxx_x, s.Pyx_y, s.Pxy_x, s.Pyy_y, s.av_x, s.av_y);
 }
 
 // ---- mixed form over halo tiles.  The same per-row arithmetic, in the same order, as
@@ -597,13 +803,13 @@ __global__ void __launch_bounds__(TL_TILE) k_tlA32t(TLArgs a) {
 	const float4* rec4 = (const float4*)a.recB;
 	for (uint32_t e = threadIdx.x; e < 2 * hn; e += TL_TILE) {
 		uint32_t s_ = e >> 1, j = a.t_halo[h0 + s_];
-		cp16(smA + (e & 1u) * HM + s_, (e & 1u) ? rec4 + 4 * (size_t)j + 2 : recA + j);  // u, or RecB::v
+		cp16(smA + (e & 1u) * HM + s_, (e & 1u) ? rec4 + (size_t)RB_V * a.n_total + j : recA + j);  // u, or v
 	}
 	const uint32_t p = t * TL_TILE + threadIdx.x;
 	const bool live = p < a.n_total;
 	const uint32_t i = live ? a.t_rows[p] : 0u;
 	const float4 ui = recA[i];
-	const float4 vi = rec4[4 * (size_t)i + 2];
+	const float4 vi = rec4[(size_t)RB_V * a.n_total + i];
 	const uint32_t c = live ? a.t_cnt[p] : 0u;
 	cp_wait_all();
 	__syncthreads();
@@ -644,14 +850,14 @@ __global__ void __launch_bounds__(TL_TILE, 8) k_tlB32t(TLArgs a) {
 	const uint32_t h0 = a.t_halo_off[t], hn = a.t_halo_off[t + 1] - h0;
 	const float4* rec4 = (const float4*)a.recB;
 	for (uint32_t e = threadIdx.x; e < 4 * hn; e += TL_TILE) {
-		uint32_t s_ = e >> 2, f = e & 3u;  // four threads copy one 64-byte record
-		cp16(smB + f * HM + s_, rec4 + 4 * (size_t)a.t_halo[h0 + s_] + f);
+		uint32_t s_ = e >> 2, f = e & 3u;  // four threads copy one row's four fields
+		cp16(smB + f * HM + s_, rec4 + (size_t)f * a.n_total + a.t_halo[h0 + s_]);
 	}
 	// this row's own data, requested while the copies are in flight
 	const uint32_t p = t * TL_TILE + threadIdx.x;
 	const bool live = p < a.n_total;
 	const uint32_t i = live ? a.t_rows[p] : 0u;
-	const RecB ri = ((const RecB*)a.recB)[i];
+	const RecB ri = rb_load(a.recB, a.n_total, i);
 	const uint32_t c = live ? a.t_cnt[p] : 0u;
 	const uint32_t bi = a.body_of[i];
 	cp_wait_all();
@@ -764,8 +970,14 @@ size_t tl_sort_tmp_bytes(uint32_t n, int bits) {
 
 cudaError_t tl_rl(uint32_t n, const uint32_t* off, const uint32_t* nbr, const double* x, const double* y,
                   const double* m, const double* rho, const float* rho_f, const double* h, double* wx, double* wy,
-                  void* status, cudaStream_t s) {
-	k_rl<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, x, y, m, rho, rho_f, h, wx, wy, reinterpret_cast<DevStatus*>(status));
+                  void* g32, void* status, cudaStream_t s) {
+	k_rl<<<grid1(n, 128), 128, 0, s>>>(n, off, nbr, x, y, m, rho, rho_f, h, wx, wy, (float4*)g32,
+	                                   reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t tl_ref_positions(uint32_t n, const double* X, const double* Y, void* XF, cudaStream_t s) {
+	if (n) k_xf<<<grid1(n, 256), 256, 0, s>>>(n, X, Y, (float4*)XF);
 	return cudaGetLastError();
 }
 
@@ -816,6 +1028,8 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	case 2: {
 		unsigned bs = a.block ? a.block : 128;
 		if (mixed && a.t_rows) k_tlA32t<<<a.n_tiles, TL_TILE, tl_tile_smem(0, a.halo_max, a.t_ent_max), s>>>(a);
+		else if (mixed && a.runs && a.unroll == 2) k_tlA32r<2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs) k_tlA32r<1><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed) k_tlA32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlA64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
@@ -823,6 +1037,8 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	case 3: {
 		unsigned bs = a.block ? a.block : 128;
 		if (mixed && a.t_rows) k_tlB32t<<<a.n_tiles, TL_TILE, tl_tile_smem(1, a.halo_max, a.t_ent_max), s>>>(a);
+		else if (mixed && a.runs && a.unroll == 2) k_tlB32r<2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs) k_tlB32r<1><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlB64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;

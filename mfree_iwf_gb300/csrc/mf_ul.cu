@@ -98,6 +98,17 @@ __device__ __forceinline__ Rec32 load_rec_tail(const Rec32* p, float4 head) {
 	return r;
 }
 
+// ------------------------------------------------------- per-body failures
+// With per-body masking (failed != nullptr) an error found on a row fails the row's
+// body alone; without it, it fails the step (the status word).
+__device__ __forceinline__ void fail_body(uint32_t* failed, DevStatus* st, uint32_t bit, uint32_t row, uint32_t body) {
+	if (failed) atomicOr(&failed[body], bit);
+	else raise(st, bit, row);
+}
+__device__ __forceinline__ bool is_failed(const uint32_t* failed, uint32_t body) {
+	return failed && *(volatile const uint32_t*)&failed[body];
+}
+
 // --------------------------------------------------------------- grid build
 __global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
 	uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,10 +127,15 @@ __global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
 // stay valid for all four stages of a step.
 __global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ h, const double* __restrict__ vx, const double* __restrict__ vy,
-                       const uint32_t* __restrict__ body_of, int mixed, unsigned long long* bb) {
+                       const uint32_t* __restrict__ body_of, int mixed, unsigned long long* bb,
+                       const uint32_t* failed) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool valid = i < n;
 	uint32_t b = valid ? body_of[i] : 0xffffffffu;
+	if (valid && is_failed(failed, b)) {  // a failed body's rows are left out
+		valid = false;
+		b = 0xffffffffu;
+	}
 	unsigned long long mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull, mh = 0ull, mv = 0ull;
 	if (valid) {
 		mnx = mxx = ord_encode(x[i]);
@@ -161,7 +177,7 @@ __global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* _
 // Cell geometry per body (grid.h:105-115) and the exclusive scan of cell counts.
 // One block; bodies are processed serially in chunks for the scan.
 __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyParams* P, int mixed, Geom* G,
-                       uint32_t* total_cells, uint32_t cell_cap, DevStatus* st) {
+                       uint32_t* total_cells, uint32_t cell_cap, DevStatus* st, uint32_t* failed) {
 	__shared__ uint32_t s_cnt[1024];
 	__shared__ uint32_t s_base;
 	if (threadIdx.x == 0) s_base = 0;
@@ -170,7 +186,11 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 		uint32_t b = c0 + threadIdx.x;
 		uint32_t cnt = 0;
 		Geom g{};
-		if (b < nb) {
+		if (b < nb && is_failed(failed, b)) {  // a failed body gets no cells
+			g.nx = g.ny = 1;
+			g.dx = 1.;
+			g.span = 1;
+		} else if (b < nb) {
 			double bminx = ord_decode(bb[6 * b + 0]), bminy = ord_decode(bb[6 * b + 1]);
 			double bmaxx = ord_decode(bb[6 * b + 2]), bmaxy = ord_decode(bb[6 * b + 3]);
 			double hmax = ord_decode(bb[6 * b + 4]);
@@ -196,14 +216,18 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 			double fnx = ceil(lx / dx), fny = ceil(ly / dx);
 			uint32_t nx = (uint32_t)fnx, ny = (uint32_t)fny;
 			uint32_t num_cell = nx * ny;
+			bool bad = false;
 			if (!(num_cell < P[b].n) && !mixed) {
-				raise(st, ERR_GRID, P[b].off);
+				fail_body(failed, st, ERR_GRID, P[b].off, b);
+				bad = true;
 			}
 			if (!(fnx * fny < 4.0e9) || nx == 0 || ny == 0) {
-				raise(st, ERR_GRID, P[b].off);
+				fail_body(failed, st, ERR_GRID, P[b].off, b);
 				nx = ny = 1;
 				num_cell = 1;
+				bad = true;
 			}
+			if (bad && failed) num_cell = 0;  // masked from this stage on
 			g.bbmin_x = bminx; g.bbmin_y = bminy; g.dx = dx; g.slack = slack;
 			g.nx = nx; g.ny = ny; g.num_cell = num_cell; g.span = span;
 			cnt = num_cell;
@@ -240,20 +264,31 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 // Global cell key of each row (grid.h:35-41): cell_off + ix*ny + iy.
 __global__ void k_hash(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const uint32_t* __restrict__ body_of, const Geom* __restrict__ G,
-                       const uint32_t* __restrict__ total_cells, uint32_t* keys, uint32_t* vals, DevStatus* st) {
+                       const uint32_t* __restrict__ total_cells, uint32_t* keys, uint32_t* vals, DevStatus* st,
+                       uint32_t* failed) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
-	Geom g = G[body_of[i]];
+	const uint32_t b = body_of[i], tot = *total_cells;
+	vals[i] = i;
+	if (is_failed(failed, b) && tot != 0) {  // past every cell: no stencil reaches it
+		keys[i] = tot;
+		return;
+	}
+	Geom g = G[b];
 	uint32_t ix = (uint32_t)((x[i] - g.bbmin_x) / g.dx);
 	uint32_t iy = (uint32_t)((y[i] - g.bbmin_y) / g.dx);
-	if (ix >= g.nx || iy >= g.ny || *total_cells == 0) {
+	if (ix >= g.nx || iy >= g.ny || tot == 0) {
+		if (tot != 0 && failed) {
+			atomicOr(&failed[b], ERR_GRID);
+			keys[i] = tot;
+			return;
+		}
 		raise(st, ERR_GRID, i);
 		ix = min(ix, g.nx - 1);
 		iy = min(iy, g.ny - 1);
 	}
 	uint32_t key = g.cell_off + ix * g.ny + iy;
-	keys[i] = (*total_cells == 0) ? 0u : key;
-	vals[i] = i;
+	keys[i] = (tot == 0) ? 0u : key;
 }
 
 // Cell start table over all bodies' cells (grid.h:48-81): cell_start[c] is the
@@ -495,9 +530,10 @@ __device__ __forceinline__ void stencil(const Geom& g, uint32_t key, int& lo_i, 
 // ----------------------------------------------------------- pair kernel FP64
 __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __restrict__ P,
                                            const Geom* __restrict__ G, DevStatus* st, uint32_t k) {
+	uint32_t b = a.rec_body[k];
+	if (is_failed(a.failed, b)) return;  // a failed body stays as it was
 	const Rec64* rec = reinterpret_cast<const Rec64*>(a.rec);
 	const Rec64 ri = load_rec(rec + k);
-	uint32_t b = a.rec_body[k];
 	const BodyParams& pr = P[b];
 	Geom g = G[b];
 	uint32_t i = a.perm[k];
@@ -626,8 +662,8 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 			}
 		}
 	}
-	if (a.max_nbh && cnt >= a.max_nbh) raise(st, ERR_NBH_OVERFLOW, i);
-	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
+	if (a.max_nbh && cnt >= a.max_nbh) fail_body(a.failed, st, ERR_NBH_OVERFLOW, i, b);
+	if (cnt == 0) fail_body(a.failed, st, ERR_NO_NEIGHBOR, i, b);
 
 	// per-particle actions, in the reference's list order
 	double d[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
@@ -654,7 +690,7 @@ __device__ __forceinline__ void pair64_row(const ULArgs& a, const BodyParams* __
 	rk_update_f64<double>(a, i, pr.dt, d);
 	if (a.stage == 3 && !(isfinite(a.base.x[i]) && isfinite(a.base.y[i]) && isfinite(a.base.vx[i]) &&
 	                      isfinite(a.base.vy[i]) && isfinite(a.base.rho[i])))
-		raise(st, ERR_NONFINITE, i);
+		fail_body(a.failed, st, ERR_NONFINITE, i, b);
 }
 
 // ---------------------------------------------------------- pair kernel mixed
@@ -667,9 +703,10 @@ template <bool GOD, int L = 1>
 __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __restrict__ P,
                                            const Geom* __restrict__ G, DevStatus* st, uint32_t k,
                                            uint32_t lane = 0) {
+	uint32_t b = a.rec_body[k];
+	if (is_failed(a.failed, b)) return;  // a failed body stays as it was (all L lanes of the row)
 	const Rec32* rec = reinterpret_cast<const Rec32*>(a.rec);
 	const Rec32 ri = load_rec(rec + k);
-	uint32_t b = a.rec_body[k];
 	const BodyParams& pr = P[b];
 	Geom g = G[b];
 	uint32_t i = a.perm[k];
@@ -819,7 +856,7 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	if (a.stage > 0) {
 		// the cells were sized at stage 0 for moves up to g.slack; check that held
 		double mx = a.st.x[i] - a.base.x[i], my = a.st.y[i] - a.base.y[i];
-		if (mx * mx + my * my > g.slack * g.slack) raise(st, ERR_GRID, i);
+		if (mx * mx + my * my > g.slack * g.slack) fail_body(a.failed, st, ERR_GRID, i, b);
 	}
 	// advection: the FP64 velocity enters the FP64 position update below
 	double dd0 = (double)d[0], dd1 = (double)d[1];
@@ -858,7 +895,7 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 		}
 		if (!(isfinite(bp[0][i]) && isfinite(bp[1][i]) && isfinite(bp[2][i]) && isfinite(bp[3][i]) &&
 		      isfinite(bq[0][i])))
-			raise(st, ERR_NONFINITE, i);
+			fail_body(a.failed, st, ERR_NONFINITE, i, b);
 	}
 }
 
@@ -945,11 +982,11 @@ cudaError_t build_grid(const ULArgs& a, bool mixed, cudaStream_t s) {
 	k_bbox_init<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, a.bbox);
 	const mfk_host::StateSoA& sv = a.stage == 0 ? a.base : a.st;
 	k_bbox<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.h, sv.vx, sv.vy, a.body_of, mixed ? 1 : 0,
-	                                              a.bbox);
+	                                              a.bbox, a.failed);
 	k_geom<<<1, 1024, 0, s>>>(a.n_bodies, a.bbox, a.params, mixed ? 1 : 0, a.geom, a.total_cells,
-	                          a.cell_cap ? a.cell_cap : a.n_total + 1, st);
+	                          a.cell_cap ? a.cell_cap : a.n_total + 1, st, a.failed);
 	k_hash<<<grid1(a.n_total, 256), 256, 0, s>>>(a.n_total, sv.x, sv.y, a.body_of, a.geom, a.total_cells, a.keys,
-	                                              a.perm_in, st);
+	                                              a.perm_in, st, a.failed);
 	size_t tmp = a.sort_tmp_bytes;
 	cudaError_t e = cub::DeviceRadixSort::SortPairs(a.sort_tmp, tmp, a.keys, a.keys_sorted, a.perm_in, a.perm,
 	                                                (int)a.n_total, 0, a.sort_bits, s);

@@ -99,3 +99,70 @@ def test_all_bodies_state_io_equals_per_body(lib, precision):
             np.testing.assert_array_equal(a[k][f], b[k][f])
     for s in sims:
         s.close()
+
+
+def instance_alone(ens, k):
+    b = ens.bodies[k]
+    return S.Scenario(method=ens.method, bodies=[b], actions=ens.actions, dt=b.params["dt"], nu=b.params["nu"],
+                      E=b.params["E"], rho0=b.params["rho0"], wdeltap=b.params["wdeltap"], corr_exp=ens.corr_exp,
+                      mghn_eps=ens.mghn_eps, alpha=ens.alpha, beta=ens.beta, eta=ens.eta, xsph_eps=ens.xsph_eps,
+                      nbh_eps=ens.nbh_eps)
+
+
+@pytest.mark.parametrize("precision", ["fp64_strict", "mixed"])
+def test_failed_instance_is_masked(lib, precision):
+    """Per-body failure masking ("mask_failed"): a NaN planted from the host into one
+    of six instances after 5 steps fails that instance alone -- mf_step reports
+    MF_ERR_BODY_FAILED, the failure word names it, and its state stays frozen -- while
+    the other five step on bit for bit as they do alone (20 steps)."""
+    import mfree_iwf_gb300 as M
+    ens = small_ensemble()
+    nb = len(ens.bodies)
+    sim = M.from_scenario(ens, precision=precision)
+    sim.set_option("mask_failed", 1)
+    assert sim.get_option("mask_failed") == 1
+    sim.step(5)
+    bad = 2
+    st = sim.get_state(bad, FIELDS)
+    st["vx"][len(st["vx"]) // 2] = np.nan
+    sim.set_state(bad, st)
+    with pytest.raises(M.BodyFailed) as ei:
+        sim.step(15)
+    assert ei.value.status == M.ERR_BODY_FAILED
+    failed = sim.failed()
+    assert list(np.nonzero(failed)[0]) == [bad], failed
+    assert failed[bad] & (4 | 8), failed  # a grid error or a non-finite state
+    got = states(sim, nb)
+    frozen = got[bad]
+    with pytest.raises(M.BodyFailed):  # the failed body stays frozen, the others go on
+        sim.step(1)
+    again = sim.get_state(bad, FIELDS)
+    for f in FIELDS:
+        np.testing.assert_array_equal(again[f], frozen[f], err_msg=f)
+    sim.close()
+    for k in range(nb):
+        if k == bad:
+            continue
+        s1 = M.from_scenario(instance_alone(ens, k), precision=precision)
+        s1.step(20)
+        alone = s1.get_state(0, FIELDS)
+        s1.close()
+        for f in FIELDS:
+            assert np.array_equal(alone[f], got[k][f]), (k, f)
+
+
+def test_without_masking_a_failure_fails_the_step(lib):
+    """Without the option a NaN in one instance fails mf_step as a whole (the
+    reference's behaviour is an abort)."""
+    import mfree_iwf_gb300 as M
+    ens = small_ensemble()
+    sim = M.from_scenario(ens, precision="fp64_strict")
+    sim.step(2)
+    st = sim.get_state(1, FIELDS)
+    st["x"][0] = np.nan
+    sim.set_state(1, st)
+    with pytest.raises(M.MfError) as ei:
+        sim.step(3)
+    assert not isinstance(ei.value, M.BodyFailed)
+    assert ei.value.status in (-4, -7)  # non-finite state / grid
+    sim.close()
