@@ -349,9 +349,23 @@ def weak_bytes(kind: int, n_p: int, n_g: int, e_g: int, e_t: int) -> float:
             + 16 + 32 + 24 + 24 + 40)   # RK4 FP64 x y vx vy: stage v, base, acc (1-3), acc (0-2), stage/base
 
 
-def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool, family: str = "") -> float:
+def algorithmic_bytes(kind: int, mixed: bool, nnz_per_row: float, tl: bool, family: str = "",
+                      runs_per_row: float = 0.0) -> float:
     """Unique bytes per row of one launch: each row's own data once, the lists once, and
-    neighbour records assumed served on chip (their unique bytes are the rows' own)."""
+    neighbour records assumed served on chip (their unique bytes are the rows' own).
+    runs_per_row > 0: the mixed TL run-walk passes (run words instead of per-pair
+    entries; per row the reference position and the correction, 32 B, and h)."""
+    if tl and mixed and runs_per_row > 0 and family not in ("corot", "potential"):
+        if kind == 1:  # pass A
+            return (2 + 4 * runs_per_row + 32 + 4  # run count and words; XF, G; h
+                    + 16 + 16 + 16 + 4            # own displacement and velocity records, rho - rho0, S, body id
+                    + 16 + 16)                    # writes: nominal stress P, rate terms
+        if kind == 2:  # pass B
+            return (2 + 4 * runs_per_row + 32     # run count and words; XF, G
+                    + 64 + 16 + 16 + 24           # own record fields, rate terms, stage vx vy, fc and m
+                    + 32 + 24 + 32 + 32 + 8       # RK4 FP64 x y vx vy
+                    + 16 + 12 + 16 + 16 + 4       # RK4 FP32 rho S
+                    + 24 + 64)                    # next-stage records
     if family in ("corot", "potential") and mixed:
         if kind == 1:  # pass A: index + qw-weighted gradient (+ X_j - X_i, corotational) per pair
             per_pair = 20 if family == "corot" else 12
@@ -411,6 +425,9 @@ def ours(args, cfg_desc):
     sim.synchronize()
     stream = torch.cuda.ExternalStream(sim.stream())
     nnz = float(np.mean(sim.neighbor_counts(0))) if tl else 0.0
+    runs_per_row = 0.0
+    if sc.method == M.METHOD_TL and mixed and sim.get_option("tl_runs") and sim.get_option("tl_runs_built"):
+        runs_per_row = sim.get_option("tl_run_words") / n
 
     # ---- device-resident timed region (graph replay of whole steps)
     l0 = sim.launch_count()
@@ -445,17 +462,27 @@ def ours(args, cfg_desc):
     sim.set_timing(False)
 
     # ---- end to end through the C ABI with host buffers: per step the state of all
-    # bodies goes host -> device (pinned), one step runs, the state comes back
+    # bodies goes host -> device (pinned), one step runs, the state comes back into the
+    # same host arrays (stream-ordered transfers: each field's host -> device copy of a
+    # step waits for its device -> host copy of the step before; the two directions
+    # overlap field by field); the timed region ends when the last state is on the host
     fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy")
     host = {f: torch.empty(n, dtype=torch.float64).pin_memory().numpy() for f in fields}
     sim.get_state_all_into(host)
     k2 = max(3, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    weak = sc.method in (M.METHOD_TL_WEAK, M.METHOD_UL_WEAK)  # (their transfers are synchronous)
     for _ in range(k2):
-        sim.set_state_all(host)
-        sim.step(1)
-        sim.get_state_all_into(host)
+        if weak:
+            sim.set_state_all(host)
+            sim.step(1)
+            sim.get_state_all_into(host)
+        else:
+            sim.set_state_all_async(host)
+            sim.step(1)
+            sim.get_state_all_async_into(host)
+    sim.synchronize()
     wall = time.perf_counter() - t0
     _, e2e_value = job_throughput(dist, wall, n * k2)
     bytes_io = 8 * len(fields) * n
@@ -544,13 +571,15 @@ def ours(args, cfg_desc):
         if weak_model:
             abytes = weak_bytes(dom, n, weak_lists[0], weak_lists[1], weak_lists[2]) * per_launch_rows
         else:
-            abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload) * per_launch_rows
+            abytes = algorithmic_bytes(dom, mixed, nnz, tl, args.workload, runs_per_row) * per_launch_rows
         achieved = abytes / (kms / klaunch / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_kind,
                 "launches": klaunch, "avg_launch_ms": kms / klaunch,
                 "algorithmic_bytes_per_launch": abytes,
-                "byte_model": "itemised: every byte the kernel must move (lists and per-pair weights streamed)"}
+                "byte_model": ("itemised: every byte the kernel must move (" +
+                               ("run words per row, gradients recomputed on chip" if runs_per_row else
+                                "lists and per-pair weights streamed") + ")")}
         fam = "tl" if sc.method == M.METHOD_TL else "ul" if sc.method == M.METHOD_UL else None
         if fam is not None:
             per_ps = SURVEY_BYTES[(fam, mixed)]

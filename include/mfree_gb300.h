@@ -226,6 +226,15 @@ MF_API mf_status mf_set_state(mf_ctx* ctx, int32_t body, const mf_particles* p);
  * for ensembles of hundreds of bodies). */
 MF_API mf_status mf_get_state_all(mf_ctx* ctx, const mf_state* out);
 MF_API mf_status mf_set_state_all(mf_ctx* ctx, const mf_particles* p);
+/* The same transfers stream-ordered (strong forms): each returns once its work is
+ * queued behind the steps already issued; host buffers (pinned, for the copies to run
+ * asynchronously) are valid / reusable after mf_synchronize.  Per field, the
+ * device->host copies run on one copy stream and the host->device copies on another;
+ * a set waits, field by field, for an earlier get of the same field, so that a get and
+ * a set of the same host arrays are ordered while the two directions of the host link
+ * overlap.  No counterpart in the reference (its state lives in host memory). */
+MF_API mf_status mf_get_state_all_async(mf_ctx* ctx, const mf_state* out);
+MF_API mf_status mf_set_state_all_async(mf_ctx* ctx, const mf_particles* p);
 MF_API mf_status mf_get_time(mf_ctx* ctx, int32_t body, double* t);
 MF_API mf_status mf_num_particles(mf_ctx* ctx, int32_t body, uint32_t* n);
 /* The stress the method evaluates at a body's current state, per particle.  TL (strong
@@ -390,6 +399,11 @@ MF_API mf_status mf_mlp_train(mf_mlp* model, int32_t steps, float lr0, float lr1
 MF_API mf_status mf_mlp_predict(mf_mlp* model, const float* x, int32_t n, float* y);
 MF_API mf_status mf_mlp_launch_count(const mf_mlp* model, uint64_t* launches);
 MF_API mf_status mf_mlp_get_stream(const mf_mlp* model, void** stream);
+/* Options: "tcgen05" (1: the forward products with K a multiple of 64 and N <= 256 run
+ * on Blackwell's tcgen05 tensor cores with TMEM accumulators and TMA-staged operands,
+ * the default on compute capability 10.x; 0: the mma.sync kernels). */
+MF_API mf_status mf_mlp_set_option(mf_mlp* model, const char* key, int64_t value);
+MF_API mf_status mf_mlp_get_option(const mf_mlp* model, const char* key, int64_t* value);
 
 #ifdef __cplusplus
 }

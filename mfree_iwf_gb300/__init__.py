@@ -130,6 +130,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_get_time": (C.c_int32, [C.c_void_p, C.c_int32, _DP]),
         "mf_num_particles": (C.c_int32, [C.c_void_p, C.c_int32, _UP]),
         "mf_get_stress": (C.c_int32, [C.c_void_p, C.c_int32, _DP, _DP, _DP, _DP]),
+        "mf_get_state_all_async": (C.c_int32, [C.c_void_p, C.POINTER(MfState)]),
+        "mf_set_state_all_async": (C.c_int32, [C.c_void_p, C.POINTER(MfParticles)]),
         "mf_get_failed": (C.c_int32, [C.c_void_p, _UP, C.c_uint32]),
         "mf_get_gauss_state": (C.c_int32, [C.c_void_p, _DP, _DP, _DP, _DP, C.c_uint32, _UP]),
         "mf_get_neighbors": (C.c_int32, [C.c_void_p, C.c_int32, _UP, _UP, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -370,6 +372,24 @@ class Simulation:
         self._check(self._lib.mf_get_gauss_state(self._h, *[_dptr(out[k]) for k in ("rho", "Sxx", "Sxy", "Syy")],
                                                  n.value, ctypes.byref(n)), "mf_get_gauss_state")
         return out
+
+    def get_state_all_async_into(self, out: Dict[str, np.ndarray]) -> None:
+        """Stream-ordered get_state_all_into: queued behind the steps issued so far; the
+        arrays (contiguous float64, pinned for asynchronous copies) hold the state after
+        synchronize()."""
+        s = MfState(*[_dptr(out.get(f)) for f in _SFIELDS])
+        self._check(self._lib.mf_get_state_all_async(self._h, ctypes.byref(s)), "mf_get_state_all_async")
+
+    def set_state_all_async(self, arrays: Dict[str, np.ndarray]) -> None:
+        """Stream-ordered set_state_all from contiguous float64 arrays (pinned for
+        asynchronous copies; kept alive and unchanged until synchronize()).  Each field
+        waits for an earlier get_state_all_async of the same field."""
+        for f in _PFIELDS:
+            a = arrays.get(f)
+            if a is not None and not (a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]):
+                raise ValueError(f"{f}: the asynchronous transfer needs contiguous float64 arrays")
+        p = MfParticles(*[_dptr(arrays.get(f)) for f in _PFIELDS])
+        self._check(self._lib.mf_set_state_all_async(self._h, ctypes.byref(p)), "mf_set_state_all_async")
 
     def time(self, body: int = 0) -> float:
         t = ctypes.c_double()

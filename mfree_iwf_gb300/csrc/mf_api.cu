@@ -254,6 +254,7 @@ struct mf_ctx {
 	DevBuf<uint16_t> rw_cnt;
 	DevBuf<float4> rw_XF, rw_G;
 	bool rw_ok = false;
+	uint64_t rw_words = 0;
 	DevBuf<float> qw32, m32, h32;
 	DevBuf<float4> recA, recB, dA32;
 	DevBuf<float4> recB2;             // mixed TL: records ping-pong between recB and recB2 by stage parity
@@ -299,6 +300,12 @@ struct mf_ctx {
 	unsigned char* io_host = nullptr;
 	size_t io_host_bytes = 0;
 	cudaStream_t io_stream = nullptr;
+	// stream-ordered state transfers (mf_*_state_all_async): a device->host and a
+	// host->device copy stream, FP64 staging of all fields, one event per field
+	cudaStream_t xs_d2h = nullptr, xs_h2d = nullptr;
+	cudaEvent_t xe_main = nullptr, xe_h2d = nullptr, xe_d2h[10] = {};
+	bool xe_pending[10] = {};  // a get of field q was queued since the last synchronize
+	DevBuf<double> x_out, x_in;
 	cudaEvent_t io_ready = nullptr;
 	std::thread io_thread;
 	mf_status io_status = MF_OK;
@@ -741,6 +748,7 @@ mf_status build_tl_runs(mf_ctx* c, const std::vector<uint32_t>& off) {
 		if (words.size() - roff[i] > 0xffffu) return fail(c, MF_ERR_CAPACITY, "more than 65535 runs in one list");
 	}
 	roff[n] = (uint32_t)words.size();
+	c->rw_words = words.size();
 	const uint32_t ns = (n + 31) / 32;
 	std::vector<uint32_t> sl(ns + 1, 0);
 	uint64_t ent = 0;
@@ -2087,6 +2095,17 @@ mf_status contact_run(mf_ctx* c) {
 
 mf_ctx::~mf_ctx() {
 	if (io_thread.joinable()) io_thread.join();
+	for (cudaStream_t xs : {xs_d2h, xs_h2d})
+		if (xs) {
+			cudaStreamSynchronize(xs);
+			cudaStreamDestroy(xs);
+		}
+	for (cudaEvent_t e : {xe_main, xe_h2d})
+		if (e) cudaEventDestroy(e);
+	for (cudaEvent_t e : xe_d2h)
+		if (e) cudaEventDestroy(e);
+	x_out.free();
+	x_in.free();
 	if (io_stream) cudaStreamDestroy(io_stream);
 	if (io_ready) cudaEventDestroy(io_ready);
 	if (io_host) cudaFreeHost(io_host);
@@ -2446,6 +2465,9 @@ MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
 MF_API mf_status mf_synchronize(mf_ctx* c) {
 	if (!c) return MF_ERR_ARG;
 	if (!c->ready) return MF_OK;
+	for (cudaStream_t xs : {c->xs_d2h, c->xs_h2d})
+		if (xs) CK(cudaStreamSynchronize(xs));
+	std::fill(c->xe_pending, c->xe_pending + 10, false);
 	return check_status(c);
 }
 
@@ -2657,6 +2679,88 @@ MF_API mf_status mf_set_state_all(mf_ctx* c, const mf_particles* p) {
 	if (pst != MF_OK) return pst;
 	CK(cudaStreamSynchronize(c->stream));
 	return MF_OK;
+}
+
+// ---- stream-ordered transfers of all bodies' state
+namespace {
+mf_status xfer_setup(mf_ctx* c) {
+	if (c->xs_d2h) return MF_OK;
+	CK(cudaStreamCreateWithFlags(&c->xs_d2h, cudaStreamNonBlocking));
+	CK(cudaStreamCreateWithFlags(&c->xs_h2d, cudaStreamNonBlocking));
+	CK(cudaEventCreateWithFlags(&c->xe_main, cudaEventDisableTiming));
+	CK(cudaEventCreateWithFlags(&c->xe_h2d, cudaEventDisableTiming));
+	for (auto& e : c->xe_d2h) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+	CK(c->x_out.alloc(10 * (size_t)c->n_total));
+	CK(c->x_in.alloc(8 * (size_t)c->n_total));
+	return MF_OK;
+}
+}  // namespace
+
+// The state of every body into out (host memory, pinned for the copies to run
+// asynchronously): stream-ordered after the steps already queued; returns at once.
+// The fields are valid after mf_synchronize.  One kernel writes all fields as FP64
+// into device staging, then each field goes to the host by its own copy on the
+// device->host copy stream.
+MF_API mf_status mf_get_state_all_async(mf_ctx* c, const mf_state* out) {
+	if (!c || !out) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK)
+		return fail(c, MF_ERR_PIPELINE, "the asynchronous transfers cover the strong forms");
+	CK(cudaSetDevice(c->cfg.device));
+	if ((st = xfer_setup(c)) != MF_OK) return st;
+	const uint32_t n = c->n_total;
+	double* o[10] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy, out->fcx, out->fcy};
+	StateIO io = state_io(c, false);
+	for (int q = 0; q < 10; q++) io.dst[q] = o[q] ? c->x_out.p + (size_t)q * n : nullptr;
+	// the staging is rewritten only once the previous get's copies have left it
+	CK(cudaStreamWaitEvent(c->stream, c->xe_d2h[9], 0));
+	if (n) k_get_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
+	CK(cudaGetLastError());
+	CK(cudaEventRecord(c->xe_main, c->stream));
+	CK(cudaStreamWaitEvent(c->xs_d2h, c->xe_main, 0));
+	for (int q = 0; q < 10; q++) {
+		if (o[q]) {
+			CK(cudaMemcpyAsync(o[q], c->x_out.p + (size_t)q * n, (size_t)n * 8, cudaMemcpyDeviceToHost, c->xs_d2h));
+			c->xe_pending[q] = true;
+		}
+		CK(cudaEventRecord(c->xe_d2h[q], c->xs_d2h));
+	}
+	return MF_OK;
+}
+
+// Overwrite the state of every body from p (host memory, pinned): stream-ordered;
+// returns at once, and the host arrays may be reused after mf_synchronize.  Each field
+// is copied on the host->device copy stream, after the device->host copy of the same
+// field by an earlier mf_get_state_all_async (so a get followed by a set of the same
+// host arrays reads what the get wrote, and the two directions overlap field by field);
+// then one kernel writes the device state from the staging.
+MF_API mf_status mf_set_state_all_async(mf_ctx* c, const mf_particles* p) {
+	if (!c || !p) return MF_ERR_ARG;
+	mf_status st = finalize(c);
+	if (st != MF_OK) return st;
+	if (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK)
+		return fail(c, MF_ERR_PIPELINE, "the asynchronous transfers cover the strong forms");
+	CK(cudaSetDevice(c->cfg.device));
+	if ((st = xfer_setup(c)) != MF_OK) return st;
+	const uint32_t n = c->n_total;
+	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
+	// the staging is rewritten only after the previous set's kernel has read it
+	CK(cudaEventRecord(c->xe_main, c->stream));
+	CK(cudaStreamWaitEvent(c->xs_h2d, c->xe_main, 0));
+	for (int q = 0; q < 8; q++) {
+		if (!src[q]) continue;
+		if (c->xe_pending[q]) CK(cudaStreamWaitEvent(c->xs_h2d, c->xe_d2h[q], 0));
+		CK(cudaMemcpyAsync(c->x_in.p + (size_t)q * n, src[q], (size_t)n * 8, cudaMemcpyHostToDevice, c->xs_h2d));
+	}
+	CK(cudaEventRecord(c->xe_h2d, c->xs_h2d));
+	CK(cudaStreamWaitEvent(c->stream, c->xe_h2d, 0));
+	StateIO io = state_io(c, c->cfg.method != MF_METHOD_UL);  // TL stage 0 starts from its own copy (set 2)
+	for (int q = 0; q < 8; q++) io.src[q] = src[q] ? c->x_in.p + (size_t)q * n : nullptr;
+	if (n) k_set_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
+	CK(cudaGetLastError());
+	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the new state
+	return tl_prepack(c);
 }
 
 // The stress the method evaluates at the body's current state.  TL (strong form):
@@ -3111,6 +3215,10 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	}
 	if (!strcmp(key, "tl_runs_built")) {
 		*value = c->rw_ok ? 1 : 0;
+		return MF_OK;
+	}
+	if (!strcmp(key, "tl_run_words")) {  // run words over all rows (the lists as runs)
+		*value = (int64_t)c->rw_words;
 		return MF_OK;
 	}
 	if (!strcmp(key, "tl_tiles_built")) {

@@ -23,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched from the driver at run time
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -271,6 +272,251 @@ __global__ void __launch_bounds__(256) k_gemm_nt(GemmArgs g) {
 			}
 }
 
+// ---- The forward products on Blackwell's tensor cores: tcgen05.mma with the FP32
+// accumulators in tensor memory (TMEM), operands staged by TMA.  Z = H W^T for K a
+// multiple of 64 and N <= 256 (the 256-wide layers and the output layer).
+//
+// One persistent CTA per (slice of the row tiles, member); 6 warps with fixed roles:
+//   warp 0     one thread issues the TMA copies: the member's whole W once (N x K,
+//              K-major, 128-byte swizzled, resident for all of the CTA's tiles), then
+//              128-row x 64-column slices of H through a 4-stage ring;
+//   warp 1     allocates TMEM (two accumulators of N columns, so that a tile's
+//              epilogue overlaps the next tile's products); one thread issues
+//              tcgen05.mma (M = 128, N, K = 16, BF16 x BF16 -> FP32) and tcgen05.commit,
+//              which releases each H stage and, after a tile's last slice, hands the
+//              accumulator to the epilogue;
+//   warps 2-5  the epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31 -- one tile row
+//              per thread -- 32 columns at a time (tcgen05.ld), adds the bias, applies
+//              ReLU and stores FP32 and/or BF16 rows.
+// Every mbarrier wait is bounded: past the limit the thread sets the error word and
+// leaves its loop; all threads meet at the end, where warp 1 frees the TMEM.
+namespace tc {
+
+constexpr int BM = 128;      // tile rows: one TMEM lane each
+constexpr int BK = 64;       // K per stage: 64 BF16 = 128 bytes, one 128-byte swizzle span
+constexpr int STAGES = 4;
+constexpr int THREADS = 192;
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(b)) : "memory");
+}
+// Wait until the phase of parity `ph` has completed; false after SPIN_LIMIT tries.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t ph) {
+	const uint32_t a = saddr(b);
+	for (uint32_t it = 0; it < SPIN_LIMIT; it++) {
+		uint32_t done;
+		asm volatile(
+		    "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+		    : "=r"(done)
+		    : "r"(a), "r"(ph)
+		    : "memory");
+		if (done) return true;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+	asm volatile(
+	    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+	        saddr(dst)),
+	    "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(saddr(bar))
+	    : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int x, int y, int z, uint64_t* bar) {
+	asm volatile(
+	    "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+	        saddr(dst)),
+	    "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
+	    : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte-swizzled layout
+// that TMA writes: rows of 128 bytes, 8-row groups 1024 bytes apart (stride byte
+// offset), descriptor version 1, swizzle mode 2 (128 bytes).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t a) {
+	return (uint64_t)((a >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+	       ((uint64_t)2 << 61);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+	asm volatile(
+	    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+	    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bar))
+	             : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+	             : "r"(taddr));
+	asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// dynamic shared memory: the member's W (K/64 blocks of N rows x 128 B), the H stages
+// (128 rows x 128 B each), the mbarriers and the TMEM address; +1 KB for the 1 KB
+// alignment that the 128-byte swizzle needs
+__host__ __device__ constexpr size_t smem_bytes(int N, int K) {
+	return 1024 + (size_t)(K / BK) * N * 128 + (size_t)STAGES * BM * 128 + 8 * (1 + 2 * STAGES + 4) + 16;
+}
+__host__ __device__ constexpr uint32_t tmem_cols(int N) { return N <= 128 ? 256u : 512u; }
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, GemmArgs g,
+              int rows_per_member, uint32_t* err) {
+	extern __shared__ uint8_t smem_raw[];
+	const int N = g.N, KB = g.K / BK, G = gridDim.x, z = blockIdx.y;
+	const uint32_t raw = saddr(smem_raw);
+	uint8_t* sW = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+	uint8_t* sA = sW + (size_t)KB * N * 128;
+	uint64_t* w_full = reinterpret_cast<uint64_t*>(sA + (size_t)STAGES * BM * 128);
+	uint64_t* a_full = w_full + 1;
+	uint64_t* a_empty = a_full + STAGES;
+	uint64_t* acc_full = a_empty + STAGES;
+	uint64_t* acc_empty = acc_full + 2;
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int tiles = (g.M + BM - 1) / BM;
+	const uint32_t ncols = tmem_cols(N), acc_stride = ncols / 2;
+
+	if (threadIdx.x == 0) {
+		mbar_init(w_full, 1);
+		for (int s = 0; s < STAGES; s++) {
+			mbar_init(a_full + s, 1);
+			mbar_init(a_empty + s, 1);
+		}
+		for (int b = 0; b < 2; b++) {
+			mbar_init(acc_full + b, 1);
+			mbar_init(acc_empty + b, 4);  // one arrival per epilogue warp
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+	}
+	if (warp == 1) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tmem_slot)),
+		             "r"(ncols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+	}
+	fence_before();
+	__syncthreads();
+	fence_after();
+	const uint32_t tmem = *tmem_slot;
+	bool ok = true;
+
+	if (warp == 0) {
+		if (lane == 0) {  // TMA producer
+			mbar_expect_tx(w_full, (uint32_t)(KB * N * 128));
+			for (int kb = 0; kb < KB; kb++) tma_load_3d(sW + (size_t)kb * N * 128, &tmW, kb * BK, 0, z, w_full);
+			uint32_t it = 0;
+			for (int t = blockIdx.x; t < tiles && ok; t += G)
+				for (int kb = 0; kb < KB; kb++, it++) {
+					const int s = (int)(it % STAGES);
+					const uint32_t use = it / STAGES;
+					if (use > 0 && !(ok = mbar_wait(a_empty + s, (use - 1) & 1u))) break;
+					mbar_expect_tx(a_full + s, BM * 128);
+					tma_load_2d(sA + (size_t)s * BM * 128, &tmA, kb * BK, z * rows_per_member + t * BM, a_full + s);
+				}
+		}
+	} else if (warp == 1) {
+		if (lane == 0) {  // MMA issuer
+			const uint32_t idesc = idesc_bf16(BM, N);
+			ok = mbar_wait(w_full, 0);
+			uint32_t it = 0, i = 0;
+			for (int t = blockIdx.x; t < tiles && ok; t += G, i++) {
+				const uint32_t ab = i & 1u, use = i >> 1;
+				if (use > 0 && !(ok = mbar_wait(acc_empty + ab, (use - 1) & 1u))) break;
+				fence_after();
+				const uint32_t d = tmem + ab * acc_stride;
+				for (int kb = 0; kb < KB; kb++, it++) {
+					const int s = (int)(it % STAGES);
+					if (!(ok = mbar_wait(a_full + s, (it / STAGES) & 1u))) break;
+					fence_after();
+					const uint32_t a0 = saddr(sA + (size_t)s * BM * 128), b0 = saddr(sW + (size_t)kb * N * 128);
+#pragma unroll
+					for (int k = 0; k < BK / 16; k++)  // K = 16 per instruction: 32 bytes along the swizzled row
+						mma_bf16(d, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k), idesc, (kb | k) != 0);
+					mma_commit(a_empty + s);  // the stage is free once these products are done
+				}
+				if (ok) mma_commit(acc_full + ab);
+			}
+		}
+	} else {  // epilogue
+		const int q = warp & 3;
+		const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
+		float* C = g.C ? g.C + z * g.sC : nullptr;
+		bf16* Cb = g.Cb ? g.Cb + z * g.sCb : nullptr;
+		uint32_t i = 0;
+		for (int t = blockIdx.x; t < tiles && ok; t += G, i++) {
+			const uint32_t ab = i & 1u;
+			if (!(ok = mbar_wait(acc_full + ab, (i >> 1) & 1u))) break;
+			fence_after();
+			const int m = t * BM + 32 * q + lane;
+			const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + ab * acc_stride;
+			for (int c0 = 0; c0 < N; c0 += 32) {
+				uint32_t r[32];
+				tmem_ld32(taddr + (uint32_t)c0, r);  // (columns past N, when N % 32 != 0, are not stored)
+				if (m >= g.M) continue;
+				float v[32];
+#pragma unroll
+				for (int j = 0; j < 32; j++) {
+					float x = __uint_as_float(r[j]);
+					if (bias && c0 + j < N) x += bias[c0 + j];
+					if (g.relu) x = fmaxf(x, 0.f);
+					v[j] = x;
+				}
+				if (C) {
+					float4* dst = reinterpret_cast<float4*>(C + (long long)m * g.ldc + c0);
+#pragma unroll
+					for (int j = 0; j < 8; j++)
+						if (c0 + 4 * j < N) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+				}
+				if (Cb) {
+					uint4* dst = reinterpret_cast<uint4*>(Cb + (long long)m * g.ldcb + c0);
+#pragma unroll
+					for (int j = 0; j < 4; j++)
+						if (c0 + 8 * j < N) {
+							__nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * j], v[8 * j + 1]);
+							__nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * j + 2], v[8 * j + 3]);
+							__nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * j + 4], v[8 * j + 5]);
+							__nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * j + 6], v[8 * j + 7]);
+							dst[j] = make_uint4(*reinterpret_cast<uint32_t*>(&h0), *reinterpret_cast<uint32_t*>(&h1),
+							                    *reinterpret_cast<uint32_t*>(&h2), *reinterpret_cast<uint32_t*>(&h3));
+						}
+				}
+			}
+			fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(acc_empty + ab);
+		}
+	}
+	if (!ok) atomicOr(err, 1u);
+	fence_before();
+	__syncthreads();
+	fence_after();
+	if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
+}  // namespace tc
+
 // Training control block in device memory, read by the graph's kernels on every replay.
 struct TrainCtl {
 	uint32_t step;   // Adam steps taken so far (the current step's number inside a step)
@@ -464,6 +710,9 @@ struct mf_mlp {
 	cudaGraphExec_t graph = nullptr;
 	uint64_t launches = 0, step_launches = 0;
 	std::string err;
+	bool tc = false;       // forward products with K % 64 == 0 on tcgen05 (else mma.sync)
+	int sm_count = 1;
+	Buf<uint32_t> dev_err; // set by a bounded wait of the tcgen05 GEMM that gave up
 	~mf_mlp() {
 		if (graph) cudaGraphExecDestroy(graph);
 		if (stream) cudaStreamDestroy(stream);
@@ -482,9 +731,64 @@ mf_status mlp_fail(mf_mlp* m, const std::string& what, cudaError_t e) {
 		if (e_ != cudaSuccess) return mlp_fail(m, #call, e_); \
 	} while (0)
 
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda)
+EncodeTiled tensor_map_encoder() {
+	static EncodeTiled fn = [] {
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q{};
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess)
+			p = nullptr;
+		return reinterpret_cast<EncodeTiled>(p);
+	}();
+	return fn;
+}
+
+constexpr size_t TC_SMEM_MAX = 227 * 1024;
+
+// The tcgen05 path takes the forward products Z = H W^T whose operands are contiguous
+// K-major rows with K a multiple of 64, N a multiple of 16 up to 256, and whose staged
+// operands fit the shared memory; H is [members][rows][K], W [N][K] per member.
+bool tc_eligible(const mf_mlp* m, bool ta, bool tb, const GemmArgs& g) {
+	return m->tc && !ta && tb && g.K % tc::BK == 0 && g.N % 16 == 0 && g.N <= 256 && g.lda == g.K && g.ldb == g.K &&
+	       g.sA == (long long)m->rows * g.K && g.M <= m->rows && tc::smem_bytes(g.N, g.K) <= TC_SMEM_MAX &&
+	       (!g.Cb || g.ldcb % 8 == 0) && (!g.C || g.ldc % 4 == 0) && g.sB % 8 == 0;
+}
+
+cudaError_t gemm_tc(mf_mlp* m, const GemmArgs& g) {
+	EncodeTiled enc = tensor_map_encoder();
+	CUtensorMap tA, tW;
+	// H as [members * rows][K]; boxes of 64 K x 128 rows, 128-byte swizzle, zero fill past the end
+	const cuuint64_t dA[2] = {(cuuint64_t)g.K, (cuuint64_t)m->members * m->rows};
+	const cuuint64_t sA[1] = {(cuuint64_t)g.K * 2};
+	const cuuint32_t bA[2] = {tc::BK, tc::BM}, e1[3] = {1, 1, 1};
+	// W as [members][N][K] (member stride sB elements); boxes of 64 K x N rows x 1 member
+	const cuuint64_t dW[3] = {(cuuint64_t)g.K, (cuuint64_t)g.N, (cuuint64_t)m->members};
+	const cuuint64_t sW[2] = {(cuuint64_t)g.K * 2, (cuuint64_t)g.sB * 2};
+	const cuuint32_t bW[3] = {tc::BK, (cuuint32_t)g.N, 1};
+	if (enc(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(g.A), dA, sA, bA, e1,
+	        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+	        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+	    enc(&tW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(g.B), dW, sW, bW, e1,
+	        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+	        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+		return cudaErrorInvalidValue;
+	const int tiles = (g.M + tc::BM - 1) / tc::BM;
+	const int G = std::max(1, std::min(tiles, m->sm_count / m->members));
+	tc::k_gemm_tc<<<dim3(G, m->members), tc::THREADS, tc::smem_bytes(g.N, g.K), m->stream>>>(tA, tW, g, m->rows,
+	                                                                                         m->dev_err.p);
+	m->launches++;
+	return cudaGetLastError();
+}
+
 cudaError_t gemm(mf_mlp* m, bool ta, bool tb, GemmArgs g) {
 	dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, m->members);
 	cudaStream_t s = m->stream;
+	if (tc_eligible(m, ta, tb, g)) return gemm_tc(m, g);
 	if (!ta && tb && g.K % 8 == 0 && g.lda % 8 == 0 && g.ldb % 8 == 0 && g.N % 2 == 0 && (!g.C || g.ldc % 2 == 0) &&
 	    (!g.Cb || g.ldcb % 2 == 0)) {
 		dim3 gnt((g.N + NT_BN - 1) / NT_BN, (g.M + NT_BM - 1) / NT_BM, m->members);
@@ -580,6 +884,17 @@ cudaError_t train_step_launches(mf_mlp* m) {
 	k_step_end<<<1, 64, 0, s>>>(m->ctl.p, m->loss.p, m->members);
 	m->launches++;
 	return cudaGetLastError();
+}
+
+// MF_ERR_TIMEOUT (and the error word cleared) when a tcgen05 GEMM gave up a wait
+mf_status tc_status(mf_mlp* m) {
+	if (!m->tc) return MF_OK;
+	uint32_t e = 0;
+	MCK(cudaMemcpy(&e, m->dev_err.p, 4, cudaMemcpyDeviceToHost));
+	if (!e) return MF_OK;
+	MCK(cudaMemset(m->dev_err.p, 0, 4));
+	m->err = "tcgen05 GEMM: a bounded wait gave up";
+	return MF_ERR_TIMEOUT;
 }
 
 void drop_graph(mf_mlp* m) {
@@ -682,6 +997,16 @@ MF_API mf_status mf_mlp_create(const mf_mlp_config* cfg, mf_mlp** out) {
 		MCK(m->Xin.alloc((size_t)m->members * m->rows * m->dims[0]));
 		MCK(m->Yin.alloc((size_t)m->members * m->rows * m->dims[m->L]));
 		MCK(m->ctl.alloc(1));
+		MCK(m->dev_err.alloc(1));
+		MCK(cudaMemset(m->dev_err.p, 0, 4));
+		// the tcgen05 forward products on Blackwell (compute capability 10.x), where the
+		// driver provides the tensor-map encoder
+		int major = 0;
+		MCK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, m->device));
+		MCK(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
+		m->tc = major == 10 && tensor_map_encoder() != nullptr;
+		if (m->tc)
+			MCK(cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
 		m->h_ctl = TrainCtl{};
 		m->h_ctl.seed = cfg->seed * 0x2545F4914F6CDD1Dull + 1;
 		MCK(cudaMemcpy(m->ctl.p, &m->h_ctl, sizeof(TrainCtl), cudaMemcpyHostToDevice));
@@ -826,7 +1151,7 @@ MF_API mf_status mf_mlp_train(mf_mlp* m, int32_t steps, float lr0, float lr1, fl
 	if (loss_history)
 		MCK(cudaMemcpyAsync(loss_history, m->hist.p, (size_t)steps * m->members * 4, cudaMemcpyDefault, s));
 	MCK(cudaStreamSynchronize(s));
-	return MF_OK;
+	return tc_status(m);
 }
 
 MF_API mf_status mf_mlp_predict(mf_mlp* m, const float* x, int32_t n, float* y) {
@@ -852,7 +1177,7 @@ MF_API mf_status mf_mlp_predict(mf_mlp* m, const float* x, int32_t n, float* y) 
 		                      (size_t)b * out * 4, m->members, cudaMemcpyDefault, s));
 	}
 	MCK(cudaStreamSynchronize(s));
-	return MF_OK;
+	return tc_status(m);
 }
 
 MF_API mf_status mf_mlp_launch_count(const mf_mlp* m, uint64_t* launches) {
@@ -865,6 +1190,35 @@ MF_API mf_status mf_mlp_get_stream(const mf_mlp* m, void** stream) {
 	if (!m || !stream) return MF_ERR_ARG;
 	*stream = (void*)m->stream;
 	return MF_OK;
+}
+
+MF_API mf_status mf_mlp_set_option(mf_mlp* m, const char* key, int64_t value) {
+	if (!m || !key) return MF_ERR_ARG;
+	if (!strcmp(key, "tcgen05")) {
+		if (value != 0 && value != 1) return MF_ERR_ARG;
+		int major = 0;
+		MCK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, m->device));
+		if (value && !(major == 10 && tensor_map_encoder())) {
+			m->err = "tcgen05: needs a compute capability 10.x device and the driver's tensor-map encoder";
+			return MF_ERR_STATE;
+		}
+		if (value && !m->tc)
+			MCK(cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+		m->tc = value != 0;
+		drop_graph(m);  // the captured training step holds the old launches
+		return MF_OK;
+	}
+	m->err = std::string("unknown option ") + key;
+	return MF_ERR_ARG;
+}
+
+MF_API mf_status mf_mlp_get_option(const mf_mlp* m, const char* key, int64_t* value) {
+	if (!m || !key || !value) return MF_ERR_ARG;
+	if (!strcmp(key, "tcgen05")) {
+		*value = m->tc ? 1 : 0;
+		return MF_OK;
+	}
+	return MF_ERR_ARG;
 }
 
 }  // extern "C"

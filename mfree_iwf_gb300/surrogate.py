@@ -305,6 +305,8 @@ def _mlp_lib():
         "mf_mlp_predict": (C.c_int32, [C.c_void_p, FP, C.c_int32, FP]),
         "mf_mlp_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
         "mf_mlp_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
+        "mf_mlp_set_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_int64]),
+        "mf_mlp_get_option": (C.c_int32, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -401,6 +403,14 @@ class Mlp:
         n = ctypes.c_uint64()
         self._check(self._lib.mf_mlp_launch_count(self._h, ctypes.byref(n)), "mf_mlp_launch_count")
         return n.value
+
+    def set_option(self, key: str, value: int) -> None:
+        self._check(self._lib.mf_mlp_set_option(self._h, key.encode(), int(value)), f"mf_mlp_set_option({key})")
+
+    def get_option(self, key: str) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.mf_mlp_get_option(self._h, key.encode(), ctypes.byref(v)), f"mf_mlp_get_option({key})")
+        return v.value
 
 
 # ---------------------------------------------------------------- the screen
@@ -544,14 +554,18 @@ def run_experiment(n_train: int = 20000, n_test: int = 1000, val_frac: float = 0
 
 
 
-def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device: int = 0) -> dict:
+def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device: int = 0,
+                   tcgen05: Optional[int] = None) -> dict:
     """Inference throughput of the ensemble on device-resident inputs: `chunks` passes of
     `rows` rows through 6 -> 256 -> 256 -> 256 -> 66, timed with CUDA events on the
-    library's stream; FLOPs counted on the true (unpadded) layer sizes."""
+    library's stream; FLOPs counted on the true (unpadded) layer sizes.  `tcgen05`
+    selects the tensor-core path of the forward products (None: the library's default)."""
     import torch
 
     dims = [len(FEATURE_LIMITS), 256, 256, 256, N_OUT]
     mlp = Mlp(dims, members=members, max_batch=rows, seed=1, device=device)
+    if tcgen05 is not None:
+        mlp.set_option("tcgen05", tcgen05)
     n = rows * chunks
     x = torch.rand(n, dims[0], device=f"cuda:{device}", dtype=torch.float32) * 2 - 1
     y = torch.empty(members, n, dims[-1], device=f"cuda:{device}", dtype=torch.float32)
@@ -573,9 +587,11 @@ def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device
     secs = e0.elapsed_time(e1) / 1e3 / reps
     flop_row = 2 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
     flops = flop_row * members * n
+    tc = mlp.get_option("tcgen05")
     mlp.close()
     return {"rows_per_pass": rows, "instances": n, "members": members, "seconds": secs,
-            "instances_per_s": n / secs, "tflops": flops / secs / 1e12, "flop_per_instance_member": flop_row}
+            "instances_per_s": n / secs, "tflops": flops / secs / 1e12, "flop_per_instance_member": flop_row,
+            "tcgen05": tc}
 
 
 if __name__ == "__main__":
@@ -589,8 +605,10 @@ if __name__ == "__main__":
     ap.add_argument("--data", default=None, help=".npz cache of the training set's solver outputs")
     ap.add_argument("--out", default=None, help="write the JSON result here too")
     ap.add_argument("--gemm-bench", action="store_true", help="only time the ensemble's inference GEMMs")
+    ap.add_argument("--tcgen05", type=int, choices=[0, 1], default=None, help="with --gemm-bench: the GEMM path")
     a = ap.parse_args()
-    r = gemm_benchmark() if a.gemm_bench else run_experiment(a.train, a.test, train_steps=a.steps, data=a.data)
+    r = (gemm_benchmark(tcgen05=a.tcgen05) if a.gemm_bench
+         else run_experiment(a.train, a.test, train_steps=a.steps, data=a.data))
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:

@@ -180,3 +180,53 @@ def test_screened_sweep_beats_the_solver(lib):
     np.testing.assert_array_equal(res.targets[fb], test_t[fb])  # fallbacks are the solver's own answer
     t_screened = res.seconds_network + res.seconds_solver
     assert t_screened < truth.seconds + truth.setup_seconds
+
+
+# ------------------------------------------------------- tcgen05 GEMM
+@pytest.mark.parametrize("rows", [300, 4096])
+def test_tcgen05_forward_matches_mma_sync(lib, rows):
+    """The forward products with K a multiple of 64 (the 256-wide layers and the output
+    layer) on tcgen05 -- TMEM accumulators, TMA-staged 128-byte-swizzled operands --
+    against the mma.sync kernels on the same parameters and inputs: both accumulate the
+    same BF16 products in FP32 in different orders, so the FP32 outputs agree to within
+    the BF16 rounding of the hidden activations they pass between layers (relative L2
+    <= 5e-3 per member; in practice ~1e-3).  300 rows: one partial tile per member;
+    4096 rows: 32 tiles per member, several per persistent CTA, both accumulators."""
+    from mfree_iwf_gb300.surrogate import Mlp
+    mlp = Mlp(DIMS, members=5, max_batch=rows, seed=11)
+    assert mlp.get_option("tcgen05") == 1  # the default on a GB300
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-1, 1, size=(rows, DIMS[0])).astype(np.float32)
+    y_tc = mlp.predict(x)
+    mlp.set_option("tcgen05", 0)
+    y_ref = mlp.predict(x)
+    mlp.set_option("tcgen05", 1)
+    y_tc2 = mlp.predict(x)
+    mlp.close()
+    assert y_tc.shape == (5, rows, DIMS[-1])
+    np.testing.assert_array_equal(y_tc, y_tc2)  # deterministic
+    for z in range(5):
+        e = _rel(y_tc[z], y_ref[z])
+        print(f"member {z}: relative L2 {e:.2e}")
+        assert e <= 5e-3, (z, e)
+
+
+def test_tcgen05_training_matches_mma_sync(lib):
+    """A short training run (captured step graph) with the forward products on tcgen05
+    follows the mma.sync run: the loss histories agree within 2 % and both fall."""
+    from mfree_iwf_gb300.surrogate import Mlp
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, size=(2048, DIMS[0])).astype(np.float32)
+    y = np.tanh(x @ rng.normal(size=(DIMS[0], DIMS[-1])).astype(np.float32))
+    hist = {}
+    for tc in (1, 0):
+        mlp = Mlp(DIMS, members=3, max_batch=512, seed=2)
+        mlp.set_option("tcgen05", tc)
+        mlp.set_data(x, y)
+        hist[tc] = mlp.train(60, 1e-3, 1e-4)
+        mlp.close()
+    for tc in (1, 0):
+        assert hist[tc][-5:].mean() < 0.5 * hist[tc][:5].mean(), tc
+    e = _rel(hist[1][-10:], hist[0][-10:])
+    print(f"loss histories: relative L2 {e:.2e}")
+    assert e <= 2e-2
