@@ -236,6 +236,9 @@ def reference_arm(args, cfg_desc):
 # smaller case of the same workload; the bench scales it by its own rows per launch.
 # (bytes per row, description of the capture)
 MEASURED_TRAFFIC = {
+    # k_tlB32r, stages 0-3 of one step at dx = 0.1 mm: (140.7 + 3 x 161.9) MB / 4 / 439,860 rows
+    ("c2", "mixed", "TL pass B"): (356.0, "ncu, the run-walk pass B alone, the four stages of one step of the ring "
+                                          "impact at dx = 0.1 mm (439,860 rows), mean per row, scaled by rows"),
     ("c3", "mixed", "weak TL Gauss-point pass"): (367.8, "ncu, the Gauss-point pass alone at dx = 0.1 mm "
                                                          "(800k Gauss points), scaled by Gauss points"),
 }
@@ -589,6 +592,8 @@ def ours(args, cfg_desc):
             roof["frac_survey_model"] = per_ps / 4 * per_launch_rows / (kms / klaunch / 1e3) / 1e9 / peaks["hbm_gbs"]
             roof["step_frac_survey_model"] = per_ps * value / world / 1e9 / peaks["hbm_gbs"]
         t = MEASURED_TRAFFIC.get((args.workload, args.precision, names[dom]))
+        if t is not None and names[dom] == "TL pass B" and not runs_per_row:
+            t = None  # (the capture is of the run-walk pass)
         if t is not None:
             roof["traffic"] = t[0] * per_launch_rows
             roof["traffic_source"] = t[1]
