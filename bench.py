@@ -16,8 +16,8 @@ Metric: particle-steps/s = particles x RK4 steps / time, the whole step included
                   [--precision mixed|fp64|fp64_strict]
 
 The family workloads (corot, godunov, potential, ulweak, tlweak, tlfem, ulfem) are
-ensembles of the reference's own two-ring set-up of that family (ulweak and ulfem: FP64
-forms only).
+ensembles of the reference's own two-ring set-up of that family (ulfem: FP64 forms
+only).
 
 With --impl reference it times the reference's CPU implementation of the same path
 (single-threaded; the reference's own build where this host has one, else the oracle
@@ -54,7 +54,7 @@ def measured_peaks():
 
 
 FAMILIES = ("corot", "godunov", "potential", "ulweak", "tlweak", "tlfem", "ulfem")
-FP64_ONLY = ("ulweak", "ulfem")  # the weak UL form runs in the FP64 forms only
+FP64_ONLY = ("ulfem",)  # the weak UL form on element maps has no mixed form (no per-stage RKPM)
 
 
 def workload_desc(name: str, dx: float | None, instances: int = 512) -> dict:

@@ -244,9 +244,10 @@ MF_API mf_status mf_num_particles(mf_ctx* ctx, int32_t body, uint32_t* n);
  * their initial values; UL: the state's S (Pxy = Pyx = Sxy).  Other methods return
  * MF_ERR_STATE. */
 MF_API mf_status mf_get_stress(mf_ctx* ctx, int32_t body, double* Pxx, double* Pxy, double* Pyx, double* Pyy);
-/* The weak TL form's Gauss-point state (rho, Sxx, Sxy, Syy; NULL fields skipped), the
- * bodies' points concatenated in id order; *n_out = number of Gauss points (all NULL:
- * only the count).  The particles' own rho and S are not evolved by this form. */
+/* The weak forms' Gauss-point (TL) or stress-point (UL) state (rho, Sxx, Sxy, Syy;
+ * NULL fields skipped), the bodies' points concatenated in id order; *n_out = number of
+ * points (all NULL: only the count).  The particles' own S is not evolved by these
+ * forms. */
 /* Per-body failure words of an updated-Lagrangian context (0: running; otherwise the
  * bits of what failed it: 1 neighbour capacity, 2 no neighbour, 4 cell grid, 8
  * non-finite state).  Bodies fail alone only with the option "mask_failed" set

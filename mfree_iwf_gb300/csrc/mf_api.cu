@@ -214,6 +214,7 @@ struct mf_ctx {
 	uint32_t n_total = 0;
 	uint32_t flags = 0;
 	bool mixed = false, strict = false;
+	bool uw_mixed = false;  // weak UL, mixed form: FP32 moment sums in the neighbourhood kernel
 	uint64_t launches = 0;
 	Timing timing;
 
@@ -565,6 +566,10 @@ mf_status finalize(mf_ctx* c) {
 		if (b.actions != acts) return fail(c, MF_ERR_PIPELINE, "all bodies of a context must share one action list");
 	c->mixed = c->cfg.precision == MF_PREC_MIXED;
 	c->strict = c->cfg.precision == MF_PREC_FP64_STRICT;
+	// the weak UL form's mixed precision lives in its neighbourhood kernel alone: its
+	// state and passes stay FP64
+	c->uw_mixed = c->mixed && c->cfg.method == MF_METHOD_UL_WEAK;
+	if (c->uw_mixed) c->mixed = false;
 	mf_status st = MF_OK;
 	if (c->cfg.method == MF_METHOD_UL) {
 		st = validate_ul(c, acts, c->flags);
@@ -1752,7 +1757,6 @@ mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t&
 	                            MF_MATERIAL_STRESS_RATE_JAUMANN_GP, MF_CONTMECH_MOMENTUM_UL, MF_CONTMECH_MOMENTUM_UL_WEAK,
 	                            MF_CONTMECH_CONTINUITY, MF_CONTMECH_CONTINUITY_GP, MF_CONTMECH_ADVECTION,
 	                            MF_INTERPOLATION_INTERPOLATE_VELOCITY, MF_CONTMECH_ADVECTION_GP};
-	if (c->cfg.precision == MF_PREC_MIXED) return fail(c, MF_ERR_PIPELINE, "the weak UL form runs in the FP64 forms");
 	flags = 0;
 	size_t pos = 0;
 	for (int32_t a : acts) {
@@ -1952,9 +1956,9 @@ cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refr
 	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
 	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qs, double* qd) {
 		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
-		                                     qs, qd, c->d_status, c->stream)
+		                                     qs, qd, c->d_status, 0, c->stream)
 		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qs,
-		                                   qd, c->d_status, c->stream);
+		                                   qd, c->d_status, c->uw_mixed ? 1 : 0, c->stream);
 	};
 	const bool riemann = (c->flags & abit(MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS)) != 0;
 	const double* qs = refresh_qw ? nullptr : (riemann ? nullptr : a.qw_base);
@@ -2815,7 +2819,8 @@ MF_API mf_status mf_get_gauss_state(mf_ctx* c, double* rho, double* Sxx, double*
 	if (!c || !n_out) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
-	if (c->cfg.method != MF_METHOD_TL_WEAK) return fail(c, MF_ERR_STATE, "Gauss points belong to the weak TL form");
+	if (c->cfg.method != MF_METHOD_TL_WEAK && c->cfg.method != MF_METHOD_UL_WEAK)
+		return fail(c, MF_ERR_STATE, "Gauss points and stress points belong to the weak forms");
 	const uint32_t ng = c->n_g;
 	*n_out = ng;
 	if (!rho && !Sxx && !Sxy && !Syy) return MF_OK;
@@ -2823,6 +2828,11 @@ MF_API mf_status mf_get_gauss_state(mf_ctx* c, double* rho, double* Sxx, double*
 	CK(cudaSetDevice(c->cfg.device));
 	CK(cudaStreamSynchronize(c->stream));
 	double* out[4] = {rho, Sxx, Sxy, Syy};
+	if (c->cfg.method == MF_METHOD_UL_WEAK) {  // the stress points' state (FP64 in every form)
+		for (int q = 0; q < 4; q++)
+			if (out[q]) CK(cudaMemcpy(out[q], c->uw_g[0][2 + q].p, (size_t)ng * 8, cudaMemcpyDeviceToHost));
+		return check_status(c);
+	}
 	if (c->mixed) {
 		std::vector<uint32_t> gb(ng);
 		CK(cudaMemcpy(gb.data(), c->gp_body.p, (size_t)ng * 4, cudaMemcpyDeviceToHost));

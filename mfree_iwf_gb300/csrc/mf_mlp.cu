@@ -50,6 +50,7 @@ struct GemmArgs {
 	const float* bias;  // per output column, optional
 	long long sBias;
 	int relu;
+	int n_store;  // tcgen05 path: FP32 output columns stored (0: all N), any ldc
 };
 
 constexpr int BM = 64, BN = 64, BK = 32, PADK = BK + 8;  // 80-byte rows: conflict-free fragment loads
@@ -375,8 +376,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 // dynamic shared memory: the member's W (K/64 blocks of N rows x 128 B), the H stages
 // (128 rows x 128 B each), the mbarriers and the TMEM address; +1 KB for the 1 KB
 // alignment that the 128-byte swizzle needs
+constexpr int STG_ROW = 144;  // epilogue staging row: 32 FP32 (or 32 BF16) + 16 bytes of padding
 __host__ __device__ constexpr size_t smem_bytes(int N, int K) {
-	return 1024 + (size_t)(K / BK) * N * 128 + (size_t)STAGES * BM * 128 + 8 * (1 + 2 * STAGES + 4) + 16;
+	return 1024 + (size_t)(K / BK) * N * 128 + (size_t)STAGES * BM * 128 + 4 * 32 * STG_ROW + 8 * (1 + 2 * STAGES + 4) + 16;
 }
 __host__ __device__ constexpr uint32_t tmem_cols(int N) { return N <= 128 ? 256u : 512u; }
 
@@ -388,7 +390,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 	const uint32_t raw = saddr(smem_raw);
 	uint8_t* sW = smem_raw + (((raw + 1023u) & ~1023u) - raw);
 	uint8_t* sA = sW + (size_t)KB * N * 128;
-	uint64_t* w_full = reinterpret_cast<uint64_t*>(sA + (size_t)STAGES * BM * 128);
+	uint8_t* sStg = sA + (size_t)STAGES * BM * 128;  // 4 epilogue warps x 32 rows x STG_ROW
+	uint64_t* w_full = reinterpret_cast<uint64_t*>(sStg + 4 * 32 * STG_ROW);
 	uint64_t* a_full = w_full + 1;
 	uint64_t* a_empty = a_full + STAGES;
 	uint64_t* acc_full = a_empty + STAGES;
@@ -460,21 +463,26 @@ __global__ void __launch_bounds__(THREADS, 1)
 			}
 		}
 	} else {  // epilogue
+		// each warp stages its 32 rows x 32 columns in shared memory (rows padded to
+		// 144 bytes: the 16-byte accesses of 8 lanes hit distinct banks) and writes
+		// them out coalesced -- BF16: 16-byte chunks, 8 rows of 64 bytes per
+		// instruction; FP32: one row of up to 128 bytes per instruction, any ldc
 		const int q = warp & 3;
+		uint8_t* stg = sStg + (size_t)(warp - 2) * 32 * STG_ROW;
 		const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
 		float* C = g.C ? g.C + z * g.sC : nullptr;
 		bf16* Cb = g.Cb ? g.Cb + z * g.sCb : nullptr;
+		const int nst = g.n_store > 0 ? g.n_store : N;
 		uint32_t i = 0;
 		for (int t = blockIdx.x; t < tiles && ok; t += G, i++) {
 			const uint32_t ab = i & 1u;
 			if (!(ok = mbar_wait(acc_full + ab, (i >> 1) & 1u))) break;
 			fence_after();
-			const int m = t * BM + 32 * q + lane;
+			const int row0 = t * BM + 32 * q;  // this warp's first row
 			const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + ab * acc_stride;
 			for (int c0 = 0; c0 < N; c0 += 32) {
 				uint32_t r[32];
-				tmem_ld32(taddr + (uint32_t)c0, r);  // (columns past N, when N % 32 != 0, are not stored)
-				if (m >= g.M) continue;
+				tmem_ld32(taddr + (uint32_t)c0, r);  // row 32q + lane, columns c0..c0+31
 				float v[32];
 #pragma unroll
 				for (int j = 0; j < 32; j++) {
@@ -483,24 +491,38 @@ __global__ void __launch_bounds__(THREADS, 1)
 					if (g.relu) x = fmaxf(x, 0.f);
 					v[j] = x;
 				}
-				if (C) {
-					float4* dst = reinterpret_cast<float4*>(C + (long long)m * g.ldc + c0);
-#pragma unroll
-					for (int j = 0; j < 8; j++)
-						if (c0 + 4 * j < N) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-				}
 				if (Cb) {
-					uint4* dst = reinterpret_cast<uint4*>(Cb + (long long)m * g.ldcb + c0);
+					uint4* srow = reinterpret_cast<uint4*>(stg + lane * STG_ROW);
 #pragma unroll
-					for (int j = 0; j < 4; j++)
-						if (c0 + 8 * j < N) {
-							__nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * j], v[8 * j + 1]);
-							__nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * j + 2], v[8 * j + 3]);
-							__nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * j + 4], v[8 * j + 5]);
-							__nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * j + 6], v[8 * j + 7]);
-							dst[j] = make_uint4(*reinterpret_cast<uint32_t*>(&h0), *reinterpret_cast<uint32_t*>(&h1),
-							                    *reinterpret_cast<uint32_t*>(&h2), *reinterpret_cast<uint32_t*>(&h3));
+					for (int j = 0; j < 4; j++) {
+						__nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * j], v[8 * j + 1]);
+						__nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * j + 2], v[8 * j + 3]);
+						__nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * j + 4], v[8 * j + 5]);
+						__nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * j + 6], v[8 * j + 7]);
+						srow[j] = make_uint4(*reinterpret_cast<uint32_t*>(&h0), *reinterpret_cast<uint32_t*>(&h1),
+						                     *reinterpret_cast<uint32_t*>(&h2), *reinterpret_cast<uint32_t*>(&h3));
+					}
+					__syncwarp();
+#pragma unroll
+					for (int k = 0; k < 4; k++) {
+						const int e = lane + 32 * k, rr = e >> 2, ch = e & 3, m = row0 + rr;
+						if (m < g.M && c0 + 8 * ch < N)
+							*reinterpret_cast<uint4*>(Cb + (long long)m * g.ldcb + c0 + 8 * ch) =
+							    *reinterpret_cast<const uint4*>(stg + rr * STG_ROW + 16 * ch);
+					}
+					__syncwarp();
+				}
+				if (C) {
+					float4* srow = reinterpret_cast<float4*>(stg + lane * STG_ROW);
+#pragma unroll
+					for (int j = 0; j < 8; j++) srow[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+					__syncwarp();
+					if (c0 + lane < nst)
+						for (int rr = 0; rr < 32; rr++) {
+							const int m = row0 + rr;
+							if (m < g.M) C[(long long)m * g.ldc + c0 + lane] = reinterpret_cast<const float*>(stg + rr * STG_ROW)[lane];
 						}
+					__syncwarp();
 				}
 			}
 			fence_before();
@@ -756,7 +778,7 @@ constexpr size_t TC_SMEM_MAX = 227 * 1024;
 bool tc_eligible(const mf_mlp* m, bool ta, bool tb, const GemmArgs& g) {
 	return m->tc && !ta && tb && g.K % tc::BK == 0 && g.N % 16 == 0 && g.N <= 256 && g.lda == g.K && g.ldb == g.K &&
 	       g.sA == (long long)m->rows * g.K && g.M <= m->rows && tc::smem_bytes(g.N, g.K) <= TC_SMEM_MAX &&
-	       (!g.Cb || g.ldcb % 8 == 0) && (!g.C || g.ldc % 4 == 0) && g.sB % 8 == 0;
+	       (!g.Cb || g.ldcb % 8 == 0) && g.sB % 8 == 0;
 }
 
 cudaError_t gemm_tc(mf_mlp* m, const GemmArgs& g) {
@@ -804,7 +826,10 @@ cudaError_t gemm(mf_mlp* m, bool ta, bool tb, GemmArgs g) {
 long long sH(const mf_mlp* m, int l) { return (long long)m->rows * m->pd[l]; }
 
 // forward pass of all members over `batch` rows already in H[0]
-cudaError_t forward_layers(mf_mlp* m, int batch) {
+// direct_out: when the last layer runs on tcgen05, write its unpadded outputs straight
+// into Yin ([members][rows][out], FP32) and set *wrote_direct (no unpadding pass then)
+cudaError_t forward_layers(mf_mlp* m, int batch, bool direct_out = false, bool* wrote_direct = nullptr) {
+	if (wrote_direct) *wrote_direct = false;
 	for (int l = 0; l < m->L; l++) {
 		GemmArgs g{};
 		g.M = batch; g.N = m->pd[l + 1]; g.K = m->pd[l];
@@ -816,6 +841,11 @@ cudaError_t forward_layers(mf_mlp* m, int batch) {
 			g.relu = 1;
 		} else {
 			g.C = m->Yp.p; g.ldc = m->pd[l + 1]; g.sC = sH(m, l + 1);
+			if (direct_out && tc_eligible(m, false, true, g)) {
+				g.C = m->Yin.p; g.ldc = m->dims[m->L]; g.sC = (long long)m->rows * m->dims[m->L];
+				g.n_store = m->dims[m->L];
+				if (wrote_direct) *wrote_direct = true;
+			}
 		}
 		cudaError_t e = gemm(m, false, true, g);
 		if (e != cudaSuccess) return e;
@@ -1166,13 +1196,17 @@ MF_API mf_status mf_mlp_predict(mf_mlp* m, const float* x, int32_t n, float* y) 
 		k_input<<<nblk(per * m->members, 256), 256, 0, s>>>(m->members, b, in, m->pd[0], m->Xin.p, 0, m->H[0].p, sH(m, 0));
 		m->launches++;
 		MCK(cudaGetLastError());
-		MCK(forward_layers(m, b));
-		// unpadded outputs into Yin ([members][rows][out]), then one 2D copy per chunk
-		const long long po = (long long)b * out;
-		k_output<<<nblk(po * m->members, 256), 256, 0, s>>>(m->members, b, out, m->pd[m->L], m->Yp.p, sH(m, m->L),
-		                                                   m->Yin.p, (long long)m->rows * out);
-		m->launches++;
-		MCK(cudaGetLastError());
+		bool direct = false;
+		MCK(forward_layers(m, b, true, &direct));
+		// unpadded outputs into Yin ([members][rows][out]) -- written there by the last
+		// layer itself on the tcgen05 path -- then one 2D copy per chunk
+		if (!direct) {
+			const long long po = (long long)b * out;
+			k_output<<<nblk(po * m->members, 256), 256, 0, s>>>(m->members, b, out, m->pd[m->L], m->Yp.p, sH(m, m->L),
+			                                                   m->Yin.p, (long long)m->rows * out);
+			m->launches++;
+			MCK(cudaGetLastError());
+		}
 		MCK(cudaMemcpy2DAsync(y + (size_t)r0 * out, (size_t)n * out * 4, m->Yin.p, (size_t)m->rows * out * 4,
 		                      (size_t)b * out * 4, m->members, cudaMemcpyDefault, s));
 	}

@@ -113,5 +113,99 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 }
 
 
+// The same shape functions for the mixed weak updated-Lagrangian form: the 27 moment
+// sums per neighbour in FP32, the three 3x3 solves (Cramer) in FP64, the shape
+// functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
+// with the gradient scaled by h (d/ds = h d/dx), so that every moment entry is of
+// order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
+// M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
+// Corr = C'0 + s.C'(1,2), h Corr_x = s.C'_x(1,2) + C'1 + C'_x0 -- the reference's
+// expressions (precomp_shape_functions.h:52-173) in scaled units.  Offsets are FP64
+// differences rounded once; volumes m_j / rho_j in FP32.
+template <class Rho, class Use, class Out>
+__device__ __forceinline__ bool rkpm_row32(double xi, double yi, double hi, uint32_t q0, uint32_t q1,
+                                           const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
+                                           const double* __restrict__ fy, const double* __restrict__ fm, Rho rho,
+                                           Use use, Out out) {
+	const float h = (float)hi, ih = 1.f / h;
+	const float fac = (float)(10 * (mfk::K_1_PI) / 7.0) * ih * ih;
+	float M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
+	      My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row], scaled; upper triangle
+	for (uint32_t q = q0; q < q1; q++) {
+		if (!use(q)) continue;
+		const uint32_t j = nbr[q];
+		const float vj = (float)fm[j] / (float)rho(j);
+		const float rx = (float)(xi - fx[j]), ry = (float)(yi - fy[j]);
+		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
+		const float sx = rx * ih, sy = ry * ih, gx = w.w_x * h, gy = w.w_y * h;
+		const float W = w.w * vj, Gx = gx * vj, Gy = gy * vj;
+		M[0][0] += W;            M[0][1] += W * sx;       M[0][2] += W * sy;
+		M[1][1] += sx * sx * W;  M[1][2] += sx * sy * W;  M[2][2] += sy * sy * W;
+		Mx[0][0] += Gx;
+		Mx[0][1] += Gx * sx + W;
+		Mx[0][2] += Gx * sy;
+		Mx[1][1] += sx * sx * Gx + 2.f * sx * W;
+		Mx[1][2] += sx * sy * Gx + sy * W;
+		Mx[2][2] += sy * sy * Gx;
+		My[0][0] += Gy;
+		My[0][1] += Gy * sx;
+		My[0][2] += Gy * sy + W;
+		My[1][1] += sx * sx * Gy;
+		My[1][2] += sx * sy * Gy + sx * W;
+		My[2][2] += sy * sy * Gy + 2.f * sy * W;
+	}
+	// the matrices are symmetric (M[a][b] = M[b][a]); the solves in FP64
+	double A[3][3], Ax[3][3], Ay[3][3];
+#pragma unroll
+	for (int a_ = 0; a_ < 3; a_++)
+#pragma unroll
+		for (int b_ = a_; b_ < 3; b_++) {
+			A[a_][b_] = A[b_][a_] = (double)M[a_][b_];
+			Ax[a_][b_] = Ax[b_][a_] = (double)Mx[a_][b_];
+			Ay[a_][b_] = Ay[b_][a_] = (double)My[a_][b_];
+		}
+	bool ok = true;
+	auto solve = [&](const double r[3], double x[3]) {
+		double delta = A[0][0] * A[1][1] * A[2][2] + A[1][0] * A[2][1] * A[0][2] + A[2][0] * A[0][1] * A[1][2] -
+		               A[0][2] * A[1][1] * A[2][0] - A[1][2] * A[2][1] * A[0][0] - A[2][2] * A[0][1] * A[1][0];
+		double delta_x = r[0] * A[1][1] * A[2][2] + A[1][0] * A[2][1] * r[2] + A[2][0] * r[1] * A[1][2] -
+		                 r[2] * A[1][1] * A[2][0] - A[1][2] * A[2][1] * r[0] - A[2][2] * r[1] * A[1][0];
+		double delta_y = A[0][0] * r[1] * A[2][2] + r[0] * A[2][1] * A[0][2] + A[2][0] * A[0][1] * r[2] -
+		                 A[0][2] * r[1] * A[2][0] - r[2] * A[2][1] * A[0][0] - A[2][2] * A[0][1] * r[0];
+		double delta_z = A[0][0] * A[1][1] * r[2] + A[1][0] * r[1] * A[0][2] + r[0] * A[0][1] * A[1][2] -
+		                 A[0][2] * A[1][1] * r[0] - A[1][2] * r[1] * A[0][0] - r[2] * A[0][1] * A[1][0];
+		if (!(fabs(delta) > 0.)) ok = false;
+		const double id = 1. / delta;
+		x[0] = delta_x * id;
+		x[1] = delta_y * id;
+		x[2] = delta_z * id;
+	};
+	double P[3] = {1., 0., 0.}, C[3], Cx[3], Cy[3];
+	solve(P, C);
+	double rx_[3], ry_[3];
+#pragma unroll
+	for (int r = 0; r < 3; r++) {
+		rx_[r] = -(Ax[0][r] * C[0] + Ax[1][r] * C[1] + Ax[2][r] * C[2]);
+		ry_[r] = -(Ay[0][r] * C[0] + Ay[1][r] * C[1] + Ay[2][r] * C[2]);
+	}
+	solve(rx_, Cx);
+	solve(ry_, Cy);
+	const float c0 = (float)C[0], c1 = (float)C[1], c2 = (float)C[2];
+	const float cx0 = (float)Cx[0], cx1 = (float)Cx[1], cx2 = (float)Cx[2];
+	const float cy0 = (float)Cy[0], cy1 = (float)Cy[1], cy2 = (float)Cy[2];
+	for (uint32_t q = q0; q < q1; q++) {
+		if (!use(q)) continue;
+		const uint32_t j = nbr[q];
+		const float rx = (float)(xi - fx[j]), ry = (float)(yi - fy[j]);
+		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
+		const float sx = rx * ih, sy = ry * ih;
+		const float Corr = (sx * c1 + sy * c2) + c0;
+		const float Corr_x = (sx * cx1 + sy * cx2) + c1 + cx0;  // h Corr_x
+		const float Corr_y = (sx * cy1 + sy * cy2) + c2 + cy0;  // h Corr_y
+		out(q, Corr * w.w, Corr_x * ih * w.w + Corr * w.w_x, Corr_y * ih * w.w + Corr * w.w_y);
+	}
+	return ok;
+}
+
 }  // namespace
 }  // namespace MF_NS

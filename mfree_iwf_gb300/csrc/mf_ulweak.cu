@@ -51,6 +51,7 @@ enum : uint32_t {
 // the candidates inside the ellipse.  With qw_dst the row also stores its integration
 // weight for the passes: m / rho (riemann_update_integration_weights) when qw_src is
 // null, else qw_src (the weights of the last update).
+template <bool MIXED>
 __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
                          const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
@@ -121,7 +122,11 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 	auto rho = [&](uint32_t j) { return frho[j]; };
 	auto use = [&](uint32_t q) { return mask[q] != 0; };
 	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
-	if (!rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)) raise(st, ERR_SINGULAR, i);
+	// the mixed form: the moment sums and the shape functions in FP32 (the ellipse above,
+	// and with it the neighbour sets, stay FP64)
+	const bool ok = MIXED ? rkpm_row32(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)
+	                      : rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out);
+	if (!ok) raise(st, ERR_SINGULAR, i);
 }
 
 // the particles' integration weight of this evaluation (riemann_update_integration_weights),
@@ -273,10 +278,14 @@ __global__ void k_uw_smooth_copy(UWArgs a) {
 cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
                    const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,
                    uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,
-                   void* status, cudaStream_t s) {
+                   void* status, int mixed, cudaStream_t s) {
 	if (n_to == 0) return cudaSuccess;
-	k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx, wy,
-	                                          qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
+	if (mixed)
+		k_uw_nbh<true><<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx,
+		                                                wy, qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
+	else
+		k_uw_nbh<false><<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx,
+		                                                 wy, qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
 	return cudaGetLastError();
 }
 

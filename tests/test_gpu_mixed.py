@@ -5,11 +5,12 @@ Fields, each a relative L2 norm over all particles of all bodies:
   * displacement  x - X0, y - Y0 (|x| ~ 0.1 m would hide errors in the motion itself);
   * velocity      vx, vy;
   * density       the density change where the method evolves a density: rho - rho0 of
-                  the particles (UL) or of the Gauss points (weak TL); the strong-form TL
-                  method keeps rho constant, as the reference does (None);
+                  the particles (UL) or of the Gauss / stress points (weak TL / UL); the
+                  strong-form TL method keeps rho constant, as the reference does (None);
   * stress        the stress the method evaluates: the state's S (UL), the nominal
                   stress P = J F^-1 sigma on the final state (strong-form TL, its
-                  F^-1 taken in FP32 by the mixed form), the Gauss points' S (weak TL).
+                  F^-1 taken in FP32 by the mixed form), the Gauss / stress points' S
+                  (weak TL / UL).
 Density and stress norms are floored at those of a uniform 1e-6 strain (1e-6 rho0,
 1e-6 E), so that a field still at round-off level (rings in free flight) is not
 compared by its own noise.
@@ -31,11 +32,12 @@ def run(sc, steps, precision):
     import mfree_iwf_gb300 as M
     sim = M.from_scenario(sc, precision=precision)
     extra = {}
-    if sc.method == M.METHOD_TL_WEAK:
+    weak = sc.method in (M.METHOD_TL_WEAK, M.METHOD_UL_WEAK)
+    if weak:
         extra["gauss0"] = sim.get_gauss_state()
     sim.step(steps)
     out = [sim.get_state(b) for b in range(len(sc.bodies))]
-    if sc.method == M.METHOD_TL_WEAK:
+    if weak:
         extra["gauss"] = sim.get_gauss_state()
     elif sc.method in (M.METHOD_TL, M.METHOD_UL):
         extra["stress"] = [sim.get_stress(b) for b in range(len(sc.bodies))]
@@ -65,7 +67,7 @@ def errors(sc, a, b):
     res = {"displacement": rel([(p[f] - x0[f], q[f] - x0[f]) for p, q, x0 in zip(sa, sb, X0) for f in ("x", "y")]),
            "velocity": rel([(p[f], q[f]) for p, q in zip(sa, sb) for f in ("vx", "vy")])}
     E, rho0 = sc.E, sc.rho0
-    if sc.method == M.METHOD_TL_WEAK:
+    if sc.method in (M.METHOD_TL_WEAK, M.METHOD_UL_WEAK):
         g0 = eb["gauss0"]["rho"]
         ng = len(g0)
         res["density"] = rel([(ea["gauss"]["rho"] - g0, eb["gauss"]["rho"] - g0)], STRAIN_FLOOR * rho0 * ng ** 0.5)
@@ -104,6 +106,12 @@ def scenario(case):
         return S.rings_tl_fem_contact(81)
     if case == "weak_rkpm_disc":
         return S.rotation_tl_weak(61)
+    if case == "ul_weak_rings_contact":
+        return S.rings_ul_weak_contact(41)
+    if case == "ul_weak_plate":
+        return S.tensile_ul_weak(41)
+    if case == "ul_weak_disc":
+        return S.rotation_ul_weak(41)
     raise KeyError(case)
 
 
@@ -119,6 +127,9 @@ def scenario(case):
 #    1000 steps at dx = 0.2 mm.
 #  * the weak form on explicit element maps: the meshed rings with the elements' own
 #    functions through contact, the meshed disc with RKPM.
+#  * the weak UL form (ellipse neighbourhoods and RKPM every stage; the mixed form sums
+#    the moments in FP32): the reference's rings through contact, plate and spinning
+#    disc at nbox = 41.
 V = 1e-4  # the velocity and displacement target
 CASES = [
     ("c1_ul_rings_dx1mm", 1000, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
@@ -130,6 +141,9 @@ CASES = [
     ("c3_weak_plate_dx0.2mm", 1000, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
     ("weak_fem_rings_contact", 600, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
     ("weak_rkpm_disc", 400, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
+    ("ul_weak_rings_contact", 600, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
+    ("ul_weak_plate", 400, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
+    ("ul_weak_disc", 400, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
 ]
 
 
