@@ -606,8 +606,9 @@ if __name__ == "__main__":
     ap.add_argument("--out", default=None, help="write the JSON result here too")
     ap.add_argument("--gemm-bench", action="store_true", help="only time the ensemble's inference GEMMs")
     ap.add_argument("--tcgen05", type=int, choices=[0, 1], default=None, help="with --gemm-bench: the GEMM path")
+    ap.add_argument("--chunks", type=int, default=16, help="with --gemm-bench: passes of 65,535 rows")
     a = ap.parse_args()
-    r = (gemm_benchmark(tcgen05=a.tcgen05) if a.gemm_bench
+    r = (gemm_benchmark(chunks=a.chunks, tcgen05=a.tcgen05) if a.gemm_bench
          else run_experiment(a.train, a.test, train_steps=a.steps, data=a.data))
     s = json.dumps(r, indent=1)
     print(s)
