@@ -162,7 +162,8 @@ struct TLArgs {
 	const uint16_t* r_cnt;
 	const uint32_t* runs;
 	const void *XF, *G;
-	uint32_t unroll;                     // run walk: pairs per loop iteration (1 or 2; same results)
+	uint32_t unroll;                     // run walk: 1 or 2 pairs per loop iteration; 3: one pair, pass B
+	                                     // with 64 registers (all give the same results)
 	const uint32_t* bc_rows;
 	const double* bc_v;
 	uint32_t n_bc;

@@ -277,26 +277,29 @@ __global__ void __launch_bounds__(256) k_gemm_nt(GemmArgs g) {
 // accumulators in tensor memory (TMEM), operands staged by TMA.  Z = H W^T for K a
 // multiple of 64 and N <= 256 (the 256-wide layers and the output layer).
 //
-// One persistent CTA per (slice of the row tiles, member); 6 warps with fixed roles:
+// One persistent CTA per (slice of the row tiles, member); 10 warps with fixed roles:
 //   warp 0     one thread issues the TMA copies: the member's whole W once (N x K,
 //              K-major, 128-byte swizzled, resident for all of the CTA's tiles), then
-//              128-row x 64-column slices of H through a 4-stage ring;
+//              128-row x 64-column slices of H through a 3-stage ring;
 //   warp 1     allocates TMEM (two accumulators of N columns, so that a tile's
 //              epilogue overlaps the next tile's products); one thread issues
 //              tcgen05.mma (M = 128, N, K = 16, BF16 x BF16 -> FP32) and tcgen05.commit,
 //              which releases each H stage and, after a tile's last slice, hands the
 //              accumulator to the epilogue;
-//   warps 2-5  the epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31 -- one tile row
-//              per thread -- 32 columns at a time (tcgen05.ld), adds the bias, applies
-//              ReLU and stores FP32 and/or BF16 rows.
+//   warps 2-9  the epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31 -- one tile row
+//              per thread -- 32 columns at a time (tcgen05.ld; warps 2-5 the even
+//              32-column chunks, warps 6-9 the odd ones), adds the bias, applies ReLU
+//              and stores FP32 and/or BF16 rows.  Two warps per scheduler in the
+//              epilogue hide each other's TMEM-load and store latencies.
 // Every mbarrier wait is bounded: past the limit the thread sets the error word and
 // leaves its loop; all threads meet at the end, where warp 1 frees the TMEM.
 namespace tc {
 
 constexpr int BM = 128;      // tile rows: one TMEM lane each
 constexpr int BK = 64;       // K per stage: 64 BF16 = 128 bytes, one 128-byte swizzle span
-constexpr int STAGES = 4;
-constexpr int THREADS = 192;
+constexpr int STAGES = 3;
+constexpr int EPI = 8;  // epilogue warps: two per TMEM lane quarter, splitting the columns
+constexpr int THREADS = 64 + 32 * EPI;
 constexpr uint32_t SPIN_LIMIT = 1u << 24;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -378,7 +381,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 // alignment that the 128-byte swizzle needs
 constexpr int STG_ROW = 144;  // epilogue staging row: 32 FP32 (or 32 BF16) + 16 bytes of padding
 __host__ __device__ constexpr size_t smem_bytes(int N, int K) {
-	return 1024 + (size_t)(K / BK) * N * 128 + (size_t)STAGES * BM * 128 + 4 * 32 * STG_ROW + 8 * (1 + 2 * STAGES + 4) + 16;
+	return 1024 + (size_t)(K / BK) * N * 128 + (size_t)STAGES * BM * 128 + EPI * 32 * STG_ROW + 8 * (1 + 2 * STAGES + 4) + 16;
 }
 __host__ __device__ constexpr uint32_t tmem_cols(int N) { return N <= 128 ? 256u : 512u; }
 
@@ -390,8 +393,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 	const uint32_t raw = saddr(smem_raw);
 	uint8_t* sW = smem_raw + (((raw + 1023u) & ~1023u) - raw);
 	uint8_t* sA = sW + (size_t)KB * N * 128;
-	uint8_t* sStg = sA + (size_t)STAGES * BM * 128;  // 4 epilogue warps x 32 rows x STG_ROW
-	uint64_t* w_full = reinterpret_cast<uint64_t*>(sStg + 4 * 32 * STG_ROW);
+	uint8_t* sStg = sA + (size_t)STAGES * BM * 128;  // EPI epilogue warps x 32 rows x STG_ROW
+	uint64_t* w_full = reinterpret_cast<uint64_t*>(sStg + EPI * 32 * STG_ROW);
 	uint64_t* a_full = w_full + 1;
 	uint64_t* a_empty = a_full + STAGES;
 	uint64_t* acc_full = a_empty + STAGES;
@@ -409,7 +412,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 		}
 		for (int b = 0; b < 2; b++) {
 			mbar_init(acc_full + b, 1);
-			mbar_init(acc_empty + b, 4);  // one arrival per epilogue warp
+			mbar_init(acc_empty + b, EPI);  // one arrival per epilogue warp
 		}
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 	}
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 		// 144 bytes: the 16-byte accesses of 8 lanes hit distinct banks) and writes
 		// them out coalesced -- BF16: 16-byte chunks, 8 rows of 64 bytes per
 		// instruction; FP32: one row of up to 128 bytes per instruction, any ldc
-		const int q = warp & 3;
+		const int q = warp & 3, grp = (warp - 2) >> 2;  // lane quarter; column group (chunks grp, grp + 2, ...)
 		uint8_t* stg = sStg + (size_t)(warp - 2) * 32 * STG_ROW;
 		const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
 		float* C = g.C ? g.C + z * g.sC : nullptr;
@@ -480,7 +483,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 			fence_after();
 			const int row0 = t * BM + 32 * q;  // this warp's first row
 			const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + ab * acc_stride;
-			for (int c0 = 0; c0 < N; c0 += 32) {
+			for (int c0 = 32 * grp; c0 < N; c0 += 64) {
 				uint32_t r[32];
 				tmem_ld32(taddr + (uint32_t)c0, r);  // row 32q + lane, columns c0..c0+31
 				float v[32];

@@ -747,8 +747,10 @@ __device__ __forceinline__ void tlB_add(uint32_t flags, const PairB& p, const Re
 	}
 }
 
-template <int U>
-__global__ void __launch_bounds__(256, U == 1 ? 3 : 2) k_tlB32r(TLArgs a) {
+// MB: blocks of 256 per SM the register budget is cut for (3: 72 registers; 4: 64,
+// with a few bytes of spills) -- the same arithmetic, so the same results.
+template <int U, int MB>
+__global__ void __launch_bounds__(256, MB) k_tlB32r(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const uint32_t flags = a.flags;
@@ -1037,8 +1039,9 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	case 3: {
 		unsigned bs = a.block ? a.block : 128;
 		if (mixed && a.t_rows) k_tlB32t<<<a.n_tiles, TL_TILE, tl_tile_smem(1, a.halo_max, a.t_ent_max), s>>>(a);
-		else if (mixed && a.runs && a.unroll == 2) k_tlB32r<2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
-		else if (mixed && a.runs) k_tlB32r<1><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs && a.unroll == 2) k_tlB32r<2, 2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs && a.unroll == 3) k_tlB32r<1, 4><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs) k_tlB32r<1, 3><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlB64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
