@@ -198,7 +198,8 @@ struct Tune {
 	uint32_t ul_split = 1;  // mixed UL, plain grid: threads per row of the pair pass
 	uint32_t tl_tiled = 0;  // mixed TL: the halo-tile passes (built at set-up when requested)
 	uint32_t tl_runs = 1;   // mixed TL: the run-walk passes (gradients recomputed on chip)
-	uint32_t tl_unroll = 1; // run walk: 1 or 2 pairs per iteration, 3: pass B at 64 registers (same results)
+	uint32_t tl_unroll = 1; // run walk: 1 or 2 pairs per iteration, 3: pass B at 64 registers, 4: and pass A at
+	                        // 48 (same results)
 };
 std::mutex g_tune_mutex;
 std::map<std::string, Tune> g_tune_cache;
@@ -3097,7 +3098,7 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 			t.tl_tiled = 0;
 			// (tl_runs stays as set: it changes results in the last FP32 bits; the
 			// unroll factor of the run walk does not)
-			for (uint32_t u : {1u, 2u, 3u}) {
+			for (uint32_t u : {1u, 2u, 3u, 4u}) {
 				t.tl_unroll = u;
 				if (u == 1 || (c->cfg.method == MF_METHOD_TL && c->mixed && c->rw_ok && t.tl_runs)) cands.push_back(t);
 			}

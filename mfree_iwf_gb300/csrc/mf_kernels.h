@@ -163,7 +163,7 @@ struct TLArgs {
 	const uint32_t* runs;
 	const void *XF, *G;
 	uint32_t unroll;                     // run walk: 1 or 2 pairs per loop iteration; 3: one pair, pass B
-	                                     // with 64 registers (all give the same results)
+	                                     // with 64 registers; 4: also pass A with 48 (all: the same results)
 	const uint32_t* bc_rows;
 	const double* bc_v;
 	uint32_t n_bc;

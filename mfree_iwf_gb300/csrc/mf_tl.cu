@@ -673,8 +673,10 @@ __device__ __forceinline__ void tlA_add(uint32_t flags, const PairA& p, float4 X
 // U pairs per iteration: the gathers of both pairs are issued before either pair's
 // arithmetic, and the pairs are added in list order, so U = 1 and U = 2 give the same
 // bits; U = 2 keeps twice the loads in flight at the cost of registers.
-template <int U>
-__global__ void __launch_bounds__(256, U == 1 ? 4 : 3) k_tlA32r(TLArgs a) {
+// MB: blocks of 256 per SM the register budget is cut for (4: 64 registers; 5: 48,
+// with spills) -- the same arithmetic, so the same results.
+template <int U, int MB>
+__global__ void __launch_bounds__(256, MB) k_tlA32r(TLArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_total) return;
 	const uint32_t flags = a.flags;
@@ -1030,8 +1032,9 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	case 2: {
 		unsigned bs = a.block ? a.block : 128;
 		if (mixed && a.t_rows) k_tlA32t<<<a.n_tiles, TL_TILE, tl_tile_smem(0, a.halo_max, a.t_ent_max), s>>>(a);
-		else if (mixed && a.runs && a.unroll == 2) k_tlA32r<2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
-		else if (mixed && a.runs) k_tlA32r<1><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs && a.unroll == 2) k_tlA32r<2, 3><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs && a.unroll == 4) k_tlA32r<1, 5><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs) k_tlA32r<1, 4><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed) k_tlA32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlA64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		break;
@@ -1040,7 +1043,7 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 		unsigned bs = a.block ? a.block : 128;
 		if (mixed && a.t_rows) k_tlB32t<<<a.n_tiles, TL_TILE, tl_tile_smem(1, a.halo_max, a.t_ent_max), s>>>(a);
 		else if (mixed && a.runs && a.unroll == 2) k_tlB32r<2, 2><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
-		else if (mixed && a.runs && a.unroll == 3) k_tlB32r<1, 4><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
+		else if (mixed && a.runs && (a.unroll == 3 || a.unroll == 4)) k_tlB32r<1, 4><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed && a.runs) k_tlB32r<1, 3><<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else if (mixed) k_tlB32<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
 		else k_tlB64<<<grid1(a.n_total, bs), bs, 0, s>>>(a);
