@@ -542,6 +542,337 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 }  // namespace tc
 
+// Fused inference: the whole forward pass of every member in one persistent kernel,
+// the hidden activations never leaving the SM.  A CTA takes tiles of 256 rows of one
+// member (two halves of 128 rows, one TMEM accumulator of up to 256 FP32 columns each)
+// and runs them through all layers:
+//   - the epilogue warps write the tile's input rows (FP32 -> BF16, zero padded to the
+//     first layer's K) into shared memory in the 128-byte-swizzled K-major layout that
+//     a TMA load would produce, so the tensor core reads them as the A operand;
+//   - the producer (warp 0) streams each layer's BF16 weights, 64-wide K chunks of all
+//     N rows, through a ring of shared-memory stages with TMA;
+//   - the MMA issuer (warp 1) multiplies, per K chunk, both halves into their
+//     accumulators and commits each half's accumulator after its last chunk;
+//   - the epilogue warps (8: four TMEM lane quarters x two halves) read their half's
+//     accumulator, add the bias, apply ReLU, round to BF16 and write the next layer's A
+//     operand over the current one (whose products are complete by then); after the last
+//     layer they add the bias and store the FP32 outputs, 32 rows x 32 columns at a
+//     time staged through their own rows of shared memory so that each store
+//     instruction writes one contiguous row segment.
+// Only the inputs (in FP32), the weights (from L2: every CTA on a member reads the same
+// ones) and the outputs move through memory.  The products are the per-layer path's --
+// BF16 operands, FP32 accumulation in K order, the bias added in FP32 -- with K padded
+// to 64 by zeros.  Every wait is bounded; on a timeout the kernel sets the error word,
+// waits (bounded) for its own copies and products in flight, frees the TMEM and returns.
+namespace fz {
+
+constexpr int TILE = 256, HALF = 128;
+constexpr int CHUNK = HALF * 128;  // one 64-wide K chunk of a half: 128 rows x 128 bytes
+constexpr int EPI = 8;
+constexpr int THREADS = 64 + 32 * EPI;
+constexpr uint32_t TMEM_COLS = 512;  // two accumulators of up to 256 columns
+
+struct Maps {
+	CUtensorMap w[MF_MLP_MAX_LAYERS];  // per layer: [members][N][K] BF16, boxes of 64 K x N rows
+};
+struct Args {
+	int L, in, out, rows, stages, kc_max, n_max;
+	int N[MF_MLP_MAX_LAYERS], KC[MF_MLP_MAX_LAYERS];  // MMA width (padded to 16); K / 64 (K padded to 64)
+	int b_off[MF_MLP_MAX_LAYERS];
+	const float* bias;
+	long long b_per;
+	const float* x;  // x[z * sx + r * in + c] (sx = 0: one input shared by the members)
+	long long sx;
+	float* y;  // y[z * sy + r * ldy + c]
+	long long sy;
+	int ldy;
+	int members;
+};
+
+// the mbarriers (2 per weight stage, 2 x 2 per half, 1 to drain) and the TMEM address,
+// rounded up to 16 bytes
+__host__ __device__ constexpr size_t bar_bytes(int stages) { return (8 * (2 * stages + 5) + 4 + 15) / 16 * 16; }
+// shared memory: 1 KB for the 1 KB alignment of the swizzled operands, the two halves'
+// A operands, the weight stages, the barriers and one layer's bias
+__host__ __device__ constexpr size_t smem_bytes(int kc_max, int n_max, int stages) {
+	return 1024 + (size_t)2 * kc_max * CHUNK + (size_t)stages * n_max * 128 + bar_bytes(stages) + (size_t)n_max * 4;
+}
+
+// one 16-byte unit (8 BF16 columns starting at col, a multiple of 8) of row r of a
+// half, at its place in the 128-byte swizzle: chunk col / 64, unit (col % 64) / 8
+// XOR (r % 8)
+__device__ __forceinline__ void put_unit(uint8_t* half, int r, int col, uint4 v) {
+	const int kc = col >> 6, u = (col >> 3) & 7;
+	*reinterpret_cast<uint4*>(half + (size_t)kc * CHUNK + r * 128 + ((u ^ (r & 7)) << 4)) = v;
+}
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+	__nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+	return *reinterpret_cast<uint32_t*>(&h);
+}
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// max(a, 0) and max(b, 0) rounded to BF16, a in the low half
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
+	uint32_t d;
+	asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(d) : "f"(b), "f"(a));
+	return d;
+}
+// 32 columns of the warp's 32 TMEM lanes without waiting (tmem_wait before use)
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t* r) {
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+	             : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+// named barrier 1 over the 256 epilogue threads; epi_all also returns the AND of p over them
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+__device__ __forceinline__ bool epi_all(bool p) {
+	uint32_t r;
+	asm volatile("{\n.reg .pred q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred q, 1, 256, q;\nselp.u32 %0, 1, 0, q;\n}\n"
+	             : "=r"(r)
+	             : "r"((uint32_t)p)
+	             : "memory");
+	return r != 0;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_mlp_fused(const __grid_constant__ Maps maps, const Args a, uint32_t* err) {
+	using namespace tc;
+	extern __shared__ uint8_t smem_raw[];
+	const uint32_t raw = saddr(smem_raw);
+	uint8_t* act = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+	const size_t half_bytes = (size_t)a.kc_max * CHUNK, wst = (size_t)a.n_max * 128;
+	const int S = a.stages;
+	uint8_t* sW = act + 2 * half_bytes;
+	uint64_t* w_full = reinterpret_cast<uint64_t*>(sW + (size_t)S * wst);
+	uint64_t* w_empty = w_full + S;
+	uint64_t* acc_full = w_empty + S;    // per half: the layer's products are complete
+	uint64_t* act_ready = acc_full + 2;  // per half: the A operand of the next layer is written
+	uint64_t* fin = act_ready + 2;
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+	float* sbias = reinterpret_cast<float*>(sW + (size_t)S * wst + bar_bytes(S));  // the current layer's bias
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int tpm = (a.rows + TILE - 1) / TILE, total = tpm * a.members;
+
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < S; s++) {
+			mbar_init(w_full + s, 1);
+			mbar_init(w_empty + s, 1);
+		}
+		for (int h = 0; h < 2; h++) {
+			mbar_init(acc_full + h, 1);
+			mbar_init(act_ready + h, 32 * EPI / 2);  // every thread of the half's four warps
+		}
+		mbar_init(fin, 1);
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+	}
+	if (warp == 1) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tmem_slot)),
+		             "r"(TMEM_COLS)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+	}
+	fence_before();
+	__syncthreads();
+	fence_after();
+	const uint32_t tmem = *tmem_slot;
+	bool ok = true;
+
+	if (warp == 0) {
+		if (lane == 0) {  // weight producer
+			uint32_t it = 0;
+			for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+				const int z = t % a.members;
+				for (int l = 0; l < a.L && ok; l++)
+					for (int kc = 0; kc < a.KC[l]; kc++, it++) {
+						const int s = (int)(it % S);
+						const uint32_t use = it / S;
+						if (use > 0 && !(ok = mbar_wait(w_empty + s, (use - 1) & 1u))) break;
+						mbar_expect_tx(w_full + s, (uint32_t)a.N[l] * 128u);
+						tma_load_3d(sW + (size_t)s * wst, &maps.w[l], kc * 64, 0, z, w_full + s);
+					}
+			}
+			// the loads still in flight land before the CTA leaves (consumed ones: at once)
+			for (uint32_t k = it > (uint32_t)S ? it - S : 0; k < it; k++) mbar_wait(w_full + k % S, (k / S) & 1u);
+		}
+	} else if (warp == 1) {
+		if (lane == 0) {  // MMA issuer
+			uint32_t it = 0, step = 0;
+			bool issued = false;
+			for (int t = blockIdx.x; t < total && ok; t += gridDim.x)
+				for (int l = 0; l < a.L && ok; l++, step++) {
+					if (!(ok = mbar_wait(act_ready, step & 1u)) || !(ok = mbar_wait(act_ready + 1, step & 1u))) break;
+					fence_after();
+					const uint32_t idesc = idesc_bf16(HALF, a.N[l]);
+					for (int kc = 0; kc < a.KC[l]; kc++, it++) {
+						const int s = (int)(it % S);
+						if (!(ok = mbar_wait(w_full + s, (it / S) & 1u))) break;
+						fence_after();
+						const uint32_t b0 = saddr(sW + (size_t)s * wst);
+						for (int h = 0; h < 2; h++) {
+							const uint32_t a0 = saddr(act + h * half_bytes + (size_t)kc * CHUNK);
+#pragma unroll
+							for (int k = 0; k < 4; k++)  // K = 16 per instruction: 32 bytes along the swizzled row
+								mma_bf16(tmem + (uint32_t)(h * 256), sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k), idesc,
+								         (kc | k) != 0);
+							if (kc == a.KC[l] - 1) mma_commit(acc_full + h);
+						}
+						mma_commit(w_empty + s);  // the stage is free once both halves' products are done
+						issued = true;
+					}
+				}
+			if (issued) {  // nothing of this CTA's left in the tensor pipe before the TMEM is freed
+				mma_commit(fin);
+				mbar_wait(fin, 0);
+			}
+		}
+	} else {  // epilogue: half h, TMEM lane quarter q, row r of the half
+		const int h = (warp - 2) >> 2, q = warp & 3, r = 32 * q + lane, et = threadIdx.x - 64, rx = r & 7;
+		uint8_t* actH = act + h * half_bytes;
+		const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(h * 256);
+		const float4* sb4 = reinterpret_cast<const float4*>(sbias);
+		// tile tt: member tt % members (CTAs running side by side read different members'
+		// weights), rows (tt / members) * 256 + ...; the first 8 input columns of this
+		// thread's row are fetched ahead into registers
+		float xp[8];
+		auto x_fetch = [&](int tt) {
+			const int grow = (tt / a.members) * TILE + h * HALF + r;
+			const bool live = grow < a.rows;
+			const float* xr = a.x + (tt % a.members) * a.sx + (long long)(live ? grow : 0) * a.in;
+#pragma unroll
+			for (int j = 0; j < 8; j++) xp[j] = live && j < a.in ? xr[j] : 0.f;
+		};
+		auto x_write = [&](int tt) {  // the input row, BF16, zero padded to the first layer's K
+			*reinterpret_cast<uint4*>(actH + r * 128 + (rx << 4)) =
+			    make_uint4(pack2(xp[0], xp[1]), pack2(xp[2], xp[3]), pack2(xp[4], xp[5]), pack2(xp[6], xp[7]));
+			const int grow = (tt / a.members) * TILE + h * HALF + r;
+			const bool live = grow < a.rows;
+			const float* xr = a.x + (tt % a.members) * a.sx + (long long)(live ? grow : 0) * a.in;
+			for (int col = 8; col < a.KC[0] * 64; col += 8) {
+				float f[8];
+#pragma unroll
+				for (int j = 0; j < 8; j++) f[j] = live && col + j < a.in ? xr[col + j] : 0.f;
+				put_unit(actH, r, col, make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7])));
+			}
+			proxy_fence();  // generic-proxy writes, read next by the tensor core
+			mbar_arrive(act_ready + h);
+		};
+		// the bias of layer l of tile tt's member into shared memory (all 256 threads)
+		auto fill = [&](int tt, int l) {
+			const float* src = a.bias + (tt % a.members) * a.b_per + a.b_off[l];
+			for (int i = et; i < a.N[l]; i += 32 * EPI) sbias[i] = src[i];
+		};
+		int t = blockIdx.x;
+		if (t < total) {
+			x_fetch(t);
+			fill(t, 0);
+		}
+		epi_sync();
+		if (t < total) x_write(t);
+		uint32_t step = 0;
+		for (; t < total && ok; t += gridDim.x) {
+			const int z = t % a.members, row0 = (t / a.members) * TILE + h * HALF, tn = t + gridDim.x;
+			for (int l = 0; l < a.L; l++, step++) {
+				const bool last = l + 1 == a.L;
+				if (last && tn < total) x_fetch(tn);  // its latency hides under the products
+				const bool mine = mbar_wait(acc_full + h, step & 1u);
+				if (mine) {
+					fence_after();
+					const int N = a.N[l];
+					if (!last) {
+						// per 64-wide K chunk of the next layer: two TMEM loads, one wait; the
+						// row's eight 16-byte units at their swizzled places
+						const int KCn = a.KC[l + 1];
+						for (int kc = 0; kc < KCn; kc++) {
+							const int c0 = 64 * kc;
+							uint32_t v[64];
+							if (c0 < N) {
+								tmem_ld32_async(tq + (uint32_t)c0, v);
+								if (c0 + 32 < N) tmem_ld32_async(tq + (uint32_t)(c0 + 32), v + 32);
+								tmem_wait();
+							}
+							uint8_t* dst = actH + (size_t)kc * CHUNK + r * 128;
+#pragma unroll
+							for (int u = 0; u < 8; u++) {
+								const int col = c0 + 8 * u;
+								uint4 w = make_uint4(0, 0, 0, 0);
+								if (col < N) {
+									const float4 b0 = sb4[col >> 2], b1 = sb4[(col >> 2) + 1];
+									float f[8];
+#pragma unroll
+									for (int e = 0; e < 8; e++) f[e] = __uint_as_float(v[8 * u + e]);
+									w = make_uint4(pack2_relu(f[0] + b0.x, f[1] + b0.y), pack2_relu(f[2] + b0.z, f[3] + b0.w),
+									               pack2_relu(f[4] + b1.x, f[5] + b1.y), pack2_relu(f[6] + b1.z, f[7] + b1.w));
+								}
+								*reinterpret_cast<uint4*>(dst + ((u ^ rx) << 4)) = w;
+							}
+						}
+						fence_before();
+						proxy_fence();
+						mbar_arrive(act_ready + h);
+					} else {
+						// FP32 outputs: each 32 x 32 block through this warp's own 32 rows of
+						// chunk 0 (swizzled like the operands: conflict-free both ways), then
+						// one row segment per store instruction
+						uint8_t* stg = actH + 32 * q * 128;
+						float* yz = a.y + z * a.sy;
+						for (int c0 = 0; c0 < N && c0 < a.out; c0 += 32) {
+							uint32_t v[32];
+							tmem_ld32(tq + (uint32_t)c0, v);
+							__syncwarp();
+#pragma unroll
+							for (int j = 0; j < 8; j++) {
+								const float4 bj = c0 + 4 * j < N ? sb4[(c0 >> 2) + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+								const float4 o = make_float4(__uint_as_float(v[4 * j]) + bj.x, __uint_as_float(v[4 * j + 1]) + bj.y,
+								                             __uint_as_float(v[4 * j + 2]) + bj.z, __uint_as_float(v[4 * j + 3]) + bj.w);
+								*reinterpret_cast<float4*>(stg + lane * 128 + ((j ^ (lane & 7)) << 4)) = o;
+							}
+							__syncwarp();
+							const int col = c0 + lane;
+							for (int rr = 0; rr < 32; rr++) {
+								const int gr = row0 + 32 * q + rr;
+								const float val =
+								    *reinterpret_cast<const float*>(stg + rr * 128 + (((lane >> 2) ^ (rr & 7)) << 4) + (lane & 3) * 4);
+								if (gr < a.rows && col < a.out) yz[(long long)gr * a.ldy + col] = val;
+							}
+						}
+						fence_before();
+						__syncwarp();  // this warp's staging rows take the next tile's input now
+						if (tn < total) x_write(tn);
+					}
+				}
+				// every epilogue thread is done with this step's bias, and all agree on
+				// going on (a wait that gave up ends the loop for all 256 together)
+				ok = epi_all(mine);
+				if (!ok) break;
+				if (!last) fill(t, l + 1);
+				else if (tn < total) fill(tn, 0);
+				epi_sync();
+			}
+		}
+	}
+	if (!ok) atomicOr(err, 1u);
+	fence_before();
+	__syncthreads();
+	fence_after();
+	if (warp == 1)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// weights of one layer for the fused kernel: [members][N][Kp] BF16, K padded to Kp
+// (a multiple of 64) by zeros
+__global__ void k_pack_layer(int members, int N, int K, int Kp, const bf16* src, long long s_per, bf16* dst,
+                             long long d_per) {
+	const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	const long long per = (long long)N * Kp;
+	if (e >= per * members) return;
+	const int z = (int)(e / per);
+	const long long w = e % per;
+	const int o = (int)(w / Kp), i = (int)(w % Kp);
+	dst[z * d_per + w] = i < K ? src[z * s_per + (long long)o * K + i] : __float2bfloat16(0.f);
+}
+
+}  // namespace fz
+
 // Training control block in device memory, read by the graph's kernels on every replay.
 struct TrainCtl {
 	uint32_t step;   // Adam steps taken so far (the current step's number inside a step)
@@ -736,7 +1067,16 @@ struct mf_mlp {
 	uint64_t launches = 0, step_launches = 0;
 	std::string err;
 	bool tc = false;       // forward products with K % 64 == 0 on tcgen05 (else mma.sync)
+	bool fused = true;     // with tc: inference through the fused whole-network kernel when it applies
 	int sm_count = 1;
+	// fused inference: the BF16 weights re-laid per layer as [members][N][K padded to 64],
+	// their tensor maps, and the kernel's shared-memory plan
+	Buf<bf16> Wf;
+	std::vector<long long> wf_off;
+	long long wf_per = 0;
+	bool wf_dirty = true;  // Wb changed since Wf was packed
+	fz::Maps maps{};
+	int fz_kc = 1, fz_n = 16, fz_stages = 0;
 	Buf<uint32_t> dev_err; // set by a bounded wait of the tcgen05 GEMM that gave up
 	~mf_mlp() {
 		if (graph) cudaGraphExecDestroy(graph);
@@ -827,6 +1167,102 @@ cudaError_t gemm(mf_mlp* m, bool ta, bool tb, GemmArgs g) {
 }
 
 long long sH(const mf_mlp* m, int l) { return (long long)m->rows * m->pd[l]; }
+
+// The fused inference kernel takes models whose padded widths are all at most 256 (one
+// accumulator per half tile, at most four K chunks) and whose operands leave room for at
+// least two weight stages in shared memory.
+void fused_plan(mf_mlp* m) {
+	m->fz_kc = 1;
+	m->fz_n = 16;
+	bool fits = true;
+	for (int l = 0; l < m->L; l++) {
+		m->fz_kc = std::max(m->fz_kc, (m->pd[l] + 63) / 64);
+		m->fz_n = std::max(m->fz_n, m->pd[l + 1]);
+		fits = fits && m->pd[l] <= 256 && m->pd[l + 1] <= 256;
+	}
+	m->fz_stages = 0;
+	if (fits)
+		for (int st = 4; st >= 2 && !m->fz_stages; st--)
+			if (fz::smem_bytes(m->fz_kc, m->fz_n, st) <= TC_SMEM_MAX) m->fz_stages = st;
+}
+
+bool fused_eligible(const mf_mlp* m) { return m->tc && m->fused && m->fz_stages >= 2; }
+
+// (re)packs the BF16 weights for the fused kernel and encodes one tensor map per layer:
+// [members][N][Kp] with member stride wf_per, boxes of 64 K x N rows x 1 member
+mf_status fused_prepare(mf_mlp* m) {
+	if (!m->wf_dirty) return MF_OK;
+	if (!m->Wf.p) {
+		m->wf_off.clear();
+		m->wf_per = 0;
+		for (int l = 0; l < m->L; l++) {
+			m->wf_off.push_back(m->wf_per);
+			m->wf_per += (long long)m->pd[l + 1] * ((m->pd[l] + 63) / 64 * 64);
+		}
+		MCK(m->Wf.alloc((size_t)m->wf_per * m->members));
+	}
+	EncodeTiled enc = tensor_map_encoder();
+	for (int l = 0; l < m->L; l++) {
+		const int N = m->pd[l + 1], K = m->pd[l], Kp = (K + 63) / 64 * 64;
+		const long long per = (long long)N * Kp * m->members;
+		fz::k_pack_layer<<<nblk(per, 256), 256, 0, m->stream>>>(m->members, N, K, Kp, m->Wb.p + m->w_off[l], m->w_per,
+		                                                      m->Wf.p + m->wf_off[l], m->wf_per);
+		m->launches++;
+		MCK(cudaGetLastError());
+		const cuuint64_t dW[3] = {(cuuint64_t)Kp, (cuuint64_t)N, (cuuint64_t)m->members};
+		const cuuint64_t sW[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)m->wf_per * 2};
+		const cuuint32_t bW[3] = {64, (cuuint32_t)N, 1}, e1[3] = {1, 1, 1};
+		if (enc(&m->maps.w[l], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, m->Wf.p + m->wf_off[l], dW, sW, bW, e1,
+		        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+		        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+			m->err = "fused inference: encoding a weight tensor map failed";
+			return MF_ERR_CUDA;
+		}
+	}
+	m->wf_dirty = false;
+	return MF_OK;
+}
+
+// all members over `rows` rows: x[z * sx + r * in + c] -> y[z * sy + r * ldy + c]
+cudaError_t fused_forward(mf_mlp* m, const float* x, long long sx, int rows, float* y, long long sy, int ldy) {
+	if (rows <= 0) return cudaSuccess;
+	fz::Args a{};
+	a.L = m->L;
+	a.in = m->dims[0];
+	a.out = m->dims[m->L];
+	a.rows = rows;
+	a.stages = m->fz_stages;
+	a.kc_max = m->fz_kc;
+	a.n_max = m->fz_n;
+	for (int l = 0; l < m->L; l++) {
+		a.N[l] = m->pd[l + 1];
+		a.KC[l] = (m->pd[l] + 63) / 64;
+		a.b_off[l] = (int)m->b_off[l];
+	}
+	a.bias = m->Bias.p;
+	a.b_per = m->b_per;
+	a.x = x;
+	a.sx = sx;
+	a.y = y;
+	a.sy = sy;
+	a.ldy = ldy;
+	a.members = m->members;
+	const long long tiles = (long long)(rows + fz::TILE - 1) / fz::TILE * m->members;
+	const int G = (int)std::min<long long>(tiles, m->sm_count);
+	fz::k_mlp_fused<<<G, fz::THREADS, fz::smem_bytes(a.kc_max, a.n_max, a.stages), m->stream>>>(m->maps, a,
+	                                                                                           m->dev_err.p);
+	m->launches++;
+	return cudaGetLastError();
+}
+
+bool device_pointer(const void* p) {
+	cudaPointerAttributes at{};
+	if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
 
 // forward pass of all members over `batch` rows already in H[0]
 // direct_out: when the last layer runs on tcgen05, write its unpadded outputs straight
@@ -1038,8 +1474,11 @@ MF_API mf_status mf_mlp_create(const mf_mlp_config* cfg, mf_mlp** out) {
 		MCK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, m->device));
 		MCK(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
 		m->tc = major == 10 && tensor_map_encoder() != nullptr;
-		if (m->tc)
+		fused_plan(m);
+		if (m->tc) {
 			MCK(cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+			MCK(cudaFuncSetAttribute(fz::k_mlp_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+		}
 		m->h_ctl = TrainCtl{};
 		m->h_ctl.seed = cfg->seed * 0x2545F4914F6CDD1Dull + 1;
 		MCK(cudaMemcpy(m->ctl.p, &m->h_ctl, sizeof(TrainCtl), cudaMemcpyHostToDevice));
@@ -1094,6 +1533,7 @@ MF_API mf_status mf_mlp_set_params(mf_mlp* m, int32_t member, const float* host)
 	const long long nw = m->w_per * m->members;
 	k_to_bf16<<<nblk(nw, 256), 256, 0, m->stream>>>(nw, m->W.p, m->Wb.p);
 	m->launches++;
+	m->wf_dirty = true;
 	MCK(cudaGetLastError());
 	MCK(cudaStreamSynchronize(m->stream));
 	return MF_OK;
@@ -1179,6 +1619,7 @@ MF_API mf_status mf_mlp_train(mf_mlp* m, int32_t steps, float lr0, float lr1, fl
 			return mlp_fail(m, "cudaGraphInstantiate", e);
 		}
 	}
+	m->wf_dirty = true;
 	for (int t = 0; t < steps; t++) MCK(cudaGraphLaunch(m->graph, s));
 	m->launches += m->step_launches * (uint64_t)steps;
 	if (loss_history)
@@ -1192,6 +1633,31 @@ MF_API mf_status mf_mlp_predict(mf_mlp* m, const float* x, int32_t n, float* y) 
 	MCK(cudaSetDevice(m->device));
 	cudaStream_t s = m->stream;
 	const int in = m->dims[0], out = m->dims[m->L];
+	if (n > 0 && fused_eligible(m)) {
+		mf_status st = fused_prepare(m);
+		if (st != MF_OK) return st;
+		const bool xd = device_pointer(x), yd = device_pointer(y);
+		if (xd && yd) {  // one launch over every row, straight from x into y
+			MCK(fused_forward(m, x, 0, n, y, (long long)n * out, out));
+		} else
+			for (int r0 = 0; r0 < n; r0 += m->rows) {
+				const int b = std::min(m->rows, n - r0);
+				const float* xs = x + (size_t)r0 * in;
+				if (!xd) {
+					MCK(cudaMemcpyAsync(m->Xin.p, xs, (size_t)b * in * 4, cudaMemcpyDefault, s));
+					xs = m->Xin.p;
+				}
+				if (yd) {
+					MCK(fused_forward(m, xs, 0, b, y + (size_t)r0 * out, (long long)n * out, out));
+				} else {
+					MCK(fused_forward(m, xs, 0, b, m->Yin.p, (long long)m->rows * out, out));
+					MCK(cudaMemcpy2DAsync(y + (size_t)r0 * out, (size_t)n * out * 4, m->Yin.p, (size_t)m->rows * out * 4,
+					                      (size_t)b * out * 4, m->members, cudaMemcpyDefault, s));
+				}
+			}
+		MCK(cudaStreamSynchronize(s));
+		return tc_status(m);
+	}
 	for (int r0 = 0; r0 < n; r0 += m->rows) {
 		const int b = std::min(m->rows, n - r0);
 		MCK(cudaMemcpyAsync(m->Xin.p, x + (size_t)r0 * in, (size_t)b * in * 4, cudaMemcpyDefault, s));
@@ -1239,10 +1705,17 @@ MF_API mf_status mf_mlp_set_option(mf_mlp* m, const char* key, int64_t value) {
 			m->err = "tcgen05: needs a compute capability 10.x device and the driver's tensor-map encoder";
 			return MF_ERR_STATE;
 		}
-		if (value && !m->tc)
+		if (value && !m->tc) {
 			MCK(cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+			MCK(cudaFuncSetAttribute(fz::k_mlp_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+		}
 		m->tc = value != 0;
 		drop_graph(m);  // the captured training step holds the old launches
+		return MF_OK;
+	}
+	if (!strcmp(key, "fused")) {
+		if (value != 0 && value != 1) return MF_ERR_ARG;
+		m->fused = value != 0;
 		return MF_OK;
 	}
 	m->err = std::string("unknown option ") + key;
@@ -1253,6 +1726,10 @@ MF_API mf_status mf_mlp_get_option(const mf_mlp* m, const char* key, int64_t* va
 	if (!m || !key || !value) return MF_ERR_ARG;
 	if (!strcmp(key, "tcgen05")) {
 		*value = m->tc ? 1 : 0;
+		return MF_OK;
+	}
+	if (!strcmp(key, "fused")) {  // 1 when predict runs the fused kernel
+		*value = fused_eligible(m) ? 1 : 0;
 		return MF_OK;
 	}
 	return MF_ERR_ARG;

@@ -555,17 +555,21 @@ def run_experiment(n_train: int = 20000, n_test: int = 1000, val_frac: float = 0
 
 
 def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device: int = 0,
-                   tcgen05: Optional[int] = None) -> dict:
-    """Inference throughput of the ensemble on device-resident inputs: `chunks` passes of
-    `rows` rows through 6 -> 256 -> 256 -> 256 -> 66, timed with CUDA events on the
-    library's stream; FLOPs counted on the true (unpadded) layer sizes.  `tcgen05`
-    selects the tensor-core path of the forward products (None: the library's default)."""
+                   tcgen05: Optional[int] = None, fused: Optional[int] = None) -> dict:
+    """Inference throughput of the ensemble on device-resident inputs and outputs:
+    `chunks` x `rows` rows through 6 -> 256 -> 256 -> 256 -> 66, timed with CUDA events
+    on the library's stream; FLOPs counted on the true (unpadded) layer sizes.  `tcgen05`
+    selects the tensor-core path of the forward products and `fused` the whole-network
+    kernel (one launch over every row) against per-layer GEMMs over passes of `rows`
+    rows (None: the library's defaults)."""
     import torch
 
     dims = [len(FEATURE_LIMITS), 256, 256, 256, N_OUT]
     mlp = Mlp(dims, members=members, max_batch=rows, seed=1, device=device)
     if tcgen05 is not None:
         mlp.set_option("tcgen05", tcgen05)
+    if fused is not None:
+        mlp.set_option("fused", fused)
     n = rows * chunks
     x = torch.rand(n, dims[0], device=f"cuda:{device}", dtype=torch.float32) * 2 - 1
     y = torch.empty(members, n, dims[-1], device=f"cuda:{device}", dtype=torch.float32)
@@ -587,11 +591,11 @@ def gemm_benchmark(rows: int = 65535, chunks: int = 16, members: int = 5, device
     secs = e0.elapsed_time(e1) / 1e3 / reps
     flop_row = 2 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
     flops = flop_row * members * n
-    tc = mlp.get_option("tcgen05")
+    tc, fz = mlp.get_option("tcgen05"), mlp.get_option("fused")
     mlp.close()
     return {"rows_per_pass": rows, "instances": n, "members": members, "seconds": secs,
             "instances_per_s": n / secs, "tflops": flops / secs / 1e12, "flop_per_instance_member": flop_row,
-            "tcgen05": tc}
+            "tcgen05": tc, "fused": fz}
 
 
 if __name__ == "__main__":
@@ -606,9 +610,11 @@ if __name__ == "__main__":
     ap.add_argument("--out", default=None, help="write the JSON result here too")
     ap.add_argument("--gemm-bench", action="store_true", help="only time the ensemble's inference GEMMs")
     ap.add_argument("--tcgen05", type=int, choices=[0, 1], default=None, help="with --gemm-bench: the GEMM path")
+    ap.add_argument("--fused", type=int, choices=[0, 1], default=None,
+                    help="with --gemm-bench: the whole-network kernel (1) or per-layer GEMMs (0)")
     ap.add_argument("--chunks", type=int, default=16, help="with --gemm-bench: passes of 65,535 rows")
     a = ap.parse_args()
-    r = (gemm_benchmark(chunks=a.chunks, tcgen05=a.tcgen05) if a.gemm_bench
+    r = (gemm_benchmark(chunks=a.chunks, tcgen05=a.tcgen05, fused=a.fused) if a.gemm_bench
          else run_experiment(a.train, a.test, train_steps=a.steps, data=a.data))
     s = json.dumps(r, indent=1)
     print(s)

@@ -185,30 +185,105 @@ def test_screened_sweep_beats_the_solver(lib):
 # ------------------------------------------------------- tcgen05 GEMM
 @pytest.mark.parametrize("rows", [300, 4096])
 def test_tcgen05_forward_matches_mma_sync(lib, rows):
-    """The forward products with K a multiple of 64 (the 256-wide layers and the output
-    layer) on tcgen05 -- TMEM accumulators, TMA-staged 128-byte-swizzled operands --
-    against the mma.sync kernels on the same parameters and inputs: both accumulate the
-    same BF16 products in FP32 in different orders, so the FP32 outputs agree to within
-    the BF16 rounding of the hidden activations they pass between layers (relative L2
-    <= 5e-3 per member; in practice ~1e-3).  300 rows: one partial tile per member;
-    4096 rows: 32 tiles per member, several per persistent CTA, both accumulators."""
+    """Inference on tcgen05 -- the fused whole-network kernel (the default) and the
+    per-layer GEMM (option fused 0: TMEM accumulators, TMA-staged 128-byte-swizzled
+    operands for the products with K a multiple of 64) -- against the mma.sync kernels on
+    the same parameters and inputs: all accumulate the same BF16 products in FP32 in
+    different orders, so the FP32 outputs agree to within the BF16 rounding of the hidden
+    activations they pass between layers (relative L2 <= 5e-3 per member; in practice
+    ~1e-3).  300 rows: one partial tile per member; 4096 rows: several tiles per
+    persistent CTA, both accumulators."""
     from mfree_iwf_gb300.surrogate import Mlp
     mlp = Mlp(DIMS, members=5, max_batch=rows, seed=11)
     assert mlp.get_option("tcgen05") == 1  # the default on a GB300
+    assert mlp.get_option("fused") == 1
     rng = np.random.default_rng(4)
     x = rng.uniform(-1, 1, size=(rows, DIMS[0])).astype(np.float32)
+    y_fz = mlp.predict(x)
+    mlp.set_option("fused", 0)
+    assert mlp.get_option("fused") == 0
     y_tc = mlp.predict(x)
     mlp.set_option("tcgen05", 0)
     y_ref = mlp.predict(x)
     mlp.set_option("tcgen05", 1)
     y_tc2 = mlp.predict(x)
+    mlp.set_option("fused", 1)
+    y_fz2 = mlp.predict(x)
     mlp.close()
-    assert y_tc.shape == (5, rows, DIMS[-1])
+    assert y_tc.shape == y_fz.shape == (5, rows, DIMS[-1])
     np.testing.assert_array_equal(y_tc, y_tc2)  # deterministic
+    np.testing.assert_array_equal(y_fz, y_fz2)
     for z in range(5):
-        e = _rel(y_tc[z], y_ref[z])
-        print(f"member {z}: relative L2 {e:.2e}")
-        assert e <= 5e-3, (z, e)
+        e, ef = _rel(y_tc[z], y_ref[z]), _rel(y_fz[z], y_ref[z])
+        print(f"member {z}: relative L2 per-layer {e:.2e} fused {ef:.2e}")
+        assert e <= 5e-3 and ef <= 5e-3, (z, e, ef)
+
+
+@pytest.mark.parametrize("dims", [[6, 100, 40, 66], [3, 64, 2], [70, 256, 130, 8]])
+def test_fused_predict_on_padded_widths(lib, dims):
+    """The fused kernel on widths that are not multiples of 64 (the hidden activations
+    zero padded to the next layer's K, output blocks narrower than 32 columns, an input
+    wider than 64) against the FP64 network oracle with BF16 rounding at the same points,
+    and against the mma.sync kernels."""
+    from mfree_iwf_gb300.surrogate import Mlp
+    mlp = Mlp(dims, members=3, max_batch=300, seed=7)
+    assert mlp.get_option("fused") == 1
+    rng = np.random.default_rng(8)
+    for z in range(3):  # non-zero biases too
+        p = mlp.get_params(z)
+        mlp.set_params(z, p + rng.normal(scale=0.1, size=p.shape).astype(np.float32))
+    x = rng.uniform(-1, 1, size=(700, dims[0])).astype(np.float32)  # 3 chunks, the last ragged
+    y = mlp.predict(x)
+    mlp.set_option("tcgen05", 0)
+    y_ref = mlp.predict(x)
+    for z in range(3):
+        ye, _ = R.forward(mlp.get_params(z).astype(np.float64), dims, x, emulate=True)
+        e, er = _rel(y[z], ye), _rel(y[z], y_ref[z])
+        print(dims, z, f"oracle {e:.2e} mma.sync {er:.2e}")
+        assert e < 3e-3 and er < 5e-3, (z, e, er)
+    mlp.close()
+
+
+def test_fused_predict_not_taken_past_256_wide(lib):
+    """A layer wider than 256 leaves inference on the per-layer kernels."""
+    from mfree_iwf_gb300.surrogate import Mlp
+    mlp = Mlp([6, 300, 4], members=2, max_batch=64, seed=3)
+    assert mlp.get_option("tcgen05") == 1 and mlp.get_option("fused") == 0
+    x = np.random.default_rng(2).uniform(-1, 1, size=(50, 6)).astype(np.float32)
+    y = mlp.predict(x)
+    for z in range(2):
+        ye, _ = R.forward(mlp.get_params(z).astype(np.float64), [6, 300, 4], x, emulate=True)
+        assert _rel(y[z], ye) < 3e-3
+    mlp.close()
+
+
+def test_fused_predict_device_buffers_one_launch(lib):
+    """With device-resident inputs and outputs the fused path runs every row in one
+    launch, straight into the caller's [members][n][out] buffer, and equals the chunked
+    host-buffer path bit for bit (rows are independent of the tiling); new parameters
+    are re-packed before the next inference."""
+    import ctypes
+    import torch
+    from mfree_iwf_gb300.surrogate import Mlp
+    mlp = Mlp(DIMS, members=4, max_batch=512, seed=21)
+    rng = np.random.default_rng(6)
+    n = 3000
+    x = rng.uniform(-1, 1, size=(n, DIMS[0])).astype(np.float32)
+    y_host = mlp.predict(x)  # 6 chunks of 512 rows through host staging
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty((4, n, DIMS[-1]), device="cuda", dtype=torch.float32)
+    fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+    before = mlp.launch_count()
+    mlp._check(mlp._lib.mf_mlp_predict(mlp._h, fp(xd), n, fp(yd)), "mf_mlp_predict")
+    assert mlp.launch_count() - before == 1
+    np.testing.assert_array_equal(yd.cpu().numpy(), y_host)
+    p = mlp.get_params(2) * 0.5
+    mlp.set_params(2, p)
+    mlp._check(mlp._lib.mf_mlp_predict(mlp._h, fp(xd), n, fp(yd)), "mf_mlp_predict")
+    ye, _ = R.forward(p.astype(np.float64), DIMS, x, emulate=True)
+    assert _rel(yd[2].cpu().numpy(), ye) < 3e-3
+    np.testing.assert_array_equal(yd[0].cpu().numpy(), y_host[0])
+    mlp.close()
 
 
 def test_tcgen05_training_matches_mma_sync(lib):
