@@ -548,17 +548,22 @@ __global__ void __launch_bounds__(THREADS, 1)
 // and runs them through all layers:
 //   - the epilogue warps write the tile's input rows (FP32 -> BF16, zero padded to the
 //     first layer's K) into shared memory in the 128-byte-swizzled K-major layout that
-//     a TMA load would produce, so the tensor core reads them as the A operand;
+//     a TMA load would produce, so the tensor core reads them as an operand: per 64-wide
+//     K chunk the 256 rows in order (half 0's 128, then half 1's);
 //   - the producer (warp 0) streams each layer's BF16 weights, 64-wide K chunks of all
 //     N rows, through a ring of shared-memory stages with TMA;
-//   - the MMA issuer (warp 1) multiplies, per K chunk, both halves into their
-//     accumulators and commits each half's accumulator after its last chunk;
+//   - the MMA issuer (warp 1) multiplies, per K chunk, both halves (A = the half's rows,
+//     B = the weights: M = 128, N = the layer's width) and commits each half's
+//     accumulator after its last chunk.  An M = 128 product takes about as long for any
+//     N up to 256, so the narrow output layer runs transposed: A = its weights (the
+//     outputs padded to 128 or 256 rows by the tensor map's zero fill), B = all 256 rows
+//     of the tile (N = 256), half the products of two M = 128 halves;
 //   - the epilogue warps (8: four TMEM lane quarters x two halves) read their half's
-//     accumulator, add the bias, apply ReLU, round to BF16 and write the next layer's A
-//     operand over the current one (whose products are complete by then); after the last
-//     layer they add the bias and store the FP32 outputs, 32 rows x 32 columns at a
-//     time staged through their own rows of shared memory so that each store
-//     instruction writes one contiguous row segment.
+//     accumulator (two TMEM loads in flight: the next 32 columns load while these are
+//     converted), add the bias, apply ReLU, round to BF16 and write the next layer's
+//     operand over the current one (whose products are complete by then); after the
+//     output layer a warp holds 32 consecutive outputs (TMEM lanes) of its half's rows
+//     (columns), adds the bias and stores each row's 32 outputs with one coalesced store.
 // Only the inputs (in FP32), the weights (from L2: every CTA on a member reads the same
 // ones) and the outputs move through memory.  The products are the per-layer path's --
 // BF16 operands, FP32 accumulation in K order, the bias added in FP32 -- with K padded
@@ -578,6 +583,7 @@ struct Maps {
 struct Args {
 	int L, in, out, rows, stages, kc_max, n_max;
 	int N[MF_MLP_MAX_LAYERS], KC[MF_MLP_MAX_LAYERS];  // MMA width (padded to 16); K / 64 (K padded to 64)
+	int mb_last;                                       // 128-row blocks of the transposed output layer (1 or 2)
 	int b_off[MF_MLP_MAX_LAYERS];
 	const float* bias;
 	long long b_per;
@@ -592,18 +598,18 @@ struct Args {
 // the mbarriers (2 per weight stage, 2 x 2 per half, 1 to drain) and the TMEM address,
 // rounded up to 16 bytes
 __host__ __device__ constexpr size_t bar_bytes(int stages) { return (8 * (2 * stages + 5) + 4 + 15) / 16 * 16; }
-// shared memory: 1 KB for the 1 KB alignment of the swizzled operands, the two halves'
-// A operands, the weight stages, the barriers and one layer's bias
+// shared memory: 1 KB for the 1 KB alignment of the swizzled operands, the operand
+// chunks of the tile, the weight stages, the barriers and one layer's bias
 __host__ __device__ constexpr size_t smem_bytes(int kc_max, int n_max, int stages) {
 	return 1024 + (size_t)2 * kc_max * CHUNK + (size_t)stages * n_max * 128 + bar_bytes(stages) + (size_t)n_max * 4;
 }
 
-// one 16-byte unit (8 BF16 columns starting at col, a multiple of 8) of row r of a
-// half, at its place in the 128-byte swizzle: chunk col / 64, unit (col % 64) / 8
-// XOR (r % 8)
-__device__ __forceinline__ void put_unit(uint8_t* half, int r, int col, uint4 v) {
+// the 16-byte unit holding columns col .. col + 7 (col a multiple of 8) of row r of half
+// h: K chunk col / 64 (the chunk's 256 rows: half 0, then half 1), unit (col % 64) / 8
+// XOR (r % 8) -- the 128-byte swizzle
+__device__ __forceinline__ uint4* unit_at(uint8_t* act, int h, int r, int col) {
 	const int kc = col >> 6, u = (col >> 3) & 7;
-	*reinterpret_cast<uint4*>(half + (size_t)kc * CHUNK + r * 128 + ((u ^ (r & 7)) << 4)) = v;
+	return reinterpret_cast<uint4*>(act + (size_t)(2 * kc + h) * CHUNK + r * 128 + ((u ^ (r & 7)) << 4));
 }
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
 	__nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -634,19 +640,40 @@ __device__ __forceinline__ bool epi_all(bool p) {
 	return r != 0;
 }
 
+// 32 accumulator columns col0 .. col0 + 31 of row r (in v) -> bias (sb4: the layer's bias
+// in shared memory), ReLU, BF16 -> their four 16-byte units of the next operand; columns
+// at or past N (the layer's width) become zeros up to the next layer's K
+__device__ __forceinline__ void hidden_units(uint8_t* act, int h, int r, int col0, int N, const uint32_t* v,
+                                             const float4* sb4) {
+#pragma unroll
+	for (int u = 0; u < 4; u++) {
+		const int col = col0 + 8 * u;
+		uint4 w = make_uint4(0, 0, 0, 0);
+		if (col < N) {
+			const float4 b0 = sb4[col >> 2], b1 = sb4[(col >> 2) + 1];
+			float f[8];
+#pragma unroll
+			for (int e = 0; e < 8; e++) f[e] = __uint_as_float(v[8 * u + e]);
+			w = make_uint4(pack2_relu(f[0] + b0.x, f[1] + b0.y), pack2_relu(f[2] + b0.z, f[3] + b0.w),
+			               pack2_relu(f[4] + b1.x, f[5] + b1.y), pack2_relu(f[6] + b1.z, f[7] + b1.w));
+		}
+		*unit_at(act, h, r, col) = w;
+	}
+}
+
 __global__ void __launch_bounds__(THREADS, 1)
     k_mlp_fused(const __grid_constant__ Maps maps, const Args a, uint32_t* err) {
 	using namespace tc;
 	extern __shared__ uint8_t smem_raw[];
 	const uint32_t raw = saddr(smem_raw);
 	uint8_t* act = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-	const size_t half_bytes = (size_t)a.kc_max * CHUNK, wst = (size_t)a.n_max * 128;
-	const int S = a.stages;
-	uint8_t* sW = act + 2 * half_bytes;
+	const size_t wst = (size_t)a.n_max * 128;
+	const int S = a.stages, L = a.L;
+	uint8_t* sW = act + (size_t)2 * a.kc_max * CHUNK;
 	uint64_t* w_full = reinterpret_cast<uint64_t*>(sW + (size_t)S * wst);
 	uint64_t* w_empty = w_full + S;
 	uint64_t* acc_full = w_empty + S;    // per half: the layer's products are complete
-	uint64_t* act_ready = acc_full + 2;  // per half: the A operand of the next layer is written
+	uint64_t* act_ready = acc_full + 2;  // per half: the operand of the next layer is written
 	uint64_t* fin = act_ready + 2;
 	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
 	float* sbias = reinterpret_cast<float*>(sW + (size_t)S * wst + bar_bytes(S));  // the current layer's bias
@@ -682,14 +709,17 @@ __global__ void __launch_bounds__(THREADS, 1)
 			uint32_t it = 0;
 			for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
 				const int z = t % a.members;
-				for (int l = 0; l < a.L && ok; l++)
+				for (int l = 0; l < L && ok; l++) {
+					// the output layer's box is 128 * mb_last rows, zero filled past its width
+					const uint32_t bytes = (uint32_t)(l + 1 < L ? a.N[l] : 128 * a.mb_last) * 128u;
 					for (int kc = 0; kc < a.KC[l]; kc++, it++) {
 						const int s = (int)(it % S);
 						const uint32_t use = it / S;
 						if (use > 0 && !(ok = mbar_wait(w_empty + s, (use - 1) & 1u))) break;
-						mbar_expect_tx(w_full + s, (uint32_t)a.N[l] * 128u);
+						mbar_expect_tx(w_full + s, bytes);
 						tma_load_3d(sW + (size_t)s * wst, &maps.w[l], kc * 64, 0, z, w_full + s);
 					}
+				}
 			}
 			// the loads still in flight land before the CTA leaves (consumed ones: at once)
 			for (uint32_t k = it > (uint32_t)S ? it - S : 0; k < it; k++) mbar_wait(w_full + k % S, (k / S) & 1u);
@@ -699,24 +729,39 @@ __global__ void __launch_bounds__(THREADS, 1)
 			uint32_t it = 0, step = 0;
 			bool issued = false;
 			for (int t = blockIdx.x; t < total && ok; t += gridDim.x)
-				for (int l = 0; l < a.L && ok; l++, step++) {
+				for (int l = 0; l < L && ok; l++, step++) {
 					if (!(ok = mbar_wait(act_ready, step & 1u)) || !(ok = mbar_wait(act_ready + 1, step & 1u))) break;
 					fence_after();
-					const uint32_t idesc = idesc_bf16(HALF, a.N[l]);
+					const bool last = l + 1 == L;
+					const uint32_t idesc = last ? idesc_bf16(HALF, TILE) : idesc_bf16(HALF, a.N[l]);
 					for (int kc = 0; kc < a.KC[l]; kc++, it++) {
 						const int s = (int)(it % S);
 						if (!(ok = mbar_wait(w_full + s, (it / S) & 1u))) break;
 						fence_after();
-						const uint32_t b0 = saddr(sW + (size_t)s * wst);
-						for (int h = 0; h < 2; h++) {
-							const uint32_t a0 = saddr(act + h * half_bytes + (size_t)kc * CHUNK);
+						const uint32_t wb = saddr(sW + (size_t)s * wst), ab = saddr(act + (size_t)2 * kc * CHUNK);
+						if (!last) {
+							for (int h = 0; h < 2; h++) {  // D[row][n] of half h: A = its rows, B = the weights
+								const uint32_t a0 = ab + (uint32_t)(h * CHUNK);
 #pragma unroll
-							for (int k = 0; k < 4; k++)  // K = 16 per instruction: 32 bytes along the swizzled row
-								mma_bf16(tmem + (uint32_t)(h * 256), sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k), idesc,
-								         (kc | k) != 0);
-							if (kc == a.KC[l] - 1) mma_commit(acc_full + h);
+								for (int k = 0; k < 4; k++)  // K = 16 per instruction: 32 bytes along the swizzled row
+									mma_bf16(tmem + (uint32_t)(h * 256), sw128_desc(a0 + 32u * k), sw128_desc(wb + 32u * k), idesc,
+									         (kc | k) != 0);
+								if (kc == a.KC[l] - 1) mma_commit(acc_full + h);
+							}
+						} else {
+							for (int mb = 0; mb < a.mb_last; mb++) {  // D[out][row]: A = 128 weight rows, B = the tile's 256 rows
+								const uint32_t w0 = wb + (uint32_t)(mb * CHUNK);
+#pragma unroll
+								for (int k = 0; k < 4; k++)
+									mma_bf16(tmem + (uint32_t)(mb * 256), sw128_desc(w0 + 32u * k), sw128_desc(ab + 32u * k), idesc,
+									         (kc | k) != 0);
+							}
+							if (kc == a.KC[l] - 1) {
+								mma_commit(acc_full);
+								mma_commit(acc_full + 1);
+							}
 						}
-						mma_commit(w_empty + s);  // the stage is free once both halves' products are done
+						mma_commit(w_empty + s);  // the stage is free once these products are done
 						issued = true;
 					}
 				}
@@ -726,9 +771,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 			}
 		}
 	} else {  // epilogue: half h, TMEM lane quarter q, row r of the half
-		const int h = (warp - 2) >> 2, q = warp & 3, r = 32 * q + lane, et = threadIdx.x - 64, rx = r & 7;
-		uint8_t* actH = act + h * half_bytes;
-		const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(h * 256);
+		const int h = (warp - 2) >> 2, q = warp & 3, r = 32 * q + lane, et = threadIdx.x - 64;
+		const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);  // this warp's lane quarter
 		const float4* sb4 = reinterpret_cast<const float4*>(sbias);
 		// tile tt: member tt % members (CTAs running side by side read different members'
 		// weights), rows (tt / members) * 256 + ...; the first 8 input columns of this
@@ -742,8 +786,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 			for (int j = 0; j < 8; j++) xp[j] = live && j < a.in ? xr[j] : 0.f;
 		};
 		auto x_write = [&](int tt) {  // the input row, BF16, zero padded to the first layer's K
-			*reinterpret_cast<uint4*>(actH + r * 128 + (rx << 4)) =
-			    make_uint4(pack2(xp[0], xp[1]), pack2(xp[2], xp[3]), pack2(xp[4], xp[5]), pack2(xp[6], xp[7]));
+			*unit_at(act, h, r, 0) = make_uint4(pack2(xp[0], xp[1]), pack2(xp[2], xp[3]), pack2(xp[4], xp[5]), pack2(xp[6], xp[7]));
 			const int grow = (tt / a.members) * TILE + h * HALF + r;
 			const bool live = grow < a.rows;
 			const float* xr = a.x + (tt % a.members) * a.sx + (long long)(live ? grow : 0) * a.in;
@@ -751,7 +794,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 				float f[8];
 #pragma unroll
 				for (int j = 0; j < 8; j++) f[j] = live && col + j < a.in ? xr[col + j] : 0.f;
-				put_unit(actH, r, col, make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7])));
+				*unit_at(act, h, r, col) = make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
 			}
 			proxy_fence();  // generic-proxy writes, read next by the tensor core
 			mbar_arrive(act_ready + h);
@@ -771,72 +814,62 @@ __global__ void __launch_bounds__(THREADS, 1)
 		uint32_t step = 0;
 		for (; t < total && ok; t += gridDim.x) {
 			const int z = t % a.members, row0 = (t / a.members) * TILE + h * HALF, tn = t + gridDim.x;
-			for (int l = 0; l < a.L; l++, step++) {
-				const bool last = l + 1 == a.L;
+			for (int l = 0; l < L; l++, step++) {
+				const bool last = l + 1 == L;
 				if (last && tn < total) x_fetch(tn);  // its latency hides under the products
 				const bool mine = mbar_wait(acc_full + h, step & 1u);
 				if (mine) {
 					fence_after();
 					const int N = a.N[l];
+					uint32_t va[32], vb[32];
 					if (!last) {
-						// per 64-wide K chunk of the next layer: two TMEM loads, one wait; the
-						// row's eight 16-byte units at their swizzled places
-						const int KCn = a.KC[l + 1];
-						for (int kc = 0; kc < KCn; kc++) {
-							const int c0 = 64 * kc;
-							uint32_t v[64];
-							if (c0 < N) {
-								tmem_ld32_async(tq + (uint32_t)c0, v);
-								if (c0 + 32 < N) tmem_ld32_async(tq + (uint32_t)(c0 + 32), v + 32);
-								tmem_wait();
-							}
-							uint8_t* dst = actH + (size_t)kc * CHUNK + r * 128;
-#pragma unroll
-							for (int u = 0; u < 8; u++) {
-								const int col = c0 + 8 * u;
-								uint4 w = make_uint4(0, 0, 0, 0);
-								if (col < N) {
-									const float4 b0 = sb4[col >> 2], b1 = sb4[(col >> 2) + 1];
-									float f[8];
-#pragma unroll
-									for (int e = 0; e < 8; e++) f[e] = __uint_as_float(v[8 * u + e]);
-									w = make_uint4(pack2_relu(f[0] + b0.x, f[1] + b0.y), pack2_relu(f[2] + b0.z, f[3] + b0.w),
-									               pack2_relu(f[4] + b1.x, f[5] + b1.y), pack2_relu(f[6] + b1.z, f[7] + b1.w));
-								}
-								*reinterpret_cast<uint4*>(dst + ((u ^ rx) << 4)) = w;
-							}
+						// this half's accumulator, 32 columns at a time, the next 32 loading
+						// while these are converted
+						const uint32_t acc = tq + (uint32_t)(h * 256);
+						const int Kn = 64 * a.KC[l + 1];
+						if (N > 0) tmem_ld32_async(acc, va);
+						tmem_wait();
+						for (int c0 = 0; c0 < Kn; c0 += 64) {
+							if (c0 + 32 < N) tmem_ld32_async(acc + (uint32_t)(c0 + 32), vb);
+							hidden_units(act, h, r, c0, N, va, sb4);
+							tmem_wait();
+							if (c0 + 64 < N) tmem_ld32_async(acc + (uint32_t)(c0 + 64), va);
+							hidden_units(act, h, r, c0 + 32, N, vb, sb4);
+							tmem_wait();
 						}
 						fence_before();
 						proxy_fence();
 						mbar_arrive(act_ready + h);
 					} else {
-						// FP32 outputs: each 32 x 32 block through this warp's own 32 rows of
-						// chunk 0 (swizzled like the operands: conflict-free both ways), then
-						// one row segment per store instruction
-						uint8_t* stg = actH + 32 * q * 128;
+						// D[output f][tile row]: this warp holds outputs 128 mb + 32 q + lane of
+						// its half's 128 rows (columns 128 h ..); one coalesced store per row
 						float* yz = a.y + z * a.sy;
-						for (int c0 = 0; c0 < N && c0 < a.out; c0 += 32) {
-							uint32_t v[32];
-							tmem_ld32(tq + (uint32_t)c0, v);
-							__syncwarp();
+						for (int mb = 0; mb < a.mb_last; mb++) {
+							if (128 * mb + 32 * q >= a.out) continue;  // no output of this warp here
+							const int f = 128 * mb + 32 * q + lane;
+							const float bf = f < N ? sbias[f] : 0.f;
+							const bool fo = f < a.out;
+							const uint32_t acc = tq + (uint32_t)(mb * 256 + h * HALF);
+							tmem_ld32_async(acc, va);
+							tmem_wait();
+							for (int p = 0; p < 4; p += 2) {
+								tmem_ld32_async(acc + (uint32_t)(32 * (p + 1)), vb);
 #pragma unroll
-							for (int j = 0; j < 8; j++) {
-								const float4 bj = c0 + 4 * j < N ? sb4[(c0 >> 2) + j] : make_float4(0.f, 0.f, 0.f, 0.f);
-								const float4 o = make_float4(__uint_as_float(v[4 * j]) + bj.x, __uint_as_float(v[4 * j + 1]) + bj.y,
-								                             __uint_as_float(v[4 * j + 2]) + bj.z, __uint_as_float(v[4 * j + 3]) + bj.w);
-								*reinterpret_cast<float4*>(stg + lane * 128 + ((j ^ (lane & 7)) << 4)) = o;
-							}
-							__syncwarp();
-							const int col = c0 + lane;
-							for (int rr = 0; rr < 32; rr++) {
-								const int gr = row0 + 32 * q + rr;
-								const float val =
-								    *reinterpret_cast<const float*>(stg + rr * 128 + (((lane >> 2) ^ (rr & 7)) << 4) + (lane & 3) * 4);
-								if (gr < a.rows && col < a.out) yz[(long long)gr * a.ldy + col] = val;
+								for (int j = 0; j < 32; j++) {
+									const int gr = row0 + 32 * p + j;
+									if (fo && gr < a.rows) yz[(long long)gr * a.ldy + f] = __uint_as_float(va[j]) + bf;
+								}
+								tmem_wait();
+								if (p + 2 < 4) tmem_ld32_async(acc + (uint32_t)(32 * (p + 2)), va);
+#pragma unroll
+								for (int j = 0; j < 32; j++) {
+									const int gr = row0 + 32 * (p + 1) + j;
+									if (fo && gr < a.rows) yz[(long long)gr * a.ldy + f] = __uint_as_float(vb[j]) + bf;
+								}
+								tmem_wait();
 							}
 						}
 						fence_before();
-						__syncwarp();  // this warp's staging rows take the next tile's input now
 						if (tn < total) x_write(tn);
 					}
 				}
@@ -1177,7 +1210,8 @@ void fused_plan(mf_mlp* m) {
 	bool fits = true;
 	for (int l = 0; l < m->L; l++) {
 		m->fz_kc = std::max(m->fz_kc, (m->pd[l] + 63) / 64);
-		m->fz_n = std::max(m->fz_n, m->pd[l + 1]);
+		// the output layer's weight box: 128 or 256 rows (it runs transposed, M = 128 per block)
+		m->fz_n = std::max(m->fz_n, l + 1 < m->L ? m->pd[l + 1] : (m->pd[l + 1] + 127) / 128 * 128);
 		fits = fits && m->pd[l] <= 256 && m->pd[l + 1] <= 256;
 	}
 	m->fz_stages = 0;
@@ -1211,7 +1245,8 @@ mf_status fused_prepare(mf_mlp* m) {
 		MCK(cudaGetLastError());
 		const cuuint64_t dW[3] = {(cuuint64_t)Kp, (cuuint64_t)N, (cuuint64_t)m->members};
 		const cuuint64_t sW[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)m->wf_per * 2};
-		const cuuint32_t bW[3] = {64, (cuuint32_t)N, 1}, e1[3] = {1, 1, 1};
+		const cuuint32_t box_rows = l + 1 < m->L ? (cuuint32_t)N : (cuuint32_t)((N + 127) / 128 * 128);  // zero filled past N
+		const cuuint32_t bW[3] = {64, box_rows, 1}, e1[3] = {1, 1, 1};
 		if (enc(&m->maps.w[l], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, m->Wf.p + m->wf_off[l], dW, sW, bW, e1,
 		        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
 		        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
@@ -1234,6 +1269,7 @@ cudaError_t fused_forward(mf_mlp* m, const float* x, long long sx, int rows, flo
 	a.stages = m->fz_stages;
 	a.kc_max = m->fz_kc;
 	a.n_max = m->fz_n;
+	a.mb_last = (m->pd[m->L] + 127) / 128;
 	for (int l = 0; l < m->L; l++) {
 		a.N[l] = m->pd[l + 1];
 		a.KC[l] = (m->pd[l] + 63) / 64;

@@ -219,12 +219,13 @@ def test_tcgen05_forward_matches_mma_sync(lib, rows):
         assert e <= 5e-3 and ef <= 5e-3, (z, e, ef)
 
 
-@pytest.mark.parametrize("dims", [[6, 100, 40, 66], [3, 64, 2], [70, 256, 130, 8]])
+@pytest.mark.parametrize("dims", [[6, 100, 40, 66], [3, 64, 2], [70, 256, 130, 8], [6, 64, 200]])
 def test_fused_predict_on_padded_widths(lib, dims):
     """The fused kernel on widths that are not multiples of 64 (the hidden activations
-    zero padded to the next layer's K, output blocks narrower than 32 columns, an input
-    wider than 64) against the FP64 network oracle with BF16 rounding at the same points,
-    and against the mma.sync kernels."""
+    zero padded to the next layer's K, outputs fewer than 32 or more than 128 -- two
+    blocks of the transposed output layer --, an input wider than 64) against the FP64
+    network oracle with BF16 rounding at the same points, and against the mma.sync
+    kernels."""
     from mfree_iwf_gb300.surrogate import Mlp
     mlp = Mlp(dims, members=3, max_batch=300, seed=7)
     assert mlp.get_option("fused") == 1
