@@ -293,6 +293,15 @@ MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
  *   "ul_split"        1 (default) / 4 / 8: threads per row of the mixed UL pair pass
  *                     (plain grid; partial sums added across the row's threads, so the
  *                     pair sums change order); mf_autotune tries all three
+ *   "contact_overlap" 1 (default) / 0: mixed total-Lagrangian bodies with contact run
+ *                     the contact query of the positions a step ends with at the start
+ *                     of the next step, beside stage 0's pass A on a second stream (the
+ *                     pass reads no contact force), instead of at the end of the step:
+ *                     bit-identical results.  Every call that reads the state or the
+ *                     forces, replaces the state, dumps or tunes runs a pending query
+ *                     first; off while the monitor or per-kernel timing is on.  Work a
+ *                     caller enqueues on mf_get_stream between steps does not see the
+ *                     forces of the last step until such a call.
  * read-only, through mf_get_option:
  *   "tl_tiles_built"  1 when the halo tiles exist (mixed TL, after the first step)
  *   "tl_halo_max"     the largest tile halo, in rows

@@ -322,12 +322,19 @@ struct mf_ctx {
 	Tune tune;
 	int sm_count = 0;
 	DevBuf<uint32_t> work;
-	cudaGraph_t graph = nullptr;
-	cudaGraphExec_t graph_exec = nullptr;
-	uint64_t graph_launches = 0;
+	// [0]: a step; [1]: a step that starts with the pending contact query (contact_pending)
+	cudaGraph_t graph[2] = {nullptr, nullptr};
+	cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+	uint64_t graph_launches[2] = {0, 0};
+	bool graph_deferred = false;  // contact_deferred() when the graphs were captured
 
 	// contact
 	bool contact_on = false;
+	// mixed TL: the contact query of the positions a step ends with runs at the start of
+	// the next step, beside stage 0's pass A on a side stream (contact_overlap, default on)
+	bool contact_overlap = true, contact_pending = false;
+	cudaStream_t side = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	DevBuf<uint32_t> bnd_rows, bnd_start, bnd_len, tile_first, tile_end, slave_rows, slave_master, m_tile_off, m_tile_n;
 	DevBuf<double4> bnd;
 	DevBuf<float4> tile_bb, bnd_ff;
@@ -962,10 +969,14 @@ cudaError_t tl_launch(mf_ctx* c, const TLArgs& a, int part) {
 	return c->strict ? mf_strict::tl_stage(a, c->mixed, part, c->stream) : mf_fast::tl_stage(a, c->mixed, part, c->stream);
 }
 
+mf_status contact_run(mf_ctx* c, cudaStream_t s);
+
 // One RK4 step of every TL body: per stage the BCs, (pack), pass A, pass B; the
 // stage state ping-pongs between sets 2 and 3 so that pass B never overwrites data
-// its neighbours still read.
-mf_status tl_step_all(mf_ctx* c) {
+// its neighbours still read.  fork_contact: the pending contact query of the particles'
+// positions (set 0, written only by stage 3) runs on the side stream beside stage 0's
+// pass A, and pass B (the first reader of the forces) waits for it.
+mf_status tl_step_all(mf_ctx* c, bool fork_contact = false) {
 	TLArgs a = tl_args(c);
 	StateSoA S0 = a.st, S1 = a.nxt;
 	// mixed form: pass B writes the next stage's records (no pack kernel), except with
@@ -1001,9 +1012,18 @@ mf_status tl_step_all(mf_ctx* c) {
 			c->launches += (corot ? 3 : 2) + (c->mixed ? 1 : 0) + (c->n_bc ? 1 : 0);
 			continue;
 		}
+		const bool fork = fork_contact && st == 0;
+		if (fork) {
+			CK(cudaEventRecord(c->ev_fork, c->stream));
+			CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+			mf_status cs = contact_run(c, c->side);
+			if (cs != MF_OK) return cs;
+			CK(cudaEventRecord(c->ev_join, c->side));
+		}
 		timing_begin(c, 1, slot);
 		if ((e = tl_launch(c, a, 2)) != cudaSuccess) return cuda_fail(c, e, "tl pass A");
 		timing_end(c, slot, c->n_total);
+		if (fork) CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
 		timing_begin(c, 2, slot);
 		if ((e = tl_launch(c, a, 3)) != cudaSuccess) return cuda_fail(c, e, "tl pass B");
 		timing_end(c, slot, c->n_total);
@@ -2061,6 +2081,11 @@ mf_status contact_setup(mf_ctx* c) {
 	c->n_slave = (uint32_t)srows.size();
 	c->contact_on = c->cfg.contact && c->n_slave > 0;
 	if (!c->contact_on) return MF_OK;
+	if (!c->side) {  // for the contact query beside pass A (contact_deferred)
+		CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+		CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+		CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+	}
 	auto up = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
 		CK(d.alloc(v.size()));
 		if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
@@ -2079,7 +2104,7 @@ mf_status contact_setup(mf_ctx* c) {
 	return MF_OK;
 }
 
-mf_status contact_run(mf_ctx* c) {
+mf_status contact_run(mf_ctx* c, cudaStream_t s) {
 	ContactArgs a{};
 	a.n_bnd = c->n_bnd; a.n_tiles = c->n_tiles; a.n_slave = c->n_slave;
 	a.bnd_rows = c->bnd_rows.p; a.bnd_start = c->bnd_start.p; a.bnd_len = c->bnd_len.p;
@@ -2087,13 +2112,33 @@ mf_status contact_run(mf_ctx* c) {
 	a.slave_rows = c->slave_rows.p; a.slave_master = c->slave_master.p; a.dt = c->slave_dt.p;
 	a.m_tile_off = c->m_tile_off.p; a.m_tile_n = c->m_tile_n.p;
 	a.x = c->sd[0][0].p; a.y = c->sd[0][1].p; a.m = c->m.p; a.fcx = c->fcx.p; a.fcy = c->fcy.p;
-	int slot;
-	timing_begin(c, 3, slot);
-	cudaError_t e = c->strict ? mf_strict::contact_step(a, c->stream) : mf_fast::contact_step(a, c->stream);
+	int slot = -1;
+	if (s == c->stream) timing_begin(c, 3, slot);
+	cudaError_t e = c->strict ? mf_strict::contact_step(a, s) : mf_fast::contact_step(a, s);
 	timing_end(c, slot, c->n_slave);
 	if (e != cudaSuccess) return cuda_fail(c, e, "contact");
 	c->launches += 3;
 	return MF_OK;
+}
+
+// Mixed TL with contact: the contact query of the positions a step ends with is left
+// pending and runs at the start of the next step on a side stream, beside stage 0's
+// pass A (which reads no contact force); pass B waits for it.  The same kernels on the
+// same positions, so the same results: only when the forces are computed moves.  Off
+// with the monitor (it reads the forces at the end of every step) and with per-kernel
+// timing.
+bool contact_deferred(const mf_ctx* c) {
+	return c->contact_on && c->contact_overlap && c->cfg.method == MF_METHOD_TL && c->mixed && !c->mon_cap &&
+	       !c->timing.on;
+}
+
+// Runs a pending contact query now (before anything reads the forces or replaces the
+// positions it belongs to).
+mf_status contact_flush(mf_ctx* c) {
+	if (!c->contact_pending) return MF_OK;
+	c->contact_pending = false;
+	CK(cudaSetDevice(c->cfg.device));
+	return contact_run(c, c->stream);
 }
 
 }  // namespace
@@ -2116,8 +2161,13 @@ mf_ctx::~mf_ctx() {
 	if (io_host) cudaFreeHost(io_host);
 	io_dev.free();
 	if (stream) cudaStreamSynchronize(stream);
-	if (graph_exec) cudaGraphExecDestroy(graph_exec);
-	if (graph) cudaGraphDestroy(graph);
+	for (int k = 0; k < 2; k++) {
+		if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
+		if (graph[k]) cudaGraphDestroy(graph[k]);
+	}
+	if (side) cudaStreamDestroy(side);
+	if (ev_fork) cudaEventDestroy(ev_fork);
+	if (ev_join) cudaEventDestroy(ev_join);
 	work.free();
 	DevBuf<double>* d[] = {&m, &h, &qw0, &fcx, &fcy, &X, &Y};
 	for (auto* p : d) p->free();
@@ -2388,12 +2438,16 @@ namespace {
 mf_status one_step(mf_ctx* c) {
 	const bool tl_lists =
 	    c->cfg.method == MF_METHOD_TL || c->cfg.method == MF_METHOD_COROT || c->cfg.method == MF_METHOD_POTENTIAL;
-	mf_status st = c->cfg.method == MF_METHOD_UL        ? ul_step(c)
-	               : tl_lists                            ? tl_step_all(c)
-	               : c->cfg.method == MF_METHOD_UL_WEAK ? uw_step(c)
-	                                                     : weak_step(c);
+	const bool deferred = contact_deferred(c);
+	mf_status st = deferred ? MF_OK : contact_flush(c);
 	if (st != MF_OK) return st;
-	if (c->contact_on) st = contact_run(c);
+	st = c->cfg.method == MF_METHOD_UL        ? ul_step(c)
+	     : tl_lists                            ? tl_step_all(c, deferred && c->contact_pending)
+	     : c->cfg.method == MF_METHOD_UL_WEAK ? uw_step(c)
+	                                           : weak_step(c);
+	if (st != MF_OK) return st;
+	if (deferred) c->contact_pending = true;  // this step's query runs with the next step
+	else if (c->contact_on) st = contact_run(c, c->stream);
 	if (st == MF_OK && c->mon_cap) {
 		uint32_t nb = (uint32_t)c->bodies.size();
 		bool eos = (c->flags & abit(MF_MATERIAL_EOS)) != 0;
@@ -2410,30 +2464,36 @@ mf_status one_step(mf_ctx* c) {
 }
 
 void drop_graph(mf_ctx* c) {
-	if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-	if (c->graph) cudaGraphDestroy(c->graph);
-	c->graph_exec = nullptr;
-	c->graph = nullptr;
+	for (int k = 0; k < 2; k++) {
+		if (c->graph_exec[k]) cudaGraphExecDestroy(c->graph_exec[k]);
+		if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
+		c->graph_exec[k] = nullptr;
+		c->graph[k] = nullptr;
+	}
 }
 
 // Capture one step on the context's stream and instantiate it for replay.
-mf_status capture_step(mf_ctx* c) {
-	drop_graph(c);
+// Capture one step on the context's stream and instantiate it for replay; w = 1: the
+// step that starts with the pending contact query.
+mf_status capture_step(mf_ctx* c, int w) {
 	mf_status pst = tl_prepack(c);
 	if (pst != MF_OK) return pst;
+	const bool pending = c->contact_pending;
+	c->contact_pending = w == 1;
 	uint64_t l0 = c->launches;
 	CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
 	mf_status st = one_step(c);
 	cudaGraph_t g = nullptr;
 	cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+	c->contact_pending = pending;
 	if (st != MF_OK) {
 		if (g) cudaGraphDestroy(g);
 		return st;
 	}
 	if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
-	c->graph = g;
-	CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
-	c->graph_launches = c->launches - l0;
+	c->graph[w] = g;
+	CK(cudaGraphInstantiate(&c->graph_exec[w], g, 0));
+	c->graph_launches[w] = c->launches - l0;
 	c->launches = l0;
 	return MF_OK;
 }
@@ -2449,14 +2509,17 @@ MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
 	if (st != MF_OK) return st;
 	CK(cudaSetDevice(c->cfg.device));
 	bool use_graph = c->cfg.graph && !c->timing.on;
-	if (use_graph && !c->graph_exec && nsteps > 0) {
-		st = capture_step(c);
-		if (st != MF_OK) return st;
-	}
+	const bool deferred = contact_deferred(c);
+	if (use_graph && c->graph_deferred != deferred) drop_graph(c);  // captured for the other contact order
+	c->graph_deferred = deferred;
 	for (int32_t k = 0; k < nsteps; k++) {
 		if (use_graph) {
-			CK(cudaGraphLaunch(c->graph_exec, c->stream));
-			c->launches += c->graph_launches;
+			if (!deferred && (st = contact_flush(c)) != MF_OK) return st;
+			const int w = deferred && c->contact_pending ? 1 : 0;
+			if (!c->graph_exec[w] && (st = capture_step(c, w)) != MF_OK) return st;
+			CK(cudaGraphLaunch(c->graph_exec[w], c->stream));
+			c->launches += c->graph_launches[w];
+			if (deferred) c->contact_pending = true;
 		} else {
 			st = one_step(c);
 			if (st != MF_OK) return st;
@@ -2479,6 +2542,8 @@ MF_API mf_status mf_synchronize(mf_ctx* c) {
 MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
 	if (!c || !out) return MF_ERR_ARG;
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	mf_status fst = contact_flush(c);
+	if (fst != MF_OK) return fst;
 	const HostBody& b = c->bodies[body];
 	if (!c->ready) {
 		double* o[10] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy, out->fcx, out->fcy};
@@ -2512,6 +2577,8 @@ MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
 MF_API mf_status mf_set_state(mf_ctx* c, int32_t body, const mf_particles* p) {
 	if (!c || !p) return MF_ERR_ARG;
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "bad body id %d", body);
+	mf_status fst = contact_flush(c);  // the pending query belongs to the positions being replaced
+	if (fst != MF_OK) return fst;
 	HostBody& b = c->bodies[body];
 	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
 	const int fld[8] = {0, 1, 8, 9, 5, 10, 11, 12};
@@ -2581,6 +2648,8 @@ StateIO state_io(mf_ctx* c, bool stage_copy) {
 
 MF_API mf_status mf_get_state_all(mf_ctx* c, const mf_state* out) {
 	if (!c || !out) return MF_ERR_ARG;
+	mf_status fst = contact_flush(c);
+	if (fst != MF_OK) return fst;
 	if (!c->ready) {
 		for (int32_t b = 0; b < (int32_t)c->bodies.size(); b++) {
 			const uint32_t o = c->bodies[b].off;
@@ -2631,6 +2700,8 @@ MF_API mf_status mf_get_state_all(mf_ctx* c, const mf_state* out) {
 
 MF_API mf_status mf_set_state_all(mf_ctx* c, const mf_particles* p) {
 	if (!c || !p) return MF_ERR_ARG;
+	mf_status fst = contact_flush(c);
+	if (fst != MF_OK) return fst;
 	if (!c->ready) {
 		for (int32_t b = 0; b < (int32_t)c->bodies.size(); b++) {
 			const uint32_t o = c->bodies[b].off;
@@ -2710,6 +2781,7 @@ MF_API mf_status mf_get_state_all_async(mf_ctx* c, const mf_state* out) {
 	if (!c || !out) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if ((st = contact_flush(c)) != MF_OK) return st;
 	if (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK)
 		return fail(c, MF_ERR_PIPELINE, "the asynchronous transfers cover the strong forms");
 	CK(cudaSetDevice(c->cfg.device));
@@ -2744,6 +2816,7 @@ MF_API mf_status mf_set_state_all_async(mf_ctx* c, const mf_particles* p) {
 	if (!c || !p) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if ((st = contact_flush(c)) != MF_OK) return st;
 	if (c->cfg.method == MF_METHOD_TL_WEAK || c->cfg.method == MF_METHOD_UL_WEAK)
 		return fail(c, MF_ERR_PIPELINE, "the asynchronous transfers cover the strong forms");
 	CK(cudaSetDevice(c->cfg.device));
@@ -2777,6 +2850,7 @@ MF_API mf_status mf_get_stress(mf_ctx* c, int32_t body, double* Pxx, double* Pxy
 	if (!c || !Pxx || !Pxy || !Pyx || !Pyy) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if ((st = contact_flush(c)) != MF_OK) return st;
 	if (body < 0 || body >= (int32_t)c->bodies.size()) return fail(c, MF_ERR_ARG, "no body %d", body);
 	const HostBody& b = c->bodies[body];
 	if (c->cfg.method == MF_METHOD_UL) {
@@ -3016,6 +3090,7 @@ mf_status snapshot_restore(mf_ctx* c, Snapshot& s) {
 	for (size_t i = 0; i < s.bufs.size(); i++)
 		CK(cudaMemcpyAsync(s.src[i].first, s.bufs[i].p, s.src[i].second, cudaMemcpyDeviceToDevice, c->stream));
 	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the restored state
+	c->contact_pending = false;  // the snapshot holds the forces of its positions
 	mf_status pst = tl_prepack(c);
 	if (pst != MF_OK) return pst;
 	for (size_t b = 0; b < c->bodies.size(); b++) c->bodies[b].time = s.times[b];
@@ -3055,6 +3130,7 @@ MF_API mf_status mf_autotune(mf_ctx* c, int32_t trial_steps, char* report, uint3
 	if (!c || trial_steps < 1) return MF_ERR_ARG;
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if ((st = contact_flush(c)) != MF_OK) return st;
 	if (c->cfg.method == MF_METHOD_UL_WEAK) {  // fixed launch shapes: nothing to try
 		if (report && report_len) snprintf(report, report_len, "fixed launch shapes");
 		return MF_OK;
@@ -3185,6 +3261,14 @@ MF_API mf_status mf_set_option(mf_ctx* c, const char* key, int64_t value) {
 		drop_graph(c);
 		return MF_OK;
 	}
+	if (!strcmp(key, "contact_overlap")) {
+		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "contact_overlap must be 0 or 1");
+		mf_status fst = contact_flush(c);
+		if (fst != MF_OK) return fst;
+		c->contact_overlap = value != 0;
+		drop_graph(c);
+		return MF_OK;
+	}
 	if (!strcmp(key, "tl_runs")) {
 		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "tl_runs must be 0 or 1");
 		c->tune.tl_runs = (uint32_t)value;
@@ -3202,6 +3286,10 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	}
 	if (!strcmp(key, "ul_split")) {
 		*value = c->tune.ul_split;
+		return MF_OK;
+	}
+	if (!strcmp(key, "contact_overlap")) {
+		*value = c->contact_overlap ? 1 : 0;
 		return MF_OK;
 	}
 	if (!strcmp(key, "weak_gp_entries")) {
@@ -3421,6 +3509,7 @@ MF_API mf_status mf_dump_async(mf_ctx* c, const char* path, int32_t kind) {
 		return fail(c, MF_ERR_STATE, "checkpoints cover updated- and total-Lagrangian bodies (not the weak form's Gauss points)");
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
+	if ((st = contact_flush(c)) != MF_OK) return st;
 	if ((st = io_join(c)) != MF_OK) return st;  // one dump in flight at a time
 	CK(cudaSetDevice(c->cfg.device));
 	const uint32_t n = c->n_total;
@@ -3503,6 +3592,7 @@ MF_API mf_status mf_checkpoint_load(mf_ctx* c, const char* path) {
 	mf_status st = finalize(c);
 	if (st != MF_OK) return st;
 	if ((st = io_join(c)) != MF_OK) return st;
+	c->contact_pending = false;  // the checkpoint brings the forces of its positions
 	FILE* fp = fopen(path, "rb");
 	if (!fp) return fail(c, MF_ERR_ARG, "cannot open %s", path);
 	char magic[8];

@@ -245,6 +245,39 @@ def test_run_walk_matches_streamed_weights(case, lib):
         assert e[f] <= 1e-5, (f, e[f])
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_contact_overlap_is_bitwise(graph, lib):
+    """Mixed TL with contact: the contact query of the positions a step ends with runs at
+    the start of the next step beside stage 0's pass A (option contact_overlap, the
+    default) -- the same kernels on the same positions, so 560 steps through the impact
+    (penetration forces from step ~410, by the oracle) give the state and the contact
+    forces bit for bit as the query at the end of every step; a read of the state
+    between steps, a state round trip and a monitor switched on midway see the current
+    forces."""
+    import mfree_iwf_gb300 as M
+    sc = S.c2_rings_tl(dx=4e-4)
+    fields = ("x", "y", "vx", "vy", "rho", "Sxx", "Sxy", "Syy", "fcx", "fcy")
+    out = {}
+    for ov in (1, 0):
+        sim = M.from_scenario(sc, precision="mixed", graph=graph)
+        sim.set_option("contact_overlap", ov)
+        assert sim.get_option("contact_overlap") == ov
+        sim.step(460)
+        mid = [sim.get_state(b, fields) for b in range(2)]
+        for b in range(2):  # a round trip through the host
+            sim.set_state(b, {f: mid[b][f] for f in fields[:8]})
+        sim.step(60)
+        sim.set_monitor(4)
+        sim.step(40)
+        out[ov] = (mid, [sim.get_state(b, fields) for b in range(2)])
+        sim.close()
+    assert max(np.abs(out[0][0][b]["fcx"]).max() for b in range(2)) > 0  # in contact
+    for k in range(2):
+        for b in range(2):
+            for f in fields:
+                assert np.array_equal(out[1][k][b][f], out[0][k][b][f]), (k, b, f)
+
+
 @pytest.mark.parametrize("split", [4, 8])
 def test_ul_split_rows_match_one_thread_per_row(split, lib):
     """The mixed UL pair pass with 4 or 8 threads per row adds the same pair terms in
