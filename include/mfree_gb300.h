@@ -293,6 +293,10 @@ MF_API mf_status mf_get_monitor(mf_ctx* ctx, float* out, uint32_t* rows);
  *   "ul_split"        1 (default) / 4 / 8: threads per row of the mixed UL pair pass
  *                     (plain grid; partial sums added across the row's threads, so the
  *                     pair sums change order); mf_autotune tries all three
+ *   "async_steps"     0 (default) / 1: mf_step queues the steps and returns without
+ *                     reading the device status word (no host synchronization per
+ *                     call); errors -- and, with "mask_failed", failed bodies -- are
+ *                     reported by the next mf_synchronize instead
  *   "contact_overlap" 1 (default) / 0: mixed total-Lagrangian bodies with contact run
  *                     the contact query of the positions a step ends with at the start
  *                     of the next step, beside stage 0's pass A on a second stream (the

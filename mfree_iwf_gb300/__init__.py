@@ -319,7 +319,12 @@ class Simulation:
         return out
 
     def synchronize(self) -> None:
-        self._check(self._lib.mf_synchronize(self._h), "mf_synchronize")
+        """Wait for the queued work; with the option "async_steps" this is where the steps'
+        errors surface (BodyFailed for bodies failed under "mask_failed")."""
+        st = self._lib.mf_synchronize(self._h)
+        if st == ERR_BODY_FAILED:
+            raise BodyFailed(st, self._lib.mf_last_error(self._h).decode(), self.failed())
+        self._check(st, "mf_synchronize")
 
     # -- state
     def num_particles(self, body: int) -> int:

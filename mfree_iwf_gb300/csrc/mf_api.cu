@@ -306,6 +306,7 @@ struct mf_ctx {
 	// host->device copy stream, FP64 staging of all fields, one event per field
 	cudaStream_t xs_d2h = nullptr, xs_h2d = nullptr;
 	cudaEvent_t xe_main = nullptr, xe_h2d = nullptr, xe_d2h[10] = {};
+	cudaEvent_t xe_conv[10] = {}, xe_in[8] = {};  // per field: converted into the staging / copied in
 	bool xe_pending[10] = {};  // a get of field q was queued since the last synchronize
 	DevBuf<double> x_out, x_in;
 	cudaEvent_t io_ready = nullptr;
@@ -333,6 +334,7 @@ struct mf_ctx {
 	// mixed TL: the contact query of the positions a step ends with runs at the start of
 	// the next step, beside stage 0's pass A on a side stream (contact_overlap, default on)
 	bool contact_overlap = true, contact_pending = false;
+	bool async_steps = false;  // mf_step queues only; the status is read at the next synchronization
 	cudaStream_t side = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	DevBuf<uint32_t> bnd_rows, bnd_start, bnd_len, tile_first, tile_end, slave_rows, slave_master, m_tile_off, m_tile_n;
@@ -2152,6 +2154,10 @@ mf_ctx::~mf_ctx() {
 		}
 	for (cudaEvent_t e : {xe_main, xe_h2d})
 		if (e) cudaEventDestroy(e);
+	for (cudaEvent_t e : xe_conv)
+		if (e) cudaEventDestroy(e);
+	for (cudaEvent_t e : xe_in)
+		if (e) cudaEventDestroy(e);
 	for (cudaEvent_t e : xe_d2h)
 		if (e) cudaEventDestroy(e);
 	x_out.free();
@@ -2526,6 +2532,7 @@ MF_API mf_status mf_step(mf_ctx* c, int32_t nsteps) {
 		}
 		for (auto& b : c->bodies) b.time += b.dt;  // rk4.h:107 (each body's own clock)
 	}
+	if (c->async_steps) return MF_OK;  // mf_synchronize reads the status
 	if ((st = check_status(c)) != MF_OK) return st;
 	return failed_status(c);
 }
@@ -2536,7 +2543,8 @@ MF_API mf_status mf_synchronize(mf_ctx* c) {
 	for (cudaStream_t xs : {c->xs_d2h, c->xs_h2d})
 		if (xs) CK(cudaStreamSynchronize(xs));
 	std::fill(c->xe_pending, c->xe_pending + 10, false);
-	return check_status(c);
+	mf_status st = check_status(c);
+	return st != MF_OK || !c->async_steps ? st : failed_status(c);  // (synchronous steps report failures themselves)
 }
 
 MF_API mf_status mf_get_state(mf_ctx* c, int32_t body, const mf_state* out) {
@@ -2766,6 +2774,8 @@ mf_status xfer_setup(mf_ctx* c) {
 	CK(cudaEventCreateWithFlags(&c->xe_main, cudaEventDisableTiming));
 	CK(cudaEventCreateWithFlags(&c->xe_h2d, cudaEventDisableTiming));
 	for (auto& e : c->xe_d2h) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+	for (auto& e : c->xe_conv) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+	for (auto& e : c->xe_in) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 	CK(c->x_out.alloc(10 * (size_t)c->n_total));
 	CK(c->x_in.alloc(8 * (size_t)c->n_total));
 	return MF_OK;
@@ -2788,16 +2798,19 @@ MF_API mf_status mf_get_state_all_async(mf_ctx* c, const mf_state* out) {
 	if ((st = xfer_setup(c)) != MF_OK) return st;
 	const uint32_t n = c->n_total;
 	double* o[10] = {out->x, out->y, out->vx, out->vy, out->rho, out->Sxx, out->Sxy, out->Syy, out->fcx, out->fcy};
-	StateIO io = state_io(c, false);
-	for (int q = 0; q < 10; q++) io.dst[q] = o[q] ? c->x_out.p + (size_t)q * n : nullptr;
-	// the staging is rewritten only once the previous get's copies have left it
-	CK(cudaStreamWaitEvent(c->stream, c->xe_d2h[9], 0));
-	if (n) k_get_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
-	CK(cudaGetLastError());
-	CK(cudaEventRecord(c->xe_main, c->stream));
-	CK(cudaStreamWaitEvent(c->xs_d2h, c->xe_main, 0));
+	// field by field: each field's staging is rewritten once the previous get's copy of
+	// it has left, converted by its own small kernel, and sent at once -- the copies of
+	// the first fields run while the later ones convert
+	const StateIO io = state_io(c, false);
 	for (int q = 0; q < 10; q++) {
 		if (o[q]) {
+			StateIO one = io;
+			for (int r = 0; r < 10; r++) one.dst[r] = r == q ? c->x_out.p + (size_t)q * n : nullptr;
+			CK(cudaStreamWaitEvent(c->stream, c->xe_d2h[q], 0));
+			if (n) k_get_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, one, c->body_of.p, c->params.p);
+			CK(cudaGetLastError());
+			CK(cudaEventRecord(c->xe_conv[q], c->stream));
+			CK(cudaStreamWaitEvent(c->xs_d2h, c->xe_conv[q], 0));
 			CK(cudaMemcpyAsync(o[q], c->x_out.p + (size_t)q * n, (size_t)n * 8, cudaMemcpyDeviceToHost, c->xs_d2h));
 			c->xe_pending[q] = true;
 		}
@@ -2823,20 +2836,44 @@ MF_API mf_status mf_set_state_all_async(mf_ctx* c, const mf_particles* p) {
 	if ((st = xfer_setup(c)) != MF_OK) return st;
 	const uint32_t n = c->n_total;
 	const double* src[8] = {p->x, p->y, p->vx, p->vy, p->rho, p->Sxx, p->Sxy, p->Syy};
-	// the staging is rewritten only after the previous set's kernel has read it
+	// the staging is rewritten only after the previous set's kernels have read it; then
+	// field by field: copied in, and converted into the state by its own small kernel as
+	// soon as it has arrived (the later fields' copies run meanwhile)
 	CK(cudaEventRecord(c->xe_main, c->stream));
 	CK(cudaStreamWaitEvent(c->xs_h2d, c->xe_main, 0));
+	const StateIO io = state_io(c, c->cfg.method != MF_METHOD_UL);  // TL stage 0 starts from its own copy (set 2)
+	// mixed TL: the stage-0 records packed in parts as their fields land (positions after
+	// y, velocities after vy, {h, m, rho, c} after rho), off the path to the step
+	const bool parts = c->cfg.method == MF_METHOD_TL && c->mixed && !c->n_bc && src[0] && src[1] && src[2] && src[3] &&
+	                   src[4];
+	TLArgs ta{};
+	if (parts) {
+		ta = tl_args(c);
+		ta.stage = 0;
+		ta.recB = c->recB.p;
+	}
 	for (int q = 0; q < 8; q++) {
 		if (!src[q]) continue;
 		if (c->xe_pending[q]) CK(cudaStreamWaitEvent(c->xs_h2d, c->xe_d2h[q], 0));
 		CK(cudaMemcpyAsync(c->x_in.p + (size_t)q * n, src[q], (size_t)n * 8, cudaMemcpyHostToDevice, c->xs_h2d));
+		CK(cudaEventRecord(c->xe_in[q], c->xs_h2d));
+		CK(cudaStreamWaitEvent(c->stream, c->xe_in[q], 0));
+		StateIO one = io;
+		for (int r = 0; r < 8; r++) one.src[r] = r == q ? c->x_in.p + (size_t)q * n : nullptr;
+		if (n) k_set_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, one, c->body_of.p, c->params.p);
+		CK(cudaGetLastError());
+		const int part = q == 1 ? 6 : q == 3 ? 7 : q == 4 ? 8 : 0;
+		if (parts && part) {
+			cudaError_t e = tl_launch(c, ta, part);
+			if (e != cudaSuccess) return cuda_fail(c, e, "tl pack");
+			c->launches++;
+		}
 	}
 	CK(cudaEventRecord(c->xe_h2d, c->xs_h2d));
-	CK(cudaStreamWaitEvent(c->stream, c->xe_h2d, 0));
-	StateIO io = state_io(c, c->cfg.method != MF_METHOD_UL);  // TL stage 0 starts from its own copy (set 2)
-	for (int q = 0; q < 8; q++) io.src[q] = src[q] ? c->x_in.p + (size_t)q * n : nullptr;
-	if (n) k_set_state_io<<<(n + 255) / 256, 256, 0, c->stream>>>(n, io, c->body_of.p, c->params.p);
-	CK(cudaGetLastError());
+	if (parts) {
+		c->tl_recs_valid = true;
+		return MF_OK;
+	}
 	c->tl_recs_valid = false;  // mixed TL: re-pack the records from the new state
 	return tl_prepack(c);
 }
@@ -3261,6 +3298,11 @@ MF_API mf_status mf_set_option(mf_ctx* c, const char* key, int64_t value) {
 		drop_graph(c);
 		return MF_OK;
 	}
+	if (!strcmp(key, "async_steps")) {
+		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "async_steps must be 0 or 1");
+		c->async_steps = value != 0;
+		return MF_OK;
+	}
 	if (!strcmp(key, "contact_overlap")) {
 		if (value != 0 && value != 1) return fail(c, MF_ERR_ARG, "contact_overlap must be 0 or 1");
 		mf_status fst = contact_flush(c);
@@ -3290,6 +3332,10 @@ MF_API mf_status mf_get_option(mf_ctx* c, const char* key, int64_t* value) {
 	}
 	if (!strcmp(key, "contact_overlap")) {
 		*value = c->contact_overlap ? 1 : 0;
+		return MF_OK;
+	}
+	if (!strcmp(key, "async_steps")) {
+		*value = c->async_steps ? 1 : 0;
 		return MF_OK;
 	}
 	if (!strcmp(key, "weak_gp_entries")) {

@@ -417,6 +417,31 @@ __global__ void k_tl_pack(TLArgs a) {
 	tl_pack_row(a, i, a.params[a.body_of[i]], s.x[i], s.y[i], s.vx[i], s.vy[i], s.rho_f[i], a.recB);
 }
 
+// The same records in three parts, each as soon as its fields are in the state (a state
+// arriving field by field from the host): 0 = the displacement record and the positions
+// (x, y), 1 = the velocities, 2 = {h, m, rho, c} (rho).  Same values as k_tl_pack.
+__global__ void k_tl_pack_part(TLArgs a, int part) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.n_total) return;
+	const mfk_host::StateSoA& s = a.st;
+	float4* r = (float4*)a.recB;
+	const size_t n = a.n_total;
+	if (part == 0) {
+		const double x = s.x[i], y = s.y[i];
+		FF ux = ff_split_bits(x - a.X[i]), uy = ff_split_bits(y - a.Y[i]);
+		((float4*)a.recA)[i] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+		FF fx = ff_split_bits(x), fy = ff_split_bits(y);
+		r[RB_X * n + i] = make_float4(fx.hi, fx.lo, fy.hi, fy.lo);
+	} else if (part == 1) {
+		FF fvx = ff_split_bits(s.vx[i]), fvy = ff_split_bits(s.vy[i]);
+		r[RB_V * n + i] = make_float4(fvx.hi, fvx.lo, fvy.hi, fvy.lo);
+	} else {
+		const BodyParams& pr = a.params[a.body_of[i]];
+		float rho = s.rho_f[i] + pr.frho0;
+		r[RB_H * n + i] = make_float4(((const float*)a.h32)[i], ((const float*)a.m32)[i], rho, sqrtf(pr.fK / rho));
+	}
+}
+
 __device__ __forceinline__ float ffd(float ahi, float alo, float bhi, float blo) { return (ahi - bhi) + (alo - blo); }
 
 // v_ij . x_ij of a pair, FP32.  The FP32 pair passes (plain and halo tiles) share this
@@ -1021,7 +1046,8 @@ cudaError_t tl_tile_attrs(uint32_t halo_max, uint32_t ent_max) {
 
 cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 	// part 0: BCs on the stage state, 1: pack (mixed), 2: pass A, 3: pass B,
-	// 4: BCs on the particles after the combine, 5: advance the body clocks
+	// 4: BCs on the particles after the combine, 5: advance the body clocks,
+	// 6-8: pack one part of the records (mixed)
 	switch (part) {
 	case 0:
 		if (a.n_bc) k_tl_bc<<<grid1(a.n_bc, 128), 128, 0, s>>>(a, 0);
@@ -1054,6 +1080,11 @@ cudaError_t tl_stage(const TLArgs& a, bool mixed, int part, cudaStream_t s) {
 		break;
 	case 5:
 		k_advance_time<<<grid1(a.n_bodies, 128), 128, 0, s>>>(a.n_bodies, const_cast<BodyParams*>(a.params));
+		break;
+	case 6:
+	case 7:
+	case 8:  // the records' positions, velocities, {h, m, rho, c} (mixed)
+		if (mixed) k_tl_pack_part<<<grid1(a.n_total, 256), 256, 0, s>>>(a, part - 6);
 		break;
 	}
 	return cudaGetLastError();

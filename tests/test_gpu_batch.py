@@ -151,6 +151,30 @@ def test_failed_instance_is_masked(lib, precision):
             assert np.array_equal(alone[f], got[k][f]), (k, f)
 
 
+@pytest.mark.parametrize("masked", [False, True])
+def test_async_steps_report_at_synchronize(lib, masked):
+    """Option async_steps: mf_step queues the steps and returns at once; a NaN planted
+    from the host surfaces at the next mf_synchronize -- as a non-finite state, or with
+    mask_failed as the failed body -- instead of at the step."""
+    import mfree_iwf_gb300 as M
+    ens = small_ensemble()
+    sim = M.from_scenario(ens, precision="mixed")
+    if masked:
+        sim.set_option("mask_failed", 1)
+    sim.set_option("async_steps", 1)
+    assert sim.get_option("async_steps") == 1
+    sim.step(3)
+    sim.synchronize()
+    st = sim.get_state(1, FIELDS)
+    st["vx"][len(st["vx"]) // 2] = np.nan
+    sim.set_state(1, st)
+    sim.step(5)  # no error here: nothing read the status yet
+    with pytest.raises(M.MfError) as ei:
+        sim.synchronize()
+    assert isinstance(ei.value, M.BodyFailed) == masked, ei.value
+    sim.close()
+
+
 def test_without_masking_a_failure_fails_the_step(lib):
     """Without the option a NaN in one instance fails mf_step as a whole (the
     reference's behaviour is an abort)."""
