@@ -2071,10 +2071,32 @@ mf_status contact_setup(mf_ctx* c) {
 			for (uint32_t i = 0; i < nb; i++)
 				if (i != j && !c->bodies[i].hull.empty() && c->bodies[i].group == c->bodies[j].group) master = (int)i;
 			if (master < 0) continue;
-			for (uint32_t r = 0; r < c->bodies[j].n; r++) {
-				srows.push_back(c->bodies[j].off + r);
+			// the body's queries along a Morton curve of the set-up positions (cells of one
+			// smoothing length): a warp's 32 queries form a compact patch, so the master
+			// tiles that can hold their nearest points are few (a column of 32 rows would
+			// span 32 lattice spacings); each query writes only its own row's force, so the
+			// order changes no result
+			const HostBody& S = c->bodies[j];
+			std::vector<std::pair<uint32_t, uint32_t>> order(S.n);
+			double x0 = 0., y0 = 0., hcell = 1.;
+			if (S.n) {
+				x0 = *std::min_element(S.in[0].begin(), S.in[0].end());
+				y0 = *std::min_element(S.in[1].begin(), S.in[1].end());
+				hcell = S.in[6][0] > 0. ? S.in[6][0] : 1.;
+			}
+			for (uint32_t r = 0; r < S.n; r++) {
+				const double fx = std::floor((S.in[0][r] - x0) / hcell), fy = std::floor((S.in[1][r] - y0) / hcell);
+				const uint32_t ix = (uint32_t)std::min(std::max(fx, 0.), 65535.), iy = (uint32_t)std::min(std::max(fy, 0.), 65535.);
+				order[r] = {morton_spread(ix) | (morton_spread(iy) << 1), r};
+			}
+			std::stable_sort(order.begin(), order.end(),
+			                 [](const std::pair<uint32_t, uint32_t>& a, const std::pair<uint32_t, uint32_t>& b) {
+				                 return a.first < b.first;
+			                 });
+			for (const auto& o : order) {
+				srows.push_back(S.off + o.second);
 				smaster.push_back((uint32_t)master);
-				sdt.push_back(c->bodies[j].dt);
+				sdt.push_back(S.dt);
 			}
 		}
 	}
