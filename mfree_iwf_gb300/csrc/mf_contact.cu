@@ -149,8 +149,15 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
 			x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
 			y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
 		}
+		// an upper bound of every query's nearest squared distance: the farthest a query of
+		// the box can be from some tile's first point (a tile box's farthest corner would
+		// add up to a tile's length, and with it every tile within that much more)
 		float ubmin = 3.4e38f;
-		for (uint32_t t = lane; t < nt; t += 32) ubmin = fminf(ubmin, box_ub(a.tile_bb[t0 + t], x0, y0, x1, y1));
+		for (uint32_t t = lane; t < nt; t += 32) {
+			const float4 p = a.bnd_ff[a.tile_first[t0 + t]];  // hi parts: within TILE_MARGIN of the point
+			const float4 pb = make_float4(p.x - TILE_MARGIN, p.z - TILE_MARGIN, p.x + TILE_MARGIN, p.z + TILE_MARGIN);
+			ubmin = fminf(ubmin, box_ub(pb, x0, y0, x1, y1));
+		}
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) ubmin = fminf(ubmin, __shfl_xor_sync(FULL, ubmin, o));
 		float cut = ubmin * (1.f + 1e-5f);
