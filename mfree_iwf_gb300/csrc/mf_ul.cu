@@ -732,94 +732,125 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	float av_x = 0.f, av_y = 0.f, xs_x = 0.f, xs_y = 0.f;
 	float god_rho = 0.f, god_vx = 0.f, god_vy = 0.f;
 	const float two_rhoi = 2.f / ri.rho;
+	// the pair terms of candidate kj within reach (xij, yij: x_i - x_j; r2 = |x_i - x_j|^2)
+	auto pair = [&](uint32_t kj, float4 head, float xij, float yij, float r2) {
+		const Rec32 rj = load_rec_tail(rec + kj, head);
+		KR32 w = cubic_spline_f(xij, yij, h1, fac);
+		if (flags & A_STRESS_MGHN) {
+			float Rxx = 0.f, Rxy = 0.f, Ryy = 0.f;
+			if (wdp1 > 0.f) {
+				float fab = w.w * wdp1;
+				if (exp4) {
+					float f2 = fab * fab;
+					fab = f2 * f2;
+				} else {
+					fab = powf(fab, corr_exp);
+				}
+				Rxx = fab * (ri.Rxx + rj.Rxx);
+				Rxy = fab * (ri.Rxy + rj.Rxy);
+				Ryy = fab * (ri.Ryy + rj.Ryy);
+			}
+			float tsx = rj.m * (ri.sxy * rhoi21 + rj.sxy * rj.rho21 + Rxy);
+			Sxx_x += rj.m * (ri.sxx * rhoi21 + rj.sxx * rj.rho21 + Rxx) * w.w_x;
+			Sxy_y += tsx * w.w_y;
+			Sxy_x += tsx * w.w_x;
+			Syy_y += rj.m * (ri.syy * rhoi21 + rj.syy * rj.rho21 + Ryy) * w.w_y;
+		}
+		float dvx = ff_diff(rj.vx, ri.vx), dvy = ff_diff(rj.vy, ri.vy);
+		if (flags & A_DERIVE_VEL) {
+			float qx = w.w_x * rj.qw, qy = w.w_y * rj.qw;
+			vx_x += dvx * qx;
+			vx_y += dvx * qy;
+			vy_x += dvy * qx;
+			vy_y += dvy * qy;
+		}
+		if (flags & A_ART_VISC) {
+			float vijposij = -(dvx * xij + dvy * yij);
+			if (vijposij < 0.f) {
+				float cij = 0.5f * (ri.c + rj.c);
+				float hij = 0.5f * (hi + rj.h);
+				float rhoij = 0.5f * (ri.rho + rj.rho);
+				float muij = __fdividef(hij * vijposij, r2 + eta2 * hij * hij);
+				float piij = __fdividef(-alpha * cij * muij + beta * muij * muij, rhoij);
+				av_x += -rj.m * piij * w.w_x;
+				av_y += -rj.m * piij * w.w_y;
+			}
+		}
+		if (flags & A_XSPH) {
+			float rhoij = 0.5f * (ri.rho + rj.rho);
+			float f = __fdividef(-xeps * w.w * ri.m, rhoij);
+			xs_x -= f * dvx;
+			xs_y -= f * dvy;
+		}
+		if (GOD && kj != k) {
+			// godunov_continuity / godunov_momentum (godunov.h:86-187) in FP32: velocity
+			// differences from the float-float records, the Riemann state in the form
+			// v_i - u* = (Z_j (v_i - v_j).n + p_i - p_j) / (Z_i + Z_j), Z = rho c;
+			// Rxx holds p, Rxy the stress Syy itself
+			const float mag_r = sqrtf(r2), inv = 1.f / mag_r;
+			const float Zi = ri.rho * ri.c, Zj = rj.rho * rj.c;
+			const float frac = 1.f / (Zi + Zj);
+			if (flags & A_GOD_CONT) {
+				float nx = xij * inv, ny = yij * inv;
+				float dvn = -(dvx * nx + dvy * ny);  // (v_i - v_j).n
+				float vi_us = frac * (Zj * dvn + (ri.Rxx - rj.Rxx));
+				god_rho += 2.f * ri.rho * vi_us * (w.w_x * nx + w.w_y * ny) * rj.qw;
+			}
+			if (flags & A_GOD_MOM) {
+				float rx = -xij, ry = -yij;
+				float Rx = rx * inv, Ry = ry * inv, Sx = ry * inv, Sy = -rx * inv;  // the float frame
+				float siR0 = ri.sxx * Rx + ri.sxy * Ry;
+				float sjR0 = rj.sxx * Rx + rj.sxy * Ry, sjR1 = rj.sxy * Rx + rj.Rxy * Ry;
+				float si0 = Rx * siR0 + Sx * (ri.sxy * Rx + ri.Rxy * Ry);
+				float sj0 = Rx * sjR0 + Sx * sjR1, sj1 = Ry * sjR0 + Sy * sjR1;
+				float dv0 = Rx * dvx + Sx * dvy, dv1 = Ry * dvx + Sy * dvy;  // frame (v_j - v_i)
+				// the second component takes sigma_j twice (godunov.h:116), as the reference does
+				float S0 = frac * (sj0 * Zi + si0 * Zj + Zi * Zj * dv0);
+				float S1 = frac * (sj1 * Zi + sj1 * Zj + Zi * Zj * dv1);
+				float SR0 = Rx * S0 + Ry * S1, SR1 = Sx * S0 + Sy * S1;
+				if (fabsf(rx) > 0.f) god_vx += two_rhoi * __fdividef(w.w_x * mag_r, rx) * SR0 * rj.qw;
+				if (fabsf(ry) > 0.f) god_vy += two_rhoi * __fdividef(w.w_y * mag_r, ry) * SR1 * rj.qw;
+			}
+		}
+	};
+	// candidate offsets and squared distance, one rounding each (the same values in both
+	// walks below)
+	auto offs = [&](float4 head, float& xij, float& yij) {
+		xij = __fadd_rn(__fsub_rn(ri.x.hi, head.x), __fsub_rn(ri.x.lo, head.y));
+		yij = __fadd_rn(__fsub_rn(ri.y.hi, head.z), __fsub_rn(ri.y.lo, head.w));
+		return __fmaf_rn(yij, yij, __fmul_rn(xij, xij));
+	};
 	for (int ni = lo_i; ni < hi_i; ni++) {
 		uint32_t c0 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)lo_j, tot);
 		uint32_t c1 = min(g.cell_off + (uint32_t)ni * g.ny + (uint32_t)hi_j, tot);
 		uint32_t j0 = a.cell_start[c0], j1 = a.cell_start[c1];
-		for (uint32_t kj = j0 + lane; kj < j1; kj += L) {
-			// positions first: most candidates of the stencil lie beyond the reach
-			const float4 head = __ldg(reinterpret_cast<const float4*>(rec + kj));
-			float xij = (ri.x.hi - head.x) + (ri.x.lo - head.y);
-			float yij = (ri.y.hi - head.z) + (ri.y.lo - head.w);
-			float r2 = xij * xij + yij * yij;
-			if (r2 > reach2) continue;
-			const Rec32 rj = load_rec_tail(rec + kj, head);
-			KR32 w = cubic_spline_f(xij, yij, h1, fac);
-			if (flags & A_STRESS_MGHN) {
-				float Rxx = 0.f, Rxy = 0.f, Ryy = 0.f;
-				if (wdp1 > 0.f) {
-					float fab = w.w * wdp1;
-					if (exp4) {
-						float f2 = fab * fab;
-						fab = f2 * f2;
-					} else {
-						fab = powf(fab, corr_exp);
-					}
-					Rxx = fab * (ri.Rxx + rj.Rxx);
-					Rxy = fab * (ri.Rxy + rj.Rxy);
-					Ryy = fab * (ri.Ryy + rj.Ryy);
-				}
-				float tsx = rj.m * (ri.sxy * rhoi21 + rj.sxy * rj.rho21 + Rxy);
-				Sxx_x += rj.m * (ri.sxx * rhoi21 + rj.sxx * rj.rho21 + Rxx) * w.w_x;
-				Sxy_y += tsx * w.w_y;
-				Sxy_x += tsx * w.w_x;
-				Syy_y += rj.m * (ri.syy * rhoi21 + rj.syy * rj.rho21 + Ryy) * w.w_y;
+		if (L == 1 && j1 - j0 <= 32u) {
+			// this stencil column's candidates tested first, into one mask, then the pair
+			// terms of those within reach in ascending order: a warp runs as many pair
+			// evaluations as its lane with the most neighbours in the column, instead of one
+			// for every candidate that some lane accepts (the same pairs in the same order)
+			uint32_t mask = 0u;
+			for (uint32_t kj = j0; kj < j1; kj++) {
+				float xij, yij;
+				const float r2 = offs(__ldg(reinterpret_cast<const float4*>(rec + kj)), xij, yij);
+				if (!(r2 > reach2)) mask |= 1u << (kj - j0);
 			}
-			float dvx = ff_diff(rj.vx, ri.vx), dvy = ff_diff(rj.vy, ri.vy);
-			if (flags & A_DERIVE_VEL) {
-				float qx = w.w_x * rj.qw, qy = w.w_y * rj.qw;
-				vx_x += dvx * qx;
-				vx_y += dvx * qy;
-				vy_x += dvy * qx;
-				vy_y += dvy * qy;
+			while (mask) {
+				const uint32_t kj = j0 + (uint32_t)(__ffs(mask) - 1);
+				mask &= mask - 1u;
+				const float4 head = __ldg(reinterpret_cast<const float4*>(rec + kj));
+				float xij, yij;
+				const float r2 = offs(head, xij, yij);
+				pair(kj, head, xij, yij, r2);
 			}
-			if (flags & A_ART_VISC) {
-				float vijposij = -(dvx * xij + dvy * yij);
-				if (vijposij < 0.f) {
-					float cij = 0.5f * (ri.c + rj.c);
-					float hij = 0.5f * (hi + rj.h);
-					float rhoij = 0.5f * (ri.rho + rj.rho);
-					float muij = __fdividef(hij * vijposij, r2 + eta2 * hij * hij);
-					float piij = __fdividef(-alpha * cij * muij + beta * muij * muij, rhoij);
-					av_x += -rj.m * piij * w.w_x;
-					av_y += -rj.m * piij * w.w_y;
-				}
-			}
-			if (flags & A_XSPH) {
-				float rhoij = 0.5f * (ri.rho + rj.rho);
-				float f = __fdividef(-xeps * w.w * ri.m, rhoij);
-				xs_x -= f * dvx;
-				xs_y -= f * dvy;
-			}
-			if (GOD && kj != k) {
-				// godunov_continuity / godunov_momentum (godunov.h:86-187) in FP32: velocity
-				// differences from the float-float records, the Riemann state in the form
-				// v_i - u* = (Z_j (v_i - v_j).n + p_i - p_j) / (Z_i + Z_j), Z = rho c;
-				// Rxx holds p, Rxy the stress Syy itself
-				const float mag_r = sqrtf(r2), inv = 1.f / mag_r;
-				const float Zi = ri.rho * ri.c, Zj = rj.rho * rj.c;
-				const float frac = 1.f / (Zi + Zj);
-				if (flags & A_GOD_CONT) {
-					float nx = xij * inv, ny = yij * inv;
-					float dvn = -(dvx * nx + dvy * ny);  // (v_i - v_j).n
-					float vi_us = frac * (Zj * dvn + (ri.Rxx - rj.Rxx));
-					god_rho += 2.f * ri.rho * vi_us * (w.w_x * nx + w.w_y * ny) * rj.qw;
-				}
-				if (flags & A_GOD_MOM) {
-					float rx = -xij, ry = -yij;
-					float Rx = rx * inv, Ry = ry * inv, Sx = ry * inv, Sy = -rx * inv;  // the float frame
-					float siR0 = ri.sxx * Rx + ri.sxy * Ry;
-					float sjR0 = rj.sxx * Rx + rj.sxy * Ry, sjR1 = rj.sxy * Rx + rj.Rxy * Ry;
-					float si0 = Rx * siR0 + Sx * (ri.sxy * Rx + ri.Rxy * Ry);
-					float sj0 = Rx * sjR0 + Sx * sjR1, sj1 = Ry * sjR0 + Sy * sjR1;
-					float dv0 = Rx * dvx + Sx * dvy, dv1 = Ry * dvx + Sy * dvy;  // frame (v_j - v_i)
-					// the second component takes sigma_j twice (godunov.h:116), as the reference does
-					float S0 = frac * (sj0 * Zi + si0 * Zj + Zi * Zj * dv0);
-					float S1 = frac * (sj1 * Zi + sj1 * Zj + Zi * Zj * dv1);
-					float SR0 = Rx * S0 + Ry * S1, SR1 = Sx * S0 + Sy * S1;
-					if (fabsf(rx) > 0.f) god_vx += two_rhoi * __fdividef(w.w_x * mag_r, rx) * SR0 * rj.qw;
-					if (fabsf(ry) > 0.f) god_vy += two_rhoi * __fdividef(w.w_y * mag_r, ry) * SR1 * rj.qw;
-				}
+		} else {
+			for (uint32_t kj = j0 + lane; kj < j1; kj += L) {
+				// positions first: most candidates of the stencil lie beyond the reach
+				const float4 head = __ldg(reinterpret_cast<const float4*>(rec + kj));
+				float xij, yij;
+				const float r2 = offs(head, xij, yij);
+				if (r2 > reach2) continue;
+				pair(kj, head, xij, yij, r2);
 			}
 		}
 	}
