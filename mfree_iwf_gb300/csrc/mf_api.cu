@@ -235,6 +235,7 @@ struct mf_ctx {
 	DevBuf<unsigned long long> bbox;
 	DevBuf<uint32_t> total_cells, keys, keys_sorted, perm_in, perm, cell_start, rec_body;
 	DevBuf<unsigned char> rec, sort_tmp;
+	DevBuf<unsigned char> rec2;  // mixed UL: the second record buffer (stages alternate between the two)
 	int sort_bits = 1;
 	uint32_t cell_cap = 0;
 
@@ -467,6 +468,15 @@ ULArgs ul_args(mf_ctx* c, uint32_t stage) {
 	a.cell_start = c->cell_start.p;
 	a.rec = c->rec.p;
 	a.rec_body = c->rec_body.p;
+	if (c->mixed && c->rec2.p && !a.strict_grid) {
+		// the cell order holds for the whole step: stage s reads record buffer s % 2, and
+		// its pair pass (stages 0-2) writes the next stage's records into the other one
+		unsigned char* rb[2] = {c->rec.p, c->rec2.p};
+		a.rec = rb[stage & 1];
+		a.rec_next = rb[(stage + 1) & 1];
+		a.write_recs = stage < 3 ? 1u : 0u;
+		a.skip_gather = stage > 0 ? 1u : 0u;
+	}
 	a.sort_tmp = c->sort_tmp.p;
 	a.sort_tmp_bytes = c->sort_tmp.n;
 	a.sort_bits = c->sort_bits;
@@ -673,6 +683,7 @@ mf_status finalize(mf_ctx* c) {
 		CK(c->cell_start.alloc((size_t)c->cell_cap + 1));
 		CK(c->rec_body.alloc(n));
 		CK(c->rec.alloc((size_t)n * 128));
+		if (c->mixed) CK(c->rec2.alloc((size_t)n * 128));
 		int bits = 1;
 		while (bits < 32 && (1ull << bits) < (uint64_t)c->cell_cap + 1) bits++;
 		c->sort_bits = bits;
@@ -713,7 +724,7 @@ mf_status ul_step(mf_ctx* c) {
 		timing_count(c, slot_pair, c->n_total);
 		timing_end(c, slot_all, c->n_total);
 		if (e != cudaSuccess) return cuda_fail(c, e, "ul_stage");
-		c->launches += (a.strict_grid || s == 0) ? 8 + 4 : 2;
+		c->launches += (a.strict_grid || s == 0) ? 8 + 4 : (a.skip_gather ? 1 : 2);
 	}
 	if (c->n_bc) {  // rk4.h:105: the conditions act on the particles after the combine
 		cudaError_t e = c->strict ? mf_strict::ul_bc(c->n_bc, c->bc_rows.p, c->bc_v.p, c->sd[0][2].p, c->sd[0][3].p, c->stream)
@@ -2204,7 +2215,7 @@ mf_ctx::~mf_ctx() {
 		for (int q = 0; q < 4; q++) sf[k][q].free();
 	}
 	body_of.free(); params.free(); geom.free(); bbox.free(); total_cells.free(); keys.free(); keys_sorted.free();
-	perm_in.free(); perm.free(); cell_start.free(); rec_body.free(); rec.free(); sort_tmp.free();
+	perm_in.free(); perm.free(); cell_start.free(); rec_body.free(); rec.free(); rec2.free(); sort_tmp.free();
 	{
 		DevBuf<uint32_t>* w32s[] = {&gp_body, &g_sl, &g_snbr, &t_sl, &t_snbr, &p_sl, &p_snbr};
 		for (auto* p : w32s) p->free();

@@ -96,6 +96,11 @@ struct ULArgs {
 	// whole step.  When set, a row's error marks its body failed instead, and a failed
 	// body's rows are left out of the grid and the pair pass from then on (frozen).
 	uint32_t* failed;
+	// mixed: the pair pass of stages 0-2 also writes each row's record of the next stage
+	// into rec_next (the cell order holds for the whole step), and the next stage skips
+	// the gather
+	void* rec_next;
+	uint32_t write_recs, skip_gather;
 };
 
 // Neighbour search of the total-Lagrangian set-up (find_neighbors,

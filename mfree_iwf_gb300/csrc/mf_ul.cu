@@ -433,6 +433,27 @@ __global__ void k_gather64(ULArgs a, const BodyParams* __restrict__ P) {
 	a.rec_body[k] = b;
 }
 
+// The record of particle i (body parameters pr) from its stage state, into out.
+__device__ __forceinline__ void put_rec32(const ULArgs& a, const BodyParams& pr, uint32_t i, Rec32* out, double x,
+                                          double y, double vx, double vy, float rho_dev, float Sxx, float Sxy,
+                                          float Syy) {
+	const float rho = rho_dev + pr.frho0;  // the mixed state holds rho - rho0
+	Rec32 r;
+	r.x = ff_split_bits(x); r.y = ff_split_bits(y); r.vx = ff_split_bits(vx); r.vy = ff_split_bits(vy);
+	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
+	per_particle32(a.flags, pr, r.m, rho, rho_dev, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy,
+	               r.c, r.qw, r.rho21);
+	r.sxy = Sxy;
+	if (a.flags & (A_GOD_CONT | A_GOD_MOM)) {  // p from the stored deviation, the stress Syy itself
+		r.Rxx = (a.flags & A_EOS) ? pr.fc0sq * rho_dev : 0.f;
+		r.Rxy = Syy;
+	}
+	const float4* s = reinterpret_cast<const float4*>(&r);
+	float4* d = reinterpret_cast<float4*>(out);
+#pragma unroll
+	for (int q = 0; q < 5; q++) d[q] = s[q];
+}
+
 __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= a.n_total) return;
@@ -442,23 +463,7 @@ __global__ void k_gather32(ULArgs a, const BodyParams* __restrict__ P) {
 	float rho, Sxx, Sxy, Syy;
 	v.load(i, x, y, vx, vy, rho, Sxx, Sxy, Syy);
 	uint32_t b = a.body_of[i];
-	const float rho_dev = rho;  // the mixed state holds rho - rho0
-	rho += P[b].frho0;
-	Rec32 r;
-	r.x = ff_split_bits(x); r.y = ff_split_bits(y); r.vx = ff_split_bits(vx); r.vy = ff_split_bits(vy);
-	r.m = (float)a.m[i]; r.h = (float)a.h[i]; r.rho = rho;
-	per_particle32(a.flags, P[b], r.m, rho, rho_dev, (float)a.qw0[i], Sxx, Sxy, Syy, r.sxx, r.syy, r.Rxx, r.Rxy, r.Ryy,
-	               r.c, r.qw, r.rho21);
-	r.sxy = Sxy;
-	if (a.flags & (A_GOD_CONT | A_GOD_MOM)) {  // p from the stored deviation, the stress Syy itself
-		r.Rxx = (a.flags & A_EOS) ? P[b].fc0sq * rho_dev : 0.f;
-		r.Rxy = Syy;
-	}
-	Rec32* out = reinterpret_cast<Rec32*>(a.rec) + k;
-	const float4* s = reinterpret_cast<const float4*>(&r);
-	float4* d = reinterpret_cast<float4*>(out);
-#pragma unroll
-	for (int q = 0; q < 5; q++) d[q] = s[q];
+	put_rec32(a, P[b], i, reinterpret_cast<Rec32*>(a.rec) + k, x, y, vx, vy, rho, Sxx, Sxy, Syy);
 	a.rec_body[k] = b;
 }
 
@@ -909,14 +914,21 @@ __device__ __forceinline__ void pair32_row(const ULArgs& a, const BodyParams* __
 	float* sq[4] = {a.st.rho_f, a.st.Sxx_f, a.st.Sxy_f, a.st.Syy_f};
 	if (s < 3) {
 		double dts = (s == 2 ? 1.0 : 0.5) * dt;
+		double nv[4];  // the next stage's x, y, vx, vy
+		float nf[4];   // and its rho - rho0, Sxx, Sxy, Syy
 #pragma unroll
 		for (int q = 0; q < 4; q++) {
 			ap[q][i] = (s == 0) ? dq[q] : ap[q][i] + 2 * dq[q];
-			sp[q][i] = bp[q][i] + dq[q] * dts;
+			nv[q] = bp[q][i] + dq[q] * dts;
+			sp[q][i] = nv[q];
 			float dr = d[4 + q];
 			aq[q][i] = (s == 0) ? dr : aq[q][i] + 2.f * dr;
-			sq[q][i] = bq[q][i] + dr * (float)dts;
+			nf[q] = bq[q][i] + dr * (float)dts;
+			sq[q][i] = nf[q];
 		}
+		if (a.write_recs)
+			put_rec32(a, pr, i, reinterpret_cast<Rec32*>(a.rec_next) + k, nv[0], nv[1], nv[2], nv[3], nf[0], nf[1], nf[2],
+			          nf[3]);
 	} else {
 		double w6 = dt * 1. / 6.;
 #pragma unroll
@@ -1045,7 +1057,7 @@ cudaError_t ul_stage(const ULArgs& a, bool mixed, cudaStream_t s) {
 		if (e != cudaSuccess) return e;
 	}
 	if (mixed) {
-		k_gather32<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
+		if (!a.skip_gather) k_gather32<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
 	} else {
 		k_gather64<<<grid1(a.n_total, 256), 256, 0, s>>>(a, a.params);
 	}
