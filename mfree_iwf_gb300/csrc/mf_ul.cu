@@ -118,7 +118,7 @@ __global__ void k_bbox_init(uint32_t nb, unsigned long long* bb) {
 	bb[6 * b + 2] = ord_encode(-1.7976931348623157e308);  // max x
 	bb[6 * b + 3] = ord_encode(-1.7976931348623157e308);  // max y
 	bb[6 * b + 4] = ord_encode(-1.7976931348623157e308);  // h_max
-	bb[6 * b + 5] = ord_encode(0.);                       // max |v| (mixed form)
+	bb[6 * b + 5] = ord_encode(0.);                       // max |v|^2 (mixed form)
 }
 
 // Bounding box and h_max per body (grid.h:83-104).  Rows of a body are contiguous,
@@ -141,7 +141,9 @@ __global__ void k_bbox(uint32_t n, const double* __restrict__ x, const double* _
 		mnx = mxx = ord_encode(x[i]);
 		mny = mxy = ord_encode(y[i]);
 		mh = ord_encode(h[i]);
-		mv = mixed ? ord_encode(sqrt(vx[i] * vx[i] + vy[i] * vy[i])) : ord_encode(0.);
+		// the square of the speed (the square root once per body: a correctly rounded root
+		// is monotonic, so the root of the largest square is the largest root)
+		mv = mixed ? ord_encode(vx[i] * vx[i] + vy[i] * vy[i]) : ord_encode(0.);
 	}
 	uint32_t lane = threadIdx.x & 31;
 	uint32_t b0 = __shfl_sync(0xffffffffu, b, 0);
@@ -202,7 +204,7 @@ __global__ void k_geom(uint32_t nb, const unsigned long long* bb, const BodyPara
 			double lx = bmaxx - bminx, ly = bmaxy - bminy;
 			if (mixed) {
 				// a particle moves at most ~ |v| dt per step; allow twice the fastest speed
-				slack = 2. * ord_decode(bb[6 * b + 5]) * P[b].dt;
+				slack = 2. * sqrt(ord_decode(bb[6 * b + 5])) * P[b].dt;
 				dx = 2. * hmax + 2. * slack;
 				// half-size cells with a 5x5 stencil cover the same reach with ~40 % fewer
 				// candidates than 3x3 cells of the full reach; used while the body's cells
