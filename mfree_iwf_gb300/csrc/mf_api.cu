@@ -306,7 +306,7 @@ struct mf_ctx {
 	// stream-ordered state transfers (mf_*_state_all_async): a device->host and a
 	// host->device copy stream, FP64 staging of all fields, one event per field
 	cudaStream_t xs_d2h = nullptr, xs_h2d = nullptr;
-	cudaEvent_t xe_main = nullptr, xe_h2d = nullptr, xe_d2h[10] = {};
+	cudaEvent_t xe_main = nullptr, xe_d2h[10] = {};
 	cudaEvent_t xe_conv[10] = {}, xe_in[8] = {};  // per field: converted into the staging / copied in
 	bool xe_pending[10] = {};  // a get of field q was queued since the last synchronize
 	DevBuf<double> x_out, x_in;
@@ -2185,8 +2185,7 @@ mf_ctx::~mf_ctx() {
 			cudaStreamSynchronize(xs);
 			cudaStreamDestroy(xs);
 		}
-	for (cudaEvent_t e : {xe_main, xe_h2d})
-		if (e) cudaEventDestroy(e);
+	if (xe_main) cudaEventDestroy(xe_main);
 	for (cudaEvent_t e : xe_conv)
 		if (e) cudaEventDestroy(e);
 	for (cudaEvent_t e : xe_in)
@@ -2805,7 +2804,6 @@ mf_status xfer_setup(mf_ctx* c) {
 	CK(cudaStreamCreateWithFlags(&c->xs_d2h, cudaStreamNonBlocking));
 	CK(cudaStreamCreateWithFlags(&c->xs_h2d, cudaStreamNonBlocking));
 	CK(cudaEventCreateWithFlags(&c->xe_main, cudaEventDisableTiming));
-	CK(cudaEventCreateWithFlags(&c->xe_h2d, cudaEventDisableTiming));
 	for (auto& e : c->xe_d2h) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 	for (auto& e : c->xe_conv) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 	for (auto& e : c->xe_in) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -2902,7 +2900,6 @@ MF_API mf_status mf_set_state_all_async(mf_ctx* c, const mf_particles* p) {
 			c->launches++;
 		}
 	}
-	CK(cudaEventRecord(c->xe_h2d, c->xs_h2d));
 	if (parts) {
 		c->tl_recs_valid = true;
 		return MF_OK;
