@@ -291,6 +291,7 @@ struct mf_ctx {
 	DevBuf<uint8_t> uw_pmask, uw_gmask;
 	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
 	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
+	DevBuf<float> uw_ff, uw_vol;  // mixed form: the stage's float-float positions, FP32 volumes
 	DevBuf<uint32_t> uw_quads;  // element maps (global ll lr tr tl) when a gauss_int replaces the ellipse
 	uint32_t uw_order = 0, uw_nelem = 0;
 
@@ -1875,6 +1876,7 @@ mf_status uw_setup(mf_ctx* c) {
 	CK(c->uw_qwp.alloc(n));
 	CK(cudaMemcpy(c->uw_qwp.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
 	CK(c->uw_ph.alloc(n)); CK(c->uw_qws.alloc(n));
+	if (c->uw_mixed) { CK(c->uw_ff.alloc(4 * (size_t)n)); CK(c->uw_vol.alloc(n)); }
 	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
 	std::vector<uint32_t> goff(ng + 1), gnbr;
 	uint64_t ep, eg;
@@ -1987,16 +1989,24 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 // rk4.h:201), else this evaluation's weights into qw_stage (m / rho when the pipeline
 // updates them, the stored ones otherwise).
 cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refresh_qw) {
+	// the mixed form reads the candidates' positions as float-float pairs
+	const bool mixed = c->uw_mixed && !c->strict;
 	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
 	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qs, double* qd) {
 		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
-		                                     qs, qd, c->d_status, 0, c->stream)
+		                                     qs, qd, nullptr, nullptr, c->d_status, c->stream)
 		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qs,
-		                                   qd, c->d_status, c->uw_mixed ? 1 : 0, c->stream);
+		                                   qd, mixed ? c->uw_ff.p : nullptr, mixed ? c->uw_vol.p : nullptr,
+		                                   c->d_status, c->stream);
 	};
 	const bool riemann = (c->flags & abit(MF_RIEMANN_UPDATE_INTEGRATION_WEIGHTS)) != 0;
 	const double* qs = refresh_qw ? nullptr : (riemann ? nullptr : a.qw_base);
 	double* qd = refresh_qw ? a.qw_base : a.qw_stage;
+	if (mixed) {
+		cudaError_t e = mf_fast::uw_ff(a.n_p, a.rd.x, a.rd.y, a.m, a.rd.rho, c->uw_ff.p, c->uw_vol.p, c->stream);
+		if (e != cudaSuccess) return e;
+		c->launches++;
+	}
 	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc_off, a.pc_nbr, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy, qs, qd);
 	if (e == cudaSuccess && points)
 		e = nbh(a.n_g, a.grd.x, a.grd.y, a.gc_off, a.gc_nbr, c->uw_gh.p, a.gmask, a.gw, a.gwx, a.gwy, nullptr, nullptr);
@@ -2232,7 +2242,7 @@ mf_ctx::~mf_ctx() {
 		DevBuf<uint32_t>* uws[] = {&uw_gbody, &uw_pc_off, &uw_pc_nbr, &uw_gc_off, &uw_gc_nbr, &uw_tp_off, &uw_tp_gp,
 		                           &uw_tp_slot, &uw_bc_of, &uw_quads};
 		for (auto* p : uws) p->free();
-		uw_pmask.free(); uw_gmask.free();
+		uw_pmask.free(); uw_gmask.free(); uw_ff.free(); uw_vol.free();
 		DevBuf<double>* uwd[] = {&uw_pw, &uw_pwx, &uw_pwy, &uw_gw, &uw_gwx, &uw_gwy, &uw_gsig, &uw_ph, &uw_gh, &uw_qwp,
 		                         &uw_qws, &uw_gm, &uw_gqw};
 		for (auto* p : uwd) p->free();

@@ -315,7 +315,9 @@ struct ContactArgs {
 	cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr, \
 	                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,  \
 	                   uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,   \
-	                   void* status, int mixed, cudaStream_t s);                                            \
+	                   const void* ff, const float* vol, void* status, cudaStream_t s);                     \
+	cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* m, const double* rho, void* ff, \
+	                  float* vol, cudaStream_t s);                                                          \
 	cudaError_t uw_stage(const mfk_host::UWArgs& a, int part, cudaStream_t s);                                \
 	}
 

@@ -120,13 +120,11 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 // order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
 // M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
 // Corr = C'0 + s.C'(1,2), h Corr_x = s.C'_x(1,2) + C'1 + C'_x0 -- the reference's
-// expressions (precomp_shape_functions.h:52-173) in scaled units.  Offsets are FP64
-// differences rounded once; volumes m_j / rho_j in FP32.
-template <class Rho, class Use, class Out>
-__device__ __forceinline__ bool rkpm_row32(double xi, double yi, double hi, uint32_t q0, uint32_t q1,
-                                           const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
-                                           const double* __restrict__ fy, const double* __restrict__ fm, Rho rho,
-                                           Use use, Out out) {
+// expressions (precomp_shape_functions.h:52-173) in scaled units.  offs(j) gives the
+// FP32 offset x_i - x_j of neighbour j, vol(j) its FP32 volume m_j / rho_j.
+template <class Offs, class Vol, class Use, class Out>
+__device__ __forceinline__ bool rkpm_row32(double hi, uint32_t q0, uint32_t q1, const uint32_t* __restrict__ nbr,
+                                           Offs offs, Vol vol, Use use, Out out) {
 	const float h = (float)hi, ih = 1.f / h;
 	const float fac = (float)(10 * (mfk::K_1_PI) / 7.0) * ih * ih;
 	float M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
@@ -134,8 +132,9 @@ __device__ __forceinline__ bool rkpm_row32(double xi, double yi, double hi, uint
 	for (uint32_t q = q0; q < q1; q++) {
 		if (!use(q)) continue;
 		const uint32_t j = nbr[q];
-		const float vj = (float)fm[j] / (float)rho(j);
-		const float rx = (float)(xi - fx[j]), ry = (float)(yi - fy[j]);
+		const float vj = vol(j);
+		const float2 r = offs(j);
+		const float rx = r.x, ry = r.y;
 		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
 		const float sx = rx * ih, sy = ry * ih, gx = w.w_x * h, gy = w.w_y * h;
 		const float W = w.w * vj, Gx = gx * vj, Gy = gy * vj;
@@ -195,8 +194,8 @@ __device__ __forceinline__ bool rkpm_row32(double xi, double yi, double hi, uint
 	const float cy0 = (float)Cy[0], cy1 = (float)Cy[1], cy2 = (float)Cy[2];
 	for (uint32_t q = q0; q < q1; q++) {
 		if (!use(q)) continue;
-		const uint32_t j = nbr[q];
-		const float rx = (float)(xi - fx[j]), ry = (float)(yi - fy[j]);
+		const float2 r = offs(nbr[q]);
+		const float rx = r.x, ry = r.y;
 		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
 		const float sx = rx * ih, sy = ry * ih;
 		const float Corr = (sx * c1 + sy * c2) + c0;

@@ -47,20 +47,12 @@ enum : uint32_t {
 	A_JAUMANN_GP = 1u << 24,
 };
 
-// nbh_ellipse for query point i over its candidates, then the RKPM shape functions of
-// the candidates inside the ellipse.  With qw_dst the row also stores its integration
-// weight for the passes: m / rho (riemann_update_integration_weights) when qw_src is
-// null, else qw_src (the weights of the last update).
-template <bool MIXED>
-__global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
-                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
-                         const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
-                         const double* __restrict__ frho, double* h_out, uint8_t* mask, double* w, double* wx,
-                         double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
-	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n_to) return;
-	const double px = tx[i], py = ty[i];
-	const uint32_t q0 = off[i], q1 = off[i + 1];
+// nbh_ellipse (neighbor_ellipse.h:62-127) of the query point (px, py) over its
+// candidates q0..q1, FP64: h = half the farthest candidate's distance, mask[q] = 1 for
+// the candidates inside the ellipse; returns their number.
+__device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0, uint32_t q1,
+                                              const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
+                                              const double* __restrict__ fy, double& h_row, uint8_t* mask) {
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0., h = 0.;
 	for (uint32_t q = q0; q < q1; q++) {
 		uint32_t j = nbr[q];
@@ -72,7 +64,7 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 	}
 	h = sqrt(h);
 	h /= 2;
-	h_out[i] = h;
+	h_row = h;
 	// eigen (neighbor_ellipse.h:29-60) of A = (Hxx, Hyx; Hxy, Hyy) / n, columns first
 	const double nc = (double)(q1 - q0);
 	const double A00 = Hxx / nc, A01 = Hyx / nc, A10 = Hxy / nc, A11 = Hyy / nc;
@@ -117,16 +109,145 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 		mask[q] = in ? 1 : 0;
 		cnt += in ? 1u : 0u;
 	}
+	return cnt;
+}
+
+// nbh_ellipse for query point i over its candidates, then the RKPM shape functions of
+// the candidates inside the ellipse (FP64).  With qw_dst the row also stores its
+// integration weight for the passes: m / rho (riemann_update_integration_weights) when
+// qw_src is null, else qw_src (the weights of the last update).
+__global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
+                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
+                         const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
+                         const double* __restrict__ frho, double* h_out, uint8_t* mask, double* w, double* wx,
+                         double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_to) return;
+	const double px = tx[i], py = ty[i];
+	const uint32_t q0 = off[i], q1 = off[i + 1];
+	double h;
+	const uint32_t cnt = ellipse64(px, py, q0, q1, nbr, fx, fy, h, mask);
+	h_out[i] = h;
 	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
 	if (qw_dst) qw_dst[i] = qw_src ? qw_src[i] : fm[i] / frho[i];
 	auto rho = [&](uint32_t j) { return frho[j]; };
 	auto use = [&](uint32_t q) { return mask[q] != 0; };
 	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
-	// the mixed form: the moment sums and the shape functions in FP32 (the ellipse above,
-	// and with it the neighbour sets, stay FP64)
-	const bool ok = MIXED ? rkpm_row32(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)
-	                      : rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out);
-	if (!ok) raise(st, ERR_SINGULAR, i);
+	if (!rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)) raise(st, ERR_SINGULAR, i);
+}
+
+// The stage's particle positions as float-float pairs (x = hi + lo to 48 bits) and
+// their FP32 volumes m / rho, for the mixed form's neighbourhood kernel.
+__global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
+                        const double* __restrict__ m, const double* __restrict__ rho, float4* ff, float* vol) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const double xi = x[i], yi = y[i];
+	const float xh = (float)xi, yh = (float)yi;
+	ff[i] = make_float4(xh, (float)(xi - (double)xh), yh, (float)(yi - (double)yh));
+	vol[i] = (float)m[i] / (float)rho[i];
+}
+
+// The mixed form's neighbourhood kernel: the ellipse in FP32 from the float-float
+// positions, with the FP64 ellipse (ellipse64) taken over for every row whose FP32
+// result could differ from it, so the neighbour sets are the FP64 form's; then the
+// RKPM moment sums and shape functions in FP32 (rkpm_row32).
+//
+// Error bound of the FP32 ellipse (first order in u = 2^-24).  An offset x_i - x_j
+// from the float-float pairs is within 3u of the exact difference, so a moment sum over
+// n candidates is within (n + 7) u of its exact value relative to the sum of its terms'
+// magnitudes (|dx dy| <= (dx^2 + dy^2) / 2), and every entry of A = H / n is within
+// e = (n + 8) u T of FP64's, T = A00 + A11 (FP64's own error is ~1e-16 relative).
+// Axis-aligned (the reference's branch for |A01| < 1e-9): s = x^2 / (k A00) +
+// y^2 / (k A11) is within (n + 19) u s.  Otherwise the eigen-decomposition uses the
+// discriminant ((A00 - A11)/2)^2 + A01^2 (no cancellation) and the better-conditioned
+// of the eigenvector forms (l1 - A11, A01) and (A01, l1 - A00): the smaller eigenvalue
+// is within e + 3u T, the larger within e + 3u T relative to T / 2, and the axis
+// within 2e / (l2 - l1) + 5u radians, whose effect on s is at most s (l2 - l1) / l1
+// per radian; together |s32 - s64| <= (3n + 48) u s T / l1.  The kernel's margin is
+// twice the bound: a candidate with |s32 - 1| inside it, an |A01| within e of the
+// 1e-9 threshold, or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the
+// row to ellipse64.  h is the FP64 distance of the farthest candidate, taken over the
+// candidates whose FP32 distance is within 64u of the FP32 maximum.
+__global__ void __launch_bounds__(128)
+    k_uw_nbh32(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
+               const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr, const float4* __restrict__ ff,
+               const float* __restrict__ vol, const double* __restrict__ fx, const double* __restrict__ fy,
+               const double* __restrict__ fm, const double* __restrict__ frho, double* h_out, uint8_t* mask,
+               double* w, double* wx, double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
+	constexpr float U = 5.9604645e-8f;  // 2^-24
+	constexpr float K2 = 1.6651f * 1.6651f;
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_to) return;
+	const double px = tx[i], py = ty[i];
+	const float pxh = (float)px, pyh = (float)py;
+	const float pxl = (float)(px - (double)pxh), pyl = (float)(py - (double)pyh);
+	auto offs = [&](uint32_t j) {  // x_i - x_j
+		const float4 f = ff[j];
+		return make_float2((pxh - f.x) + (pxl - f.y), (pyh - f.z) + (pyl - f.w));
+	};
+	const uint32_t q0 = off[i], q1 = off[i + 1];
+	float Hxx = 0.f, Hxy = 0.f, Hyy = 0.f, r2m = 0.f;
+	for (uint32_t q = q0; q < q1; q++) {
+		const float2 d = offs(nbr[q]);
+		r2m = fmaxf(r2m, d.x * d.x + d.y * d.y);
+		Hxx += d.x * d.x; Hxy += d.x * d.y; Hyy += d.y * d.y;
+	}
+	const float nf = (float)(q1 - q0);
+	const float A00 = Hxx / nf, A01 = Hxy / nf, A11 = Hyy / nf, T = A00 + A11;
+	const float e = (nf + 8.f) * U * T;  // bound on each entry's error
+	// the reference's branch: axis-aligned when |A01| < 1e-9
+	const double a01 = fabs((double)A01);
+	bool sure = T > 0.f && (a01 + e < 1e-9 || a01 - e >= 1e-9);
+	float cs, sn, ia2, ib2, bound;
+	if (a01 < 1e-9) {
+		cs = 1.f; sn = 0.f;
+		ia2 = 1.f / (K2 * A00); ib2 = 1.f / (K2 * A11);
+		bound = nf + 19.f;
+		sure = sure && A00 > 0.f && A11 > 0.f;
+	} else {
+		const float d = 0.5f * (A00 - A11), r = sqrtf(d * d + A01 * A01);
+		const float l1 = 0.5f * T - r, l2 = 0.5f * T + r;
+		const float vx = d >= 0.f ? A01 : d - r, vy = d >= 0.f ? -(d + r) : A01;
+		const float inv = rsqrtf(vx * vx + vy * vy);
+		cs = vx * inv; sn = vy * inv;
+		ia2 = 1.f / (K2 * l1); ib2 = 1.f / (K2 * l2);
+		const float cond = T / l1;
+		bound = (3.f * nf + 48.f) * cond;
+		sure = sure && l1 > 0.f && cond < 1e4f;
+	}
+	const float m = 2.f * bound * U;
+	const float lo = 1.f - m, hi = 1.f + m, band = r2m * (1.f - 64.f * U);
+	uint32_t cnt = 0;
+	double h2 = 0.;
+	for (uint32_t q = q0; q < q1 && sure; q++) {
+		const uint32_t j = nbr[q];
+		const float2 d = offs(j);
+		const float left = cs * d.x + sn * d.y, right = sn * d.x - cs * d.y;
+		const float s = left * left * ia2 + right * right * ib2;
+		sure = s < lo || s > hi;  // false for NaN
+		const bool in = s <= 1.f;
+		mask[q] = in ? 1 : 0;
+		cnt += in ? 1u : 0u;
+		if (d.x * d.x + d.y * d.y >= band) {
+			const double dx = px - fx[j], dy = py - fy[j];
+			h2 = fmax(h2, dx * dx + dy * dy);
+		}
+	}
+	double h;
+	if (sure) {
+		h = sqrt(h2);
+		h /= 2;
+	} else {
+		cnt = ellipse64(px, py, q0, q1, nbr, fx, fy, h, mask);
+	}
+	h_out[i] = h;
+	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
+	if (qw_dst) qw_dst[i] = qw_src ? qw_src[i] : fm[i] / frho[i];
+	auto volume = [&](uint32_t j) { return vol[j]; };
+	auto use = [&](uint32_t q) { return mask[q] != 0; };
+	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
+	if (!rkpm_row32(h, q0, q1, nbr, offs, volume, use, out)) raise(st, ERR_SINGULAR, i);
 }
 
 // the particles' integration weight of this evaluation (riemann_update_integration_weights),
@@ -278,14 +399,22 @@ __global__ void k_uw_smooth_copy(UWArgs a) {
 cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
                    const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,
                    uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,
-                   void* status, int mixed, cudaStream_t s) {
+                   const void* ff, const float* vol, void* status, cudaStream_t s) {
 	if (n_to == 0) return cudaSuccess;
-	if (mixed)
-		k_uw_nbh<true><<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx,
-		                                                wy, qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
+	if (ff)
+		k_uw_nbh32<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, reinterpret_cast<const float4*>(ff), vol,
+		                                            fx, fy, fm, frho, h_out, mask, w, wx, wy, qw_src, qw_dst,
+		                                            reinterpret_cast<DevStatus*>(status));
 	else
-		k_uw_nbh<false><<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx,
-		                                                 wy, qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
+		k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx, wy,
+		                                          qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
+	return cudaGetLastError();
+}
+
+cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* m, const double* rho, void* ff,
+                  float* vol, cudaStream_t s) {
+	if (n == 0) return cudaSuccess;
+	k_uw_ff<<<grid1(n, 256), 256, 0, s>>>(n, x, y, m, rho, reinterpret_cast<float4*>(ff), vol);
 	return cudaGetLastError();
 }
 

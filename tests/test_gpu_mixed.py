@@ -321,3 +321,36 @@ def test_mixed_tl_resume_through_set_state(graph, lib):
     for g, w in zip(got, want):
         for f in fields:
             np.testing.assert_array_equal(g[f], w[f], err_msg=f)
+
+
+UW_CHECKPOINTS = [("ul_weak_rings_contact", (0, 300, 600)), ("ul_weak_plate", (0, 400)), ("ul_weak_disc", (0, 400))]
+
+
+@pytest.mark.parametrize("case,checkpoints", UW_CHECKPOINTS, ids=[c[0] for c in UW_CHECKPOINTS])
+def test_ul_weak_mixed_neighbour_sets_are_fp64s(case, checkpoints, lib):
+    """The mixed weak UL form selects its ellipse neighbours in FP32 (float-float
+    offsets, the FP64 ellipse taken over for a row with a decision inside the FP32
+    error bound): on the same particle state, its neighbour sets are the FP64 form's,
+    at checkpoints along a mixed run (rings through contact, the stretched plate, the
+    spinning disc)."""
+    import mfree_iwf_gb300 as M
+    sc = scenario(case)
+    mix = M.from_scenario(sc, precision="mixed")
+    ref = M.from_scenario(sc, precision="fp64")
+    done = 0
+    rows = 0
+    for k in checkpoints:
+        if k > done:
+            mix.step(k - done)
+            done = k
+        for b in range(len(sc.bodies)):
+            ref.set_state(b, mix.get_state(b))
+        for b in range(len(sc.bodies)):
+            got, want = mix.neighbors(b), ref.neighbors(b)
+            assert len(got) == len(want)
+            bad = [i for i, (g, w) in enumerate(zip(got, want)) if not np.array_equal(g, w)]
+            assert not bad, (k, b, bad[:5])
+            rows += len(got)
+    mix.close()
+    ref.close()
+    assert rows > 0
