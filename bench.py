@@ -458,7 +458,7 @@ def ours(args, cfg_desc):
     sim.set_timing(True)
     sim.step(max(2, min(args.steps, 10)))
     sim.synchronize()
-    kstats = {k: sim.kernel_stats(k) for k in range(6)}
+    kstats = {k: sim.kernel_stats(k) for k in range(8)}
     weak_lists = None
     if sc.method == M.METHOD_TL_WEAK:  # list sizes for the weak passes' byte model
         weak_lists = (sim.get_option("weak_gauss_points"), sim.get_option("weak_gp_entries"),
@@ -565,7 +565,8 @@ def ours(args, cfg_desc):
     names = {0: "UL pair (+RK)", 1: "TL pass A", 2: "TL pass B", 3: "contact", 4: "UL stage (grid + gather + pair)",
              5: "weak"}
     if sc.method == M.METHOD_UL_WEAK:
-        names.update({2: "weak UL particle pass", 5: "weak UL stress-point pass"})
+        names.update({2: "weak UL particle pass", 5: "weak UL stress-point pass",
+                      6: "weak UL neighbourhoods (ellipse + RKPM)"})
     elif sc.method == M.METHOD_TL_WEAK:
         names.update({2: "weak TL particle pass", 5: "weak TL Gauss-point pass"})
     elif sc.method in (M.METHOD_COROT, M.METHOD_POTENTIAL):

@@ -2034,8 +2034,11 @@ mf_status uw_step(mf_ctx* c) {
 			                                           c->d_status, c->stream);
 			if (e != cudaSuccess) return cuda_fail(c, e, "weak UL Gauss points");
 			c->launches++;
-		} else if ((e = uw_neighbourhoods(c, a, true, false)) != cudaSuccess) {
-			return cuda_fail(c, e, "weak UL neighbourhoods");
+		} else {
+			int slot;
+			timing_begin(c, 6, slot);
+			if ((e = uw_neighbourhoods(c, a, true, false)) != cudaSuccess) return cuda_fail(c, e, "weak UL neighbourhoods");
+			timing_end(c, slot, (uint64_t)c->n_total + c->n_g);
 		}
 		int slot;
 		timing_begin(c, 5, slot);
@@ -2054,7 +2057,10 @@ mf_status uw_step(mf_ctx* c) {
 	}
 	if (c->do_smooth) {  // rk4.h:198-204
 		UWArgs a = uw_args(c, 0);  // reads the particles themselves
+		int slot;
+		timing_begin(c, 6, slot);
 		if ((e = uw_neighbourhoods(c, a, false, true)) != cudaSuccess) return cuda_fail(c, e, "weak UL smoothing");
+		timing_end(c, slot, c->n_total);
 		if ((e = launch(a, 2)) != cudaSuccess || (e = launch(a, 3)) != cudaSuccess)
 			return cuda_fail(c, e, "weak UL smoothing");
 		c->launches += 3;

@@ -114,27 +114,34 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 
 
 // The same shape functions for the mixed weak updated-Lagrangian form: the 27 moment
-// sums per neighbour in FP32, the three 3x3 solves (Cramer) in FP64, the shape
-// functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
+// sums per neighbour in FP32, the three 3x3 solves in FP64 (through the adjugate), the
+// shape functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
 // with the gradient scaled by h (d/ds = h d/dx), so that every moment entry is of
 // order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
 // M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
 // Corr = C'0 + s.C'(1,2), h Corr_x = s.C'_x(1,2) + C'1 + C'_x0 -- the reference's
-// expressions (precomp_shape_functions.h:52-173) in scaled units.  offs(j) gives the
-// FP32 offset x_i - x_j of neighbour j, vol(j) its FP32 volume m_j / rho_j.
-template <class Offs, class Vol, class Use, class Out>
-__device__ __forceinline__ bool rkpm_row32(double hi, uint32_t q0, uint32_t q1, const uint32_t* __restrict__ nbr,
-                                           Offs offs, Vol vol, Use use, Out out) {
-	const float h = (float)hi, ih = 1.f / h;
-	const float fac = (float)(10 * (mfk::K_1_PI) / 7.0) * ih * ih;
-	float M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
-	      My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row], scaled; upper triangle
-	for (uint32_t q = q0; q < q1; q++) {
-		if (!use(q)) continue;
-		const uint32_t j = nbr[q];
-		const float vj = vol(j);
-		const float2 r = offs(j);
-		const float rx = r.x, ry = r.y;
+// expressions (precomp_shape_functions.h:52-173) in scaled units.  A row is init(h),
+// add() per neighbour in ascending slot order, then finish(): each(g) calls g(q, d) for
+// the row's neighbours (slot q, FP32 offset d = x_i - x_j) in that order, and out(q, w,
+// w_x, w_y) takes the FP32 shape function and its gradient.  rkpm_row32 is the whole
+// row: each(f) calls f(q, j) per neighbour (particle j), offs(j) gives the offset and
+// vol(j) the FP32 volume m_j / rho_j.
+struct Rkpm32 {
+	float h, ih, fac;
+	float M[3][3], Mx[3][3], My[3][3];  // [col][row], scaled; upper triangle
+
+	__device__ __forceinline__ void init(double hi) {
+		h = (float)hi;
+		ih = 1.f / h;
+		fac = (float)(10 * (mfk::K_1_PI) / 7.0) * ih * ih;
+#pragma unroll
+		for (int a_ = 0; a_ < 3; a_++)
+#pragma unroll
+			for (int b_ = 0; b_ < 3; b_++) M[a_][b_] = Mx[a_][b_] = My[a_][b_] = 0.f;
+	}
+
+	// the moments of one neighbour at offset (rx, ry) = x_i - x_j with volume vj
+	__device__ __forceinline__ void add(float rx, float ry, float vj) {
 		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
 		const float sx = rx * ih, sy = ry * ih, gx = w.w_x * h, gy = w.w_y * h;
 		const float W = w.w * vj, Gx = gx * vj, Gy = gy * vj;
@@ -153,57 +160,70 @@ __device__ __forceinline__ bool rkpm_row32(double hi, uint32_t q0, uint32_t q1, 
 		My[1][2] += sx * sy * Gy + sx * W;
 		My[2][2] += sy * sy * Gy + 2.f * sy * W;
 	}
-	// the matrices are symmetric (M[a][b] = M[b][a]); the solves in FP64
-	double A[3][3], Ax[3][3], Ay[3][3];
+
+	// the solves and the shape functions of the neighbours each(f) visits
+	template <class Each, class Out>
+	__device__ __forceinline__ bool finish(Each each, Out out) const {
+		// the three solves in FP64 through the adjugate of the symmetric moment matrix
+		// (A^-1 r = adj(A) r / det A, Cramer's rule with the cofactors shared)
+		double A[3][3], Ax[3][3], Ay[3][3];
 #pragma unroll
-	for (int a_ = 0; a_ < 3; a_++)
+		for (int a_ = 0; a_ < 3; a_++)
 #pragma unroll
-		for (int b_ = a_; b_ < 3; b_++) {
-			A[a_][b_] = A[b_][a_] = (double)M[a_][b_];
-			Ax[a_][b_] = Ax[b_][a_] = (double)Mx[a_][b_];
-			Ay[a_][b_] = Ay[b_][a_] = (double)My[a_][b_];
+			for (int b_ = a_; b_ < 3; b_++) {
+				A[a_][b_] = A[b_][a_] = mfk::f2d(M[a_][b_]);
+				Ax[a_][b_] = Ax[b_][a_] = mfk::f2d(Mx[a_][b_]);
+				Ay[a_][b_] = Ay[b_][a_] = mfk::f2d(My[a_][b_]);
+			}
+		const double j00 = A[1][1] * A[2][2] - A[1][2] * A[1][2];
+		const double j01 = A[0][2] * A[1][2] - A[0][1] * A[2][2];
+		const double j02 = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+		const double j11 = A[0][0] * A[2][2] - A[0][2] * A[0][2];
+		const double j12 = A[0][1] * A[0][2] - A[0][0] * A[1][2];
+		const double j22 = A[0][0] * A[1][1] - A[0][1] * A[0][1];
+		const double det = A[0][0] * j00 + A[0][1] * j01 + A[0][2] * j02;
+		const bool ok = fabs(det) > 0.;
+		const double id = 1. / det;
+		auto solve = [&](const double r[3], double x[3]) {
+			x[0] = (j00 * r[0] + j01 * r[1] + j02 * r[2]) * id;
+			x[1] = (j01 * r[0] + j11 * r[1] + j12 * r[2]) * id;
+			x[2] = (j02 * r[0] + j12 * r[1] + j22 * r[2]) * id;
+		};
+		const double C[3] = {j00 * id, j01 * id, j02 * id};  // the solution for P = (1, 0, 0)
+		double Cx[3], Cy[3];
+		double rx_[3], ry_[3];
+#pragma unroll
+		for (int r = 0; r < 3; r++) {
+			rx_[r] = -(Ax[0][r] * C[0] + Ax[1][r] * C[1] + Ax[2][r] * C[2]);
+			ry_[r] = -(Ay[0][r] * C[0] + Ay[1][r] * C[1] + Ay[2][r] * C[2]);
 		}
-	bool ok = true;
-	auto solve = [&](const double r[3], double x[3]) {
-		double delta = A[0][0] * A[1][1] * A[2][2] + A[1][0] * A[2][1] * A[0][2] + A[2][0] * A[0][1] * A[1][2] -
-		               A[0][2] * A[1][1] * A[2][0] - A[1][2] * A[2][1] * A[0][0] - A[2][2] * A[0][1] * A[1][0];
-		double delta_x = r[0] * A[1][1] * A[2][2] + A[1][0] * A[2][1] * r[2] + A[2][0] * r[1] * A[1][2] -
-		                 r[2] * A[1][1] * A[2][0] - A[1][2] * A[2][1] * r[0] - A[2][2] * r[1] * A[1][0];
-		double delta_y = A[0][0] * r[1] * A[2][2] + r[0] * A[2][1] * A[0][2] + A[2][0] * A[0][1] * r[2] -
-		                 A[0][2] * r[1] * A[2][0] - r[2] * A[2][1] * A[0][0] - A[2][2] * A[0][1] * r[0];
-		double delta_z = A[0][0] * A[1][1] * r[2] + A[1][0] * r[1] * A[0][2] + r[0] * A[0][1] * A[1][2] -
-		                 A[0][2] * A[1][1] * r[0] - A[1][2] * r[1] * A[0][0] - r[2] * A[0][1] * A[1][0];
-		if (!(fabs(delta) > 0.)) ok = false;
-		const double id = 1. / delta;
-		x[0] = delta_x * id;
-		x[1] = delta_y * id;
-		x[2] = delta_z * id;
-	};
-	double P[3] = {1., 0., 0.}, C[3], Cx[3], Cy[3];
-	solve(P, C);
-	double rx_[3], ry_[3];
-#pragma unroll
-	for (int r = 0; r < 3; r++) {
-		rx_[r] = -(Ax[0][r] * C[0] + Ax[1][r] * C[1] + Ax[2][r] * C[2]);
-		ry_[r] = -(Ay[0][r] * C[0] + Ay[1][r] * C[1] + Ay[2][r] * C[2]);
+		solve(rx_, Cx);
+		solve(ry_, Cy);
+		const float c0 = (float)C[0], c1 = (float)C[1], c2 = (float)C[2];
+		const float cx0 = (float)Cx[0], cx1 = (float)Cx[1], cx2 = (float)Cx[2];
+		const float cy0 = (float)Cy[0], cy1 = (float)Cy[1], cy2 = (float)Cy[2];
+		each([&](uint32_t q, float2 r) {
+			const float rx = r.x, ry = r.y;
+			const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
+			const float sx = rx * ih, sy = ry * ih;
+			const float Corr = (sx * c1 + sy * c2) + c0;
+			const float Corr_x = (sx * cx1 + sy * cx2) + c1 + cx0;  // h Corr_x
+			const float Corr_y = (sx * cy1 + sy * cy2) + c2 + cy0;  // h Corr_y
+			out(q, Corr * w.w, Corr_x * ih * w.w + Corr * w.w_x, Corr_y * ih * w.w + Corr * w.w_y);
+		});
+		return ok;
 	}
-	solve(rx_, Cx);
-	solve(ry_, Cy);
-	const float c0 = (float)C[0], c1 = (float)C[1], c2 = (float)C[2];
-	const float cx0 = (float)Cx[0], cx1 = (float)Cx[1], cx2 = (float)Cx[2];
-	const float cy0 = (float)Cy[0], cy1 = (float)Cy[1], cy2 = (float)Cy[2];
-	for (uint32_t q = q0; q < q1; q++) {
-		if (!use(q)) continue;
-		const float2 r = offs(nbr[q]);
-		const float rx = r.x, ry = r.y;
-		const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);
-		const float sx = rx * ih, sy = ry * ih;
-		const float Corr = (sx * c1 + sy * c2) + c0;
-		const float Corr_x = (sx * cx1 + sy * cx2) + c1 + cx0;  // h Corr_x
-		const float Corr_y = (sx * cy1 + sy * cy2) + c2 + cy0;  // h Corr_y
-		out(q, Corr * w.w, Corr_x * ih * w.w + Corr * w.w_x, Corr_y * ih * w.w + Corr * w.w_y);
-	}
-	return ok;
+};
+
+template <class Each, class Offs, class Vol, class Out>
+__device__ __forceinline__ bool rkpm_row32(double hi, Each each, Offs offs, Vol vol, Out out) {
+	Rkpm32 k;
+	k.init(hi);
+	each([&](uint32_t, uint32_t j) {
+		const float2 r = offs(j);
+		k.add(r.x, r.y, vol(j));
+	});
+	return k.finish([&](auto g) { each([&](uint32_t q, uint32_t j) { g(q, offs(j)); }); }, out);
 }
 
 }  // namespace

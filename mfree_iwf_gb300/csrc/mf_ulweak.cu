@@ -148,6 +148,29 @@ __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* 
 	vol[i] = (float)m[i] / (float)rho[i];
 }
 
+// Candidates q0..q1 in batches of four while cont() holds: a batch's list entries and
+// float-float positions are all loaded before f(q, j, position) runs on any of them, so
+// a thread keeps four gathers in flight.
+template <class F, class Cont>
+__device__ __forceinline__ void cand4(uint32_t q0, uint32_t q1, const uint32_t* __restrict__ nbr,
+                                      const float4* __restrict__ ff, F f, Cont cont) {
+	uint32_t q = q0;
+	for (; q + 4 <= q1 && cont(); q += 4) {
+		uint32_t j[4];
+		float4 v[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) j[u] = nbr[q + u];
+#pragma unroll
+		for (int u = 0; u < 4; u++) v[u] = ff[j[u]];
+#pragma unroll
+		for (int u = 0; u < 4; u++) f(q + u, j[u], v[u]);
+	}
+	for (; q < q1 && cont(); q++) {
+		const uint32_t j = nbr[q];
+		f(q, j, ff[j]);
+	}
+}
+
 // The mixed form's neighbourhood kernel: the ellipse in FP32 from the float-float
 // positions, with the FP64 ellipse (ellipse64) taken over for every row whose FP32
 // result could differ from it, so the neighbour sets are the FP64 form's; then the
@@ -167,8 +190,8 @@ __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* 
 // per radian; together |s32 - s64| <= (3n + 48) u s T / l1.  The kernel's margin is
 // twice the bound: a candidate with |s32 - 1| inside it, an |A01| within e of the
 // 1e-9 threshold, or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the
-// row to ellipse64.  h is the FP64 distance of the farthest candidate, taken over the
-// candidates whose FP32 distance is within 64u of the FP32 maximum.
+// row to ellipse64.  h is the FP64 distance of the candidate farthest in FP32 (FP64's
+// h, or one within FP32 rounding of it where two candidates tie in FP32).
 __global__ void __launch_bounds__(128)
     k_uw_nbh32(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
                const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr, const float4* __restrict__ ff,
@@ -182,17 +205,21 @@ __global__ void __launch_bounds__(128)
 	const double px = tx[i], py = ty[i];
 	const float pxh = (float)px, pyh = (float)py;
 	const float pxl = (float)(px - (double)pxh), pyl = (float)(py - (double)pyh);
-	auto offs = [&](uint32_t j) {  // x_i - x_j
-		const float4 f = ff[j];
+	auto offs = [&](const float4 f) {  // x_i - x_j from j's float-float position
 		return make_float2((pxh - f.x) + (pxl - f.y), (pyh - f.z) + (pyl - f.w));
 	};
 	const uint32_t q0 = off[i], q1 = off[i + 1];
-	float Hxx = 0.f, Hxy = 0.f, Hyy = 0.f, r2m = 0.f;
-	for (uint32_t q = q0; q < q1; q++) {
-		const float2 d = offs(nbr[q]);
-		r2m = fmaxf(r2m, d.x * d.x + d.y * d.y);
-		Hxx += d.x * d.x; Hxy += d.x * d.y; Hyy += d.y * d.y;
-	}
+	float Hxx = 0.f, Hxy = 0.f, Hyy = 0.f, r2m = -1.f;
+	uint32_t jm = 0;  // the candidate farthest in FP32
+	cand4(
+	    q0, q1, nbr, ff,
+	    [&](uint32_t, uint32_t j, float4 v) {
+		    const float2 d = offs(v);
+		    const float r2 = d.x * d.x + d.y * d.y;
+		    if (r2 > r2m) { r2m = r2; jm = j; }
+		    Hxx += d.x * d.x; Hxy += d.x * d.y; Hyy += d.y * d.y;
+	    },
+	    [] { return true; });
 	const float nf = (float)(q1 - q0);
 	const float A00 = Hxx / nf, A01 = Hxy / nf, A11 = Hyy / nf, T = A00 + A11;
 	const float e = (nf + 8.f) * U * T;  // bound on each entry's error
@@ -217,37 +244,85 @@ __global__ void __launch_bounds__(128)
 		sure = sure && l1 > 0.f && cond < 1e4f;
 	}
 	const float m = 2.f * bound * U;
-	const float lo = 1.f - m, hi = 1.f + m, band = r2m * (1.f - 64.f * U);
-	uint32_t cnt = 0;
-	double h2 = 0.;
-	for (uint32_t q = q0; q < q1 && sure; q++) {
-		const uint32_t j = nbr[q];
-		const float2 d = offs(j);
-		const float left = cs * d.x + sn * d.y, right = sn * d.x - cs * d.y;
-		const float s = left * left * ia2 + right * right * ib2;
-		sure = s < lo || s > hi;  // false for NaN
-		const bool in = s <= 1.f;
-		mask[q] = in ? 1 : 0;
-		cnt += in ? 1u : 0u;
-		if (d.x * d.x + d.y * d.y >= band) {
-			const double dx = px - fx[j], dy = py - fy[j];
-			h2 = fmax(h2, dx * dx + dy * dy);
-		}
-	}
-	double h;
+	const float lo = 1.f - m, hi = 1.f + m;
+	double h = 0.;
 	if (sure) {
-		h = sqrt(h2);
+		// FP64's h up to FP32 ties: the FP64 distance of the candidate farthest in FP32
+		const double dx = px - fx[jm], dy = py - fy[jm];
+		h = sqrt(dx * dx + dy * dy);
 		h /= 2;
-	} else {
+	}
+	// the selection, with the RKPM moments of the selected candidates summed as they
+	// are found
+	Rkpm32 k;
+	k.init(h);
+	uint32_t cnt = 0;
+	uint64_t bits = 0;  // the selection of the first 64 candidates
+	cand4(
+	    q0, q1, nbr, ff,
+	    [&](uint32_t q, uint32_t j, float4 v) {
+		    const float2 d = offs(v);
+		    const float left = cs * d.x + sn * d.y, right = sn * d.x - cs * d.y;
+		    const float s = left * left * ia2 + right * right * ib2;
+		    sure = sure && (s < lo || s > hi);  // false for NaN
+		    const bool in = s <= 1.f;
+		    mask[q] = in ? 1 : 0;
+		    if (in) {
+			    cnt++;
+			    if (q - q0 < 64) bits |= 1ull << (q - q0);
+			    k.add(d.x, d.y, vol[j]);
+		    }
+	    },
+	    [&] { return sure; });
+	// the selected candidates in slot order, g(q, offset): the set bits in batches of
+	// four (loads first), then (rows of more than 64 candidates) the stored mask
+	auto each = [&](auto g) {
+		uint64_t b = bits;
+		while (b) {
+			uint32_t qs[4], js[4];
+			float4 vs[4];
+			int nb = 0;
+#pragma unroll
+			for (int u = 0; u < 4; u++)
+				if (b) {
+					qs[u] = q0 + (uint32_t)(__ffsll((long long)b) - 1);
+					b &= b - 1;
+					nb = u + 1;
+				}
+#pragma unroll
+			for (int u = 0; u < 4; u++)
+				if (u < nb) js[u] = nbr[qs[u]];
+#pragma unroll
+			for (int u = 0; u < 4; u++)
+				if (u < nb) vs[u] = ff[js[u]];
+#pragma unroll
+			for (int u = 0; u < 4; u++)
+				if (u < nb) g(qs[u], offs(vs[u]));
+		}
+		for (uint32_t q = q0 + 64; q < q1; q++)
+			if (mask[q]) g(q, offs(ff[nbr[q]]));
+	};
+	if (!sure) {
 		cnt = ellipse64(px, py, q0, q1, nbr, fx, fy, h, mask);
+		bits = 0;
+		for (uint32_t q = q0; q < q1 && q - q0 < 64; q++)
+			if (mask[q]) bits |= 1ull << (q - q0);
+		k.init(h);
+		// the moments in slot order again (each's offsets; the volumes by slot)
+		for (uint32_t q = q0; q < q1; q++)
+			if (mask[q]) {
+				const uint32_t j = nbr[q];
+				const float2 d = offs(ff[j]);
+				k.add(d.x, d.y, vol[j]);
+			}
 	}
 	h_out[i] = h;
 	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
 	if (qw_dst) qw_dst[i] = qw_src ? qw_src[i] : fm[i] / frho[i];
-	auto volume = [&](uint32_t j) { return vol[j]; };
-	auto use = [&](uint32_t q) { return mask[q] != 0; };
-	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
-	if (!rkpm_row32(h, q0, q1, nbr, offs, volume, use, out)) raise(st, ERR_SINGULAR, i);
+	auto out = [&](uint32_t q, float ww, float wwx, float wwy) {
+		w[q] = mfk::f2d(ww); wx[q] = mfk::f2d(wwx); wy[q] = mfk::f2d(wwy);
+	};
+	if (!k.finish(each, out)) raise(st, ERR_SINGULAR, i);
 }
 
 // the particles' integration weight of this evaluation (riemann_update_integration_weights),
