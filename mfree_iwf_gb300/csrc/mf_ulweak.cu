@@ -358,6 +358,7 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 		if (!a.gmask[q]) continue;
 		uint32_t j = a.gc_nbr[q];
 		double vxj = a.rd.vx[j], vyj = a.rd.vy[j], qwj = p_qw(a, j);
+#if MF_STRICT_FORM
 		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
 			vx_x += vxj * a.gwx[q] * qwj;
 			vx_y += vxj * a.gwy[q] * qwj;
@@ -368,6 +369,18 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 			vxi += vxj * a.gw[q] * qwj;
 			vyi += vyj * a.gw[q] * qwj;
 		}
+#else
+		// the fast form weights each gradient once (w_x q_j), then one FMA per sum
+		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
+			const double tx = a.gwx[q] * qwj, ty = a.gwy[q] * qwj;
+			vx_x += vxj * tx; vx_y += vxj * ty;
+			vy_x += vyj * tx; vy_y += vyj * ty;
+		}
+		if (flags & mfk_host::FLAG_UW_INTERP) {
+			const double tw = a.gw[q] * qwj;
+			vxi += vxj * tw; vyi += vyj * tw;
+		}
+#endif
 	}
 	const double Sxx = g.Sxx[i], Sxy = g.Sxy[i], Syy = g.Syy[i];
 	double d[6] = {0., 0., 0., 0., 0., 0.};  // x_t y_t rho_t Sxx_t Sxy_t Syy_t
@@ -401,10 +414,16 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 			if (!a.gmask[q]) continue;
 			uint32_t gi = a.tp_gp[t];
 			double Sxxi = a.gsig[gi], Sxyi = a.gsig[ng + gi], Syyi = a.gsig[2 * ng + gi], qwi = a.gsig[3 * ng + gi];
+#if MF_STRICT_FORM
 			Sxx_x -= Sxxi * a.gwx[q] * qwi * qwj;
 			Sxy_y -= Sxyi * a.gwy[q] * qwi * qwj;
 			Sxy_x -= Sxyi * a.gwx[q] * qwi * qwj;
 			Syy_y -= Syyi * a.gwy[q] * qwi * qwj;
+#else
+			const double c = qwi * qwj, tx = a.gwx[q] * c, ty = a.gwy[q] * c;
+			Sxx_x -= Sxxi * tx; Sxy_y -= Sxyi * ty;
+			Sxy_x -= Sxyi * tx; Syy_y -= Syyi * ty;
+#endif
 		}
 	}
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
@@ -413,10 +432,17 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 			if (!a.pmask[q]) continue;
 			uint32_t k = a.pc_nbr[q];
 			double qwk = p_qw(a, k);
+#if MF_STRICT_FORM
 			vx_x += (s.vx[k] - vxj) * a.pwx[q] * qwk;
 			vx_y += (s.vx[k] - vxj) * a.pwy[q] * qwk;
 			vy_x += (s.vy[k] - vyj) * a.pwx[q] * qwk;
 			vy_y += (s.vy[k] - vyj) * a.pwy[q] * qwk;
+#else
+			const double tx = a.pwx[q] * qwk, ty = a.pwy[q] * qwk;
+			const double dvx = s.vx[k] - vxj, dvy = s.vy[k] - vyj;
+			vx_x += dvx * tx; vx_y += dvx * ty;
+			vy_x += dvy * tx; vy_y += dvy * ty;
+#endif
 		}
 	}
 	double d[5] = {0., 0., 0., 0., 0.};  // x_t y_t vx_t vy_t rho_t
