@@ -288,6 +288,8 @@ struct mf_ctx {
 	// UL_WEAK: stress points (state sets as the particles: base, accumulator, two stage
 	// sets), fixed candidate lists, per-evaluation ellipse masks and shape functions
 	DevBuf<uint32_t> uw_gbody, uw_pc_off, uw_pc_nbr, uw_gc_off, uw_gc_nbr, uw_tp_off, uw_tp_gp, uw_tp_slot, uw_bc_of;
+	DevBuf<uint32_t> uw_pc_cnt, uw_gc_cnt;  // candidates per row; *_off hold the rows' first slots
+	uint32_t uw_pc_stride = 1, uw_gc_stride = 1;
 	DevBuf<uint8_t> uw_pmask, uw_gmask;
 	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
 	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
@@ -1826,6 +1828,32 @@ mf_status validate_ulweak(mf_ctx* c, const std::vector<int32_t>& acts, uint32_t&
 	return MF_OK;
 }
 
+// CSR lists (off, nbr) of n rows laid out in slices of 32 rows: the k-th candidate of
+// row i in slot base(i / 32) + 32 k + i % 32, each slice as wide as its longest row.
+// Gives the rows' first slots and counts and the sliced list (slots past a row's count
+// are padding, never read); false when the slots do not fit 32-bit indices.
+bool slice_lists(const std::vector<uint32_t>& off, const std::vector<uint32_t>& nbr, uint32_t n,
+                 std::vector<uint32_t>& start, std::vector<uint32_t>& cnt, std::vector<uint32_t>& sliced) {
+	start.assign((size_t)n + 1, 0);
+	cnt.assign((size_t)n + 1, 0);
+	uint64_t base = 0;
+	for (uint32_t s0 = 0; s0 < n; s0 += 32) {
+		const uint32_t s1 = std::min(n, s0 + 32);
+		uint32_t width = 0;
+		for (uint32_t i = s0; i < s1; i++) width = std::max(width, off[i + 1] - off[i]);
+		for (uint32_t i = s0; i < s1; i++) {
+			start[i] = (uint32_t)(base + (i - s0));
+			cnt[i] = off[i + 1] - off[i];
+		}
+		base += 32ull * width;
+		if (base >= 0xffffffffull) return false;
+	}
+	sliced.assign(base, 0);
+	for (uint32_t i = 0; i < n; i++)
+		for (uint32_t k = 0; k < cnt[i]; k++) sliced[start[i] + 32ull * k] = nbr[off[i] + k];
+	return true;
+}
+
 // Weak UL set-up: stress points, candidate lists by the Manhattan search
 // (tensile.cpp:706-707), the transposed stress-point candidates, per-candidate scratch.
 mf_status uw_setup(mf_ctx* c) {
@@ -1878,7 +1906,7 @@ mf_status uw_setup(mf_ctx* c) {
 	CK(c->uw_ph.alloc(n)); CK(c->uw_qws.alloc(n));
 	if (c->uw_mixed) { CK(c->uw_ff.alloc(4 * (size_t)n)); CK(c->uw_vol.alloc(n)); }
 	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
-	std::vector<uint32_t> goff(ng + 1), gnbr;
+	std::vector<uint32_t> goff(ng + 1), gnbr, gstart;
 	uint64_t ep, eg;
 	if (fem) {
 		// the particles have no lists; a stress point's candidates are its element's
@@ -1902,6 +1930,12 @@ mf_status uw_setup(mf_ctx* c) {
 		CK(cudaMemcpy(c->uw_gc_off.p, goff.data(), ((size_t)ng + 1) * 4, cudaMemcpyHostToDevice));
 		CK(cudaMemcpy(c->uw_gc_nbr.p, gnbr.data(), gnbr.size() * 4, cudaMemcpyHostToDevice));
 		CK(cudaMemcpy(c->uw_qws.p, c->qw0.p, (size_t)n * 8, cudaMemcpyDeviceToDevice));
+		std::vector<uint32_t> four(ng + 1, 4);
+		CK(c->uw_pc_cnt.alloc(n + 1)); CK(c->uw_gc_cnt.alloc(ng + 1));
+		CK(cudaMemcpy(c->uw_pc_cnt.p, zoff.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_gc_cnt.p, four.data(), ((size_t)ng + 1) * 4, cudaMemcpyHostToDevice));
+		c->uw_pc_stride = c->uw_gc_stride = 1;
+		gstart.assign(goff.begin(), goff.end());
 		ep = 0;
 		eg = gnbr.size();
 	} else {
@@ -1914,31 +1948,50 @@ mf_status uw_setup(mf_ctx* c) {
 		if ((st = build_lists(c, px, py, c->body_of.p, n, c->uw_g[0][0].p, c->uw_g[0][1].p, c->uw_gbody.p, ng,
 		                      c->cfg.max_nbh, c->uw_gc_off, c->uw_gc_nbr, gc, true)))
 			return st;
-		ep = c->uw_pc_nbr.n;
-		eg = c->uw_gc_nbr.n;
-		gnbr.resize(eg);
+		gnbr.resize(c->uw_gc_nbr.n);
 		CK(cudaMemcpy(goff.data(), c->uw_gc_off.p, ((size_t)ng + 1) * 4, cudaMemcpyDeviceToHost));
-		if (eg) CK(cudaMemcpy(gnbr.data(), c->uw_gc_nbr.p, eg * 4, cudaMemcpyDeviceToHost));
+		if (!gnbr.empty()) CK(cudaMemcpy(gnbr.data(), c->uw_gc_nbr.p, gnbr.size() * 4, cudaMemcpyDeviceToHost));
+		std::vector<uint32_t> poff(n + 1), pnbr(c->uw_pc_nbr.n);
+		CK(cudaMemcpy(poff.data(), c->uw_pc_off.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+		if (!pnbr.empty()) CK(cudaMemcpy(pnbr.data(), c->uw_pc_nbr.p, pnbr.size() * 4, cudaMemcpyDeviceToHost));
+		// the ellipse kernels and the passes walk the lists one row per thread: sliced,
+		// a warp's 32 rows reach their k-th candidates in one line
+		std::vector<uint32_t> pstart, pcnt, psl, gcnt, gsl;
+		if (!slice_lists(poff, pnbr, n, pstart, pcnt, psl) || !slice_lists(goff, gnbr, ng, gstart, gcnt, gsl))
+			return fail(c, MF_ERR_CAPACITY, "weak UL candidate slots exceed 2^32");
+		auto upload = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& v) -> mf_status {
+			d.free();
+			CK(d.alloc(v.size()));
+			if (!v.empty()) CK(cudaMemcpy(d.p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+			return MF_OK;
+		};
+		if ((st = upload(c->uw_pc_off, pstart)) || (st = upload(c->uw_pc_cnt, pcnt)) || (st = upload(c->uw_pc_nbr, psl)) ||
+		    (st = upload(c->uw_gc_off, gstart)) || (st = upload(c->uw_gc_cnt, gcnt)) || (st = upload(c->uw_gc_nbr, gsl)))
+			return st;
+		c->uw_pc_stride = c->uw_gc_stride = 32;
+		ep = psl.size();
+		eg = gsl.size();
 	}
 	CK(c->uw_pmask.alloc(ep)); CK(c->uw_pw.alloc(ep)); CK(c->uw_pwx.alloc(ep)); CK(c->uw_pwy.alloc(ep));
 	CK(c->uw_gmask.alloc(eg)); CK(c->uw_gw.alloc(eg)); CK(c->uw_gwx.alloc(eg)); CK(c->uw_gwy.alloc(eg));
 	if (fem) CK(cudaMemset(c->uw_gmask.p, 1, eg));
 	// per particle, the stress points whose candidates hold it (ascending) and the slot
-	std::vector<uint32_t> toff(n + 1, 0), tgp(eg), tslot(eg);
-	for (uint64_t q = 0; q < eg; q++) toff[gnbr[q] + 1]++;
+	const uint64_t et = gnbr.size();  // stress-point candidates (the transposed entries)
+	std::vector<uint32_t> toff(n + 1, 0), tgp(et), tslot(et);
+	for (uint64_t q = 0; q < et; q++) toff[gnbr[q] + 1]++;
 	for (uint32_t j = 0; j < n; j++) toff[j + 1] += toff[j];
 	std::vector<uint32_t> fill(toff.begin(), toff.end() - 1);
 	for (uint32_t i = 0; i < ng; i++)
 		for (uint32_t q = goff[i]; q < goff[i + 1]; q++) {
 			uint32_t t = fill[gnbr[q]]++;
 			tgp[t] = i;
-			tslot[t] = q;
+			tslot[t] = gstart[i] + (q - goff[i]) * c->uw_gc_stride;
 		}
-	CK(c->uw_tp_off.alloc(n + 1)); CK(c->uw_tp_gp.alloc(eg)); CK(c->uw_tp_slot.alloc(eg));
+	CK(c->uw_tp_off.alloc(n + 1)); CK(c->uw_tp_gp.alloc(et)); CK(c->uw_tp_slot.alloc(et));
 	CK(cudaMemcpy(c->uw_tp_off.p, toff.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
-	if (eg) {
-		CK(cudaMemcpy(c->uw_tp_gp.p, tgp.data(), eg * 4, cudaMemcpyHostToDevice));
-		CK(cudaMemcpy(c->uw_tp_slot.p, tslot.data(), eg * 4, cudaMemcpyHostToDevice));
+	if (et) {
+		CK(cudaMemcpy(c->uw_tp_gp.p, tgp.data(), et * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_tp_slot.p, tslot.data(), et * 4, cudaMemcpyHostToDevice));
 	}
 	// boundary conditions: the rows' index into the value list
 	if ((st = upload_bcs(c))) return st;
@@ -1973,7 +2026,8 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 	const int wr = stage % 2 == 0 ? 2 : 3;
 	a.base = soa(0); a.acc = soa(1); a.rd = soa(rd); a.wr = soa(wr);
 	a.gbase = gsoa(0); a.gacc = gsoa(1); a.grd = gsoa(rd); a.gwr = gsoa(wr);
-	a.pc_off = c->uw_pc_off.p; a.pc_nbr = c->uw_pc_nbr.p; a.gc_off = c->uw_gc_off.p; a.gc_nbr = c->uw_gc_nbr.p;
+	a.pc = {c->uw_pc_off.p, c->uw_pc_cnt.p, c->uw_pc_nbr.p, c->uw_pc_stride};
+	a.gc = {c->uw_gc_off.p, c->uw_gc_cnt.p, c->uw_gc_nbr.p, c->uw_gc_stride};
 	a.pmask = c->uw_pmask.p; a.gmask = c->uw_gmask.p;
 	a.pw = c->uw_pw.p; a.pwx = c->uw_pwx.p; a.pwy = c->uw_pwy.p;
 	a.gw = c->uw_gw.p; a.gwx = c->uw_gwx.p; a.gwy = c->uw_gwy.p;
@@ -1991,11 +2045,11 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refresh_qw) {
 	// the mixed form reads the candidates' positions as float-float pairs
 	const bool mixed = c->uw_mixed && !c->strict;
-	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
-	               double* h, uint8_t* mask, double* w, double* wx, double* wy, const double* qs, double* qd) {
-		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
+	auto nbh = [&](uint32_t n_to, const double* tx, const double* ty, const mfk_host::SlotList& cand, double* h,
+	               uint8_t* mask, double* w, double* wx, double* wy, const double* qs, double* qd) {
+		return c->strict ? mf_strict::uw_nbh(n_to, tx, ty, cand, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy,
 		                                     qs, qd, nullptr, nullptr, c->d_status, c->stream)
-		                 : mf_fast::uw_nbh(n_to, tx, ty, off, nbr, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qs,
+		                 : mf_fast::uw_nbh(n_to, tx, ty, cand, a.rd.x, a.rd.y, a.m, a.rd.rho, h, mask, w, wx, wy, qs,
 		                                   qd, mixed ? c->uw_ff.p : nullptr, mixed ? c->uw_vol.p : nullptr,
 		                                   c->d_status, c->stream);
 	};
@@ -2007,9 +2061,9 @@ cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refr
 		if (e != cudaSuccess) return e;
 		c->launches++;
 	}
-	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc_off, a.pc_nbr, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy, qs, qd);
+	cudaError_t e = nbh(a.n_p, a.rd.x, a.rd.y, a.pc, c->uw_ph.p, a.pmask, a.pw, a.pwx, a.pwy, qs, qd);
 	if (e == cudaSuccess && points)
-		e = nbh(a.n_g, a.grd.x, a.grd.y, a.gc_off, a.gc_nbr, c->uw_gh.p, a.gmask, a.gw, a.gwx, a.gwy, nullptr, nullptr);
+		e = nbh(a.n_g, a.grd.x, a.grd.y, a.gc, c->uw_gh.p, a.gmask, a.gw, a.gwx, a.gwy, nullptr, nullptr);
 	return e;
 }
 
@@ -2245,7 +2299,8 @@ mf_ctx::~mf_ctx() {
 	cm_sw.free(); cm_swA.free(); cm_sX.free(); cm_swji.free(); cm_sW.free();
 	cm_U.free(); cm_X.free(); cm_V.free(); cm_P.free(); cm_R.free(); cm_H.free();
 	{
-		DevBuf<uint32_t>* uws[] = {&uw_gbody, &uw_pc_off, &uw_pc_nbr, &uw_gc_off, &uw_gc_nbr, &uw_tp_off, &uw_tp_gp,
+		DevBuf<uint32_t>* uws[] = {&uw_gbody, &uw_pc_off, &uw_pc_nbr, &uw_gc_off, &uw_gc_nbr, &uw_pc_cnt, &uw_gc_cnt,
+		                           &uw_tp_off, &uw_tp_gp,
 		                           &uw_tp_slot, &uw_bc_of, &uw_quads};
 		for (auto* p : uws) p->free();
 		uw_pmask.free(); uw_gmask.free(); uw_ff.free(); uw_vol.free();
@@ -3075,9 +3130,10 @@ MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uin
 		}
 		CK(cudaStreamSynchronize(c->stream));
 		uint64_t ec = c->uw_pc_nbr.n;
-		std::vector<uint32_t> off(n + 1), cand(ec);
+		std::vector<uint32_t> start(n + 1), cnt(n + 1), cand(ec);
 		std::vector<uint8_t> mask(ec);
-		CK(cudaMemcpy(off.data(), c->uw_pc_off.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(start.data(), c->uw_pc_off.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(cnt.data(), c->uw_pc_cnt.p, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
 		if (ec) {
 			CK(cudaMemcpy(cand.data(), c->uw_pc_nbr.p, ec * 4, cudaMemcpyDeviceToHost));
 			CK(cudaMemcpy(mask.data(), c->uw_pmask.p, ec, cudaMemcpyDeviceToHost));
@@ -3085,7 +3141,7 @@ MF_API mf_status mf_get_neighbors(mf_ctx* c, int32_t body, uint32_t* counts, uin
 		st = check_status(c);
 		if (st != MF_OK) return st;
 		for (uint32_t i = 0; i < n; i++) {
-			for (uint32_t q = off[i]; q < off[i + 1]; q++)
+			for (uint64_t k = 0, q = start[i]; k < cnt[i]; k++, q += c->uw_pc_stride)
 				if (mask[q]) all_idx.push_back(cand[q]);
 			all_counts[i] = (uint32_t)(all_idx.size() - offs[i]);
 			offs[i + 1] = all_idx.size();

@@ -219,8 +219,17 @@ struct WeakArgs {
 };
 
 // Weak updated-Lagrangian form (particle_ul_weak): particles and stress points, both
-// with fixed candidate lists (CSR, ascending) and, per derivative evaluation, the
+// with fixed candidate lists (ascending) and, per derivative evaluation, the
 // candidates inside the neighbour ellipse (mask) with their RKPM shape functions.
+//
+// A row's k-th candidate sits in slot start[i] + k * stride, k < cnt[i]; masks and
+// shape functions share the slots.  The ellipse lists are sliced (stride 32: the 32
+// rows of a slice interleaved, so the 32 rows of a warp reach their k-th slots in one
+// contiguous line); element maps keep rows contiguous (stride 1).
+struct SlotList {
+	const uint32_t *start, *cnt, *nbr;
+	uint32_t stride;
+};
 struct GSoA {
 	double *x, *y, *rho, *Sxx, *Sxy, *Syy;
 };
@@ -233,7 +242,7 @@ struct UWArgs {
 	double* qw_stage;                    // the particles' weights of this evaluation
 	StateSoA base, acc, rd, wr;          // particles: this stage reads rd, writes wr
 	GSoA gbase, gacc, grd, gwr;          // stress points
-	const uint32_t *pc_off, *pc_nbr, *gc_off, *gc_nbr;  // candidate lists
+	SlotList pc, gc;                     // candidate lists of the particles / stress points
 	uint8_t *pmask, *gmask;              // per candidate: inside this evaluation's ellipse
 	double *pw, *pwx, *pwy, *gw, *gwx, *gwy;  // per candidate: shape function and gradient
 	const uint32_t *tp_off, *tp_gp, *tp_slot;  // per particle: the stress points listing it, ascending
@@ -312,7 +321,7 @@ struct ContactArgs {
 	                      const uint32_t* sl_off, uint16_t* cnt, uint32_t* snbr, void* out64, void* out32,     \
 	                      const double* mul_row, const double* mul_nbr, cudaStream_t s);                      \
 	cudaError_t weak_stage(const mfk_host::WeakArgs& a, bool mixed, int part, cudaStream_t s);               \
-	cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr, \
+	cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const mfk_host::SlotList& cand,          \
 	                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,  \
 	                   uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,   \
 	                   const void* ff, const float* vol, void* status, cudaStream_t s);                     \

@@ -1,6 +1,7 @@
 // RKPM shape functions with a linear basis: compute_rkpm_correctors and
 // compute_rkpm_shape_function (precomp_shape_functions.h:31-173), in the reference's
-// operation order, for one query point over the entries q0..q1 of its neighbour list.
+// operation order, for one query point over the entries q0, q0 + stride, ... before q1
+// of its neighbour list.
 // Shared by the weak total-Lagrangian set-up and the per-stage shape functions of the
 // weak updated-Lagrangian form.
 #pragma once
@@ -26,11 +27,11 @@ template <class Rho, class Use, class Out>
 __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32_t q0, uint32_t q1,
                                          const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
                                          const double* __restrict__ fy, const double* __restrict__ fm, Rho rho, Use use,
-                                         Out out) {
+                                         Out out, uint32_t stride = 1) {
 	bool ok = true;
 	double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Mx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
 	       My[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [col][row]
-	for (uint32_t q = q0; q < q1; q++) {
+	for (uint32_t q = q0; q != q1; q += stride) {
 		if (!use(q)) continue;
 		uint32_t j = nbr[q];
 		double mj = fm[j], rhoj = rho(j);
@@ -97,7 +98,7 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 	}
 	solve(rx_, Cx);
 	solve(ry_, Cy);
-	for (uint32_t q = q0; q < q1; q++) {
+	for (uint32_t q = q0; q != q1; q += stride) {
 		if (!use(q)) continue;
 		uint32_t j = nbr[q];
 		double xj = fx[j], yj = fy[j];

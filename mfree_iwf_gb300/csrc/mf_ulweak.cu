@@ -47,14 +47,15 @@ enum : uint32_t {
 	A_JAUMANN_GP = 1u << 24,
 };
 
-// nbh_ellipse (neighbor_ellipse.h:62-127) of the query point (px, py) over its
-// candidates q0..q1, FP64: h = half the farthest candidate's distance, mask[q] = 1 for
-// the candidates inside the ellipse; returns their number.
-__device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0, uint32_t q1,
+// nbh_ellipse (neighbor_ellipse.h:62-127) of the query point (px, py) over its nq
+// candidates in slots q0, q0 + stride, ..., FP64: h = half the farthest candidate's
+// distance, mask[q] = 1 for the candidates inside the ellipse; returns their number.
+__device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0, uint32_t nq, uint32_t stride,
                                               const uint32_t* __restrict__ nbr, const double* __restrict__ fx,
                                               const double* __restrict__ fy, double& h_row, uint8_t* mask) {
+	const uint32_t q1 = q0 + nq * stride;
 	double Hxx = 0., Hxy = 0., Hyx = 0., Hyy = 0., h = 0.;
-	for (uint32_t q = q0; q < q1; q++) {
+	for (uint32_t q = q0; q != q1; q += stride) {
 		uint32_t j = nbr[q];
 		double dx = px - fx[j], dy = py - fy[j];
 		double r2 = dx * dx + dy * dy;
@@ -66,7 +67,7 @@ __device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0,
 	h /= 2;
 	h_row = h;
 	// eigen (neighbor_ellipse.h:29-60) of A = (Hxx, Hyx; Hxy, Hyy) / n, columns first
-	const double nc = (double)(q1 - q0);
+	const double nc = (double)nq;
 	const double A00 = Hxx / nc, A01 = Hyx / nc, A10 = Hxy / nc, A11 = Hyy / nc;
 	double D0, D1, rax, ray;
 	if (fabs(A10) < 1e-9 && fabs(A01) < 1e-9) {
@@ -95,7 +96,7 @@ __device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0,
 	const double cs = rax, sn = ray, ia = 1. / a, ib = 1. / b;
 #endif
 	uint32_t cnt = 0;
-	for (uint32_t q = q0; q < q1; q++) {
+	for (uint32_t q = q0; q != q1; q += stride) {
 		uint32_t j = nbr[q];
 		double xc = fx[j] - px, yc = fy[j] - py;
 #if MF_STRICT_FORM
@@ -117,23 +118,23 @@ __device__ __forceinline__ uint32_t ellipse64(double px, double py, uint32_t q0,
 // integration weight for the passes: m / rho (riemann_update_integration_weights) when
 // qw_src is null, else qw_src (the weights of the last update).
 __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
-                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr,
-                         const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
+                         const mfk_host::SlotList cand, const double* __restrict__ fx, const double* __restrict__ fy, const double* __restrict__ fm,
                          const double* __restrict__ frho, double* h_out, uint8_t* mask, double* w, double* wx,
                          double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n_to) return;
 	const double px = tx[i], py = ty[i];
-	const uint32_t q0 = off[i], q1 = off[i + 1];
+	const uint32_t q0 = cand.start[i], nq = cand.cnt[i], S = cand.stride;
+	const uint32_t* __restrict__ nbr = cand.nbr;
 	double h;
-	const uint32_t cnt = ellipse64(px, py, q0, q1, nbr, fx, fy, h, mask);
+	const uint32_t cnt = ellipse64(px, py, q0, nq, S, nbr, fx, fy, h, mask);
 	h_out[i] = h;
 	if (cnt == 0) raise(st, ERR_NO_NEIGHBOR, i);
 	if (qw_dst) qw_dst[i] = qw_src ? qw_src[i] : fm[i] / frho[i];
 	auto rho = [&](uint32_t j) { return frho[j]; };
 	auto use = [&](uint32_t q) { return mask[q] != 0; };
 	auto out = [&](uint32_t q, double ww, double wwx, double wwy) { w[q] = ww; wx[q] = wwx; wy[q] = wwy; };
-	if (!rkpm_row(px, py, h, q0, q1, nbr, fx, fy, fm, rho, use, out)) raise(st, ERR_SINGULAR, i);
+	if (!rkpm_row(px, py, h, q0, q0 + nq * S, nbr, fx, fy, fm, rho, use, out, S)) raise(st, ERR_SINGULAR, i);
 }
 
 // The stage's particle positions as float-float pairs (x = hi + lo to 48 bits) and
@@ -148,26 +149,26 @@ __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* 
 	vol[i] = (float)m[i] / (float)rho[i];
 }
 
-// Candidates q0..q1 in batches of four while cont() holds: a batch's list entries and
-// float-float positions are all loaded before f(q, j, position) runs on any of them, so
-// a thread keeps four gathers in flight.
+// The nq candidates in slots q0, q0 + S, ... in batches of four while cont() holds: a
+// batch's list entries and float-float positions are all loaded before f(k, q, j,
+// position) runs on any of them, so a thread keeps four gathers in flight.
 template <class F, class Cont>
-__device__ __forceinline__ void cand4(uint32_t q0, uint32_t q1, const uint32_t* __restrict__ nbr,
+__device__ __forceinline__ void cand4(uint32_t q0, uint32_t nq, uint32_t S, const uint32_t* __restrict__ nbr,
                                       const float4* __restrict__ ff, F f, Cont cont) {
-	uint32_t q = q0;
-	for (; q + 4 <= q1 && cont(); q += 4) {
+	uint32_t k = 0;
+	for (; k + 4 <= nq && cont(); k += 4) {
 		uint32_t j[4];
 		float4 v[4];
 #pragma unroll
-		for (int u = 0; u < 4; u++) j[u] = nbr[q + u];
+		for (int u = 0; u < 4; u++) j[u] = nbr[q0 + (k + u) * S];
 #pragma unroll
 		for (int u = 0; u < 4; u++) v[u] = ff[j[u]];
 #pragma unroll
-		for (int u = 0; u < 4; u++) f(q + u, j[u], v[u]);
+		for (int u = 0; u < 4; u++) f(k + u, q0 + (k + u) * S, j[u], v[u]);
 	}
-	for (; q < q1 && cont(); q++) {
-		const uint32_t j = nbr[q];
-		f(q, j, ff[j]);
+	for (; k < nq && cont(); k++) {
+		const uint32_t q = q0 + k * S, j = nbr[q];
+		f(k, q, j, ff[j]);
 	}
 }
 
@@ -194,7 +195,7 @@ __device__ __forceinline__ void cand4(uint32_t q0, uint32_t q1, const uint32_t* 
 // h, or one within FP32 rounding of it where two candidates tie in FP32).
 __global__ void __launch_bounds__(128)
     k_uw_nbh32(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
-               const uint32_t* __restrict__ off, const uint32_t* __restrict__ nbr, const float4* __restrict__ ff,
+               const mfk_host::SlotList cand, const float4* __restrict__ ff,
                const float* __restrict__ vol, const double* __restrict__ fx, const double* __restrict__ fy,
                const double* __restrict__ fm, const double* __restrict__ frho, double* h_out, uint8_t* mask,
                double* w, double* wx, double* wy, const double* __restrict__ qw_src, double* qw_dst, DevStatus* st) {
@@ -208,19 +209,20 @@ __global__ void __launch_bounds__(128)
 	auto offs = [&](const float4 f) {  // x_i - x_j from j's float-float position
 		return make_float2((pxh - f.x) + (pxl - f.y), (pyh - f.z) + (pyl - f.w));
 	};
-	const uint32_t q0 = off[i], q1 = off[i + 1];
+	const uint32_t q0 = cand.start[i], nq = cand.cnt[i], S = cand.stride;
+	const uint32_t* __restrict__ nbr = cand.nbr;
 	float Hxx = 0.f, Hxy = 0.f, Hyy = 0.f, r2m = -1.f;
 	uint32_t jm = 0;  // the candidate farthest in FP32
 	cand4(
-	    q0, q1, nbr, ff,
-	    [&](uint32_t, uint32_t j, float4 v) {
+	    q0, nq, S, nbr, ff,
+	    [&](uint32_t, uint32_t, uint32_t j, float4 v) {
 		    const float2 d = offs(v);
 		    const float r2 = d.x * d.x + d.y * d.y;
 		    if (r2 > r2m) { r2m = r2; jm = j; }
 		    Hxx += d.x * d.x; Hxy += d.x * d.y; Hyy += d.y * d.y;
 	    },
 	    [] { return true; });
-	const float nf = (float)(q1 - q0);
+	const float nf = (float)nq;
 	const float A00 = Hxx / nf, A01 = Hxy / nf, A11 = Hyy / nf, T = A00 + A11;
 	const float e = (nf + 8.f) * U * T;  // bound on each entry's error
 	// the reference's branch: axis-aligned when |A01| < 1e-9
@@ -259,8 +261,8 @@ __global__ void __launch_bounds__(128)
 	uint32_t cnt = 0;
 	uint64_t bits = 0;  // the selection of the first 64 candidates
 	cand4(
-	    q0, q1, nbr, ff,
-	    [&](uint32_t q, uint32_t j, float4 v) {
+	    q0, nq, S, nbr, ff,
+	    [&](uint32_t kk, uint32_t q, uint32_t j, float4 v) {
 		    const float2 d = offs(v);
 		    const float left = cs * d.x + sn * d.y, right = sn * d.x - cs * d.y;
 		    const float s = left * left * ia2 + right * right * ib2;
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(128)
 		    mask[q] = in ? 1 : 0;
 		    if (in) {
 			    cnt++;
-			    if (q - q0 < 64) bits |= 1ull << (q - q0);
+			    if (kk < 64) bits |= 1ull << kk;
 			    k.add(d.x, d.y, vol[j]);
 		    }
 	    },
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
 			for (int u = 0; u < 4; u++)
 				if (b) {
-					qs[u] = q0 + (uint32_t)(__ffsll((long long)b) - 1);
+					qs[u] = q0 + (uint32_t)(__ffsll((long long)b) - 1) * S;
 					b &= b - 1;
 					nb = u + 1;
 				}
@@ -299,18 +301,20 @@ __global__ void __launch_bounds__(128)
 			for (int u = 0; u < 4; u++)
 				if (u < nb) g(qs[u], offs(vs[u]));
 		}
-		for (uint32_t q = q0 + 64; q < q1; q++)
+		for (uint32_t kk = 64; kk < nq; kk++) {
+			const uint32_t q = q0 + kk * S;
 			if (mask[q]) g(q, offs(ff[nbr[q]]));
+		}
 	};
 	if (!sure) {
-		cnt = ellipse64(px, py, q0, q1, nbr, fx, fy, h, mask);
+		cnt = ellipse64(px, py, q0, nq, S, nbr, fx, fy, h, mask);
 		bits = 0;
-		for (uint32_t q = q0; q < q1 && q - q0 < 64; q++)
-			if (mask[q]) bits |= 1ull << (q - q0);
+		for (uint32_t kk = 0; kk < nq && kk < 64; kk++)
+			if (mask[q0 + kk * S]) bits |= 1ull << kk;
 		k.init(h);
 		// the moments in slot order again (each's offsets; the volumes by slot)
-		for (uint32_t q = q0; q < q1; q++)
-			if (mask[q]) {
+		for (uint32_t kk = 0; kk < nq; kk++)
+			if (const uint32_t q = q0 + kk * S; mask[q]) {
 				const uint32_t j = nbr[q];
 				const float2 d = offs(ff[j]);
 				k.add(d.x, d.y, vol[j]);
@@ -354,9 +358,10 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 	const double qw = (flags & mfk_host::FLAG_UW_RIEMANN_GP) ? a.gm[i] / rho : a.gqw_base[i];
 	const double p = (flags & A_EOS_GP) ? pr.c0sq * (rho - pr.rho0) : 0.;
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0., vxi = 0., vyi = 0.;
-	for (uint32_t q = a.gc_off[i]; q < a.gc_off[i + 1]; q++) {
+	const uint32_t q1 = a.gc.start[i] + a.gc.cnt[i] * a.gc.stride;
+	for (uint32_t q = a.gc.start[i]; q != q1; q += a.gc.stride) {
 		if (!a.gmask[q]) continue;
-		uint32_t j = a.gc_nbr[q];
+		uint32_t j = a.gc.nbr[q];
 		double vxj = a.rd.vx[j], vyj = a.rd.vy[j], qwj = p_qw(a, j);
 #if MF_STRICT_FORM
 		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
@@ -428,9 +433,10 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 	}
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
 	if (flags & A_DERIVE_VEL) {
-		for (uint32_t q = a.pc_off[j]; q < a.pc_off[j + 1]; q++) {
+		const uint32_t q1 = a.pc.start[j] + a.pc.cnt[j] * a.pc.stride;
+		for (uint32_t q = a.pc.start[j]; q != q1; q += a.pc.stride) {
 			if (!a.pmask[q]) continue;
-			uint32_t k = a.pc_nbr[q];
+			uint32_t k = a.pc.nbr[q];
 			double qwk = p_qw(a, k);
 #if MF_STRICT_FORM
 			vx_x += (s.vx[k] - vxj) * a.pwx[q] * qwk;
@@ -478,9 +484,10 @@ __global__ void k_uw_smooth(UWArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_p) return;
 	double vsx = 0., vsy = 0.;
-	for (uint32_t q = a.pc_off[i]; q < a.pc_off[i + 1]; q++) {
+	const uint32_t q1 = a.pc.start[i] + a.pc.cnt[i] * a.pc.stride;
+	for (uint32_t q = a.pc.start[i]; q != q1; q += a.pc.stride) {
 		if (!a.pmask[q]) continue;
-		uint32_t k = a.pc_nbr[q];
+		uint32_t k = a.pc.nbr[q];
 		vsx += a.base.vx[k] * a.pw[q] * a.qw_base[k];
 		vsy += a.base.vy[k] * a.pw[q] * a.qw_base[k];
 	}
@@ -497,17 +504,17 @@ __global__ void k_uw_smooth_copy(UWArgs a) {
 
 }  // namespace
 
-cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const uint32_t* off, const uint32_t* nbr,
+cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const mfk_host::SlotList& cand,
                    const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,
                    uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,
                    const void* ff, const float* vol, void* status, cudaStream_t s) {
 	if (n_to == 0) return cudaSuccess;
 	if (ff)
-		k_uw_nbh32<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, reinterpret_cast<const float4*>(ff), vol,
+		k_uw_nbh32<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, cand, reinterpret_cast<const float4*>(ff), vol,
 		                                            fx, fy, fm, frho, h_out, mask, w, wx, wy, qw_src, qw_dst,
 		                                            reinterpret_cast<DevStatus*>(status));
 	else
-		k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, off, nbr, fx, fy, fm, frho, h_out, mask, w, wx, wy,
+		k_uw_nbh<<<grid1(n_to, 128), 128, 0, s>>>(n_to, tx, ty, cand, fx, fy, fm, frho, h_out, mask, w, wx, wy,
 		                                          qw_src, qw_dst, reinterpret_cast<DevStatus*>(status));
 	return cudaGetLastError();
 }
