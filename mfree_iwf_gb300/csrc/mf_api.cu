@@ -288,7 +288,7 @@ struct mf_ctx {
 	// UL_WEAK: stress points (state sets as the particles: base, accumulator, two stage
 	// sets), fixed candidate lists, per-evaluation ellipse masks and shape functions
 	DevBuf<uint32_t> uw_gbody, uw_pc_off, uw_pc_nbr, uw_gc_off, uw_gc_nbr, uw_tp_off, uw_tp_gp, uw_tp_slot, uw_bc_of;
-	DevBuf<uint32_t> uw_pc_cnt, uw_gc_cnt;  // candidates per row; *_off hold the rows' first slots
+	DevBuf<uint32_t> uw_pc_cnt, uw_gc_cnt, uw_tp_cnt;  // entries per row; *_off hold the rows' first slots
 	uint32_t uw_pc_stride = 1, uw_gc_stride = 1;
 	DevBuf<uint8_t> uw_pmask, uw_gmask;
 	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
@@ -1987,11 +1987,17 @@ mf_status uw_setup(mf_ctx* c) {
 			tgp[t] = i;
 			tslot[t] = gstart[i] + (q - goff[i]) * c->uw_gc_stride;
 		}
-	CK(c->uw_tp_off.alloc(n + 1)); CK(c->uw_tp_gp.alloc(et)); CK(c->uw_tp_slot.alloc(et));
-	CK(cudaMemcpy(c->uw_tp_off.p, toff.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
-	if (et) {
-		CK(cudaMemcpy(c->uw_tp_gp.p, tgp.data(), et * 4, cudaMemcpyHostToDevice));
-		CK(cudaMemcpy(c->uw_tp_slot.p, tslot.data(), et * 4, cudaMemcpyHostToDevice));
+	// sliced like the candidate lists (the particle pass walks them one row per thread)
+	std::vector<uint32_t> tstart, tcnt, tgp_sl, tslot_sl;
+	if (!slice_lists(toff, tgp, n, tstart, tcnt, tgp_sl) || !slice_lists(toff, tslot, n, tstart, tcnt, tslot_sl))
+		return fail(c, MF_ERR_CAPACITY, "weak UL transposed slots exceed 2^32");
+	CK(c->uw_tp_off.alloc(n + 1)); CK(c->uw_tp_cnt.alloc(n + 1));
+	CK(c->uw_tp_gp.alloc(tgp_sl.size())); CK(c->uw_tp_slot.alloc(tslot_sl.size()));
+	CK(cudaMemcpy(c->uw_tp_off.p, tstart.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(c->uw_tp_cnt.p, tcnt.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+	if (!tgp_sl.empty()) {
+		CK(cudaMemcpy(c->uw_tp_gp.p, tgp_sl.data(), tgp_sl.size() * 4, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->uw_tp_slot.p, tslot_sl.data(), tslot_sl.size() * 4, cudaMemcpyHostToDevice));
 	}
 	// boundary conditions: the rows' index into the value list
 	if ((st = upload_bcs(c))) return st;
@@ -2031,7 +2037,8 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 	a.pmask = c->uw_pmask.p; a.gmask = c->uw_gmask.p;
 	a.pw = c->uw_pw.p; a.pwx = c->uw_pwx.p; a.pwy = c->uw_pwy.p;
 	a.gw = c->uw_gw.p; a.gwx = c->uw_gwx.p; a.gwy = c->uw_gwy.p;
-	a.tp_off = c->uw_tp_off.p; a.tp_gp = c->uw_tp_gp.p; a.tp_slot = c->uw_tp_slot.p;
+	a.tp = {c->uw_tp_off.p, c->uw_tp_cnt.p, c->uw_tp_gp.p, 32};
+	a.tp_slot = c->uw_tp_slot.p;
 	a.gsig = c->uw_gsig.p; a.bc_of = c->uw_bc_of.p; a.bc_v = c->bc_v.p;
 	a.status = c->d_status;
 	return a;
@@ -2300,7 +2307,7 @@ mf_ctx::~mf_ctx() {
 	cm_U.free(); cm_X.free(); cm_V.free(); cm_P.free(); cm_R.free(); cm_H.free();
 	{
 		DevBuf<uint32_t>* uws[] = {&uw_gbody, &uw_pc_off, &uw_pc_nbr, &uw_gc_off, &uw_gc_nbr, &uw_pc_cnt, &uw_gc_cnt,
-		                           &uw_tp_off, &uw_tp_gp,
+		                           &uw_tp_off, &uw_tp_cnt, &uw_tp_gp,
 		                           &uw_tp_slot, &uw_bc_of, &uw_quads};
 		for (auto* p : uws) p->free();
 		uw_pmask.free(); uw_gmask.free(); uw_ff.free(); uw_vol.free();

@@ -245,7 +245,8 @@ struct UWArgs {
 	SlotList pc, gc;                     // candidate lists of the particles / stress points
 	uint8_t *pmask, *gmask;              // per candidate: inside this evaluation's ellipse
 	double *pw, *pwx, *pwy, *gw, *gwx, *gwy;  // per candidate: shape function and gradient
-	const uint32_t *tp_off, *tp_gp, *tp_slot;  // per particle: the stress points listing it, ascending
+	SlotList tp;                         // per particle: the stress points listing it, ascending (sliced)
+	const uint32_t* tp_slot;             // their candidate slots, in tp's slots
 	double* gsig;                        // per stress point: Sxx - p, Sxy, Syy - p, quad weight
 	const uint32_t* bc_of;               // per particle: index into bc_v, or ~0u
 	const double* bc_v;

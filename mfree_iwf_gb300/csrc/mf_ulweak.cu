@@ -414,10 +414,11 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 	double Sxx_x = 0., Sxy_y = 0., Sxy_x = 0., Syy_y = 0.;
 	if (flags & mfk_host::FLAG_UW_STRESS) {
 		const uint32_t ng = a.n_g;
-		for (uint32_t t = a.tp_off[j]; t < a.tp_off[j + 1]; t++) {
+		const uint32_t t1 = a.tp.start[j] + a.tp.cnt[j] * a.tp.stride;
+		for (uint32_t t = a.tp.start[j]; t != t1; t += a.tp.stride) {
 			uint32_t q = a.tp_slot[t];
 			if (!a.gmask[q]) continue;
-			uint32_t gi = a.tp_gp[t];
+			uint32_t gi = a.tp.nbr[t];
 			double Sxxi = a.gsig[gi], Sxyi = a.gsig[ng + gi], Syyi = a.gsig[2 * ng + gi], qwi = a.gsig[3 * ng + gi];
 #if MF_STRICT_FORM
 			Sxx_x -= Sxxi * a.gwx[q] * qwi * qwj;
