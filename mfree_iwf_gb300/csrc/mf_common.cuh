@@ -78,13 +78,20 @@ MF_DEV KR64 cubic_spline(double xij, double yij, double h) {
 // precomputed per particle, 1/r through rsqrt.
 // float -> double by integer operations, exact: the sign and the 23 mantissa bits move
 // across and the exponent is re-biased (127 -> 1023); zeros, infinities and NaNs keep
-// their class, subnormal floats take the hardware conversion.  Conversions to and from
-// FP64 issue on the FP64 pipe, GB300's narrowest.
+// their class; a subnormal float's mantissa is normalised (its leading one shifted to
+// the implicit bit, the exponent lowered by the shift).  Conversions to and from FP64
+// issue on the FP64 pipe, GB300's narrowest, so none is used here.
 MF_DEV double f2d(float f) {
 	const uint32_t u = __float_as_uint(f);
-	const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-	if (e == 0u && m != 0u) return (double)f;
-	const uint32_t e64 = e == 0u ? 0u : (e == 255u ? 2047u : e + 896u);
+	const uint32_t e = (u >> 23) & 0xffu;
+	uint32_t m = u & 0x7fffffu, e64;
+	if (e == 0u) {
+		const uint32_t sh = m ? (uint32_t)__clz(m) - 8u : 0u;  // 1..23 for a subnormal
+		e64 = m ? 897u - sh : 0u;
+		m = (m << sh) & 0x7fffffu;
+	} else {
+		e64 = e == 255u ? 2047u : e + 896u;
+	}
 	return __hiloint2double((int)((u & 0x80000000u) | (e64 << 20) | (m >> 3)), (int)(m << 29));
 }
 
