@@ -5,12 +5,15 @@
 //
 // Set-up (host side): candidate lists of the particles and of the stress points among
 // the particles (find_neighbors with distance_manhattan, neighbor_search.h:84-180), and
-// per particle the stress points whose candidates hold it, ascending.
+// per particle the stress points whose candidates hold it, ascending; all sliced by 32
+// rows (mfk_host::SlotList).
 //
 // Per derivative evaluation:
 //   k_uw_nbh  (particles, then stress points)  nbh_ellipse (neighbor_ellipse.h:62-127):
 //             h and the candidates inside the ellipse, then precomp_rkpm over those
-//             (precomp_shape_functions.h:143-208)
+//             (precomp_shape_functions.h:143-208); the mixed form runs k_uw_ff (the
+//             stage's float-float positions and FP32 volumes) and k_uw_nbh32 (the
+//             ellipse in FP32 within a derived error bound, else FP64; FP32 moments)
 //   k_uw_gp   per stress point: integration weight, EOS, velocity gradient
 //             (derivatives.h:68-99), Jaumann rate, continuity, interpolated velocity
 //             (interpolation.h:32-59) and advection, its stress for the particles,
