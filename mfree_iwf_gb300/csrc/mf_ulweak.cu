@@ -192,9 +192,9 @@ __device__ __forceinline__ void cand4(uint32_t q0, uint32_t nq, uint32_t S, cons
 // is within e + 3u T, the larger within e + 3u T relative to T / 2, and the axis
 // within 2e / (l2 - l1) + 5u radians, whose effect on s is at most s (l2 - l1) / l1
 // per radian; together |s32 - s64| <= (3n + 48) u s T / l1.  The kernel's margin is
-// twice the bound: a candidate with |s32 - 1| inside it, an |A01| within e of the
-// 1e-9 threshold, or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the
-// row to ellipse64.  h is the FP64 distance of the candidate farthest in FP32 (FP64's
+// twice the bound: a candidate with |s32 - 1| inside it, an FP64 |A01| within its
+// rounding spread of the 1e-9 threshold (summed in FP64 when FP32's is within e of it),
+// or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the row to ellipse64.  h is the FP64 distance of the candidate farthest in FP32 (FP64's
 // h, or one within FP32 rounding of it where two candidates tie in FP32).
 __global__ void __launch_bounds__(128)
     k_uw_nbh32(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
@@ -228,11 +228,27 @@ __global__ void __launch_bounds__(128)
 	const float nf = (float)nq;
 	const float A00 = Hxx / nf, A01 = Hxy / nf, A11 = Hyy / nf, T = A00 + A11;
 	const float e = (nf + 8.f) * U * T;  // bound on each entry's error
-	// the reference's branch: axis-aligned when |A01| < 1e-9
+	// the reference's branch: axis-aligned when |A01| < 1e-9.  Where FP32 cannot tell
+	// (an absolute threshold: at coarse spacings e exceeds it, and a symmetric
+	// neighbourhood has A01 ~ 0), A01 itself is summed in FP64 as the FP64 form sums it;
+	// an FP64 A01 closer to the threshold than that sum's own rounding spread (at most
+	// (n + 2) 2^-53 T / 2 for n <= ~100 candidates, taken as 1e-14 T) stays undecided.
 	const double a01 = fabs((double)A01);
-	bool sure = T > 0.f && (a01 + e < 1e-9 || a01 - e >= 1e-9);
+	bool branch = a01 + e < 1e-9 || a01 - e >= 1e-9, axis = a01 < 1e-9;
+	if (!branch && T > 0.f) {
+		double hxy = 0.;
+		for (uint32_t kk = 0, q = q0; kk < nq; kk++, q += S) {
+			const uint32_t j = nbr[q];
+			const double dx = px - fx[j], dy = py - fy[j];
+			hxy += dx * dy;
+		}
+		const double a01d = fabs(hxy / (double)nq);
+		branch = fabs(a01d - 1e-9) > 1e-15 + 1e-14 * (double)T;
+		axis = a01d < 1e-9;
+	}
+	bool sure = T > 0.f && branch;
 	float cs, sn, ia2, ib2, bound;
-	if (a01 < 1e-9) {
+	if (axis) {
 		cs = 1.f; sn = 0.f;
 		ia2 = 1.f / (K2 * A00); ib2 = 1.f / (K2 * A11);
 		bound = nf + 19.f;
