@@ -95,6 +95,28 @@ MF_DEV double f2d(float f) {
 	return __hiloint2double((int)((u & 0x80000000u) | (e64 << 20) | (m >> 3)), (int)(m << 29));
 }
 
+// double -> float for a double that holds an FP32 value exactly (an f2d result), by
+// integer operations: the exponent re-biased, the mantissa's 23 leading bits kept;
+// doubles below FP32's normal range become the FP32 subnormal of the same value.
+MF_DEV float d2f_exact(double d) {
+	const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+	const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+	const uint32_t e = (hi >> 20) & 0x7ffu;
+	uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29), e32;
+	if (e == 0u) {
+		e32 = 0u;
+		m = 0u;
+	} else if (e == 2047u) {
+		e32 = 255u;
+	} else if (e >= 897u) {
+		e32 = e - 896u;
+	} else {  // an FP32 subnormal: the implicit bit shifted into the mantissa
+		e32 = 0u;
+		m = e > 873u ? (0x800000u | m) >> (897u - e) : 0u;
+	}
+	return __uint_as_float((hi & 0x80000000u) | (e32 << 23) | m);
+}
+
 struct KR32 {
 	float w, w_x, w_y;
 };

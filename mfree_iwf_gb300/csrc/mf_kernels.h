@@ -248,6 +248,11 @@ struct UWArgs {
 	SlotList tp;                         // per particle: the stress points listing it, ascending (sliced)
 	const uint32_t* tp_slot;             // their candidate slots, in tp's slots
 	double* gsig;                        // per stress point: Sxx - p, Sxy, Syy - p, quad weight
+	// mixed form (null otherwise): the particles' float-float velocities and FP32
+	// weights of the evaluation, the stress points' gsig in FP32
+	const float4* vff;
+	const float* qw32;
+	float4* gsig32;
 	const uint32_t* bc_of;               // per particle: index into bc_v, or ~0u
 	const double* bc_v;
 	void* status;
@@ -326,8 +331,9 @@ struct ContactArgs {
 	                   const double* fx, const double* fy, const double* fm, const double* frho, double* h_out,  \
 	                   uint8_t* mask, double* w, double* wx, double* wy, const double* qw_src, double* qw_dst,   \
 	                   const void* ff, const float* vol, void* status, cudaStream_t s);                     \
-	cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* m, const double* rho, void* ff, \
-	                  float* vol, cudaStream_t s);                                                          \
+	cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* vx, const double* vy,           \
+	                  const double* m, const double* rho, const double* qw_src, double* qw_dst, void* ff,      \
+	                  void* vff, float* vol, float* qw32, cudaStream_t s);                                  \
 	cudaError_t uw_stage(const mfk_host::UWArgs& a, int part, cudaStream_t s);                                \
 	}
 

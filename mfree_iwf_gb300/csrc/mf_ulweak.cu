@@ -140,16 +140,23 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 	if (!rkpm_row(px, py, h, q0, q0 + nq * S, nbr, fx, fy, fm, rho, use, out, S)) raise(st, ERR_SINGULAR, i);
 }
 
-// The stage's particle positions as float-float pairs (x = hi + lo to 48 bits) and
-// their FP32 volumes m / rho, for the mixed form's neighbourhood kernel.
+// The mixed form's per-particle inputs of one derivative evaluation: the stage's
+// positions and velocities as float-float pairs (x = hi + lo to 48 bits), the FP32
+// volumes m / rho, and the particles' integration weights of the evaluation (qw_src, or
+// m / rho without it: riemann_update_integration_weights) in FP64 and FP32.
 __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
-                        const double* __restrict__ m, const double* __restrict__ rho, float4* ff, float* vol) {
+                        const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ m,
+                        const double* __restrict__ rho, const double* __restrict__ qw_src, double* qw_dst,
+                        float4* ff, float4* vff, float* vol, float* qw32) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
-	const double xi = x[i], yi = y[i];
-	const float xh = (float)xi, yh = (float)yi;
-	ff[i] = make_float4(xh, (float)(xi - (double)xh), yh, (float)(yi - (double)yh));
+	const FF px = ff_split(x[i]), py = ff_split(y[i]), pvx = ff_split(vx[i]), pvy = ff_split(vy[i]);
+	ff[i] = make_float4(px.hi, px.lo, py.hi, py.lo);
+	vff[i] = make_float4(pvx.hi, pvx.lo, pvy.hi, pvy.lo);
 	vol[i] = (float)m[i] / (float)rho[i];
+	const double qw = qw_src ? qw_src[i] : m[i] / rho[i];
+	qw_dst[i] = qw;
+	qw32[i] = (float)qw;
 }
 
 // The nq candidates in slots q0, q0 + S, ... in batches of four while cont() holds: a
@@ -416,12 +423,52 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 	a.gsig[n + i] = Sxy;
 	a.gsig[2 * n + i] = Syy - p;
 	a.gsig[3 * n + i] = qw;
+	if (a.gsig32) a.gsig32[i] = make_float4((float)(Sxx - p), (float)Sxy, (float)(Syy - p), (float)qw);
 	double* bp[6] = {a.gbase.x, a.gbase.y, a.gbase.rho, a.gbase.Sxx, a.gbase.Sxy, a.gbase.Syy};
 	double* ap[6] = {a.gacc.x, a.gacc.y, a.gacc.rho, a.gacc.Sxx, a.gacc.Sxy, a.gacc.Syy};
 	double* wp[6] = {a.gwr.x, a.gwr.y, a.gwr.rho, a.gwr.Sxx, a.gwr.Sxy, a.gwr.Syy};
 	uw_rk(a.stage, pr.dt, i, 6, bp, ap, wp, d);
 }
 
+// The mixed form's sums of k_uw_p in FP32: the stress divergence from the stress points'
+// FP32 stress and weights (gsig32), the velocity gradient from float-float velocity
+// differences; the shape-function gradients are the FP32 values the mixed
+// neighbourhood kernel stored (as FP64, read back exactly).  Both feed FP64 rates.
+__device__ __forceinline__ void uw_p_sums32(const UWArgs& a, uint32_t j, uint32_t flags, double& Sxx_x, double& Sxy_y,
+                                            double& Sxy_x, double& Syy_y, double& vx_x, double& vx_y, double& vy_x,
+                                            double& vy_y) {
+	const float qwj = a.qw32[j];
+	float sxx_x = 0.f, sxy_y = 0.f, sxy_x = 0.f, syy_y = 0.f;
+	if (flags & mfk_host::FLAG_UW_STRESS) {
+		const uint32_t t1 = a.tp.start[j] + a.tp.cnt[j] * a.tp.stride;
+		for (uint32_t t = a.tp.start[j]; t != t1; t += a.tp.stride) {
+			const uint32_t q = a.tp_slot[t];
+			if (!a.gmask[q]) continue;
+			const float4 g = a.gsig32[a.tp.nbr[t]];  // Sxx - p, Sxy, Syy - p, qw
+			const float c = g.w * qwj, tx = d2f_exact(a.gwx[q]) * c, ty = d2f_exact(a.gwy[q]) * c;
+			sxx_x -= g.x * tx; sxy_y -= g.y * ty;
+			sxy_x -= g.y * tx; syy_y -= g.z * ty;
+		}
+	}
+	float lxx = 0.f, lxy = 0.f, lyx = 0.f, lyy = 0.f;
+	if (flags & A_DERIVE_VEL) {
+		const float4 vj = a.vff[j];
+		const uint32_t q1 = a.pc.start[j] + a.pc.cnt[j] * a.pc.stride;
+		for (uint32_t q = a.pc.start[j]; q != q1; q += a.pc.stride) {
+			if (!a.pmask[q]) continue;
+			const uint32_t k = a.pc.nbr[q];
+			const float4 vk = a.vff[k];
+			const float qwk = a.qw32[k], tx = d2f_exact(a.pwx[q]) * qwk, ty = d2f_exact(a.pwy[q]) * qwk;
+			const float dvx = (vk.x - vj.x) + (vk.y - vj.y), dvy = (vk.z - vj.z) + (vk.w - vj.w);
+			lxx += dvx * tx; lxy += dvx * ty;
+			lyx += dvy * tx; lyy += dvy * ty;
+		}
+	}
+	Sxx_x = f2d(sxx_x); Sxy_y = f2d(sxy_y); Sxy_x = f2d(sxy_x); Syy_y = f2d(syy_y);
+	vx_x = f2d(lxx); vx_y = f2d(lxy); vy_x = f2d(lyx); vy_y = f2d(lyy);
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 	uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
 	if (j >= a.n_p) return;
@@ -429,8 +476,12 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 	const BodyParams& pr = a.params[a.body_of[j]];
 	const mfk_host::StateSoA& s = a.rd;
 	const double rho = s.rho[j], m = a.m[j], vxj = s.vx[j], vyj = s.vy[j];
-	const double qwj = p_qw(a, j);
 	double Sxx_x = 0., Sxy_y = 0., Sxy_x = 0., Syy_y = 0.;
+	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
+	if (MIXED) {
+		uw_p_sums32(a, j, flags, Sxx_x, Sxy_y, Sxy_x, Syy_y, vx_x, vx_y, vy_x, vy_y);
+	} else {
+	const double qwj = p_qw(a, j);
 	if (flags & mfk_host::FLAG_UW_STRESS) {
 		const uint32_t ng = a.n_g;
 		const uint32_t t1 = a.tp.start[j] + a.tp.cnt[j] * a.tp.stride;
@@ -451,7 +502,6 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 #endif
 		}
 	}
-	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0.;
 	if (flags & A_DERIVE_VEL) {
 		const uint32_t q1 = a.pc.start[j] + a.pc.cnt[j] * a.pc.stride;
 		for (uint32_t q = a.pc.start[j]; q != q1; q += a.pc.stride) {
@@ -470,6 +520,7 @@ __global__ void __launch_bounds__(128) k_uw_p(UWArgs a) {
 			vy_x += dvy * tx; vy_y += dvy * ty;
 #endif
 		}
+	}
 	}
 	double d[5] = {0., 0., 0., 0., 0.};  // x_t y_t vx_t vy_t rho_t
 	if (flags & A_MOMENTUM_UL) {
@@ -539,10 +590,12 @@ cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const mfk_
 	return cudaGetLastError();
 }
 
-cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* m, const double* rho, void* ff,
-                  float* vol, cudaStream_t s) {
+cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* vx, const double* vy, const double* m,
+                  const double* rho, const double* qw_src, double* qw_dst, void* ff, void* vff, float* vol,
+                  float* qw32, cudaStream_t s) {
 	if (n == 0) return cudaSuccess;
-	k_uw_ff<<<grid1(n, 256), 256, 0, s>>>(n, x, y, m, rho, reinterpret_cast<float4*>(ff), vol);
+	k_uw_ff<<<grid1(n, 256), 256, 0, s>>>(n, x, y, vx, vy, m, rho, qw_src, qw_dst, reinterpret_cast<float4*>(ff),
+	                                      reinterpret_cast<float4*>(vff), vol, qw32);
 	return cudaGetLastError();
 }
 
@@ -551,7 +604,10 @@ cudaError_t uw_stage(const UWArgs& a, int part, cudaStream_t s) {
 	const unsigned bs = 128;  // the passes' launch bounds
 	switch (part) {
 	case 0: if (a.n_g) k_uw_gp<<<grid1(a.n_g, bs), bs, 0, s>>>(a); break;
-	case 1: if (a.n_p) k_uw_p<<<grid1(a.n_p, bs), bs, 0, s>>>(a); break;
+	case 1:
+		if (a.n_p && a.vff) k_uw_p<true><<<grid1(a.n_p, bs), bs, 0, s>>>(a);
+		else if (a.n_p) k_uw_p<false><<<grid1(a.n_p, bs), bs, 0, s>>>(a);
+		break;
 	case 2: if (a.n_p) k_uw_smooth<<<grid1(a.n_p, 128), 128, 0, s>>>(a); break;
 	case 3: if (a.n_p) k_uw_smooth_copy<<<grid1(a.n_p, 128), 128, 0, s>>>(a); break;
 	}
