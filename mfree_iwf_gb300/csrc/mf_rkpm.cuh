@@ -115,8 +115,8 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 
 
 // The same shape functions for the mixed weak updated-Lagrangian form: the 27 moment
-// sums per neighbour in FP32, the three 3x3 solves in FP64 (through the adjugate), the
-// shape functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
+// sums per neighbour in FP32, the three 3x3 solves in float-float (through the
+// adjugate), the shape functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
 // with the gradient scaled by h (d/ds = h d/dx), so that every moment entry is of
 // order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
 // M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
@@ -127,6 +127,43 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 // w_x, w_y) takes the FP32 shape function and its gradient.  rkpm_row32 is the whole
 // row: each(f) calls f(q, j) per neighbour (particle j), offs(j) gives the offset and
 // vol(j) the FP32 volume m_j / rho_j.
+// Float-float arithmetic (an unevaluated sum hi + lo, ~48 significant bits) on the FP32
+// pipe, for the mixed form's moment solves: Knuth's TwoSum, Dekker's Fast2Sum and the
+// exact product error by one FMA (the error-free steps in explicitly rounded
+// operations, so nothing is contracted or reordered).
+struct F2 {
+	float hi, lo;
+};
+__device__ __forceinline__ F2 f2_fast(float a, float b) {  // |a| >= |b| (or a = 0)
+	const float s = __fadd_rn(a, b);
+	return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y) {
+	const float s = __fadd_rn(x.hi, y.hi);
+	const float bb = __fsub_rn(s, x.hi);
+	const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+	return f2_fast(s, __fadd_rn(e, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ F2 f2_neg(F2 x) { return F2{-x.hi, -x.lo}; }
+__device__ __forceinline__ F2 f2_prod(float a, float b) {  // exact
+	const float p = __fmul_rn(a, b);
+	return F2{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ F2 f2_mul(float a, F2 y) {
+	const float p = __fmul_rn(a, y.hi);
+	return f2_fast(p, __fmaf_rn(a, y.lo, __fmaf_rn(a, y.hi, -p)));
+}
+__device__ __forceinline__ F2 f2_mul(F2 x, F2 y) {
+	const float p = __fmul_rn(x.hi, y.hi);
+	return f2_fast(p, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.hi, -p))));
+}
+// 1 / d: the FP32 reciprocal and one Newton step in float-float, r + r (1 - d r)
+__device__ __forceinline__ F2 f2_recip(F2 d) {
+	const float r = 1.f / d.hi;
+	const F2 e = f2_add(F2{1.f, 0.f}, f2_neg(f2_mul(r, d)));
+	return f2_add(F2{r, 0.f}, f2_mul(r, e));
+}
+
 struct Rkpm32 {
 	float h, ih, fac;
 	float M[3][3], Mx[3][3], My[3][3];  // [col][row], scaled; upper triangle
@@ -165,44 +202,42 @@ struct Rkpm32 {
 	// the solves and the shape functions of the neighbours each(f) visits
 	template <class Each, class Out>
 	__device__ __forceinline__ bool finish(Each each, Out out) const {
-		// the three solves in FP64 through the adjugate of the symmetric moment matrix
-		// (A^-1 r = adj(A) r / det A, Cramer's rule with the cofactors shared)
-		double A[3][3], Ax[3][3], Ay[3][3];
-#pragma unroll
-		for (int a_ = 0; a_ < 3; a_++)
-#pragma unroll
-			for (int b_ = a_; b_ < 3; b_++) {
-				A[a_][b_] = A[b_][a_] = mfk::f2d(M[a_][b_]);
-				Ax[a_][b_] = Ax[b_][a_] = mfk::f2d(Mx[a_][b_]);
-				Ay[a_][b_] = Ay[b_][a_] = mfk::f2d(My[a_][b_]);
-			}
-		const double j00 = A[1][1] * A[2][2] - A[1][2] * A[1][2];
-		const double j01 = A[0][2] * A[1][2] - A[0][1] * A[2][2];
-		const double j02 = A[0][1] * A[1][2] - A[0][2] * A[1][1];
-		const double j11 = A[0][0] * A[2][2] - A[0][2] * A[0][2];
-		const double j12 = A[0][1] * A[0][2] - A[0][0] * A[1][2];
-		const double j22 = A[0][0] * A[1][1] - A[0][1] * A[0][1];
-		const double det = A[0][0] * j00 + A[0][1] * j01 + A[0][2] * j02;
-		const bool ok = fabs(det) > 0.;
-		const double id = 1. / det;
-		auto solve = [&](const double r[3], double x[3]) {
-			x[0] = (j00 * r[0] + j01 * r[1] + j02 * r[2]) * id;
-			x[1] = (j01 * r[0] + j11 * r[1] + j12 * r[2]) * id;
-			x[2] = (j02 * r[0] + j12 * r[1] + j22 * r[2]) * id;
+		// the three solves through the adjugate of the symmetric moment matrix
+		// (A^-1 r = adj(A) r / det A, Cramer's rule with the cofactors shared), in
+		// float-float: FP64's accuracy for the solve on the FP32 pipe
+		const float a00 = M[0][0], a01 = M[0][1], a02 = M[0][2], a11 = M[1][1], a12 = M[1][2], a22 = M[2][2];
+		auto cof = [](float p, float q, float r, float t) {  // p q - r t
+			return f2_add(f2_prod(p, q), f2_neg(f2_prod(r, t)));
 		};
-		const double C[3] = {j00 * id, j01 * id, j02 * id};  // the solution for P = (1, 0, 0)
-		double Cx[3], Cy[3];
-		double rx_[3], ry_[3];
+		const F2 j00 = cof(a11, a22, a12, a12), j01 = cof(a02, a12, a01, a22), j02 = cof(a01, a12, a02, a11);
+		const F2 j11 = cof(a00, a22, a02, a02), j12 = cof(a01, a02, a00, a12), j22 = cof(a00, a11, a01, a01);
+		const F2 det = f2_add(f2_add(f2_mul(a00, j00), f2_mul(a01, j01)), f2_mul(a02, j02));
+		const bool ok = fabsf(det.hi) > 0.f;
+		const F2 id = f2_recip(det);
+		auto dot3 = [](F2 x0, F2 y0, F2 x1, F2 y1, F2 x2, F2 y2) {
+			return f2_add(f2_add(f2_mul(x0, y0), f2_mul(x1, y1)), f2_mul(x2, y2));
+		};
+		auto solve = [&](const F2 r[3], F2 x[3]) {
+			x[0] = f2_mul(dot3(j00, r[0], j01, r[1], j02, r[2]), id);
+			x[1] = f2_mul(dot3(j01, r[0], j11, r[1], j12, r[2]), id);
+			x[2] = f2_mul(dot3(j02, r[0], j12, r[1], j22, r[2]), id);
+		};
+		const F2 C[3] = {f2_mul(j00, id), f2_mul(j01, id), f2_mul(j02, id)};  // the solution for P = (1, 0, 0)
+		// rx_ = -Ax C, ry_ = -Ay C over the symmetric matrices (stored upper triangle)
+		auto sym = [](const float (&X)[3][3], int a_, int b_) { return a_ <= b_ ? X[a_][b_] : X[b_][a_]; };
+		F2 rx_[3], ry_[3], Cx[3], Cy[3];
 #pragma unroll
 		for (int r = 0; r < 3; r++) {
-			rx_[r] = -(Ax[0][r] * C[0] + Ax[1][r] * C[1] + Ax[2][r] * C[2]);
-			ry_[r] = -(Ay[0][r] * C[0] + Ay[1][r] * C[1] + Ay[2][r] * C[2]);
+			rx_[r] = f2_neg(f2_add(f2_add(f2_mul(sym(Mx, 0, r), C[0]), f2_mul(sym(Mx, 1, r), C[1])),
+			                       f2_mul(sym(Mx, 2, r), C[2])));
+			ry_[r] = f2_neg(f2_add(f2_add(f2_mul(sym(My, 0, r), C[0]), f2_mul(sym(My, 1, r), C[1])),
+			                       f2_mul(sym(My, 2, r), C[2])));
 		}
 		solve(rx_, Cx);
 		solve(ry_, Cy);
-		const float c0 = (float)C[0], c1 = (float)C[1], c2 = (float)C[2];
-		const float cx0 = (float)Cx[0], cx1 = (float)Cx[1], cx2 = (float)Cx[2];
-		const float cy0 = (float)Cy[0], cy1 = (float)Cy[1], cy2 = (float)Cy[2];
+		const float c0 = C[0].hi, c1 = C[1].hi, c2 = C[2].hi;
+		const float cx0 = Cx[0].hi, cx1 = Cx[1].hi, cx2 = Cx[2].hi;
+		const float cy0 = Cy[0].hi, cy1 = Cy[1].hi, cy2 = Cy[2].hi;
 		each([&](uint32_t q, float2 r) {
 			const float rx = r.x, ry = r.y;
 			const mfk::KR32 w = mfk::cubic_spline_f(rx, ry, ih, fac);

@@ -150,7 +150,8 @@ __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* 
                         float4* ff, float4* vff, float* vol, float* qw32) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
-	const FF px = ff_split(x[i]), py = ff_split(y[i]), pvx = ff_split(vx[i]), pvy = ff_split(vy[i]);
+	const FF px = ff_split_bits(x[i]), py = ff_split_bits(y[i]);
+	const FF pvx = ff_split_bits(vx[i]), pvy = ff_split_bits(vy[i]);
 	ff[i] = make_float4(px.hi, px.lo, py.hi, py.lo);
 	vff[i] = make_float4(pvx.hi, pvx.lo, pvy.hi, pvy.lo);
 	vol[i] = (float)m[i] / (float)rho[i];
@@ -214,8 +215,8 @@ __global__ void __launch_bounds__(128)
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n_to) return;
 	const double px = tx[i], py = ty[i];
-	const float pxh = (float)px, pyh = (float)py;
-	const float pxl = (float)(px - (double)pxh), pyl = (float)(py - (double)pyh);
+	const FF qx = ff_split_bits(px), qy = ff_split_bits(py);  // the candidates' split (k_uw_ff)
+	const float pxh = qx.hi, pxl = qx.lo, pyh = qy.hi, pyl = qy.lo;
 	auto offs = [&](const float4 f) {  // x_i - x_j from j's float-float position
 		return make_float2((pxh - f.x) + (pxl - f.y), (pyh - f.z) + (pyl - f.w));
 	};
