@@ -294,7 +294,7 @@ struct mf_ctx {
 	DevBuf<double> uw_pw, uw_pwx, uw_pwy, uw_gw, uw_gwx, uw_gwy, uw_gsig, uw_ph, uw_gh, uw_qwp, uw_qws, uw_gm, uw_gqw;
 	DevBuf<double> uw_g[4][6];  // x y rho Sxx Sxy Syy
 	DevBuf<float> uw_ff, uw_vol;  // mixed form: the stage's float-float positions, FP32 volumes
-	DevBuf<float> uw_vff, uw_qw32, uw_gsig32;  // and velocities, FP32 weights, stress points' gsig
+	DevBuf<float> uw_vff, uw_qw32, uw_qwlo, uw_gsig32;  // and velocities, weights, stress points' gsig
 	DevBuf<uint32_t> uw_quads;  // element maps (global ll lr tr tl) when a gauss_int replaces the ellipse
 	uint32_t uw_order = 0, uw_nelem = 0;
 
@@ -1907,7 +1907,8 @@ mf_status uw_setup(mf_ctx* c) {
 	CK(c->uw_ph.alloc(n)); CK(c->uw_qws.alloc(n));
 	if (c->uw_mixed) {
 		CK(c->uw_ff.alloc(4 * (size_t)n)); CK(c->uw_vol.alloc(n));
-		CK(c->uw_vff.alloc(4 * (size_t)n)); CK(c->uw_qw32.alloc(n)); CK(c->uw_gsig32.alloc(4 * (size_t)ng));
+		CK(c->uw_vff.alloc(4 * (size_t)n)); CK(c->uw_qw32.alloc(n)); CK(c->uw_qwlo.alloc(n));
+		CK(c->uw_gsig32.alloc(4 * (size_t)ng));
 	}
 	for (int q = 0; q < 8; q++) CK(c->sd[3][q].alloc(n));
 	std::vector<uint32_t> goff(ng + 1), gnbr, gstart;
@@ -2047,6 +2048,7 @@ UWArgs uw_args(mf_ctx* c, uint32_t stage) {
 	if (c->uw_mixed && !c->strict && !c->uw_order) {
 		a.vff = reinterpret_cast<const float4*>(c->uw_vff.p);
 		a.qw32 = c->uw_qw32.p;
+		a.qwlo = c->uw_qwlo.p;
 		a.gsig32 = reinterpret_cast<float4*>(c->uw_gsig32.p);
 	}
 	a.status = c->d_status;
@@ -2074,7 +2076,7 @@ cudaError_t uw_neighbourhoods(mf_ctx* c, const UWArgs& a, bool points, bool refr
 	double* qd = refresh_qw ? a.qw_base : a.qw_stage;
 	if (mixed) {  // the particles' weights come with the float-float inputs
 		cudaError_t e = mf_fast::uw_ff(a.n_p, a.rd.x, a.rd.y, a.rd.vx, a.rd.vy, a.m, a.rd.rho, qs, qd, c->uw_ff.p,
-		                               c->uw_vff.p, c->uw_vol.p, c->uw_qw32.p, c->stream);
+		                               c->uw_vff.p, c->uw_vol.p, c->uw_qw32.p, c->uw_qwlo.p, c->stream);
 		if (e != cudaSuccess) return e;
 		c->launches++;
 		qs = nullptr;
@@ -2322,7 +2324,8 @@ mf_ctx::~mf_ctx() {
 		                           &uw_tp_off, &uw_tp_cnt, &uw_tp_gp,
 		                           &uw_tp_slot, &uw_bc_of, &uw_quads};
 		for (auto* p : uws) p->free();
-		uw_pmask.free(); uw_gmask.free(); uw_ff.free(); uw_vol.free(); uw_vff.free(); uw_qw32.free(); uw_gsig32.free();
+		uw_pmask.free(); uw_gmask.free(); uw_ff.free(); uw_vol.free(); uw_vff.free(); uw_qw32.free(); uw_qwlo.free();
+		uw_gsig32.free();
 		DevBuf<double>* uwd[] = {&uw_pw, &uw_pwx, &uw_pwy, &uw_gw, &uw_gwx, &uw_gwy, &uw_gsig, &uw_ph, &uw_gh, &uw_qwp,
 		                         &uw_qws, &uw_gm, &uw_gqw};
 		for (auto* p : uwd) p->free();

@@ -248,10 +248,10 @@ struct UWArgs {
 	SlotList tp;                         // per particle: the stress points listing it, ascending (sliced)
 	const uint32_t* tp_slot;             // their candidate slots, in tp's slots
 	double* gsig;                        // per stress point: Sxx - p, Sxy, Syy - p, quad weight
-	// mixed form (null otherwise): the particles' float-float velocities and FP32
-	// weights of the evaluation, the stress points' gsig in FP32
+	// mixed form (null otherwise): the particles' float-float velocities and weights of
+	// the evaluation (qw32 + qwlo), the stress points' gsig in FP32
 	const float4* vff;
-	const float* qw32;
+	const float *qw32, *qwlo;
 	float4* gsig32;
 	const uint32_t* bc_of;               // per particle: index into bc_v, or ~0u
 	const double* bc_v;
@@ -333,7 +333,7 @@ struct ContactArgs {
 	                   const void* ff, const float* vol, void* status, cudaStream_t s);                     \
 	cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* vx, const double* vy,           \
 	                  const double* m, const double* rho, const double* qw_src, double* qw_dst, void* ff,      \
-	                  void* vff, float* vol, float* qw32, cudaStream_t s);                                  \
+	                  void* vff, float* vol, float* qw32, float* qwlo, cudaStream_t s);                     \
 	cudaError_t uw_stage(const mfk_host::UWArgs& a, int part, cudaStream_t s);                                \
 	}
 

@@ -143,11 +143,12 @@ __global__ void k_uw_nbh(uint32_t n_to, const double* __restrict__ tx, const dou
 // The mixed form's per-particle inputs of one derivative evaluation: the stage's
 // positions and velocities as float-float pairs (x = hi + lo to 48 bits), the FP32
 // volumes m / rho, and the particles' integration weights of the evaluation (qw_src, or
-// m / rho without it: riemann_update_integration_weights) in FP64 and FP32.
+// m / rho without it: riemann_update_integration_weights) in FP64 and as a float-float
+// pair (qw32: the FP32 rounding, qwlo: the rest).
 __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* __restrict__ y,
                         const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ m,
                         const double* __restrict__ rho, const double* __restrict__ qw_src, double* qw_dst,
-                        float4* ff, float4* vff, float* vol, float* qw32) {
+                        float4* ff, float4* vff, float* vol, float* qw32, float* qwlo) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	const FF px = ff_split_bits(x[i]), py = ff_split_bits(y[i]);
@@ -157,7 +158,9 @@ __global__ void k_uw_ff(uint32_t n, const double* __restrict__ x, const double* 
 	vol[i] = (float)m[i] / (float)rho[i];
 	const double qw = qw_src ? qw_src[i] : m[i] / rho[i];
 	qw_dst[i] = qw;
-	qw32[i] = (float)qw;
+	const FF w = ff_split(qw);
+	qw32[i] = w.hi;
+	qwlo[i] = w.lo;
 }
 
 // The nq candidates in slots q0, q0 + S, ... in batches of four while cont() holds: a
@@ -375,6 +378,34 @@ __device__ __forceinline__ void uw_rk(uint32_t stg, double dt, uint32_t i, int n
 	}
 }
 
+// The mixed form's sums of k_uw_gp in float-float on the FP32 pipe (the stress points'
+// velocity gradient sets their stress rate, so they keep FP64's accuracy): the same
+// products and order as the fast FP64 form, from the float-float velocities and
+// weights and the FP32 shape functions the mixed neighbourhood kernel stored.
+__device__ __forceinline__ void uw_gp_sums_ff(const UWArgs& a, uint32_t i, uint32_t flags, double& vx_x, double& vx_y,
+                                              double& vy_x, double& vy_y, double& vxi, double& vyi) {
+	F2 lxx{0.f, 0.f}, lxy{0.f, 0.f}, lyx{0.f, 0.f}, lyy{0.f, 0.f}, ix{0.f, 0.f}, iy{0.f, 0.f};
+	const uint32_t q1 = a.gc.start[i] + a.gc.cnt[i] * a.gc.stride;
+	for (uint32_t q = a.gc.start[i]; q != q1; q += a.gc.stride) {
+		if (!a.gmask[q]) continue;
+		const uint32_t j = a.gc.nbr[q];
+		const float4 v = a.vff[j];
+		const F2 vx{v.x, v.y}, vy{v.z, v.w}, qwj{a.qw32[j], a.qwlo[j]};
+		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
+			const F2 tx = f2_mul(d2f_exact(a.gwx[q]), qwj), ty = f2_mul(d2f_exact(a.gwy[q]), qwj);
+			lxx = f2_add(lxx, f2_mul(vx, tx)); lxy = f2_add(lxy, f2_mul(vx, ty));
+			lyx = f2_add(lyx, f2_mul(vy, tx)); lyy = f2_add(lyy, f2_mul(vy, ty));
+		}
+		if (flags & mfk_host::FLAG_UW_INTERP) {
+			const F2 tw = f2_mul(d2f_exact(a.gw[q]), qwj);
+			ix = f2_add(ix, f2_mul(vx, tw)); iy = f2_add(iy, f2_mul(vy, tw));
+		}
+	}
+	auto dbl = [](F2 x) { return f2d(x.hi) + f2d(x.lo); };
+	vx_x = dbl(lxx); vx_y = dbl(lxy); vy_x = dbl(lyx); vy_y = dbl(lyy); vxi = dbl(ix); vyi = dbl(iy);
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.n_g) return;
@@ -385,6 +416,9 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 	const double qw = (flags & mfk_host::FLAG_UW_RIEMANN_GP) ? a.gm[i] / rho : a.gqw_base[i];
 	const double p = (flags & A_EOS_GP) ? pr.c0sq * (rho - pr.rho0) : 0.;
 	double vx_x = 0., vx_y = 0., vy_x = 0., vy_y = 0., vxi = 0., vyi = 0.;
+	if (MIXED) {
+		uw_gp_sums_ff(a, i, flags, vx_x, vx_y, vy_x, vy_y, vxi, vyi);
+	} else {
 	const uint32_t q1 = a.gc.start[i] + a.gc.cnt[i] * a.gc.stride;
 	for (uint32_t q = a.gc.start[i]; q != q1; q += a.gc.stride) {
 		if (!a.gmask[q]) continue;
@@ -413,6 +447,7 @@ __global__ void __launch_bounds__(128) k_uw_gp(UWArgs a) {
 			vxi += vxj * tw; vyi += vyj * tw;
 		}
 #endif
+	}
 	}
 	const double Sxx = g.Sxx[i], Sxy = g.Sxy[i], Syy = g.Syy[i];
 	double d[6] = {0., 0., 0., 0., 0., 0.};  // x_t y_t rho_t Sxx_t Sxy_t Syy_t
@@ -593,10 +628,10 @@ cudaError_t uw_nbh(uint32_t n_to, const double* tx, const double* ty, const mfk_
 
 cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* vx, const double* vy, const double* m,
                   const double* rho, const double* qw_src, double* qw_dst, void* ff, void* vff, float* vol,
-                  float* qw32, cudaStream_t s) {
+                  float* qw32, float* qwlo, cudaStream_t s) {
 	if (n == 0) return cudaSuccess;
 	k_uw_ff<<<grid1(n, 256), 256, 0, s>>>(n, x, y, vx, vy, m, rho, qw_src, qw_dst, reinterpret_cast<float4*>(ff),
-	                                      reinterpret_cast<float4*>(vff), vol, qw32);
+	                                      reinterpret_cast<float4*>(vff), vol, qw32, qwlo);
 	return cudaGetLastError();
 }
 
@@ -604,7 +639,10 @@ cudaError_t uw_ff(uint32_t n, const double* x, const double* y, const double* vx
 cudaError_t uw_stage(const UWArgs& a, int part, cudaStream_t s) {
 	const unsigned bs = 128;  // the passes' launch bounds
 	switch (part) {
-	case 0: if (a.n_g) k_uw_gp<<<grid1(a.n_g, bs), bs, 0, s>>>(a); break;
+	case 0:
+		if (a.n_g && a.vff) k_uw_gp<true><<<grid1(a.n_g, bs), bs, 0, s>>>(a);
+		else if (a.n_g) k_uw_gp<false><<<grid1(a.n_g, bs), bs, 0, s>>>(a);
+		break;
 	case 1:
 		if (a.n_p && a.vff) k_uw_p<true><<<grid1(a.n_p, bs), bs, 0, s>>>(a);
 		else if (a.n_p) k_uw_p<false><<<grid1(a.n_p, bs), bs, 0, s>>>(a);
