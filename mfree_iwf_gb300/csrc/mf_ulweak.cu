@@ -188,8 +188,9 @@ __device__ __forceinline__ void cand4(uint32_t q0, uint32_t nq, uint32_t S, cons
 
 // The mixed form's neighbourhood kernel: the ellipse in FP32 from the float-float
 // positions, with the FP64 ellipse (ellipse64) taken over for every row whose FP32
-// result could differ from it, so the neighbour sets are the FP64 form's; then the
-// RKPM moment sums and shape functions in FP32 (rkpm_row32).
+// result could differ from it, so the neighbour sets are the FP64 form's; the RKPM
+// moments summed in FP32 during the selection, then the solves (float-float) and the
+// shape functions (FP32) of Rkpm32.
 //
 // Error bound of the FP32 ellipse (first order in u = 2^-24).  An offset x_i - x_j
 // from the float-float pairs is within 3u of the exact difference, so a moment sum over
@@ -205,8 +206,9 @@ __device__ __forceinline__ void cand4(uint32_t q0, uint32_t nq, uint32_t S, cons
 // per radian; together |s32 - s64| <= (3n + 48) u s T / l1.  The kernel's margin is
 // twice the bound: a candidate with |s32 - 1| inside it, an FP64 |A01| within its
 // rounding spread of the 1e-9 threshold (summed in FP64 when FP32's is within e of it),
-// or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the row to ellipse64.  h is the FP64 distance of the candidate farthest in FP32 (FP64's
-// h, or one within FP32 rounding of it where two candidates tie in FP32).
+// or a non-finite or near-singular ellipse (T / l1 > 1e4) sends the row to ellipse64.
+// h is the FP64 distance of the candidate farthest in FP32 (FP64's h, or one within
+// FP32 rounding of it where two candidates tie in FP32).
 __global__ void __launch_bounds__(128)
     k_uw_nbh32(uint32_t n_to, const double* __restrict__ tx, const double* __restrict__ ty,
                const mfk_host::SlotList cand, const float4* __restrict__ ff,
