@@ -113,20 +113,6 @@ __device__ __forceinline__ bool rkpm_row(double xi, double yi, double hi, uint32
 	return ok;
 }
 
-
-// The same shape functions for the mixed weak updated-Lagrangian form: the 27 moment
-// sums per neighbour in FP32, the three 3x3 solves in float-float (through the
-// adjugate), the shape functions in FP32.  The sums run over the offsets scaled by 1/h, s = (x_i - x_j)/h,
-// with the gradient scaled by h (d/ds = h d/dx), so that every moment entry is of
-// order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
-// M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
-// Corr = C'0 + s.C'(1,2), h Corr_x = s.C'_x(1,2) + C'1 + C'_x0 -- the reference's
-// expressions (precomp_shape_functions.h:52-173) in scaled units.  A row is init(h),
-// add() per neighbour in ascending slot order, then finish(): each(g) calls g(q, d) for
-// the row's neighbours (slot q, FP32 offset d = x_i - x_j) in that order, and out(q, w,
-// w_x, w_y) takes the FP32 shape function and its gradient.  rkpm_row32 is the whole
-// row: each(f) calls f(q, j) per neighbour (particle j), offs(j) gives the offset and
-// vol(j) the FP32 volume m_j / rho_j.
 // Float-float arithmetic (an unevaluated sum hi + lo, ~48 significant bits) on the FP32
 // pipe, for the mixed form's moment solves: Knuth's TwoSum, Dekker's Fast2Sum and the
 // exact product error by one FMA (the error-free steps in explicitly rounded
@@ -164,6 +150,17 @@ __device__ __forceinline__ F2 f2_recip(F2 d) {
 	return f2_add(F2{r, 0.f}, f2_mul(r, e));
 }
 
+// The same shape functions for the mixed weak updated-Lagrangian form: the 27 moment
+// sums per neighbour in FP32, the three 3x3 solves in float-float (through the
+// adjugate), the shape functions in FP32.  The sums run over the offsets scaled by
+// 1/h, s = (x_i - x_j)/h, with the gradient scaled by h (d/ds = h d/dx), so that every
+// moment entry is of order one: with D = diag(1, 1/h, 1/h) the scaled matrices are M' = D M D and
+// M'_x = h D M_x D, their solutions C' = D^-1 C and C'_x = h D^-1 C_x, and
+// Corr = C'0 + s.C'(1,2), h Corr_x = s.C'_x(1,2) + C'1 + C'_x0 -- the reference's
+// expressions (precomp_shape_functions.h:52-173) in scaled units.  A row is init(h),
+// add() per neighbour in ascending slot order, then finish(): each(g) calls g(q, d) for
+// the row's neighbours (slot q, FP32 offset d = x_i - x_j) in that order, and out(q, w,
+// w_x, w_y) takes the FP32 shape function and its gradient.
 struct Rkpm32 {
 	float h, ih, fac;
 	float M[3][3], Mx[3][3], My[3][3];  // [col][row], scaled; upper triangle
@@ -250,17 +247,6 @@ struct Rkpm32 {
 		return ok;
 	}
 };
-
-template <class Each, class Offs, class Vol, class Out>
-__device__ __forceinline__ bool rkpm_row32(double hi, Each each, Offs offs, Vol vol, Out out) {
-	Rkpm32 k;
-	k.init(hi);
-	each([&](uint32_t, uint32_t j) {
-		const float2 r = offs(j);
-		k.add(r.x, r.y, vol(j));
-	});
-	return k.finish([&](auto g) { each([&](uint32_t q, uint32_t j) { g(q, offs(j)); }); }, out);
-}
 
 }  // namespace
 }  // namespace MF_NS
