@@ -215,7 +215,7 @@ struct mf_ctx {
 	uint32_t n_total = 0;
 	uint32_t flags = 0;
 	bool mixed = false, strict = false;
-	bool uw_mixed = false;  // weak UL, mixed form: FP32 moment sums in the neighbourhood kernel
+	bool uw_mixed = false;  // weak UL, mixed form: FP32 ellipse and moments, FP32 / float-float pass sums
 	uint64_t launches = 0;
 	Timing timing;
 

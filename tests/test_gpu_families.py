@@ -258,7 +258,8 @@ def test_ul_weak_graph_and_pipeline_checks(lib):
     for ga, gb in zip(a, b):
         for f in FIELDS:
             assert np.array_equal(ga[f], gb[f]), f
-    # the mixed form (FP32 moment sums in the neighbourhood kernel) replays the same way
+    # the mixed form (FP32 ellipse and moments, float-float solves, FP32 and
+    # float-float pass sums) replays the same way
     am = run(sc, 20, precision="mixed")
     bm = run(sc, 20, precision="mixed", graph=True)
     for ga, gb in zip(am, bm):

@@ -127,9 +127,10 @@ def scenario(case):
 #    1000 steps at dx = 0.2 mm.
 #  * the weak form on explicit element maps: the meshed rings with the elements' own
 #    functions through contact, the meshed disc with RKPM.
-#  * the weak UL form (ellipse neighbourhoods and RKPM every stage; the mixed form sums
-#    the moments in FP32): the reference's rings through contact, plate and spinning
-#    disc at nbox = 41.
+#  * the weak UL form (ellipse neighbourhoods and RKPM every stage; the mixed form
+#    selects in FP32 within an error bound and sums the moments and the particles'
+#    terms in FP32, the solves and the stress points' terms in float-float): the
+#    reference's rings through contact, plate and spinning disc at nbox = 41.
 V = 1e-4  # the velocity and displacement target
 CASES = [
     ("c1_ul_rings_dx1mm", 1000, dict(displacement=V, velocity=V, density=1e-3, stress=1e-3)),
