@@ -65,14 +65,16 @@ typedef enum {
 	MF_METHOD_POTENTIAL = 5, /* particle_potential: TL neighbours, symmetric Randles-Libersky weights, elastic-potential
 	                           pair forces */
 	MF_METHOD_UL_WEAK = 6   /* particle_ul_weak: weak-form UL with stress points (mf_set_stress_points), per-stage
-	                           neighbour ellipses from Manhattan candidates and RKPM shape functions (FP64 forms) */
+	                           neighbour ellipses from Manhattan candidates and RKPM shape functions */
 } mf_method;
 
 /* Arithmetic forms. */
 typedef enum {
 	MF_PREC_FP64_STRICT = 0, /* FP64, no FMA contraction: the reference-parity form */
 	MF_PREC_FP64 = 1,        /* FP64 with FMA contraction */
-	MF_PREC_MIXED = 2        /* FP32 pair sums; FP64 position/velocity RK4 state and 2x2/3x3 inversions */
+	MF_PREC_MIXED = 2        /* FP32 pair sums and per-row algebra over float-float position and velocity
+	                            differences (float-float where a sum sets a stress rate, as in the weak UL
+	                            stress points); FP64 position/velocity RK4 state; the same neighbour sets */
 } mf_precision;
 
 /* Action callbacks of the reference, by id (body<T>::add_action). */
