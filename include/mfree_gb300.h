@@ -74,7 +74,7 @@ typedef enum {
 	MF_PREC_FP64 = 1,        /* FP64 with FMA contraction */
 	MF_PREC_MIXED = 2        /* FP32 pair sums and per-row algebra over float-float position and velocity
 	                            differences (float-float where a sum sets a stress rate, as in the weak UL
-	                            stress points); FP64 position/velocity RK4 state; the same neighbour sets */
+	                            stress points); FP64 position/velocity RK4 state */
 } mf_precision;
 
 /* Action callbacks of the reference, by id (body<T>::add_action). */
