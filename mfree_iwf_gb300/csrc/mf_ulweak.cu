@@ -478,14 +478,38 @@ __device__ __forceinline__ void uw_p_sums32(const UWArgs& a, uint32_t j, uint32_
 	const float qwj = a.qw32[j];
 	float sxx_x = 0.f, sxy_y = 0.f, sxy_x = 0.f, syy_y = 0.f;
 	if (flags & mfk_host::FLAG_UW_STRESS) {
-		const uint32_t t1 = a.tp.start[j] + a.tp.cnt[j] * a.tp.stride;
-		for (uint32_t t = a.tp.start[j]; t != t1; t += a.tp.stride) {
-			const uint32_t q = a.tp_slot[t];
-			if (!a.gmask[q]) continue;
-			const float4 g = a.gsig32[a.tp.nbr[t]];  // Sxx - p, Sxy, Syy - p, qw
-			const float c = g.w * qwj, tx = d2f_exact(a.gwx[q]) * c, ty = d2f_exact(a.gwy[q]) * c;
+		// one transposed entry: the stress point's FP32 stress and weight (Sxx - p, Sxy,
+		// Syy - p, qw) and its gradient at the particle, if the particle is in its ellipse
+		auto entry = [&](uint8_t in, float4 g, double gx, double gy) {
+			if (!in) return;
+			const float c = g.w * qwj, tx = d2f_exact(gx) * c, ty = d2f_exact(gy) * c;
 			sxx_x -= g.x * tx; sxy_y -= g.y * ty;
 			sxy_x -= g.y * tx; syy_y -= g.z * ty;
+		};
+		// the entries' loads are scattered over the stress points' slots: four entries'
+		// loads are issued before any is used
+		const uint32_t S = a.tp.stride, n = a.tp.cnt[j];
+		uint32_t t = a.tp.start[j], k = 0;
+		for (; k + 4 <= n; k += 4, t += 4 * S) {
+			uint32_t q[4], gi[4];
+			uint8_t in[4];
+			float4 g[4];
+			double gx[4], gy[4];
+#pragma unroll
+			for (int u = 0; u < 4; u++) { q[u] = a.tp_slot[t + u * S]; gi[u] = a.tp.nbr[t + u * S]; }
+#pragma unroll
+			for (int u = 0; u < 4; u++) {
+				in[u] = a.gmask[q[u]];
+				g[u] = a.gsig32[gi[u]];
+				gx[u] = a.gwx[q[u]];
+				gy[u] = a.gwy[q[u]];
+			}
+#pragma unroll
+			for (int u = 0; u < 4; u++) entry(in[u], g[u], gx[u], gy[u]);
+		}
+		for (; k < n; k++, t += S) {
+			const uint32_t q = a.tp_slot[t];
+			entry(a.gmask[q], a.gsig32[a.tp.nbr[t]], a.gwx[q], a.gwy[q]);
 		}
 	}
 	float lxx = 0.f, lxy = 0.f, lyx = 0.f, lyy = 0.f;
