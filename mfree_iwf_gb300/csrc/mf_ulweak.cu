@@ -515,15 +515,37 @@ __device__ __forceinline__ void uw_p_sums32(const UWArgs& a, uint32_t j, uint32_
 	float lxx = 0.f, lxy = 0.f, lyx = 0.f, lyy = 0.f;
 	if (flags & A_DERIVE_VEL) {
 		const float4 vj = a.vff[j];
-		const uint32_t q1 = a.pc.start[j] + a.pc.cnt[j] * a.pc.stride;
-		for (uint32_t q = a.pc.start[j]; q != q1; q += a.pc.stride) {
-			if (!a.pmask[q]) continue;
-			const uint32_t k = a.pc.nbr[q];
-			const float4 vk = a.vff[k];
-			const float qwk = a.qw32[k], tx = d2f_exact(a.pwx[q]) * qwk, ty = d2f_exact(a.pwy[q]) * qwk;
+		auto cand = [&](uint8_t in, float4 vk, float qwk, double gx, double gy) {
+			if (!in) return;
+			const float tx = d2f_exact(gx) * qwk, ty = d2f_exact(gy) * qwk;
 			const float dvx = (vk.x - vj.x) + (vk.y - vj.y), dvy = (vk.z - vj.z) + (vk.w - vj.w);
 			lxx += dvx * tx; lxy += dvx * ty;
 			lyx += dvy * tx; lyy += dvy * ty;
+		};
+		// four candidates' loads (the neighbours' velocities and weights gathered) in flight
+		const uint32_t S = a.pc.stride, n = a.pc.cnt[j];
+		uint32_t q = a.pc.start[j], k = 0;
+		for (; k + 4 <= n; k += 4, q += 4 * S) {
+			uint32_t nb[4];
+			uint8_t in[4];
+			float4 vk[4];
+			float qw[4];
+			double gx[4], gy[4];
+#pragma unroll
+			for (int u = 0; u < 4; u++) {
+				in[u] = a.pmask[q + u * S];
+				nb[u] = a.pc.nbr[q + u * S];
+				gx[u] = a.pwx[q + u * S];
+				gy[u] = a.pwy[q + u * S];
+			}
+#pragma unroll
+			for (int u = 0; u < 4; u++) { vk[u] = a.vff[nb[u]]; qw[u] = a.qw32[nb[u]]; }
+#pragma unroll
+			for (int u = 0; u < 4; u++) cand(in[u], vk[u], qw[u], gx[u], gy[u]);
+		}
+		for (; k < n; k++, q += S) {
+			const uint32_t nb = a.pc.nbr[q];
+			cand(a.pmask[q], a.vff[nb], a.qw32[nb], a.pwx[q], a.pwy[q]);
 		}
 	}
 	Sxx_x = f2d(sxx_x); Sxy_y = f2d(sxy_y); Sxy_x = f2d(sxy_x); Syy_y = f2d(syy_y);
