@@ -387,21 +387,44 @@ __device__ __forceinline__ void uw_rk(uint32_t stg, double dt, uint32_t i, int n
 __device__ __forceinline__ void uw_gp_sums_ff(const UWArgs& a, uint32_t i, uint32_t flags, double& vx_x, double& vx_y,
                                               double& vy_x, double& vy_y, double& vxi, double& vyi) {
 	F2 lxx{0.f, 0.f}, lxy{0.f, 0.f}, lyx{0.f, 0.f}, lyy{0.f, 0.f}, ix{0.f, 0.f}, iy{0.f, 0.f};
-	const uint32_t q1 = a.gc.start[i] + a.gc.cnt[i] * a.gc.stride;
-	for (uint32_t q = a.gc.start[i]; q != q1; q += a.gc.stride) {
-		if (!a.gmask[q]) continue;
-		const uint32_t j = a.gc.nbr[q];
-		const float4 v = a.vff[j];
-		const F2 vx{v.x, v.y}, vy{v.z, v.w}, qwj{a.qw32[j], a.qwlo[j]};
+	auto cand = [&](uint8_t in, float4 v, F2 qwj, double gx, double gy, double gw) {
+		if (!in) return;
+		const F2 vx{v.x, v.y}, vy{v.z, v.w};
 		if (flags & mfk_host::FLAG_UW_VEL_WEAK) {
-			const F2 tx = f2_mul(d2f_exact(a.gwx[q]), qwj), ty = f2_mul(d2f_exact(a.gwy[q]), qwj);
+			const F2 tx = f2_mul(d2f_exact(gx), qwj), ty = f2_mul(d2f_exact(gy), qwj);
 			lxx = f2_add(lxx, f2_mul(vx, tx)); lxy = f2_add(lxy, f2_mul(vx, ty));
 			lyx = f2_add(lyx, f2_mul(vy, tx)); lyy = f2_add(lyy, f2_mul(vy, ty));
 		}
 		if (flags & mfk_host::FLAG_UW_INTERP) {
-			const F2 tw = f2_mul(d2f_exact(a.gw[q]), qwj);
+			const F2 tw = f2_mul(d2f_exact(gw), qwj);
 			ix = f2_add(ix, f2_mul(vx, tw)); iy = f2_add(iy, f2_mul(vy, tw));
 		}
+	};
+	// four candidates' loads (the neighbours' velocities and weights gathered) in flight
+	const uint32_t S = a.gc.stride, n = a.gc.cnt[i];
+	uint32_t q = a.gc.start[i], k = 0;
+	for (; k + 4 <= n; k += 4, q += 4 * S) {
+		uint32_t nb[4];
+		uint8_t in[4];
+		float4 v[4];
+		F2 qw[4];
+		double gx[4], gy[4], gw[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			in[u] = a.gmask[q + u * S];
+			nb[u] = a.gc.nbr[q + u * S];
+			gx[u] = a.gwx[q + u * S];
+			gy[u] = a.gwy[q + u * S];
+			gw[u] = a.gw[q + u * S];
+		}
+#pragma unroll
+		for (int u = 0; u < 4; u++) { v[u] = a.vff[nb[u]]; qw[u] = F2{a.qw32[nb[u]], a.qwlo[nb[u]]}; }
+#pragma unroll
+		for (int u = 0; u < 4; u++) cand(in[u], v[u], qw[u], gx[u], gy[u], gw[u]);
+	}
+	for (; k < n; k++, q += S) {
+		const uint32_t nb = a.gc.nbr[q];
+		cand(a.gmask[q], a.vff[nb], F2{a.qw32[nb], a.qwlo[nb]}, a.gwx[q], a.gwy[q], a.gw[q]);
 	}
 	auto dbl = [](F2 x) { return f2d(x.hi) + f2d(x.lo); };
 	vx_x = dbl(lxx); vx_y = dbl(lxy); vy_x = dbl(lyx); vy_y = dbl(lyy); vxi = dbl(ix); vyi = dbl(iy);
